@@ -1,0 +1,125 @@
+"""Build and load libdgpu.so (the sm_103a CUDA library behind include/dgpu.h) through ctypes.
+
+The library is compiled in-tree with nvcc for sm_103a only. There is no fallback: if the library is missing
+or no GB300 is present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+LIB_PATH = os.path.join(PKG_DIR, "libdgpu.so")
+SOURCES = ["dgpu.cu"]
+HEADERS = ["dgpu_tp.cuh", "dgpu_physics.cuh"]
+NVCC_FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
+              "-Xcompiler", "-fPIC", "-shared"]
+
+
+def nvcc_path() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(REPO_DIR, "include", "dgpu.h")]
+    return any(os.path.getmtime(p) > t for p in deps)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile libdgpu.so for sm_103a (nvcc cross-compiles without a GPU)."""
+    if not force and not _stale():
+        return LIB_PATH
+    cmd = [nvcc_path()] + NVCC_FLAGS + ["-o", LIB_PATH] + [os.path.join(CSRC, s) for s in SOURCES]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int_p = ctypes.POINTER(ctypes.c_int)
+
+
+class Physics(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_int), ("pde", ctypes.c_int), ("num_flux", ctypes.c_int),
+                ("positivity", ctypes.c_int), ("b_adv", ctypes.c_double * 3)]
+
+
+class TPOperators(ctypes.Structure):
+    _fields_ = [("elem_type", ctypes.c_int), ("p", ctypes.c_int),
+                ("cv0_vs_vc", c_double_p), ("cv1_vs_vc", c_double_p), ("cv0_vs_fc", c_double_p),
+                ("w_vc", c_double_p), ("ccSB0_vs_vs", c_double_p), ("ccBS0_vs_vs", c_double_p)]
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("n_volumes", ctypes.c_int), ("metrics_vc", c_double_p), ("jacobian_det_vc", c_double_p),
+                ("n_faces", ctypes.c_int), ("face_vol", c_int_p), ("face_lf", c_int_p), ("nc_fc", c_int_p),
+                ("normals_fc", c_double_p), ("jacobian_det_fc", c_double_p)]
+
+
+EXPORTS = {
+    # name: (restype, argtypes)
+    "dgpu_create": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.POINTER(TPOperators), ctypes.POINTER(Mesh),
+                                   ctypes.POINTER(ctypes.c_void_p)]),
+    "dgpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dgpu_state_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
+    "dgpu_upload_state": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_download_state": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_download_rhs": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_compute_rhs": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_compute_rhs_host": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
+    "dgpu_ssp_rk3_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, c_double_p]),
+    "dgpu_ssp_rk3_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, c_double_p]),
+    "dgpu_positivity_corrections": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "dgpu_kernel_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "dgpu_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "dgpu_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dgpu_set_kernel_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dgpu_kernel_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, c_double_p,
+                                        ctypes.POINTER(ctypes.c_longlong)]),
+    "dgpu_probe_fp64": (ctypes.c_int, [ctypes.c_int, c_double_p]),
+    "dgpu_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "dgpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+}
+
+
+def load(build_if_missing: bool = True):
+    """Load libdgpu.so; raises if it cannot be built or loaded (no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise RuntimeError(f"{LIB_PATH} is missing: call dpgsolver_gb300.build()")
+        build()
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class DGPUError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"dgpu status {status}: {message}")
+        self.status = status
+
+
+def check(status: int, ctx=None):
+    if status != 0:
+        lib = load()
+        msg = lib.dgpu_last_error(ctx)
+        raise DGPUError(status, (msg or b"").decode() or lib.dgpu_status_string(status).decode())

@@ -1,0 +1,851 @@
+// C ABI of the GB300 explicit DG residual (declared in include/dgpu.h).
+//
+// Host side: validates and packs the caller's operators and geometry once (dgpu_create), owns all device
+// memory, launches the TP kernels of dgpu_tp.cuh on one stream per context, and replays each SSP-RK3 step
+// from a captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/dgpu.h"
+#include "dgpu_tp.cuh"
+
+using namespace dgpu;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct KernelTimer {
+	const char* name;
+	cudaEvent_t start, stop;
+};
+
+}  // namespace
+
+struct dgpu_ctx {
+	// problem
+	int d = 0, q = 0, N = 0, NF = 0, nv = 0, pde = 0, flux = 0, positivity = 0;
+	int n_vol = 0, n_face = 0;
+	double b_adv[3] = {0, 0, 0};
+	TPOps ops;
+	// device memory
+	double *u = nullptr, *u0 = nullptr, *rhs = nullptr;
+	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
+	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
+	double *traces = nullptr, *nnf = nullptr, *vol_gl = nullptr;
+	unsigned long long* max_bits = nullptr;
+	int* err_flag = nullptr;
+	unsigned long long* n_corr = nullptr;
+	// execution
+	cudaStream_t stream = nullptr;
+	bool own_stream = false;
+	cudaGraphExec_t rk_graph = nullptr;
+	double rk_graph_dt = 0.0;
+	long long launches = 0;
+	std::string err;
+	// launchers for the instantiated (D, Q, NV, PDE, FLUX)
+	cudaError_t (*launch_volume)(dgpu_ctx*) = nullptr;
+	cudaError_t (*launch_face)(dgpu_ctx*) = nullptr;
+	cudaError_t (*launch_lift_rhs)(dgpu_ctx*) = nullptr;
+	cudaError_t (*launch_lift_rk)(dgpu_ctx*, double dt, int stage) = nullptr;
+	// optional per-kernel timing (eager launches only)
+	bool timing = false;
+	std::vector<KernelTimer> timers;
+
+	TPParams params() const
+	{
+		TPParams P;
+		P.n_vol = n_vol;
+		P.n_face = n_face;
+		P.b_adv[0] = b_adv[0];
+		P.b_adv[1] = b_adv[1];
+		P.b_adv[2] = b_adv[2];
+		P.vol_face = vol_face;
+		P.gmet = gmet;
+		P.inv_wJ = inv_wJ;
+		P.fgeo = fgeo;
+		P.nc = nc;
+		P.nc_inv = nc_inv;
+		P.traces = traces;
+		P.nnf = nnf;
+		P.vol_gl = vol_gl;
+		P.max_bits = max_bits;
+		P.err_flag = err_flag;
+		P.n_corr = n_corr;
+		return P;
+	}
+};
+
+namespace {
+
+dgpu_status fail(dgpu_ctx* c, dgpu_status st, const std::string& msg)
+{
+	if (c)
+		c->err = msg;
+	else
+		g_create_error = msg;
+	return st;
+}
+
+dgpu_status cuda_fail(dgpu_ctx* c, cudaError_t e, const char* what)
+{
+	std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+	return fail(c, DGPU_ERR_CUDA, m);
+}
+
+#define DGPU_CUDA(ctx, call)                                   \
+	do {                                                       \
+		cudaError_t e_ = (call);                               \
+		if (e_ != cudaSuccess)                                 \
+			return cuda_fail((ctx), e_, #call);                \
+	} while (0)
+
+// Gauss-Jordan inverse with partial pivoting of a small row-major matrix.
+bool invert_small(int n, const double* A, double* Ainv)
+{
+	double a[kQMax * kQMax];
+	for (int i = 0; i < n * n; ++i)
+		a[i] = A[i];
+	for (int i = 0; i < n; ++i)
+		for (int j = 0; j < n; ++j)
+			Ainv[i * n + j] = (i == j) ? 1.0 : 0.0;
+	for (int col = 0; col < n; ++col) {
+		int piv = col;
+		for (int r = col + 1; r < n; ++r)
+			if (fabs(a[r * n + col]) > fabs(a[piv * n + col]))
+				piv = r;
+		if (!(fabs(a[piv * n + col]) > 1e-300))
+			return false;
+		if (piv != col)
+			for (int j = 0; j < n; ++j) {
+				double t = a[col * n + j]; a[col * n + j] = a[piv * n + j]; a[piv * n + j] = t;
+				t = Ainv[col * n + j]; Ainv[col * n + j] = Ainv[piv * n + j]; Ainv[piv * n + j] = t;
+			}
+		const double inv = 1.0 / a[col * n + col];
+		for (int j = 0; j < n; ++j) {
+			a[col * n + j] *= inv;
+			Ainv[col * n + j] *= inv;
+		}
+		for (int r = 0; r < n; ++r) {
+			if (r == col)
+				continue;
+			const double f = a[r * n + col];
+			for (int j = 0; j < n; ++j) {
+				a[r * n + j] -= f * a[col * n + j];
+				Ainv[r * n + j] -= f * Ainv[col * n + j];
+			}
+		}
+	}
+	return true;
+}
+
+template <int D, int Q, int NV>
+size_t volume_smem_bytes()
+{
+	using S = TPShape<D, Q>;
+	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * (NV * S::N * 2 + D * NV * S::N) * sizeof(double);
+}
+
+template <int D, int Q, int NV>
+size_t lift_smem_bytes()
+{
+	using S = TPShape<D, Q>;
+	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * (3 * NV * S::N) * sizeof(double);
+}
+
+void record_start(dgpu_ctx* c, const char* name)
+{
+	if (!c->timing)
+		return;
+	KernelTimer t;
+	t.name = name;
+	cudaEventCreate(&t.start);
+	cudaEventCreate(&t.stop);
+	cudaEventRecord(t.start, c->stream);
+	c->timers.push_back(t);
+}
+
+void record_stop(dgpu_ctx* c)
+{
+	if (!c->timing)
+		return;
+	cudaEventRecord(c->timers.back().stop, c->stream);
+}
+
+template <int D, int Q, int NV, int PDE>
+cudaError_t launch_volume_t(dgpu_ctx* c)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	record_start(c, "tp_volume_kernel");
+	tp_volume_kernel<D, Q, NV, PDE><<<blocks, S::THREADS, volume_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, c->params(), c->u);
+	record_stop(c);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV, int PDE, int FLUX>
+cudaError_t launch_face_t(dgpu_ctx* c)
+{
+	using S = TPShape<D, Q>;
+	const long long n = (long long)c->n_face * S::NF;
+	const int blocks = (int)((n + 255) / 256);
+	record_start(c, "tp_face_kernel");
+	tp_face_kernel<D, Q, NV, PDE, FLUX><<<blocks, 256, 0, c->stream>>>(c->params());
+	record_stop(c);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV>
+cudaError_t launch_lift_rhs_t(dgpu_ctx* c)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	RkArgs rk;
+	rk.u = c->u;
+	rk.u0 = c->u0;
+	rk.rhs = c->rhs;
+	rk.dt = 0.0;
+	rk.stage = 0;
+	rk.positivity = 0;
+	record_start(c, "tp_lift_kernel");
+	tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, c->params(), rk);
+	record_stop(c);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV>
+cudaError_t launch_lift_rk_t(dgpu_ctx* c, double dt, int stage)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	RkArgs rk;
+	rk.u = c->u;
+	rk.u0 = c->u0;
+	rk.rhs = c->rhs;
+	rk.dt = dt;
+	rk.stage = stage;
+	rk.positivity = c->positivity;
+	record_start(c, "tp_lift_kernel");
+	tp_lift_kernel<D, Q, NV, kModeRk><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, c->params(), rk);
+	record_stop(c);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV, int PDE, int FLUX>
+cudaError_t bind(dgpu_ctx* c)
+{
+	c->launch_volume = launch_volume_t<D, Q, NV, PDE>;
+	c->launch_face = launch_face_t<D, Q, NV, PDE, FLUX>;
+	c->launch_lift_rhs = launch_lift_rhs_t<D, Q, NV>;
+	c->launch_lift_rk = launch_lift_rk_t<D, Q, NV>;
+	cudaError_t e;
+	e = cudaFuncSetAttribute(tp_volume_kernel<D, Q, NV, PDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                         (int)volume_smem_bytes<D, Q, NV>());
+	if (e != cudaSuccess)
+		return e;
+	e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRhs>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                         (int)lift_smem_bytes<D, Q, NV>());
+	if (e != cudaSuccess)
+		return e;
+	return cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                            (int)lift_smem_bytes<D, Q, NV>());
+}
+
+template <int D, int Q>
+cudaError_t bind_pde(dgpu_ctx* c)
+{
+	if (c->pde == DGPU_PDE_ADVECTION)
+		return bind<D, Q, 1, kAdvection, kUpwind>(c);
+	if (c->flux == DGPU_NUM_FLUX_ROE_PIKE)
+		return bind<D, Q, D + 2, kEuler, kRoePike>(c);
+	return bind<D, Q, D + 2, kEuler, kLaxFriedrichs>(c);
+}
+
+template <int D>
+cudaError_t bind_q(dgpu_ctx* c)
+{
+	switch (c->q) {
+	case 2: return bind_pde<D, 2>(c);
+	case 3: return bind_pde<D, 3>(c);
+	case 4: return bind_pde<D, 4>(c);
+	case 5: return bind_pde<D, 5>(c);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+void free_all(dgpu_ctx* c)
+{
+	if (c->rk_graph)
+		cudaGraphExecDestroy(c->rk_graph);
+	for (auto& t : c->timers) {
+		cudaEventDestroy(t.start);
+		cudaEventDestroy(t.stop);
+	}
+	c->timers.clear();
+	void* ptrs[] = {c->u, c->u0, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
+	                c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
+	for (void* p : ptrs)
+		if (p)
+			cudaFree(p);
+	if (c->own_stream && c->stream)
+		cudaStreamDestroy(c->stream);
+}
+
+template <typename T>
+cudaError_t upload(T** dst, const std::vector<T>& src)
+{
+	cudaError_t e = cudaMalloc((void**)dst, src.size() * sizeof(T));
+	if (e != cudaSuccess)
+		return e;
+	return cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+size_t state_size(const dgpu_ctx* c) { return (size_t)c->n_vol * c->nv * c->N; }
+
+// One residual (volume, face, lift) on the stream.
+dgpu_status enqueue_rhs(dgpu_ctx* c)
+{
+	DGPU_CUDA(c, c->launch_volume(c));
+	DGPU_CUDA(c, c->launch_face(c));
+	DGPU_CUDA(c, c->launch_lift_rhs(c));
+	return DGPU_OK;
+}
+
+dgpu_status enqueue_rk_step(dgpu_ctx* c, double dt)
+{
+	for (int stage = 0; stage < 3; ++stage) {
+		DGPU_CUDA(c, c->launch_volume(c));
+		DGPU_CUDA(c, c->launch_face(c));
+		DGPU_CUDA(c, c->launch_lift_rk(c, dt, stage));
+	}
+	return DGPU_OK;
+}
+
+dgpu_status read_max(dgpu_ctx* c, double* max_rhs)
+{
+	if (!max_rhs)
+		return DGPU_OK;
+	unsigned long long bits = 0;
+	DGPU_CUDA(c, cudaMemcpyAsync(&bits, c->max_bits, sizeof bits, cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	double v;
+	memcpy(&v, &bits, sizeof v);
+	*max_rhs = v;
+	return DGPU_OK;
+}
+
+dgpu_status check_positivity_flag(dgpu_ctx* c)
+{
+	if (!c->positivity)
+		return DGPU_OK;
+	int flag = 0;
+	DGPU_CUDA(c, cudaMemcpyAsync(&flag, c->err_flag, sizeof flag, cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	if (flag)
+		return fail(c, DGPU_ERR_POSITIVITY, "average density or pressure below EPS_PHYS");
+	return DGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dgpu_status_string(dgpu_status st)
+{
+	switch (st) {
+	case DGPU_OK: return "ok";
+	case DGPU_ERR_INVALID_ARGUMENT: return "invalid argument";
+	case DGPU_ERR_UNSUPPORTED: return "unsupported";
+	case DGPU_ERR_CUDA: return "CUDA error";
+	case DGPU_ERR_POSITIVITY: return "positivity failure";
+	case DGPU_ERR_NO_DEVICE: return "no sm_103 device";
+	default: return "unknown status";
+	}
+}
+
+const char* dgpu_last_error(const dgpu_ctx* ctx)
+{
+	return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, const dgpu_mesh* mesh,
+                        dgpu_ctx** out)
+{
+	g_create_error.clear();
+	if (!phys || !ops || !mesh || !out)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+	*out = nullptr;
+	const int d = phys->d;
+	if (d != 2 && d != 3)
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "d must be 2 or 3");
+	if ((d == 2 && ops->elem_type != DGPU_QUAD) || (d == 3 && ops->elem_type != DGPU_HEX))
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "element type must be QUAD (d=2) or HEX (d=3)");
+	if (ops->p < 1 || ops->p > kQMax - 1)
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "p must be in 1..4");
+	if (phys->pde == DGPU_PDE_ADVECTION) {
+		if (phys->num_flux != DGPU_NUM_FLUX_UPWIND)
+			return fail(nullptr, DGPU_ERR_UNSUPPORTED, "advection supports the upwind flux");
+	} else if (phys->pde == DGPU_PDE_EULER) {
+		if (phys->num_flux != DGPU_NUM_FLUX_ROE_PIKE && phys->num_flux != DGPU_NUM_FLUX_LAX_FRIEDRICHS)
+			return fail(nullptr, DGPU_ERR_UNSUPPORTED, "Euler supports Roe-Pike and Lax-Friedrichs");
+	} else {
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "pde must be advection or Euler");
+	}
+	if (!ops->cv0_vs_vc || !ops->cv1_vs_vc || !ops->cv0_vs_fc || !ops->w_vc)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL operator");
+	if (phys->pde == DGPU_PDE_EULER && phys->positivity && (!ops->ccSB0_vs_vs || !ops->ccBS0_vs_vs))
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "positivity needs ccSB0/ccBS0");
+	if (mesh->n_volumes < 1 || mesh->n_faces < 1 || !mesh->metrics_vc || !mesh->jacobian_det_vc ||
+	    !mesh->face_vol || !mesh->face_lf || !mesh->normals_fc || !mesh->jacobian_det_fc)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "incomplete mesh");
+
+	int dev = 0, n_dev = 0;
+	if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1)
+		return fail(nullptr, DGPU_ERR_NO_DEVICE, "no CUDA device");
+	cudaGetDevice(&dev);
+	cudaDeviceProp prop;
+	if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess || prop.major * 10 + prop.minor != 103)
+		return fail(nullptr, DGPU_ERR_NO_DEVICE, "device is not compute capability 10.3 (sm_103a build)");
+
+	dgpu_ctx* c = new dgpu_ctx();
+	c->d = d;
+	c->q = ops->p + 1;
+	const int q = c->q;
+	c->N = (d == 2 ? q * q : q * q * q);
+	c->NF = (d == 2 ? q : q * q);
+	c->pde = phys->pde;
+	c->flux = phys->num_flux;
+	c->nv = (phys->pde == DGPU_PDE_EULER ? d + 2 : 1);
+	c->positivity = (phys->pde == DGPU_PDE_EULER && phys->positivity) ? 1 : 0;
+	c->n_vol = mesh->n_volumes;
+	c->n_face = mesh->n_faces;
+	for (int k = 0; k < 3; ++k)
+		c->b_adv[k] = phys->b_adv[k];
+	const int N = c->N, NF = c->NF;
+
+	// ---- 1D operators: B, B^-1, GL collocation derivative, GL boundary values ----
+	memset(&c->ops, 0, sizeof c->ops);
+	double Bm[kQMax * kQMax], Bi[kQMax * kQMax];
+	for (int i = 0; i < q * q; ++i)
+		Bm[i] = ops->cv0_vs_vc[i];
+	if (!invert_small(q, Bm, Bi)) {
+		delete c;
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "cv0_vs_vc is singular");
+	}
+	for (int a = 0; a < q; ++a)
+		for (int m = 0; m < q; ++m) {
+			c->ops.B[a][m] = Bm[a * q + m];
+			c->ops.Binv[a][m] = Bi[a * q + m];
+			double s = 0.0;  // Dgl = cv1_vs_vc * B^-1
+			for (int k = 0; k < q; ++k)
+				s += ops->cv1_vs_vc[a * q + k] * Bi[k * q + m];
+			c->ops.Dgl[a][m] = s;
+			if (ops->ccSB0_vs_vs) c->ops.SB[a][m] = ops->ccSB0_vs_vs[a * q + m];
+			if (ops->ccBS0_vs_vs) c->ops.BS[a][m] = ops->ccBS0_vs_vs[a * q + m];
+		}
+	for (int s = 0; s < 2; ++s)
+		for (int m = 0; m < q; ++m) {
+			double acc = 0.0;  // l_gl(+-1) = cv0_vs_fc row * B^-1
+			for (int k = 0; k < q; ++k)
+				acc += ops->cv0_vs_fc[s * q + k] * Bi[k * q + m];
+			c->ops.lb[s][m] = acc;
+		}
+
+	// ---- weights: TP products of the 1D GL rule (first direction fastest) ----
+	std::vector<double> w(N), wf(NF);
+	for (int n = 0; n < N; ++n) {
+		int r = n;
+		double x = 1.0;
+		for (int k = 0; k < d; ++k) {
+			x *= ops->w_vc[r % q];
+			r /= q;
+		}
+		w[n] = x;
+	}
+	for (int n = 0; n < NF; ++n) {
+		int r = n;
+		double x = 1.0;
+		for (int k = 0; k < d - 1; ++k) {
+			x *= ops->w_vc[r % q];
+			r /= q;
+		}
+		wf[n] = x;
+	}
+
+	// ---- volume geometry ----
+	const size_t nV = (size_t)c->n_vol;
+	std::vector<double> gmet(nV * d * d * N), inv_wJ(nV * N);
+	for (size_t v = 0; v < nV; ++v) {
+		const double* m = mesh->metrics_vc + v * (size_t)N * d * d;
+		const double* J = mesh->jacobian_det_vc + v * (size_t)N;
+		for (int j = 0; j < d; ++j)
+			for (int i = 0; i < d; ++i)
+				for (int n = 0; n < N; ++n)
+					gmet[((v * d + j) * d + i) * N + n] = w[n] * m[n + (size_t)N * (i + d * j)];
+		for (int n = 0; n < N; ++n) {
+			if (!(J[n] > 0.0)) {
+				delete c;
+				return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "non-positive jacobian_det_vc");
+			}
+			inv_wJ[v * N + n] = 1.0 / (w[n] * J[n]);
+		}
+	}
+
+	// ---- faces ----
+	const size_t nF = (size_t)c->n_face;
+	std::vector<double> fgeo(nF * (d + 1) * NF);
+	std::vector<int> vol_face(nV * 2 * d, -1);
+	bool any_perm = false;
+	std::vector<int> nc, nc_inv;
+	if (mesh->nc_fc) {
+		nc.assign(mesh->nc_fc, mesh->nc_fc + nF * NF);
+		nc_inv.assign(nF * NF, -1);
+	}
+	for (size_t f = 0; f < nF; ++f) {
+		for (int s = 0; s < 2; ++s) {
+			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
+			if (v < 0) {
+				delete c;
+				return fail(nullptr, DGPU_ERR_UNSUPPORTED, "boundary faces are not supported (periodic meshes)");
+			}
+			if (v >= c->n_vol || lf < 0 || lf >= 2 * d || vol_face[(size_t)v * 2 * d + lf] != -1) {
+				delete c;
+				return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "bad face connectivity");
+			}
+			vol_face[(size_t)v * 2 * d + lf] = (int)(2 * f + s);
+		}
+		for (int i = 0; i < NF; ++i) {
+			for (int k = 0; k < d; ++k)
+				fgeo[(f * (d + 1) + k) * NF + i] = mesh->normals_fc[(f * NF + i) * d + k];
+			fgeo[(f * (d + 1) + d) * NF + i] = wf[i] * mesh->jacobian_det_fc[f * NF + i];
+		}
+		if (mesh->nc_fc) {
+			for (int i = 0; i < NF; ++i) {
+				const int t = nc[f * NF + i];
+				if (t < 0 || t >= NF || nc_inv[f * NF + t] != -1) {
+					delete c;
+					return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "nc_fc is not a permutation");
+				}
+				nc_inv[f * NF + t] = i;
+				if (t != i)
+					any_perm = true;
+			}
+		}
+	}
+	for (size_t i = 0; i < vol_face.size(); ++i)
+		if (vol_face[i] < 0) {
+			delete c;
+			return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "a volume face is missing from the face list");
+		}
+
+	// ---- device allocations ----
+	const size_t ns = state_size(c);
+#define DG_TRY(call)                                        \
+	do {                                                    \
+		cudaError_t e_ = (call);                            \
+		if (e_ != cudaSuccess) {                            \
+			std::string m_ = std::string(#call) + ": " + cudaGetErrorString(e_); \
+			free_all(c);                                    \
+			delete c;                                       \
+			return fail(nullptr, DGPU_ERR_CUDA, m_);        \
+		}                                                   \
+	} while (0)
+	DG_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+	c->own_stream = true;
+	DG_TRY(cudaMalloc((void**)&c->u, ns * sizeof(double)));
+	DG_TRY(cudaMalloc((void**)&c->u0, ns * sizeof(double)));
+	DG_TRY(cudaMalloc((void**)&c->rhs, ns * sizeof(double)));
+	DG_TRY(cudaMalloc((void**)&c->vol_gl, ns * sizeof(double)));
+	DG_TRY(cudaMalloc((void**)&c->traces, nF * 2 * c->nv * NF * sizeof(double)));
+	DG_TRY(cudaMalloc((void**)&c->nnf, nF * c->nv * NF * sizeof(double)));
+	DG_TRY(cudaMalloc((void**)&c->max_bits, sizeof(unsigned long long)));
+	DG_TRY(cudaMalloc((void**)&c->err_flag, sizeof(int)));
+	DG_TRY(cudaMalloc((void**)&c->n_corr, sizeof(unsigned long long)));
+	DG_TRY(cudaMemset(c->u, 0, ns * sizeof(double)));
+	DG_TRY(cudaMemset(c->u0, 0, ns * sizeof(double)));
+	DG_TRY(cudaMemset(c->rhs, 0, ns * sizeof(double)));
+	DG_TRY(cudaMemset(c->max_bits, 0, sizeof(unsigned long long)));
+	DG_TRY(cudaMemset(c->err_flag, 0, sizeof(int)));
+	DG_TRY(cudaMemset(c->n_corr, 0, sizeof(unsigned long long)));
+	DG_TRY(upload(&c->gmet, gmet));
+	DG_TRY(upload(&c->inv_wJ, inv_wJ));
+	DG_TRY(upload(&c->fgeo, fgeo));
+	DG_TRY(upload(&c->vol_face, vol_face));
+	if (any_perm) {
+		DG_TRY(upload(&c->nc, nc));
+		DG_TRY(upload(&c->nc_inv, nc_inv));
+	}
+	cudaError_t be = (d == 2 ? bind_q<2>(c) : bind_q<3>(c));
+	if (be != cudaSuccess) {
+		std::string m_ = std::string("kernel set-up: ") + cudaGetErrorString(be);
+		free_all(c);
+		delete c;
+		return fail(nullptr, DGPU_ERR_CUDA, m_);
+	}
+#undef DG_TRY
+	*out = c;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_destroy(dgpu_ctx* ctx)
+{
+	if (!ctx)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (ctx->stream)
+		cudaStreamSynchronize(ctx->stream);
+	free_all(ctx);
+	delete ctx;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_state_size(const dgpu_ctx* ctx, size_t* n)
+{
+	if (!ctx || !n)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	*n = state_size(ctx);
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_upload_state(dgpu_ctx* c, const double* sol)
+{
+	if (!c || !sol)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	DGPU_CUDA(c, cudaMemcpyAsync(c->u, sol, state_size(c) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_download_state(dgpu_ctx* c, double* sol)
+{
+	if (!c || !sol)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	DGPU_CUDA(c, cudaMemcpyAsync(sol, c->u, state_size(c) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_download_rhs(dgpu_ctx* c, double* rhs)
+{
+	if (!c || !rhs)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	DGPU_CUDA(c, cudaMemcpyAsync(rhs, c->rhs, state_size(c) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_compute_rhs(dgpu_ctx* c, double* max_rhs)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	dgpu_status st = enqueue_rhs(c);
+	if (st != DGPU_OK)
+		return st;
+	return read_max(c, max_rhs);
+}
+
+dgpu_status dgpu_compute_rhs_host(dgpu_ctx* c, const double* sol, double* rhs, double* max_rhs)
+{
+	if (!c || !sol || !rhs)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	const size_t bytes = state_size(c) * sizeof(double);
+	DGPU_CUDA(c, cudaMemcpyAsync(c->u, sol, bytes, cudaMemcpyHostToDevice, c->stream));
+	dgpu_status st = enqueue_rhs(c);
+	if (st != DGPU_OK)
+		return st;
+	DGPU_CUDA(c, cudaMemcpyAsync(rhs, c->rhs, bytes, cudaMemcpyDeviceToHost, c->stream));
+	if (max_rhs)
+		return read_max(c, max_rhs);
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_ssp_rk3_steps(dgpu_ctx* c, double dt, int n_steps, double* max_rhs)
+{
+	if (!c || n_steps < 0 || !(dt == dt))
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->timing) {
+		for (int s = 0; s < n_steps; ++s) {
+			dgpu_status st = enqueue_rk_step(c, dt);
+			if (st != DGPU_OK)
+				return st;
+		}
+	} else {
+		if (!c->rk_graph || c->rk_graph_dt != dt) {
+			if (c->rk_graph) {
+				cudaGraphExecDestroy(c->rk_graph);
+				c->rk_graph = nullptr;
+			}
+			cudaGraph_t g;
+			DGPU_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+			const long long before = c->launches;
+			dgpu_status st = enqueue_rk_step(c, dt);
+			c->launches = before;  // captured, not launched
+			cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+			if (st != DGPU_OK)
+				return st;
+			DGPU_CUDA(c, ec);
+			DGPU_CUDA(c, cudaGraphInstantiate(&c->rk_graph, g, 0));
+			cudaGraphDestroy(g);
+			c->rk_graph_dt = dt;
+		}
+		for (int s = 0; s < n_steps; ++s) {
+			DGPU_CUDA(c, cudaGraphLaunch(c->rk_graph, c->stream));
+			c->launches += 9;
+		}
+	}
+	dgpu_status st = check_positivity_flag(c);
+	if (st != DGPU_OK)
+		return st;
+	return read_max(c, max_rhs);
+}
+
+dgpu_status dgpu_ssp_rk3_step(dgpu_ctx* c, double dt, double* max_rhs)
+{
+	return dgpu_ssp_rk3_steps(c, dt, 1, max_rhs);
+}
+
+dgpu_status dgpu_positivity_corrections(dgpu_ctx* c, long long* n)
+{
+	if (!c || !n)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	unsigned long long v = 0;
+	DGPU_CUDA(c, cudaMemcpyAsync(&v, c->n_corr, sizeof v, cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	*n = (long long)v;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_kernel_launches(const dgpu_ctx* c, long long* n)
+{
+	if (!c || !n)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	*n = c->launches;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_synchronize(dgpu_ctx* c)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_set_stream(dgpu_ctx* c, void* stream)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	if (c->own_stream)
+		cudaStreamDestroy(c->stream);
+	c->own_stream = false;
+	c->stream = (cudaStream_t)stream;
+	if (c->rk_graph) {
+		cudaGraphExecDestroy(c->rk_graph);
+		c->rk_graph = nullptr;
+	}
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_set_kernel_timing(dgpu_ctx* c, int enable)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	for (auto& t : c->timers) {
+		cudaEventDestroy(t.start);
+		cudaEventDestroy(t.stop);
+	}
+	c->timers.clear();
+	c->timing = enable != 0;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_kernel_time(dgpu_ctx* c, const char* name, double* total_ms, long long* count)
+{
+	if (!c || !name || !total_ms || !count)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	double tot = 0.0;
+	long long n = 0;
+	for (auto& t : c->timers) {
+		if (strcmp(t.name, name) != 0)
+			continue;
+		float ms = 0.f;
+		DGPU_CUDA(c, cudaEventElapsedTime(&ms, t.start, t.stop));
+		tot += ms;
+		++n;
+	}
+	*total_ms = tot;
+	*count = n;
+	return DGPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// FP64 FMA throughput probe: 8 independent dependency chains per thread, no memory traffic in the loop.
+__global__ void fp64_fma_probe_kernel(double* out, int iters, double a, double b)
+{
+	double x[8];
+#pragma unroll
+	for (int k = 0; k < 8; ++k)
+		x[k] = (threadIdx.x + 1) * 1e-9 + k;
+	for (int i = 0; i < iters; ++i) {
+#pragma unroll
+		for (int k = 0; k < 8; ++k)
+			x[k] = fma(x[k], a, b);
+	}
+	double s = 0.0;
+#pragma unroll
+	for (int k = 0; k < 8; ++k)
+		s += x[k];
+	out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" dgpu_status dgpu_probe_fp64(int iters, double* tflops)
+{
+	if (iters < 1 || !tflops)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	int dev = 0, sms = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+		return DGPU_ERR_NO_DEVICE;
+	const int threads = 256, blocks = sms * 8;
+	double* out = nullptr;
+	if (cudaMalloc((void**)&out, (size_t)threads * blocks * sizeof(double)) != cudaSuccess)
+		return DGPU_ERR_CUDA;
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	fp64_fma_probe_kernel<<<blocks, threads>>>(out, 16, 0.999999, 1e-7);  // warm-up
+	cudaEventRecord(e0);
+	fp64_fma_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+	cudaEventRecord(e1);
+	cudaError_t e = cudaEventSynchronize(e1);
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(out);
+	if (e != cudaSuccess)
+		return DGPU_ERR_CUDA;
+	const double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+	*tflops = flops / (ms * 1e-3) / 1e12;
+	return DGPU_OK;
+}

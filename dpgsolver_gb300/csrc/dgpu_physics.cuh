@@ -1,0 +1,199 @@
+// Flux physics for the explicit DG residual, FP64, as device inline functions.
+//
+// Each function states the reference routine whose arithmetic it follows. The numerical fluxes keep the
+// reference's operation order where it matters for the result's rounding (sums of normal-flux components,
+// the entropy-fix comparisons on real parts).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace dgpu {
+
+constexpr double kGamma = 1.4;          // definitions_physics.h:23
+constexpr double kGm1 = 0.4;            // definitions_physics.h:24
+constexpr double kEpsPhys = 1.0e-13;    // definitions_physics.h:30
+constexpr double kEps = 1.0e-15;        // definitions_tol.h:23
+
+enum Pde { kAdvection = 1, kEuler = 3 };
+enum NumFlux { kUpwind = 11, kRoePike = 31, kLaxFriedrichs = 32 };
+
+// min_abs_real_T / max_abs_real_T (general/math_functions_T.c:222-236), real instantiation.
+__device__ __forceinline__ double min_abs_real(double a, double b)
+{
+	double c = (fabs(a) < fabs(b) ? a : b);
+	return (c < 0.0 ? -c : c);
+}
+__device__ __forceinline__ double max_abs_real(double a, double b)
+{
+	double c = (fabs(a) > fabs(b) ? a : b);
+	return (c < 0.0 ? -c : c);
+}
+
+// Contravariant volume flux at one cubature node for the Euler equations:
+//   fr_j[eq] = sum_i g[j*D+i] f_i[eq]
+// with f the physical flux of compute_Flux_T_euler / compute_Flux_euler_0 (flux_euler_T.c:71-143, 259-298)
+// and g the metric terms (pre-multiplied by the cubature weight) of constructor_flux_ref_piece_T
+// (compute_rlhs_T.c:71-110). The contraction is regrouped through the contravariant velocity
+// U_j = sum_i g[j*D+i] u_i, which is the same sum with fewer FP64 operations.
+template <int D>
+__device__ __forceinline__ void euler_flux_ref(const double* W, const double* g, double (*fr)[D + 2])
+{
+	const double rho = W[0], E = W[D + 1];
+	const double rho_inv = 1.0 / rho;
+	double u[D];
+	double V2 = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		u[k] = rho_inv * W[1 + k];
+		V2 += u[k] * u[k];
+	}
+	const double p = kGm1 * (E - 0.5 * rho * V2);
+	const double Ep = E + p;
+#pragma unroll
+	for (int j = 0; j < D; ++j) {
+		double U = 0.0;
+#pragma unroll
+		for (int i = 0; i < D; ++i)
+			U += g[j * D + i] * u[i];
+		fr[j][0] = rho * U;
+#pragma unroll
+		for (int m = 0; m < D; ++m)
+			fr[j][1 + m] = W[1 + m] * U + p * g[j * D + m];
+		fr[j][D + 1] = Ep * U;
+	}
+}
+
+// Physical Euler flux f[k][eq] (compute_Flux_euler_0, flux_euler_T.c:259-298).
+template <int D>
+__device__ __forceinline__ void euler_flux(const double* W, double (*f)[D + 2])
+{
+	const double rho = W[0], E = W[D + 1];
+	const double rho_inv = 1.0 / rho;
+	double u[D];
+	double V2 = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		u[k] = rho_inv * W[1 + k];
+		V2 += u[k] * u[k];
+	}
+	const double p = kGm1 * (E - 0.5 * rho * V2);
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		f[k][0] = W[1 + k];
+#pragma unroll
+		for (int m = 0; m < D; ++m)
+			f[k][1 + m] = W[1 + m] * u[k] + (m == k ? p : 0.0);
+		f[k][D + 1] = (E + p) * u[k];
+	}
+}
+
+// Lax-Friedrichs (compute_Numerical_Flux_T_euler_lax_friedrichs, numerical_flux_euler_T.c:60-327).
+template <int D>
+__device__ __forceinline__ void num_flux_lax_friedrichs(const double* WL, const double* WR, const double* n,
+                                                        double* nF)
+{
+	double VL, VR, cL, cR;
+	{
+		const double rho = WL[0], rho_inv = 1.0 / rho;
+		double V2 = 0.0;
+#pragma unroll
+		for (int k = 0; k < D; ++k) {
+			const double u = WL[1 + k] * rho_inv;
+			V2 += u * u;
+		}
+		VL = sqrt(V2);
+		const double p = kGm1 * (WL[D + 1] - 0.5 * rho * V2);
+		cL = sqrt(kGamma * p / rho);
+	}
+	{
+		const double rho = WR[0], rho_inv = 1.0 / rho;
+		double V2 = 0.0;
+#pragma unroll
+		for (int k = 0; k < D; ++k) {
+			const double u = WR[1 + k] * rho_inv;
+			V2 += u * u;
+		}
+		VR = sqrt(V2);
+		const double p = kGm1 * (WR[D + 1] - 0.5 * rho * V2);
+		cR = sqrt(kGamma * p / rho);
+	}
+	const double maxlL = VL + cL, maxlR = VR + cR;
+	const double maxV = (maxlL > maxlR ? maxlL : maxlR);
+	double FL[D][D + 2], FR[D][D + 2];
+	euler_flux<D>(WL, FL);
+	euler_flux<D>(WR, FR);
+#pragma unroll
+	for (int eq = 0; eq < D + 2; ++eq) {
+		double s = 0.0;
+#pragma unroll
+		for (int k = 0; k < D; ++k)
+			s += n[k] * (FL[k][eq] + FR[k][eq]);
+		nF[eq] = 0.5 * (s + maxV * (WL[eq] - WR[eq]));
+	}
+}
+
+// Roe-Pike with the entropy fix of Qu et al. 2015 (compute_Numerical_Flux_T_euler_roe_pike,
+// numerical_flux_euler_T.c:470-778).
+template <int D>
+__device__ __forceinline__ void num_flux_roe_pike(const double* WL, const double* WR, const double* n, double* nF)
+{
+	const double rhoL = WL[0], rhoR = WR[0], EL = WL[D + 1], ER = WR[D + 1];
+	const double rhoL_inv = 1.0 / rhoL, rhoR_inv = 1.0 / rhoR;
+	double uL[D], uR[D];
+	double V2L = 0.0, V2R = 0.0, VnL = 0.0, VnR = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		uL[k] = WL[1 + k] * rhoL_inv;
+		uR[k] = WR[1 + k] * rhoR_inv;
+		V2L += uL[k] * uL[k];
+		V2R += uR[k] * uR[k];
+		VnL += n[k] * uL[k];
+		VnR += n[k] * uR[k];
+	}
+	const double pL = kGm1 * (EL - 0.5 * rhoL * V2L), HL = (EL + pL) * rhoL_inv;
+	const double pR = kGm1 * (ER - 0.5 * rhoR * V2R), HR = (ER + pR) * rhoR_inv;
+
+	const double r = sqrt(rhoR / rhoL), rP1 = r + 1.0, rho = r * rhoL;
+	double u[D];
+	double Vn = 0.0, V2 = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		u[k] = (r * uR[k] + uL[k]) / rP1;
+		Vn += n[k] * u[k];
+		V2 += u[k] * u[k];
+	}
+	const double H = (r * HR + HL) / rP1, c2 = kGm1 * (H - 0.5 * V2), c = sqrt(c2);
+
+	const double l1 = min_abs_real(VnL - c, Vn - c), l5 = max_abs_real(VnR + c, Vn + c);
+	const double l234 = (Vn > 0.0 ? Vn : -Vn);
+
+	const double drho = rhoR - rhoL, dE = ER - EL, dp = pR - pL, dVn = VnR - VnL;
+	const double lc1 = 0.5 * (l5 + l1) - l234, lc2 = 0.5 * (l5 - l1);
+	const double disInter1 = lc1 * dp / (c * c) + lc2 * rho * dVn / c;
+	const double disInter2 = lc1 * rho * dVn + lc2 * dp / c;
+
+	const double rhoVnL = rhoL * VnL, rhoVnR = rhoR * VnR, pLR = pL + pR;
+	nF[0] = 0.5 * ((rhoVnL + rhoVnR) - (l234 * drho + disInter1));
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		const double drhou = rhoR * uR[k] - rhoL * uL[k];
+		const double nFk = rhoVnL * uL[k] + rhoVnR * uR[k] + n[k] * pLR;
+		const double disk = l234 * drhou + disInter1 * u[k] + disInter2 * n[k];
+		nF[1 + k] = 0.5 * (nFk - disk);
+	}
+	nF[D + 1] = 0.5 * ((VnL * (EL + pL) + VnR * (ER + pR)) - (l234 * dE + disInter1 * H + disInter2 * Vn));
+}
+
+// Upwind advection flux (compute_Numerical_Flux_T_advection_upwind, numerical_flux_advection_T.c:39-75).
+template <int D>
+__device__ __forceinline__ double num_flux_upwind(double uL, double uR, const double* n, const double* b)
+{
+	double b_dot_n = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		b_dot_n += b[k] * n[k];
+	return (b_dot_n > kEps ? b_dot_n * uL : b_dot_n * uR);
+}
+
+}  // namespace dgpu

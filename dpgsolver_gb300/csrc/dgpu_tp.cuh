@@ -1,0 +1,556 @@
+// Tensor-product (QUAD/HEX) explicit DG residual kernels for sm_103a, FP64.
+//
+// Formulation. The reference applies dense per-element operators (operator_T.c:96-156 -> cblas_dgemm):
+//   R = M^-1 [ sum_d tw1_vt_vc[d] fr_d - sum_faces tw0_vt_fc nnf ],   M = V^T diag(w J) V,
+// with V = cv0_vs_vc. On TP elements with GLL solution nodes and (p+1)-point GL cubature V = B (x) B (x) B is
+// square and invertible (B = 1D GLL->GL interpolation), cv1_vs_vc[d] = Dgl_d V (GL collocation derivative,
+// exact for degree p), and cv0_vs_fc[lf] = E_lf V (E_lf = GL Lagrange values at the face). Hence
+//   R = V^-1 diag(1/(w J)) [ sum_d Dgl_d^T (w fr_d) - sum_lf E_lf^T (w_f J_f F*) ],
+// which is the same operator in exact arithmetic with the V^-T V^T pair cancelled: every contraction is a
+// 1D sum-factorised pass of q FMAs per node, and the dense per-element M^-1 (n_vs^2 doubles per element in
+// the reference) is never formed.
+//
+// Kernels per residual:
+//   tp_volume_kernel   u (GLL coefficients) -> u_gl = V u; volume term in GL space; face traces of u_gl.
+//   tp_face_kernel     per face node: numerical flux of the two traces, scaled by w_f J_f.
+//   tp_lift_kernel     lift of the face fluxes, diag(1/(wJ)), V^-1, then either the residual (with the
+//                      max |rhs| reduction of compute_max_rhs_dg_like) or an SSP-RK3 stage update followed by
+//                      the positivity check of enforce_positivity_highorder.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dgpu_physics.cuh"
+
+namespace dgpu {
+
+constexpr int kQMax = 5;  // p <= 4
+
+// 1D operators of one (element type, p), derived on the host from the caller's ops_tp factors.
+struct TPOps {
+	double B[kQMax][kQMax];     // GLL -> GL interpolation  B[m][a]
+	double Binv[kQMax][kQMax];  // GL -> GLL                 Binv[a][m]
+	double Dgl[kQMax][kQMax];   // GL collocation derivative Dgl[m][k] = l_k'(x_m)
+	double lb[2][kQMax];        // GL Lagrange basis at r = -1 / +1
+	double SB[kQMax][kQMax];    // ccSB0 1D (Lagrange -> Bezier)
+	double BS[kQMax][kQMax];    // ccBS0 1D (Bezier -> Lagrange)
+};
+
+struct TPParams {
+	int n_vol;
+	int n_face;
+	double b_adv[3];
+	const int* vol_face;       // [v][2D]: face * 2 + side
+	const double* gmet;        // [v][D*D][N]: w_vc * metrics, component j*D+i = w J dr_j/dx_i
+	const double* inv_wJ;      // [v][N]: 1 / (w_vc J_vc)
+	const double* fgeo;        // [f][D+1][NF]: unit normal (D) and w_fc J_f
+	const int* nc;             // [f][NF] right-trace gather permutation, or nullptr (identity)
+	const int* nc_inv;         // [f][NF] its inverse, or nullptr
+	double* traces;            // [f][2][NV][NF]
+	double* nnf;               // [f][NV][NF]
+	double* vol_gl;            // [v][NV][N]
+	unsigned long long* max_bits;  // max |rhs| as the bit pattern of a non-negative double
+	int* err_flag;             // positivity failure flag
+	unsigned long long* n_corr;    // positivity corrections applied
+};
+
+template <int D, int Q>
+struct TPShape {
+	static constexpr int N = (D == 2 ? Q * Q : Q * Q * Q);
+	static constexpr int NF = (D == 2 ? Q : Q * Q);
+	static constexpr int E = (N >= 256 ? 1 : 256 / N);   // elements per CTA
+	static constexpr int THREADS = ((E * N + 31) / 32) * 32;  // whole warps; surplus threads idle
+};
+
+__device__ __forceinline__ int pow_q(int q, int k) { return k == 0 ? 1 : (k == 1 ? q : q * q); }
+
+// Index of the node along direction `dir`.
+template <int Q>
+__device__ __forceinline__ int node_coord(int node, int dir)
+{
+	return dir == 0 ? node % Q : (dir == 1 ? (node / Q) % Q : node / (Q * Q));
+}
+
+// One sum-factorised pass along `dir`: out[var][node] = sum_m M[a(node)][m] in[var][node with a -> m].
+// TRANS selects M^T (M[m][a]).
+template <int D, int Q, int NV, bool TRANS>
+__device__ __forceinline__ void tp_pass(const double* __restrict__ in, double* __restrict__ out,
+                                        const double (*M)[kQMax], int dir, int node)
+{
+	constexpr int N = TPShape<D, Q>::N;
+	const int stride = (dir == 0 ? 1 : (dir == 1 ? Q : Q * Q));
+	const int a = node_coord<Q>(node, dir);
+	const int base = node - a * stride;
+	double w[Q];
+#pragma unroll
+	for (int m = 0; m < Q; ++m)
+		w[m] = TRANS ? M[m][a] : M[a][m];
+#pragma unroll
+	for (int v = 0; v < NV; ++v) {
+		double s = 0.0;
+#pragma unroll
+		for (int m = 0; m < Q; ++m)
+			s += w[m] * in[v * N + base + m * stride];
+		out[v * N + node] = s;
+	}
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double x)
+{
+	atomicMax(addr, (unsigned long long)__double_as_longlong(x));
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Volume term + traces
+// ---------------------------------------------------------------------------------------------------------------
+template <int D, int Q, int NV, int PDE>
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
+tp_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u)
+{
+	using S = TPShape<D, Q>;
+	constexpr int N = S::N, NF = S::NF, E = S::E;
+	extern __shared__ double smem[];
+	TPOps* sops = reinterpret_cast<TPOps*>(smem);
+	double* base = smem + (sizeof(TPOps) + 7) / 8;
+	// per element: su[NV*N] (u, then u_gl), st[NV*N] (tmp), sf[D*NV*N] (reference flux)
+	constexpr int PER_E = NV * N * 2 + D * NV * N;
+
+	const int tid = threadIdx.x;
+	for (int i = tid; i < (int)(sizeof(TPOps) / 8); i += blockDim.x)
+		reinterpret_cast<double*>(sops)[i] = reinterpret_cast<const double*>(&ops)[i];
+
+	const int v0 = blockIdx.x * E;
+	const int n_here = min(E, P.n_vol - v0);
+	// coalesced load of n_here contiguous element blocks
+	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {
+		const int e = i / (NV * N), r = i % (NV * N);
+		base[e * PER_E + r] = u[(size_t)v0 * NV * N + i];
+	}
+	if (blockIdx.x == 0 && tid == 0 && P.max_bits)
+		*P.max_bits = 0ull;
+	__syncthreads();
+
+	const int e = tid / N, node = tid % N;
+	const bool active = e < n_here;
+	double* su = base + e * PER_E;
+	double* st = su + NV * N;
+	double* sf = st + NV * N;
+
+	// u_gl = V u : D passes of B, ending in su
+	if (D == 2) {
+		if (active) tp_pass<D, Q, NV, false>(su, st, sops->B, 0, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(st, su, sops->B, 1, node);
+	} else {
+		if (active) tp_pass<D, Q, NV, false>(su, st, sops->B, 0, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(st, sf, sops->B, 1, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(sf, su, sops->B, 2, node);
+	}
+	__syncthreads();
+
+	const int v = v0 + e;
+	if (active) {
+		double W[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			W[k] = su[k * N + node];
+		double g[D * D];
+#pragma unroll
+		for (int c = 0; c < D * D; ++c)
+			g[c] = P.gmet[((size_t)v * D * D + c) * N + node];
+		if constexpr (PDE == kEuler) {
+			double fr[D][D + 2];
+			euler_flux_ref<D>(W, g, fr);
+#pragma unroll
+			for (int j = 0; j < D; ++j)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					sf[(j * NV + k) * N + node] = fr[j][k];
+		} else {
+			// advection: f_i = b_i u ; fr_j = sum_i g[j][i] b_i u
+#pragma unroll
+			for (int j = 0; j < D; ++j) {
+				double gb = 0.0;
+#pragma unroll
+				for (int i = 0; i < D; ++i)
+					gb += g[j * D + i] * P.b_adv[i];
+				sf[j * N + node] = gb * W[0];
+			}
+		}
+	}
+	__syncthreads();
+
+	if (active) {
+		// volume term in GL space: sum_j Dgl_j^T (w fr_j)
+		double acc[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			acc[k] = 0.0;
+#pragma unroll
+		for (int j = 0; j < D; ++j) {
+			const int stride = (j == 0 ? 1 : (j == 1 ? Q : Q * Q));
+			const int a = node_coord<Q>(node, j);
+			const int b0 = node - a * stride;
+			double w[Q];
+#pragma unroll
+			for (int m = 0; m < Q; ++m)
+				w[m] = sops->Dgl[m][a];
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				const double* f = sf + (j * NV + k) * N + b0;
+#pragma unroll
+				for (int m = 0; m < Q; ++m)
+					acc[k] += w[m] * f[m * stride];
+			}
+		}
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			P.vol_gl[((size_t)v * NV + k) * N + node] = acc[k];
+
+		// traces of u_gl on the 2D local faces
+		for (int it = node; it < 2 * D * NF; it += N) {
+			const int lf = it / NF, t = it % NF;
+			const int nd = lf >> 1, side = lf & 1;
+			int t0, t1;
+			if (D == 2) {
+				t0 = t; t1 = 0;
+			} else {
+				t0 = t % Q; t1 = t / Q;
+			}
+			// node index with coordinate m along nd and tangential (t0, t1) in ascending direction order
+			int stride_n, base_n;
+			if (D == 2) {
+				stride_n = (nd == 0 ? 1 : Q);
+				base_n = (nd == 0 ? t0 * Q : t0);
+			} else {
+				stride_n = (nd == 0 ? 1 : (nd == 1 ? Q : Q * Q));
+				base_n = (nd == 0 ? t0 * Q + t1 * Q * Q : (nd == 1 ? t0 + t1 * Q * Q : t0 + t1 * Q));
+			}
+			const int fs = P.vol_face[(size_t)v * 2 * D + lf];
+			double* dst = P.traces + (size_t)fs * NV * NF;
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				double s = 0.0;
+#pragma unroll
+				for (int m = 0; m < Q; ++m)
+					s += sops->lb[side][m] * su[k * N + base_n + m * stride_n];
+				dst[k * NF + t] = s;
+			}
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Face numerical flux
+// ---------------------------------------------------------------------------------------------------------------
+template <int D, int Q, int NV, int PDE, int FLUX>
+__global__ void __launch_bounds__(256)
+tp_face_kernel(const TPParams P)
+{
+	using S = TPShape<D, Q>;
+	constexpr int NF = S::NF;
+	const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= P.n_face * NF)
+		return;
+	const int f = gid / NF, i = gid % NF;
+	const int iR = P.nc ? P.nc[(size_t)f * NF + i] : i;
+	const double* tL = P.traces + (size_t)(2 * f) * NV * NF;
+	const double* tR = P.traces + (size_t)(2 * f + 1) * NV * NF;
+	double WL[NV], WR[NV], n[D];
+#pragma unroll
+	for (int k = 0; k < NV; ++k) {
+		WL[k] = tL[k * NF + i];
+		WR[k] = tR[k * NF + iR];
+	}
+	const double* fg = P.fgeo + (size_t)f * (D + 1) * NF;
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		n[k] = fg[k * NF + i];
+	const double sc = fg[D * NF + i];
+	double* out = P.nnf + (size_t)f * NV * NF;
+	if constexpr (PDE == kEuler) {
+		double nF[NV];
+		if constexpr (FLUX == kRoePike)
+			num_flux_roe_pike<D>(WL, WR, n, nF);
+		else
+			num_flux_lax_friedrichs<D>(WL, WR, n, nF);
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			out[k * NF + i] = nF[k] * sc;
+	} else {
+		out[i] = num_flux_upwind<D>(WL[0], WR[0], n, P.b_adv) * sc;
+	}
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Lift + M^-1 + (residual | RK stage + positivity)
+// ---------------------------------------------------------------------------------------------------------------
+enum LiftMode { kModeRhs = 0, kModeRk = 1 };
+
+struct RkArgs {
+	double* u;         // state (GLL coefficients), updated in place
+	double* u0;        // stage-0 copy (sol_coef_p)
+	double* rhs;       // residual output (kModeRhs)
+	double dt;
+	int stage;         // 0, 1, 2
+	int positivity;
+};
+
+// enforce_positivity_highorder (solve.c:187-233) on one element held in shared memory. `c` holds the element's
+// conserved state (GLL coefficients) [NV][N]; `b` is scratch [NV][N]. Returns true when a correction was made
+// (c then holds the corrected coefficients). Runs the reference's serial averages/minima on one thread; the
+// Bezier transforms are sum-factorised passes by the element's threads.
+template <int D, int Q, int NV>
+__device__ bool tp_positivity(const TPOps* ops, double* c, double* b, double* tmp, int node, bool active,
+                              int* flag_out, const TPParams& P)
+{
+	constexpr int N = TPShape<D, Q>::N;
+	// Bezier coefficients: ccSB0 passes  (c -> b)
+	if (D == 2) {
+		if (active) tp_pass<D, Q, NV, false>(c, tmp, ops->SB, 0, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(tmp, b, ops->SB, 1, node);
+	} else {
+		if (active) tp_pass<D, Q, NV, false>(c, b, ops->SB, 0, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(b, tmp, ops->SB, 1, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(tmp, b, ops->SB, 2, node);
+	}
+	__syncthreads();
+	// convert_variables c -> p per coefficient (solution_euler_T.c:173-194)
+	if (active) {
+		const double rho = b[node];
+		const double rho_inv = 1.0 / rho;
+		double rho2V2 = 0.0;
+#pragma unroll
+		for (int k = 0; k < D; ++k) {
+			const double m = b[(1 + k) * N + node];
+			rho2V2 += m * m;
+			b[(1 + k) * N + node] = m * rho_inv;
+		}
+		b[(D + 1) * N + node] = kGm1 * (b[(D + 1) * N + node] - 0.5 * rho2V2 * rho_inv);
+	}
+	__syncthreads();
+	int corrected = 0;
+	if (active && node == 0) {
+		for (int vr = 0; vr < NV; vr += NV - 1) {
+			const double* vd = b + vr * N;
+			double s = 0.0, mn = vd[0];
+			for (int i = 0; i < N; ++i) {
+				s += vd[i];
+				if (vd[i] < mn)
+					mn = vd[i];
+			}
+			const double avg = s / N;
+			if (avg < kEpsPhys) {
+				*flag_out = 1;
+				break;
+			}
+			if (mn < kEpsPhys) {
+				double p_ho = (avg - kEpsPhys) / (avg - mn);
+				p_ho = fmax(0.0, fmin(1.0, p_ho));
+				// correct_coef (solve.c:356-374)
+				for (int w = 0; w < NV; ++w) {
+					double* data = b + w * N;
+					double aw = 0.0;
+					for (int i = 0; i < N; ++i)
+						aw += data[i];
+					aw /= N;
+					if ((w == 0 || w == NV - 1) && aw < kEpsPhys)
+						aw = kEpsPhys;
+					for (int i = 0; i < N; ++i)
+						data[i] = p_ho * data[i] + (1 - p_ho) * aw;
+				}
+				corrected = 1;
+			}
+		}
+		tmp[0] = corrected;  // broadcast through shared memory (tmp is free here)
+	}
+	__syncthreads();
+	corrected = active ? (int)tmp[0] : 0;
+	__syncthreads();
+	// The whole CTA must take the same barriers: the slow path runs when any element corrected.
+	const int any = __syncthreads_or(corrected);
+	if (!any)
+		return false;
+	if (corrected) {
+		// convert p -> c per coefficient, then ccBS0 passes back to GLL coefficients
+		const double rho = b[node];
+		double V2 = 0.0;
+#pragma unroll
+		for (int k = 0; k < D; ++k) {
+			const double uu = b[(1 + k) * N + node];
+			V2 += uu * uu;
+			b[(1 + k) * N + node] = rho * uu;
+		}
+		b[(D + 1) * N + node] = b[(D + 1) * N + node] / kGm1 + 0.5 * rho * V2;
+	}
+	__syncthreads();
+	if (D == 2) {
+		if (corrected) tp_pass<D, Q, NV, false>(b, tmp, ops->BS, 0, node);
+		__syncthreads();
+		if (corrected) tp_pass<D, Q, NV, false>(tmp, c, ops->BS, 1, node);
+	} else {
+		if (corrected) tp_pass<D, Q, NV, false>(b, tmp, ops->BS, 0, node);
+		__syncthreads();
+		if (corrected) tp_pass<D, Q, NV, false>(tmp, b, ops->BS, 1, node);
+		__syncthreads();
+		if (corrected) tp_pass<D, Q, NV, false>(b, c, ops->BS, 2, node);
+	}
+	__syncthreads();
+	return corrected != 0;
+}
+
+template <int D, int Q, int NV, int MODE>
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
+tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
+{
+	using S = TPShape<D, Q>;
+	constexpr int N = S::N, NF = S::NF, E = S::E;
+	extern __shared__ double smem[];
+	TPOps* sops = reinterpret_cast<TPOps*>(smem);
+	double* base = smem + (sizeof(TPOps) + 7) / 8;
+	constexpr int PER_E = 3 * NV * N;
+
+	const int tid = threadIdx.x;
+	for (int i = tid; i < (int)(sizeof(TPOps) / 8); i += blockDim.x)
+		reinterpret_cast<double*>(sops)[i] = reinterpret_cast<const double*>(&ops)[i];
+
+	const int v0 = blockIdx.x * E;
+	const int n_here = min(E, P.n_vol - v0);
+	const int e = tid / N, node = tid % N;
+	const bool active = e < n_here;
+	const int v = v0 + e;
+	double* sa = base + e * PER_E;
+	double* sb = sa + NV * N;
+	double* sc = sb + NV * N;
+
+	if (active) {
+		double r[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			r[k] = P.vol_gl[((size_t)v * NV + k) * N + node];
+#pragma unroll
+		for (int lf = 0; lf < 2 * D; ++lf) {
+			const int fs = P.vol_face[(size_t)v * 2 * D + lf];
+			const int f = fs >> 1, s = fs & 1;
+			const int nd = lf >> 1;
+			const int a = node_coord<Q>(node, nd);
+			int t;
+			if (D == 2) {
+				t = (nd == 0 ? node_coord<Q>(node, 1) : node_coord<Q>(node, 0));
+			} else {
+				const int c0 = node_coord<Q>(node, 0), c1 = node_coord<Q>(node, 1), c2 = node_coord<Q>(node, 2);
+				t = (nd == 0 ? c1 + Q * c2 : (nd == 1 ? c0 + Q * c2 : c0 + Q * c1));
+			}
+			const int idx = (s == 1 && P.nc_inv) ? P.nc_inv[(size_t)f * NF + t] : t;
+			// side 0: rhs -= E^T nnf ; side 1: rhs -= E^T (-nnf)   (compute_face_rlhs_T.c:297-310)
+			const double l = (s == 0 ? -1.0 : 1.0) * sops->lb[lf & 1][a];
+			const double* src = P.nnf + (size_t)f * NV * NF;
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				r[k] += l * src[k * NF + idx];
+		}
+		const double iw = P.inv_wJ[(size_t)v * N + node];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			sa[k * N + node] = r[k] * iw;
+	}
+	__syncthreads();
+	// V^-1: D passes of Binv, result in sa (D even) / sc (D odd)
+	double* res;
+	if (D == 2) {
+		if (active) tp_pass<D, Q, NV, false>(sa, sb, sops->Binv, 0, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(sb, sa, sops->Binv, 1, node);
+		res = sa;
+	} else {
+		if (active) tp_pass<D, Q, NV, false>(sa, sb, sops->Binv, 0, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(sb, sc, sops->Binv, 1, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV, false>(sc, sa, sops->Binv, 2, node);
+		res = sa;
+	}
+	__syncthreads();
+
+	// max |rhs| (compute_max_rhs_dg_like): integer max over the bit patterns of |R|
+	unsigned long long mx = 0ull;
+	double R[NV];
+	if (active) {
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			R[k] = res[k * N + node];
+			const unsigned long long bits = (unsigned long long)__double_as_longlong(R[k]) & 0x7fffffffffffffffull;
+			mx = bits > mx ? bits : mx;
+		}
+	}
+#pragma unroll
+	for (int off = 16; off > 0; off >>= 1) {
+		const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
+		mx = o > mx ? o : mx;
+	}
+	if ((tid & 31) == 0 && mx && P.max_bits)
+		atomicMax(P.max_bits, mx);
+
+	if constexpr (MODE == kModeRhs) {
+		if (active) {
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				rk.rhs[((size_t)v * NV + k) * N + node] = R[k];
+		}
+		return;
+	}
+
+	// SSP-RK3 stage update (solve_explicit.c:277-295)
+	double snew[NV];
+	if (active) {
+		const size_t o = (size_t)v * NV * N + node;
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			const double s = rk.u[o + (size_t)k * N];
+			if (rk.stage == 0) {
+				rk.u0[o + (size_t)k * N] = s;
+				snew[k] = s + rk.dt * R[k];
+			} else if (rk.stage == 1) {
+				const double sp = rk.u0[o + (size_t)k * N];
+				snew[k] = (1.0 / 4.0) * (3.0 * sp + s + rk.dt * R[k]);
+			} else {
+				const double sp = rk.u0[o + (size_t)k * N];
+				snew[k] = (1.0 / 3.0) * (sp + 2.0 * s + 2.0 * rk.dt * R[k]);
+			}
+		}
+	}
+	if (rk.positivity) {
+		// element state to shared memory for the Bezier check
+		if (active) {
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				sb[k * N + node] = snew[k];
+		}
+		__syncthreads();
+		int flag = 0;
+		const bool corr = tp_positivity<D, Q, NV>(sops, sb, sc, sa, node, active, &flag, P);
+		if (flag)
+			atomicExch(P.err_flag, 1);
+		if (corr) {
+			if (node == 0)
+				atomicAdd(P.n_corr, 1ull);
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				snew[k] = sb[k * N + node];
+		}
+	}
+	if (active) {
+		const size_t o = (size_t)v * NV * N + node;
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			rk.u[o + (size_t)k * N] = snew[k];
+	}
+}
+
+}  // namespace dgpu

@@ -1,0 +1,171 @@
+"""Host-side mirror of the reference's explicit DG entry points, over the C ABI of include/dgpu.h.
+
+    sim = Simulation(problem)             # constructor_derived_computational_elements + m_inv set-up
+    max_rhs = compute_rhs_dg(sim)         # solvers/dg/solve_dg.c:130-136
+    max_rhs = time_step_ssp_rk_33(dt, sim)  # solvers/solve_explicit.c:252-301 (static there)
+    solve_explicit(sim, n_steps)          # the time loop of solvers/solve_explicit.c:78-118
+
+``sim.sol_coef`` / ``sim.rhs`` give the per-volume (n_vs x n_var) column-major blocks, as arrays of shape
+(n_volumes, n_var, n_vs). Errors raise DGPUError with the library's status; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import DGPUError, check  # noqa: F401  (re-exported)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_lib.c_double_p)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_lib.c_int_p)
+
+
+class Simulation:
+    """One dgpu context for a TP DGProblem (dpgsolver_gb300.host.problem)."""
+
+    def __init__(self, prob, stream=None):
+        lib = _lib.load()
+        ops, mesh, geom = prob.ops, prob.mesh, prob.geom
+        d = prob.d
+        self._keep = keep = {}
+
+        def arr(name, a, dtype=np.float64):
+            keep[name] = np.ascontiguousarray(a, dtype=dtype)
+            return keep[name]
+
+        phys = _lib.Physics()
+        phys.d, phys.pde, phys.num_flux = d, prob.pde, prob.num_flux
+        phys.positivity = 1 if prob.positivity else 0
+        for k in range(3):
+            phys.b_adv[k] = float(prob.b_adv[k])
+        tp = _lib.TPOperators()
+        tp.elem_type = ops.e_type
+        tp.p = ops.p
+        tp.cv0_vs_vc = _dp(arr("cv0", ops.cv0_1d))
+        tp.cv1_vs_vc = _dp(arr("cv1", ops.cv1_1d))
+        tp.cv0_vs_fc = _dp(arr("cv0f", ops.cv0_bnd_1d))
+        tp.w_vc = _dp(arr("w", ops.w_vc_1d))
+        tp.ccSB0_vs_vs = _dp(arr("sb", ops.ccSB0_1d))
+        tp.ccBS0_vs_vs = _dp(arr("bs", ops.ccBS0_1d))
+        m = _lib.Mesh()
+        m.n_volumes = mesh.n_volumes
+        m.metrics_vc = _dp(arr("m", np.transpose(geom.metrics_vc, (0, 3, 2, 1))))
+        m.jacobian_det_vc = _dp(arr("J", geom.jacobian_det_vc))
+        m.n_faces = mesh.n_faces
+        m.face_vol = _ip(arr("fv", mesh.face_vol, np.int32))
+        m.face_lf = _ip(arr("flf", mesh.face_lf, np.int32))
+        nc = prob.nc_fc()
+        m.nc_fc = _ip(arr("nc", nc, np.int32))
+        m.normals_fc = _dp(arr("nrm", geom.normals_fc))
+        m.jacobian_det_fc = _dp(arr("Jf", geom.jacobian_det_fc))
+        h = ctypes.c_void_p()
+        st = lib.dgpu_create(ctypes.byref(phys), ctypes.byref(tp), ctypes.byref(m), ctypes.byref(h))
+        check(st, None)
+        self._lib = lib
+        self._h = h
+        self._keep = {}  # the library copied everything
+        self.prob = prob
+        self.shape = prob.sol.shape
+        if stream is not None:
+            check(lib.dgpu_set_stream(h, ctypes.c_void_p(stream)), h)
+        self.upload_state(prob.sol)
+
+    # -- lifetime ------------------------------------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.dgpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- state ---------------------------------------------------------------------------------------------------
+    def upload_state(self, sol):
+        s = np.ascontiguousarray(sol, dtype=np.float64)
+        if s.shape != self.shape:
+            raise ValueError(f"state shape {s.shape} != {self.shape}")
+        check(self._lib.dgpu_upload_state(self._h, _dp(s)), self._h)
+
+    @property
+    def sol_coef(self):
+        out = np.empty(self.shape)
+        check(self._lib.dgpu_download_state(self._h, _dp(out)), self._h)
+        return out
+
+    @property
+    def rhs(self):
+        out = np.empty(self.shape)
+        check(self._lib.dgpu_download_rhs(self._h, _dp(out)), self._h)
+        return out
+
+    # -- compute -------------------------------------------------------------------------------------------------
+    def compute_rhs(self, want_max: bool = True):
+        mx = ctypes.c_double()
+        check(self._lib.dgpu_compute_rhs(self._h, ctypes.byref(mx) if want_max else None), self._h)
+        return mx.value if want_max else None
+
+    def compute_rhs_host(self, sol, out=None):
+        s = np.ascontiguousarray(sol, dtype=np.float64)
+        r = out if out is not None else np.empty(self.shape)
+        mx = ctypes.c_double()
+        check(self._lib.dgpu_compute_rhs_host(self._h, _dp(s), _dp(r), ctypes.byref(mx)), self._h)
+        return r, mx.value
+
+    def ssp_rk3_steps(self, dt: float, n_steps: int = 1, want_max: bool = True):
+        mx = ctypes.c_double()
+        check(self._lib.dgpu_ssp_rk3_steps(self._h, float(dt), int(n_steps), ctypes.byref(mx) if want_max else None),
+              self._h)
+        return mx.value if want_max else None
+
+    def synchronize(self):
+        check(self._lib.dgpu_synchronize(self._h), self._h)
+
+    def positivity_corrections(self) -> int:
+        n = ctypes.c_longlong()
+        check(self._lib.dgpu_positivity_corrections(self._h, ctypes.byref(n)), self._h)
+        return n.value
+
+    def kernel_launches(self) -> int:
+        n = ctypes.c_longlong()
+        check(self._lib.dgpu_kernel_launches(self._h, ctypes.byref(n)), self._h)
+        return n.value
+
+    def set_kernel_timing(self, enable: bool):
+        check(self._lib.dgpu_set_kernel_timing(self._h, 1 if enable else 0), self._h)
+
+    def kernel_time(self, name: str):
+        tot = ctypes.c_double()
+        cnt = ctypes.c_longlong()
+        check(self._lib.dgpu_kernel_time(self._h, name.encode(), ctypes.byref(tot), ctypes.byref(cnt)), self._h)
+        return tot.value, cnt.value
+
+
+def compute_rhs_dg(sim: Simulation) -> float:
+    """compute_rhs_dg (solvers/dg/solve_dg.c:130-136): residual of sim's state into sim's rhs; max |rhs|."""
+    return sim.compute_rhs()
+
+
+def time_step_ssp_rk_33(dt: float, sim: Simulation) -> float:
+    """time_step_ssp_rk_33 (solvers/solve_explicit.c:252-301): one SSP-RK3 step; max |rhs| of the last stage."""
+    return sim.ssp_rk3_steps(dt, 1)
+
+
+def solve_explicit(sim: Simulation, n_steps: int, dt: float | None = None) -> float:
+    """The explicit time loop (solvers/solve_explicit.c:78-118) for a fixed number of steps."""
+    return sim.ssp_rk3_steps(sim.prob.dt if dt is None else dt, n_steps)

@@ -1,0 +1,142 @@
+/* dgpu.h -- C ABI of the GB300 (sm_103a) explicit DG residual for DPGSolver.
+ *
+ * Plain C, no C++ or CUDA types in any signature. Every entry returns a dgpu_status (DGPU_OK == 0); the
+ * library never aborts. All device memory is owned by the opaque context; one CUDA stream per context; no
+ * global state, so separate contexts may be used from separate host threads.
+ *
+ * Entry points and the reference interface each one replaces (paths inside DPGSolver):
+ *   dgpu_create            set-up of the DG solver volumes/faces that solve_explicit performs before its time loop:
+ *                          constructor_derived_computational_elements(IL_SOLVER_DG) and the inverse mass matrices
+ *                          (src/simulation/solvers/solve_explicit.c:86-89,
+ *                           src/simulation/solvers/dg/volume_solver_dg_T.c:49-78)
+ *   dgpu_upload_state      writes every Solver_Volume_T::sol_coef (src/simulation/solvers/volume_solver_T.h:31-104)
+ *   dgpu_download_state    reads them back
+ *   dgpu_compute_rhs       double compute_rhs_dg(const struct Simulation*)  (src/simulation/solvers/dg/solve_dg.c:130-136)
+ *                          = compute_volume_rlhs_dg (compute_volume_rlhs_dg.h) + compute_face_rlhs_dg
+ *                          (compute_face_rlhs_dg.h) + scale_rhs_by_m_inv + compute_max_rhs_dg_like
+ *   dgpu_download_rhs      reads every Solver_Volume_T::rhs
+ *   dgpu_compute_rhs_host  compute_rhs_dg with host sol_coef in and host rhs out (one call, copies included)
+ *   dgpu_ssp_rk3_step      static double time_step_ssp_rk_33(double dt, const struct Simulation*)
+ *                          (src/simulation/solvers/solve_explicit.c:252-301), positivity included
+ *                          (enforce_positivity_highorder, src/simulation/solvers/solve.c:187-233)
+ *   dgpu_ssp_rk3_steps     n_steps iterations of the time loop body of solve_explicit (solve_explicit.c:92-112)
+ */
+#ifndef DGPU_H
+#define DGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int dgpu_status;
+#define DGPU_OK                   0
+#define DGPU_ERR_INVALID_ARGUMENT 1  /* a NULL, size or index out of range                                  */
+#define DGPU_ERR_UNSUPPORTED      2  /* element type, order, PDE or flux not provided by this library        */
+#define DGPU_ERR_CUDA             3  /* a CUDA runtime call failed (dgpu_last_error names it)                */
+#define DGPU_ERR_POSITIVITY       4  /* average density or pressure below EPS_PHYS (reference: EXIT_ERROR,
+                                        src/simulation/solvers/solve.c:204-208)                             */
+#define DGPU_ERR_NO_DEVICE        5  /* no CUDA device of compute capability 10.3                            */
+
+/* PDE, numerical flux and element codes: the reference's own values
+ * (src/simulation/test_case/definitions_test_case.h, src/simulation/solvers/numerical_flux/
+ *  definitions_numerical_flux.h, src/element/definitions_elements.h). */
+#define DGPU_PDE_ADVECTION 1
+#define DGPU_PDE_EULER     3
+#define DGPU_NUM_FLUX_UPWIND          11
+#define DGPU_NUM_FLUX_ROE_PIKE        31
+#define DGPU_NUM_FLUX_LAX_FRIEDRICHS  32
+#define DGPU_QUAD 3
+#define DGPU_HEX  5
+
+typedef struct dgpu_ctx dgpu_ctx;
+
+/* Test-case parameters (Test_Case_T fields pde_index, num_flux_1st, and the advection velocity of
+ * solution_advection_T.c; constant velocity only). */
+typedef struct {
+	int d;              /* 2 or 3 (the reference's compile-time DIM)                       */
+	int pde;            /* DGPU_PDE_*                                                       */
+	int num_flux;       /* DGPU_NUM_FLUX_*                                                  */
+	int positivity;     /* 1: enforce_positivity_highorder after every RK stage (Euler)     */
+	double b_adv[3];    /* advection velocity (advection only)                              */
+} dgpu_physics;
+
+/* Tensor-product operator set of one (element type, p): the 1D factors of the reference's Operator::ops_tp
+ * (src/simulation/operators/operator.h:40-44) for the solution basis (Lagrange on GLL nodes, q = p+1) and
+ * the GL cubature (q points). All matrices row-major. */
+typedef struct {
+	int elem_type;               /* DGPU_QUAD or DGPU_HEX                                      */
+	int p;                       /* 1..4                                                       */
+	const double* cv0_vs_vc;     /* (q x q): basis at the volume cubature nodes                */
+	const double* cv1_vs_vc;     /* (q x q): first derivative at the volume cubature nodes     */
+	const double* cv0_vs_fc;     /* (2 x q): basis at r = -1 and r = +1                        */
+	const double* w_vc;          /* (q):     GL cubature weights                               */
+	const double* ccSB0_vs_vs;   /* (q x q): Lagrange -> Bezier coefficients (positivity)      */
+	const double* ccBS0_vs_vs;   /* (q x q): Bezier -> Lagrange coefficients (positivity)      */
+} dgpu_tp_operators;
+
+/* Geometry and connectivity packed from the Solver_Volume / Solver_Face lists in list order. */
+typedef struct {
+	int n_volumes;
+	const double* metrics_vc;      /* n_volumes x (n_vc, d, d) column-major: Solver_Volume_T::metrics_vc */
+	const double* jacobian_det_vc; /* n_volumes x n_vc: Solver_Volume_T::jacobian_det_vc                */
+	int n_faces;
+	const int* face_vol;           /* n_faces x 2: volume index of neigh_info[0] / neigh_info[1]        */
+	const int* face_lf;            /* n_faces x 2: neigh_info[s].ind_lf                                 */
+	const int* nc_fc;              /* n_faces x n_fc or NULL: right-trace gather permutation
+	                                  (get_operator__nc_fc_T(1, face), compute_face_rlhs_T.c:133-146);
+	                                  NULL means the identity for every face                           */
+	const double* normals_fc;      /* n_faces x (n_fc x d) row-major: Solver_Face_T::normals_fc         */
+	const double* jacobian_det_fc; /* n_faces x n_fc: Solver_Face_T::jacobian_det_fc                    */
+} dgpu_mesh;
+
+/* Create a context on the current CUDA device and copy everything it needs; the caller may free its arrays
+ * when this returns. State size = n_volumes * n_var * q^d doubles, per volume the reference's (n_vs x n_var)
+ * column-major sol_coef block. */
+dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, const dgpu_mesh* mesh,
+                        dgpu_ctx** out);
+dgpu_status dgpu_destroy(dgpu_ctx* ctx);
+
+dgpu_status dgpu_state_size(const dgpu_ctx* ctx, size_t* n_doubles);
+dgpu_status dgpu_upload_state(dgpu_ctx* ctx, const double* sol);      /* host -> device, synchronous */
+dgpu_status dgpu_download_state(dgpu_ctx* ctx, double* sol);          /* device -> host, synchronous */
+dgpu_status dgpu_download_rhs(dgpu_ctx* ctx, double* rhs);            /* device -> host, synchronous */
+
+/* Residual of the device state into the device rhs (M^-1 applied). max_rhs may be NULL (then nothing is
+ * synchronised); otherwise it receives max |rhs| after the stream finishes. */
+dgpu_status dgpu_compute_rhs(dgpu_ctx* ctx, double* max_rhs);
+/* Same with host buffers: sol (host) -> device, residual, device -> rhs (host). */
+dgpu_status dgpu_compute_rhs_host(dgpu_ctx* ctx, const double* sol, double* rhs, double* max_rhs);
+
+/* One SSP-RK3 step on the device state (three residuals, stage updates and positivity), replayed from a CUDA
+ * graph captured on first use for each dt. max_rhs: as for dgpu_compute_rhs (last stage's residual). */
+dgpu_status dgpu_ssp_rk3_step(dgpu_ctx* ctx, double dt, double* max_rhs);
+dgpu_status dgpu_ssp_rk3_steps(dgpu_ctx* ctx, double dt, int n_steps, double* max_rhs);
+
+/* Number of positivity corrections applied since creation (enforce_positivity_highorder's correct_coef). */
+dgpu_status dgpu_positivity_corrections(dgpu_ctx* ctx, long long* n);
+/* Kernels this context has launched (graph replays count each kernel node). */
+dgpu_status dgpu_kernel_launches(const dgpu_ctx* ctx, long long* n);
+/* Synchronise the context's stream. */
+dgpu_status dgpu_synchronize(dgpu_ctx* ctx);
+/* Run the context's work on the caller's cudaStream_t (passed as void*) instead of its own stream. The
+ * caller keeps ownership of the stream; any captured step graph is discarded. No reference counterpart
+ * (the reference is serial host code). */
+dgpu_status dgpu_set_stream(dgpu_ctx* ctx, void* cuda_stream);
+/* Per-kernel timing with CUDA events around every eager launch (steps then run without a graph).
+ * dgpu_kernel_time sums the recorded durations of the kernels named `name` ("tp_volume_kernel",
+ * "tp_face_kernel", "tp_lift_kernel"). Measurement aids; no reference counterpart. */
+dgpu_status dgpu_set_kernel_timing(dgpu_ctx* ctx, int enable);
+dgpu_status dgpu_kernel_time(dgpu_ctx* ctx, const char* name, double* total_ms, long long* count);
+/* Text of the last error recorded on this context (or of the last failed dgpu_create when ctx is NULL). */
+const char* dgpu_last_error(const dgpu_ctx* ctx);
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (8 independent chains per thread, `iters`
+ * iterations): the denominator of the FP64-pipe roofline. Measurement aid; no reference counterpart. */
+dgpu_status dgpu_probe_fp64(int iters, double* tflops);
+const char* dgpu_status_string(dgpu_status st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DGPU_H */

@@ -1,0 +1,399 @@
+/* CPU oracle for the explicit DG residual path of DPGSolver.
+ *
+ * TEST INFRASTRUCTURE ONLY. This plain-C restatement of the reference's algorithm is the checker that the
+ * CUDA path is compared against; only tests, the smoke check and the CPU-baseline leg of the benchmark load
+ * it. Nothing in the product links or calls it.
+ *
+ * It follows the reference's own data flow with dense ("op_std", op_format 'd') operators, element by
+ * element, in volume-list and face-list order:
+ *   compute_rhs_dg            src/simulation/solvers/dg/solve_dg.c:130-136
+ *   compute_rlhs_common_dg    src/simulation/solvers/dg/solve_dg.c:182-189
+ *   scale_rhs_by_m_inv_std    src/simulation/solvers/dg/solve_dg.c:265-272
+ *   compute_max_rhs_dg_like   src/simulation/solvers/compute_rlhs.c:59-71
+ *   time_step_ssp_rk_33       src/simulation/solvers/solve_explicit.c:252-301
+ *   enforce_positivity_highorder  src/simulation/solvers/solve.c:187-233, correct_coef :356-374
+ *   constructor_mass_T / constructor_inverse_mass_T  src/simulation/solvers/volume_solver_T.c:115-145
+ * The double instantiation gives the residual and the time step; the double complex instantiation gives the
+ * complex-step linearisation the reference uses in test_support_solve_dg.c:83-110.
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "dg_oracle.h"
+
+#define GAMMA 1.4          /* definitions_physics.h:23 */
+#define GM1 0.4            /* definitions_physics.h:24 */
+#define EPS_PHYS 1.0e-13   /* definitions_physics.h:30 */
+#define ORACLE_EPS 1.0e-15 /* definitions_tol.h:23 */
+
+struct oracle_ctx {
+	struct oracle_problem P;
+	double* m_inv;   /* per volume n_vs x n_vs row-major */
+	/* owned copies of the problem arrays */
+	double *cv0_vs_vc, *tw1_vt_vc, *cv0_vs_fc, *tw0_vt_fc, *w_vc, *ccSB0, *ccBS0;
+	double *metrics_vc, *jacobian_det_vc, *normals_fc, *jacobian_det_fc;
+	int *face_vol, *face_lf, *nc_fc;
+};
+
+/* ---- double instantiation ---- */
+#define Type double
+#define SUF(name) name##_d
+#define REAL_T(x) (x)
+#define ABS_T(x) fabs(x)
+#define SQRT_T(x) sqrt(x)
+#include "dg_oracle_T.h"
+#undef Type
+#undef SUF
+#undef REAL_T
+#undef ABS_T
+#undef SQRT_T
+
+/* ---- double complex instantiation ---- */
+#define Type double complex
+#define SUF(name) name##_c
+#define REAL_T(x) creal(x)
+#define ABS_T(x) cabs(x)
+#define SQRT_T(x) csqrt(x)
+#include "dg_oracle_T.h"
+#undef Type
+#undef SUF
+#undef REAL_T
+#undef ABS_T
+#undef SQRT_T
+
+static double* dup_d(const double* src, size_t n)
+{
+	if (!src || n == 0)
+		return NULL;
+	double* p = malloc(sizeof(double) * n);
+	memcpy(p, src, sizeof(double) * n);
+	return p;
+}
+
+static int* dup_i(const int* src, size_t n)
+{
+	if (!src || n == 0)
+		return NULL;
+	int* p = malloc(sizeof(int) * n);
+	memcpy(p, src, sizeof(int) * n);
+	return p;
+}
+
+/* Inverse by Gauss-Jordan elimination with partial pivoting (the reference solves with the identity as
+ * right-hand side through LAPACKE, matrix_constructors_T.c constructor_inverse_const_Matrix_T). */
+static int invert(const int n, const double* A, double* Ainv)
+{
+	double* a = malloc(sizeof(double) * (size_t)n * n);
+	memcpy(a, A, sizeof(double) * (size_t)n * n);
+	for (int i = 0; i < n; ++i)
+		for (int j = 0; j < n; ++j)
+			Ainv[i * n + j] = (i == j ? 1.0 : 0.0);
+	for (int col = 0; col < n; ++col) {
+		int piv = col;
+		for (int r = col + 1; r < n; ++r)
+			if (fabs(a[r * n + col]) > fabs(a[piv * n + col]))
+				piv = r;
+		if (a[piv * n + col] == 0.0) {
+			free(a);
+			return ORACLE_ERR_SINGULAR;
+		}
+		if (piv != col) {
+			for (int j = 0; j < n; ++j) {
+				double t = a[col * n + j]; a[col * n + j] = a[piv * n + j]; a[piv * n + j] = t;
+				t = Ainv[col * n + j]; Ainv[col * n + j] = Ainv[piv * n + j]; Ainv[piv * n + j] = t;
+			}
+		}
+		const double inv = 1.0 / a[col * n + col];
+		for (int j = 0; j < n; ++j) {
+			a[col * n + j] *= inv;
+			Ainv[col * n + j] *= inv;
+		}
+		for (int r = 0; r < n; ++r) {
+			if (r == col)
+				continue;
+			const double fct = a[r * n + col];
+			if (fct == 0.0)
+				continue;
+			for (int j = 0; j < n; ++j) {
+				a[r * n + j] -= fct * a[col * n + j];
+				Ainv[r * n + j] -= fct * Ainv[col * n + j];
+			}
+		}
+	}
+	free(a);
+	return ORACLE_OK;
+}
+
+int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
+{
+	if (!in || !out)
+		return ORACLE_ERR_ARG;
+	if (in->d < 2 || in->d > 3 || in->n_volumes < 1 || in->n_vs < 1 || in->n_vc < 1 || in->n_fc < 1)
+		return ORACLE_ERR_ARG;
+	if (in->pde == ORACLE_PDE_EULER && in->n_var != in->d + 2)
+		return ORACLE_ERR_ARG;
+	if (in->pde == ORACLE_PDE_ADVECTION && in->n_var != 1)
+		return ORACLE_ERR_ARG;
+	struct oracle_ctx* c = calloc(1, sizeof *c);
+	c->P = *in;
+	const int d = in->d, n_vs = in->n_vs, n_vc = in->n_vc, n_fc = in->n_fc, n_lf = 2 * d;
+	const size_t nV = (size_t)in->n_volumes, nF = (size_t)in->n_faces;
+	c->P.cv0_vs_vc = c->cv0_vs_vc = dup_d(in->cv0_vs_vc, (size_t)n_vc * n_vs);
+	c->P.tw1_vt_vc = c->tw1_vt_vc = dup_d(in->tw1_vt_vc, (size_t)d * n_vs * n_vc);
+	c->P.cv0_vs_fc = c->cv0_vs_fc = dup_d(in->cv0_vs_fc, (size_t)n_lf * n_fc * n_vs);
+	c->P.tw0_vt_fc = c->tw0_vt_fc = dup_d(in->tw0_vt_fc, (size_t)n_lf * n_vs * n_fc);
+	c->P.w_vc = c->w_vc = dup_d(in->w_vc, (size_t)n_vc);
+	c->P.ccSB0 = c->ccSB0 = dup_d(in->ccSB0, (size_t)n_vs * n_vs);
+	c->P.ccBS0 = c->ccBS0 = dup_d(in->ccBS0, (size_t)n_vs * n_vs);
+	c->P.metrics_vc = c->metrics_vc = dup_d(in->metrics_vc, nV * n_vc * d * d);
+	c->P.jacobian_det_vc = c->jacobian_det_vc = dup_d(in->jacobian_det_vc, nV * n_vc);
+	c->P.normals_fc = c->normals_fc = dup_d(in->normals_fc, nF * n_fc * d);
+	c->P.jacobian_det_fc = c->jacobian_det_fc = dup_d(in->jacobian_det_fc, nF * n_fc);
+	c->P.face_vol = c->face_vol = dup_i(in->face_vol, nF * 2);
+	c->P.face_lf = c->face_lf = dup_i(in->face_lf, nF * 2);
+	c->P.nc_fc = c->nc_fc = dup_i(in->nc_fc, nF * n_fc);
+
+	/* M = cv0_vs_vc^T diag(w_vc J_vc) cv0_vs_vc, m_inv = M^-1 (volume_solver_T.c:115-145) */
+	c->m_inv = malloc(sizeof(double) * nV * n_vs * n_vs);
+	double* M = malloc(sizeof(double) * (size_t)n_vs * n_vs);
+	for (size_t v = 0; v < nV; ++v) {
+		const double* J = &c->jacobian_det_vc[v * n_vc];
+		for (int i = 0; i < n_vs; ++i)
+			for (int j = 0; j < n_vs; ++j) {
+				double s = 0.0;
+				for (int k = 0; k < n_vc; ++k)
+					s += c->cv0_vs_vc[k * n_vs + i] * (c->w_vc[k] * J[k]) * c->cv0_vs_vc[k * n_vs + j];
+				M[i * n_vs + j] = s;
+			}
+		int st = invert(n_vs, M, &c->m_inv[v * n_vs * n_vs]);
+		if (st != ORACLE_OK) {
+			free(M);
+			oracle_destroy(c);
+			return st;
+		}
+	}
+	free(M);
+	*out = c;
+	return ORACLE_OK;
+}
+
+void oracle_destroy(struct oracle_ctx* c)
+{
+	if (!c)
+		return;
+	free(c->m_inv);
+	free(c->cv0_vs_vc); free(c->tw1_vt_vc); free(c->cv0_vs_fc); free(c->tw0_vt_fc); free(c->w_vc);
+	free(c->ccSB0); free(c->ccBS0);
+	free(c->metrics_vc); free(c->jacobian_det_vc); free(c->normals_fc); free(c->jacobian_det_fc);
+	free(c->face_vol); free(c->face_lf); free(c->nc_fc);
+	free(c);
+}
+
+size_t oracle_state_size(const struct oracle_ctx* c)
+{
+	return (size_t)c->P.n_volumes * c->P.n_vs * c->P.n_var;
+}
+
+int oracle_compute_rhs(const struct oracle_ctx* c, const double* sol, double* rhs, double* max_rhs)
+{
+	int st = residual_raw_d(c, sol, rhs);
+	if (st != ORACLE_OK)
+		return st;
+	scale_m_inv_d(c, rhs);
+	double mx = 0.0;
+	const size_t n = oracle_state_size(c);
+	for (size_t i = 0; i < n; ++i)
+		if (fabs(rhs[i]) > mx)
+			mx = fabs(rhs[i]);
+	if (max_rhs)
+		*max_rhs = mx;
+	return ORACLE_OK;
+}
+
+int oracle_compute_rhs_raw(const struct oracle_ctx* c, const double* sol, double* rhs)
+{
+	return residual_raw_d(c, sol, rhs);
+}
+
+int oracle_compute_rhs_cmplx(const struct oracle_ctx* c, const double* sol_re, const double* sol_im,
+                             double* rhs_re, double* rhs_im)
+{
+	const size_t n = oracle_state_size(c);
+	double complex* s = malloc(sizeof(double complex) * n);
+	double complex* r = malloc(sizeof(double complex) * n);
+	for (size_t i = 0; i < n; ++i)
+		s[i] = sol_re[i] + I * (sol_im ? sol_im[i] : 0.0);
+	int st = residual_raw_c(c, s, r);
+	if (st == ORACLE_OK) {
+		scale_m_inv_c(c, r);
+		for (size_t i = 0; i < n; ++i) {
+			rhs_re[i] = creal(r[i]);
+			rhs_im[i] = cimag(r[i]);
+		}
+	}
+	free(s);
+	free(r);
+	return st;
+}
+
+/* convert_variables_T (solution_euler_T.c:136-200) on one volume's (n_n x n_var) column-major block. */
+static void convert_c_to_p(const int d, const int n_n, double* v)
+{
+	double* rho = &v[0];
+	double* E = &v[(size_t)n_n * (d + 1)];
+	for (int i = 0; i < n_n; ++i) {
+		const double rho_inv = 1.0 / rho[i];
+		double rho2V2 = 0.0;
+		for (int k = 0; k < d; ++k) {
+			double* m = &v[(size_t)n_n * (1 + k)];
+			rho2V2 += m[i] * m[i];
+			m[i] = m[i] * rho_inv;
+		}
+		E[i] = GM1 * (E[i] - 0.5 * rho2V2 * rho_inv);
+	}
+}
+
+static void convert_p_to_c(const int d, const int n_n, double* v)
+{
+	double* rho = &v[0];
+	double* p = &v[(size_t)n_n * (d + 1)];
+	for (int i = 0; i < n_n; ++i) {
+		double V2 = 0.0;
+		for (int k = 0; k < d; ++k) {
+			double* u = &v[(size_t)n_n * (1 + k)];
+			V2 += u[i] * u[i];
+			u[i] = rho[i] * u[i];
+		}
+		p[i] = p[i] / GM1 + 0.5 * rho[i] * V2;
+	}
+}
+
+static double average(const double* a, int n)
+{
+	double s = 0.0;
+	for (int i = 0; i < n; ++i)
+		s += a[i];
+	return s / n;
+}
+
+/* enforce_positivity_highorder (solve.c:187-233) for one volume. Returns 1 when correct_coef was applied
+ * (for density, pressure or both), 0 when not, or a negative error. */
+static int enforce_positivity(const struct oracle_ctx* c, double* s_coef)
+{
+	const struct oracle_problem* P = &c->P;
+	const int n_n = P->n_vs, n_vr = P->n_var, d = P->d;
+	double* sb = calloc((size_t)n_n * n_vr, sizeof(double));
+	mm_acc_d(n_n, n_n, n_vr, 1.0, P->ccSB0, s_coef, sb);
+	convert_c_to_p(d, n_n, sb);
+	int n_corr = 0;
+	for (int vr = 0; vr < n_vr; vr += n_vr - 1) {
+		double* vd = &sb[(size_t)vr * n_n];
+		const double vr_avg = average(vd, n_n);
+		if (vr_avg < EPS_PHYS) {
+			free(sb);
+			return ORACLE_ERR_POSITIVITY;
+		}
+		double vr_min = vd[0];
+		for (int i = 1; i < n_n; ++i)
+			if (vd[i] < vr_min)
+				vr_min = vd[i];
+		if (vr_min < EPS_PHYS) {
+			double p_ho = (vr_avg - EPS_PHYS) / (vr_avg - vr_min);
+			p_ho = fmax(0.0, fmin(1.0, p_ho));
+			/* correct_coef (solve.c:356-374) */
+			for (int w = 0; w < n_vr; ++w) {
+				double* data = &sb[(size_t)w * n_n];
+				double avg = average(data, n_n);
+				if ((w == 0 || w == n_vr - 1) && avg < EPS_PHYS)
+					avg = EPS_PHYS;
+				for (int i = 0; i < n_n; ++i)
+					data[i] = p_ho * data[i] + (1 - p_ho) * avg;
+			}
+			n_corr = 1;
+		}
+		if (n_vr == 1)
+			break;
+	}
+	convert_p_to_c(d, n_n, sb);
+	for (size_t i = 0; i < (size_t)n_n * n_vr; ++i)
+		s_coef[i] = 0.0;
+	mm_acc_d(n_n, n_n, n_vr, 1.0, P->ccBS0, sb, s_coef);
+	free(sb);
+	return n_corr;
+}
+
+int oracle_ssp_rk3_step(const struct oracle_ctx* c, const double dt, double* sol, double* max_rhs,
+                        int* n_corrections)
+{
+	const struct oracle_problem* P = &c->P;
+	const size_t n = oracle_state_size(c);
+	const size_t vs_sz = (size_t)P->n_vs * P->n_var;
+	double* rhs = malloc(sizeof(double) * n);
+	double* sp = malloc(sizeof(double) * n);
+	double mx = 0.0;
+	int ncorr = 0;
+	int st = ORACLE_OK;
+	for (int rk = 0; rk < 3 && st == ORACLE_OK; ++rk) {
+		st = oracle_compute_rhs(c, sol, rhs, &mx);
+		if (st != ORACLE_OK)
+			break;
+		for (int v = 0; v < P->n_volumes; ++v) {
+			double* s = &sol[(size_t)v * vs_sz];
+			double* p = &sp[(size_t)v * vs_sz];
+			const double* r = &rhs[(size_t)v * vs_sz];
+			switch (rk) {
+			case 0:
+				for (size_t i = 0; i < vs_sz; ++i) {
+					p[i] = s[i];
+					s[i] += dt * r[i];
+				}
+				break;
+			case 1:
+				for (size_t i = 0; i < vs_sz; ++i)
+					s[i] = (1.0 / 4.0) * (3.0 * p[i] + s[i] + dt * r[i]);
+				break;
+			default:
+				for (size_t i = 0; i < vs_sz; ++i)
+					s[i] = (1.0 / 3.0) * (p[i] + 2.0 * s[i] + 2.0 * dt * r[i]);
+				break;
+			}
+			if (P->positivity) {
+				int k = enforce_positivity(c, s);
+				if (k < 0) {
+					st = k;
+					break;
+				}
+				ncorr += k;
+			}
+		}
+	}
+	free(rhs);
+	free(sp);
+	if (max_rhs)
+		*max_rhs = mx;
+	if (n_corrections)
+		*n_corrections = ncorr;
+	return st;
+}
+
+int oracle_enforce_positivity(const struct oracle_ctx* c, double* sol, int* n_corrections)
+{
+	const size_t vs_sz = (size_t)c->P.n_vs * c->P.n_var;
+	int ncorr = 0;
+	for (int v = 0; v < c->P.n_volumes; ++v) {
+		int k = enforce_positivity(c, &sol[(size_t)v * vs_sz]);
+		if (k < 0)
+			return k;
+		ncorr += k;
+	}
+	if (n_corrections)
+		*n_corrections = ncorr;
+	return ORACLE_OK;
+}
+
+const double* oracle_m_inv(const struct oracle_ctx* c)
+{
+	return c->m_inv;
+}

@@ -1,0 +1,275 @@
+/* Templated body of the CPU oracle; included twice by dg_oracle.c (Type = double, Type = double complex),
+ * the way the reference compiles each *_T.c for 'd' and 'dc' (e.g.
+ * src/simulation/solvers/dg/compute_volume_rlhs_dg.c:65-71).
+ *
+ * TEST INFRASTRUCTURE ONLY: this is the checker, not the product.
+ *
+ * Required macros: Type, SUF(name) (name suffix), REAL_T(x), ABS_T(x), SQRT_T(x).
+ */
+
+/* Type min_abs_real_T / max_abs_real_T: src/general/math_functions_T.c:222-236. */
+static Type SUF(min_abs_real)(const Type a, const Type b)
+{
+	Type c = (ABS_T(a) < ABS_T(b) ? a : b);
+	if (REAL_T(c) < 0.0)
+		c *= -1.0;
+	return c;
+}
+
+static Type SUF(max_abs_real)(const Type a, const Type b)
+{
+	Type c = (ABS_T(a) > ABS_T(b) ? a : b);
+	if (REAL_T(c) < 0.0)
+		c *= -1.0;
+	return c;
+}
+
+/* out (m x nc, column-major) += alpha * A (m x k, row-major) * B (k x nc, column-major).
+ * The reference's mm_NNC_* products through cblas_dgemm (src/containers/matrix_math_T.c:178-201). */
+static void SUF(mm_acc)(const int m, const int k, const int nc, const double alpha, const double* A,
+                        const Type* B, Type* out)
+{
+	for (int c = 0; c < nc; ++c) {
+		for (int i = 0; i < m; ++i) {
+			Type s = 0.0;
+			const double* a = &A[(size_t)i * k];
+			const Type* b = &B[(size_t)k * c];
+			for (int j = 0; j < k; ++j)
+				s += a[j] * b[j];
+			out[i + (size_t)m * c] += alpha * s;
+		}
+	}
+}
+
+/* Physical Euler flux at one node, f[dim + d*eq]: compute_Flux_T_euler + compute_Flux_euler_0
+ * (src/simulation/test_case/flux/flux_euler_T.c:71-143, 259-298). */
+static void SUF(flux_euler)(const int d, const Type* W, Type* f)
+{
+	const Type rho = W[0], E = W[d + 1];
+	const Type rho_inv = 1.0 / rho;
+	Type uvw[3] = {0.0, 0.0, 0.0}, V2 = 0.0;
+	for (int k = 0; k < d; ++k) {
+		uvw[k] = rho_inv * W[1 + k];
+		V2 += uvw[k] * uvw[k];
+	}
+	const Type p = GM1 * (E - 0.5 * rho * V2);
+	int ind = 0;
+	for (int k = 0; k < d; ++k)
+		f[ind++] = W[1 + k];
+	for (int m = 0; m < d; ++m)
+		for (int k = 0; k < d; ++k)
+			f[ind++] = W[1 + m] * uvw[k] + (m == k ? p : 0.0);
+	for (int k = 0; k < d; ++k)
+		f[ind++] = (E + p) * uvw[k];
+}
+
+/* Lax-Friedrichs: numerical_flux_euler_T.c:60-327. WL/WR are per-node state vectors, n is the node's
+ * unit normal; writes nF[eq]. */
+static void SUF(num_flux_lf)(const int d, const Type* WL, const Type* WR, const double* n, Type* nF)
+{
+	const int neq = d + 2;
+	Type VL, VR, cL, cR;
+	{
+		const Type rho = WL[0], rho_inv = 1.0 / rho;
+		Type V2 = 0.0;
+		for (int k = 0; k < d; ++k) {
+			const Type u = WL[1 + k] * rho_inv;
+			V2 += u * u;
+		}
+		VL = SQRT_T(V2);
+		const Type p = GM1 * (WL[d + 1] - 0.5 * rho * V2);
+		cL = SQRT_T(GAMMA * p / rho);
+	}
+	{
+		const Type rho = WR[0], rho_inv = 1.0 / rho;
+		Type V2 = 0.0;
+		for (int k = 0; k < d; ++k) {
+			const Type u = WR[1 + k] * rho_inv;
+			V2 += u * u;
+		}
+		VR = SQRT_T(V2);
+		const Type p = GM1 * (WR[d + 1] - 0.5 * rho * V2);
+		cR = SQRT_T(GAMMA * p / rho);
+	}
+	const Type maxlL = VL + cL, maxlR = VR + cR;
+	const Type maxV = (REAL_T(maxlL) > REAL_T(maxlR) ? maxlL : maxlR);
+	Type FL[15], FR[15];
+	SUF(flux_euler)(d, WL, FL);
+	SUF(flux_euler)(d, WR, FR);
+	for (int eq = 0; eq < neq; ++eq) {
+		Type s = 0.0;
+		for (int k = 0; k < d; ++k)
+			s += n[k] * (FL[k + d * eq] + FR[k + d * eq]);
+		nF[eq] = 0.5 * (s + maxV * (WL[eq] - WR[eq]));
+	}
+}
+
+/* Roe-Pike with the entropy fix of Qu et al. (2015), numerical_flux_euler_T.c:470-778. */
+static void SUF(num_flux_roe)(const int d, const Type* WL, const Type* WR, const double* n, Type* nF)
+{
+	const Type rhoL = WL[0], rhoR = WR[0], EL = WL[d + 1], ER = WR[d + 1];
+	const Type rhoL_inv = 1.0 / rhoL, rhoR_inv = 1.0 / rhoR;
+	Type uL[3] = {0, 0, 0}, uR[3] = {0, 0, 0};
+	Type V2L = 0.0, V2R = 0.0, VnL = 0.0, VnR = 0.0;
+	for (int k = 0; k < d; ++k) {
+		uL[k] = WL[1 + k] * rhoL_inv;
+		uR[k] = WR[1 + k] * rhoR_inv;
+		V2L += uL[k] * uL[k];
+		V2R += uR[k] * uR[k];
+		VnL += n[k] * uL[k];
+		VnR += n[k] * uR[k];
+	}
+	const Type pL = GM1 * (EL - 0.5 * rhoL * V2L), HL = (EL + pL) * rhoL_inv;
+	const Type pR = GM1 * (ER - 0.5 * rhoR * V2R), HR = (ER + pR) * rhoR_inv;
+
+	const Type r = SQRT_T(rhoR / rhoL), rP1 = r + 1.0, rho = r * rhoL;
+	Type u[3] = {0, 0, 0}, Vn = 0.0, V2 = 0.0;
+	for (int k = 0; k < d; ++k) {
+		u[k] = (r * uR[k] + uL[k]) / rP1;
+		Vn += n[k] * u[k];
+		V2 += u[k] * u[k];
+	}
+	const Type H = (r * HR + HL) / rP1, c2 = GM1 * (H - 0.5 * V2), c = SQRT_T(c2);
+
+	const Type l1 = SUF(min_abs_real)(VnL - c, Vn - c), l5 = SUF(max_abs_real)(VnR + c, Vn + c),
+	           l234 = (REAL_T(Vn) > 0.0 ? Vn : -Vn);
+
+	const Type drho = rhoR - rhoL, dE = ER - EL, dp = pR - pL, dVn = VnR - VnL;
+	const Type lc1 = 0.5 * (l5 + l1) - l234, lc2 = 0.5 * (l5 - l1);
+	const Type disInter1 = lc1 * dp / (c * c) + lc2 * rho * dVn / c, disInter2 = lc1 * rho * dVn + lc2 * dp / c;
+
+	const Type rhoVnL = rhoL * VnL, rhoVnR = rhoR * VnR, pLR = pL + pR;
+	nF[0] = 0.5 * ((rhoVnL + rhoVnR) - (l234 * drho + disInter1));
+	for (int k = 0; k < d; ++k) {
+		const Type drhou = rhoR * uR[k] - rhoL * uL[k];
+		const Type nFk = rhoVnL * uL[k] + rhoVnR * uR[k] + n[k] * pLR;
+		const Type disk = l234 * drhou + disInter1 * u[k] + disInter2 * n[k];
+		nF[1 + k] = 0.5 * (nFk - disk);
+	}
+	nF[d + 1] = 0.5 * ((VnL * (EL + pL) + VnR * (ER + pR)) - (l234 * dE + disInter1 * H + disInter2 * Vn));
+}
+
+/* Explicit DG residual (before M^-1): compute_rlhs_common_dg (solve_dg.c:182-189) with
+ * compute_volume_rlhs_dg (compute_volume_rlhs_dg_T.c:53-72 -> compute_volume_rlhs_T.c:145-177,
+ * compute_rlhs_T.c:71-110) and compute_face_rlhs_dg (compute_face_rlhs_dg_T.c:88-114 ->
+ * boundary_T.c:42-145, compute_face_rlhs_T.c:297-359). sol/rhs: per volume (n_vs x n_var) column-major. */
+static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* rhs)
+{
+	const struct oracle_problem* P = &c->P;
+	const int d = P->d, nv = P->n_var, neq = P->n_var;
+	const int n_vs = P->n_vs, n_vc = P->n_vc, n_fc = P->n_fc;
+	const size_t vs_sz = (size_t)n_vs * nv;
+
+	for (size_t i = 0; i < (size_t)P->n_volumes * vs_sz; ++i)
+		rhs[i] = 0.0;
+
+	Type* s_vc = malloc(sizeof(Type) * (size_t)n_vc * nv);
+	Type* fr = malloc(sizeof(Type) * (size_t)n_vc * neq * d);
+	Type* sL = malloc(sizeof(Type) * (size_t)n_fc * nv);
+	Type* sR0 = malloc(sizeof(Type) * (size_t)n_fc * nv);
+	Type* sR = malloc(sizeof(Type) * (size_t)n_fc * nv);
+	Type* nnf = malloc(sizeof(Type) * (size_t)n_fc * neq);
+	Type* nnfR = malloc(sizeof(Type) * (size_t)n_fc * neq);
+
+	/* ---- volume term ---- */
+	for (int v = 0; v < P->n_volumes; ++v) {
+		const Type* s = &sol[(size_t)v * vs_sz];
+		Type* r = &rhs[(size_t)v * vs_sz];
+		const double* m = &P->metrics_vc[(size_t)v * n_vc * d * d];
+		for (size_t i = 0; i < (size_t)n_vc * nv; ++i)
+			s_vc[i] = 0.0;
+		SUF(mm_acc)(n_vc, n_vs, nv, 1.0, P->cv0_vs_vc, s, s_vc);
+		for (size_t i = 0; i < (size_t)n_vc * neq * d; ++i)
+			fr[i] = 0.0;
+		for (int n = 0; n < n_vc; ++n) {
+			Type W[5], f[15];
+			for (int k = 0; k < nv; ++k)
+				W[k] = s_vc[n + (size_t)n_vc * k];
+			if (P->pde == ORACLE_PDE_EULER) {
+				SUF(flux_euler)(d, W, f);
+			} else {
+				for (int k = 0; k < d; ++k)
+					f[k] = P->b_adv[k] * W[0];
+			}
+			/* fr(n,eq,dim0) = sum_dim1 m(n,dim1,dim0) f(n,dim1,eq)  (compute_rlhs_T.c:71-110) */
+			for (int eq = 0; eq < neq; ++eq)
+				for (int d0 = 0; d0 < d; ++d0)
+					for (int d1 = 0; d1 < d; ++d1)
+						fr[n + (size_t)n_vc * (eq + (size_t)neq * d0)] +=
+							m[n + (size_t)n_vc * (d1 + d * d0)] * f[d1 + d * eq];
+		}
+		/* rhs += sum_dim tw1_vt_vc[dim] . fr(:,:,dim)  (compute_volume_rlhs_T.c:166-177) */
+		for (int dim = 0; dim < d; ++dim)
+			SUF(mm_acc)(n_vs, n_vc, neq, 1.0, &P->tw1_vt_vc[(size_t)dim * n_vs * n_vc],
+			            &fr[(size_t)n_vc * neq * dim], r);
+	}
+
+	/* ---- face term ---- */
+	for (int f = 0; f < P->n_faces; ++f) {
+		const int vL = P->face_vol[2 * f], vR = P->face_vol[2 * f + 1];
+		const int lfL = P->face_lf[2 * f], lfR = P->face_lf[2 * f + 1];
+		const int* nc = &P->nc_fc[(size_t)f * n_fc];
+		const double* nrm = &P->normals_fc[(size_t)f * n_fc * d];
+		const double* jf = &P->jacobian_det_fc[(size_t)f * n_fc];
+		for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
+			sL[i] = sR0[i] = 0.0;
+		SUF(mm_acc)(n_fc, n_vs, nv, 1.0, &P->cv0_vs_fc[(size_t)lfL * n_fc * n_vs], &sol[(size_t)vL * vs_sz], sL);
+		SUF(mm_acc)(n_fc, n_vs, nv, 1.0, &P->cv0_vs_fc[(size_t)lfR * n_fc * n_vs], &sol[(size_t)vR * vs_sz], sR0);
+		/* right trace reordered to the left's face-node order (boundary_T.c:80-92) */
+		for (int k = 0; k < nv; ++k)
+			for (int i = 0; i < n_fc; ++i)
+				sR[i + (size_t)n_fc * k] = sR0[nc[i] + (size_t)n_fc * k];
+		for (int i = 0; i < n_fc; ++i) {
+			Type WL[5], WR[5], nF[5];
+			for (int k = 0; k < nv; ++k) {
+				WL[k] = sL[i + (size_t)n_fc * k];
+				WR[k] = sR[i + (size_t)n_fc * k];
+			}
+			const double* ni = &nrm[(size_t)i * d];
+			if (P->pde == ORACLE_PDE_EULER) {
+				if (P->num_flux == ORACLE_NUM_FLUX_ROE_PIKE)
+					SUF(num_flux_roe)(d, WL, WR, ni, nF);
+				else
+					SUF(num_flux_lf)(d, WL, WR, ni, nF);
+			} else {
+				/* numerical_flux_advection_T.c:39-75 */
+				double b_dot_n = 0.0;
+				for (int k = 0; k < d; ++k)
+					b_dot_n += P->b_adv[k] * ni[k];
+				nF[0] = (b_dot_n > ORACLE_EPS ? b_dot_n * WL[0] : b_dot_n * WR[0]);
+			}
+			/* scale_by_Jacobian_e_T (compute_face_rlhs_T.c:337-342) */
+			for (int k = 0; k < neq; ++k)
+				nnf[i + (size_t)n_fc * k] = nF[k] * jf[i];
+		}
+		/* rhs_L -= tw0_vt_fc[L] nnf ; rhs_R -= tw0_vt_fc[R] (-nnf in the right's node order)
+		 * (compute_face_rlhs_T.c:297-310, 347-359). The right side is brought back to its own face-node
+		 * order with the inverse of the trace permutation; the reference applies nc_fc itself, which is the
+		 * same whenever nc_fc is an involution. */
+		SUF(mm_acc)(n_vs, n_fc, neq, -1.0, &P->tw0_vt_fc[(size_t)lfL * n_vs * n_fc], nnf, &rhs[(size_t)vL * vs_sz]);
+		for (int k = 0; k < neq; ++k)
+			for (int i = 0; i < n_fc; ++i)
+				nnfR[nc[i] + (size_t)n_fc * k] = -nnf[i + (size_t)n_fc * k];
+		SUF(mm_acc)(n_vs, n_fc, neq, -1.0, &P->tw0_vt_fc[(size_t)lfR * n_vs * n_fc], nnfR, &rhs[(size_t)vR * vs_sz]);
+	}
+
+	free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);
+	return ORACLE_OK;
+}
+
+/* rhs <- M^-1 rhs per volume: scale_rhs_by_m_inv_std (solve_dg.c:265-272). */
+static void SUF(scale_m_inv)(const struct oracle_ctx* c, Type* rhs)
+{
+	const struct oracle_problem* P = &c->P;
+	const int n_vs = P->n_vs, nv = P->n_var;
+	Type* tmp = malloc(sizeof(Type) * (size_t)n_vs * nv);
+	for (int v = 0; v < P->n_volumes; ++v) {
+		Type* r = &rhs[(size_t)v * n_vs * nv];
+		for (size_t i = 0; i < (size_t)n_vs * nv; ++i)
+			tmp[i] = 0.0;
+		SUF(mm_acc)(n_vs, n_vs, nv, 1.0, &c->m_inv[(size_t)v * n_vs * n_vs], r, tmp);
+		for (size_t i = 0; i < (size_t)n_vs * nv; ++i)
+			r[i] = tmp[i];
+	}
+	free(tmp);
+}
