@@ -70,6 +70,19 @@ class DGProblem:
         return apply_nodes(L, self.geom.X_geom)
 
 
+def stable_dt(prob: "DGProblem", cfl: float = 0.1) -> float:
+    """dt = cfl * h / ((2p + 1) * max(|V| + c)) over the solution nodes of the current state."""
+    d = prob.d
+    U = prob.sol
+    rho = U[:, 0]
+    vel = U[:, 1:1 + d] / rho[:, None]
+    V2 = np.sum(vel * vel, axis=1)
+    p = GM1 * (U[:, d + 1] - 0.5 * rho * V2)
+    lam = float(np.max(np.sqrt(V2) + np.sqrt(GAMMA * p / rho)))
+    h = float(np.min(prob.mesh.h))
+    return cfl * h / ((2 * prob.ops.p + 1) * lam)
+
+
 def primitive_to_conserved(d, rho, vel, p):
     E = p / GM1 + 0.5 * rho * np.sum(vel * vel, axis=0)
     return np.stack([rho] + [rho * vel[k] for k in range(d)] + [E], axis=0)
@@ -111,29 +124,30 @@ def advection_2d(n: int = 16, p: int = 2, b=(1.0, 0.5), cfl: float = 0.1, n_step
 
 
 def euler_vortex_2d(n: int = 64, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, amplitude: float = 0.05,
-                    dt: float = 0.005, n_steps: int = 1000) -> DGProblem:
+                    dt: float | None = None, n_steps: int = 1000) -> DGProblem:
     L = 10.0
     mesh = StructuredMesh(2, n, 0.0, L)
     ops = TPOperatorSet(mesh.e_type, p)
     geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_2d(amplitude, L), curved=True)
     prob = DGProblem("euler_vortex_2d", 2, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
-                     sol=np.zeros((mesh.n_volumes, 4, ops.n_vs)), dt=dt, n_steps=n_steps)
+                     sol=np.zeros((mesh.n_volumes, 4, ops.n_vs)), dt=0.0, n_steps=n_steps)
     xyz = prob.solution_node_xyz()
     rho, u, v, pr = isentropic_vortex(xyz, 5.0, 5.0, 5.0)
     U = primitive_to_conserved(2, rho, np.stack([u, v]), pr)
     prob.sol = _pack_state(U)
+    prob.dt = stable_dt(prob) if dt is None else dt
     prob.meta.update(n=n, p=p, amplitude=amplitude)
     return prob
 
 
 def euler_hex_3d(n: int = 32, p: int = 3, num_flux: int = NUM_FLUX_LAX_FRIEDRICHS, amplitude: float = 0.03,
-                 seed: int = 0, perturb: float = 1e-3, dt: float = 0.01, n_steps: int = 200) -> DGProblem:
+                 seed: int = 0, perturb: float = 1e-3, dt: float | None = None, n_steps: int = 200) -> DGProblem:
     L = 10.0
     mesh = StructuredMesh(3, n, 0.0, L)
     ops = TPOperatorSet(mesh.e_type, p)
     geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_3d(amplitude, L), curved=True)
     prob = DGProblem("euler_hex_3d", 3, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
-                     sol=np.zeros((mesh.n_volumes, 5, ops.n_vs)), dt=dt, n_steps=n_steps)
+                     sol=np.zeros((mesh.n_volumes, 5, ops.n_vs)), dt=0.0, n_steps=n_steps)
     xyz = prob.solution_node_xyz()
     rho, u, v, pr = isentropic_vortex(xyz, 5.0, 5.0, 5.0)
     rng = np.random.default_rng(seed)
@@ -141,6 +155,7 @@ def euler_hex_3d(n: int = 32, p: int = 3, num_flux: int = NUM_FLUX_LAX_FRIEDRICH
     w = np.zeros_like(u)
     U = primitive_to_conserved(3, rho, np.stack([u, v, w]), pr)
     prob.sol = _pack_state(U)
+    prob.dt = stable_dt(prob) if dt is None else dt
     prob.meta.update(n=n, p=p, amplitude=amplitude, seed=seed)
     return prob
 
