@@ -419,6 +419,7 @@ tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 	const int tid = threadIdx.x;
 	for (int i = tid; i < (int)(sizeof(TPOps) / 8); i += blockDim.x)
 		reinterpret_cast<double*>(sops)[i] = reinterpret_cast<const double*>(&ops)[i];
+	__syncthreads();  // the lift below reads sops->lb written by other warps
 
 	const int v0 = blockIdx.x * E;
 	const int n_here = min(E, P.n_vol - v0);

@@ -36,6 +36,10 @@ CASES = {
     "hex_roe_p2_3": lambda: P.euler_hex_3d(3, 2, num_flux=P.NUM_FLUX_ROE_PIKE),
     "hex_roe_p1_2": lambda: P.euler_hex_3d(2, 1, num_flux=P.NUM_FLUX_ROE_PIKE),
     "hex_lf_p4_2": lambda: P.euler_hex_3d(2, 4),
+    # many CTAs per SM: catches races between the warps of a CTA and between co-resident CTAs
+    "hex_lf_p3_12": lambda: P.euler_hex_3d(12, 3),
+    "hex_roe_p2_16": lambda: P.euler_hex_3d(16, 2, num_flux=P.NUM_FLUX_ROE_PIKE),
+    "vortex2d_roe_p3_32": lambda: P.euler_vortex_2d(32, 3),
 }
 
 
@@ -51,12 +55,12 @@ def test_residual_matches_oracle(gpu_lib, name):
     assert abs(mx - mx_ref) <= TOL * mx_ref
 
 
-@pytest.mark.parametrize("name", ["adv2d_p2_16", "vortex2d_roe_p3_8", "hex_lf_p3_4", "hex_roe_p2_3"])
-def test_rk3_steps_match_oracle(gpu_lib, name):
+@pytest.mark.parametrize("name,n_steps", [("adv2d_p2_16", 5), ("vortex2d_roe_p3_8", 5), ("hex_lf_p3_4", 5),
+                                          ("hex_roe_p2_3", 5), ("hex_lf_p3_12", 3)])
+def test_rk3_steps_match_oracle(gpu_lib, name, n_steps):
     from dpgsolver_gb300.solver import Simulation
     prob = CASES[name]()
     ref = oracle.Oracle(prob)
-    n_steps = 5
     s_ref = prob.sol.copy()
     for _ in range(n_steps):
         s_ref, mx_ref, _ = ref.ssp_rk3_step(s_ref, prob.dt)
@@ -120,7 +124,7 @@ def test_positivity_correction_matches_oracle(gpu_lib):
 
 def test_deterministic(gpu_lib):
     from dpgsolver_gb300.solver import Simulation
-    prob = P.euler_hex_3d(4, 3)
+    prob = P.euler_hex_3d(16, 3)
     with Simulation(prob) as sim:
         sim.compute_rhs()
         a = sim.rhs
