@@ -849,3 +849,321 @@ extern "C" dgpu_status dgpu_probe_fp64(int iters, double* tflops)
 	*tflops = flops / (ms * 1e-3) / 1e12;
 	return DGPU_OK;
 }
+
+// ---------------------------------------------------------------------------------------------------------------
+// Residual evaluation without any device allocation (dgpu_compute_rhs_noalloc).
+//
+// Some callers cannot call cudaMalloc at all: a host application whose device memory is owned by its own pool
+// or framework and that hands the library only its buffers, or code that must not allocate while it runs (a
+// pre-allocated real-time loop). For them the residual's intermediates -- packed geometry, connectivity, volume
+// term, face traces and face fluxes -- live in one file-scope device array of fixed size instead of buffers
+// owned by a dgpu_ctx. Every GPU that loads this library keeps that array until the process exits.
+// ---------------------------------------------------------------------------------------------------------------
+
+#define DGPU_NOALLOC_SCRATCH_DOUBLES ((size_t)DGPU_NOALLOC_SCRATCH_BYTES / sizeof(double))
+
+static __device__ __align__(256) double g_noalloc_scratch[DGPU_NOALLOC_SCRATCH_DOUBLES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+double* g_noalloc_ptr[kMaxDevices];   // device address of g_noalloc_scratch, per device, set at first use
+
+struct NoallocWeights {
+	double w[kQMax * kQMax * kQMax];     // volume cubature weights, TP order
+	double wf[kQMax * kQMax];            // face cubature weights
+};
+
+// Packs the caller's reference-layout volume data into the library's layout inside the scratch array.
+template <int D, int Q>
+__global__ void noalloc_pack_volumes(const NoallocWeights W, int n_vol, const double* __restrict__ metrics,
+                                     const double* __restrict__ jac, double* gmet, double* inv_wJ, int* err)
+{
+	constexpr int N = TPShape<D, Q>::N;
+	const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= (long long)n_vol * N)
+		return;
+	const long long v = gid / N;
+	const int n = (int)(gid % N);
+	const double* m = metrics + v * N * D * D;
+	for (int j = 0; j < D; ++j)
+		for (int i = 0; i < D; ++i)
+			gmet[((v * D + j) * D + i) * N + n] = W.w[n] * m[n + (size_t)N * (i + D * j)];
+	const double J = jac[v * N + n];
+	if (!(J > 0.0))
+		atomicExch(err, 1);
+	inv_wJ[v * N + n] = 1.0 / (W.w[n] * J);
+}
+
+// Face data, connectivity (vol_face) and the inverse right-trace permutation, with bounds checks: an entry
+// outside the mesh raises the error flag and is skipped.
+template <int D, int Q>
+__global__ void noalloc_pack_faces(const NoallocWeights W, int n_vol, int n_face, const int* __restrict__ face_vol,
+                                   const int* __restrict__ face_lf, const int* __restrict__ nc,
+                                   const double* __restrict__ normals, const double* __restrict__ jf,
+                                   double* fgeo, int* vol_face, int* nc_inv, int* err)
+{
+	constexpr int NF = TPShape<D, Q>::NF;
+	const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= (long long)n_face * NF)
+		return;
+	const long long f = gid / NF;
+	const int i = (int)(gid % NF);
+	for (int k = 0; k < D; ++k)
+		fgeo[(f * (D + 1) + k) * NF + i] = normals[(f * NF + i) * D + k];
+	fgeo[(f * (D + 1) + D) * NF + i] = W.wf[i] * jf[f * NF + i];
+	if (i == 0) {
+		for (int s = 0; s < 2; ++s) {
+			const int v = face_vol[2 * f + s], lf = face_lf[2 * f + s];
+			if (v < 0 || v >= n_vol || lf < 0 || lf >= 2 * D) {
+				atomicExch(err, 1);
+				continue;
+			}
+			vol_face[(size_t)v * 2 * D + lf] = (int)(2 * f + s);
+		}
+	}
+	if (nc) {
+		const int t = nc[f * NF + i];
+		if (t < 0 || t >= NF)
+			atomicExch(err, 1);
+		else
+			nc_inv[f * NF + t] = i;
+	}
+}
+
+// Every (volume, local face) must have been written exactly by the face list; -1 left over means a gap.
+__global__ void noalloc_check_ints(const int* a, long long n, int hi, int* err)
+{
+	const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid < n && (a[gid] < 0 || a[gid] >= hi))
+		atomicExch(err, 1);
+}
+
+template <int D, int Q>
+cudaError_t noalloc_pack(const NoallocWeights& W, const dgpu_mesh* m, double* gmet, double* inv_wJ, double* fgeo,
+                         int* vol_face, int* nc_inv, int* err, cudaStream_t st)
+{
+	constexpr int N = TPShape<D, Q>::N, NF = TPShape<D, Q>::NF;
+	const long long nv = (long long)m->n_volumes * N, nf = (long long)m->n_faces * NF;
+	noalloc_pack_volumes<D, Q><<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(W, m->n_volumes, m->metrics_vc,
+	                                                                          m->jacobian_det_vc, gmet, inv_wJ, err);
+	noalloc_pack_faces<D, Q><<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(
+		W, m->n_volumes, m->n_faces, m->face_vol, m->face_lf, m->nc_fc, m->normals_fc, m->jacobian_det_fc, fgeo,
+		vol_face, nc_inv, err);
+	const long long nvf = (long long)m->n_volumes * 2 * D;
+	noalloc_check_ints<<<(unsigned)((nvf + 255) / 256), 256, 0, st>>>(vol_face, nvf, 2 * m->n_faces, err);
+	if (m->nc_fc)
+		noalloc_check_ints<<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(nc_inv, nf, NF, err);
+	return cudaGetLastError();
+}
+
+template <int D>
+cudaError_t noalloc_pack_q(int q, const NoallocWeights& W, const dgpu_mesh* m, double* gmet, double* inv_wJ,
+                           double* fgeo, int* vol_face, int* nc_inv, int* err, cudaStream_t st)
+{
+	switch (q) {
+	case 2: return noalloc_pack<D, 2>(W, m, gmet, inv_wJ, fgeo, vol_face, nc_inv, err, st);
+	case 3: return noalloc_pack<D, 3>(W, m, gmet, inv_wJ, fgeo, vol_face, nc_inv, err, st);
+	case 4: return noalloc_pack<D, 4>(W, m, gmet, inv_wJ, fgeo, vol_face, nc_inv, err, st);
+	case 5: return noalloc_pack<D, 5>(W, m, gmet, inv_wJ, fgeo, vol_face, nc_inv, err, st);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+size_t round_up_256(size_t doubles) { return (doubles + 31) / 32 * 32; }
+
+bool is_device_pointer(const void* p)
+{
+	if (!p)
+		return false;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+extern "C" dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const dgpu_tp_operators* ops,
+                                                const dgpu_mesh* d_mesh, const double* d_sol, double* d_rhs,
+                                                double* max_rhs, void* cuda_stream)
+{
+	g_create_error.clear();
+	if (!phys || !ops || !d_mesh || !d_sol || !d_rhs)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+	const int d = phys->d;
+	if (d != 2 && d != 3)
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "d must be 2 or 3");
+	if ((d == 2 && ops->elem_type != DGPU_QUAD) || (d == 3 && ops->elem_type != DGPU_HEX))
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "element type must be QUAD (d=2) or HEX (d=3)");
+	if (ops->p < 1 || ops->p > kQMax - 1)
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "p must be in 1..4");
+	if (phys->pde == DGPU_PDE_ADVECTION) {
+		if (phys->num_flux != DGPU_NUM_FLUX_UPWIND)
+			return fail(nullptr, DGPU_ERR_UNSUPPORTED, "advection supports the upwind flux");
+	} else if (phys->pde == DGPU_PDE_EULER) {
+		if (phys->num_flux != DGPU_NUM_FLUX_ROE_PIKE && phys->num_flux != DGPU_NUM_FLUX_LAX_FRIEDRICHS)
+			return fail(nullptr, DGPU_ERR_UNSUPPORTED, "Euler supports Roe-Pike and Lax-Friedrichs");
+	} else {
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "pde must be advection or Euler");
+	}
+	if (!ops->cv0_vs_vc || !ops->cv1_vs_vc || !ops->cv0_vs_fc || !ops->w_vc)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL operator");
+	if (d_mesh->n_volumes < 1 || d_mesh->n_faces < 1)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "empty mesh");
+	if (!is_device_pointer(d_sol) || !is_device_pointer(d_rhs) || !is_device_pointer(d_mesh->metrics_vc) ||
+	    !is_device_pointer(d_mesh->jacobian_det_vc) || !is_device_pointer(d_mesh->face_vol) ||
+	    !is_device_pointer(d_mesh->face_lf) || !is_device_pointer(d_mesh->normals_fc) ||
+	    !is_device_pointer(d_mesh->jacobian_det_fc) || (d_mesh->nc_fc && !is_device_pointer(d_mesh->nc_fc)))
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "state, residual and mesh arrays must be device memory");
+
+	const int q = ops->p + 1;
+	const int N = (d == 2 ? q * q : q * q * q), NF = (d == 2 ? q : q * q);
+	const int nv = (phys->pde == DGPU_PDE_EULER ? d + 2 : 1);
+	const size_t n_vol = (size_t)d_mesh->n_volumes, n_face = (size_t)d_mesh->n_faces;
+
+	// scratch layout (each region 256-byte aligned), checked against the fixed size
+	const size_t o_gmet = 0;
+	const size_t o_inv = o_gmet + round_up_256(n_vol * d * d * N);
+	const size_t o_fgeo = o_inv + round_up_256(n_vol * N);
+	const size_t o_vgl = o_fgeo + round_up_256(n_face * (d + 1) * NF);
+	const size_t o_tr = o_vgl + round_up_256(n_vol * nv * N);
+	const size_t o_nnf = o_tr + round_up_256(n_face * 2 * nv * NF);
+	const size_t o_vf = o_nnf + round_up_256(n_face * nv * NF);
+	const size_t o_nci = o_vf + round_up_256((n_vol * 2 * d + 1) / 2);
+	const size_t o_misc = o_nci + round_up_256(d_mesh->nc_fc ? (n_face * NF + 1) / 2 : 0);
+	const size_t total = o_misc + 32;
+	if (total > DGPU_NOALLOC_SCRATCH_DOUBLES) {
+		char msg[256];
+		snprintf(msg, sizeof msg, "mesh needs %zu bytes of scratch; dgpu_compute_rhs_noalloc has %zu (use dgpu_create)",
+		         total * sizeof(double), (size_t)DGPU_NOALLOC_SCRATCH_BYTES);
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, msg);
+	}
+
+	// set-up once per device, with that device current: the device address of the scratch array
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+		return fail(nullptr, DGPU_ERR_NO_DEVICE, "no current CUDA device");
+	cudaDeviceProp prop;
+	if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess || prop.major * 10 + prop.minor != 103)
+		return fail(nullptr, DGPU_ERR_NO_DEVICE, "device is not compute capability 10.3 (sm_103a build)");
+	if (!g_noalloc_ptr[dev]) {
+		double* p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+		if (e != cudaSuccess || !p)
+			return cuda_fail(nullptr, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+		g_noalloc_ptr[dev] = p;
+	}
+	double* S = g_noalloc_ptr[dev];
+	cudaStream_t st = (cudaStream_t)cuda_stream;
+
+	// host-side operator derivation (same algebra as dgpu_create)
+	dgpu_ctx c;   // stack context: no device memory of its own, only views into the scratch and caller buffers
+	c.d = d;
+	c.q = q;
+	c.N = N;
+	c.NF = NF;
+	c.nv = nv;
+	c.pde = phys->pde;
+	c.flux = phys->num_flux;
+	c.positivity = 0;
+	c.n_vol = d_mesh->n_volumes;
+	c.n_face = d_mesh->n_faces;
+	for (int k = 0; k < 3; ++k)
+		c.b_adv[k] = phys->b_adv[k];
+	memset(&c.ops, 0, sizeof c.ops);
+	double Bm[kQMax * kQMax], Bi[kQMax * kQMax];
+	for (int i = 0; i < q * q; ++i)
+		Bm[i] = ops->cv0_vs_vc[i];
+	if (!invert_small(q, Bm, Bi))
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "cv0_vs_vc is singular");
+	for (int a = 0; a < q; ++a)
+		for (int m = 0; m < q; ++m) {
+			c.ops.B[a][m] = Bm[a * q + m];
+			c.ops.Binv[a][m] = Bi[a * q + m];
+			double s = 0.0;
+			for (int k = 0; k < q; ++k)
+				s += ops->cv1_vs_vc[a * q + k] * Bi[k * q + m];
+			c.ops.Dgl[a][m] = s;
+		}
+	for (int s = 0; s < 2; ++s)
+		for (int m = 0; m < q; ++m) {
+			double acc = 0.0;
+			for (int k = 0; k < q; ++k)
+				acc += ops->cv0_vs_fc[s * q + k] * Bi[k * q + m];
+			c.ops.lb[s][m] = acc;
+		}
+	NoallocWeights W;
+	memset(&W, 0, sizeof W);
+	for (int n = 0; n < N; ++n) {
+		int r = n;
+		double x = 1.0;
+		for (int k = 0; k < d; ++k) {
+			x *= ops->w_vc[r % q];
+			r /= q;
+		}
+		W.w[n] = x;
+	}
+	for (int n = 0; n < NF; ++n) {
+		int r = n;
+		double x = 1.0;
+		for (int k = 0; k < d - 1; ++k) {
+			x *= ops->w_vc[r % q];
+			r /= q;
+		}
+		W.wf[n] = x;
+	}
+
+	int* vol_face = reinterpret_cast<int*>(S + o_vf);
+	int* nc_inv = d_mesh->nc_fc ? reinterpret_cast<int*>(S + o_nci) : nullptr;
+	unsigned long long* max_bits = reinterpret_cast<unsigned long long*>(S + o_misc);
+	int* err = reinterpret_cast<int*>(S + o_misc + 1);
+	c.u = const_cast<double*>(d_sol);
+	c.rhs = d_rhs;
+	c.gmet = S + o_gmet;
+	c.inv_wJ = S + o_inv;
+	c.fgeo = S + o_fgeo;
+	c.vol_gl = S + o_vgl;
+	c.traces = S + o_tr;
+	c.nnf = S + o_nnf;
+	c.vol_face = vol_face;
+	c.nc = const_cast<int*>(d_mesh->nc_fc);
+	c.nc_inv = nc_inv;
+	c.max_bits = max_bits;
+	c.err_flag = err;
+	c.n_corr = nullptr;
+	c.stream = st;
+	c.own_stream = false;
+
+	// the previous call's contents are still in the array: reset what must start cleared
+	DGPU_CUDA(nullptr, cudaMemsetAsync(vol_face, 0xff, n_vol * 2 * d * sizeof(int), st));
+	if (nc_inv)
+		DGPU_CUDA(nullptr, cudaMemsetAsync(nc_inv, 0xff, n_face * NF * sizeof(int), st));
+	DGPU_CUDA(nullptr, cudaMemsetAsync(err, 0, sizeof(int), st));
+	cudaError_t pe = (d == 2 ? noalloc_pack_q<2>(q, W, d_mesh, c.gmet, c.inv_wJ, c.fgeo, vol_face, nc_inv, err, st)
+	                         : noalloc_pack_q<3>(q, W, d_mesh, c.gmet, c.inv_wJ, c.fgeo, vol_face, nc_inv, err, st));
+	DGPU_CUDA(nullptr, pe);
+	int h_err = 0;
+	DGPU_CUDA(nullptr, cudaMemcpyAsync(&h_err, err, sizeof h_err, cudaMemcpyDeviceToHost, st));
+	DGPU_CUDA(nullptr, cudaStreamSynchronize(st));
+	if (h_err)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT,
+		            "bad mesh: a face index, local face, permutation or jacobian_det_vc is out of range");
+
+	// the residual kernels of dgpu_compute_rhs, unchanged, on the scratch views
+	DGPU_CUDA(nullptr, d == 2 ? bind_q<2>(&c) : bind_q<3>(&c));
+	DGPU_CUDA(nullptr, c.launch_volume(&c));
+	DGPU_CUDA(nullptr, c.launch_face(&c));
+	DGPU_CUDA(nullptr, c.launch_lift_rhs(&c));
+	if (max_rhs) {
+		unsigned long long bits = 0;
+		DGPU_CUDA(nullptr, cudaMemcpyAsync(&bits, max_bits, sizeof bits, cudaMemcpyDeviceToHost, st));
+		DGPU_CUDA(nullptr, cudaStreamSynchronize(st));
+		double v;
+		memcpy(&v, &bits, sizeof v);
+		*max_rhs = v;
+	}
+	return DGPU_OK;
+}

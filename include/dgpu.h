@@ -114,6 +114,25 @@ dgpu_status dgpu_compute_rhs_host(dgpu_ctx* ctx, const double* sol, double* rhs,
 dgpu_status dgpu_ssp_rk3_step(dgpu_ctx* ctx, double dt, double* max_rhs);
 dgpu_status dgpu_ssp_rk3_steps(dgpu_ctx* ctx, double dt, int n_steps, double* max_rhs);
 
+/* Residual without any device allocation. No counterpart in the reference (its residual is host code).
+ *
+ * For callers that cannot call cudaMalloc: a host application whose GPU memory belongs to its own pool or
+ * framework and which passes the library only the buffers it owns, or a loop that must not allocate while it
+ * runs. It computes what dgpu_compute_rhs computes, from a context-free description: `phys` and `ops` are host
+ * structs as for dgpu_create, while every array in `d_mesh` (same layouts as dgpu_create), `d_sol` and
+ * `d_rhs` must be device memory of the current device. The intermediates live in one fixed array of
+ * DGPU_NOALLOC_SCRATCH_BYTES inside the library (held by every GPU that loads it until the process exits);
+ * a mesh that needs more returns DGPU_ERR_INVALID_ARGUMENT naming the size it needs (a HEX p=3 Euler element
+ * needs about 15 KB, so about 2,200 such elements fit). The first call on each device looks up the array's
+ * device address, so make that first call before any stream capture. All calls share the array and each
+ * call overwrites it: calls that overlap on the GPU (concurrent streams or host threads) race, so serialise
+ * them. The call synchronises `cuda_stream` (NULL = legacy default stream) after validating the mesh on the
+ * device, and again when max_rhs is not NULL. */
+#define DGPU_NOALLOC_SCRATCH_BYTES (32u << 20)
+dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const dgpu_tp_operators* ops,
+                                     const dgpu_mesh* d_mesh, const double* d_sol, double* d_rhs,
+                                     double* max_rhs, void* cuda_stream);
+
 /* Number of positivity corrections applied since creation (enforce_positivity_highorder's correct_coef). */
 dgpu_status dgpu_positivity_corrections(dgpu_ctx* ctx, long long* n);
 /* Kernels this context has launched (graph replays count each kernel node). */
