@@ -36,6 +36,8 @@ struct dgpu_ctx {
 	TPOps ops;
 	// device memory
 	double *u = nullptr, *u0 = nullptr, *rhs = nullptr;
+	double* ug = nullptr;                 // state as GL nodal values (time stepping); u0 holds the stage-0 copy
+	bool coef_valid = true, gl_valid = false;   // which of u / ug holds the current state
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
 	double *traces = nullptr, *nnf = nullptr, *vol_gl = nullptr;
@@ -45,15 +47,18 @@ struct dgpu_ctx {
 	// execution
 	cudaStream_t stream = nullptr;
 	bool own_stream = false;
-	cudaGraphExec_t rk_graph = nullptr;
-	double rk_graph_dt = 0.0;
+	cudaGraphExec_t rk_graph = nullptr;       // one SSP-RK3 step
+	cudaGraphExec_t rk_graph_max = nullptr;   // the same step reducing max|rhs| in its last stage
+	double rk_graph_dt = 0.0, rk_graph_max_dt = 0.0;
 	long long launches = 0;
 	std::string err;
 	// launchers for the instantiated (D, Q, NV, PDE, FLUX)
-	cudaError_t (*launch_volume)(dgpu_ctx*) = nullptr;
+	cudaError_t (*launch_volume)(dgpu_ctx*) = nullptr;      // input: GLL coefficients u
+	cudaError_t (*launch_volume_gl)(dgpu_ctx*) = nullptr;   // input: GL nodal values ug
 	cudaError_t (*launch_face)(dgpu_ctx*) = nullptr;
 	cudaError_t (*launch_lift_rhs)(dgpu_ctx*) = nullptr;
-	cudaError_t (*launch_lift_rk)(dgpu_ctx*, double dt, int stage) = nullptr;
+	cudaError_t (*launch_lift_rk)(dgpu_ctx*, double dt, int stage, int want_max) = nullptr;
+	cudaError_t (*launch_convert)(dgpu_ctx*, bool to_gl) = nullptr;
 	// optional per-kernel timing (eager launches only)
 	bool timing = false;
 	std::vector<KernelTimer> timers;
@@ -156,6 +161,13 @@ template <int D, int Q, int NV>
 size_t lift_smem_bytes()
 {
 	using S = TPShape<D, Q>;
+	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * (3 * NV * S::N + 8) * sizeof(double);
+}
+
+template <int D, int Q, int NV>
+size_t convert_smem_bytes()
+{
+	using S = TPShape<D, Q>;
 	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * (3 * NV * S::N) * sizeof(double);
 }
 
@@ -178,14 +190,14 @@ void record_stop(dgpu_ctx* c)
 	cudaEventRecord(c->timers.back().stop, c->stream);
 }
 
-template <int D, int Q, int NV, int PDE>
+template <int D, int Q, int NV, int PDE, bool GLL_IN>
 cudaError_t launch_volume_t(dgpu_ctx* c)
 {
 	using S = TPShape<D, Q>;
 	const int blocks = (c->n_vol + S::E - 1) / S::E;
 	record_start(c, "tp_volume_kernel");
-	tp_volume_kernel<D, Q, NV, PDE><<<blocks, S::THREADS, volume_smem_bytes<D, Q, NV>(), c->stream>>>(
-		c->ops, c->params(), c->u);
+	tp_volume_kernel<D, Q, NV, PDE, GLL_IN><<<blocks, S::THREADS, volume_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, c->params(), GLL_IN ? c->u : c->ug);
 	record_stop(c);
 	c->launches++;
 	return cudaGetLastError();
@@ -216,6 +228,7 @@ cudaError_t launch_lift_rhs_t(dgpu_ctx* c)
 	rk.dt = 0.0;
 	rk.stage = 0;
 	rk.positivity = 0;
+	rk.want_max = 1;
 	record_start(c, "tp_lift_kernel");
 	tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
 		c->ops, c->params(), rk);
@@ -225,20 +238,38 @@ cudaError_t launch_lift_rhs_t(dgpu_ctx* c)
 }
 
 template <int D, int Q, int NV>
-cudaError_t launch_lift_rk_t(dgpu_ctx* c, double dt, int stage)
+cudaError_t launch_lift_rk_t(dgpu_ctx* c, double dt, int stage, int want_max)
 {
 	using S = TPShape<D, Q>;
 	const int blocks = (c->n_vol + S::E - 1) / S::E;
 	RkArgs rk;
-	rk.u = c->u;
+	rk.u = c->ug;
 	rk.u0 = c->u0;
 	rk.rhs = c->rhs;
 	rk.dt = dt;
 	rk.stage = stage;
 	rk.positivity = c->positivity;
+	rk.want_max = want_max;
 	record_start(c, "tp_lift_kernel");
-	tp_lift_kernel<D, Q, NV, kModeRk><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
+	tp_lift_kernel<D, Q, NV, kModeRkGl><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
 		c->ops, c->params(), rk);
+	record_stop(c);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV>
+cudaError_t launch_convert_t(dgpu_ctx* c, bool to_gl)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	record_start(c, "tp_convert_kernel");
+	if (to_gl)
+		tp_convert_kernel<D, Q, NV, true><<<blocks, S::THREADS, convert_smem_bytes<D, Q, NV>(), c->stream>>>(
+			c->ops, c->n_vol, c->u, c->ug);
+	else
+		tp_convert_kernel<D, Q, NV, false><<<blocks, S::THREADS, convert_smem_bytes<D, Q, NV>(), c->stream>>>(
+			c->ops, c->n_vol, c->ug, c->u);
 	record_stop(c);
 	c->launches++;
 	return cudaGetLastError();
@@ -247,21 +278,25 @@ cudaError_t launch_lift_rk_t(dgpu_ctx* c, double dt, int stage)
 template <int D, int Q, int NV, int PDE, int FLUX>
 cudaError_t bind(dgpu_ctx* c)
 {
-	c->launch_volume = launch_volume_t<D, Q, NV, PDE>;
+	c->launch_volume = launch_volume_t<D, Q, NV, PDE, true>;
+	c->launch_volume_gl = launch_volume_t<D, Q, NV, PDE, false>;
 	c->launch_face = launch_face_t<D, Q, NV, PDE, FLUX>;
 	c->launch_lift_rhs = launch_lift_rhs_t<D, Q, NV>;
 	c->launch_lift_rk = launch_lift_rk_t<D, Q, NV>;
+	c->launch_convert = launch_convert_t<D, Q, NV>;
+	const cudaFuncAttribute smem = cudaFuncAttributeMaxDynamicSharedMemorySize;
 	cudaError_t e;
-	e = cudaFuncSetAttribute(tp_volume_kernel<D, Q, NV, PDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                         (int)volume_smem_bytes<D, Q, NV>());
-	if (e != cudaSuccess)
+	if ((e = cudaFuncSetAttribute(tp_volume_kernel<D, Q, NV, PDE, true>, smem, (int)volume_smem_bytes<D, Q, NV>())))
 		return e;
-	e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRhs>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                         (int)lift_smem_bytes<D, Q, NV>());
-	if (e != cudaSuccess)
+	if ((e = cudaFuncSetAttribute(tp_volume_kernel<D, Q, NV, PDE, false>, smem, (int)volume_smem_bytes<D, Q, NV>())))
 		return e;
-	return cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                            (int)lift_smem_bytes<D, Q, NV>());
+	if ((e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRhs>, smem, (int)lift_smem_bytes<D, Q, NV>())))
+		return e;
+	if ((e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRkGl>, smem, (int)lift_smem_bytes<D, Q, NV>())))
+		return e;
+	if ((e = cudaFuncSetAttribute(tp_convert_kernel<D, Q, NV, true>, smem, (int)convert_smem_bytes<D, Q, NV>())))
+		return e;
+	return cudaFuncSetAttribute(tp_convert_kernel<D, Q, NV, false>, smem, (int)convert_smem_bytes<D, Q, NV>());
 }
 
 template <int D, int Q>
@@ -290,12 +325,14 @@ void free_all(dgpu_ctx* c)
 {
 	if (c->rk_graph)
 		cudaGraphExecDestroy(c->rk_graph);
+	if (c->rk_graph_max)
+		cudaGraphExecDestroy(c->rk_graph_max);
 	for (auto& t : c->timers) {
 		cudaEventDestroy(t.start);
 		cudaEventDestroy(t.stop);
 	}
 	c->timers.clear();
-	void* ptrs[] = {c->u, c->u0, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
+	void* ptrs[] = {c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
 	                c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -324,12 +361,33 @@ dgpu_status enqueue_rhs(dgpu_ctx* c)
 	return DGPU_OK;
 }
 
-dgpu_status enqueue_rk_step(dgpu_ctx* c, double dt)
+// One SSP-RK3 step on the GL nodal state ug (3 x volume, face, lift); max|rhs| of the last stage on request.
+dgpu_status enqueue_rk_step(dgpu_ctx* c, double dt, bool want_max)
 {
 	for (int stage = 0; stage < 3; ++stage) {
-		DGPU_CUDA(c, c->launch_volume(c));
+		DGPU_CUDA(c, c->launch_volume_gl(c));
 		DGPU_CUDA(c, c->launch_face(c));
-		DGPU_CUDA(c, c->launch_lift_rk(c, dt, stage));
+		DGPU_CUDA(c, c->launch_lift_rk(c, dt, stage, (want_max && stage == 2) ? 1 : 0));
+	}
+	return DGPU_OK;
+}
+
+// Make u (GLL coefficients) current: V^-1 of ug after time stepping.
+dgpu_status ensure_coef(dgpu_ctx* c)
+{
+	if (!c->coef_valid) {
+		DGPU_CUDA(c, c->launch_convert(c, false));
+		c->coef_valid = true;
+	}
+	return DGPU_OK;
+}
+
+// Make ug (GL nodal values) current: V u after an upload.
+dgpu_status ensure_gl(dgpu_ctx* c)
+{
+	if (!c->gl_valid) {
+		DGPU_CUDA(c, c->launch_convert(c, true));
+		c->gl_valid = true;
 	}
 	return DGPU_OK;
 }
@@ -463,6 +521,25 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 				acc += ops->cv0_vs_fc[s * q + k] * Bi[k * q + m];
 			c->ops.lb[s][m] = acc;
 		}
+	// positivity on GL nodal values: SBg = ccSB0 B^-1, BSg = B ccBS0, and the FP32 pre-filter's error factor
+	// 2 (D (q+1) + 1) 2^-24 L^D with L the largest absolute row sum of SBg
+	double L = 0.0;
+	for (int a = 0; a < q; ++a) {
+		double row = 0.0;
+		for (int m = 0; m < q; ++m) {
+			double sbg = 0.0, bsg = 0.0;
+			for (int k = 0; k < q; ++k) {
+				sbg += c->ops.SB[a][k] * Bi[k * q + m];
+				bsg += Bm[a * q + k] * c->ops.BS[k][m];
+			}
+			c->ops.SBg[a][m] = sbg;
+			c->ops.BSg[a][m] = bsg;
+			c->ops.SBf[a][m] = (float)sbg;
+			row += fabs(sbg);
+		}
+		L = fmax(L, row);
+	}
+	c->ops.pos_err = (float)(2.0 * (d * (q + 1) + 1) * ldexp(1.0, -24) * pow(L, d));
 
 	// ---- weights: TP products of the 1D GL rule (first direction fastest) ----
 	std::vector<double> w(N), wf(NF);
@@ -567,6 +644,7 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 	c->own_stream = true;
 	DG_TRY(cudaMalloc((void**)&c->u, ns * sizeof(double)));
 	DG_TRY(cudaMalloc((void**)&c->u0, ns * sizeof(double)));
+	DG_TRY(cudaMalloc((void**)&c->ug, ns * sizeof(double)));
 	DG_TRY(cudaMalloc((void**)&c->rhs, ns * sizeof(double)));
 	DG_TRY(cudaMalloc((void**)&c->vol_gl, ns * sizeof(double)));
 	DG_TRY(cudaMalloc((void**)&c->traces, nF * 2 * c->nv * NF * sizeof(double)));
@@ -625,6 +703,8 @@ dgpu_status dgpu_upload_state(dgpu_ctx* c, const double* sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	DGPU_CUDA(c, cudaMemcpyAsync(c->u, sol, state_size(c) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
 	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	c->coef_valid = true;
+	c->gl_valid = false;
 	return DGPU_OK;
 }
 
@@ -632,6 +712,9 @@ dgpu_status dgpu_download_state(dgpu_ctx* c, double* sol)
 {
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	dgpu_status st = ensure_coef(c);
+	if (st != DGPU_OK)
+		return st;
 	DGPU_CUDA(c, cudaMemcpyAsync(sol, c->u, state_size(c) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
 	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
 	return DGPU_OK;
@@ -650,7 +733,10 @@ dgpu_status dgpu_compute_rhs(dgpu_ctx* c, double* max_rhs)
 {
 	if (!c)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	dgpu_status st = enqueue_rhs(c);
+	dgpu_status st = ensure_coef(c);
+	if (st != DGPU_OK)
+		return st;
+	st = enqueue_rhs(c);
 	if (st != DGPU_OK)
 		return st;
 	return read_max(c, max_rhs);
@@ -662,6 +748,8 @@ dgpu_status dgpu_compute_rhs_host(dgpu_ctx* c, const double* sol, double* rhs, d
 		return DGPU_ERR_INVALID_ARGUMENT;
 	const size_t bytes = state_size(c) * sizeof(double);
 	DGPU_CUDA(c, cudaMemcpyAsync(c->u, sol, bytes, cudaMemcpyHostToDevice, c->stream));
+	c->coef_valid = true;
+	c->gl_valid = false;
 	dgpu_status st = enqueue_rhs(c);
 	if (st != DGPU_OK)
 		return st;
@@ -672,41 +760,64 @@ dgpu_status dgpu_compute_rhs_host(dgpu_ctx* c, const double* sol, double* rhs, d
 	return DGPU_OK;
 }
 
+// Captures one step into *graph (for dt) unless the cached one matches.
+static dgpu_status capture_step(dgpu_ctx* c, double dt, bool want_max, cudaGraphExec_t* graph, double* graph_dt)
+{
+	if (*graph && *graph_dt == dt)
+		return DGPU_OK;
+	if (*graph) {
+		cudaGraphExecDestroy(*graph);
+		*graph = nullptr;
+	}
+	cudaGraph_t g;
+	DGPU_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+	const long long before = c->launches;
+	dgpu_status st = enqueue_rk_step(c, dt, want_max);
+	c->launches = before;  // captured, not launched
+	cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+	if (st != DGPU_OK)
+		return st;
+	DGPU_CUDA(c, ec);
+	cudaError_t ei = cudaGraphInstantiate(graph, g, 0);
+	cudaGraphDestroy(g);
+	DGPU_CUDA(c, ei);
+	*graph_dt = dt;
+	return DGPU_OK;
+}
+
 dgpu_status dgpu_ssp_rk3_steps(dgpu_ctx* c, double dt, int n_steps, double* max_rhs)
 {
 	if (!c || n_steps < 0 || !(dt == dt))
 		return DGPU_ERR_INVALID_ARGUMENT;
+	dgpu_status st = ensure_gl(c);
+	if (st != DGPU_OK)
+		return st;
+	const bool want_max = (max_rhs != nullptr);
 	if (c->timing) {
 		for (int s = 0; s < n_steps; ++s) {
-			dgpu_status st = enqueue_rk_step(c, dt);
+			st = enqueue_rk_step(c, dt, want_max && s == n_steps - 1);
 			if (st != DGPU_OK)
 				return st;
 		}
 	} else {
-		if (!c->rk_graph || c->rk_graph_dt != dt) {
-			if (c->rk_graph) {
-				cudaGraphExecDestroy(c->rk_graph);
-				c->rk_graph = nullptr;
-			}
-			cudaGraph_t g;
-			DGPU_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-			const long long before = c->launches;
-			dgpu_status st = enqueue_rk_step(c, dt);
-			c->launches = before;  // captured, not launched
-			cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
-			if (st != DGPU_OK)
-				return st;
-			DGPU_CUDA(c, ec);
-			DGPU_CUDA(c, cudaGraphInstantiate(&c->rk_graph, g, 0));
-			cudaGraphDestroy(g);
-			c->rk_graph_dt = dt;
-		}
-		for (int s = 0; s < n_steps; ++s) {
+		const int plain = want_max ? n_steps - 1 : n_steps;
+		if (plain > 0 && (st = capture_step(c, dt, false, &c->rk_graph, &c->rk_graph_dt)) != DGPU_OK)
+			return st;
+		if (want_max && n_steps > 0 &&
+		    (st = capture_step(c, dt, true, &c->rk_graph_max, &c->rk_graph_max_dt)) != DGPU_OK)
+			return st;
+		for (int s = 0; s < plain; ++s) {
 			DGPU_CUDA(c, cudaGraphLaunch(c->rk_graph, c->stream));
 			c->launches += 9;
 		}
+		if (want_max && n_steps > 0) {
+			DGPU_CUDA(c, cudaGraphLaunch(c->rk_graph_max, c->stream));
+			c->launches += 9;
+		}
 	}
-	dgpu_status st = check_positivity_flag(c);
+	if (n_steps > 0)
+		c->coef_valid = false;   // the current state is ug
+	st = check_positivity_flag(c);
 	if (st != DGPU_OK)
 		return st;
 	return read_max(c, max_rhs);
@@ -756,6 +867,10 @@ dgpu_status dgpu_set_stream(dgpu_ctx* c, void* stream)
 	if (c->rk_graph) {
 		cudaGraphExecDestroy(c->rk_graph);
 		c->rk_graph = nullptr;
+	}
+	if (c->rk_graph_max) {
+		cudaGraphExecDestroy(c->rk_graph_max);
+		c->rk_graph_max = nullptr;
 	}
 	return DGPU_OK;
 }

@@ -1,8 +1,10 @@
 // Flux physics for the explicit DG residual, FP64, as device inline functions.
 //
-// Each function states the reference routine whose arithmetic it follows. The numerical fluxes keep the
-// reference's operation order where it matters for the result's rounding (sums of normal-flux components,
-// the entropy-fix comparisons on real parts).
+// Each function states the reference routine it computes. The GB300 FP64 pipe (2 DFMA per cycle per SM) is the
+// binding resource, so the numerical fluxes are written to need as few FP64 instructions as the same
+// mathematics allows: each side's state is reduced once (one reciprocal of the density), the normal flux is
+// formed from the normal velocity instead of contracting the full physical flux with the normal, and
+// divisions by the same quantity are replaced by one reciprocal. These regroupings change rounding only.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -64,73 +66,43 @@ __device__ __forceinline__ void euler_flux_ref(const double* W, const double* g,
 	}
 }
 
-// Physical Euler flux f[k][eq] (compute_Flux_euler_0, flux_euler_T.c:259-298).
+// One side of a face node: the normal physical flux n.f(W) (compute_Flux_euler_0 contracted with n) and the
+// Lax-Friedrichs wave speed |V| + c.
 template <int D>
-__device__ __forceinline__ void euler_flux(const double* W, double (*f)[D + 2])
+__device__ __forceinline__ double euler_normal_flux(const double* W, const double* n, double* Fn)
 {
 	const double rho = W[0], E = W[D + 1];
 	const double rho_inv = 1.0 / rho;
-	double u[D];
-	double V2 = 0.0;
+	double V2 = 0.0, Vn = 0.0, mn = 0.0;
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
-		u[k] = rho_inv * W[1 + k];
-		V2 += u[k] * u[k];
+		const double u = W[1 + k] * rho_inv;
+		V2 += u * u;
+		Vn += n[k] * u;
+		mn += n[k] * W[1 + k];
 	}
 	const double p = kGm1 * (E - 0.5 * rho * V2);
+	Fn[0] = mn;
 #pragma unroll
-	for (int k = 0; k < D; ++k) {
-		f[k][0] = W[1 + k];
-#pragma unroll
-		for (int m = 0; m < D; ++m)
-			f[k][1 + m] = W[1 + m] * u[k] + (m == k ? p : 0.0);
-		f[k][D + 1] = (E + p) * u[k];
-	}
+	for (int k = 0; k < D; ++k)
+		Fn[1 + k] = W[1 + k] * Vn + p * n[k];
+	Fn[D + 1] = (E + p) * Vn;
+	return sqrt(V2) + sqrt(kGamma * p * rho_inv);
 }
 
-// Lax-Friedrichs (compute_Numerical_Flux_T_euler_lax_friedrichs, numerical_flux_euler_T.c:60-327).
+// Lax-Friedrichs (compute_Numerical_Flux_T_euler_lax_friedrichs, numerical_flux_euler_T.c:60-327):
+//   nF = 1/2 [ n.(F_L + F_R) + max(|V_L| + c_L, |V_R| + c_R) (W_L - W_R) ].
 template <int D>
 __device__ __forceinline__ void num_flux_lax_friedrichs(const double* WL, const double* WR, const double* n,
                                                         double* nF)
 {
-	double VL, VR, cL, cR;
-	{
-		const double rho = WL[0], rho_inv = 1.0 / rho;
-		double V2 = 0.0;
-#pragma unroll
-		for (int k = 0; k < D; ++k) {
-			const double u = WL[1 + k] * rho_inv;
-			V2 += u * u;
-		}
-		VL = sqrt(V2);
-		const double p = kGm1 * (WL[D + 1] - 0.5 * rho * V2);
-		cL = sqrt(kGamma * p / rho);
-	}
-	{
-		const double rho = WR[0], rho_inv = 1.0 / rho;
-		double V2 = 0.0;
-#pragma unroll
-		for (int k = 0; k < D; ++k) {
-			const double u = WR[1 + k] * rho_inv;
-			V2 += u * u;
-		}
-		VR = sqrt(V2);
-		const double p = kGm1 * (WR[D + 1] - 0.5 * rho * V2);
-		cR = sqrt(kGamma * p / rho);
-	}
-	const double maxlL = VL + cL, maxlR = VR + cR;
+	double FL[D + 2], FR[D + 2];
+	const double maxlL = euler_normal_flux<D>(WL, n, FL);
+	const double maxlR = euler_normal_flux<D>(WR, n, FR);
 	const double maxV = (maxlL > maxlR ? maxlL : maxlR);
-	double FL[D][D + 2], FR[D][D + 2];
-	euler_flux<D>(WL, FL);
-	euler_flux<D>(WR, FR);
 #pragma unroll
-	for (int eq = 0; eq < D + 2; ++eq) {
-		double s = 0.0;
-#pragma unroll
-		for (int k = 0; k < D; ++k)
-			s += n[k] * (FL[k][eq] + FR[k][eq]);
-		nF[eq] = 0.5 * (s + maxV * (WL[eq] - WR[eq]));
-	}
+	for (int eq = 0; eq < D + 2; ++eq)
+		nF[eq] = 0.5 * ((FL[eq] + FR[eq]) + maxV * (WL[eq] - WR[eq]));
 }
 
 // Roe-Pike with the entropy fix of Qu et al. 2015 (compute_Numerical_Flux_T_euler_roe_pike,
@@ -154,30 +126,31 @@ __device__ __forceinline__ void num_flux_roe_pike(const double* WL, const double
 	const double pL = kGm1 * (EL - 0.5 * rhoL * V2L), HL = (EL + pL) * rhoL_inv;
 	const double pR = kGm1 * (ER - 0.5 * rhoR * V2R), HR = (ER + pR) * rhoR_inv;
 
-	const double r = sqrt(rhoR / rhoL), rP1 = r + 1.0, rho = r * rhoL;
+	// Roe averages (divisions by r + 1 through one reciprocal)
+	const double r = sqrt(rhoR * rhoL_inv), rP1_inv = 1.0 / (r + 1.0), rho = r * rhoL;
 	double u[D];
 	double Vn = 0.0, V2 = 0.0;
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
-		u[k] = (r * uR[k] + uL[k]) / rP1;
+		u[k] = (r * uR[k] + uL[k]) * rP1_inv;
 		Vn += n[k] * u[k];
 		V2 += u[k] * u[k];
 	}
-	const double H = (r * HR + HL) / rP1, c2 = kGm1 * (H - 0.5 * V2), c = sqrt(c2);
+	const double H = (r * HR + HL) * rP1_inv, c2 = kGm1 * (H - 0.5 * V2), c = sqrt(c2), c_inv = 1.0 / c;
 
 	const double l1 = min_abs_real(VnL - c, Vn - c), l5 = max_abs_real(VnR + c, Vn + c);
 	const double l234 = (Vn > 0.0 ? Vn : -Vn);
 
 	const double drho = rhoR - rhoL, dE = ER - EL, dp = pR - pL, dVn = VnR - VnL;
 	const double lc1 = 0.5 * (l5 + l1) - l234, lc2 = 0.5 * (l5 - l1);
-	const double disInter1 = lc1 * dp / (c * c) + lc2 * rho * dVn / c;
-	const double disInter2 = lc1 * rho * dVn + lc2 * dp / c;
+	const double disInter1 = (lc1 * dp * c_inv + lc2 * rho * dVn) * c_inv;
+	const double disInter2 = lc1 * rho * dVn + lc2 * dp * c_inv;
 
 	const double rhoVnL = rhoL * VnL, rhoVnR = rhoR * VnR, pLR = pL + pR;
 	nF[0] = 0.5 * ((rhoVnL + rhoVnR) - (l234 * drho + disInter1));
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
-		const double drhou = rhoR * uR[k] - rhoL * uL[k];
+		const double drhou = WR[1 + k] - WL[1 + k];
 		const double nFk = rhoVnL * uL[k] + rhoVnR * uR[k] + n[k] * pLR;
 		const double disk = l234 * drhou + disInter1 * u[k] + disInter2 * n[k];
 		nF[1 + k] = 0.5 * (nFk - disk);

@@ -5,17 +5,20 @@
 // with V = cv0_vs_vc. On TP elements with GLL solution nodes and (p+1)-point GL cubature V = B (x) B (x) B is
 // square and invertible (B = 1D GLL->GL interpolation), cv1_vs_vc[d] = Dgl_d V (GL collocation derivative,
 // exact for degree p), and cv0_vs_fc[lf] = E_lf V (E_lf = GL Lagrange values at the face). Hence
-//   R = V^-1 diag(1/(w J)) [ sum_d Dgl_d^T (w fr_d) - sum_lf E_lf^T (w_f J_f F*) ],
-// which is the same operator in exact arithmetic with the V^-T V^T pair cancelled: every contraction is a
-// 1D sum-factorised pass of q FMAs per node, and the dense per-element M^-1 (n_vs^2 doubles per element in
-// the reference) is never formed.
+//   R = V^-1 R_gl,   R_gl = diag(1/(w J)) [ sum_d Dgl_d^T (w fr_d) - sum_lf E_lf^T (w_f J_f F*) ],
+// the same operator in exact arithmetic with the V^-T V^T pair cancelled: every contraction is a 1D
+// sum-factorised pass of q FMAs per node, and the dense per-element M^-1 is never formed.
 //
-// Kernels per residual:
-//   tp_volume_kernel   u (GLL coefficients) -> u_gl = V u; volume term in GL space; face traces of u_gl.
+// Because the SSP-RK3 stage update is linear, V u_new = a V u0 + b (V u + dt R) = a ug0 + b (ug + dt R_gl): the
+// time stepper keeps the state as GL nodal values ug = V u and never applies V or V^-1 inside a step; the
+// reference's GLL coefficients are recovered (V^-1) only when the caller reads the state.
+//
+// Kernels:
+//   tp_volume_kernel   [V u ->] ug; Euler/advection flux and metric contraction; sum_j Dgl_j^T; face traces.
 //   tp_face_kernel     per face node: numerical flux of the two traces, scaled by w_f J_f.
-//   tp_lift_kernel     lift of the face fluxes, diag(1/(wJ)), V^-1, then either the residual (with the
-//                      max |rhs| reduction of compute_max_rhs_dg_like) or an SSP-RK3 stage update followed by
-//                      the positivity check of enforce_positivity_highorder.
+//   tp_lift_kernel     lift of the face fluxes and diag(1/(wJ)); then either V^-1 + residual + max|rhs| (the
+//                      reference's compute_rhs_dg), or the RK stage update in GL space + positivity check.
+//   tp_convert_kernel  u <-> ug.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -35,7 +38,12 @@ struct TPOps {
 	double lb[2][kQMax];        // GL Lagrange basis at r = -1 / +1
 	double SB[kQMax][kQMax];    // ccSB0 1D (Lagrange -> Bezier)
 	double BS[kQMax][kQMax];    // ccBS0 1D (Bezier -> Lagrange)
+	double SBg[kQMax][kQMax];   // ccSB0 B^-1: GL nodal values -> Bezier coefficients
+	double BSg[kQMax][kQMax];   // B ccBS0:   Bezier coefficients -> GL nodal values
+	float SBf[kQMax][kQMax];    // SBg rounded to FP32 (positivity pre-filter)
+	float pos_err;              // |FP32 Bezier coefficient - exact| <= pos_err * max_i |x_i| (per variable)
 };
+static_assert(sizeof(TPOps) % 8 == 0, "TPOps is copied to shared memory as doubles");
 
 struct TPParams {
 	int n_vol;
@@ -63,8 +71,6 @@ struct TPShape {
 	static constexpr int THREADS = ((E * N + 31) / 32) * 32;  // whole warps; surplus threads idle
 };
 
-__device__ __forceinline__ int pow_q(int q, int k) { return k == 0 ? 1 : (k == 1 ? q : q * q); }
-
 // Index of the node along direction `dir`.
 template <int Q>
 __device__ __forceinline__ int node_coord(int node, int dir)
@@ -73,22 +79,21 @@ __device__ __forceinline__ int node_coord(int node, int dir)
 }
 
 // One sum-factorised pass along `dir`: out[var][node] = sum_m M[a(node)][m] in[var][node with a -> m].
-// TRANS selects M^T (M[m][a]).
-template <int D, int Q, int NV, bool TRANS>
-__device__ __forceinline__ void tp_pass(const double* __restrict__ in, double* __restrict__ out,
-                                        const double (*M)[kQMax], int dir, int node)
+template <int D, int Q, int NV, typename T, typename TM>
+__device__ __forceinline__ void tp_pass(const T* __restrict__ in, T* __restrict__ out, const TM (*M)[kQMax],
+                                        int dir, int node)
 {
 	constexpr int N = TPShape<D, Q>::N;
 	const int stride = (dir == 0 ? 1 : (dir == 1 ? Q : Q * Q));
 	const int a = node_coord<Q>(node, dir);
 	const int base = node - a * stride;
-	double w[Q];
+	T w[Q];
 #pragma unroll
 	for (int m = 0; m < Q; ++m)
-		w[m] = TRANS ? M[m][a] : M[a][m];
+		w[m] = (T)M[a][m];
 #pragma unroll
 	for (int v = 0; v < NV; ++v) {
-		double s = 0.0;
+		T s = 0;
 #pragma unroll
 		for (int m = 0; m < Q; ++m)
 			s += w[m] * in[v * N + base + m * stride];
@@ -96,15 +101,41 @@ __device__ __forceinline__ void tp_pass(const double* __restrict__ in, double* _
 	}
 }
 
-__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double x)
+// The D passes of M (x) M (x) M over one element block: in -> out, `tmp` as scratch (in, out, tmp distinct).
+// Every thread of the CTA must call it (it synchronises); `active` selects the threads that compute.
+template <int D, int Q, int NV, typename T, typename TM>
+__device__ __forceinline__ void tp_apply(const T* in, T* out, T* tmp, const TM (*M)[kQMax], int node, bool active)
 {
-	atomicMax(addr, (unsigned long long)__double_as_longlong(x));
+	if (D == 2) {
+		if (active) tp_pass<D, Q, NV>(in, tmp, M, 0, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV>(tmp, out, M, 1, node);
+	} else {
+		if (active) tp_pass<D, Q, NV>(in, out, M, 0, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV>(out, tmp, M, 1, node);
+		__syncthreads();
+		if (active) tp_pass<D, Q, NV>(tmp, out, M, 2, node);
+	}
+	__syncthreads();
+}
+
+__device__ __forceinline__ unsigned long long abs_bits(double x)
+{
+	return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
+// Copies the operator set into shared memory; the caller synchronises before use.
+__device__ __forceinline__ void load_ops(TPOps* sops, const TPOps& ops)
+{
+	for (int i = threadIdx.x; i < (int)(sizeof(TPOps) / 8); i += blockDim.x)
+		reinterpret_cast<double*>(sops)[i] = reinterpret_cast<const double*>(&ops)[i];
 }
 
 // ---------------------------------------------------------------------------------------------------------------
 // Volume term + traces
 // ---------------------------------------------------------------------------------------------------------------
-template <int D, int Q, int NV, int PDE>
+template <int D, int Q, int NV, int PDE, bool GLL_IN>
 __global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
 tp_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u)
 {
@@ -112,18 +143,15 @@ tp_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u
 	constexpr int N = S::N, NF = S::NF, E = S::E;
 	extern __shared__ double smem[];
 	TPOps* sops = reinterpret_cast<TPOps*>(smem);
-	double* base = smem + (sizeof(TPOps) + 7) / 8;
-	// per element: su[NV*N] (u, then u_gl), st[NV*N] (tmp), sf[D*NV*N] (reference flux)
+	double* base = smem + sizeof(TPOps) / 8;
+	// per element: su[NV*N] (state, GL nodal), st[NV*N] (tmp), sf[D*NV*N] (reference flux)
 	constexpr int PER_E = NV * N * 2 + D * NV * N;
 
 	const int tid = threadIdx.x;
-	for (int i = tid; i < (int)(sizeof(TPOps) / 8); i += blockDim.x)
-		reinterpret_cast<double*>(sops)[i] = reinterpret_cast<const double*>(&ops)[i];
-
+	load_ops(sops, ops);
 	const int v0 = blockIdx.x * E;
 	const int n_here = min(E, P.n_vol - v0);
-	// coalesced load of n_here contiguous element blocks
-	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {
+	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {   // coalesced: contiguous element blocks
 		const int e = i / (NV * N), r = i % (NV * N);
 		base[e * PER_E + r] = u[(size_t)v0 * NV * N + i];
 	}
@@ -137,19 +165,15 @@ tp_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u
 	double* st = su + NV * N;
 	double* sf = st + NV * N;
 
-	// u_gl = V u : D passes of B, ending in su
-	if (D == 2) {
-		if (active) tp_pass<D, Q, NV, false>(su, st, sops->B, 0, node);
+	if (GLL_IN) {
+		// ug = V u: passes su -> st (-> sf) -> ... ; copy into su so the traces and flux read one buffer
+		tp_apply<D, Q, NV>(su, st, sf, sops->B, node, active);
+		if (active)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				su[k * N + node] = st[k * N + node];
 		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(st, su, sops->B, 1, node);
-	} else {
-		if (active) tp_pass<D, Q, NV, false>(su, st, sops->B, 0, node);
-		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(st, sf, sops->B, 1, node);
-		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(sf, su, sops->B, 2, node);
 	}
-	__syncthreads();
 
 	const int v = v0 + e;
 	if (active) {
@@ -210,7 +234,7 @@ tp_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u
 		for (int k = 0; k < NV; ++k)
 			P.vol_gl[((size_t)v * NV + k) * N + node] = acc[k];
 
-		// traces of u_gl on the 2D local faces
+		// traces of ug on the 2D local faces
 		for (int it = node; it < 2 * D * NF; it += N) {
 			const int lf = it / NF, t = it % NF;
 			const int nd = lf >> 1, side = lf & 1;
@@ -288,39 +312,29 @@ tp_face_kernel(const TPParams P)
 // ---------------------------------------------------------------------------------------------------------------
 // Lift + M^-1 + (residual | RK stage + positivity)
 // ---------------------------------------------------------------------------------------------------------------
-enum LiftMode { kModeRhs = 0, kModeRk = 1 };
+enum LiftMode { kModeRhs = 0, kModeRkGl = 1 };
 
 struct RkArgs {
-	double* u;         // state (GLL coefficients), updated in place
-	double* u0;        // stage-0 copy (sol_coef_p)
-	double* rhs;       // residual output (kModeRhs)
+	double* u;         // kModeRkGl: state as GL nodal values (ug), updated in place
+	double* u0;        // kModeRkGl: stage-0 copy (ug of sol_coef_p)
+	double* rhs;       // kModeRhs: residual output (GLL coefficients)
 	double dt;
 	int stage;         // 0, 1, 2
 	int positivity;
+	int want_max;      // kModeRkGl: also reduce max |rhs| (needs V^-1 of the GL residual)
 };
 
-// enforce_positivity_highorder (solve.c:187-233) on one element held in shared memory. `c` holds the element's
-// conserved state (GLL coefficients) [NV][N]; `b` is scratch [NV][N]. Returns true when a correction was made
-// (c then holds the corrected coefficients). Runs the reference's serial averages/minima on one thread; the
-// Bezier transforms are sum-factorised passes by the element's threads.
+// enforce_positivity_highorder (solve.c:187-233) on one element held in shared memory.
+// `c` holds the element's conserved state [NV][N] in the basis that `toB` maps to Bezier coefficients (`fromB`
+// maps back); `b` and `tmp` are scratch [NV][N]. Returns true when this element was corrected (c then holds the
+// corrected state). The reference's serial averages and minima run on one thread per element; the Bezier
+// transforms are sum-factorised passes by the element's threads. All threads of the CTA must call it.
 template <int D, int Q, int NV>
-__device__ bool tp_positivity(const TPOps* ops, double* c, double* b, double* tmp, int node, bool active,
-                              int* flag_out, const TPParams& P)
+__device__ bool tp_positivity_exact(const double (*toB)[kQMax], const double (*fromB)[kQMax], double* c, double* b,
+                                    double* tmp, int node, bool active, int* flag_out)
 {
 	constexpr int N = TPShape<D, Q>::N;
-	// Bezier coefficients: ccSB0 passes  (c -> b)
-	if (D == 2) {
-		if (active) tp_pass<D, Q, NV, false>(c, tmp, ops->SB, 0, node);
-		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(tmp, b, ops->SB, 1, node);
-	} else {
-		if (active) tp_pass<D, Q, NV, false>(c, b, ops->SB, 0, node);
-		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(b, tmp, ops->SB, 1, node);
-		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(tmp, b, ops->SB, 2, node);
-	}
-	__syncthreads();
+	tp_apply<D, Q, NV>(c, b, tmp, toB, node, active);
 	// convert_variables c -> p per coefficient (solution_euler_T.c:173-194)
 	if (active) {
 		const double rho = b[node];
@@ -373,12 +387,11 @@ __device__ bool tp_positivity(const TPOps* ops, double* c, double* b, double* tm
 	__syncthreads();
 	corrected = active ? (int)tmp[0] : 0;
 	__syncthreads();
-	// The whole CTA must take the same barriers: the slow path runs when any element corrected.
 	const int any = __syncthreads_or(corrected);
 	if (!any)
 		return false;
 	if (corrected) {
-		// convert p -> c per coefficient, then ccBS0 passes back to GLL coefficients
+		// convert p -> c per coefficient, then back to the state's basis
 		const double rho = b[node];
 		double V2 = 0.0;
 #pragma unroll
@@ -390,20 +403,17 @@ __device__ bool tp_positivity(const TPOps* ops, double* c, double* b, double* tm
 		b[(D + 1) * N + node] = b[(D + 1) * N + node] / kGm1 + 0.5 * rho * V2;
 	}
 	__syncthreads();
-	if (D == 2) {
-		if (corrected) tp_pass<D, Q, NV, false>(b, tmp, ops->BS, 0, node);
-		__syncthreads();
-		if (corrected) tp_pass<D, Q, NV, false>(tmp, c, ops->BS, 1, node);
-	} else {
-		if (corrected) tp_pass<D, Q, NV, false>(b, tmp, ops->BS, 0, node);
-		__syncthreads();
-		if (corrected) tp_pass<D, Q, NV, false>(tmp, b, ops->BS, 1, node);
-		__syncthreads();
-		if (corrected) tp_pass<D, Q, NV, false>(b, c, ops->BS, 2, node);
-	}
-	__syncthreads();
+	tp_apply<D, Q, NV>(b, c, tmp, fromB, node, corrected != 0);
 	return corrected != 0;
 }
+
+// Positivity in the RK epilogue. The exact check is the reference's FP64 computation above. It is preceded by
+// an FP32 pre-filter that proves, for most elements, that the exact check cannot trigger: every FP32 Bezier
+// coefficient carries an absolute error of at most pos_err * max_i |x_i| of its variable (a forward bound for D
+// passes of q-term FMA dot products with FP32-rounded inputs and coefficients, computed on the host with a factor
+// 2 margin); density and pressure are bounded below from those intervals, with a further relative margin of
+// 1e-5 on the pressure bound for its own FP32 arithmetic. Only CTAs holding an element that fails the filter run
+// the exact check, so the decisions are those of the exact FP64 check.
 
 template <int D, int Q, int NV, int MODE>
 __global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
@@ -413,14 +423,11 @@ tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 	constexpr int N = S::N, NF = S::NF, E = S::E;
 	extern __shared__ double smem[];
 	TPOps* sops = reinterpret_cast<TPOps*>(smem);
-	double* base = smem + (sizeof(TPOps) + 7) / 8;
-	constexpr int PER_E = 3 * NV * N;
+	double* base = smem + sizeof(TPOps) / 8;
+	constexpr int PER_E = 3 * NV * N + 8;   // sa, sb, sc + per-element scalars
 
 	const int tid = threadIdx.x;
-	for (int i = tid; i < (int)(sizeof(TPOps) / 8); i += blockDim.x)
-		reinterpret_cast<double*>(sops)[i] = reinterpret_cast<const double*>(&ops)[i];
-	__syncthreads();  // the lift below reads sops->lb written by other warps
-
+	load_ops(sops, ops);
 	const int v0 = blockIdx.x * E;
 	const int n_here = min(E, P.n_vol - v0);
 	const int e = tid / N, node = tid % N;
@@ -429,12 +436,16 @@ tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 	double* sa = base + e * PER_E;
 	double* sb = sa + NV * N;
 	double* sc = sb + NV * N;
+	int* sscale = reinterpret_cast<int*>(sc + NV * N);   // NV ints (FP32 scales) + spare
+	if (active && node < 8)
+		reinterpret_cast<double*>(sscale)[node] = 0.0;
+	__syncthreads();  // the lift below reads sops->lb written by other warps
 
+	double Rg[NV];  // GL-space residual R_gl of this node
 	if (active) {
-		double r[NV];
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			r[k] = P.vol_gl[((size_t)v * NV + k) * N + node];
+			Rg[k] = P.vol_gl[((size_t)v * NV + k) * N + node];
 #pragma unroll
 		for (int lf = 0; lf < 2 * D; ++lf) {
 			const int fs = P.vol_face[(size_t)v * 2 * D + lf];
@@ -454,49 +465,43 @@ tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 			const double* src = P.nnf + (size_t)f * NV * NF;
 #pragma unroll
 			for (int k = 0; k < NV; ++k)
-				r[k] += l * src[k * NF + idx];
+				Rg[k] += l * src[k * NF + idx];
 		}
 		const double iw = P.inv_wJ[(size_t)v * N + node];
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			sa[k * N + node] = r[k] * iw;
+			Rg[k] *= iw;
 	}
-	__syncthreads();
-	// V^-1: D passes of Binv, result in sa (D even) / sc (D odd)
-	double* res;
-	if (D == 2) {
-		if (active) tp_pass<D, Q, NV, false>(sa, sb, sops->Binv, 0, node);
-		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(sb, sa, sops->Binv, 1, node);
-		res = sa;
-	} else {
-		if (active) tp_pass<D, Q, NV, false>(sa, sb, sops->Binv, 0, node);
-		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(sb, sc, sops->Binv, 1, node);
-		__syncthreads();
-		if (active) tp_pass<D, Q, NV, false>(sc, sa, sops->Binv, 2, node);
-		res = sa;
-	}
-	__syncthreads();
 
-	// max |rhs| (compute_max_rhs_dg_like): integer max over the bit patterns of |R|
+	const bool need_coef = (MODE == kModeRhs) || rk.want_max;   // uniform across the grid
 	unsigned long long mx = 0ull;
 	double R[NV];
-	if (active) {
+	if (need_coef) {
+		// R = V^-1 R_gl (GLL coefficients): D passes of Binv
+		if (active)
 #pragma unroll
-		for (int k = 0; k < NV; ++k) {
-			R[k] = res[k * N + node];
-			const unsigned long long bits = (unsigned long long)__double_as_longlong(R[k]) & 0x7fffffffffffffffull;
-			mx = bits > mx ? bits : mx;
+			for (int k = 0; k < NV; ++k)
+				sa[k * N + node] = Rg[k];
+		__syncthreads();
+		tp_apply<D, Q, NV>(sa, sb, sc, sops->Binv, node, active);
+		if (active) {
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				R[k] = sb[k * N + node];
+				const unsigned long long bits = abs_bits(R[k]);
+				mx = bits > mx ? bits : mx;
+			}
 		}
-	}
+		// max |rhs| (compute_max_rhs_dg_like): integer max over the bit patterns of |R|
 #pragma unroll
-	for (int off = 16; off > 0; off >>= 1) {
-		const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
-		mx = o > mx ? o : mx;
+		for (int off = 16; off > 0; off >>= 1) {
+			const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
+			mx = o > mx ? o : mx;
+		}
+		if ((tid & 31) == 0 && mx && P.max_bits)
+			atomicMax(P.max_bits, mx);
+		__syncthreads();   // sa/sb/sc are reused below
 	}
-	if ((tid & 31) == 0 && mx && P.max_bits)
-		atomicMax(P.max_bits, mx);
 
 	if constexpr (MODE == kModeRhs) {
 		if (active) {
@@ -505,53 +510,124 @@ tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 				rk.rhs[((size_t)v * NV + k) * N + node] = R[k];
 		}
 		return;
-	}
-
-	// SSP-RK3 stage update (solve_explicit.c:277-295)
-	double snew[NV];
-	if (active) {
-		const size_t o = (size_t)v * NV * N + node;
+	} else {
+		// SSP-RK3 stage update in GL space (solve_explicit.c:277-295; linear, so V commutes with it)
+		double snew[NV];
+		if (active) {
+			const size_t o = (size_t)v * NV * N + node;
 #pragma unroll
-		for (int k = 0; k < NV; ++k) {
-			const double s = rk.u[o + (size_t)k * N];
-			if (rk.stage == 0) {
-				rk.u0[o + (size_t)k * N] = s;
-				snew[k] = s + rk.dt * R[k];
-			} else if (rk.stage == 1) {
-				const double sp = rk.u0[o + (size_t)k * N];
-				snew[k] = (1.0 / 4.0) * (3.0 * sp + s + rk.dt * R[k]);
-			} else {
-				const double sp = rk.u0[o + (size_t)k * N];
-				snew[k] = (1.0 / 3.0) * (sp + 2.0 * s + 2.0 * rk.dt * R[k]);
+			for (int k = 0; k < NV; ++k) {
+				const double s = rk.u[o + (size_t)k * N];
+				if (rk.stage == 0) {
+					rk.u0[o + (size_t)k * N] = s;
+					snew[k] = s + rk.dt * Rg[k];
+				} else if (rk.stage == 1) {
+					const double sp = rk.u0[o + (size_t)k * N];
+					snew[k] = (1.0 / 4.0) * (3.0 * sp + s + rk.dt * Rg[k]);
+				} else {
+					const double sp = rk.u0[o + (size_t)k * N];
+					snew[k] = (1.0 / 3.0) * (sp + 2.0 * s + 2.0 * rk.dt * Rg[k]);
+				}
 			}
 		}
-	}
-	if (rk.positivity) {
-		// element state to shared memory for the Bezier check
+		if (rk.positivity) {
+			if (active)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					sb[k * N + node] = snew[k];
+			__syncthreads();
+			// FP32 pre-filter (sa as float [NV][N] x2, sscale per element)
+			float* xf = reinterpret_cast<float*>(sa);
+			float* tf = xf + NV * N;
+			float* tmpf = reinterpret_cast<float*>(sc);
+			if (active) {
+#pragma unroll
+				for (int k = 0; k < NV; ++k) {
+					const float x = (float)snew[k];
+					xf[k * N + node] = x;
+					atomicMax(&sscale[k], __float_as_int(fabsf(x)));
+				}
+			}
+			__syncthreads();
+			tp_apply<D, Q, NV>(xf, tf, tmpf, sops->SBf, node, active);
+			bool safe = true;
+			if (active) {
+				const float err = sops->pos_err;
+				const float rho = tf[node];
+				const float erho = err * __int_as_float(sscale[0]);
+				const float rho_lo = rho - erho;
+				safe = rho_lo > 1e-6f * __int_as_float(sscale[0]) + 1e-12f;
+				if (safe) {
+					float m2 = 0.f;
+#pragma unroll
+					for (int k = 0; k < D; ++k) {
+						const float mk = fabsf(tf[(1 + k) * N + node]) + err * __int_as_float(sscale[1 + k]);
+						m2 += mk * mk;
+					}
+					const float E_lo = tf[(D + 1) * N + node] - err * __int_as_float(sscale[D + 1]);
+					const float ke = 0.5f * m2 / rho_lo;
+					const float p_lo = 0.4f * (E_lo - ke);
+					const float mag = fabsf(E_lo) + ke;
+					safe = p_lo > 1e-5f * mag + 1e-12f;   // NaN/Inf fail this test and go to the exact path
+				}
+			}
+			const int unsafe = __syncthreads_or(active && !safe);
+			if (unsafe) {
+				int flag = 0;
+				const bool corr =
+					tp_positivity_exact<D, Q, NV>(sops->SBg, sops->BSg, sb, sc, sa, node, active, &flag);
+				if (flag)
+					atomicExch(P.err_flag, 1);
+				if (corr) {
+					if (node == 0)
+						atomicAdd(P.n_corr, 1ull);
+#pragma unroll
+					for (int k = 0; k < NV; ++k)
+						snew[k] = sb[k * N + node];
+				}
+			}
+		}
 		if (active) {
+			const size_t o = (size_t)v * NV * N + node;
 #pragma unroll
 			for (int k = 0; k < NV; ++k)
-				sb[k * N + node] = snew[k];
-		}
-		__syncthreads();
-		int flag = 0;
-		const bool corr = tp_positivity<D, Q, NV>(sops, sb, sc, sa, node, active, &flag, P);
-		if (flag)
-			atomicExch(P.err_flag, 1);
-		if (corr) {
-			if (node == 0)
-				atomicAdd(P.n_corr, 1ull);
-#pragma unroll
-			for (int k = 0; k < NV; ++k)
-				snew[k] = sb[k * N + node];
+				rk.u[o + (size_t)k * N] = snew[k];
 		}
 	}
-	if (active) {
-		const size_t o = (size_t)v * NV * N + node;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// u (GLL coefficients) <-> ug (GL nodal values)
+// ---------------------------------------------------------------------------------------------------------------
+template <int D, int Q, int NV, bool TO_GL>
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
+tp_convert_kernel(const TPOps ops, int n_vol, const double* __restrict__ in, double* __restrict__ out)
+{
+	using S = TPShape<D, Q>;
+	constexpr int N = S::N, E = S::E;
+	extern __shared__ double smem[];
+	TPOps* sops = reinterpret_cast<TPOps*>(smem);
+	double* base = smem + sizeof(TPOps) / 8;
+	constexpr int PER_E = 3 * NV * N;
+	const int tid = threadIdx.x;
+	load_ops(sops, ops);
+	const int v0 = blockIdx.x * E;
+	const int n_here = min(E, n_vol - v0);
+	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {
+		const int e = i / (NV * N), r = i % (NV * N);
+		base[e * PER_E + r] = in[(size_t)v0 * NV * N + i];
+	}
+	__syncthreads();
+	const int e = tid / N, node = tid % N;
+	const bool active = e < n_here;
+	double* sa = base + e * PER_E;
+	double* sb = sa + NV * N;
+	double* sc = sb + NV * N;
+	tp_apply<D, Q, NV>(sa, sb, sc, TO_GL ? sops->B : sops->Binv, node, active);
+	if (active)
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			rk.u[o + (size_t)k * N] = snew[k];
-	}
+			out[((size_t)(v0 + e) * NV + k) * N + node] = sb[k * N + node];
 }
 
 }  // namespace dgpu

@@ -141,3 +141,27 @@ def test_launch_count(gpu_lib):
         assert sim.kernel_launches() == 3
         sim.ssp_rk3_steps(prob.dt, 2)
         assert sim.kernel_launches() == 3 + 18
+
+
+def test_state_round_trips_between_rk_and_residual(gpu_lib):
+    """The time stepper keeps the state as GL nodal values; reading it back, continuing in several calls and
+    evaluating the residual afterwards all agree with the oracle on the reference's GLL coefficients."""
+    from dpgsolver_gb300.solver import Simulation
+    prob = P.euler_hex_3d(4, 3, num_flux=P.NUM_FLUX_ROE_PIKE)
+    ref = oracle.Oracle(prob)
+    s_ref = prob.sol.copy()
+    for _ in range(5):
+        s_ref, mx_ref, _ = ref.ssp_rk3_step(s_ref, prob.dt)
+    r_ref, rmx_ref = ref.compute_rhs(s_ref)
+    with Simulation(prob) as sim:
+        sim.ssp_rk3_steps(prob.dt, 2, want_max=False)
+        mid = sim.sol_coef                        # GL -> GLL conversion in the middle of the run
+        mx = sim.ssp_rk3_steps(prob.dt, 3)        # continues from the GL state; max from the last stage
+        s = sim.sol_coef
+        rmx = sim.compute_rhs()                   # residual of the GLL state
+        r = sim.rhs
+    assert np.all(np.isfinite(mid))
+    assert rel_err(s, s_ref) <= TOL
+    assert abs(mx - mx_ref) <= 1e-10 * mx_ref
+    assert rel_err(r, r_ref) <= TOL
+    assert abs(rmx - rmx_ref) <= 1e-10 * rmx_ref
