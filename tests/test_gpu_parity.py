@@ -140,7 +140,7 @@ def test_launch_count(gpu_lib):
         sim.compute_rhs()
         assert sim.kernel_launches() == 3
         sim.ssp_rk3_steps(prob.dt, 2)
-        assert sim.kernel_launches() == 3 + 18
+        assert sim.kernel_launches() == 3 + 1 + 18   # + the V u conversion to the GL state before stepping
 
 
 def test_state_round_trips_between_rk_and_residual(gpu_lib):
