@@ -6,10 +6,13 @@ Lax-Friedrichs flux, z-axis isentropic vortex plus seeded uniform density pertur
 seeded inputs; no dataset is involved.
 
 Metric: DOF-residual-evals/s (FP64) = N_s x residual evaluations per second, N_s = total state scalars.
-One step = one residual evaluation R = M^-1 (volume + face) of the whole mesh (compute_rhs_dg).
-  value   device-resident state, CUDA events on the library's stream, max over ranks.
-  e2e     the same evaluation through dgpu_compute_rhs_host from pinned host memory: H2D of the state and D2H
-          of the residual inside the timed region.
+One step = one SSP-RK3 step of the whole mesh = 3 residual evaluations R = M^-1 (volume + face), each followed
+by its stage update and positivity check (time_step_ssp_rk_33), replayed from a captured CUDA graph.
+  value           device-resident state, CUDA events on the library's stream, max over ranks.
+  plain_launches  the same stages launched kernel by kernel (the per-group form without the graph).
+  compute_rhs_dg  the residual entry alone on the reference's GLL coefficients.
+  e2e             every step through the C ABI from pinned host memory: upload sol_coef, one RK3 step,
+                  download sol_coef (84 MB each way per step inside the timed region).
 Inputs are larger than L2 (state 84 MB + metric terms 151 MB + face data 50 MB per evaluation), so no flush.
 
 --impl reference times the reference's algorithm on the host cores. The reference itself cannot be built here
@@ -132,24 +135,29 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def flops_per_element(d, q, nv, flux):
-    """FP64 flops of one residual per element, counted from the kernels (FMA = 2 flops; a division or square
-    root counted as 1 flop; the instruction sequences behind them take more FP64 issue slots)."""
+def flops_per_element(d, q, nv, flux, coef_io):
+    """FP64 flops of one residual per element, counted from the kernels (FMA = 2 flops; a division or square root
+    counted as 1 flop; the instruction sequences behind them take more FP64 issue slots). coef_io: the residual
+    reads and writes the reference's GLL coefficients (compute_rhs_dg: + V u and V^-1 R); otherwise it is the RK
+    stage on GL nodal values (+ the stage update)."""
     N = q ** d
     NF = q ** (d - 1)
     pass_ = 2 * q * N * nv                     # one sum-factorised pass over all variables
-    interp = d * pass_                         # V u
     flux_vol = N * (1 + 2 * d + 2 * d + 3 + d * (2 * d + 1 + 2 * d + 1))   # rho_inv,u,V2,p, U_j, fr
     vol = d * pass_                            # sum_j Dgl_j^T fr_j
     traces = 2 * d * NF * nv * 2 * q
     if flux == "roe_pike":
-        f_num = 150 if d == 3 else 120
+        f_num = 130 if d == 3 else 105
     else:
-        f_num = 110 if d == 3 else 90
+        f_num = 75 if d == 3 else 60
     num = d * NF * (f_num + nv)                # d faces per element, scaled by w J
     lift = 2 * d * N * nv * 2 + N * nv         # E^T nnf per face + diag(1/(wJ))
-    minv = d * pass_
-    return interp + flux_vol + vol + traces + num + lift + minv
+    total = flux_vol + vol + traces + num + lift
+    if coef_io:
+        total += 2 * d * pass_                 # V u and V^-1 R
+    else:
+        total += 3 * N * nv                    # stage update
+    return total
 
 
 def algorithmic_bytes(prob, kernel):
@@ -164,8 +172,8 @@ def algorithmic_bytes(prob, kernel):
         return s + 8 * nV * d * d * N + s + tr
     if kernel == "tp_face_kernel":
         return tr + 8 * nF * (d + 1) * NF + nnf
-    if kernel == "tp_lift_kernel":
-        return s + 2 * nnf + 8 * nV * N + s
+    if kernel == "tp_lift_kernel":      # RK stage: vol_gl + nnf + 1/(wJ) + state + stage-0 copy in, state out
+        return s + 2 * nnf + 8 * nV * N + 3 * s
     raise KeyError(kernel)
 
 
@@ -180,6 +188,17 @@ def eval_bytes(prob):
 # ------------------------------------------------------------------------------------------------------------------
 # arms
 # ------------------------------------------------------------------------------------------------------------------
+
+def _timed(torch, stream, fn, reps):
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(reps):
+        fn()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1)
+
 
 def run_ours(args, rank, world, local_rank):
     import torch
@@ -197,104 +216,104 @@ def run_ours(args, rank, world, local_rank):
     sim = Simulation(prob, stream=stream.cuda_stream)
     lib = _lib.load()
     ns = prob.n_state
-
-    # warm-up
-    for _ in range(max(args.warmup, 3)):
-        sim.compute_rhs(want_max=False)
-    torch.cuda.synchronize()
+    dt = prob.dt
+    # steps of the timed region: each step is one SSP-RK3 step = 3 residual evaluations (stages)
+    n_rk = max(1, args.steps)
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    # timed region: K device-resident residual evaluations
+    def max_over_ranks(ms):
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return ms
+
+    if args.only_residual:
+        for _ in range(max(args.warmup, 3)):
+            sim.compute_rhs(want_max=False)
+        ms = _timed(torch, stream, lambda: sim.compute_rhs(want_max=False), args.steps)
+        sim.close()
+        return {"metric": "DOF-residual-evals/sec (compute_rhs_dg, device-resident)", "value": ns * args.steps / (ms * 1e-3),
+                "unit": "DOF-residual-evals/s", "ms_per_step": ms / args.steps, "n_state": ns,
+                "elements": prob.n_volumes}
+    if args.only_rk:
+        sim.ssp_rk3_steps(dt, max(args.warmup, 3), want_max=False)
+        ms = _timed(torch, stream, lambda: sim.ssp_rk3_steps(dt, 1, want_max=False), args.steps)
+        sim.close()
+        return {"metric": "DOF-residual-evals/sec (SSP-RK3 stages, graph)", "value": 3 * ns * args.steps / (ms * 1e-3),
+                "unit": "DOF-residual-evals/s", "ms_per_step": ms / args.steps, "n_state": ns,
+                "elements": prob.n_volumes}
+
+    # ---- headline: SSP-RK3 steps replayed from the captured CUDA graph (device-resident state) ----
+    sim.ssp_rk3_steps(dt, max(args.warmup, 3), want_max=False)
+    torch.cuda.synchronize()
     launches0 = sim.kernel_launches()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clk:
         barrier()
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            sim.compute_rhs(want_max=False)
-        ev1.record(stream)
-        torch.cuda.synchronize()
+        ms = _timed(torch, stream, lambda: sim.ssp_rk3_steps(dt, n_rk, want_max=False), 1)
         barrier()
-    ms = ev0.elapsed_time(ev1)
     launches = sim.kernel_launches() - launches0
     clocks = clk.summary()
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    ms_per_step = t_max / args.steps
-    value = world * ns * args.steps / (t_max * 1e-3)
-    if args.only_residual:
-        sim.close()
-        return {"metric": "DOF-residual-evals/sec (device-resident residual only)", "value": value,
-                "unit": "DOF-residual-evals/s", "ms_per_step": ms_per_step, "n_state": ns, "elements": prob.n_volumes,
-                "gpu_launches": int(launches), "clocks": clocks}
+    t_max = max_over_ranks(ms)
+    ms_per_step = t_max / n_rk
+    value = world * ns * 3 * n_rk / (t_max * 1e-3)
 
-    # RK3 stages replayed from the captured graph (one residual + stage update + positivity per stage)
-    n_rk = max(1, args.steps // 3)
-    sim.ssp_rk3_steps(prob.dt, 1, want_max=False)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    sim.ssp_rk3_steps(prob.dt, n_rk, want_max=False)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    rk_ms = ev0.elapsed_time(ev1)
-    rk_stage_value = world * ns * 3 * n_rk / (rk_ms * 1e-3)
-
-    # e2e: host buffers (pinned), copies inside the timed region
-    sol_h = torch.empty(prob.sol.shape, dtype=torch.float64, pin_memory=True)
-    sol_h.copy_(torch.from_numpy(prob.sol))
-    rhs_h = torch.empty_like(sol_h).pin_memory()
-    c_dp = _lib.c_double_p
-    sp = ctypes.cast(sol_h.data_ptr(), c_dp)
-    rp = ctypes.cast(rhs_h.data_ptr(), c_dp)
-    for _ in range(2):
-        _lib.check(lib.dgpu_compute_rhs_host(sim.handle, sp, rp, None), sim.handle)
-    barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        _lib.check(lib.dgpu_compute_rhs_host(sim.handle, sp, rp, None), sim.handle)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * ns * args.steps / (e2e_ms * 1e-3)
-
-    # per-kernel durations (CUDA events around each launch on the same stream)
-    sim.set_kernel_timing(True)
-    n_kt = max(3, min(args.steps, 10))
-    for _ in range(n_kt):
-        sim.compute_rhs(want_max=False)
+    # ---- plain form: the same stages launched one kernel at a time (no graph) ----
+    sim.set_kernel_timing(True)       # eager launches, CUDA events around each kernel
+    n_plain = max(3, min(n_rk, 20))
+    sim.ssp_rk3_steps(dt, 1, want_max=False)
+    ms_plain = _timed(torch, stream, lambda: sim.ssp_rk3_steps(dt, n_plain, want_max=False), 1)
     kt = {}
     for name in ("tp_volume_kernel", "tp_face_kernel", "tp_lift_kernel"):
         tot, cnt = sim.kernel_time(name)
         kt[name] = tot / max(cnt, 1)
     sim.set_kernel_timing(False)
+    plain_value = world * ns * 3 * n_plain / (max_over_ranks(ms_plain) * 1e-3)
+
+    # ---- compute_rhs_dg: residual on the reference's GLL coefficients (device-resident) ----
+    for _ in range(3):
+        sim.compute_rhs(want_max=False)
+    ms_rhs = _timed(torch, stream, lambda: sim.compute_rhs(want_max=False), n_rk)
+    rhs_value = world * ns * n_rk / (max_over_ranks(ms_rhs) * 1e-3)
+
+    # ---- e2e: the reference-facing calls with pinned host buffers, copies inside the timed region ----
+    # every step: sol_coef host -> device, time_step_ssp_rk_33 (3 residuals), sol_coef device -> host
+    sol_h = torch.empty(prob.sol.shape, dtype=torch.float64, pin_memory=True)
+    sol_h.copy_(torch.from_numpy(prob.sol))
+    out_h = torch.empty_like(sol_h).pin_memory()
+    c_dp = _lib.c_double_p
+    sp = ctypes.cast(sol_h.data_ptr(), c_dp)
+    op = ctypes.cast(out_h.data_ptr(), c_dp)
+
+    def e2e_step():
+        _lib.check(lib.dgpu_upload_state(sim.handle, sp), sim.handle)
+        _lib.check(lib.dgpu_ssp_rk3_step(sim.handle, ctypes.c_double(dt), None), sim.handle)
+        _lib.check(lib.dgpu_download_state(sim.handle, op), sim.handle)
+
+    for _ in range(2):
+        e2e_step()
+    n_e2e = max(3, min(n_rk, 50))
+    barrier()
+    e2e_ms = max_over_ranks(_timed(torch, stream, e2e_step, n_e2e))
+    e2e_value = world * ns * 3 * n_e2e / (e2e_ms * 1e-3)
+
     dom = max(kt, key=kt.get)
     peak, peak_kind = hbm_peak()
     ab = algorithmic_bytes(prob, dom)
     achieved = ab / (kt[dom] * 1e-3) / 1e9
     fp64_peak = ctypes.c_double()
     _lib.check(lib.dgpu_probe_fp64(20000, ctypes.byref(fp64_peak)))
-    fpe = flops_per_element(prob.d, prob.ops.q, prob.n_var, w["flux"])
-    eval_flops = fpe * prob.n_volumes
-    eval_ms = sum(kt.values())
+    stage_flops = flops_per_element(prob.d, prob.ops.q, prob.n_var, w["flux"], coef_io=False) * prob.n_volumes
+    stage_ms = sum(kt.values())
     res = {
         "metric": "DOF-residual-evals/sec FP64 (batched graph vs plain per-group) at <=1e-12; %HBM peak",
         "value": value,
         "unit": "DOF-residual-evals/s",
         "n_gpus": world,
-        "steps": args.steps,
+        "steps": n_rk,
         "warmup": args.warmup,
         "ms_per_step": ms_per_step,
         "higher_is_better": True,
@@ -305,22 +324,28 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": w["desc"], "elements": prob.n_volumes, "p": prob.ops.p, "n_state": ns,
                    "faces": prob.mesh.n_faces, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (state 84 MB + metrics 151 MB + face data 50 MB), no flush",
-                   "step": "one residual evaluation (volume + face + lift + M^-1), device-resident state"},
+                   "step": "one SSP-RK3 step = 3 residual evaluations (volume + face + lift + stage update + "
+                           "positivity), replayed from a CUDA graph; value counts N_s per residual evaluation",
+                   "dt": dt},
+        "plain_launches": {"value": plain_value, "unit": "DOF-residual-evals/s",
+                           "note": "the same stages launched kernel by kernel without the graph"},
+        "compute_rhs_dg": {"value": rhs_value, "unit": "DOF-residual-evals/s",
+                           "note": "residual on the reference's GLL coefficients (V u and V^-1 R included)"},
         "e2e": {"value": e2e_value, "unit": "DOF-residual-evals/s", "h2d_bytes_per_step": int(ns * 8),
-                "d2h_bytes_per_step": int(ns * 8)},
+                "d2h_bytes_per_step": int(ns * 8),
+                "note": "per step: dgpu_upload_state + dgpu_ssp_rk3_step + dgpu_download_state from pinned memory"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_source": f"{peak_kind} (MEASURED_PEAKS hbm_gbs)",
                      "algorithmic_bytes_per_launch": ab, "kernel_ms": kt},
-        "fp64_pipe": {"achieved_tflops": eval_flops / (eval_ms * 1e-3) / 1e12,
+        "fp64_pipe": {"achieved_tflops": stage_flops / (stage_ms * 1e-3) / 1e12,
                       "peak_tflops": fp64_peak.value, "peak_source": "measured (dgpu_probe_fp64 DFMA loop)",
-                      "frac": eval_flops / (eval_ms * 1e-3) / 1e12 / fp64_peak.value,
-                      "flops_per_eval": eval_flops,
+                      "frac": stage_flops / (stage_ms * 1e-3) / 1e12 / fp64_peak.value,
+                      "flops_per_stage": stage_flops,
                       "note": "binding roof: FP64 issue rate, not HBM"},
-        "eval_hbm": {"bytes_per_eval": eval_bytes(prob), "achieved_gbs": eval_bytes(prob) / (ms_per_step * 1e-3) / 1e9,
-                     "frac": eval_bytes(prob) / (ms_per_step * 1e-3) / 1e9 / peak},
-        "rk3_stage": {"value": rk_stage_value, "unit": "DOF-residual-evals/s",
-                      "note": "SSP-RK3 steps replayed from a captured CUDA graph (stage = residual + update + positivity)"},
+        "eval_hbm": {"bytes_per_eval": eval_bytes(prob),
+                     "achieved_gbs": eval_bytes(prob) / (ms_per_step / 3 * 1e-3) / 1e9,
+                     "frac": eval_bytes(prob) / (ms_per_step / 3 * 1e-3) / 1e9 / peak},
         "clocks": clocks,
         "setup_s": setup_s,
     }
@@ -404,7 +429,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="hex3d")
@@ -412,7 +437,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n", type=int, default=None, help="elements per direction (profiling of smaller cases)")
     ap.add_argument("--only-residual", action="store_true",
-                    help="time the device-resident residual only (no RK, e2e, per-kernel timing or CPU baseline)")
+                    help="time compute_rhs_dg only (device-resident; profiling)")
+    ap.add_argument("--only-rk", action="store_true", help="time graph-replayed SSP-RK3 steps only (profiling)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
