@@ -330,7 +330,7 @@ struct RkArgs {
 // corrected state). The reference's serial averages and minima run on one thread per element; the Bezier
 // transforms are sum-factorised passes by the element's threads. All threads of the CTA must call it.
 template <int D, int Q, int NV>
-__device__ bool tp_positivity_exact(const double (*toB)[kQMax], const double (*fromB)[kQMax], double* c, double* b,
+__device__ __noinline__ bool tp_positivity_exact(const double (*toB)[kQMax], const double (*fromB)[kQMax], double* c, double* b,
                                     double* tmp, int node, bool active, int* flag_out)
 {
 	constexpr int N = TPShape<D, Q>::N;
@@ -416,7 +416,7 @@ __device__ bool tp_positivity_exact(const double (*toB)[kQMax], const double (*f
 // the exact check, so the decisions are those of the exact FP64 check.
 
 template <int D, int Q, int NV, int MODE>
-__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS, 2)
 tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 {
 	using S = TPShape<D, Q>;
