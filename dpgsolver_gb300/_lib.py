@@ -89,6 +89,8 @@ EXPORTS = {
     "dgpu_kernel_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, c_double_p,
                                         ctypes.POINTER(ctypes.c_longlong)]),
     "dgpu_probe_fp64": (ctypes.c_int, [ctypes.c_int, c_double_p]),
+    "dgpu_vjp_forward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
+    "dgpu_vjp_backward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
     "dgpu_compute_rhs_noalloc": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.POINTER(TPOperators),
                                                 ctypes.POINTER(Mesh), ctypes.c_void_p, ctypes.c_void_p, c_double_p,
                                                 ctypes.c_void_p]),

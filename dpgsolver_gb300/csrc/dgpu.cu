@@ -14,6 +14,7 @@
 
 #include "../../include/dgpu.h"
 #include "dgpu_tp.cuh"
+#include "dgpu_adjoint.cuh"
 
 using namespace dgpu;
 
@@ -37,6 +38,8 @@ struct dgpu_ctx {
 	// device memory
 	double *u = nullptr, *u0 = nullptr, *rhs = nullptr;
 	double* ug = nullptr;                 // state as GL nodal values (time stepping); u0 holds the stage-0 copy
+	// adjoint (allocated on first use): state kept by dgpu_vjp_forward, cotangent, gradient, adjoint face data
+	double *u_saved = nullptr, *vbar = nullptr, *ubar = nullptr, *atraces = nullptr, *wbar = nullptr;
 	bool coef_valid = true, gl_valid = false;   // which of u / ug holds the current state
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
@@ -59,6 +62,7 @@ struct dgpu_ctx {
 	cudaError_t (*launch_lift_rhs)(dgpu_ctx*) = nullptr;
 	cudaError_t (*launch_lift_rk)(dgpu_ctx*, double dt, int stage, int want_max) = nullptr;
 	cudaError_t (*launch_convert)(dgpu_ctx*, bool to_gl) = nullptr;
+	cudaError_t (*launch_adjoint)(dgpu_ctx*, const double* u, const double* rbar, double* ubar) = nullptr;
 	// optional per-kernel timing (eager launches only)
 	bool timing = false;
 	std::vector<KernelTimer> timers;
@@ -162,6 +166,13 @@ size_t lift_smem_bytes()
 {
 	using S = TPShape<D, Q>;
 	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * (3 * NV * S::N + 8) * sizeof(double);
+}
+
+template <int D, int Q, int NV>
+size_t adj_volume_smem_bytes()
+{
+	using S = TPShape<D, Q>;
+	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * (3 * NV * S::N + D * NV * S::N) * sizeof(double);
 }
 
 template <int D, int Q, int NV>
@@ -275,9 +286,43 @@ cudaError_t launch_convert_t(dgpu_ctx* c, bool to_gl)
 	return cudaGetLastError();
 }
 
+// VJP of the residual at state u (GLL): 3 kernels (volume + traces, faces, lift + V^T).
+template <int D, int Q, int NV, int PDE, int FLUX>
+cudaError_t launch_adjoint_t(dgpu_ctx* c, const double* u, const double* rbar, double* ubar)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	AdjArgs A;
+	A.u = u;
+	A.rbar = rbar;
+	A.ubar = ubar;
+	A.atraces = c->atraces;
+	A.wbar = c->wbar;
+	record_start(c, "tp_adj_volume_kernel");
+	tp_adj_volume_kernel<D, Q, NV, PDE><<<blocks, S::THREADS, adj_volume_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, c->params(), A);
+	record_stop(c);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess)
+		return e;
+	const long long nfn = (long long)c->n_face * S::NF;
+	record_start(c, "tp_adj_face_kernel");
+	tp_adj_face_kernel<D, Q, NV, PDE, FLUX><<<(unsigned)((nfn + 127) / 128), 128, 0, c->stream>>>(c->params(), A);
+	record_stop(c);
+	if ((e = cudaGetLastError()) != cudaSuccess)
+		return e;
+	record_start(c, "tp_adj_lift_kernel");
+	tp_adj_lift_kernel<D, Q, NV><<<blocks, S::THREADS, convert_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, c->params(), A);
+	record_stop(c);
+	c->launches += 3;
+	return cudaGetLastError();
+}
+
 template <int D, int Q, int NV, int PDE, int FLUX>
 cudaError_t bind(dgpu_ctx* c)
 {
+	c->launch_adjoint = launch_adjoint_t<D, Q, NV, PDE, FLUX>;
 	c->launch_volume = launch_volume_t<D, Q, NV, PDE, true>;
 	c->launch_volume_gl = launch_volume_t<D, Q, NV, PDE, false>;
 	c->launch_face = launch_face_t<D, Q, NV, PDE, FLUX>;
@@ -295,6 +340,10 @@ cudaError_t bind(dgpu_ctx* c)
 	if ((e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRkGl>, smem, (int)lift_smem_bytes<D, Q, NV>())))
 		return e;
 	if ((e = cudaFuncSetAttribute(tp_convert_kernel<D, Q, NV, true>, smem, (int)convert_smem_bytes<D, Q, NV>())))
+		return e;
+	if ((e = cudaFuncSetAttribute(tp_adj_volume_kernel<D, Q, NV, PDE>, smem, (int)adj_volume_smem_bytes<D, Q, NV>())))
+		return e;
+	if ((e = cudaFuncSetAttribute(tp_adj_lift_kernel<D, Q, NV>, smem, (int)convert_smem_bytes<D, Q, NV>())))
 		return e;
 	return cudaFuncSetAttribute(tp_convert_kernel<D, Q, NV, false>, smem, (int)convert_smem_bytes<D, Q, NV>());
 }
@@ -332,7 +381,7 @@ void free_all(dgpu_ctx* c)
 		cudaEventDestroy(t.stop);
 	}
 	c->timers.clear();
-	void* ptrs[] = {c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
+	void* ptrs[] = {c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
 	                c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -540,6 +589,11 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		L = fmax(L, row);
 	}
 	c->ops.pos_err = (float)(2.0 * (d * (q + 1) + 1) * ldexp(1.0, -24) * pow(L, d));
+	for (int a = 0; a < q; ++a)
+		for (int m = 0; m < q; ++m) {
+			c->ops.BT[a][m] = c->ops.B[m][a];
+			c->ops.BinvT[a][m] = c->ops.Binv[m][a];
+		}
 
 	// ---- weights: TP products of the 1D GL rule (first direction fastest) ----
 	std::vector<double> w(N), wf(NF);
@@ -1280,5 +1334,63 @@ extern "C" dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const 
 		memcpy(&v, &bits, sizeof v);
 		*max_rhs = v;
 	}
+	return DGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Discrete adjoint: forward/backward pair shaped like an autograd Function.
+// ---------------------------------------------------------------------------------------------------------------
+namespace {
+
+dgpu_status ensure_adjoint_buffers(dgpu_ctx* c)
+{
+	if (c->u_saved)
+		return DGPU_OK;
+	const size_t ns = state_size(c);
+	const size_t nt = (size_t)c->n_face * 2 * c->nv * c->NF;
+	DGPU_CUDA(c, cudaMalloc((void**)&c->u_saved, ns * sizeof(double)));
+	DGPU_CUDA(c, cudaMalloc((void**)&c->vbar, ns * sizeof(double)));
+	DGPU_CUDA(c, cudaMalloc((void**)&c->ubar, ns * sizeof(double)));
+	DGPU_CUDA(c, cudaMalloc((void**)&c->atraces, nt * sizeof(double)));
+	DGPU_CUDA(c, cudaMalloc((void**)&c->wbar, nt * sizeof(double)));
+	return DGPU_OK;
+}
+
+}  // namespace
+
+extern "C" dgpu_status dgpu_vjp_forward(dgpu_ctx* c, const double* sol, double* rhs, double* max_rhs)
+{
+	if (!c || !sol)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	dgpu_status st = ensure_adjoint_buffers(c);
+	if (st != DGPU_OK)
+		return st;
+	const size_t bytes = state_size(c) * sizeof(double);
+	DGPU_CUDA(c, cudaMemcpyAsync(c->u_saved, sol, bytes, cudaMemcpyHostToDevice, c->stream));
+	DGPU_CUDA(c, cudaMemcpyAsync(c->u, c->u_saved, bytes, cudaMemcpyDeviceToDevice, c->stream));
+	c->coef_valid = true;
+	c->gl_valid = false;
+	st = enqueue_rhs(c);
+	if (st != DGPU_OK)
+		return st;
+	if (rhs)
+		DGPU_CUDA(c, cudaMemcpyAsync(rhs, c->rhs, bytes, cudaMemcpyDeviceToHost, c->stream));
+	if (max_rhs)
+		return read_max(c, max_rhs);
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
+extern "C" dgpu_status dgpu_vjp_backward(dgpu_ctx* c, const double* cotangent, double* grad_sol)
+{
+	if (!c || !cotangent || !grad_sol)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (!c->u_saved)
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "dgpu_vjp_backward needs a preceding dgpu_vjp_forward");
+	const size_t bytes = state_size(c) * sizeof(double);
+	DGPU_CUDA(c, cudaMemcpyAsync(c->vbar, cotangent, bytes, cudaMemcpyHostToDevice, c->stream));
+	DGPU_CUDA(c, c->launch_adjoint(c, c->u_saved, c->vbar, c->ubar));
+	DGPU_CUDA(c, cudaMemcpyAsync(grad_sol, c->ubar, bytes, cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
 	return DGPU_OK;
 }

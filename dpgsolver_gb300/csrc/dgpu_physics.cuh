@@ -10,7 +10,12 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "dgpu_dual.cuh"
+
 namespace dgpu {
+
+using ::fabs;
+using ::sqrt;
 
 constexpr double kGamma = 1.4;          // definitions_physics.h:23
 constexpr double kGm1 = 0.4;            // definitions_physics.h:24
@@ -20,15 +25,17 @@ constexpr double kEps = 1.0e-15;        // definitions_tol.h:23
 enum Pde { kAdvection = 1, kEuler = 3 };
 enum NumFlux { kUpwind = 11, kRoePike = 31, kLaxFriedrichs = 32 };
 
-// min_abs_real_T / max_abs_real_T (general/math_functions_T.c:222-236), real instantiation.
-__device__ __forceinline__ double min_abs_real(double a, double b)
+// min_abs_real_T / max_abs_real_T (general/math_functions_T.c:222-236); T = double, or Dual for Jacobians.
+template <typename T>
+__device__ __forceinline__ T min_abs_real(const T& a, const T& b)
 {
-	double c = (fabs(a) < fabs(b) ? a : b);
+	T c = (fabs(a) < fabs(b) ? a : b);
 	return (c < 0.0 ? -c : c);
 }
-__device__ __forceinline__ double max_abs_real(double a, double b)
+template <typename T>
+__device__ __forceinline__ T max_abs_real(const T& a, const T& b)
 {
-	double c = (fabs(a) > fabs(b) ? a : b);
+	T c = (fabs(a) > fabs(b) ? a : b);
 	return (c < 0.0 ? -c : c);
 }
 
@@ -68,20 +75,20 @@ __device__ __forceinline__ void euler_flux_ref(const double* W, const double* g,
 
 // One side of a face node: the normal physical flux n.f(W) (compute_Flux_euler_0 contracted with n) and the
 // Lax-Friedrichs wave speed |V| + c.
-template <int D>
-__device__ __forceinline__ double euler_normal_flux(const double* W, const double* n, double* Fn)
+template <int D, typename T>
+__device__ __forceinline__ T euler_normal_flux(const T* W, const double* n, T* Fn)
 {
-	const double rho = W[0], E = W[D + 1];
-	const double rho_inv = 1.0 / rho;
-	double V2 = 0.0, Vn = 0.0, mn = 0.0;
+	const T rho = W[0], E = W[D + 1];
+	const T rho_inv = 1.0 / rho;
+	T V2 = 0.0, Vn = 0.0, mn = 0.0;
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
-		const double u = W[1 + k] * rho_inv;
+		const T u = W[1 + k] * rho_inv;
 		V2 += u * u;
 		Vn += n[k] * u;
 		mn += n[k] * W[1 + k];
 	}
-	const double p = kGm1 * (E - 0.5 * rho * V2);
+	const T p = kGm1 * (E - 0.5 * rho * V2);
 	Fn[0] = mn;
 #pragma unroll
 	for (int k = 0; k < D; ++k)
@@ -92,14 +99,13 @@ __device__ __forceinline__ double euler_normal_flux(const double* W, const doubl
 
 // Lax-Friedrichs (compute_Numerical_Flux_T_euler_lax_friedrichs, numerical_flux_euler_T.c:60-327):
 //   nF = 1/2 [ n.(F_L + F_R) + max(|V_L| + c_L, |V_R| + c_R) (W_L - W_R) ].
-template <int D>
-__device__ __forceinline__ void num_flux_lax_friedrichs(const double* WL, const double* WR, const double* n,
-                                                        double* nF)
+template <int D, typename T = double>
+__device__ __forceinline__ void num_flux_lax_friedrichs(const T* WL, const T* WR, const double* n, T* nF)
 {
-	double FL[D + 2], FR[D + 2];
-	const double maxlL = euler_normal_flux<D>(WL, n, FL);
-	const double maxlR = euler_normal_flux<D>(WR, n, FR);
-	const double maxV = (maxlL > maxlR ? maxlL : maxlR);
+	T FL[D + 2], FR[D + 2];
+	const T maxlL = euler_normal_flux<D>(WL, n, FL);
+	const T maxlR = euler_normal_flux<D>(WR, n, FR);
+	const T maxV = (maxlL > maxlR ? maxlL : maxlR);
 #pragma unroll
 	for (int eq = 0; eq < D + 2; ++eq)
 		nF[eq] = 0.5 * ((FL[eq] + FR[eq]) + maxV * (WL[eq] - WR[eq]));
@@ -107,13 +113,13 @@ __device__ __forceinline__ void num_flux_lax_friedrichs(const double* WL, const 
 
 // Roe-Pike with the entropy fix of Qu et al. 2015 (compute_Numerical_Flux_T_euler_roe_pike,
 // numerical_flux_euler_T.c:470-778).
-template <int D>
-__device__ __forceinline__ void num_flux_roe_pike(const double* WL, const double* WR, const double* n, double* nF)
+template <int D, typename T = double>
+__device__ __forceinline__ void num_flux_roe_pike(const T* WL, const T* WR, const double* n, T* nF)
 {
-	const double rhoL = WL[0], rhoR = WR[0], EL = WL[D + 1], ER = WR[D + 1];
-	const double rhoL_inv = 1.0 / rhoL, rhoR_inv = 1.0 / rhoR;
-	double uL[D], uR[D];
-	double V2L = 0.0, V2R = 0.0, VnL = 0.0, VnR = 0.0;
+	const T rhoL = WL[0], rhoR = WR[0], EL = WL[D + 1], ER = WR[D + 1];
+	const T rhoL_inv = 1.0 / rhoL, rhoR_inv = 1.0 / rhoR;
+	T uL[D], uR[D];
+	T V2L = 0.0, V2R = 0.0, VnL = 0.0, VnR = 0.0;
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
 		uL[k] = WL[1 + k] * rhoL_inv;
@@ -123,36 +129,36 @@ __device__ __forceinline__ void num_flux_roe_pike(const double* WL, const double
 		VnL += n[k] * uL[k];
 		VnR += n[k] * uR[k];
 	}
-	const double pL = kGm1 * (EL - 0.5 * rhoL * V2L), HL = (EL + pL) * rhoL_inv;
-	const double pR = kGm1 * (ER - 0.5 * rhoR * V2R), HR = (ER + pR) * rhoR_inv;
+	const T pL = kGm1 * (EL - 0.5 * rhoL * V2L), HL = (EL + pL) * rhoL_inv;
+	const T pR = kGm1 * (ER - 0.5 * rhoR * V2R), HR = (ER + pR) * rhoR_inv;
 
 	// Roe averages (divisions by r + 1 through one reciprocal)
-	const double r = sqrt(rhoR * rhoL_inv), rP1_inv = 1.0 / (r + 1.0), rho = r * rhoL;
-	double u[D];
-	double Vn = 0.0, V2 = 0.0;
+	const T r = sqrt(rhoR * rhoL_inv), rP1_inv = 1.0 / (r + 1.0), rho = r * rhoL;
+	T u[D];
+	T Vn = 0.0, V2 = 0.0;
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
 		u[k] = (r * uR[k] + uL[k]) * rP1_inv;
 		Vn += n[k] * u[k];
 		V2 += u[k] * u[k];
 	}
-	const double H = (r * HR + HL) * rP1_inv, c2 = kGm1 * (H - 0.5 * V2), c = sqrt(c2), c_inv = 1.0 / c;
+	const T H = (r * HR + HL) * rP1_inv, c2 = kGm1 * (H - 0.5 * V2), c = sqrt(c2), c_inv = 1.0 / c;
 
-	const double l1 = min_abs_real(VnL - c, Vn - c), l5 = max_abs_real(VnR + c, Vn + c);
-	const double l234 = (Vn > 0.0 ? Vn : -Vn);
+	const T l1 = min_abs_real(VnL - c, Vn - c), l5 = max_abs_real(VnR + c, Vn + c);
+	const T l234 = (Vn > 0.0 ? Vn : -Vn);
 
-	const double drho = rhoR - rhoL, dE = ER - EL, dp = pR - pL, dVn = VnR - VnL;
-	const double lc1 = 0.5 * (l5 + l1) - l234, lc2 = 0.5 * (l5 - l1);
-	const double disInter1 = (lc1 * dp * c_inv + lc2 * rho * dVn) * c_inv;
-	const double disInter2 = lc1 * rho * dVn + lc2 * dp * c_inv;
+	const T drho = rhoR - rhoL, dE = ER - EL, dp = pR - pL, dVn = VnR - VnL;
+	const T lc1 = 0.5 * (l5 + l1) - l234, lc2 = 0.5 * (l5 - l1);
+	const T disInter1 = (lc1 * dp * c_inv + lc2 * rho * dVn) * c_inv;
+	const T disInter2 = lc1 * rho * dVn + lc2 * dp * c_inv;
 
-	const double rhoVnL = rhoL * VnL, rhoVnR = rhoR * VnR, pLR = pL + pR;
+	const T rhoVnL = rhoL * VnL, rhoVnR = rhoR * VnR, pLR = pL + pR;
 	nF[0] = 0.5 * ((rhoVnL + rhoVnR) - (l234 * drho + disInter1));
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
-		const double drhou = WR[1 + k] - WL[1 + k];
-		const double nFk = rhoVnL * uL[k] + rhoVnR * uR[k] + n[k] * pLR;
-		const double disk = l234 * drhou + disInter1 * u[k] + disInter2 * n[k];
+		const T drhou = WR[1 + k] - WL[1 + k];
+		const T nFk = rhoVnL * uL[k] + rhoVnR * uR[k] + n[k] * pLR;
+		const T disk = l234 * drhou + disInter1 * u[k] + disInter2 * n[k];
 		nF[1 + k] = 0.5 * (nFk - disk);
 	}
 	nF[D + 1] = 0.5 * ((VnL * (EL + pL) + VnR * (ER + pR)) - (l234 * dE + disInter1 * H + disInter2 * Vn));

@@ -40,6 +40,8 @@ struct TPOps {
 	double BS[kQMax][kQMax];    // ccBS0 1D (Bezier -> Lagrange)
 	double SBg[kQMax][kQMax];   // ccSB0 B^-1: GL nodal values -> Bezier coefficients
 	double BSg[kQMax][kQMax];   // B ccBS0:   Bezier coefficients -> GL nodal values
+	double BT[kQMax][kQMax];    // B^T    (adjoint: V^T)
+	double BinvT[kQMax][kQMax]; // Binv^T (adjoint: V^-T)
 	float SBf[kQMax][kQMax];    // SBg rounded to FP32 (positivity pre-filter)
 	float pos_err;              // |FP32 Bezier coefficient - exact| <= pos_err * max_i |x_i| (per variable)
 };

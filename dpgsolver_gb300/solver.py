@@ -133,6 +133,24 @@ class Simulation:
               self._h)
         return mx.value if want_max else None
 
+    # -- discrete adjoint (autograd-Function-shaped pair) ------------------------------------------------------
+    def vjp_forward(self, sol):
+        """R(sol) (compute_rhs_dg on host buffers); keeps sol for vjp_backward. Returns (rhs, max_rhs)."""
+        s = np.ascontiguousarray(sol, dtype=np.float64)
+        r = np.empty(self.shape)
+        mx = ctypes.c_double()
+        check(self._lib.dgpu_vjp_forward(self._h, _dp(s), _dp(r), ctypes.byref(mx)), self._h)
+        return r, mx.value
+
+    def vjp_backward(self, cotangent):
+        """(dR/dsol)^T cotangent at the state kept by vjp_forward."""
+        v = np.ascontiguousarray(cotangent, dtype=np.float64)
+        if v.shape != self.shape:
+            raise ValueError(f"cotangent shape {v.shape} != {self.shape}")
+        g = np.empty(self.shape)
+        check(self._lib.dgpu_vjp_backward(self._h, _dp(v), _dp(g)), self._h)
+        return g
+
     def synchronize(self):
         check(self._lib.dgpu_synchronize(self._h), self._h)
 

@@ -133,6 +133,16 @@ dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const dgpu_tp_ope
                                      const dgpu_mesh* d_mesh, const double* d_sol, double* d_rhs,
                                      double* max_rhs, void* cuda_stream);
 
+/* Discrete adjoint of the residual, as a forward/backward pair shaped like an autograd Function.
+ * dgpu_vjp_forward computes R(sol) exactly as dgpu_compute_rhs_host does and keeps sol on the device;
+ * dgpu_vjp_backward returns grad = (dR/dsol)^T cotangent at that state (host buffers, state layout). The reference
+ * has no adjoint: it linearises the same residual by complex step (compute_lhs_cmplx_step_dg,
+ * src/testing/support/simulation/solvers/dg/test_support_solve_dg.c:83-110) and assembles its Jacobian for the
+ * implicit solver (compute_rlhs_dg, src/simulation/solvers/dg/solve_dg.c:138-145); grad is that Jacobian's
+ * transpose applied to the cotangent. Kinks of the fluxes take the derivative of the branch the value takes. */
+dgpu_status dgpu_vjp_forward(dgpu_ctx* ctx, const double* sol, double* rhs, double* max_rhs);
+dgpu_status dgpu_vjp_backward(dgpu_ctx* ctx, const double* cotangent, double* grad_sol);
+
 /* Number of positivity corrections applied since creation (enforce_positivity_highorder's correct_coef). */
 dgpu_status dgpu_positivity_corrections(dgpu_ctx* ctx, long long* n);
 /* Kernels this context has launched (graph replays count each kernel node). */
