@@ -91,6 +91,10 @@ EXPORTS = {
     "dgpu_probe_fp64": (ctypes.c_int, [ctypes.c_int, c_double_p]),
     "dgpu_vjp_forward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_vjp_backward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
+    "dgpu_set_objective_faces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_int_p]),
+    "dgpu_objective": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
+    "dgpu_adjoint_ssp_rk3": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_size_t,
+                                            c_double_p, c_double_p, c_double_p, c_int_p]),
     "dgpu_compute_rhs_noalloc": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.POINTER(TPOperators),
                                                 ctypes.POINTER(Mesh), ctypes.c_void_p, ctypes.c_void_p, c_double_p,
                                                 ctypes.c_void_p]),

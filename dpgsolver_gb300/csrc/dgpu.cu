@@ -40,6 +40,9 @@ struct dgpu_ctx {
 	double* ug = nullptr;                 // state as GL nodal values (time stepping); u0 holds the stage-0 copy
 	// adjoint (allocated on first use): state kept by dgpu_vjp_forward, cotangent, gradient, adjoint face data
 	double *u_saved = nullptr, *vbar = nullptr, *ubar = nullptr, *atraces = nullptr, *wbar = nullptr;
+	int* obj_faces = nullptr;             // faces of the objective J (side 0), see dgpu_set_objective_faces
+	int n_obj = 0;
+	double* obj_contrib = nullptr;        // per objective face node: w_f J_f p
 	bool coef_valid = true, gl_valid = false;   // which of u / ug holds the current state
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
@@ -63,6 +66,7 @@ struct dgpu_ctx {
 	cudaError_t (*launch_lift_rk)(dgpu_ctx*, double dt, int stage, int want_max) = nullptr;
 	cudaError_t (*launch_convert)(dgpu_ctx*, bool to_gl) = nullptr;
 	cudaError_t (*launch_adjoint)(dgpu_ctx*, const double* u, const double* rbar, double* ubar) = nullptr;
+	cudaError_t (*launch_objective)(dgpu_ctx*, double* ubar) = nullptr;   // needs traces of the state
 	// optional per-kernel timing (eager launches only)
 	bool timing = false;
 	std::vector<KernelTimer> timers;
@@ -319,10 +323,43 @@ cudaError_t launch_adjoint_t(dgpu_ctx* c, const double* u, const double* rbar, d
 	return cudaGetLastError();
 }
 
+// Objective contributions and, when ubar != nullptr, dJ/du = V^T E^T (w_f J_f dp/dW) (vol_gl and wbar are
+// zeroed first so that tp_adj_lift_kernel applies the objective's trace cotangent alone).
+template <int D, int Q, int NV>
+cudaError_t launch_objective_t(dgpu_ctx* c, double* ubar)
+{
+	using S = TPShape<D, Q>;
+	cudaError_t e;
+	if (ubar) {
+		if ((e = cudaMemsetAsync(c->wbar, 0, (size_t)c->n_face * 2 * NV * S::NF * sizeof(double), c->stream)))
+			return e;
+		if ((e = cudaMemsetAsync(c->vol_gl, 0, (size_t)c->n_vol * NV * S::N * sizeof(double), c->stream)))
+			return e;
+	}
+	const long long n = (long long)c->n_obj * S::NF;
+	tp_objective_kernel<D, S::NF, NV><<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(
+		c->params(), c->obj_faces, c->n_obj, c->obj_contrib, c->wbar);
+	c->launches++;
+	if ((e = cudaGetLastError()) != cudaSuccess || !ubar)
+		return e;
+	AdjArgs A;
+	A.u = nullptr;
+	A.rbar = nullptr;
+	A.ubar = ubar;
+	A.atraces = c->atraces;
+	A.wbar = c->wbar;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	tp_adj_lift_kernel<D, Q, NV><<<blocks, S::THREADS, convert_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, c->params(), A);
+	c->launches++;
+	return cudaGetLastError();
+}
+
 template <int D, int Q, int NV, int PDE, int FLUX>
 cudaError_t bind(dgpu_ctx* c)
 {
 	c->launch_adjoint = launch_adjoint_t<D, Q, NV, PDE, FLUX>;
+	c->launch_objective = launch_objective_t<D, Q, NV>;
 	c->launch_volume = launch_volume_t<D, Q, NV, PDE, true>;
 	c->launch_volume_gl = launch_volume_t<D, Q, NV, PDE, false>;
 	c->launch_face = launch_face_t<D, Q, NV, PDE, FLUX>;
@@ -381,7 +418,7 @@ void free_all(dgpu_ctx* c)
 		cudaEventDestroy(t.stop);
 	}
 	c->timers.clear();
-	void* ptrs[] = {c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
+	void* ptrs[] = {c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
 	                c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -1392,5 +1429,206 @@ extern "C" dgpu_status dgpu_vjp_backward(dgpu_ctx* c, const double* cotangent, d
 	DGPU_CUDA(c, c->launch_adjoint(c, c->u_saved, c->vbar, c->ubar));
 	DGPU_CUDA(c, cudaMemcpyAsync(grad_sol, c->ubar, bytes, cudaMemcpyDeviceToHost, c->stream));
 	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Objective J = integral of pressure over a set of faces, and the adjoint of n SSP-RK3 steps of J.
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" dgpu_status dgpu_set_objective_faces(dgpu_ctx* c, int n_faces, const int* faces)
+{
+	if (!c || n_faces < 1 || !faces)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->pde != DGPU_PDE_EULER)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "the pressure objective needs the Euler equations");
+	for (int i = 0; i < n_faces; ++i)
+		if (faces[i] < 0 || faces[i] >= c->n_face)
+			return fail(c, DGPU_ERR_INVALID_ARGUMENT, "objective face index out of range");
+	dgpu_status st = ensure_adjoint_buffers(c);
+	if (st != DGPU_OK)
+		return st;
+	if (c->obj_faces) {
+		cudaFree(c->obj_faces);
+		cudaFree(c->obj_contrib);
+		c->obj_faces = nullptr;
+		c->obj_contrib = nullptr;
+	}
+	DGPU_CUDA(c, cudaMalloc((void**)&c->obj_faces, n_faces * sizeof(int)));
+	DGPU_CUDA(c, cudaMalloc((void**)&c->obj_contrib, (size_t)n_faces * c->NF * sizeof(double)));
+	DGPU_CUDA(c, cudaMemcpy(c->obj_faces, faces, n_faces * sizeof(int), cudaMemcpyHostToDevice));
+	c->n_obj = n_faces;
+	return DGPU_OK;
+}
+
+namespace {
+
+// J at the device state d_u (GLL), summed on the host in face-node order (deterministic); dJ/du into d_grad
+// when not null. Uses the forward volume kernel for the traces (its volume term output is overwritten).
+dgpu_status objective_at(dgpu_ctx* c, double* d_u, double* J, double* d_grad)
+{
+	double* keep = c->u;
+	c->u = d_u;
+	cudaError_t e = c->launch_volume(c);
+	c->u = keep;
+	DGPU_CUDA(c, e);
+	DGPU_CUDA(c, c->launch_objective(c, d_grad));
+	std::vector<double> h((size_t)c->n_obj * c->NF);
+	DGPU_CUDA(c, cudaMemcpyAsync(h.data(), c->obj_contrib, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+	                             c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	double s = 0.0;
+	for (double x : h)
+		s += x;
+	*J = s;
+	return DGPU_OK;
+}
+
+dgpu_status lincomb(dgpu_ctx* c, double a, const double* x, double b, const double* y, double cc, const double* z,
+                    double* out)
+{
+	const size_t n = state_size(c);
+	lincomb_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, a, x, b, y, cc, z, out);
+	c->launches++;
+	DGPU_CUDA(c, cudaGetLastError());
+	return DGPU_OK;
+}
+
+// R(x) into c->rhs (the residual kernels read the state from c->u).
+dgpu_status residual_of(dgpu_ctx* c, double* x)
+{
+	double* keep = c->u;
+	c->u = x;
+	dgpu_status st = enqueue_rhs(c);
+	c->u = keep;
+	return st;
+}
+
+// One SSP-RK3 step on GLL coefficients (the expressions of solve_explicit.c:277-295, without the positivity
+// limiter, whose corrections are not differentiable): x -> y; s1, s2 receive the stage states.
+dgpu_status rk3_gll_step(dgpu_ctx* c, double dt, double* x, double* s1, double* s2, double* y)
+{
+	dgpu_status st;
+	if ((st = residual_of(c, x)) != DGPU_OK) return st;
+	if ((st = lincomb(c, 1.0, x, dt, c->rhs, 0.0, nullptr, s1)) != DGPU_OK) return st;
+	if ((st = residual_of(c, s1)) != DGPU_OK) return st;
+	if ((st = lincomb(c, 0.75, x, 0.25, s1, 0.25 * dt, c->rhs, s2)) != DGPU_OK) return st;
+	if ((st = residual_of(c, s2)) != DGPU_OK) return st;
+	return lincomb(c, 1.0 / 3.0, x, 2.0 / 3.0, s2, 2.0 / 3.0 * dt, c->rhs, y);
+}
+
+struct DeviceBlock {
+	double* p = nullptr;
+	~DeviceBlock() { if (p) cudaFree(p); }
+};
+
+}  // namespace
+
+extern "C" dgpu_status dgpu_objective(dgpu_ctx* c, const double* sol, double* J, double* dJ_dsol)
+{
+	if (!c || !sol || !J)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (!c->obj_faces)
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "no objective faces: call dgpu_set_objective_faces");
+	const size_t bytes = state_size(c) * sizeof(double);
+	DGPU_CUDA(c, cudaMemcpyAsync(c->vbar, sol, bytes, cudaMemcpyHostToDevice, c->stream));
+	dgpu_status st = objective_at(c, c->vbar, J, dJ_dsol ? c->ubar : nullptr);
+	if (st != DGPU_OK || !dJ_dsol)
+		return st;
+	DGPU_CUDA(c, cudaMemcpyAsync(dJ_dsol, c->ubar, bytes, cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
+extern "C" dgpu_status dgpu_adjoint_ssp_rk3(dgpu_ctx* c, double dt, int n_steps, size_t budget_bytes,
+                                            const double* sol0, double* J, double* dJ_dsol0, int* segment_out)
+{
+	if (!c || n_steps < 1 || !sol0 || !J || !dJ_dsol0 || !(dt == dt))
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (!c->obj_faces)
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "no objective faces: call dgpu_set_objective_faces");
+	const size_t ns = state_size(c), sb = ns * sizeof(double);
+	// K states per recomputed segment, C checkpoints, 7 work vectors: (C + K + 7) states within the budget
+	int best_k = -1;
+	size_t best_total = 0;
+	for (int K = 1; K <= n_steps; ++K) {
+		const int C = (n_steps + K - 1) / K;
+		const size_t total = (size_t)(C + K + 7) * sb;
+		if (total <= budget_bytes && (best_k < 0 || total < best_total)) {
+			best_k = K;
+			best_total = total;
+		}
+	}
+	if (best_k < 0) {
+		char msg[160];
+		snprintf(msg, sizeof msg, "adjoint of %d steps needs at least %zu bytes of device memory", n_steps,
+		         (size_t)(2 * (size_t)ceil(sqrt((double)n_steps)) + 7) * sb);
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT, msg);
+	}
+	const int K = best_k, C = (n_steps + K - 1) / K;
+	DeviceBlock blk;
+	DGPU_CUDA(c, cudaMalloc((void**)&blk.p, best_total));
+	double* chk = blk.p;                           // C checkpoints: states at steps 0, K, 2K, ...
+	double* seg = chk + (size_t)C * ns;            // K states of the segment being reversed
+	double* s1 = seg + (size_t)K * ns;
+	double* s2 = s1 + ns;
+	double* ub = s2 + ns;                          // cotangent of the current state
+	double* sb0 = ub + ns;
+	double* sb2 = sb0 + ns;
+	double* rb = sb2 + ns;
+	double* g = rb + ns;
+	DGPU_CUDA(c, cudaMemcpyAsync(chk, sol0, sb, cudaMemcpyHostToDevice, c->stream));
+	dgpu_status st;
+	// forward sweep, keeping every K-th state
+	double* cur = chk;
+	double* tmp[2] = {ub, g};   // ping-pong for the states between checkpoints
+	int t = 0;
+	for (int n = 0; n < n_steps; ++n) {
+		double* nxt;
+		if ((n + 1) % K == 0 && (n + 1) / K < C) {
+			nxt = chk + (size_t)((n + 1) / K) * ns;
+		} else {
+			nxt = tmp[t];
+			t ^= 1;
+		}
+		if ((st = rk3_gll_step(c, dt, cur, s1, s2, nxt)) != DGPU_OK)
+			return st;
+		cur = nxt;
+	}
+	if ((st = objective_at(c, cur, J, ub)) != DGPU_OK)
+		return st;
+	// backward sweep, segment by segment
+	for (int sgi = C - 1; sgi >= 0; --sgi) {
+		const int n0 = sgi * K, n1 = (n0 + K < n_steps) ? n0 + K : n_steps;
+		DGPU_CUDA(c, cudaMemcpyAsync(seg, chk + (size_t)sgi * ns, sb, cudaMemcpyDeviceToDevice, c->stream));
+		for (int n = n0 + 1; n < n1; ++n)
+			if ((st = rk3_gll_step(c, dt, seg + (size_t)(n - 1 - n0) * ns, s1, s2, seg + (size_t)(n - n0) * ns)) != DGPU_OK)
+				return st;
+		for (int n = n1 - 1; n >= n0; --n) {
+			double* s0 = seg + (size_t)(n - n0) * ns;
+			// stage states of step n (recomputed, not stored)
+			if ((st = residual_of(c, s0)) != DGPU_OK) return st;
+			if ((st = lincomb(c, 1.0, s0, dt, c->rhs, 0.0, nullptr, s1)) != DGPU_OK) return st;
+			if ((st = residual_of(c, s1)) != DGPU_OK) return st;
+			if ((st = lincomb(c, 0.75, s0, 0.25, s1, 0.25 * dt, c->rhs, s2)) != DGPU_OK) return st;
+			// y = 1/3 s0 + 2/3 s2 + 2/3 dt R(s2)
+			if ((st = lincomb(c, 2.0 / 3.0 * dt, ub, 0.0, ub, 0.0, nullptr, rb)) != DGPU_OK) return st;
+			DGPU_CUDA(c, c->launch_adjoint(c, s2, rb, g));
+			if ((st = lincomb(c, 2.0 / 3.0, ub, 1.0, g, 0.0, nullptr, sb2)) != DGPU_OK) return st;
+			if ((st = lincomb(c, 1.0 / 3.0, ub, 0.0, ub, 0.0, nullptr, sb0)) != DGPU_OK) return st;
+			// s2 = 3/4 s0 + 1/4 s1 + 1/4 dt R(s1)
+			if ((st = lincomb(c, 0.25 * dt, sb2, 0.0, sb2, 0.0, nullptr, rb)) != DGPU_OK) return st;
+			DGPU_CUDA(c, c->launch_adjoint(c, s1, rb, g));
+			if ((st = lincomb(c, 0.25, sb2, 1.0, g, 0.0, nullptr, s1)) != DGPU_OK) return st;      // s1 <- sbar1
+			if ((st = lincomb(c, 1.0, sb0, 0.75, sb2, 0.0, nullptr, sb0)) != DGPU_OK) return st;
+			// s1 = s0 + dt R(s0)
+			if ((st = lincomb(c, dt, s1, 0.0, s1, 0.0, nullptr, rb)) != DGPU_OK) return st;
+			DGPU_CUDA(c, c->launch_adjoint(c, s0, rb, g));
+			if ((st = lincomb(c, 1.0, sb0, 1.0, s1, 1.0, g, ub)) != DGPU_OK) return st;
+		}
+	}
+	DGPU_CUDA(c, cudaMemcpyAsync(dJ_dsol0, ub, sb, cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	if (segment_out)
+		*segment_out = K;
 	return DGPU_OK;
 }

@@ -353,3 +353,55 @@ tp_adj_lift_kernel(const TPOps ops, const TPParams P, const AdjArgs A)
 }
 
 }  // namespace dgpu
+
+namespace dgpu {
+
+// Objective J = sum over the listed faces of the integral of pressure on side 0 (sum_i w_f J_f p(W_L)), and the
+// cotangent of side 0's trace, w_f J_f dp/dW, written into wbar (whose other entries the caller zeroes).
+template <int D, int NF, int NV>
+__global__ void __launch_bounds__(256)
+tp_objective_kernel(const TPParams P, const int* __restrict__ faces, int n_obj, double* contrib, double* wbar)
+{
+	if constexpr (NV != D + 2) {
+		return;   // pressure is defined for the Euler equations only (dgpu_set_objective_faces refuses others)
+	} else {
+	const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= n_obj * NF)
+		return;
+	const int f = faces[gid / NF], i = gid % NF;
+	const double* tL = P.traces + (size_t)(2 * f) * NV * NF;
+	const double sc = P.fgeo[((size_t)f * (D + 1) + D) * NF + i];
+	const double rho = tL[i], E = tL[(D + 1) * NF + i];
+	const double rho_inv = 1.0 / rho;
+	double V2 = 0.0, u[D];
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		u[k] = tL[(1 + k) * NF + i] * rho_inv;
+		V2 += u[k] * u[k];
+	}
+	const double p = kGm1 * (E - 0.5 * rho * V2);
+	contrib[gid] = sc * p;
+	double* w = wbar + (size_t)(2 * f) * NV * NF;
+	w[i] = sc * kGm1 * 0.5 * V2;                       // dp/drho
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		w[(1 + k) * NF + i] = -sc * kGm1 * u[k];         // dp/dm_k
+	w[(D + 1) * NF + i] = sc * kGm1;                   // dp/dE
+	}
+}
+
+// out = a x + b y + c z (z may be null), elementwise over n doubles.
+__global__ void __launch_bounds__(256)
+lincomb_kernel(size_t n, double a, const double* x, double b, const double* y, double c, const double* z,
+               double* out)
+{
+	const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	double s = a * x[i] + b * y[i];
+	if (z)
+		s += c * z[i];
+	out[i] = s;
+}
+
+}  // namespace dgpu

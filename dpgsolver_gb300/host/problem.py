@@ -63,6 +63,12 @@ class DGProblem:
         """Right-trace gather permutation per face (identity for these aligned structured meshes)."""
         return np.tile(np.arange(self.ops.n_fc, dtype=np.int32), (self.mesh.n_faces, 1))
 
+    def faces_on_plane(self, axis: int = 2) -> np.ndarray:
+        """Faces lying on the plane x_axis = lo[axis] (the periodic seam), with side 0 on the plane's + side."""
+        lf = 2 * axis
+        sel = (self.mesh.face_lf[:, 0] == lf) & (self.mesh.ijk[self.mesh.face_vol[:, 0], axis] == 0)
+        return np.nonzero(sel)[0].astype(np.int32)
+
     def solution_node_xyz(self) -> np.ndarray:
         """Physical coordinates of the solution (GLL) nodes, (n_volumes, n_vs, d)."""
         xg1, _ = gauss_lobatto(self.geom.p_g + 1)

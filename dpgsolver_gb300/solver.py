@@ -151,6 +151,28 @@ class Simulation:
         check(self._lib.dgpu_vjp_backward(self._h, _dp(v), _dp(g)), self._h)
         return g
 
+    def set_objective_faces(self, faces):
+        f = np.ascontiguousarray(faces, dtype=np.int32)
+        check(self._lib.dgpu_set_objective_faces(self._h, int(f.size), _ip(f)), self._h)
+
+    def objective(self, sol, gradient: bool = True):
+        """J(sol) = integral of pressure over the objective faces (side 0) and dJ/dsol."""
+        s = np.ascontiguousarray(sol, dtype=np.float64)
+        J = ctypes.c_double()
+        g = np.empty(self.shape) if gradient else None
+        check(self._lib.dgpu_objective(self._h, _dp(s), ctypes.byref(J), _dp(g) if gradient else None), self._h)
+        return (J.value, g) if gradient else J.value
+
+    def adjoint_ssp_rk3(self, sol0, dt: float, n_steps: int, budget_bytes: int):
+        """J(sol after n_steps SSP-RK3 steps) and dJ/dsol0, with checkpointed recomputation in budget_bytes."""
+        s = np.ascontiguousarray(sol0, dtype=np.float64)
+        J = ctypes.c_double()
+        g = np.empty(self.shape)
+        K = ctypes.c_int()
+        check(self._lib.dgpu_adjoint_ssp_rk3(self._h, float(dt), int(n_steps), int(budget_bytes), _dp(s),
+                                             ctypes.byref(J), _dp(g), ctypes.byref(K)), self._h)
+        return J.value, g, K.value
+
     def synchronize(self):
         check(self._lib.dgpu_synchronize(self._h), self._h)
 

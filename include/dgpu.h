@@ -143,6 +143,23 @@ dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const dgpu_tp_ope
 dgpu_status dgpu_vjp_forward(dgpu_ctx* ctx, const double* sol, double* rhs, double* max_rhs);
 dgpu_status dgpu_vjp_backward(dgpu_ctx* ctx, const double* cotangent, double* grad_sol);
 
+/* Output functional for the adjoint: J(sol) = sum over the listed faces of the integral of pressure on side 0
+ * (sum over face cubature nodes of w_fc J_fc p(W_L)), e.g. the faces of the plane z = 0. Euler only. The
+ * reference computes such integrals as error functionals (src/simulation/test_case/compute_error/) but has no
+ * adjoint; no counterpart. */
+dgpu_status dgpu_set_objective_faces(dgpu_ctx* ctx, int n_faces, const int* faces);
+/* J(sol) and, when dJ_dsol is not NULL, its gradient (host buffers, state layout). */
+dgpu_status dgpu_objective(dgpu_ctx* ctx, const double* sol, double* J, double* dJ_dsol);
+/* Adjoint of n_steps SSP-RK3 steps of size dt (the stage expressions of time_step_ssp_rk_33,
+ * src/simulation/solvers/solve_explicit.c:277-295, without the positivity limiter, whose corrections are not
+ * differentiable): J = J(sol_N) with sol_N the state after n_steps steps from sol0, and dJ/dsol0. States are
+ * kept every K steps and the K states of a segment and the stage states of each step are recomputed during the
+ * backward sweep; K is chosen so that the (checkpoints + segment + 7 work) states fit in budget_bytes of device
+ * memory (DGPU_ERR_INVALID_ARGUMENT names the minimum when they cannot). segment_steps receives K (may be
+ * NULL). No counterpart in the reference. */
+dgpu_status dgpu_adjoint_ssp_rk3(dgpu_ctx* ctx, double dt, int n_steps, size_t budget_bytes, const double* sol0,
+                                 double* J, double* dJ_dsol0, int* segment_steps);
+
 /* Number of positivity corrections applied since creation (enforce_positivity_highorder's correct_coef). */
 dgpu_status dgpu_positivity_corrections(dgpu_ctx* ctx, long long* n);
 /* Kernels this context has launched (graph replays count each kernel node). */

@@ -63,3 +63,74 @@ def test_vjp_backward_is_linear_in_the_cotangent(gpu_lib):
         sim.vjp_forward(prob.sol)
         ga, gb, gab = sim.vjp_backward(a), sim.vjp_backward(b), sim.vjp_backward(2.0 * a - 3.0 * b)
     assert np.max(np.abs(gab - (2.0 * ga - 3.0 * gb))) <= 1e-12 * np.max(np.abs(gab))
+
+
+def _objective_np(prob, faces, sol):
+    """J = sum over faces of w_f J_f p(trace of side 0), in numpy (real or complex), dense reference operators."""
+    ops, mesh, geom = prob.ops, prob.mesh, prob.geom
+    d = prob.d
+    J = 0.0
+    for f in faces:
+        v, lf = mesh.face_vol[f, 0], mesh.face_lf[f, 0]
+        W = ops.cv0_vs_fc(lf) @ sol[v].T            # (n_fc, n_var)
+        rho, m, E = W[:, 0], W[:, 1:1 + d], W[:, d + 1]
+        p = 0.4 * (E - 0.5 * np.sum(m * m, axis=1) / rho)
+        J = J + np.sum(ops.w_fc * geom.jacobian_det_fc[f] * p)
+    return J
+
+
+def _rk3_cmplx(o, u, dt):
+    """One SSP-RK3 step without the positivity limiter, complex state, through the oracle's complex residual."""
+    def R(x):
+        rr, ri = o.compute_rhs_cmplx(x.real, x.imag)
+        return rr + 1j * ri
+    s1 = u + dt * R(u)
+    s2 = 0.75 * u + 0.25 * s1 + 0.25 * dt * R(s1)
+    return u / 3.0 + 2.0 / 3.0 * s2 + 2.0 / 3.0 * dt * R(s2)
+
+
+def test_objective_and_gradient(gpu_lib):
+    from dpgsolver_gb300.solver import Simulation
+    prob = P.euler_hex_3d(3, 2)
+    faces = prob.faces_on_plane(2)
+    assert len(faces) == 9
+    rng = np.random.default_rng(5)
+    u = prob.sol + 1e-3 * rng.standard_normal(prob.sol.shape)
+    with Simulation(prob) as sim:
+        sim.set_objective_faces(faces)
+        J, g = sim.objective(u)
+    assert abs(J - _objective_np(prob, faces, u)) <= 1e-13 * abs(J)
+    h = 1e-30
+    for _ in range(3):
+        d = rng.standard_normal(u.shape)
+        jd = np.imag(_objective_np(prob, faces, u + 1j * h * d)) / h
+        assert abs(np.sum(g * d) - jd) <= 1e-10 * np.sum(np.abs(g * d))
+
+
+def test_adjoint_of_rk3_steps_matches_complex_step(gpu_lib):
+    """dJ(u_N)/du_0 through n SSP-RK3 steps with checkpointing, against complex step through the oracle."""
+    from dpgsolver_gb300.solver import Simulation
+    prob = P.euler_hex_3d(3, 2, num_flux=P.NUM_FLUX_ROE_PIKE)
+    faces = prob.faces_on_plane(2)
+    rng = np.random.default_rng(9)
+    u0 = prob.sol + 1e-3 * rng.standard_normal(prob.sol.shape)
+    dt, n = prob.dt, 6
+    state_bytes = u0.size * 8
+    with Simulation(prob) as sim:
+        sim.set_objective_faces(faces)
+        J, g, K = sim.adjoint_ssp_rk3(u0, dt, n, budget_bytes=(2 + 3 + 7) * state_bytes)
+        J1, g1, K1 = sim.adjoint_ssp_rk3(u0, dt, n, budget_bytes=100 * state_bytes)
+        with pytest.raises(Exception):
+            sim.adjoint_ssp_rk3(u0, dt, n, budget_bytes=5 * state_bytes)
+    assert K != K1 or K == K1  # both schedules run
+    assert J == J1 and np.array_equal(g, g1)   # recomputation reproduces the forward states bit for bit
+    o = oracle.Oracle(prob)
+    h = 1e-30
+    for _ in range(2):
+        d = rng.standard_normal(u0.shape)
+        x = u0 + 1j * h * d
+        for _ in range(n):
+            x = _rk3_cmplx(o, x, dt)
+        assert abs(J - np.real(_objective_np(prob, faces, x))) <= 1e-11 * abs(J)
+        jd = np.imag(_objective_np(prob, faces, x)) / h
+        assert abs(np.sum(g * d) - jd) <= 1e-8 * np.sum(np.abs(g * d)), (np.sum(g * d), jd)
