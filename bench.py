@@ -349,10 +349,38 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "setup_s": setup_s,
     }
+    if not args.no_adjoint and prob.pde == 3:
+        res["adjoint"] = adjoint_measurements(torch, sim, prob, args)
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, workers=1)
     sim.close()
     return res
+
+
+def adjoint_measurements(torch, sim, prob, args):
+    """The discrete adjoint on the bench mesh: one VJP of R through the host-buffer forward/backward pair, and
+    the checkpointed adjoint of SSP-RK3 steps of J = integral of pressure over the z = 0 faces."""
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal(prob.sol.shape)
+    sim.vjp_forward(prob.sol)
+    sim.vjp_backward(v)
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sim.vjp_backward(v)
+    vjp_s = (time.perf_counter() - t0) / reps
+    sim.set_objective_faces(prob.faces_on_plane(2))
+    n_adj = args.adjoint_steps
+    budget = int(args.adjoint_budget_gb * 2**30)
+    t0 = time.perf_counter()
+    J, g, K = sim.adjoint_ssp_rk3(prob.sol, prob.dt, n_adj, budget)
+    adj_s = time.perf_counter() - t0
+    return {"vjp_backward_s": vjp_s,
+            "vjp_dof_per_s": prob.n_state / vjp_s,
+            "vjp_note": "host cotangent in, host gradient out (84 MB each way included)",
+            "rk3_adjoint_steps": n_adj, "rk3_adjoint_s": adj_s, "segment_steps": K,
+            "budget_bytes": budget, "J": J, "grad_norm": float(np.linalg.norm(g)),
+            "note": "forward sweep with checkpoints, segment recomputation, stage recomputation, 3 VJPs per step"}
 
 
 def _oracle_worker(args):
@@ -439,6 +467,9 @@ def main():
     ap.add_argument("--only-residual", action="store_true",
                     help="time compute_rhs_dg only (device-resident; profiling)")
     ap.add_argument("--only-rk", action="store_true", help="time graph-replayed SSP-RK3 steps only (profiling)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurements")
+    ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--adjoint-budget-gb", type=float, default=4.0)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -134,3 +134,24 @@ def test_adjoint_of_rk3_steps_matches_complex_step(gpu_lib):
         assert abs(J - np.real(_objective_np(prob, faces, x))) <= 1e-11 * abs(J)
         jd = np.imag(_objective_np(prob, faces, x)) / h
         assert abs(np.sum(g * d) - jd) <= 1e-8 * np.sum(np.abs(g * d)), (np.sum(g * d), jd)
+
+
+def test_vjp_on_1000_seeded_directions(gpu_lib):
+    """The residual VJP against complex step on 1000 seeded directions (small curved HEX mesh, Roe-Pike)."""
+    from dpgsolver_gb300.solver import Simulation
+    prob = P.euler_hex_3d(2, 1, num_flux=P.NUM_FLUX_ROE_PIKE)
+    rng = np.random.default_rng(1000)
+    u = prob.sol + 1e-2 * rng.standard_normal(prob.sol.shape)
+    v = rng.standard_normal(u.shape)
+    with Simulation(prob) as sim:
+        sim.vjp_forward(u)
+        g = sim.vjp_backward(v)
+    o = oracle.Oracle(prob)
+    h = 1e-30
+    worst = 0.0
+    for _ in range(1000):
+        d = rng.standard_normal(u.shape)
+        _, ri = o.compute_rhs_cmplx(u, h * d)
+        jd = ri / h
+        worst = max(worst, abs(np.sum(g * d) - np.sum(v * jd)) / np.sum(np.abs(v * jd)))
+    assert worst <= 1e-8, worst
