@@ -330,3 +330,23 @@ def face_node_permutations(q: int, face_d: int):
             perm.append(a2 + q * b2)
         perms.append(perm)
     return perms
+
+
+def face_operators(ops: "TPOperatorSet", q_f: int):
+    """cv0_vs_fc[lf] and tw0_vt_fc[lf] of a (type, p) volume at the face cubature of order p_f = q_f - 1
+    (the reference's cv0_vs_fc[lf][p_f][p_v], tw0_vt_fc = cv0^T diag(w_fc); compute_face_rlhs_T.c:51-81):
+    GL with q_f points per tangential direction; q_f >= ops.q (p_f = max(p_L, p_R), face_solver.c:123-132)."""
+    if q_f < ops.q:
+        raise ValueError("face order below the volume order")
+    x_f, w_f1 = gauss_legendre(q_f)
+    d = ops.d
+    tang = lagrange_matrix(ops.x_vs, x_f)             # (q_f x q_v)
+    w_fc = tp_weights(w_f1, d - 1)
+    cv0, tw0 = [], []
+    for lf in range(2 * d):
+        nd, side = lf // 2, lf % 2
+        one_d = [ops.cv0_bnd_1d[side:side + 1, :] if k == nd else tang for k in range(d)]
+        c = kron_tp(one_d)
+        cv0.append(c)
+        tw0.append(c.T * w_fc[None, :])
+    return cv0, tw0, w_fc

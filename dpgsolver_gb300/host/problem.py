@@ -76,6 +76,26 @@ class DGProblem:
         return apply_nodes(L, self.geom.X_geom)
 
 
+def flat_arrays(prob) -> dict:
+    """The mesh in the general (multi-group) flat layout the C ABIs take: per-volume blocks concatenated in
+    volume-list order, per-face blocks in face-list order. Works for uniform DGProblem and MixedTPProblem."""
+    if hasattr(prob, "flat"):
+        return prob.flat()
+    g = prob.geom
+    nf = prob.mesh.n_faces
+    return {
+        "groups": [prob.ops],
+        "vol_group": np.zeros(prob.n_volumes, dtype=np.int32),
+        "face_q": np.full(nf, prob.ops.q, dtype=np.int32),
+        "metrics_vc": np.ascontiguousarray(np.transpose(g.metrics_vc, (0, 3, 2, 1))).ravel(),
+        "jacobian_det_vc": np.ascontiguousarray(g.jacobian_det_vc).ravel(),
+        "normals_fc": np.ascontiguousarray(g.normals_fc).ravel(),
+        "jacobian_det_fc": np.ascontiguousarray(g.jacobian_det_fc).ravel(),
+        "nc_fc": prob.nc_fc().ravel(),
+        "sol": np.ascontiguousarray(prob.sol).ravel(),
+    }
+
+
 def stable_dt(prob: "DGProblem", cfl: float = 0.1) -> float:
     """dt = cfl * h / ((2p + 1) * max(|V| + c)) over the solution nodes of the current state."""
     d = prob.d

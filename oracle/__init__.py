@@ -20,16 +20,26 @@ _c_double_p = ctypes.POINTER(ctypes.c_double)
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 
 
+class _Group(ctypes.Structure):
+    _fields_ = [("n_vs", ctypes.c_int), ("n_vc", ctypes.c_int), ("cv0_vs_vc", _c_double_p),
+                ("tw1_vt_vc", _c_double_p), ("w_vc", _c_double_p), ("ccSB0", _c_double_p), ("ccBS0", _c_double_p)]
+
+
+class _FaceOps(ctypes.Structure):
+    _fields_ = [("n_fc", ctypes.c_int), ("n_vs", ctypes.c_int), ("cv0_vs_fc", _c_double_p),
+                ("tw0_vt_fc", _c_double_p)]
+
+
 class _Problem(ctypes.Structure):
     _fields_ = [
         ("d", ctypes.c_int), ("n_var", ctypes.c_int), ("pde", ctypes.c_int), ("num_flux", ctypes.c_int),
         ("positivity", ctypes.c_int), ("b_adv", ctypes.c_double * 3),
-        ("n_vs", ctypes.c_int), ("n_vc", ctypes.c_int), ("n_fc", ctypes.c_int),
-        ("cv0_vs_vc", _c_double_p), ("tw1_vt_vc", _c_double_p), ("cv0_vs_fc", _c_double_p),
-        ("tw0_vt_fc", _c_double_p), ("w_vc", _c_double_p), ("ccSB0", _c_double_p), ("ccBS0", _c_double_p),
-        ("n_volumes", ctypes.c_int), ("metrics_vc", _c_double_p), ("jacobian_det_vc", _c_double_p),
-        ("n_faces", ctypes.c_int), ("face_vol", _c_int_p), ("face_lf", _c_int_p), ("nc_fc", _c_int_p),
-        ("normals_fc", _c_double_p), ("jacobian_det_fc", _c_double_p),
+        ("n_groups", ctypes.c_int), ("groups", ctypes.POINTER(_Group)),
+        ("n_face_ops", ctypes.c_int), ("face_ops", ctypes.POINTER(_FaceOps)),
+        ("n_volumes", ctypes.c_int), ("vol_group", _c_int_p), ("metrics_vc", _c_double_p),
+        ("jacobian_det_vc", _c_double_p),
+        ("n_faces", ctypes.c_int), ("face_vol", _c_int_p), ("face_lf", _c_int_p), ("face_ops_idx", _c_int_p),
+        ("nc_fc", _c_int_p), ("normals_fc", _c_double_p), ("jacobian_det_fc", _c_double_p),
     ]
 
 
@@ -63,7 +73,7 @@ def _load():
         lib.oracle_ssp_rk3_step.restype = ctypes.c_int
         lib.oracle_enforce_positivity.argtypes = [ctypes.c_void_p, _c_double_p, _c_int_p]
         lib.oracle_enforce_positivity.restype = ctypes.c_int
-        lib.oracle_m_inv.argtypes = [ctypes.c_void_p]
+        lib.oracle_m_inv.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.oracle_m_inv.restype = _c_double_p
         _lib = lib
     return _lib
@@ -78,41 +88,70 @@ def _ip(a):
 
 
 class Oracle:
-    """Oracle context for one DGProblem (dense reference operators, reference data flow)."""
+    """Oracle context for a DG problem (uniform DGProblem or mixed-order MixedTPProblem): dense reference
+    operators, the reference's data flow. States are passed in the problem's own shape."""
 
     def __init__(self, prob):
-        lib = _load()
-        ops, mesh, geom = prob.ops, prob.mesh, prob.geom
-        d = prob.d
-        keep = {}
+        from dpgsolver_gb300.host.element import face_operators
+        from dpgsolver_gb300.host.problem import flat_arrays
 
-        def arr(name, a, dtype=np.float64):
-            keep[name] = np.ascontiguousarray(a, dtype=dtype)
-            return keep[name]
+        lib = _load()
+        fl = flat_arrays(prob)
+        d = prob.d
+        keep = []
+
+        def arr(a, dtype=np.float64):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            keep.append(a)
+            return a
+
+        groups = fl["groups"]
+        G = (_Group * len(groups))()
+        for gi, ops in enumerate(groups):
+            G[gi].n_vs, G[gi].n_vc = ops.n_vs, ops.n_vc
+            G[gi].cv0_vs_vc = _dp(arr(ops.cv0_vs_vc()))
+            G[gi].tw1_vt_vc = _dp(arr(np.stack([ops.tw1_vt_vc(k) for k in range(d)])))
+            G[gi].w_vc = _dp(arr(ops.w_vc))
+            G[gi].ccSB0 = _dp(arr(ops.ccSB0_vs_vs()))
+            G[gi].ccBS0 = _dp(arr(ops.ccBS0_vs_vs()))
+        # face operator sets: one per (group, face order) pair that occurs
+        vol_group = fl["vol_group"]
+        face_q = fl["face_q"]
+        mesh = prob.mesh
+        pairs = {}
+        idx = np.empty((mesh.n_faces, 2), dtype=np.int32)
+        for f in range(mesh.n_faces):
+            for s in range(2):
+                key = (int(vol_group[mesh.face_vol[f, s]]), int(face_q[f]))
+                if key not in pairs:
+                    pairs[key] = len(pairs)
+                idx[f, s] = pairs[key]
+        FO = (_FaceOps * len(pairs))()
+        for (gi, qf), k in pairs.items():
+            cv0, tw0, _ = face_operators(groups[gi], qf)
+            FO[k].n_fc, FO[k].n_vs = cv0[0].shape[0], groups[gi].n_vs
+            FO[k].cv0_vs_fc = _dp(arr(np.stack(cv0)))
+            FO[k].tw0_vt_fc = _dp(arr(np.stack(tw0)))
 
         P = _Problem()
         P.d, P.n_var, P.pde, P.num_flux = d, prob.n_var, prob.pde, prob.num_flux
         P.positivity = 1 if prob.positivity else 0
         for k in range(3):
             P.b_adv[k] = float(prob.b_adv[k])
-        P.n_vs, P.n_vc, P.n_fc = ops.n_vs, ops.n_vc, ops.n_fc
-        P.cv0_vs_vc = _dp(arr("cv0", ops.cv0_vs_vc()))
-        P.tw1_vt_vc = _dp(arr("tw1", np.stack([ops.tw1_vt_vc(k) for k in range(d)])))
-        P.cv0_vs_fc = _dp(arr("cv0f", np.stack([ops.cv0_vs_fc(lf) for lf in range(2 * d)])))
-        P.tw0_vt_fc = _dp(arr("tw0f", np.stack([ops.tw0_vt_fc(lf) for lf in range(2 * d)])))
-        P.w_vc = _dp(arr("w", ops.w_vc))
-        P.ccSB0 = _dp(arr("sb", ops.ccSB0_vs_vs()))
-        P.ccBS0 = _dp(arr("bs", ops.ccBS0_vs_vs()))
+        P.n_groups, P.groups = len(groups), G
+        P.n_face_ops, P.face_ops = len(pairs), FO
         P.n_volumes = mesh.n_volumes
-        # metrics (nv, n_vc, d, d) -> per volume column-major (n, i, j): index n + n_vc*(i + d*j)
-        P.metrics_vc = _dp(arr("m", np.transpose(geom.metrics_vc, (0, 3, 2, 1))))
-        P.jacobian_det_vc = _dp(arr("J", geom.jacobian_det_vc))
+        P.vol_group = _ip(arr(vol_group, np.int32))
+        P.metrics_vc = _dp(arr(fl["metrics_vc"]))
+        P.jacobian_det_vc = _dp(arr(fl["jacobian_det_vc"]))
         P.n_faces = mesh.n_faces
-        P.face_vol = _ip(arr("fv", mesh.face_vol, np.int32))
-        P.face_lf = _ip(arr("flf", mesh.face_lf, np.int32))
-        P.nc_fc = _ip(arr("nc", prob.nc_fc(), np.int32))
-        P.normals_fc = _dp(arr("nrm", geom.normals_fc))
-        P.jacobian_det_fc = _dp(arr("Jf", geom.jacobian_det_fc))
+        P.face_vol = _ip(arr(mesh.face_vol, np.int32))
+        P.face_lf = _ip(arr(mesh.face_lf, np.int32))
+        P.face_ops_idx = _ip(arr(idx, np.int32))
+        P.nc_fc = _ip(arr(fl["nc_fc"], np.int32))
+        P.normals_fc = _dp(arr(fl["normals_fc"]))
+        P.jacobian_det_fc = _dp(arr(fl["jacobian_det_fc"]))
+        self._keep = (keep, G, FO, P)
         h = ctypes.c_void_p()
         st = lib.oracle_create(ctypes.byref(P), ctypes.byref(h))
         if st != 0:
@@ -120,58 +159,65 @@ class Oracle:
         self._h = h
         self._lib = lib
         self.prob = prob
-        self.shape = prob.sol.shape
+        self.n_state = int(fl["sol"].size)
 
     def __del__(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             self._lib.oracle_destroy(self._h)
             self._h = None
 
+    def _flat(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.size != self.n_state:
+            raise ValueError(f"state has {a.size} values, the problem {self.n_state}")
+        return a.reshape(-1)
+
     def compute_rhs(self, sol):
-        s = np.ascontiguousarray(sol, dtype=np.float64)
+        s = self._flat(sol)
         r = np.empty_like(s)
         mx = ctypes.c_double()
         st = self._lib.oracle_compute_rhs(self._h, _dp(s), _dp(r), ctypes.byref(mx))
         if st != 0:
             raise RuntimeError(f"oracle_compute_rhs failed: {st}")
-        return r, mx.value
+        return r.reshape(np.shape(sol)), mx.value
 
     def compute_rhs_raw(self, sol):
-        s = np.ascontiguousarray(sol, dtype=np.float64)
+        s = self._flat(sol)
         r = np.empty_like(s)
         st = self._lib.oracle_compute_rhs_raw(self._h, _dp(s), _dp(r))
         if st != 0:
             raise RuntimeError(f"oracle_compute_rhs_raw failed: {st}")
-        return r
+        return r.reshape(np.shape(sol))
 
     def compute_rhs_cmplx(self, sol_re, sol_im):
-        sr = np.ascontiguousarray(sol_re, dtype=np.float64)
-        si = np.ascontiguousarray(sol_im, dtype=np.float64)
+        sr = self._flat(sol_re)
+        si = self._flat(sol_im)
         rr, ri = np.empty_like(sr), np.empty_like(sr)
         st = self._lib.oracle_compute_rhs_cmplx(self._h, _dp(sr), _dp(si), _dp(rr), _dp(ri))
         if st != 0:
             raise RuntimeError(f"oracle_compute_rhs_cmplx failed: {st}")
-        return rr, ri
+        return rr.reshape(np.shape(sol_re)), ri.reshape(np.shape(sol_re))
 
     def ssp_rk3_step(self, sol, dt):
-        """In-place on a copy; returns (new_sol, max_rhs, n_corrections)."""
-        s = np.array(sol, dtype=np.float64, copy=True, order="C")
+        """Returns (new_sol, max_rhs, n_corrections) for a copy of sol."""
+        s = np.array(self._flat(sol), copy=True)
         mx = ctypes.c_double()
         nc = ctypes.c_int()
         st = self._lib.oracle_ssp_rk3_step(self._h, dt, _dp(s), ctypes.byref(mx), ctypes.byref(nc))
         if st != 0:
             raise RuntimeError(f"oracle_ssp_rk3_step failed: {st}")
-        return s, mx.value, nc.value
+        return s.reshape(np.shape(sol)), mx.value, nc.value
 
     def enforce_positivity(self, sol):
-        s = np.array(sol, dtype=np.float64, copy=True, order="C")
+        s = np.array(self._flat(sol), copy=True)
         nc = ctypes.c_int()
         st = self._lib.oracle_enforce_positivity(self._h, _dp(s), ctypes.byref(nc))
         if st != 0:
             raise RuntimeError(f"oracle_enforce_positivity failed: {st}")
-        return s, nc.value
+        return s.reshape(np.shape(sol)), nc.value
 
-    def m_inv(self):
-        n = self.prob.ops.n_vs
-        p = self._lib.oracle_m_inv(self._h)
-        return np.ctypeslib.as_array(p, shape=(self.prob.n_volumes, n, n)).copy()
+    def m_inv(self, v: int):
+        n = self.prob.ops.n_vs if not hasattr(self.prob, "groups") else \
+            self.prob.groups[self.prob.vol_group[v]].n_vs
+        p = self._lib.oracle_m_inv(self._h, int(v))
+        return np.ctypeslib.as_array(p, shape=(n, n)).copy()

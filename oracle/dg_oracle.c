@@ -29,12 +29,11 @@
 #define ORACLE_EPS 1.0e-15 /* definitions_tol.h:23 */
 
 struct oracle_ctx {
-	struct oracle_problem P;
-	double* m_inv;   /* per volume n_vs x n_vs row-major */
-	/* owned copies of the problem arrays */
-	double *cv0_vs_vc, *tw1_vt_vc, *cv0_vs_fc, *tw0_vt_fc, *w_vc, *ccSB0, *ccBS0;
-	double *metrics_vc, *jacobian_det_vc, *normals_fc, *jacobian_det_fc;
-	int *face_vol, *face_lf, *nc_fc;
+	struct oracle_problem P;       /* pointers into the caller's arrays (they must outlive the context) */
+	size_t n_state;
+	size_t *state_off, *vc_off, *fc_off, *minv_off;   /* per volume / per face offsets */
+	int max_vs, max_vc, max_fc;
+	double* m_inv;                 /* per volume n_vs x n_vs row-major */
 };
 
 /* ---- double instantiation ---- */
@@ -62,24 +61,6 @@ struct oracle_ctx {
 #undef REAL_T
 #undef ABS_T
 #undef SQRT_T
-
-static double* dup_d(const double* src, size_t n)
-{
-	if (!src || n == 0)
-		return NULL;
-	double* p = malloc(sizeof(double) * n);
-	memcpy(p, src, sizeof(double) * n);
-	return p;
-}
-
-static int* dup_i(const int* src, size_t n)
-{
-	if (!src || n == 0)
-		return NULL;
-	int* p = malloc(sizeof(int) * n);
-	memcpy(p, src, sizeof(int) * n);
-	return p;
-}
 
 /* Inverse by Gauss-Jordan elimination with partial pivoting (the reference solves with the identity as
  * right-hand side through LAPACKE, matrix_constructors_T.c constructor_inverse_const_Matrix_T). */
@@ -130,7 +111,7 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 {
 	if (!in || !out)
 		return ORACLE_ERR_ARG;
-	if (in->d < 2 || in->d > 3 || in->n_volumes < 1 || in->n_vs < 1 || in->n_vc < 1 || in->n_fc < 1)
+	if (in->d < 2 || in->d > 3 || in->n_volumes < 1 || in->n_groups < 1 || in->n_face_ops < 1)
 		return ORACLE_ERR_ARG;
 	if (in->pde == ORACLE_PDE_EULER && in->n_var != in->d + 2)
 		return ORACLE_ERR_ARG;
@@ -138,36 +119,60 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 		return ORACLE_ERR_ARG;
 	struct oracle_ctx* c = calloc(1, sizeof *c);
 	c->P = *in;
-	const int d = in->d, n_vs = in->n_vs, n_vc = in->n_vc, n_fc = in->n_fc, n_lf = 2 * d;
+	const int d = in->d, nv = in->n_var;
 	const size_t nV = (size_t)in->n_volumes, nF = (size_t)in->n_faces;
-	c->P.cv0_vs_vc = c->cv0_vs_vc = dup_d(in->cv0_vs_vc, (size_t)n_vc * n_vs);
-	c->P.tw1_vt_vc = c->tw1_vt_vc = dup_d(in->tw1_vt_vc, (size_t)d * n_vs * n_vc);
-	c->P.cv0_vs_fc = c->cv0_vs_fc = dup_d(in->cv0_vs_fc, (size_t)n_lf * n_fc * n_vs);
-	c->P.tw0_vt_fc = c->tw0_vt_fc = dup_d(in->tw0_vt_fc, (size_t)n_lf * n_vs * n_fc);
-	c->P.w_vc = c->w_vc = dup_d(in->w_vc, (size_t)n_vc);
-	c->P.ccSB0 = c->ccSB0 = dup_d(in->ccSB0, (size_t)n_vs * n_vs);
-	c->P.ccBS0 = c->ccBS0 = dup_d(in->ccBS0, (size_t)n_vs * n_vs);
-	c->P.metrics_vc = c->metrics_vc = dup_d(in->metrics_vc, nV * n_vc * d * d);
-	c->P.jacobian_det_vc = c->jacobian_det_vc = dup_d(in->jacobian_det_vc, nV * n_vc);
-	c->P.normals_fc = c->normals_fc = dup_d(in->normals_fc, nF * n_fc * d);
-	c->P.jacobian_det_fc = c->jacobian_det_fc = dup_d(in->jacobian_det_fc, nF * n_fc);
-	c->P.face_vol = c->face_vol = dup_i(in->face_vol, nF * 2);
-	c->P.face_lf = c->face_lf = dup_i(in->face_lf, nF * 2);
-	c->P.nc_fc = c->nc_fc = dup_i(in->nc_fc, nF * n_fc);
+	c->state_off = malloc(sizeof(size_t) * (nV + 1));
+	c->vc_off = malloc(sizeof(size_t) * (nV + 1));
+	c->minv_off = malloc(sizeof(size_t) * (nV + 1));
+	c->fc_off = malloc(sizeof(size_t) * (nF + 1));
+	size_t so = 0, vo = 0, mo = 0, fo = 0;
+	for (size_t v = 0; v < nV; ++v) {
+		const int g = in->vol_group[v];
+		if (g < 0 || g >= in->n_groups) {
+			oracle_destroy(c);
+			return ORACLE_ERR_ARG;
+		}
+		const struct oracle_group* G = &in->groups[g];
+		c->state_off[v] = so;
+		c->vc_off[v] = vo;
+		c->minv_off[v] = mo;
+		so += (size_t)G->n_vs * nv;
+		vo += (size_t)G->n_vc;
+		mo += (size_t)G->n_vs * G->n_vs;
+		if (G->n_vs > c->max_vs) c->max_vs = G->n_vs;
+		if (G->n_vc > c->max_vc) c->max_vc = G->n_vc;
+	}
+	c->state_off[nV] = so;
+	c->n_state = so;
+	for (size_t f = 0; f < nF; ++f) {
+		const struct oracle_face_ops* FL = &in->face_ops[in->face_ops_idx[2 * f]];
+		const struct oracle_face_ops* FR = &in->face_ops[in->face_ops_idx[2 * f + 1]];
+		if (FL->n_fc != FR->n_fc) {
+			oracle_destroy(c);
+			return ORACLE_ERR_ARG;
+		}
+		c->fc_off[f] = fo;
+		fo += (size_t)FL->n_fc;
+		if (FL->n_fc > c->max_fc) c->max_fc = FL->n_fc;
+	}
+	c->fc_off[nF] = fo;
+	(void)d;
 
 	/* M = cv0_vs_vc^T diag(w_vc J_vc) cv0_vs_vc, m_inv = M^-1 (volume_solver_T.c:115-145) */
-	c->m_inv = malloc(sizeof(double) * nV * n_vs * n_vs);
-	double* M = malloc(sizeof(double) * (size_t)n_vs * n_vs);
+	c->m_inv = malloc(sizeof(double) * (mo ? mo : 1));
+	double* M = malloc(sizeof(double) * (size_t)c->max_vs * c->max_vs);
 	for (size_t v = 0; v < nV; ++v) {
-		const double* J = &c->jacobian_det_vc[v * n_vc];
+		const struct oracle_group* G = &in->groups[in->vol_group[v]];
+		const int n_vs = G->n_vs, n_vc = G->n_vc;
+		const double* J = &in->jacobian_det_vc[c->vc_off[v]];
 		for (int i = 0; i < n_vs; ++i)
 			for (int j = 0; j < n_vs; ++j) {
 				double s = 0.0;
 				for (int k = 0; k < n_vc; ++k)
-					s += c->cv0_vs_vc[k * n_vs + i] * (c->w_vc[k] * J[k]) * c->cv0_vs_vc[k * n_vs + j];
+					s += G->cv0_vs_vc[k * n_vs + i] * (G->w_vc[k] * J[k]) * G->cv0_vs_vc[k * n_vs + j];
 				M[i * n_vs + j] = s;
 			}
-		int st = invert(n_vs, M, &c->m_inv[v * n_vs * n_vs]);
+		int st = invert(n_vs, M, &c->m_inv[c->minv_off[v]]);
 		if (st != ORACLE_OK) {
 			free(M);
 			oracle_destroy(c);
@@ -184,16 +189,16 @@ void oracle_destroy(struct oracle_ctx* c)
 	if (!c)
 		return;
 	free(c->m_inv);
-	free(c->cv0_vs_vc); free(c->tw1_vt_vc); free(c->cv0_vs_fc); free(c->tw0_vt_fc); free(c->w_vc);
-	free(c->ccSB0); free(c->ccBS0);
-	free(c->metrics_vc); free(c->jacobian_det_vc); free(c->normals_fc); free(c->jacobian_det_fc);
-	free(c->face_vol); free(c->face_lf); free(c->nc_fc);
+	free(c->state_off);
+	free(c->vc_off);
+	free(c->minv_off);
+	free(c->fc_off);
 	free(c);
 }
 
 size_t oracle_state_size(const struct oracle_ctx* c)
 {
-	return (size_t)c->P.n_volumes * c->P.n_vs * c->P.n_var;
+	return c->n_state;
 }
 
 int oracle_compute_rhs(const struct oracle_ctx* c, const double* sol, double* rhs, double* max_rhs)
@@ -280,12 +285,13 @@ static double average(const double* a, int n)
 
 /* enforce_positivity_highorder (solve.c:187-233) for one volume. Returns 1 when correct_coef was applied
  * (for density, pressure or both), 0 when not, or a negative error. */
-static int enforce_positivity(const struct oracle_ctx* c, double* s_coef)
+static int enforce_positivity(const struct oracle_ctx* c, int v, double* s_coef)
 {
 	const struct oracle_problem* P = &c->P;
-	const int n_n = P->n_vs, n_vr = P->n_var, d = P->d;
+	const struct oracle_group* G = &P->groups[P->vol_group[v]];
+	const int n_n = G->n_vs, n_vr = P->n_var, d = P->d;
 	double* sb = calloc((size_t)n_n * n_vr, sizeof(double));
-	mm_acc_d(n_n, n_n, n_vr, 1.0, P->ccSB0, s_coef, sb);
+	mm_acc_d(n_n, n_n, n_vr, 1.0, G->ccSB0, s_coef, sb);
 	convert_c_to_p(d, n_n, sb);
 	int n_corr = 0;
 	for (int vr = 0; vr < n_vr; vr += n_vr - 1) {
@@ -319,7 +325,7 @@ static int enforce_positivity(const struct oracle_ctx* c, double* s_coef)
 	convert_p_to_c(d, n_n, sb);
 	for (size_t i = 0; i < (size_t)n_n * n_vr; ++i)
 		s_coef[i] = 0.0;
-	mm_acc_d(n_n, n_n, n_vr, 1.0, P->ccBS0, sb, s_coef);
+	mm_acc_d(n_n, n_n, n_vr, 1.0, G->ccBS0, sb, s_coef);
 	free(sb);
 	return n_corr;
 }
@@ -329,7 +335,6 @@ int oracle_ssp_rk3_step(const struct oracle_ctx* c, const double dt, double* sol
 {
 	const struct oracle_problem* P = &c->P;
 	const size_t n = oracle_state_size(c);
-	const size_t vs_sz = (size_t)P->n_vs * P->n_var;
 	double* rhs = malloc(sizeof(double) * n);
 	double* sp = malloc(sizeof(double) * n);
 	double mx = 0.0;
@@ -340,9 +345,10 @@ int oracle_ssp_rk3_step(const struct oracle_ctx* c, const double dt, double* sol
 		if (st != ORACLE_OK)
 			break;
 		for (int v = 0; v < P->n_volumes; ++v) {
-			double* s = &sol[(size_t)v * vs_sz];
-			double* p = &sp[(size_t)v * vs_sz];
-			const double* r = &rhs[(size_t)v * vs_sz];
+			const size_t o = c->state_off[v], vs_sz = c->state_off[v + 1] - o;
+			double* s = &sol[o];
+			double* p = &sp[o];
+			const double* r = &rhs[o];
 			switch (rk) {
 			case 0:
 				for (size_t i = 0; i < vs_sz; ++i) {
@@ -360,7 +366,7 @@ int oracle_ssp_rk3_step(const struct oracle_ctx* c, const double dt, double* sol
 				break;
 			}
 			if (P->positivity) {
-				int k = enforce_positivity(c, s);
+				int k = enforce_positivity(c, v, s);
 				if (k < 0) {
 					st = k;
 					break;
@@ -380,10 +386,9 @@ int oracle_ssp_rk3_step(const struct oracle_ctx* c, const double dt, double* sol
 
 int oracle_enforce_positivity(const struct oracle_ctx* c, double* sol, int* n_corrections)
 {
-	const size_t vs_sz = (size_t)c->P.n_vs * c->P.n_var;
 	int ncorr = 0;
 	for (int v = 0; v < c->P.n_volumes; ++v) {
-		int k = enforce_positivity(c, &sol[(size_t)v * vs_sz]);
+		int k = enforce_positivity(c, v, &sol[c->state_off[v]]);
 		if (k < 0)
 			return k;
 		ncorr += k;
@@ -393,7 +398,7 @@ int oracle_enforce_positivity(const struct oracle_ctx* c, double* sol, int* n_co
 	return ORACLE_OK;
 }
 
-const double* oracle_m_inv(const struct oracle_ctx* c)
+const double* oracle_m_inv(const struct oracle_ctx* c, int v)
 {
-	return c->m_inv;
+	return &c->m_inv[c->minv_off[v]];
 }

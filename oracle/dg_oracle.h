@@ -18,28 +18,45 @@ enum {
 enum { ORACLE_PDE_ADVECTION = 1, ORACLE_PDE_EULER = 3 };                  /* definitions_test_case.h */
 enum { ORACLE_NUM_FLUX_UPWIND = 11, ORACLE_NUM_FLUX_ROE_PIKE = 31, ORACLE_NUM_FLUX_LAX_FRIEDRICHS = 32 };
 
-/* One (element type, p) group with dense reference operators; all volumes share it.
- * Operators row-major; states and per-volume node arrays column-major like the reference's 'C' Multiarrays. */
-struct oracle_problem {
-	int d, n_var, pde, num_flux, positivity;
-	double b_adv[3];
-	int n_vs, n_vc, n_fc;
+/* One (element type, p): the reference's dense (op_std) volume operators. Row-major. */
+struct oracle_group {
+	int n_vs, n_vc;
 	const double* cv0_vs_vc;   /* n_vc x n_vs */
 	const double* tw1_vt_vc;   /* d x (n_vs x n_vc) */
-	const double* cv0_vs_fc;   /* 2d x (n_fc x n_vs) */
-	const double* tw0_vt_fc;   /* 2d x (n_vs x n_fc) */
 	const double* w_vc;        /* n_vc */
 	const double* ccSB0;       /* n_vs x n_vs  Lagrange -> Bezier coefficients */
 	const double* ccBS0;       /* n_vs x n_vs  Bezier -> Lagrange coefficients */
+};
+
+/* Face operators of a volume of one group at one face cubature order p_f (cv0_vs_fc[lf][p_f][p_v],
+ * tw0_vt_fc likewise: compute_face_rlhs_T.c:51-81). Row-major. */
+struct oracle_face_ops {
+	int n_fc, n_vs;
+	const double* cv0_vs_fc;   /* 2d x (n_fc x n_vs) */
+	const double* tw0_vt_fc;   /* 2d x (n_vs x n_fc) */
+};
+
+/* A mesh of volumes of any number of groups. States and per-volume node arrays are concatenated in volume-list
+ * order (per volume the reference's column-major blocks); per-face arrays in face-list order. The oracle keeps
+ * pointers to these arrays: they must outlive the context. */
+struct oracle_problem {
+	int d, n_var, pde, num_flux, positivity;
+	double b_adv[3];
+	int n_groups;
+	const struct oracle_group* groups;
+	int n_face_ops;
+	const struct oracle_face_ops* face_ops;
 	int n_volumes;
-	const double* metrics_vc;      /* n_volumes x (n_vc, d, d) column-major */
-	const double* jacobian_det_vc; /* n_volumes x n_vc */
+	const int* vol_group;
+	const double* metrics_vc;      /* per volume (n_vc, d, d) column-major */
+	const double* jacobian_det_vc; /* per volume n_vc */
 	int n_faces;
 	const int* face_vol;           /* n_faces x 2 */
 	const int* face_lf;            /* n_faces x 2 */
-	const int* nc_fc;              /* n_faces x n_fc: right trace gathered as sR[i] = sR_own[nc_fc[i]] */
-	const double* normals_fc;      /* n_faces x (n_fc x d) row-major */
-	const double* jacobian_det_fc; /* n_faces x n_fc */
+	const int* face_ops_idx;       /* n_faces x 2: face operator set of each side */
+	const int* nc_fc;              /* per face n_fc: right trace gathered as sR[i] = sR_own[nc_fc[i]] */
+	const double* normals_fc;      /* per face (n_fc x d) row-major */
+	const double* jacobian_det_fc; /* per face n_fc */
 };
 
 struct oracle_ctx;
@@ -53,7 +70,8 @@ int oracle_compute_rhs_cmplx(const struct oracle_ctx* c, const double* sol_re, c
                              double* rhs_re, double* rhs_im);
 int oracle_ssp_rk3_step(const struct oracle_ctx* c, double dt, double* sol, double* max_rhs, int* n_corrections);
 int oracle_enforce_positivity(const struct oracle_ctx* c, double* sol, int* n_corrections);
-const double* oracle_m_inv(const struct oracle_ctx* c);
+/* M^-1 of volume v (n_vs x n_vs row-major) */
+const double* oracle_m_inv(const struct oracle_ctx* c, int v);
 
 #ifdef __cplusplus
 }

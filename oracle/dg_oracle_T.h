@@ -157,28 +157,28 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 {
 	const struct oracle_problem* P = &c->P;
 	const int d = P->d, nv = P->n_var, neq = P->n_var;
-	const int n_vs = P->n_vs, n_vc = P->n_vc, n_fc = P->n_fc;
-	const size_t vs_sz = (size_t)n_vs * nv;
 
-	for (size_t i = 0; i < (size_t)P->n_volumes * vs_sz; ++i)
+	for (size_t i = 0; i < c->n_state; ++i)
 		rhs[i] = 0.0;
 
-	Type* s_vc = malloc(sizeof(Type) * (size_t)n_vc * nv);
-	Type* fr = malloc(sizeof(Type) * (size_t)n_vc * neq * d);
-	Type* sL = malloc(sizeof(Type) * (size_t)n_fc * nv);
-	Type* sR0 = malloc(sizeof(Type) * (size_t)n_fc * nv);
-	Type* sR = malloc(sizeof(Type) * (size_t)n_fc * nv);
-	Type* nnf = malloc(sizeof(Type) * (size_t)n_fc * neq);
-	Type* nnfR = malloc(sizeof(Type) * (size_t)n_fc * neq);
+	Type* s_vc = malloc(sizeof(Type) * (size_t)c->max_vc * nv);
+	Type* fr = malloc(sizeof(Type) * (size_t)c->max_vc * neq * d);
+	Type* sL = malloc(sizeof(Type) * (size_t)c->max_fc * nv);
+	Type* sR0 = malloc(sizeof(Type) * (size_t)c->max_fc * nv);
+	Type* sR = malloc(sizeof(Type) * (size_t)c->max_fc * nv);
+	Type* nnf = malloc(sizeof(Type) * (size_t)c->max_fc * neq);
+	Type* nnfR = malloc(sizeof(Type) * (size_t)c->max_fc * neq);
 
 	/* ---- volume term ---- */
 	for (int v = 0; v < P->n_volumes; ++v) {
-		const Type* s = &sol[(size_t)v * vs_sz];
-		Type* r = &rhs[(size_t)v * vs_sz];
-		const double* m = &P->metrics_vc[(size_t)v * n_vc * d * d];
+		const struct oracle_group* G = &P->groups[P->vol_group[v]];
+		const int n_vs = G->n_vs, n_vc = G->n_vc;
+		const Type* s = &sol[c->state_off[v]];
+		Type* r = &rhs[c->state_off[v]];
+		const double* m = &P->metrics_vc[c->vc_off[v] * d * d];
 		for (size_t i = 0; i < (size_t)n_vc * nv; ++i)
 			s_vc[i] = 0.0;
-		SUF(mm_acc)(n_vc, n_vs, nv, 1.0, P->cv0_vs_vc, s, s_vc);
+		SUF(mm_acc)(n_vc, n_vs, nv, 1.0, G->cv0_vs_vc, s, s_vc);
 		for (size_t i = 0; i < (size_t)n_vc * neq * d; ++i)
 			fr[i] = 0.0;
 		for (int n = 0; n < n_vc; ++n) {
@@ -200,7 +200,7 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 		}
 		/* rhs += sum_dim tw1_vt_vc[dim] . fr(:,:,dim)  (compute_volume_rlhs_T.c:166-177) */
 		for (int dim = 0; dim < d; ++dim)
-			SUF(mm_acc)(n_vs, n_vc, neq, 1.0, &P->tw1_vt_vc[(size_t)dim * n_vs * n_vc],
+			SUF(mm_acc)(n_vs, n_vc, neq, 1.0, &G->tw1_vt_vc[(size_t)dim * n_vs * n_vc],
 			            &fr[(size_t)n_vc * neq * dim], r);
 	}
 
@@ -208,13 +208,16 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 	for (int f = 0; f < P->n_faces; ++f) {
 		const int vL = P->face_vol[2 * f], vR = P->face_vol[2 * f + 1];
 		const int lfL = P->face_lf[2 * f], lfR = P->face_lf[2 * f + 1];
-		const int* nc = &P->nc_fc[(size_t)f * n_fc];
-		const double* nrm = &P->normals_fc[(size_t)f * n_fc * d];
-		const double* jf = &P->jacobian_det_fc[(size_t)f * n_fc];
+		const struct oracle_face_ops* FL = &P->face_ops[P->face_ops_idx[2 * f]];
+		const struct oracle_face_ops* FR = &P->face_ops[P->face_ops_idx[2 * f + 1]];
+		const int n_fc = FL->n_fc;
+		const int* nc = &P->nc_fc[c->fc_off[f]];
+		const double* nrm = &P->normals_fc[c->fc_off[f] * d];
+		const double* jf = &P->jacobian_det_fc[c->fc_off[f]];
 		for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
 			sL[i] = sR0[i] = 0.0;
-		SUF(mm_acc)(n_fc, n_vs, nv, 1.0, &P->cv0_vs_fc[(size_t)lfL * n_fc * n_vs], &sol[(size_t)vL * vs_sz], sL);
-		SUF(mm_acc)(n_fc, n_vs, nv, 1.0, &P->cv0_vs_fc[(size_t)lfR * n_fc * n_vs], &sol[(size_t)vR * vs_sz], sR0);
+		SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], &sol[c->state_off[vL]], sL);
+		SUF(mm_acc)(n_fc, FR->n_vs, nv, 1.0, &FR->cv0_vs_fc[(size_t)lfR * n_fc * FR->n_vs], &sol[c->state_off[vR]], sR0);
 		/* right trace reordered to the left's face-node order (boundary_T.c:80-92) */
 		for (int k = 0; k < nv; ++k)
 			for (int i = 0; i < n_fc; ++i)
@@ -246,11 +249,11 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 		 * (compute_face_rlhs_T.c:297-310, 347-359). The right side is brought back to its own face-node
 		 * order with the inverse of the trace permutation; the reference applies nc_fc itself, which is the
 		 * same whenever nc_fc is an involution. */
-		SUF(mm_acc)(n_vs, n_fc, neq, -1.0, &P->tw0_vt_fc[(size_t)lfL * n_vs * n_fc], nnf, &rhs[(size_t)vL * vs_sz]);
+		SUF(mm_acc)(FL->n_vs, n_fc, neq, -1.0, &FL->tw0_vt_fc[(size_t)lfL * FL->n_vs * n_fc], nnf, &rhs[c->state_off[vL]]);
 		for (int k = 0; k < neq; ++k)
 			for (int i = 0; i < n_fc; ++i)
 				nnfR[nc[i] + (size_t)n_fc * k] = -nnf[i + (size_t)n_fc * k];
-		SUF(mm_acc)(n_vs, n_fc, neq, -1.0, &P->tw0_vt_fc[(size_t)lfR * n_vs * n_fc], nnfR, &rhs[(size_t)vR * vs_sz]);
+		SUF(mm_acc)(FR->n_vs, n_fc, neq, -1.0, &FR->tw0_vt_fc[(size_t)lfR * FR->n_vs * n_fc], nnfR, &rhs[c->state_off[vR]]);
 	}
 
 	free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);
@@ -261,13 +264,14 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 static void SUF(scale_m_inv)(const struct oracle_ctx* c, Type* rhs)
 {
 	const struct oracle_problem* P = &c->P;
-	const int n_vs = P->n_vs, nv = P->n_var;
-	Type* tmp = malloc(sizeof(Type) * (size_t)n_vs * nv);
+	const int nv = P->n_var;
+	Type* tmp = malloc(sizeof(Type) * (size_t)c->max_vs * nv);
 	for (int v = 0; v < P->n_volumes; ++v) {
-		Type* r = &rhs[(size_t)v * n_vs * nv];
+		const int n_vs = P->groups[P->vol_group[v]].n_vs;
+		Type* r = &rhs[c->state_off[v]];
 		for (size_t i = 0; i < (size_t)n_vs * nv; ++i)
 			tmp[i] = 0.0;
-		SUF(mm_acc)(n_vs, n_vs, nv, 1.0, &c->m_inv[(size_t)v * n_vs * n_vs], r, tmp);
+		SUF(mm_acc)(n_vs, n_vs, nv, 1.0, &c->m_inv[c->minv_off[v]], r, tmp);
 		for (size_t i = 0; i < (size_t)n_vs * nv; ++i)
 			r[i] = tmp[i];
 	}
