@@ -13,10 +13,12 @@ PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 LIB_PATH = os.path.join(PKG_DIR, "libdgpu.so")
-SOURCES = ["dgpu.cu"]
-HEADERS = ["dgpu_tp.cuh", "dgpu_physics.cuh"]
+SOURCES = ["dgpu.cu", "dgpu_batched.cu"]
+HEADERS = ["dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
+           "dgpu_host_ops.h"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
-              "-Xcompiler", "-fPIC", "-shared"]
+              "-Xcompiler", "-fPIC"]
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
 
 
 def nvcc_path() -> str:
@@ -38,10 +40,21 @@ def build(force: bool = False, verbose: bool = False) -> str:
     """Compile libdgpu.so for sm_103a (nvcc cross-compiles without a GPU)."""
     if not force and not _stale():
         return LIB_PATH
-    cmd = [nvcc_path()] + NVCC_FLAGS + ["-o", LIB_PATH] + [os.path.join(CSRC, s) for s in SOURCES]
-    if verbose:
-        print(" ".join(cmd))
-    subprocess.run(cmd, check=True)
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    objs, procs = [], []
+    for src in SOURCES:   # translation units compile in parallel, then one link
+        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
+        cmd = [nvcc_path()] + NVCC_FLAGS + ["-c", "-o", obj, os.path.join(CSRC, src)]
+        if verbose:
+            print(" ".join(cmd))
+        procs.append((cmd, subprocess.Popen(cmd)))
+        objs.append(obj)
+    for cmd, pr in procs:
+        if pr.wait() != 0:
+            raise subprocess.CalledProcessError(pr.returncode, cmd)
+    tmp = LIB_PATH + ".tmp"
+    subprocess.run([nvcc_path(), "-shared", "-o", tmp] + objs, check=True)
+    os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
 
@@ -100,6 +113,26 @@ EXPORTS = {
                                                 ctypes.c_void_p]),
     "dgpu_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "dgpu_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    # batched mixed-order context
+    "dgpu_batch_create": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.c_int, ctypes.POINTER(TPOperators), c_int_p,
+                                         ctypes.POINTER(Mesh), ctypes.POINTER(ctypes.c_void_p)]),
+    "dgpu_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dgpu_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "dgpu_batch_state_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
+    "dgpu_batch_upload_state": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_batch_download_state": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_batch_download_rhs": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_batch_compute_rhs": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_batch_ssp_rk3_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, c_double_p]),
+    "dgpu_batch_set_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dgpu_batch_get_mode": (ctypes.c_int, [ctypes.c_void_p, c_int_p]),
+    "dgpu_batch_set_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dgpu_batch_set_group_tile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "dgpu_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_char_p,
+                                           ctypes.c_size_t]),
+    "dgpu_batch_kernel_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "dgpu_batch_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dgpu_batch_positivity_corrections": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
 }
 
 
@@ -127,8 +160,8 @@ class DGPUError(RuntimeError):
         self.status = status
 
 
-def check(status: int, ctx=None):
+def check(status: int, ctx=None, batch: bool = False):
     if status != 0:
         lib = load()
-        msg = lib.dgpu_last_error(ctx)
+        msg = lib.dgpu_batch_last_error(ctx) if batch else lib.dgpu_last_error(ctx)
         raise DGPUError(status, (msg or b"").decode() or lib.dgpu_status_string(status).decode())

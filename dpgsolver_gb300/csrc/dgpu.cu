@@ -15,6 +15,7 @@
 #include "../../include/dgpu.h"
 #include "dgpu_tp.cuh"
 #include "dgpu_adjoint.cuh"
+#include "dgpu_host_ops.h"
 
 using namespace dgpu;
 
@@ -119,44 +120,6 @@ dgpu_status cuda_fail(dgpu_ctx* c, cudaError_t e, const char* what)
 			return cuda_fail((ctx), e_, #call);                \
 	} while (0)
 
-// Gauss-Jordan inverse with partial pivoting of a small row-major matrix.
-bool invert_small(int n, const double* A, double* Ainv)
-{
-	double a[kQMax * kQMax];
-	for (int i = 0; i < n * n; ++i)
-		a[i] = A[i];
-	for (int i = 0; i < n; ++i)
-		for (int j = 0; j < n; ++j)
-			Ainv[i * n + j] = (i == j) ? 1.0 : 0.0;
-	for (int col = 0; col < n; ++col) {
-		int piv = col;
-		for (int r = col + 1; r < n; ++r)
-			if (fabs(a[r * n + col]) > fabs(a[piv * n + col]))
-				piv = r;
-		if (!(fabs(a[piv * n + col]) > 1e-300))
-			return false;
-		if (piv != col)
-			for (int j = 0; j < n; ++j) {
-				double t = a[col * n + j]; a[col * n + j] = a[piv * n + j]; a[piv * n + j] = t;
-				t = Ainv[col * n + j]; Ainv[col * n + j] = Ainv[piv * n + j]; Ainv[piv * n + j] = t;
-			}
-		const double inv = 1.0 / a[col * n + col];
-		for (int j = 0; j < n; ++j) {
-			a[col * n + j] *= inv;
-			Ainv[col * n + j] *= inv;
-		}
-		for (int r = 0; r < n; ++r) {
-			if (r == col)
-				continue;
-			const double f = a[r * n + col];
-			for (int j = 0; j < n; ++j) {
-				a[r * n + j] -= f * a[col * n + j];
-				Ainv[r * n + j] -= f * Ainv[col * n + j];
-			}
-		}
-	}
-	return true;
-}
 
 template <int D, int Q, int NV>
 size_t volume_smem_bytes()
@@ -580,57 +543,11 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		c->b_adv[k] = phys->b_adv[k];
 	const int N = c->N, NF = c->NF;
 
-	// ---- 1D operators: B, B^-1, GL collocation derivative, GL boundary values ----
-	memset(&c->ops, 0, sizeof c->ops);
-	double Bm[kQMax * kQMax], Bi[kQMax * kQMax];
-	for (int i = 0; i < q * q; ++i)
-		Bm[i] = ops->cv0_vs_vc[i];
-	if (!invert_small(q, Bm, Bi)) {
+	// ---- 1D operators: B, B^-1, GL collocation derivative, GL boundary values, positivity maps ----
+	if (!derive_tp_ops(ops, d, &c->ops)) {
 		delete c;
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "cv0_vs_vc is singular");
 	}
-	for (int a = 0; a < q; ++a)
-		for (int m = 0; m < q; ++m) {
-			c->ops.B[a][m] = Bm[a * q + m];
-			c->ops.Binv[a][m] = Bi[a * q + m];
-			double s = 0.0;  // Dgl = cv1_vs_vc * B^-1
-			for (int k = 0; k < q; ++k)
-				s += ops->cv1_vs_vc[a * q + k] * Bi[k * q + m];
-			c->ops.Dgl[a][m] = s;
-			if (ops->ccSB0_vs_vs) c->ops.SB[a][m] = ops->ccSB0_vs_vs[a * q + m];
-			if (ops->ccBS0_vs_vs) c->ops.BS[a][m] = ops->ccBS0_vs_vs[a * q + m];
-		}
-	for (int s = 0; s < 2; ++s)
-		for (int m = 0; m < q; ++m) {
-			double acc = 0.0;  // l_gl(+-1) = cv0_vs_fc row * B^-1
-			for (int k = 0; k < q; ++k)
-				acc += ops->cv0_vs_fc[s * q + k] * Bi[k * q + m];
-			c->ops.lb[s][m] = acc;
-		}
-	// positivity on GL nodal values: SBg = ccSB0 B^-1, BSg = B ccBS0, and the FP32 pre-filter's error factor
-	// 2 (D (q+1) + 1) 2^-24 L^D with L the largest absolute row sum of SBg
-	double L = 0.0;
-	for (int a = 0; a < q; ++a) {
-		double row = 0.0;
-		for (int m = 0; m < q; ++m) {
-			double sbg = 0.0, bsg = 0.0;
-			for (int k = 0; k < q; ++k) {
-				sbg += c->ops.SB[a][k] * Bi[k * q + m];
-				bsg += Bm[a * q + k] * c->ops.BS[k][m];
-			}
-			c->ops.SBg[a][m] = sbg;
-			c->ops.BSg[a][m] = bsg;
-			c->ops.SBf[a][m] = (float)sbg;
-			row += fabs(sbg);
-		}
-		L = fmax(L, row);
-	}
-	c->ops.pos_err = (float)(2.0 * (d * (q + 1) + 1) * ldexp(1.0, -24) * pow(L, d));
-	for (int a = 0; a < q; ++a)
-		for (int m = 0; m < q; ++m) {
-			c->ops.BT[a][m] = c->ops.B[m][a];
-			c->ops.BinvT[a][m] = c->ops.Binv[m][a];
-		}
 
 	// ---- weights: TP products of the 1D GL rule (first direction fastest) ----
 	std::vector<double> w(N), wf(NF);
@@ -1283,7 +1200,7 @@ extern "C" dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const 
 	double Bm[kQMax * kQMax], Bi[kQMax * kQMax];
 	for (int i = 0; i < q * q; ++i)
 		Bm[i] = ops->cv0_vs_vc[i];
-	if (!invert_small(q, Bm, Bi))
+	if (!host_invert_small(q, Bm, Bi))
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "cv0_vs_vc is singular");
 	for (int a = 0; a < q; ++a)
 		for (int m = 0; m < q; ++m) {

@@ -1,0 +1,609 @@
+// Batched explicit DG residual over a mesh of several (element type, p) groups (QUAD or HEX, p = 1..4 mixed).
+//
+// Elements are stored group by group. A face between volumes of orders p_L and p_R is integrated with the face
+// cubature of order p_f = max(p_L, p_R) (the reference's face order, face_solver.c:123-132): each volume
+// writes its trace at the face's q_f = p_f + 1 GL points (tangential interpolation from its own q GL points when
+// q_f > q), the face kernel evaluates the numerical flux there, and each volume applies the transpose of that
+// interpolation before its lift. With q_f = q this reduces to the single-order kernels of dgpu_tp.cuh.
+//
+// Every kernel body is a __device__ function of (D, Q, ...) with a runtime number of elements per CTA, called
+// either by one kernel launch per group ("plain per-group" form) or by one persistent kernel that walks a tile
+// list covering all groups and dispatches on each tile's Q ("fused" form).
+#pragma once
+
+#include "dgpu_tp.cuh"
+
+namespace dgpu {
+
+struct BatchOps {
+	TPOps t;
+	double Iup[kQMax + 1][kQMax][kQMax];   // Iup[qf][i][a]: GL(q) Lagrange a at GL(qf) node i, qf >= q
+};
+static_assert(sizeof(BatchOps) % 8 == 0, "BatchOps is copied to shared memory as doubles");
+
+struct BGroup {
+	int q, n_vol, E;          // order+1, volumes, elements per CTA of the per-group form
+	int first_tile;           // first tile of this group in the fused tile list
+	long long elem0;          // first element (group-sorted element index)
+	long long state_off;      // offset of the group's first element in state-sized arrays
+	long long gmet_off;       // ... in the metric array
+	long long wj_off;         // ... in the 1/(wJ) array
+};
+
+struct BParams {
+	double b_adv[3];
+	int n_groups;
+	const BatchOps* ops;      // [group]
+	const BGroup* groups;     // [group]
+	const int4* elf;          // [element][2D]: (face, side, q_f, 0)
+	const long long* fbase;   // [face]: first face node of the face (prefix sum of q_f^(D-1))
+	const double* gmet;
+	const double* inv_wJ;
+	const double* fgeo;       // [node][D+1] blocks per face: (D+1) * fbase[f] + k * NF_f + i
+	double* traces;           // per face: 2 NV NF_f at 2 NV fbase[f]: [side][NV][NF_f]
+	double* nnf;              // per face: NV NF_f at NV fbase[f]: [NV][NF_f]
+	double* vol_gl;           // state layout
+	unsigned long long* max_bits;
+	int* err_flag;
+	unsigned long long* n_corr;
+};
+
+// Fused tile list entry: group and first element within the group.
+struct BTile {
+	int group;
+	int e0;
+};
+
+// ---------------------------------------------------------------------------------------------------------------
+// shared-memory sizes (doubles per element) of the bodies
+template <int D, int Q, int NV>
+struct BSmem {
+	static constexpr int N = TPShape<D, Q>::N;
+	static constexpr int NFQ = TPShape<D, Q>::NF;
+	static constexpr int VOL = NV * N * 2 + D * NV * N + 2 * D * NV * NFQ;   // su, st, sf, own-order traces
+	static constexpr int LIFT = 3 * NV * N + 8 + 2 * D * NV * NFQ;           // sa, sb, sc, scalars, face terms
+};
+
+// ---------------------------------------------------------------------------------------------------------------
+// Volume term + traces at each face's order
+// ---------------------------------------------------------------------------------------------------------------
+template <int D, int Q, int NV, int PDE, bool GLL_IN>
+__device__ void bvol_body(const BParams& P, const BatchOps* sops, const BGroup& G, int e0, int E,
+                          const double* __restrict__ u, double* base)
+{
+	constexpr int N = TPShape<D, Q>::N, NFQ = TPShape<D, Q>::NF;
+	constexpr int PER_E = BSmem<D, Q, NV>::VOL;
+	const int tid = threadIdx.x;
+	const int n_here = min(E, G.n_vol - e0);
+	const double* ublk = u + G.state_off + (long long)e0 * NV * N;
+	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {
+		const int e = i / (NV * N), r = i % (NV * N);
+		base[e * PER_E + r] = ublk[i];
+	}
+	__syncthreads();
+	const int e = tid / N, node = tid % N;
+	const bool active = e < n_here;
+	double* su = base + e * PER_E;
+	double* st = su + NV * N;
+	double* sf = st + NV * N;
+	double* str = sf + D * NV * N;   // [lf][NV][NFQ]
+	if (GLL_IN) {
+		tp_apply<D, Q, NV>(su, st, sf, sops->t.B, node, active);
+		if (active)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				su[k * N + node] = st[k * N + node];
+		__syncthreads();
+	}
+	const long long v = G.elem0 + e0 + e;   // group-sorted element index
+	if (active) {
+		double W[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			W[k] = su[k * N + node];
+		double g[D * D];
+		const double* gm = P.gmet + G.gmet_off + (long long)(e0 + e) * D * D * N;
+#pragma unroll
+		for (int c = 0; c < D * D; ++c)
+			g[c] = gm[c * N + node];
+		if constexpr (PDE == kEuler) {
+			double fr[D][D + 2];
+			euler_flux_ref<D>(W, g, fr);
+#pragma unroll
+			for (int j = 0; j < D; ++j)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					sf[(j * NV + k) * N + node] = fr[j][k];
+		} else {
+#pragma unroll
+			for (int j = 0; j < D; ++j) {
+				double gb = 0.0;
+#pragma unroll
+				for (int i = 0; i < D; ++i)
+					gb += g[j * D + i] * P.b_adv[i];
+				sf[j * N + node] = gb * W[0];
+			}
+		}
+		// traces at this element's own GL points, all faces, into shared memory
+		for (int it = node; it < 2 * D * NFQ; it += N) {
+			const int lf = it / NFQ, t = it % NFQ;
+			const int nd = lf >> 1, side = lf & 1;
+			const int t0 = (D == 2 ? t : t % Q), t1 = (D == 2 ? 0 : t / Q);
+			int stride_n, base_n;
+			if (D == 2) {
+				stride_n = (nd == 0 ? 1 : Q);
+				base_n = (nd == 0 ? t0 * Q : t0);
+			} else {
+				stride_n = (nd == 0 ? 1 : (nd == 1 ? Q : Q * Q));
+				base_n = (nd == 0 ? t0 * Q + t1 * Q * Q : (nd == 1 ? t0 + t1 * Q * Q : t0 + t1 * Q));
+			}
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				double s = 0.0;
+#pragma unroll
+				for (int m = 0; m < Q; ++m)
+					s += sops->t.lb[side][m] * su[k * N + base_n + m * stride_n];
+				str[(lf * NV + k) * NFQ + t] = s;
+			}
+		}
+	}
+	__syncthreads();
+	if (active) {
+		// volume term in GL space
+		double acc[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			acc[k] = 0.0;
+#pragma unroll
+		for (int j = 0; j < D; ++j) {
+			const int stride = (j == 0 ? 1 : (j == 1 ? Q : Q * Q));
+			const int a = node_coord<Q>(node, j);
+			const int b0 = node - a * stride;
+			double w[Q];
+#pragma unroll
+			for (int m = 0; m < Q; ++m)
+				w[m] = sops->t.Dgl[m][a];
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				const double* f = sf + (j * NV + k) * N + b0;
+#pragma unroll
+				for (int m = 0; m < Q; ++m)
+					acc[k] += w[m] * f[m * stride];
+			}
+		}
+		double* vg = P.vol_gl + G.state_off + (long long)(e0 + e) * NV * N;
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			vg[k * N + node] = acc[k];
+		// traces at each face's order: copy (q_f == Q) or tangential interpolation Q -> q_f
+		const int4* ef = P.elf + v * 2 * D;
+		for (int lf = 0; lf < 2 * D; ++lf) {
+			const int4 fd = ef[lf];
+			const int qf = fd.z;
+			const int nff = (D == 2 ? qf : qf * qf);
+			double* dst = P.traces + 2 * NV * P.fbase[fd.x] + (long long)fd.y * NV * nff;
+			const double* src = str + lf * NV * NFQ;
+			for (int it = node; it < NV * nff; it += N) {
+				const int k = it / nff, i = it % nff;
+				double s;
+				if (qf == Q) {
+					s = src[k * NFQ + i];
+				} else {
+					const double(*I)[kQMax] = sops->Iup[qf];
+					s = 0.0;
+					if (D == 2) {
+#pragma unroll
+						for (int a = 0; a < Q; ++a)
+							s += I[i][a] * src[k * NFQ + a];
+					} else {
+						const int i0 = i % qf, i1 = i / qf;
+#pragma unroll
+						for (int b = 0; b < Q; ++b) {
+							double r = 0.0;
+#pragma unroll
+							for (int a = 0; a < Q; ++a)
+								r += I[i0][a] * src[k * NFQ + a + Q * b];
+							s += I[i1][b] * r;
+						}
+					}
+				}
+				dst[k * nff + i] = s;
+			}
+		}
+	}
+	__syncthreads();   // shared memory is reused by the next tile
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Face numerical flux at q_f points (faces of one q_f in [f_begin, f_end) of the face list)
+// ---------------------------------------------------------------------------------------------------------------
+template <int D, int QF, int NV, int PDE, int FLUX>
+__device__ __forceinline__ void bface_node(const BParams& P, int f, int i)
+{
+	constexpr int NF = TPShape<D, QF>::NF;
+	const long long fb = P.fbase[f];
+	const double* tL = P.traces + 2 * NV * fb;
+	const double* tR = tL + NV * NF;
+	double WL[NV], WR[NV], n[D];
+#pragma unroll
+	for (int k = 0; k < NV; ++k) {
+		WL[k] = tL[k * NF + i];
+		WR[k] = tR[k * NF + i];
+	}
+	const double* fg = P.fgeo + (D + 1) * fb;
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		n[k] = fg[k * NF + i];
+	const double sc = fg[D * NF + i];
+	double* out = P.nnf + NV * fb;
+	if constexpr (PDE == kEuler) {
+		double nF[NV];
+		if constexpr (FLUX == kRoePike)
+			num_flux_roe_pike<D>(WL, WR, n, nF);
+		else
+			num_flux_lax_friedrichs<D>(WL, WR, n, nF);
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			out[k * NF + i] = nF[k] * sc;
+	} else {
+		out[i] = num_flux_upwind<D>(WL[0], WR[0], n, P.b_adv) * sc;
+	}
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Lift (with the transposed tangential interpolation from q_f) + M^-1 + residual | RK stage + positivity
+// ---------------------------------------------------------------------------------------------------------------
+template <int D, int Q, int NV, int MODE>
+__device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup& G, int e0, int E, const RkArgs& rk,
+                           double* base)
+{
+	constexpr int N = TPShape<D, Q>::N, NFQ = TPShape<D, Q>::NF;
+	constexpr int PER_E = BSmem<D, Q, NV>::LIFT;
+	const int tid = threadIdx.x;
+	const int n_here = min(E, G.n_vol - e0);
+	const int e = tid / N, node = tid % N;
+	const bool active = e < n_here;
+	double* sa = base + e * PER_E;
+	double* sb = sa + NV * N;
+	double* sc = sb + NV * N;
+	int* sscale = reinterpret_cast<int*>(sc + NV * N);
+	double* sg = sc + NV * N + 8;        // [lf][NV][NFQ]: E_lf^T-side face terms at this element's points
+	const long long v = G.elem0 + e0 + e;
+	if (active && node < 8)
+		reinterpret_cast<double*>(sscale)[node] = 0.0;
+	if (active) {
+		// face terms at the element's own points: copy (q_f == Q) or transposed interpolation q_f -> Q
+		const int4* ef = P.elf + v * 2 * D;
+		for (int lf = 0; lf < 2 * D; ++lf) {
+			const int4 fd = ef[lf];
+			const int qf = fd.z;
+			const int nff = (D == 2 ? qf : qf * qf);
+			const double* src = P.nnf + NV * P.fbase[fd.x];
+			const double sgn = (fd.y == 0 ? -1.0 : 1.0);   // side 0: rhs -= ; side 1: rhs -= (-nnf)
+			for (int it = node; it < NV * NFQ; it += N) {
+				const int k = it / NFQ, t = it % NFQ;
+				double s;
+				if (qf == Q) {
+					s = src[k * nff + t];
+				} else {
+					const double(*I)[kQMax] = sops->Iup[qf];
+					s = 0.0;
+					if (D == 2) {
+						for (int i = 0; i < qf; ++i)
+							s += I[i][t] * src[k * nff + i];
+					} else {
+						const int a = t % Q, b = t / Q;
+						for (int i1 = 0; i1 < qf; ++i1) {
+							double r = 0.0;
+							for (int i0 = 0; i0 < qf; ++i0)
+								r += I[i0][a] * src[k * nff + i0 + qf * i1];
+							s += I[i1][b] * r;
+						}
+					}
+				}
+				sg[(lf * NV + k) * NFQ + t] = sgn * s;
+			}
+		}
+	}
+	__syncthreads();
+
+	double Rg[NV];
+	if (active) {
+		const double* vg = P.vol_gl + G.state_off + (long long)(e0 + e) * NV * N;
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			Rg[k] = vg[k * N + node];
+#pragma unroll
+		for (int lf = 0; lf < 2 * D; ++lf) {
+			const int nd = lf >> 1;
+			const int a = node_coord<Q>(node, nd);
+			int t;
+			if (D == 2) {
+				t = (nd == 0 ? node_coord<Q>(node, 1) : node_coord<Q>(node, 0));
+			} else {
+				const int c0 = node_coord<Q>(node, 0), c1 = node_coord<Q>(node, 1), c2 = node_coord<Q>(node, 2);
+				t = (nd == 0 ? c1 + Q * c2 : (nd == 1 ? c0 + Q * c2 : c0 + Q * c1));
+			}
+			const double l = sops->t.lb[lf & 1][a];
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				Rg[k] += l * sg[(lf * NV + k) * NFQ + t];
+		}
+		const double iw = P.inv_wJ[G.wj_off + (long long)(e0 + e) * N + node];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			Rg[k] *= iw;
+	}
+
+	const bool need_coef = (MODE == kModeRhs) || rk.want_max;
+	unsigned long long mx = 0ull;
+	double R[NV];
+	if (need_coef) {
+		if (active)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				sa[k * N + node] = Rg[k];
+		__syncthreads();
+		tp_apply<D, Q, NV>(sa, sb, sc, sops->t.Binv, node, active);
+		if (active) {
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				R[k] = sb[k * N + node];
+				const unsigned long long bits = abs_bits(R[k]);
+				mx = bits > mx ? bits : mx;
+			}
+		}
+#pragma unroll
+		for (int off = 16; off > 0; off >>= 1) {
+			const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
+			mx = o > mx ? o : mx;
+		}
+		if ((tid & 31) == 0 && mx && P.max_bits)
+			atomicMax(P.max_bits, mx);
+		__syncthreads();
+	}
+	const long long so = G.state_off + (long long)(e0 + e) * NV * N + node;
+	if constexpr (MODE == kModeRhs) {
+		if (active)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				rk.rhs[so + (long long)k * N] = R[k];
+	} else {
+		double snew[NV];
+		if (active) {
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				const double s = rk.u[so + (long long)k * N];
+				if (rk.stage == 0) {
+					rk.u0[so + (long long)k * N] = s;
+					snew[k] = s + rk.dt * Rg[k];
+				} else if (rk.stage == 1) {
+					snew[k] = (1.0 / 4.0) * (3.0 * rk.u0[so + (long long)k * N] + s + rk.dt * Rg[k]);
+				} else {
+					snew[k] = (1.0 / 3.0) * (rk.u0[so + (long long)k * N] + 2.0 * s + 2.0 * rk.dt * Rg[k]);
+				}
+			}
+		}
+		if (rk.positivity) {
+			if (active)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					sb[k * N + node] = snew[k];
+			__syncthreads();
+			float* xf = reinterpret_cast<float*>(sa);
+			float* tf = xf + NV * N;
+			float* tmpf = reinterpret_cast<float*>(sc);
+			if (active) {
+#pragma unroll
+				for (int k = 0; k < NV; ++k) {
+					const float x = (float)snew[k];
+					xf[k * N + node] = x;
+					atomicMax(&sscale[k], __float_as_int(fabsf(x)));
+				}
+			}
+			__syncthreads();
+			tp_apply<D, Q, NV>(xf, tf, tmpf, sops->t.SBf, node, active);
+			bool safe = true;
+			if (active) {
+				const float err = sops->t.pos_err;
+				const float rho_lo = tf[node] - err * __int_as_float(sscale[0]);
+				safe = rho_lo > 1e-6f * __int_as_float(sscale[0]) + 1e-12f;
+				if (safe) {
+					float m2 = 0.f;
+#pragma unroll
+					for (int k = 0; k < D; ++k) {
+						const float mk = fabsf(tf[(1 + k) * N + node]) + err * __int_as_float(sscale[1 + k]);
+						m2 += mk * mk;
+					}
+					const float E_lo = tf[(D + 1) * N + node] - err * __int_as_float(sscale[D + 1]);
+					const float ke = 0.5f * m2 / rho_lo;
+					safe = 0.4f * (E_lo - ke) > 1e-5f * (fabsf(E_lo) + ke) + 1e-12f;
+				}
+			}
+			const int unsafe = __syncthreads_or(active && !safe);
+			if (unsafe) {
+				int flag = 0;
+				const bool corr =
+					tp_positivity_exact<D, Q, NV>(sops->t.SBg, sops->t.BSg, sb, sc, sa, node, active, &flag);
+				if (flag)
+					atomicExch(P.err_flag, 1);
+				if (corr) {
+					if (node == 0)
+						atomicAdd(P.n_corr, 1ull);
+#pragma unroll
+					for (int k = 0; k < NV; ++k)
+						snew[k] = sb[k * N + node];
+				}
+			}
+		}
+		if (active)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				rk.u[so + (long long)k * N] = snew[k];
+	}
+	__syncthreads();   // shared memory is reused by the next tile
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Kernels: per group, and fused persistent over all groups
+// ---------------------------------------------------------------------------------------------------------------
+__device__ __forceinline__ void load_batch_ops(BatchOps* sops, const BatchOps* g)
+{
+	for (int i = threadIdx.x; i < (int)(sizeof(BatchOps) / 8); i += blockDim.x)
+		reinterpret_cast<double*>(sops)[i] = reinterpret_cast<const double*>(g)[i];
+}
+
+template <int D, int Q, int NV, int PDE, bool GLL_IN>
+__global__ void __launch_bounds__(256) bvol_group_kernel(const BParams P, int g, const double* __restrict__ u)
+{
+	extern __shared__ double smem[];
+	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
+	const BGroup G = P.groups[g];
+	load_batch_ops(sops, &P.ops[g]);
+	if (blockIdx.x == 0 && threadIdx.x == 0 && P.max_bits && G.elem0 == 0)   // first non-empty group
+		*P.max_bits = 0ull;
+	__syncthreads();
+	bvol_body<D, Q, NV, PDE, GLL_IN>(P, sops, G, blockIdx.x * G.E, G.E, u, smem + sizeof(BatchOps) / 8);
+}
+
+template <int D, int Q, int NV, int MODE>
+__global__ void __launch_bounds__(256, 2) blift_group_kernel(const BParams P, int g, const RkArgs rk)
+{
+	extern __shared__ double smem[];
+	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
+	const BGroup G = P.groups[g];
+	load_batch_ops(sops, &P.ops[g]);
+	__syncthreads();
+	blift_body<D, Q, NV, MODE>(P, sops, G, blockIdx.x * G.E, G.E, rk, smem + sizeof(BatchOps) / 8);
+}
+
+template <int D, int QF, int NV, int PDE, int FLUX>
+__global__ void __launch_bounds__(256) bface_group_kernel(const BParams P, const int* faces, int n)
+{
+	constexpr int NF = TPShape<D, QF>::NF;
+	const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= (long long)n * NF)
+		return;
+	bface_node<D, QF, NV, PDE, FLUX>(P, faces[gid / NF], (int)(gid % NF));
+}
+
+// Fused persistent kernels: a CTA walks the tile list (grid-stride) and dispatches on the tile's order; the
+// operator set is reloaded into shared memory when the group changes.
+template <int D, int NV, int PDE, bool GLL_IN>
+__global__ void __launch_bounds__(256) bvol_fused_kernel(const BParams P, const BTile* tiles, int n_tiles,
+                                                           const double* __restrict__ u)
+{
+	extern __shared__ double smem[];
+	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
+	double* base = smem + sizeof(BatchOps) / 8;
+	if (blockIdx.x == 0 && threadIdx.x == 0 && P.max_bits)
+		*P.max_bits = 0ull;
+	int cur = -1;
+	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+		const BTile tl = tiles[t];
+		if (tl.group != cur) {
+			__syncthreads();
+			load_batch_ops(sops, &P.ops[tl.group]);
+			cur = tl.group;
+			__syncthreads();
+		}
+		const BGroup G = P.groups[tl.group];
+		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
+		switch (G.q) {
+		case 2: bvol_body<D, 2, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 3: bvol_body<D, 3, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 4: bvol_body<D, 4, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		default: bvol_body<D, 5, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		}
+	}
+}
+
+template <int D, int NV, int MODE>
+__global__ void __launch_bounds__(256, 2) blift_fused_kernel(const BParams P, const BTile* tiles, int n_tiles,
+                                                               const RkArgs rk)
+{
+	extern __shared__ double smem[];
+	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
+	double* base = smem + sizeof(BatchOps) / 8;
+	int cur = -1;
+	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+		const BTile tl = tiles[t];
+		if (tl.group != cur) {
+			__syncthreads();
+			load_batch_ops(sops, &P.ops[tl.group]);
+			cur = tl.group;
+			__syncthreads();
+		}
+		const BGroup G = P.groups[tl.group];
+		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
+		switch (G.q) {
+		case 2: blift_body<D, 2, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 3: blift_body<D, 3, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 4: blift_body<D, 4, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		default: blift_body<D, 5, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		}
+	}
+}
+
+// Faces of all orders: the face list is sorted by q_f; face_q_begin[qf] gives each order's range.
+template <int D, int NV, int PDE, int FLUX>
+__global__ void __launch_bounds__(256) bface_fused_kernel(const BParams P, const int* faces, const int* qf_begin,
+                                                            long long n_items)
+{
+	for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < n_items;
+	     it += (long long)gridDim.x * blockDim.x) {
+		// items are laid out order by order: [qf=2 faces x NF(2)] [qf=3 ...] ...
+		long long off = 0;
+		int qf = 2;
+		for (; qf <= kQMax; ++qf) {
+			const int nf = (D == 2 ? qf : qf * qf);
+			const long long cnt = (long long)(qf_begin[qf + 1] - qf_begin[qf]) * nf;
+			if (it < off + cnt)
+				break;
+			off += cnt;
+		}
+		if (qf > kQMax)
+			return;
+		const int nf = (D == 2 ? qf : qf * qf);
+		const long long local = it - off;
+		const int f = faces[qf_begin[qf] + local / nf], i = (int)(local % nf);
+		switch (qf) {
+		case 2: bface_node<D, 2, NV, PDE, FLUX>(P, f, i); break;
+		case 3: bface_node<D, 3, NV, PDE, FLUX>(P, f, i); break;
+		case 4: bface_node<D, 4, NV, PDE, FLUX>(P, f, i); break;
+		default: bface_node<D, 5, NV, PDE, FLUX>(P, f, i); break;
+		}
+	}
+}
+
+template <int D, int Q, int NV, bool TO_GL>
+__global__ void __launch_bounds__(256) bconvert_group_kernel(const BParams P, int g, const double* __restrict__ in,
+                                                               double* __restrict__ out)
+{
+	extern __shared__ double smem[];
+	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
+	double* base = smem + sizeof(BatchOps) / 8;
+	const BGroup G = P.groups[g];
+	load_batch_ops(sops, &P.ops[g]);
+	constexpr int N = TPShape<D, Q>::N;
+	constexpr int PER_E = 3 * NV * N;
+	const int E = G.E, e0 = blockIdx.x * E, n_here = min(E, G.n_vol - e0);
+	const double* src = in + G.state_off + (long long)e0 * NV * N;
+	for (int i = threadIdx.x; i < n_here * NV * N; i += blockDim.x) {
+		const int e = i / (NV * N), r = i % (NV * N);
+		base[e * PER_E + r] = src[i];
+	}
+	__syncthreads();
+	const int e = threadIdx.x / N, node = threadIdx.x % N;
+	const bool active = e < n_here;
+	double* sa = base + e * PER_E;
+	double* sb = sa + NV * N;
+	double* sc = sb + NV * N;
+	tp_apply<D, Q, NV>(sa, sb, sc, TO_GL ? sops->t.B : sops->t.Binv, node, active);
+	if (active)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			out[G.state_off + (long long)(e0 + e) * NV * N + (long long)k * N + node] = sb[k * N + node];
+}
+
+}  // namespace dgpu

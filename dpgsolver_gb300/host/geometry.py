@@ -34,8 +34,10 @@ def apply_nodes(op: np.ndarray, x: np.ndarray) -> np.ndarray:
 
 
 class TPGeometry:
-    def __init__(self, mesh, ops: TPOperatorSet, deform=None, curved: bool | None = None):
-        """deform: callable (m, d) physical -> (m, d) physical applied to the affine element map, or None."""
+    def __init__(self, mesh, ops: TPOperatorSet, deform=None, curved: bool | None = None, vols=None):
+        """deform: callable (m, d) physical -> (m, d) physical applied to the affine element map, or None.
+        vols: indices of the volumes to compute (all volumes and their faces when None; the volume terms only
+        otherwise, as for one (type, p) group of a mixed-order mesh)."""
         d = mesh.d
         self.d = d
         if curved is None:
@@ -45,11 +47,13 @@ class TPGeometry:
         self.p_g = p_g
         x_g, _ = gauss_lobatto(p_g + 1)
         xi_g = tp_nodes(x_g, d)                      # geometry == metric nodes (p_m = p_g)
-        nv = mesh.n_volumes
+        lo = mesh.vertices_lo if vols is None else mesh.vertices_lo[np.asarray(vols)]
+        nv = len(lo)
         n_g = len(xi_g)
+        self.x_g = x_g
 
         # geometry node coordinates (nv, n_g, d)
-        X = mesh.vertices_lo[:, None, :] + 0.5 * (xi_g[None, :, :] + 1.0) * mesh.h[None, None, :]
+        X = lo[:, None, :] + 0.5 * (xi_g[None, :, :] + 1.0) * mesh.h[None, None, :]
         if deform is not None:
             X = deform(X.reshape(-1, d)).reshape(nv, n_g, d)
         self.X_geom = X
@@ -101,6 +105,8 @@ class TPGeometry:
         self.jacobian_det_vc = detJ                                   # (nv, n_vc)
         # xyz at vc (advection flux input, reference constructor_xyz_vc)
         self.xyz_vc = apply_nodes(I_mc, X)
+        if vols is not None:
+            return
 
         # faces: metrics of the side-0 volume at its face cubature nodes
         nf = mesh.n_faces

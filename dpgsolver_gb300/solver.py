@@ -196,6 +196,143 @@ class Simulation:
         return tot.value, cnt.value
 
 
+class BatchSimulation:
+    """One batched dgpu context for a mixed-order TP mesh (dpgsolver_gb300.host.mixed.MixedTPProblem, or a uniform
+    DGProblem as a one-group mesh). States are flat arrays in volume-list order (the problem's layout)."""
+
+    def __init__(self, prob, stream=None):
+        from .host.problem import flat_arrays
+
+        lib = _lib.load()
+        fl = flat_arrays(prob)
+        d = prob.d
+        keep = []
+
+        def arr(a, dtype=np.float64):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            keep.append(a)
+            return a
+
+        phys = _lib.Physics()
+        phys.d, phys.pde, phys.num_flux = d, prob.pde, prob.num_flux
+        phys.positivity = 1 if prob.positivity else 0
+        for k in range(3):
+            phys.b_adv[k] = float(prob.b_adv[k])
+        groups = fl["groups"]
+        tps = (_lib.TPOperators * len(groups))()
+        for g, ops in enumerate(groups):
+            tps[g].elem_type, tps[g].p = ops.e_type, ops.p
+            tps[g].cv0_vs_vc = _dp(arr(ops.cv0_1d))
+            tps[g].cv1_vs_vc = _dp(arr(ops.cv1_1d))
+            tps[g].cv0_vs_fc = _dp(arr(ops.cv0_bnd_1d))
+            tps[g].w_vc = _dp(arr(ops.w_vc_1d))
+            tps[g].ccSB0_vs_vs = _dp(arr(ops.ccSB0_1d))
+            tps[g].ccBS0_vs_vs = _dp(arr(ops.ccBS0_1d))
+        mesh = prob.mesh
+        m = _lib.Mesh()
+        m.n_volumes = mesh.n_volumes
+        m.metrics_vc = _dp(arr(fl["metrics_vc"]))
+        m.jacobian_det_vc = _dp(arr(fl["jacobian_det_vc"]))
+        m.n_faces = mesh.n_faces
+        m.face_vol = _ip(arr(mesh.face_vol, np.int32))
+        m.face_lf = _ip(arr(mesh.face_lf, np.int32))
+        m.nc_fc = _ip(arr(fl["nc_fc"], np.int32))
+        m.normals_fc = _dp(arr(fl["normals_fc"]))
+        m.jacobian_det_fc = _dp(arr(fl["jacobian_det_fc"]))
+        vg = arr(fl["vol_group"], np.int32)
+        h = ctypes.c_void_p()
+        check(lib.dgpu_batch_create(ctypes.byref(phys), len(groups), tps, _ip(vg), ctypes.byref(m),
+                                    ctypes.byref(h)), None, batch=True)
+        self._lib = lib
+        self._h = h
+        self.prob = prob
+        n = ctypes.c_size_t()
+        check(lib.dgpu_batch_state_size(h, ctypes.byref(n)), h, batch=True)
+        self.n_state = n.value
+        self.shape = np.shape(fl["sol"]) if np.ndim(prob.sol) == 1 else prob.sol.shape
+        if stream is not None:
+            check(lib.dgpu_batch_set_stream(h, ctypes.c_void_p(stream)), h, batch=True)
+        self.upload_state(prob.sol)
+
+    def _check(self, st):
+        check(st, self._h, batch=True)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.dgpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload_state(self, sol):
+        s = np.ascontiguousarray(sol, dtype=np.float64)
+        if s.size != self.n_state:
+            raise ValueError(f"state has {s.size} values, the mesh {self.n_state}")
+        self._check(self._lib.dgpu_batch_upload_state(self._h, _dp(s)))
+
+    @property
+    def sol_coef(self):
+        out = np.empty(self.shape)
+        self._check(self._lib.dgpu_batch_download_state(self._h, _dp(out)))
+        return out
+
+    @property
+    def rhs(self):
+        out = np.empty(self.shape)
+        self._check(self._lib.dgpu_batch_download_rhs(self._h, _dp(out)))
+        return out
+
+    def compute_rhs(self, want_max: bool = True):
+        mx = ctypes.c_double()
+        self._check(self._lib.dgpu_batch_compute_rhs(self._h, ctypes.byref(mx) if want_max else None))
+        return mx.value if want_max else None
+
+    def ssp_rk3_steps(self, dt: float, n_steps: int = 1, want_max: bool = True):
+        mx = ctypes.c_double()
+        self._check(self._lib.dgpu_batch_ssp_rk3_steps(self._h, float(dt), int(n_steps),
+                                                       ctypes.byref(mx) if want_max else None))
+        return mx.value if want_max else None
+
+    @property
+    def fused(self) -> bool:
+        v = ctypes.c_int()
+        self._check(self._lib.dgpu_batch_get_mode(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
+    @fused.setter
+    def fused(self, on: bool):
+        self._check(self._lib.dgpu_batch_set_mode(self._h, 1 if on else 0))
+
+    def set_graphs(self, enable: bool):
+        """Replay RK steps from a captured CUDA graph (default) or launch every kernel from the host."""
+        self._check(self._lib.dgpu_batch_set_graphs(self._h, 1 if enable else 0))
+
+    def set_group_tile(self, group: int, elements_per_cta: int):
+        self._check(self._lib.dgpu_batch_set_group_tile(self._h, int(group), int(elements_per_cta)))
+
+    def autotune(self, dt: float, reps: int = 3) -> str:
+        buf = ctypes.create_string_buffer(8192)
+        self._check(self._lib.dgpu_batch_autotune(self._h, float(dt), int(reps), buf, len(buf)))
+        return buf.value.decode()
+
+    def kernel_launches(self) -> int:
+        n = ctypes.c_longlong()
+        self._check(self._lib.dgpu_batch_kernel_launches(self._h, ctypes.byref(n)))
+        return n.value
+
+    def positivity_corrections(self) -> int:
+        n = ctypes.c_longlong()
+        self._check(self._lib.dgpu_batch_positivity_corrections(self._h, ctypes.byref(n)))
+        return n.value
+
+
 def compute_rhs_dg(sim: Simulation) -> float:
     """compute_rhs_dg (solvers/dg/solve_dg.c:130-136): residual of sim's state into sim's rhs; max |rhs|."""
     return sim.compute_rhs()

@@ -182,6 +182,57 @@ const char* dgpu_last_error(const dgpu_ctx* ctx);
 dgpu_status dgpu_probe_fp64(int iters, double* tflops);
 const char* dgpu_status_string(dgpu_status st);
 
+/* ---- Batched residual over a mixed-order mesh ------------------------------------------------------------------
+ * One context for a mesh whose volumes belong to several (element type, p) groups: QUAD (d = 2) or HEX (d = 3),
+ * p = 1..4, one group per p. Replaces the same reference entry points as the uniform context above
+ * (compute_rhs_dg, solve_dg.c:130-136; time_step_ssp_rk_33, solve_explicit.c:252-301) for a mesh with p
+ * adaptation, where the reference's element loops visit volumes of different operator sets
+ * (get_operator__cv0_vs_vc_T ... indexed by p, compute_volume_rlhs_dg_T.c) and integrates each face with the
+ * cubature of order p_f = max(p_L, p_R) (face_solver.c:123-132).
+ *
+ *   ops[g]            the TP operator set of group g (distinct p per group)
+ *   vol_group[v]      group of volume v
+ *   mesh              as for dgpu_create with ragged blocks: volume v holds n_vc(v) = q(v)^d nodes, face f
+ *                     holds n_fc(f) = q_f^(d-1) nodes with q_f = max(q(L), q(R)); every array concatenates the
+ *                     blocks in list order. nc_fc must be NULL or the identity (aligned faces); periodic meshes
+ *                     only (no boundary faces).
+ *
+ * The state is the volumes' (n_vs(v) x n_var) column-major sol_coef blocks concatenated in volume-list order.
+ * On the device the volumes are stored group by group; uploads and downloads permute. Each RK stage runs in one
+ * of two forms: one launch per group for the volume and lift kernels and one per face order for the face kernel
+ * (form 0), or one persistent launch each over a tile list that covers every group (form 1); a step is replayed
+ * from a captured CUDA graph in either form. No reference counterpart for the forms, the tile size or the
+ * autotuner. */
+typedef struct dgpu_batch dgpu_batch;
+dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu_tp_operators* ops,
+                              const int* vol_group, const dgpu_mesh* mesh, dgpu_batch** out);
+dgpu_status dgpu_batch_destroy(dgpu_batch* b);
+/* Text of the last error of b (of the last failed dgpu_batch_create when b is NULL). */
+const char* dgpu_batch_last_error(const dgpu_batch* b);
+dgpu_status dgpu_batch_state_size(const dgpu_batch* b, size_t* n_doubles);
+dgpu_status dgpu_batch_upload_state(dgpu_batch* b, const double* sol);   /* host, list order; synchronous */
+dgpu_status dgpu_batch_download_state(dgpu_batch* b, double* sol);
+dgpu_status dgpu_batch_download_rhs(dgpu_batch* b, double* rhs);
+/* compute_rhs_dg on the device state; max_rhs as for dgpu_compute_rhs. */
+dgpu_status dgpu_batch_compute_rhs(dgpu_batch* b, double* max_rhs);
+/* n_steps SSP-RK3 steps (positivity included), graph-replayed. */
+dgpu_status dgpu_batch_ssp_rk3_steps(dgpu_batch* b, double dt, int n_steps, double* max_rhs);
+/* Form of the stages: 0 = one launch per group / face order, 1 = fused persistent launches. */
+dgpu_status dgpu_batch_set_mode(dgpu_batch* b, int fused);
+dgpu_status dgpu_batch_get_mode(const dgpu_batch* b, int* fused);
+/* 1 (default): RK steps replay a captured CUDA graph; 0: every kernel is launched from the host each step. */
+dgpu_status dgpu_batch_set_graphs(dgpu_batch* b, int enable);
+/* Elements per CTA of group g in form 0 (1 .. 256 / q^d). */
+dgpu_status dgpu_batch_set_group_tile(dgpu_batch* b, int group, int elements_per_cta);
+/* Times every group's volume + lift kernels for each elements-per-CTA candidate (256/q^d, halved down to 1)
+ * and keeps the fastest, then times `reps` graph-replayed RK steps of size dt in both forms and keeps the
+ * faster. The device state is restored afterwards. A text report of the timings goes to `report`
+ * (may be NULL). */
+dgpu_status dgpu_batch_autotune(dgpu_batch* b, double dt, int reps, char* report, size_t report_len);
+dgpu_status dgpu_batch_kernel_launches(const dgpu_batch* b, long long* n);
+dgpu_status dgpu_batch_set_stream(dgpu_batch* b, void* cuda_stream);
+dgpu_status dgpu_batch_positivity_corrections(dgpu_batch* b, long long* n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,3 +122,64 @@ def test_rk3_step_consistent_with_residual():
     r3, _ = o.compute_rhs(r2)
     taylor = u + dt * r1 + dt ** 2 / 2 * r2 + dt ** 3 / 6 * r3
     assert np.max(np.abs(s - taylor)) < 1e-13
+
+
+# ---- mixed-order meshes (p per volume, faces at p_f = max(p_L, p_R)) ----------------------------------------------
+
+def _mixed_cases():
+    from dpgsolver_gb300.host import mixed as M
+    return [lambda: M.mixed_euler(3, 3, seed=0), lambda: M.mixed_euler(2, 5, seed=1),
+            lambda: M.mixed_advection_2d(5), lambda: M.mixed_vortex_2d(5)]
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_mixed_conservation(k):
+    """Face fluxes at p_f telescope across volumes of different p: the sum of raw residuals vanishes."""
+    prob = _mixed_cases()[k]()
+    o = oracle.Oracle(prob)
+    raw = o.compute_rhs_raw(prob.sol)
+    tot = np.zeros(prob.n_var)
+    scale = np.zeros(prob.n_var)
+    for v in range(prob.n_volumes):
+        b = prob.block(raw, v)
+        tot += b.sum(axis=1)
+        scale += np.abs(b).sum(axis=1)
+    assert np.all(np.abs(tot) <= 1e-13 * scale.max())
+
+
+def test_mixed_free_stream_on_straight_mesh():
+    from dpgsolver_gb300.host import mixed as M
+    prob = M.mixed_euler(3, 3, seed=0)
+    s = prob.sol.copy()
+    for v in range(prob.n_volumes):
+        b = prob.block(s, v)
+        for j, val in enumerate([1.0, 0.3, -0.2, 0.1, 2.5]):
+            b[j] = val
+    _, mx = oracle.Oracle(prob).compute_rhs(s)
+    assert mx < 1e-11
+
+
+def test_mixed_layout():
+    from dpgsolver_gb300.host import mixed as M
+    prob = M.mixed_euler(3, 4, seed=0)
+    fl = prob.flat()
+    q = np.array([prob.groups[g].q for g in prob.vol_group])
+    assert fl["sol"].size == np.sum(5 * q ** 3)
+    assert fl["metrics_vc"].size == np.sum(9 * q ** 3)
+    assert np.array_equal(prob.face_q, np.maximum(q[prob.mesh.face_vol[:, 0]], q[prob.mesh.face_vol[:, 1]]))
+    assert fl["jacobian_det_fc"].size == np.sum(prob.face_q.astype(np.int64) ** 2)
+    assert sorted(set(int(p) for p in prob.p_vol)) == [1, 2, 3, 4]
+
+
+def test_mixed_complex_step_matches_central_differences():
+    from dpgsolver_gb300.host import mixed as M
+    prob = M.mixed_euler(3, 3, seed=0)
+    o = oracle.Oracle(prob)
+    rng = np.random.default_rng(2)
+    base = prob.sol + 1e-2 * rng.standard_normal(prob.sol.shape)
+    dirn = rng.standard_normal(prob.sol.shape)
+    h = 1e-30
+    _, ri = o.compute_rhs_cmplx(base, h * dirn)
+    eps = 1e-6
+    jv_fd = (o.compute_rhs(base + eps * dirn)[0] - o.compute_rhs(base - eps * dirn)[0]) / (2 * eps)
+    assert np.max(np.abs(ri / h - jv_fd)) <= 1e-6 * np.max(np.abs(ri / h))
