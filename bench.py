@@ -50,6 +50,8 @@ WORKLOADS = {
                       desc="3D Euler curved HEX 32^3 p3 Roe-Pike"),
     "vortex2d": dict(kind="euler_vortex_2d", n=64, p=3, flux="roe_pike",
                      desc="2D Euler curved QUAD 64^2 p3 Roe-Pike isentropic vortex"),
+    "mixed3d": dict(kind="mixed", n=58, p=None, flux="roe_pike",
+                    desc="3D Euler mixed-order HEX 58^3 unit cube, p uniform in {1,2,3,4} (seed 0), Roe-Pike"),
 }
 
 
@@ -207,6 +209,19 @@ def run_ours(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     w = WORKLOADS[args.workload]
+    if w["kind"] == "mixed":
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        if args.only_rk:
+            return mixed_only_rk(torch, stream, args)
+        mx = mixed_measurements(torch, stream, args)
+        best = max(mx["forms"], key=lambda k: mx["forms"][k]["value"])
+        return {"metric": "DOF-residual-evals/sec FP64 (batched graph vs plain per-group) at <=1e-12; %HBM peak",
+                "value": mx["forms"][best]["value"], "unit": "DOF-residual-evals/s", "n_gpus": world,
+                "steps": mx["steps"], "warmup": args.warmup, "ms_per_step": mx["forms"][best]["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded p per volume, seeded sinusoidal state)",
+                "config": {"workload": mx["workload"], "form": best}, "mixed": mx}
     t0 = time.time()
     prob = make_problem(w, n=args.n)
     setup_s = time.time() - t0
@@ -388,9 +403,9 @@ def adjoint_measurements(torch, sim, prob, args):
 def mixed_measurements(torch, stream, args):
     """Batched mixed-order workload: periodic unit cube of n^3 HEX volumes (n = 58: 195,112 volumes), p drawn
     uniformly from {1,2,3,4} with seed 0, Roe-Pike, a seeded smooth sinusoidal state around a Mach 0.5 free stream.
-    SSP-RK3 steps of the whole mesh in four forms: one launch per group and face order from the host (plain),
-    the same launches replayed from a CUDA graph, the fused persistent launches replayed from a graph, and the
-    autotuned choice."""
+    SSP-RK3 steps of the whole mesh in five forms: one launch per group and face order from the host (plain),
+    the same launches replayed from a CUDA graph, the fused persistent launches replayed from a graph, the
+    per-group launches on parallel graph branches, and the autotuned choice (elements per CTA and form)."""
     from dpgsolver_gb300.host.mixed import mixed_euler
     from dpgsolver_gb300.solver import BatchSimulation
     t0 = time.time()
@@ -401,8 +416,8 @@ def mixed_measurements(torch, stream, args):
     n_steps = max(3, min(args.steps, 20))
     out = {}
 
-    def run(label, fused, graphs):
-        sim.fused = fused
+    def run(label, form, graphs):
+        sim.form = form
         sim.set_graphs(graphs)
         sim.upload_state(prob.sol)
         sim.ssp_rk3_steps(dt, max(args.warmup, 3), want_max=False)
@@ -411,13 +426,14 @@ def mixed_measurements(torch, stream, args):
         out[label] = {"value": 3 * ns * n_steps / (ms * 1e-3), "ms_per_step": ms / n_steps,
                       "launches_per_step": (sim.kernel_launches() - l0) / n_steps}
 
-    run("plain_per_group", False, False)
-    run("per_group_graph", False, True)
-    run("fused_graph", True, True)
+    run("plain_per_group", "plain", False)
+    run("per_group_graph", "plain", True)
+    run("fused_graph", "fused", True)
+    run("branches_graph", "branches", True)
     sim.upload_state(prob.sol)
     report = sim.autotune(dt, reps=3)
-    tuned_fused = sim.fused
-    run("autotuned_graph", tuned_fused, True)
+    tuned_form = sim.form
+    run("autotuned_graph", tuned_form, True)
     q = np.array([prob.groups[g].q for g in prob.vol_group])
     flops = sum(flops_per_element(3, int(qq), 5, "roe_pike", coef_io=False) * int(np.sum(q == qq))
                 for qq in np.unique(q))
@@ -437,8 +453,9 @@ def mixed_measurements(torch, stream, args):
         "unit": "DOF-residual-evals/s", "steps": n_steps, "dt": dt,
         "forms": out,
         "speedup_fused_graph_vs_plain": out["fused_graph"]["value"] / out["plain_per_group"]["value"],
+        "speedup_branches_graph_vs_plain": out["branches_graph"]["value"] / out["plain_per_group"]["value"],
         "speedup_best_vs_plain": out[best]["value"] / out["plain_per_group"]["value"],
-        "autotune": {"fused": bool(tuned_fused), "report": report},
+        "autotune": {"form": tuned_form, "report": report},
         "fp64_pipe": {"flops_per_stage": flops, "achieved_tflops": flops / stage_s / 1e12,
                       "peak_tflops": fp64_peak.value, "frac": flops / stage_s / 1e12 / fp64_peak.value,
                       "form": best, "note": "flops counted per element at its own order (face interpolation to "
@@ -449,6 +466,23 @@ def mixed_measurements(torch, stream, args):
     }
     sim.close()
     return res
+
+
+def mixed_only_rk(torch, stream, args):
+    """One form of the mixed-order stages, graph-replayed RK steps only (profiling)."""
+    from dpgsolver_gb300.host.mixed import mixed_euler
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = mixed_euler(3, args.mixed_n, seed=0)
+    sim = BatchSimulation(prob, stream=stream.cuda_stream)
+    sim.form = {"plain": "plain", "per_group_graph": "plain", "fused": "fused",
+                "branches": "branches"}[args.mixed_form]
+    sim.set_graphs(args.mixed_form != "plain")
+    sim.ssp_rk3_steps(prob.dt, max(args.warmup, 3), want_max=False)
+    ms = _timed(torch, stream, lambda: sim.ssp_rk3_steps(prob.dt, 1, want_max=False), args.steps)
+    sim.close()
+    return {"metric": f"DOF-residual-evals/sec (mixed-order SSP-RK3 stages, {args.mixed_form})",
+            "value": 3 * prob.n_state * args.steps / (ms * 1e-3), "unit": "DOF-residual-evals/s",
+            "ms_per_step": ms / args.steps, "n_state": prob.n_state, "elements": prob.n_volumes}
 
 
 def _oracle_worker(args):
@@ -540,6 +574,8 @@ def main():
     ap.add_argument("--adjoint-budget-gb", type=float, default=4.0)
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched mixed-order measurements")
     ap.add_argument("--mixed-n", type=int, default=58, help="volumes per direction of the mixed-order mesh")
+    ap.add_argument("--mixed-form", choices=["plain", "per_group_graph", "fused", "branches"], default="fused",
+                    help="form of the mixed-order stages for --workload mixed3d --only-rk")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -68,11 +68,13 @@ struct dgpu_batch {
 	cudaStream_t stream = nullptr;
 	bool own_stream = false;
 	bool coef_valid = true, gl_valid = false;
-	int mode = 0;   // 0: one launch per group and face order; 1: fused persistent launches
+	int mode = 0;   // 0: one launch per group and face order; 1: fused persistent launches; 2: as 0 on parallel branches
+	cudaStream_t aux[kQMax] = {nullptr};   // branches of form 2
+	cudaEvent_t ev_fork = nullptr, ev_join[kQMax] = {nullptr};
 	bool use_graphs = true;
-	cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [mode][want_max]
-	double graph_dt[2][2] = {{0, 0}, {0, 0}};
-	long long graph_launches[2][2] = {{0, 0}, {0, 0}};                         // kernels per replay
+	cudaGraphExec_t graph[3][2] = {};   // [mode][want_max]
+	double graph_dt[3][2] = {};
+	long long graph_launches[3][2] = {};   // kernels per replay
 	long long launches = 0;
 	std::string err;
 
@@ -345,6 +347,14 @@ void free_batch(dgpu_batch* c)
 			cudaFree(p);
 	if (c->own_stream && c->stream)
 		cudaStreamDestroy(c->stream);
+	for (int j = 0; j < kQMax; ++j) {
+		if (c->aux[j])
+			cudaStreamDestroy(c->aux[j]);
+		if (c->ev_join[j])
+			cudaEventDestroy(c->ev_join[j]);
+	}
+	if (c->ev_fork)
+		cudaEventDestroy(c->ev_fork);
 }
 
 template <typename T>
@@ -356,6 +366,31 @@ cudaError_t upload_vec(T** dst, const std::vector<T>& src)
 	return cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
+// Form 2: the calls of `launch(j, i)` for i in items run on the branch streams, forked from and joined back into
+// the context's stream (under stream capture: parallel branches of the graph).
+template <typename F>
+dgpu_status on_branches(dgpu_batch* c, int n_items, F launch)
+{
+	cudaStream_t main = c->stream;
+	BATCH_CUDA(c, cudaEventRecord(c->ev_fork, main));
+	int j = 0;
+	for (int i = 0; i < n_items; ++i) {
+		cudaStream_t br = c->aux[j];
+		BATCH_CUDA(c, cudaStreamWaitEvent(br, c->ev_fork, 0));
+		c->stream = br;
+		const long long before = c->launches;
+		cudaError_t e = launch(i);
+		c->stream = main;
+		BATCH_CUDA(c, e);
+		if (c->launches == before)   // nothing launched (empty group or face order): no branch
+			continue;
+		BATCH_CUDA(c, cudaEventRecord(c->ev_join[j], br));
+		BATCH_CUDA(c, cudaStreamWaitEvent(main, c->ev_join[j], 0));
+		++j;
+	}
+	return DGPU_OK;
+}
+
 // One residual on GLL coefficients, or one RK stage on GL nodal values.
 dgpu_status enqueue_stage(dgpu_batch* c, bool rhs_mode, double dt, int stage, int want_max)
 {
@@ -364,6 +399,15 @@ dgpu_status enqueue_stage(dgpu_batch* c, bool rhs_mode, double dt, int stage, in
 		BATCH_CUDA(c, c->fused_vol(c, rhs_mode));
 		BATCH_CUDA(c, c->fused_face(c));
 		BATCH_CUDA(c, c->fused_lift(c, lmode, dt, stage, want_max));
+	} else if (c->mode == 2) {
+		dgpu_status st;
+		if ((st = on_branches(c, c->n_groups, [&](int g) { return c->gl[g].vol(c, g, rhs_mode); })) != DGPU_OK)
+			return st;
+		if ((st = on_branches(c, kQMax - 1, [&](int i) { return c->face_q(c, i + 2); })) != DGPU_OK)
+			return st;
+		if ((st = on_branches(c, c->n_groups,
+		                      [&](int g) { return c->gl[g].lift(c, g, lmode, dt, stage, want_max); })) != DGPU_OK)
+			return st;
 	} else {
 		for (int g = 0; g < c->n_groups; ++g)
 			BATCH_CUDA(c, c->gl[g].vol(c, g, rhs_mode));
@@ -655,6 +699,11 @@ dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu
 	} while (0)
 	B_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
 	c->own_stream = true;
+	for (int j = 0; j < kQMax; ++j) {
+		B_TRY(cudaStreamCreateWithFlags(&c->aux[j], cudaStreamNonBlocking));
+		B_TRY(cudaEventCreateWithFlags(&c->ev_join[j], cudaEventDisableTiming));
+	}
+	B_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
 	const size_t ns = c->ns;
 	B_TRY(cudaMalloc((void**)&c->u, ns * sizeof(double)));
 	B_TRY(cudaMalloc((void**)&c->ug, ns * sizeof(double)));
@@ -823,11 +872,11 @@ dgpu_status dgpu_batch_ssp_rk3_steps(dgpu_batch* c, double dt, int n_steps, doub
 	return read_max(c, max_rhs);
 }
 
-dgpu_status dgpu_batch_set_mode(dgpu_batch* c, int fused)
+dgpu_status dgpu_batch_set_mode(dgpu_batch* c, int form)
 {
-	if (!c || (fused != 0 && fused != 1))
+	if (!c || form < 0 || form > 2)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	c->mode = fused;
+	c->mode = form;
 	return DGPU_OK;
 }
 
@@ -908,9 +957,11 @@ dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report
 	BATCH_CUDA(c, cudaMemcpyAsync(c->d_groups, c->hgroups.data(), c->hgroups.size() * sizeof(BGroup),
 	                              cudaMemcpyHostToDevice, c->stream));
 	drop_graphs(c);
-	// plain per-group launches against the fused persistent launches, on graph-replayed RK steps
-	float tmode[2] = {0.f, 0.f};
-	for (int m = 0; m < 2; ++m) {
+	// the three forms on RK steps (graph-replayed unless graphs are off)
+	static const char* names[3] = {"plain", "fused", "branches"};
+	float tmode[3] = {0.f, 0.f, 0.f};
+	int best = 0;
+	for (int m = 0; m < 3; ++m) {
 		c->mode = m;
 		if ((st = dgpu_batch_ssp_rk3_steps(c, dt, 1, nullptr)) != DGPU_OK)
 			break;
@@ -921,10 +972,12 @@ dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report
 		cudaEventSynchronize(e1);
 		cudaEventElapsedTime(&tmode[m], e0, e1);
 		char line[128];
-		snprintf(line, sizeof line, "%s: %.4f ms per RK3 step\n", m ? "fused" : "plain", tmode[m] / reps);
+		snprintf(line, sizeof line, "%s: %.4f ms per RK3 step\n", names[m], tmode[m] / reps);
 		rep += line;
+		if (tmode[m] < tmode[best])
+			best = m;
 	}
-	c->mode = (tmode[1] < tmode[0]) ? 1 : 0;
+	c->mode = best;
 	cudaMemcpyAsync(coef_was ? c->u : c->ug, saved, c->ns * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
 	cudaMemcpyAsync(c->rhs, saved + c->ns, c->ns * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
 	cudaMemcpyAsync(c->n_corr, &n_corr0, sizeof n_corr0, cudaMemcpyHostToDevice, c->stream);
@@ -948,11 +1001,11 @@ dgpu_status dgpu_batch_set_graphs(dgpu_batch* c, int enable)
 	return DGPU_OK;
 }
 
-dgpu_status dgpu_batch_get_mode(const dgpu_batch* c, int* fused)
+dgpu_status dgpu_batch_get_mode(const dgpu_batch* c, int* form)
 {
-	if (!c || !fused)
+	if (!c || !form)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	*fused = c->mode;
+	*form = c->mode;
 	return DGPU_OK;
 }
 

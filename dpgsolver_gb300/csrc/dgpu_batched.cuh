@@ -175,7 +175,9 @@ __device__ void bvol_body(const BParams& P, const BatchOps* sops, const BGroup& 
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
 			vg[k * N + node] = acc[k];
-		// traces at each face's order: copy (q_f == Q) or tangential interpolation Q -> q_f
+		// traces at each face's order: copy (q_f == Q) or tangential interpolation Q -> q_f. In 3D the
+		// interpolation is separable: a thread takes one (variable, i0) column, contracts the first tangential
+		// direction once per b (Q^2 FMAs) and reuses the Q partial sums for all q_f outputs i1.
 		const int4* ef = P.elf + v * 2 * D;
 		for (int lf = 0; lf < 2 * D; ++lf) {
 			const int4 fd = ef[lf];
@@ -183,31 +185,41 @@ __device__ void bvol_body(const BParams& P, const BatchOps* sops, const BGroup& 
 			const int nff = (D == 2 ? qf : qf * qf);
 			double* dst = P.traces + 2 * NV * P.fbase[fd.x] + (long long)fd.y * NV * nff;
 			const double* src = str + lf * NV * NFQ;
-			for (int it = node; it < NV * nff; it += N) {
-				const int k = it / nff, i = it % nff;
-				double s;
-				if (qf == Q) {
-					s = src[k * NFQ + i];
-				} else {
-					const double(*I)[kQMax] = sops->Iup[qf];
-					s = 0.0;
-					if (D == 2) {
+			if (qf == Q) {
+				for (int it = node; it < NV * nff; it += N)
+					dst[it] = src[it];
+				continue;
+			}
+			const double(*I)[kQMax] = sops->Iup[qf];
+			if (D == 2) {
+				for (int it = node; it < NV * qf; it += N) {
+					const int k = it / qf, i = it % qf;
+					double s = 0.0;
+#pragma unroll
+					for (int a = 0; a < Q; ++a)
+						s += I[i][a] * src[k * NFQ + a];
+					dst[k * qf + i] = s;
+				}
+			} else {
+				for (int it = node; it < NV * qf; it += N) {
+					const int k = it / qf, i0 = it % qf;
+					double r[Q];
+#pragma unroll
+					for (int b = 0; b < Q; ++b) {
+						double acc = 0.0;
 #pragma unroll
 						for (int a = 0; a < Q; ++a)
-							s += I[i][a] * src[k * NFQ + a];
-					} else {
-						const int i0 = i % qf, i1 = i / qf;
+							acc += I[i0][a] * src[k * NFQ + a + Q * b];
+						r[b] = acc;
+					}
+					for (int i1 = 0; i1 < qf; ++i1) {
+						double s = 0.0;
 #pragma unroll
-						for (int b = 0; b < Q; ++b) {
-							double r = 0.0;
-#pragma unroll
-							for (int a = 0; a < Q; ++a)
-								r += I[i0][a] * src[k * NFQ + a + Q * b];
-							s += I[i1][b] * r;
-						}
+						for (int b = 0; b < Q; ++b)
+							s += I[i1][b] * r[b];
+						dst[k * nff + i0 + qf * i1] = s;
 					}
 				}
-				dst[k * nff + i] = s;
 			}
 		}
 	}
@@ -273,6 +285,8 @@ __device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup&
 		reinterpret_cast<double*>(sscale)[node] = 0.0;
 	if (active) {
 		// face terms at the element's own points: copy (q_f == Q) or transposed interpolation q_f -> Q
+		// (separable in 3D: a thread takes one (variable, a) column, contracts i0 for every i1 once and reuses
+		// the q_f partial sums for all Q outputs b).
 		const int4* ef = P.elf + v * 2 * D;
 		for (int lf = 0; lf < 2 * D; ++lf) {
 			const int4 fd = ef[lf];
@@ -280,28 +294,43 @@ __device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup&
 			const int nff = (D == 2 ? qf : qf * qf);
 			const double* src = P.nnf + NV * P.fbase[fd.x];
 			const double sgn = (fd.y == 0 ? -1.0 : 1.0);   // side 0: rhs -= ; side 1: rhs -= (-nnf)
-			for (int it = node; it < NV * NFQ; it += N) {
-				const int k = it / NFQ, t = it % NFQ;
-				double s;
-				if (qf == Q) {
-					s = src[k * nff + t];
-				} else {
-					const double(*I)[kQMax] = sops->Iup[qf];
-					s = 0.0;
-					if (D == 2) {
-						for (int i = 0; i < qf; ++i)
-							s += I[i][t] * src[k * nff + i];
-					} else {
-						const int a = t % Q, b = t / Q;
-						for (int i1 = 0; i1 < qf; ++i1) {
-							double r = 0.0;
+			double* out = sg + lf * NV * NFQ;
+			if (qf == Q) {
+				for (int it = node; it < NV * NFQ; it += N)
+					out[it] = sgn * src[it];
+				continue;
+			}
+			const double(*I)[kQMax] = sops->Iup[qf];
+			if (D == 2) {
+				for (int it = node; it < NV * Q; it += N) {
+					const int k = it / Q, t = it % Q;
+					double s = 0.0;
+					for (int i = 0; i < qf; ++i)
+						s += I[i][t] * src[k * qf + i];
+					out[k * NFQ + t] = sgn * s;
+				}
+			} else {
+				for (int it = node; it < NV * Q; it += N) {
+					const int k = it / Q, a = it % Q;
+					double r[kQMax];
+#pragma unroll
+					for (int i1 = 0; i1 < kQMax; ++i1) {
+						double acc = 0.0;
+						if (i1 < qf)
 							for (int i0 = 0; i0 < qf; ++i0)
-								r += I[i0][a] * src[k * nff + i0 + qf * i1];
-							s += I[i1][b] * r;
-						}
+								acc += I[i0][a] * src[k * nff + i0 + qf * i1];
+						r[i1] = acc;
+					}
+#pragma unroll
+					for (int bb = 0; bb < Q; ++bb) {
+						double s = 0.0;
+#pragma unroll
+						for (int i1 = 0; i1 < kQMax; ++i1)
+							if (i1 < qf)
+								s += I[i1][bb] * r[i1];
+						out[k * NFQ + a + Q * bb] = sgn * s;
 					}
 				}
-				sg[(lf * NV + k) * NFQ + t] = sgn * s;
 			}
 		}
 	}

@@ -300,15 +300,27 @@ class BatchSimulation:
                                                        ctypes.byref(mx) if want_max else None))
         return mx.value if want_max else None
 
+    FORMS = {"plain": 0, "fused": 1, "branches": 2}
+
     @property
-    def fused(self) -> bool:
+    def form(self) -> str:
+        """Launch form of the stages: "plain" (one launch per group / face order), "fused" (persistent launches
+        over all groups) or "branches" (the plain launches on parallel graph branches)."""
         v = ctypes.c_int()
         self._check(self._lib.dgpu_batch_get_mode(self._h, ctypes.byref(v)))
-        return bool(v.value)
+        return {v: k for k, v in self.FORMS.items()}[v.value]
+
+    @form.setter
+    def form(self, name: str):
+        self._check(self._lib.dgpu_batch_set_mode(self._h, self.FORMS[name]))
+
+    @property
+    def fused(self) -> bool:
+        return self.form == "fused"
 
     @fused.setter
     def fused(self, on: bool):
-        self._check(self._lib.dgpu_batch_set_mode(self._h, 1 if on else 0))
+        self.form = "fused" if on else "plain"
 
     def set_graphs(self, enable: bool):
         """Replay RK steps from a captured CUDA graph (default) or launch every kernel from the host."""

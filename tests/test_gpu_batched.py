@@ -39,14 +39,17 @@ CASES = {
 }
 
 
+FORMS = ["plain", "fused", "branches"]
+
+
 @pytest.mark.parametrize("name", sorted(CASES))
-@pytest.mark.parametrize("fused", [False, True])
-def test_residual_matches_oracle(gpu_lib, name, fused):
+@pytest.mark.parametrize("form", FORMS)
+def test_residual_matches_oracle(gpu_lib, name, form):
     from dpgsolver_gb300.solver import BatchSimulation
     prob = CASES[name]()
     r_ref, mx_ref = oracle.Oracle(prob).compute_rhs(prob.sol)
     with BatchSimulation(prob) as sim:
-        sim.fused = fused
+        sim.form = form
         mx = sim.compute_rhs()
         r = sim.rhs
     assert rel_err(r, r_ref) <= TOL
@@ -55,8 +58,8 @@ def test_residual_matches_oracle(gpu_lib, name, fused):
 
 @pytest.mark.parametrize("name,n_steps", [("adv2d_mixed_8", 4), ("vortex2d_roe_mixed_8", 3), ("hex_roe_mixed_4", 3),
                                           ("hex_lf_mixed_4", 2), ("hex_roe_mixed_curved_3", 2)])
-@pytest.mark.parametrize("fused", [False, True])
-def test_rk3_steps_match_oracle(gpu_lib, name, n_steps, fused):
+@pytest.mark.parametrize("form", FORMS)
+def test_rk3_steps_match_oracle(gpu_lib, name, n_steps, form):
     from dpgsolver_gb300.solver import BatchSimulation
     prob = CASES[name]()
     ref = oracle.Oracle(prob)
@@ -64,7 +67,7 @@ def test_rk3_steps_match_oracle(gpu_lib, name, n_steps, fused):
     for _ in range(n_steps):
         s_ref, mx_ref, _ = ref.ssp_rk3_step(s_ref, prob.dt)
     with BatchSimulation(prob) as sim:
-        sim.fused = fused
+        sim.form = form
         mx = sim.ssp_rk3_steps(prob.dt, n_steps)
         s = sim.sol_coef
     assert rel_err(s, s_ref) <= TOL
@@ -88,8 +91,8 @@ def test_ill_conditioned_case_within_rounding_noise(gpu_lib):
         noise = max(noise, rel_err(ref.compute_rhs(s2)[0], r_ref))
     assert noise > TOL   # the case is below the fixed tolerance's reach
     with BatchSimulation(prob) as sim:
-        for fused in (False, True):
-            sim.fused = fused
+        for form in FORMS:
+            sim.form = form
             sim.compute_rhs()
             assert rel_err(sim.rhs, r_ref) <= 4.0 * noise
 
@@ -99,8 +102,9 @@ def test_forms_and_tiles_agree_bitwise(gpu_lib):
     prob = CASES["hex_roe_mixed_10"]()
     out = []
     with BatchSimulation(prob) as sim:
-        for fused, tiles in [(False, None), (True, None), (False, [1, 3, 2, 1])]:
-            sim.fused = fused
+        for form, tiles in [("plain", None), ("fused", None), ("branches", None), ("plain", [1, 3, 2, 1]),
+                            ("branches", [4, 9, 1, 2])]:
+            sim.form = form
             if tiles:
                 for g, e in enumerate(tiles):
                     sim.set_group_tile(g, e)
@@ -150,7 +154,7 @@ def test_autotune_keeps_state_and_results(gpu_lib):
         sim.compute_rhs()
         r0 = sim.rhs
         rep = sim.autotune(prob.dt, reps=2)
-        assert "plain" in rep and "fused" in rep and "E=" in rep
+        assert "plain" in rep and "fused" in rep and "branches" in rep and "E=" in rep
         assert np.array_equal(sim.sol_coef, prob.sol)
         sim.compute_rhs()
         assert np.array_equal(sim.rhs, r0)
@@ -168,9 +172,12 @@ def test_launch_counts(gpu_lib):
         sim.ssp_rk3_steps(prob.dt, 2)
         n1 = sim.kernel_launches()
         assert n1 == per_stage + n_groups + 2 * 3 * per_stage     # + the per-group V u conversion
-        sim.fused = True
+        sim.form = "fused"
         sim.ssp_rk3_steps(prob.dt, 1)
         assert sim.kernel_launches() == n1 + 9
+        sim.form = "branches"
+        sim.ssp_rk3_steps(prob.dt, 1)
+        assert sim.kernel_launches() == n1 + 9 + 3 * per_stage
 
 
 def test_positivity_correction_matches_oracle(gpu_lib):
@@ -187,9 +194,9 @@ def test_positivity_correction_matches_oracle(gpu_lib):
     ref = oracle.Oracle(prob)
     s_ref, _, ncorr_ref = ref.ssp_rk3_step(sol, 1e-4)
     assert ncorr_ref > 0
-    for fused in (False, True):
+    for form in FORMS:
         with BatchSimulation(prob) as sim:
-            sim.fused = fused
+            sim.form = form
             sim.upload_state(sol)
             sim.ssp_rk3_steps(1e-4, 1)
             s = sim.sol_coef
