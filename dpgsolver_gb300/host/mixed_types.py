@@ -1,0 +1,379 @@
+"""Seeded conforming mixed-type 3D meshes (HEX, TET, WEDGE, PYR) with a p per volume (caller-side set-up).
+
+The unit cube is divided into n^3 cells on a periodic grid, and each cell into volumes of one of three kinds:
+
+* ``H``  one HEX;
+* ``W``  two WEDGEs: the cell split by the diagonal plane through the diagonal (0,0)-(1,1) of its faces normal
+  to the extrusion axis a (those two faces become two triangles each, the other four stay quads);
+* ``C``  one pyramid or two tetrahedra per cell face, all sharing the cell centre as apex: a face that stays a
+  quad carries a PYR (its base), a face split along the diagonal (0,0)-(1,1) of its tangential coordinates
+  carries two TETs.
+
+A cell face is a quad or two triangles the same way from both cells (the diagonal rule is translation invariant),
+so the mesh is conforming; conflicting H/W neighbours are resolved by turning one of them into a C cell. All
+volumes are affine images of the reference elements (dpgsolver_gb300.host.simplex), so metric terms and face
+normals are constant per volume. Cell kinds, wedge axes, the quad/triangle choice between C cells and the p of
+every volume are drawn from seeded generators.
+
+The face list follows the reference's rule (face.c:86-160): volumes are visited in list order and local faces in
+index order, and the first volume met is side 0. Face nodes are laid out in one canonical vertex order per face:
+the HEX side's own order when a HEX is on the face (so HEX volumes always see their faces unpermuted), else the
+side-0 volume's order; face_ord[f, s] is the orientation index (simplex.TRI_ORDS / QUAD_ORDS) under which
+side s sees that order.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .element import HEX, PYR, QUAD, TET, TRI, WEDGE, TPOperatorSet
+from .problem import (GAMMA, GM1, NUM_FLUX_LAX_FRIEDRICHS, NUM_FLUX_ROE_PIKE, PDE_EULER,
+                      primitive_to_conserved)
+from . import simplex as S
+
+_N_VERTS = {HEX: 8, TET: 4, WEDGE: 6, PYR: 5}
+
+
+class MixedTypeMesh:
+    """Volumes (type, global vertex ids, vertex coordinates) and faces with sides, local faces and orientations."""
+
+    def __init__(self, n: int, seed: int = 0, c_blocks: float = 0.06, w_columns: float = 0.15,
+                 p_tri: float = 1.0):
+        """c_blocks: fraction of cells in 2x2x2 blocks of C cells; w_columns: fraction of the (i, j) columns made of
+        W cells (extruded along z); p_tri: probability that a face between two C cells is split into triangles.
+        The defaults give about 50 % HEX, 25 % TET, 15 % WEDGE and 10 % PYR volumes."""
+        if n % 2:
+            raise ValueError("n must be even (2x2x2 blocks)")
+        self.n = n
+        self.h = 1.0 / n
+        rng = np.random.default_rng(seed)
+        nc = n ** 3
+        idx = np.arange(nc)
+        ijk = np.stack([idx % n, (idx // n) % n, idx // (n * n)], axis=1)
+        kind = np.zeros(nc, dtype=np.int64)                       # 0 H, 1 W, 2 C
+        axis = np.full(nc, 2, dtype=np.int64)
+        col = rng.random((n, n)) < w_columns
+        kind[col[ijk[:, 0], ijk[:, 1]]] = 1
+        nb = n // 2
+        blk = rng.random((nb, nb, nb)) < c_blocks
+        kind[blk[ijk[:, 0] // 2, ijk[:, 1] // 2, ijk[:, 2] // 2]] = 2
+
+        def cell(i, j, k):
+            return (i % n) + n * ((j % n) + n * (k % n))
+
+        def need(c, a, side):
+            """Requirement of cell c on its face normal to axis a (side 0: low, 1: high): 'Q', 'T' or None."""
+            if kind[c] == 0:
+                return "Q"
+            if kind[c] == 1:
+                return "T" if axis[c] == a else "Q"
+            return None
+
+        # resolve H/W conflicts by turning one side into a C cell
+        changed = True
+        while changed:
+            changed = False
+            for c in range(nc):
+                for a in range(3):
+                    nb = cell(*(ijk[c] + np.eye(3, dtype=int)[a]))
+                    ra, rb = need(c, a, 1), need(nb, a, 0)
+                    if ra is not None and rb is not None and ra != rb:
+                        kind[nb if rng.random() < 0.5 else c] = 2
+                        changed = True
+        # face kind of every cell face (a, low corner cell): between two C cells drawn, else the requirement
+        fkind = {}
+        for c in range(nc):
+            for a in range(3):
+                nb = cell(*(ijk[c] + np.eye(3, dtype=int)[a]))
+                r = need(c, a, 1) or need(nb, a, 0)
+                fkind[(c, a)] = r if r is not None else ("T" if rng.random() < p_tri else "Q")
+        self.cell_kind = kind
+
+        # ---- volumes ----
+        V = n ** 3   # global vertex ids: corners i + n j + n^2 k (periodic), centres V + cell
+        types, gids, xs = [], [], []
+
+        def corner(c, off):
+            i, j, k = ijk[c] + np.asarray(off)
+            return cell(i, j, k), (ijk[c] + np.asarray(off)) * self.h
+
+        def face_corners(c, a, side):
+            """The 4 corners of the cell face normal to a at side 0/1, tensor order in the tangential axes."""
+            t = [x for x in range(3) if x != a]
+            out = []
+            for dv in (0, 1):
+                for du in (0, 1):
+                    off = [0, 0, 0]
+                    off[a] = side
+                    off[t[0]] = du
+                    off[t[1]] = dv
+                    out.append(corner(c, off))
+            return out
+
+        def add(t, verts):
+            g = [v[0] for v in verts]
+            x = np.array([v[1] for v in verts], dtype=np.float64)
+            A, b0 = _affine(t, x)
+            if np.linalg.det(A) < 0.0:     # mirror to a positive orientation
+                perm = {TET: [0, 2, 1, 3], WEDGE: [0, 2, 1, 3, 5, 4], PYR: [0, 2, 1, 3, 4],
+                        HEX: [0, 2, 1, 3, 4, 6, 5, 7]}[t]
+                g = [g[m] for m in perm]
+                x = x[perm]
+            types.append(t)
+            gids.append(g)
+            xs.append(x)
+
+        for c in range(nc):
+            if kind[c] == 0:
+                add(HEX, [corner(c, (dx, dy, dz)) for dz in (0, 1) for dy in (0, 1) for dx in (0, 1)])
+            elif kind[c] == 1:
+                a = int(axis[c])
+                lo, hi = face_corners(c, a, 0), face_corners(c, a, 1)
+                for tri in ((0, 1, 3), (0, 3, 2)):     # triangles of the diagonal (0,0)-(1,1)
+                    add(WEDGE, [lo[m] for m in tri] + [hi[m] for m in tri])
+            else:
+                centre = (V + c, (ijk[c] + 0.5) * self.h)
+                for a in range(3):
+                    for side in (0, 1):
+                        fk = fkind[(c, a)] if side == 1 else fkind[(cell(*(ijk[c] - np.eye(3, dtype=int)[a])), a)]
+                        fc = face_corners(c, a, side)
+                        if fk == "Q":
+                            add(PYR, fc + [centre])
+                        else:
+                            for tri in ((0, 1, 3), (0, 3, 2)):
+                                add(TET, [fc[m] for m in tri] + [centre])
+        self.types = np.array(types, dtype=np.int32)
+        self.n_volumes = len(types)
+        self.gids = gids
+        self.X = xs
+        self._faces()
+
+    def _faces(self):
+        """Face list by the reference's rule, with canonical node order and per-side orientations."""
+        seen = {}
+        fv, flf = [], []
+        for v in range(self.n_volumes):
+            t = self.types[v]
+            for lf, fve in enumerate(S.F_VE[t]):
+                key = tuple(sorted(self.gids[v][m] for m in fve))
+                if key in seen:
+                    f = seen.pop(key)
+                    fv[f][1], flf[f][1] = v, lf
+                else:
+                    seen[key] = len(fv)
+                    fv.append([v, -1])
+                    flf.append([lf, -1])
+        if seen:
+            raise AssertionError("unmatched faces: the mesh is not conforming/periodic")
+        self.face_vol = np.array(fv, dtype=np.int32)
+        self.face_lf = np.array(flf, dtype=np.int32)
+        self.n_faces = len(fv)
+        self.face_ord = np.zeros((self.n_faces, 2), dtype=np.int32)
+        self.face_canon = np.zeros(self.n_faces, dtype=np.int32)    # side whose local order is canonical
+        for f in range(self.n_faces):
+            vs = self.face_vol[f]
+            cs = 1 if (self.types[vs[1]] == HEX and self.types[vs[0]] != HEX) else 0
+            self.face_canon[f] = cs
+            canon = [self.gids[vs[cs]][m] for m in S.F_VE[self.types[vs[cs]]][self.face_lf[f, cs]]]
+            ft = S.TRI if len(canon) == 3 else S.QUAD
+            for s in range(2):
+                loc = [self.gids[vs[s]][m] for m in S.F_VE[self.types[vs[s]]][self.face_lf[f, s]]]
+                perm = tuple(loc.index(g) for g in canon)
+                ords = S.face_ords(ft)
+                if perm not in ords:
+                    raise AssertionError("face orientation outside the symmetry group")
+                self.face_ord[f, s] = ords.index(perm)
+
+    def counts(self):
+        return {int(t): int(np.sum(self.types == t)) for t in (HEX, TET, WEDGE, PYR)}
+
+
+def _affine(t, x):
+    """A, b with x_m = A r_m + b for the reference vertices r_m (affine volumes)."""
+    R = S.VERTS[t]
+    M, *_ = np.linalg.lstsq(np.hstack([R, np.ones((len(R), 1))]), x, rcond=None)
+    A, b = M[:3].T, M[3]
+    if np.max(np.abs(R @ A.T + b - x)) > 1e-12 * max(1.0, np.max(np.abs(x))):
+        raise AssertionError("volume is not an affine image of its reference element")
+    return A, b
+
+
+class MixedTypeProblem:
+    """Mixed-type mesh + per-volume p + per-(type, p) operators + affine geometry + state (flat layout as
+    MixedTPProblem: per volume the (n_var x n_vs(v)) block, volume-list order)."""
+
+    def __init__(self, mesh: MixedTypeMesh, p_vol, pde=PDE_EULER, num_flux=NUM_FLUX_ROE_PIKE):
+        self.mesh = mesh
+        self.d = 3
+        self.pde = pde
+        self.num_flux = num_flux
+        self.positivity = False
+        self.b_adv = np.zeros(3)
+        self.n_var = 5
+        self.name = "mixed_types"
+        self.meta = {}
+        p_vol = np.asarray(p_vol, dtype=np.int32)
+        keys = sorted(set((int(t), int(p)) for t, p in zip(mesh.types, p_vol)), key=lambda k: (k[0] != HEX, k))
+        self.groups = [TPOperatorSet(HEX, p) if t == HEX else S.DenseOperatorSet(t, p) for t, p in keys]
+        self.group_key = keys
+        gidx = {k: g for g, k in enumerate(keys)}
+        self.vol_group = np.array([gidx[(int(t), int(p))] for t, p in zip(mesh.types, p_vol)], dtype=np.int32)
+        self.p_vol = p_vol
+        nv = mesh.n_volumes
+        n_vs = np.array([self.groups[g].n_vs for g in self.vol_group], dtype=np.int64)
+        self.n_vs = n_vs
+        self.state_off = np.zeros(nv + 1, dtype=np.int64)
+        self.state_off[1:] = np.cumsum(self.n_var * n_vs)
+        self.group_vols = [np.nonzero(self.vol_group == g)[0] for g in range(len(self.groups))]
+        # affine geometry per volume: m = J A^-T (m(n,i,j) = J dr_j/dx_i), J = det A
+        self.A = np.empty((nv, 3, 3))
+        self.b = np.empty((nv, 3))
+        for v in range(nv):
+            self.A[v], self.b[v] = _affine(int(mesh.types[v]), mesh.X[v])
+        self.J = np.linalg.det(self.A)
+        if np.any(self.J <= 0.0):
+            raise AssertionError("non-positive Jacobian")
+        self.m = self.J[:, None, None] * np.transpose(np.linalg.inv(self.A), (0, 2, 1))
+        # faces at p_f = max(p_L, p_R): q_f^2 nodes on triangles (collapsed rule) and quads (GL)
+        q = p_vol.astype(np.int64) + 1
+        self.face_q = np.maximum(q[mesh.face_vol[:, 0]], q[mesh.face_vol[:, 1]]).astype(np.int32)
+        self.face_off = np.zeros(mesh.n_faces + 1, dtype=np.int64)
+        self.face_off[1:] = np.cumsum(self.face_q.astype(np.int64) ** 2)
+        self._face_geometry()
+        self.sol = np.zeros(int(self.state_off[-1]))
+        self.dt = 0.0
+
+    def _face_geometry(self):
+        mesh = self.mesh
+        nfn = int(self.face_off[-1])
+        self.normals_fc = np.empty((nfn, 3))
+        self.jacobian_det_fc = np.empty(nfn)
+        self.w_fc = np.empty(nfn)
+        for f in range(mesh.n_faces):
+            v0, lf0 = mesh.face_vol[f, 0], mesh.face_lf[f, 0]
+            t0 = int(mesh.types[v0])
+            nref = (self.groups[self.vol_group[v0]].normals_ref[lf0])
+            nun = self.m[v0] @ nref
+            jn = np.linalg.norm(nun)
+            o, e = self.face_off[f], self.face_off[f + 1]
+            self.normals_fc[o:e] = nun / jn
+            self.jacobian_det_fc[o:e] = jn
+            ft = S.TRI if len(S.F_VE[t0][lf0]) == 3 else S.QUAD
+            self.w_fc[o:e] = S.face_rule(ft, int(self.face_q[f]))[1]
+
+    # ---- layout helpers (as MixedTPProblem) ----
+    @property
+    def n_volumes(self) -> int:
+        return self.mesh.n_volumes
+
+    @property
+    def n_state(self) -> int:
+        return int(self.state_off[-1])
+
+    def block(self, state, v):
+        return state[self.state_off[v]:self.state_off[v + 1]].reshape(self.n_var, -1)
+
+    def group_view(self, state, g):
+        vols = self.group_vols[g]
+        n = self.n_var * self.groups[g].n_vs
+        idx = self.state_off[vols][:, None] + np.arange(n)[None, :]
+        return state[idx].reshape(len(vols), self.n_var, self.groups[g].n_vs)
+
+    def set_group(self, state, g, blocks):
+        vols = self.group_vols[g]
+        n = self.n_var * self.groups[g].n_vs
+        idx = self.state_off[vols][:, None] + np.arange(n)[None, :]
+        state[idx] = np.asarray(blocks).reshape(len(vols), n)
+
+    def vc_xyz(self, g):
+        """Physical coordinates of group g's volume cubature nodes (n_vols_g, n_vc, 3)."""
+        ops = self.groups[g]
+        vols = self.group_vols[g]
+        if getattr(ops, "dense", False):
+            xr = ops.x_vc
+        else:
+            from .element import tp_nodes
+            xr = tp_nodes(ops.x_vc, 3)
+        return np.einsum("vij,nj->vni", self.A[vols], xr) + self.b[vols][:, None, :]
+
+    def nc_fc(self) -> np.ndarray:
+        return np.concatenate([np.arange(n, dtype=np.int32) for n in np.diff(self.face_off)])
+
+    def flat(self) -> dict:
+        nv = self.mesh.n_volumes
+        mvc, jvc = [None] * nv, [None] * nv
+        for g, vols in enumerate(self.group_vols):
+            n_vc = self.groups[g].n_vc
+            for v in vols:
+                mvc[v] = np.repeat(self.m[v].T.reshape(9, 1), n_vc, axis=1).ravel()   # [j][i][n]
+                jvc[v] = np.full(n_vc, self.J[v])
+        return {
+            "groups": self.groups,
+            "vol_group": self.vol_group,
+            "face_q": self.face_q,
+            "face_ord": self.mesh.face_ord,
+            "metrics_vc": np.concatenate(mvc),
+            "jacobian_det_vc": np.concatenate(jvc),
+            "normals_fc": np.ascontiguousarray(self.normals_fc).ravel(),
+            "jacobian_det_fc": self.jacobian_det_fc.copy(),
+            "nc_fc": self.nc_fc(),
+            "sol": self.sol,
+        }
+
+    def project(self, fn):
+        """Set the state to the L2 projection of fn(xyz (m, 3)) -> (m, n_var) onto every volume's basis (volume
+        cubature; HEX groups: values at the GLL solution nodes, which are their coefficients)."""
+        from .element import tp_nodes
+        for g, ops in enumerate(self.groups):
+            vols = self.group_vols[g]
+            if len(vols) == 0:
+                continue
+            if getattr(ops, "dense", False):
+                x = self.vc_xyz(g)
+                U = fn(x.reshape(-1, 3)).reshape(len(vols), ops.n_vc, self.n_var)
+                # orthonormal basis, affine volume: coef = M_ref^-1 cv0^T diag(w) U
+                Minv = np.linalg.inv(ops.mass())
+                coef = np.einsum("ab,nb,n,vnk->vka", Minv, ops.cv0_vs_vc(), ops.w_vc, U)
+            else:
+                xs = tp_nodes(ops.x_vs, 3)
+                x = np.einsum("vij,nj->vni", self.A[vols], xs) + self.b[vols][:, None, :]
+                coef = np.transpose(fn(x.reshape(-1, 3)).reshape(len(vols), ops.n_vs, self.n_var), (0, 2, 1))
+            self.set_group(self.sol, g, coef)
+
+    def stable_dt(self, cfl: float = 0.1, lam: float = 1.0) -> float:
+        pmax = max(g.p for g in self.groups)
+        return cfl * self.mesh.h / ((2 * pmax + 1) * lam)
+
+
+def mixed_types_euler(n: int = 12, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE,
+                      mach: float = 0.5, perturb: float = 0.05, c_blocks: float = 0.06, w_columns: float = 0.15,
+                      p_tri: float = 1.0) -> MixedTypeProblem:
+    """Mixed HEX/TET/WEDGE/PYR mesh of the periodic unit cube (n^3 cells), p uniform in p_set per volume (seeded),
+    Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed.mixed_euler)."""
+    mesh = MixedTypeMesh(n, seed=seed, c_blocks=c_blocks, w_columns=w_columns, p_tri=p_tri)
+    rng = np.random.default_rng(seed + 17)
+    p_vol = rng.choice(np.asarray(p_set, dtype=np.int32), size=mesh.n_volumes)
+    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux)
+    rng2 = np.random.default_rng(seed + 1)
+    ph = rng2.uniform(0.0, 2.0 * math.pi, size=(5, 3))
+    c0 = math.sqrt(GAMMA)
+    dirn = np.array([1.0, 0.5, 0.25])
+    dirn /= np.linalg.norm(dirn)
+
+    def state(x):
+        def wave(k):
+            s = np.ones(len(x))
+            for j in range(3):
+                s = s * np.sin(2.0 * math.pi * x[:, j] + ph[k, j])
+            return s
+        rho = 1.0 + perturb * wave(0)
+        pr = 1.0 + perturb * wave(1)
+        vel = np.stack([mach * c0 * dirn[j] * (1.0 + perturb * wave(2 + j)) for j in range(3)])
+        return primitive_to_conserved(3, rho, vel, pr).T
+
+    prob.project(state)
+    lam = mach * c0 * (1.0 + perturb) + c0 * math.sqrt((1.0 + perturb) / (1.0 - perturb))
+    prob.dt = prob.stable_dt(lam=lam)
+    prob.meta.update(n=n, seed=seed, p_set=tuple(p_set), counts=mesh.counts())
+    return prob

@@ -112,24 +112,42 @@ class Oracle:
             G[gi].cv0_vs_vc = _dp(arr(ops.cv0_vs_vc()))
             G[gi].tw1_vt_vc = _dp(arr(np.stack([ops.tw1_vt_vc(k) for k in range(d)])))
             G[gi].w_vc = _dp(arr(ops.w_vc))
-            G[gi].ccSB0 = _dp(arr(ops.ccSB0_vs_vs()))
-            G[gi].ccBS0 = _dp(arr(ops.ccBS0_vs_vs()))
-        # face operator sets: one per (group, face order) pair that occurs
+            if not getattr(ops, "dense", False):    # Bezier maps exist for the TP groups only
+                G[gi].ccSB0 = _dp(arr(ops.ccSB0_vs_vs()))
+                G[gi].ccBS0 = _dp(arr(ops.ccBS0_vs_vs()))
+        # face operator sets: one per (group, face order, orientation) that occurs, stacked over local faces
         vol_group = fl["vol_group"]
         face_q = fl["face_q"]
+        face_ord = fl.get("face_ord")
         mesh = prob.mesh
         pairs = {}
         idx = np.empty((mesh.n_faces, 2), dtype=np.int32)
         for f in range(mesh.n_faces):
             for s in range(2):
-                key = (int(vol_group[mesh.face_vol[f, s]]), int(face_q[f]))
+                o = int(face_ord[f, s]) if face_ord is not None else 0
+                key = (int(vol_group[mesh.face_vol[f, s]]), int(face_q[f]), o)
                 if key not in pairs:
                     pairs[key] = len(pairs)
                 idx[f, s] = pairs[key]
         FO = (_FaceOps * len(pairs))()
-        for (gi, qf), k in pairs.items():
-            cv0, tw0, _ = face_operators(groups[gi], qf)
-            FO[k].n_fc, FO[k].n_vs = cv0[0].shape[0], groups[gi].n_vs
+        for (gi, qf, o), k in pairs.items():
+            ops = groups[gi]
+            if getattr(ops, "dense", False):
+                cv0, tw0 = [], []
+                for lf in range(ops.n_lf):
+                    if o < ops.n_ords(lf):
+                        c = ops.cv0_vs_fc(lf, o, qf)
+                        t = c.T * ops.w_fc(lf, qf)[None, :]
+                    else:   # orientation of the other face type: never selected for this local face
+                        c = np.zeros((qf * qf, ops.n_vs))
+                        t = c.T.copy()
+                    cv0.append(c)
+                    tw0.append(t)
+            else:
+                if o != 0:
+                    raise ValueError("TP volumes see their faces unpermuted")
+                cv0, tw0, _ = face_operators(ops, qf)
+            FO[k].n_fc, FO[k].n_vs = cv0[0].shape[0], ops.n_vs
             FO[k].cv0_vs_fc = _dp(arr(np.stack(cv0)))
             FO[k].tw0_vt_fc = _dp(arr(np.stack(tw0)))
 

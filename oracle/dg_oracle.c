@@ -117,6 +117,10 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 		return ORACLE_ERR_ARG;
 	if (in->pde == ORACLE_PDE_ADVECTION && in->n_var != 1)
 		return ORACLE_ERR_ARG;
+	if (in->positivity)   /* the limiter needs every group's Bezier maps */
+		for (int g = 0; g < in->n_groups; ++g)
+			if (!in->groups[g].ccSB0 || !in->groups[g].ccBS0)
+				return ORACLE_ERR_ARG;
 	struct oracle_ctx* c = calloc(1, sizeof *c);
 	c->P = *in;
 	const int d = in->d, nv = in->n_var;

@@ -1,0 +1,165 @@
+"""Non-TP reference elements (TET, WEDGE, PYR), the mixed-type mesh and the oracle on it (CPU)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from dpgsolver_gb300.host import simplex as S
+from dpgsolver_gb300.host.element import HEX, PYR, QUAD, TET, TRI, WEDGE, TPOperatorSet
+from dpgsolver_gb300.host import mixed_types as MT
+
+TYPES = (TET, WEDGE, PYR)
+VOLUMES = {TET: 8.0 / (6.0 * math.sqrt(2.0)), WEDGE: 2.0 * math.sqrt(3.0), PYR: 4.0 * math.sqrt(2.0) / 3.0}
+
+
+@pytest.mark.parametrize("alpha", [1.0, 2.0])
+def test_gauss_jacobi_moments(alpha):
+    from scipy.integrate import quad
+    x, w = S.gauss_jacobi(5, alpha)
+    for k in range(10):
+        exact = quad(lambda t: (1 - t) ** alpha * t ** k, -1, 1)[0]
+        assert abs(np.sum(w * x ** k) - exact) < 1e-14
+
+
+@pytest.mark.parametrize("e", TYPES)
+def test_volume_rules(e):
+    """Conical product rules: the reference volumes and, on the TET, the exact monomial moments of the simplex
+    (degree 2q-1) through the affine map from the standard simplex."""
+    for q in (2, 3, 4, 5):
+        x, w = S.volume_rule(e, q)
+        assert abs(w.sum() - VOLUMES[e]) < 1e-13
+    if e == TET:
+        x, w = S.volume_rule(TET, 4)   # exact to degree 7
+        A, b = S._affine_from(S._T3, S.VERTS[TET])
+        xs = np.linalg.solve(A, (x - b).T).T + 1.0          # standard simplex shifted to [0, 2]
+        for a, bb, c in [(2, 1, 3), (0, 4, 3), (1, 1, 1)]:
+            # int over {u_i >= 0, sum u <= 2} of u^a v^b w^c = 2^(a+b+c+3) a! b! c! / (a+b+c+3)!
+            ex = 2.0 ** (a + bb + c + 3) * math.factorial(a) * math.factorial(bb) * math.factorial(c) \
+                / math.factorial(a + bb + c + 3) * abs(np.linalg.det(A))
+            assert abs(np.sum(w * xs[:, 0] ** a * xs[:, 1] ** bb * xs[:, 2] ** c) - ex) < 1e-13 * max(1.0, ex)
+
+
+@pytest.mark.parametrize("e", TYPES)
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_orthonormal_basis_and_gradients(e, p):
+    o = S.DenseOperatorSet(e, p)
+    assert o.n_vs == {TET: (p + 1) * (p + 2) * (p + 3) // 6, WEDGE: (p + 1) ** 2 * (p + 2) // 2,
+                      PYR: (p + 1) * (p + 2) * (2 * p + 3) // 6}[e]
+    assert np.abs(o.mass() - np.eye(o.n_vs)).max() < 1e-12
+    x0 = o.x_vc[::7]
+    _, G = o.basis(x0)
+    h = 1e-6
+    for k in range(3):
+        dx = np.zeros(3)
+        dx[k] = h
+        fd = (o.basis(x0 + dx)[0] - o.basis(x0 - dx)[0]) / (2 * h)
+        assert np.abs(fd - G[k]).max() < 1e-6 * max(1.0, np.abs(G[k]).max())
+
+
+@pytest.mark.parametrize("e", TYPES)
+def test_reference_normals_match_geometry(e):
+    nr = S.reference_normals_3d(e)
+    V = S.VERTS[e]
+    cen = V.mean(0)
+    for lf, fv in enumerate(S.F_VE[e]):
+        P = V[fv]
+        n = np.cross(P[1] - P[0], P[2] - P[0])
+        n /= np.linalg.norm(n)
+        if np.dot(n, P[0] - cen) < 0:
+            n = -n
+        assert np.abs(n - nr[lf]).max() < 1e-14
+
+
+@pytest.mark.parametrize("e", TYPES)
+def test_faces_congruent_to_face_reference(e):
+    """Every face of the reference element has the area of its face reference element, so face-rule weights
+    and J_f = |m n_ref| measure it consistently; face points lie on the face plane."""
+    o = S.DenseOperatorSet(e, 2)
+    nr = S.reference_normals_3d(e)
+    for lf, fv in enumerate(S.F_VE[e]):
+        P = S.VERTS[e][fv]
+        if len(fv) == 3:
+            area = 0.5 * np.linalg.norm(np.cross(P[1] - P[0], P[2] - P[0]))
+            assert abs(area - math.sqrt(3.0)) < 1e-14
+        else:
+            area = np.linalg.norm(np.cross(P[1] - P[0], P[2] - P[0]))
+            assert abs(area - 4.0) < 1e-14
+        assert abs(o.w_fc(lf, 3).sum() - area) < 1e-13
+        for ord_ in range(o.n_ords(lf)):
+            x = o.face_points(lf, ord_, 3)
+            assert np.abs((x - P[0]) @ nr[lf]).max() < 1e-14
+
+
+def test_mixed_type_mesh_faces_match():
+    """Both sides of every face evaluate at the same physical points (orientations), HEX sides unpermuted."""
+    prob = MT.mixed_types_euler(4, seed=0)
+    mesh = prob.mesh
+    assert set(mesh.counts()) == {HEX, TET, WEDGE, PYR} and min(mesh.counts().values()) > 0
+    for f in range(mesh.n_faces):
+        pts = []
+        for s in range(2):
+            v = mesh.face_vol[f, s]
+            ops = prob.groups[prob.vol_group[v]]
+            lf, o = mesh.face_lf[f, s], mesh.face_ord[f, s]
+            if getattr(ops, "dense", False):
+                xr = ops.face_points(lf, o, int(prob.face_q[f]))
+            else:
+                assert o == 0
+                from dpgsolver_gb300.host.element import gauss_legendre
+                xq, _ = gauss_legendre(int(prob.face_q[f]))
+                nd, side = lf // 2, lf % 2
+                t = [k for k in range(3) if k != nd]
+                xr = np.zeros((len(xq) ** 2, 3))
+                xr[:, nd] = -1.0 if side == 0 else 1.0
+                xr[:, t[0]] = np.tile(xq, len(xq))
+                xr[:, t[1]] = np.repeat(xq, len(xq))
+            pts.append(xr @ prob.A[v].T + prob.b[v])
+        d = pts[0] - pts[1]
+        d -= np.round(d)            # periodic images
+        assert np.abs(d).max() < 1e-13
+
+
+def test_mixed_type_fractions():
+    """Default generator parameters give the target mix (HEX 50 %, TET 25 %, WEDGE 15 %, PYR 10 %) within a few %."""
+    m = MT.MixedTypeMesh(24, seed=0)
+    c = m.counts()
+    tot = sum(c.values())
+    for t, target in ((HEX, 0.5), (TET, 0.25), (WEDGE, 0.15), (PYR, 0.10)):
+        assert abs(c[t] / tot - target) < 0.05
+
+
+def _one_coefficients(ops):
+    if getattr(ops, "dense", False):
+        return np.linalg.solve(ops.mass(), ops.cv0_vs_vc().T @ ops.w_vc)
+    return np.ones(ops.n_vs)
+
+
+def test_mixed_type_oracle_free_stream_and_conservation():
+    prob = MT.mixed_types_euler(4, seed=0)
+    o = oracle.Oracle(prob)
+    raw = o.compute_rhs_raw(prob.sol)
+    tot = np.zeros(5)
+    scale = np.zeros(5)
+    for g, ops in enumerate(prob.groups):
+        one = _one_coefficients(ops)
+        B = prob.group_view(raw, g)
+        tot += np.einsum("vka,a->k", B, one)
+        scale += np.einsum("vka,a->k", np.abs(B), np.abs(one))
+    assert np.all(np.abs(tot) <= 1e-13 * scale.max())
+    vals = np.array([1.0, 0.3, -0.2, 0.1, 2.5])
+    prob.project(lambda x: np.tile(vals, (len(x), 1)))
+    _, mx = o.compute_rhs(prob.sol)
+    assert mx < 1e-11
+
+
+def test_mixed_type_complex_step():
+    prob = MT.mixed_types_euler(4, seed=1)
+    o = oracle.Oracle(prob)
+    rng = np.random.default_rng(2)
+    base = prob.sol + 1e-3 * rng.standard_normal(prob.sol.shape)
+    dirn = rng.standard_normal(prob.sol.shape)
+    _, ri = o.compute_rhs_cmplx(base, 1e-30 * dirn)
+    eps = 1e-6
+    fd = (o.compute_rhs(base + eps * dirn)[0] - o.compute_rhs(base - eps * dirn)[0]) / (2 * eps)
+    assert np.max(np.abs(ri / 1e-30 - fd)) <= 1e-6 * np.max(np.abs(fd))
