@@ -75,6 +75,17 @@ class TPOperators(ctypes.Structure):
                 ("w_vc", c_double_p), ("ccSB0_vs_vs", c_double_p), ("ccBS0_vs_vs", c_double_p)]
 
 
+class DenseOperators(ctypes.Structure):
+    _fields_ = [("elem_type", ctypes.c_int), ("p", ctypes.c_int), ("n_vs", ctypes.c_int), ("n_vc", ctypes.c_int),
+                ("cv0_vs_vc", c_double_p), ("cv1_vs_vc", c_double_p), ("w_vc", c_double_p),
+                ("n_lf", ctypes.c_int), ("n_ord", ctypes.c_int), ("n_fc", c_int_p),
+                ("cv0_vs_fc", ctypes.POINTER(c_double_p)), ("w_fc", ctypes.POINTER(c_double_p))]
+
+
+class Group(ctypes.Structure):
+    _fields_ = [("tp", ctypes.POINTER(TPOperators)), ("dense", ctypes.POINTER(DenseOperators))]
+
+
 class Mesh(ctypes.Structure):
     _fields_ = [("n_volumes", ctypes.c_int), ("metrics_vc", c_double_p), ("jacobian_det_vc", c_double_p),
                 ("n_faces", ctypes.c_int), ("face_vol", c_int_p), ("face_lf", c_int_p), ("nc_fc", c_int_p),
@@ -116,6 +127,8 @@ EXPORTS = {
     # batched mixed-order context
     "dgpu_batch_create": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.c_int, ctypes.POINTER(TPOperators), c_int_p,
                                          ctypes.POINTER(Mesh), ctypes.POINTER(ctypes.c_void_p)]),
+    "dgpu_batch_create_groups": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.c_int, ctypes.POINTER(Group), c_int_p,
+                                                ctypes.POINTER(Mesh), c_int_p, ctypes.POINTER(ctypes.c_void_p)]),
     "dgpu_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dgpu_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "dgpu_batch_state_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),

@@ -1,10 +1,13 @@
-// C ABI of the batched (mixed element order) explicit DG residual: dgpu_batch_* in include/dgpu.h.
+// C ABI of the batched (mixed element type and order) explicit DG residual: dgpu_batch_* in include/dgpu.h.
 //
-// Volumes are grouped by (element type, p) and stored group by group on the device; the caller's state stays in
-// volume-list order and is permuted on upload/download. Each RK stage runs either as one launch per group and
-// per face order ("plain") or as three persistent launches over all groups ("fused"), and a whole step is
-// replayed from a captured CUDA graph. dgpu_batch_autotune times the elements-per-CTA candidates of every group
-// and both forms on the actual mesh and keeps the fastest.
+// Volumes are grouped by (element type, p): tensor-product groups (QUAD/HEX, factored operators,
+// dgpu_batched.cuh) first, then dense-operator groups (TET/WEDGE/PYR, dgpu_dense.cuh). They are stored group by
+// group on the device; the caller's state stays in volume-list order and is permuted on upload/download. Faces
+// are renumbered internally by increasing q_f so that each face order's nodes form one range. Each RK stage runs
+// as one launch per group and per face order ("plain"), as three persistent launches over all groups ("fused"),
+// or as the plain launches on parallel graph branches ("branches"); a whole step is replayed from a captured CUDA
+// graph. dgpu_batch_autotune times the elements-per-CTA candidates of every group and the three forms on the
+// actual mesh and keeps the fastest.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -13,7 +16,7 @@
 #include <vector>
 
 #include "../../include/dgpu.h"
-#include "dgpu_batched.cuh"
+#include "dgpu_dense.cuh"
 #include "dgpu_host_ops.h"
 
 using namespace dgpu;
@@ -21,12 +24,15 @@ using namespace dgpu;
 namespace {
 
 thread_local std::string g_batch_error;
+constexpr int kBranches = 16;   // streams of the branch form
 
 struct GroupLaunch {
 	cudaError_t (*vol)(dgpu_batch*, int g, bool gll_in) = nullptr;
 	cudaError_t (*lift)(dgpu_batch*, int g, int mode, double dt, int stage, int want_max) = nullptr;
 	cudaError_t (*conv)(dgpu_batch*, int g, bool to_gl) = nullptr;
-	int N = 0, E_max = 0;
+	int E_max = 0;
+	bool dense = false;
+	int idx = 0;        // index among the TP or among the dense groups
 };
 
 }  // namespace
@@ -34,43 +40,44 @@ struct GroupLaunch {
 struct dgpu_batch {
 	int d = 0, nv = 0, pde = 0, flux = 0, positivity = 0;
 	double b_adv[3] = {0, 0, 0};
-	int n_groups = 0, n_vol = 0, n_face = 0;
-	std::vector<BGroup> hgroups;
+	int n_tp = 0, n_dense = 0, n_all = 0, n_vol = 0, n_face = 0;
+	std::vector<int> caller_to_internal;   // caller group -> internal group (TP first, then dense)
+	std::vector<BGroup> hgroups;           // TP groups
+	std::vector<DGroup> hdgroups;          // dense groups
 	std::vector<BatchOps> hops;
-	std::vector<GroupLaunch> gl;
-	std::vector<int> order;            // sorted element -> list index
-	std::vector<long long> list_off;   // list index -> offset in the caller's state
-	std::vector<long long> sorted_off; // sorted element -> offset in the device state
+	std::vector<GroupLaunch> gl;           // internal groups
+	std::vector<int> order;                // sorted element -> list index
+	std::vector<long long> list_off;       // list index -> offset in the caller's state
+	std::vector<long long> sorted_off;     // sorted element -> offset in the device state
 	size_t ns = 0;
 	// device
 	BatchOps* d_ops = nullptr;
 	BGroup* d_groups = nullptr;
+	DGroup* d_dgroups = nullptr;
+	std::vector<void*> dense_bufs;         // per dense group: operators, face operators, offsets, 1/J
 	int4* d_elf = nullptr;
 	long long* d_fbase = nullptr;
+	int* d_node_face = nullptr;
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	double *u = nullptr, *ug = nullptr, *u0 = nullptr, *rhs = nullptr, *vol_gl = nullptr;
 	double *traces = nullptr, *nnf = nullptr;
 	unsigned long long* max_bits = nullptr;
 	int* err_flag = nullptr;
 	unsigned long long* n_corr = nullptr;
-	int* d_faces_by_q = nullptr;
-	int* d_qf_begin = nullptr;
-	int qf_begin[kQMax + 2] = {0};
-	long long n_face_items = 0;
+	long long qnode[kQMax + 2] = {0};      // face nodes of order q_f: [qnode[q_f], qnode[q_f + 1])
 	BTile* d_tiles = nullptr;
 	int n_tiles = 0, fused_blocks_vol = 0, fused_blocks_lift = 0, fused_blocks_face = 0;
 	size_t fused_vol_smem = 0, fused_lift_smem = 0;
 	cudaError_t (*fused_vol)(dgpu_batch*, bool gll_in) = nullptr;
 	cudaError_t (*fused_lift)(dgpu_batch*, int mode, double dt, int stage, int want_max) = nullptr;
-	cudaError_t (*fused_face)(dgpu_batch*) = nullptr;
-	cudaError_t (*face_q)(dgpu_batch*, int qf) = nullptr;
+	cudaError_t (*face_nodes)(dgpu_batch*, long long lo, long long hi, int blocks) = nullptr;
 	// execution
 	cudaStream_t stream = nullptr;
 	bool own_stream = false;
 	bool coef_valid = true, gl_valid = false;
 	int mode = 0;   // 0: one launch per group and face order; 1: fused persistent launches; 2: as 0 on parallel branches
-	cudaStream_t aux[kQMax] = {nullptr};   // branches of form 2
-	cudaEvent_t ev_fork = nullptr, ev_join[kQMax] = {nullptr};
+	cudaStream_t aux[kBranches] = {nullptr};
+	cudaEvent_t ev_fork = nullptr, ev_join[kBranches] = {nullptr};
 	bool use_graphs = true;
 	cudaGraphExec_t graph[3][2] = {};   // [mode][want_max]
 	double graph_dt[3][2] = {};
@@ -83,7 +90,8 @@ struct dgpu_batch {
 		BParams P;
 		for (int k = 0; k < 3; ++k)
 			P.b_adv[k] = b_adv[k];
-		P.n_groups = n_groups;
+		P.n_groups = n_tp;
+		P.dgroups = d_dgroups;
 		P.ops = d_ops;
 		P.groups = d_groups;
 		P.elf = d_elf;
@@ -99,6 +107,8 @@ struct dgpu_batch {
 		P.n_corr = n_corr;
 		return P;
 	}
+	int group_n_vol(int g) const { return gl[g].dense ? hdgroups[gl[g].idx].n_vol : hgroups[gl[g].idx].n_vol; }
+	int group_E(int g) const { return gl[g].dense ? hdgroups[gl[g].idx].E : hgroups[gl[g].idx].E; }
 };
 
 namespace {
@@ -125,31 +135,13 @@ template <int D, int Q, int NV>
 size_t blift_smem(int E) { return sizeof(BatchOps) + (size_t)E * BSmem<D, Q, NV>::LIFT * sizeof(double); }
 template <int D, int Q, int NV>
 size_t bconv_smem(int E) { return sizeof(BatchOps) + (size_t)E * 3 * NV * TPShape<D, Q>::N * sizeof(double); }
+size_t dvol_smem(int nv, const DGroup& G, int E) { return (size_t)E * DSmem::vol(nv, G.n_vs, G.n_vc) * sizeof(double); }
+size_t dlift_smem(int nv, const DGroup& G, int E) { return (size_t)E * DSmem::lift(nv, G.n_vs) * sizeof(double); }
 
 int threads_for(int E, int N) { return ((E * N + 31) / 32) * 32; }
 
-template <int D, int Q, int NV, int PDE>
-cudaError_t launch_bvol(dgpu_batch* c, int g, bool gll_in)
+RkArgs rk_args(const dgpu_batch* c, double dt, int stage, int want_max)
 {
-	const BGroup& G = c->hgroups[g];
-	if (G.n_vol == 0)
-		return cudaSuccess;
-	const int blocks = (G.n_vol + G.E - 1) / G.E, thr = threads_for(G.E, TPShape<D, Q>::N);
-	if (gll_in)
-		bvol_group_kernel<D, Q, NV, PDE, true><<<blocks, thr, bvol_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), g, c->u);
-	else
-		bvol_group_kernel<D, Q, NV, PDE, false><<<blocks, thr, bvol_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), g, c->ug);
-	c->launches++;
-	return cudaGetLastError();
-}
-
-template <int D, int Q, int NV>
-cudaError_t launch_blift(dgpu_batch* c, int g, int mode, double dt, int stage, int want_max)
-{
-	const BGroup& G = c->hgroups[g];
-	if (G.n_vol == 0)
-		return cudaSuccess;
-	const int blocks = (G.n_vol + G.E - 1) / G.E, thr = threads_for(G.E, TPShape<D, Q>::N);
 	RkArgs rk;
 	rk.u = c->ug;
 	rk.u0 = c->u0;
@@ -158,10 +150,39 @@ cudaError_t launch_blift(dgpu_batch* c, int g, int mode, double dt, int stage, i
 	rk.stage = stage;
 	rk.positivity = c->positivity;
 	rk.want_max = want_max;
-	if (mode == kModeRhs)
-		blift_group_kernel<D, Q, NV, kModeRhs><<<blocks, thr, blift_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), g, rk);
+	return rk;
+}
+
+// ---- tensor-product groups ----
+template <int D, int Q, int NV, int PDE>
+cudaError_t launch_bvol(dgpu_batch* c, int g, bool gll_in)
+{
+	const int t = c->gl[g].idx;
+	const BGroup& G = c->hgroups[t];
+	if (G.n_vol == 0)
+		return cudaSuccess;
+	const int blocks = (G.n_vol + G.E - 1) / G.E, thr = threads_for(G.E, TPShape<D, Q>::N);
+	if (gll_in)
+		bvol_group_kernel<D, Q, NV, PDE, true><<<blocks, thr, bvol_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), t, c->u);
 	else
-		blift_group_kernel<D, Q, NV, kModeRkGl><<<blocks, thr, blift_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), g, rk);
+		bvol_group_kernel<D, Q, NV, PDE, false><<<blocks, thr, bvol_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), t, c->ug);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV>
+cudaError_t launch_blift(dgpu_batch* c, int g, int mode, double dt, int stage, int want_max)
+{
+	const int t = c->gl[g].idx;
+	const BGroup& G = c->hgroups[t];
+	if (G.n_vol == 0)
+		return cudaSuccess;
+	const int blocks = (G.n_vol + G.E - 1) / G.E, thr = threads_for(G.E, TPShape<D, Q>::N);
+	const RkArgs rk = rk_args(c, dt, stage, want_max);
+	if (mode == kModeRhs)
+		blift_group_kernel<D, Q, NV, kModeRhs><<<blocks, thr, blift_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), t, rk);
+	else
+		blift_group_kernel<D, Q, NV, kModeRkGl><<<blocks, thr, blift_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), t, rk);
 	c->launches++;
 	return cudaGetLastError();
 }
@@ -169,33 +190,73 @@ cudaError_t launch_blift(dgpu_batch* c, int g, int mode, double dt, int stage, i
 template <int D, int Q, int NV>
 cudaError_t launch_bconv(dgpu_batch* c, int g, bool to_gl)
 {
-	const BGroup& G = c->hgroups[g];
+	const int t = c->gl[g].idx;
+	const BGroup& G = c->hgroups[t];
 	if (G.n_vol == 0)
 		return cudaSuccess;
 	const int blocks = (G.n_vol + G.E - 1) / G.E, thr = threads_for(G.E, TPShape<D, Q>::N);
 	if (to_gl)
-		bconvert_group_kernel<D, Q, NV, true><<<blocks, thr, bconv_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), g, c->u, c->ug);
+		bconvert_group_kernel<D, Q, NV, true><<<blocks, thr, bconv_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), t, c->u, c->ug);
 	else
-		bconvert_group_kernel<D, Q, NV, false><<<blocks, thr, bconv_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), g, c->ug, c->u);
+		bconvert_group_kernel<D, Q, NV, false><<<blocks, thr, bconv_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), t, c->ug, c->u);
 	c->launches++;
 	return cudaGetLastError();
 }
 
-template <int D, int NV, int PDE, int FLUX>
-cudaError_t launch_bface_q(dgpu_batch* c, int qf)
+// ---- dense groups ----
+template <int D, int NV, int PDE>
+cudaError_t launch_dvol(dgpu_batch* c, int g, bool gll_in)
 {
-	const int n = c->qf_begin[qf + 1] - c->qf_begin[qf];
-	if (n == 0)
+	const int t = c->gl[g].idx;
+	const DGroup& G = c->hdgroups[t];
+	if (G.n_vol == 0)
 		return cudaSuccess;
-	const int* faces = c->d_faces_by_q + c->qf_begin[qf];
-	const long long items = (long long)n * (D == 2 ? qf : qf * qf);
-	const unsigned blocks = (unsigned)((items + 255) / 256);
-	switch (qf) {
-	case 2: bface_group_kernel<D, 2, NV, PDE, FLUX><<<blocks, 256, 0, c->stream>>>(c->params(), faces, n); break;
-	case 3: bface_group_kernel<D, 3, NV, PDE, FLUX><<<blocks, 256, 0, c->stream>>>(c->params(), faces, n); break;
-	case 4: bface_group_kernel<D, 4, NV, PDE, FLUX><<<blocks, 256, 0, c->stream>>>(c->params(), faces, n); break;
-	default: bface_group_kernel<D, 5, NV, PDE, FLUX><<<blocks, 256, 0, c->stream>>>(c->params(), faces, n); break;
-	}
+	const int blocks = (G.n_vol + G.E - 1) / G.E;
+	dvol_group_kernel<D, NV, PDE><<<blocks, 256, dvol_smem(NV, G, G.E), c->stream>>>(c->params(), t,
+	                                                                                  gll_in ? c->u : c->ug);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int NV>
+cudaError_t launch_dlift(dgpu_batch* c, int g, int mode, double dt, int stage, int want_max)
+{
+	const int t = c->gl[g].idx;
+	const DGroup& G = c->hdgroups[t];
+	if (G.n_vol == 0)
+		return cudaSuccess;
+	const int blocks = (G.n_vol + G.E - 1) / G.E;
+	const RkArgs rk = rk_args(c, dt, stage, want_max);
+	if (mode == kModeRhs)
+		dlift_group_kernel<NV, kModeRhs><<<blocks, 256, dlift_smem(NV, G, G.E), c->stream>>>(c->params(), t, rk);
+	else
+		dlift_group_kernel<NV, kModeRkGl><<<blocks, 256, dlift_smem(NV, G, G.E), c->stream>>>(c->params(), t, rk);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+// the RK state of a dense group is its coefficient vector: u <-> ug is a copy of the group's range
+cudaError_t copy_dense(dgpu_batch* c, int g, bool to_gl)
+{
+	const DGroup& G = c->hdgroups[c->gl[g].idx];
+	if (G.n_vol == 0)
+		return cudaSuccess;
+	const size_t n = (size_t)G.n_vol * c->nv * G.n_vs;
+	const double* src = to_gl ? c->u : c->ug;
+	double* dst = to_gl ? c->ug : c->u;
+	return cudaMemcpyAsync(dst + G.state_off, src + G.state_off, n * sizeof(double), cudaMemcpyDeviceToDevice,
+	                       c->stream);
+}
+
+// ---- all groups ----
+template <int D, int NV, int PDE, int FLUX>
+cudaError_t launch_face_nodes(dgpu_batch* c, long long lo, long long hi, int blocks)
+{
+	if (hi <= lo)
+		return cudaSuccess;
+	if (blocks <= 0)
+		blocks = (int)std::min<long long>((hi - lo + 255) / 256, 1ll << 30);
+	bface_nodes_kernel<D, NV, PDE, FLUX><<<blocks, 256, 0, c->stream>>>(c->params(), c->d_node_face, lo, hi);
 	c->launches++;
 	return cudaGetLastError();
 }
@@ -216,14 +277,7 @@ cudaError_t launch_fused_vol(dgpu_batch* c, bool gll_in)
 template <int D, int NV>
 cudaError_t launch_fused_lift(dgpu_batch* c, int mode, double dt, int stage, int want_max)
 {
-	RkArgs rk;
-	rk.u = c->ug;
-	rk.u0 = c->u0;
-	rk.rhs = c->rhs;
-	rk.dt = dt;
-	rk.stage = stage;
-	rk.positivity = c->positivity;
-	rk.want_max = want_max;
+	const RkArgs rk = rk_args(c, dt, stage, want_max);
 	if (mode == kModeRhs)
 		blift_fused_kernel<D, NV, kModeRhs><<<c->fused_blocks_lift, 256, c->fused_lift_smem, c->stream>>>(
 			c->params(), c->d_tiles, c->n_tiles, rk);
@@ -234,24 +288,14 @@ cudaError_t launch_fused_lift(dgpu_batch* c, int mode, double dt, int stage, int
 	return cudaGetLastError();
 }
 
-template <int D, int NV, int PDE, int FLUX>
-cudaError_t launch_fused_face(dgpu_batch* c)
-{
-	bface_fused_kernel<D, NV, PDE, FLUX><<<c->fused_blocks_face, 256, 0, c->stream>>>(
-		c->params(), c->d_faces_by_q, c->d_qf_begin, c->n_face_items);
-	c->launches++;
-	return cudaGetLastError();
-}
-
 template <int D, int Q, int NV, int PDE>
-cudaError_t bind_group(dgpu_batch* c, int g)
+cudaError_t bind_tp_group(dgpu_batch* c, int g)
 {
 	GroupLaunch& L = c->gl[g];
 	L.vol = launch_bvol<D, Q, NV, PDE>;
 	L.lift = launch_blift<D, Q, NV>;
 	L.conv = launch_bconv<D, Q, NV>;
-	L.N = TPShape<D, Q>::N;
-	L.E_max = std::max(1, 256 / L.N);
+	L.E_max = std::max(1, 256 / TPShape<D, Q>::N);
 	const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
 	const int E = L.E_max;
 	cudaError_t e;
@@ -273,34 +317,46 @@ cudaError_t bind_group(dgpu_batch* c, int g)
 	return cudaSuccess;
 }
 
-template <int D, int NV, int PDE>
-cudaError_t bind_groups_q(dgpu_batch* c)
+template <int D, int NV, int PDE, int FLUX>
+cudaError_t bind_all(dgpu_batch* c)
 {
-	for (int g = 0; g < c->n_groups; ++g) {
-		cudaError_t e;
-		switch (c->hgroups[g].q) {
-		case 2: e = bind_group<D, 2, NV, PDE>(c, g); break;
-		case 3: e = bind_group<D, 3, NV, PDE>(c, g); break;
-		case 4: e = bind_group<D, 4, NV, PDE>(c, g); break;
-		default: e = bind_group<D, 5, NV, PDE>(c, g); break;
+	size_t dvol_max = 0, dlift_max = 0;
+	for (int g = 0; g < c->n_all; ++g) {
+		cudaError_t e = cudaSuccess;
+		if (c->gl[g].dense) {
+			const DGroup& G = c->hdgroups[c->gl[g].idx];
+			c->gl[g].vol = launch_dvol<D, NV, PDE>;
+			c->gl[g].lift = launch_dlift<NV>;
+			c->gl[g].conv = copy_dense;
+			c->gl[g].E_max = G.E;
+			dvol_max = std::max(dvol_max, dvol_smem(NV, G, G.E));
+			dlift_max = std::max(dlift_max, dlift_smem(NV, G, G.E));
+			c->fused_vol_smem = std::max(c->fused_vol_smem, sizeof(BatchOps) + dvol_smem(NV, G, G.E_fused));
+			c->fused_lift_smem = std::max(c->fused_lift_smem, sizeof(BatchOps) + dlift_smem(NV, G, G.E_fused));
+			continue;
+		}
+		switch (c->hgroups[c->gl[g].idx].q) {
+		case 2: e = bind_tp_group<D, 2, NV, PDE>(c, g); break;
+		case 3: e = bind_tp_group<D, 3, NV, PDE>(c, g); break;
+		case 4: e = bind_tp_group<D, 4, NV, PDE>(c, g); break;
+		default: e = bind_tp_group<D, 5, NV, PDE>(c, g); break;
 		}
 		if (e != cudaSuccess)
 			return e;
 	}
-	return cudaSuccess;
-}
-
-template <int D, int NV, int PDE, int FLUX>
-cudaError_t bind_all(dgpu_batch* c)
-{
-	cudaError_t e = bind_groups_q<D, NV, PDE>(c);
-	if (e != cudaSuccess)
-		return e;
+	const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+	cudaError_t e;
+	if (c->n_dense > 0) {
+		if ((e = cudaFuncSetAttribute(dvol_group_kernel<D, NV, PDE>, A, (int)dvol_max)))
+			return e;
+		if ((e = cudaFuncSetAttribute(dlift_group_kernel<NV, kModeRhs>, A, (int)dlift_max)))
+			return e;
+		if ((e = cudaFuncSetAttribute(dlift_group_kernel<NV, kModeRkGl>, A, (int)dlift_max)))
+			return e;
+	}
 	c->fused_vol = launch_fused_vol<D, NV, PDE>;
 	c->fused_lift = launch_fused_lift<D, NV>;
-	c->fused_face = launch_fused_face<D, NV, PDE, FLUX>;
-	c->face_q = launch_bface_q<D, NV, PDE, FLUX>;
-	const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+	c->face_nodes = launch_face_nodes<D, NV, PDE, FLUX>;
 	if ((e = cudaFuncSetAttribute(bvol_fused_kernel<D, NV, PDE, true>, A, (int)c->fused_vol_smem)))
 		return e;
 	if ((e = cudaFuncSetAttribute(bvol_fused_kernel<D, NV, PDE, false>, A, (int)c->fused_vol_smem)))
@@ -317,7 +373,8 @@ cudaError_t bind_all(dgpu_batch* c)
 	c->fused_blocks_vol = std::max(1, std::min(c->n_tiles, sms * std::max(1, per_sm)));
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blift_fused_kernel<D, NV, kModeRkGl>, 256, c->fused_lift_smem);
 	c->fused_blocks_lift = std::max(1, std::min(c->n_tiles, sms * std::max(1, per_sm)));
-	c->fused_blocks_face = (int)std::max<long long>(1, std::min<long long>((c->n_face_items + 255) / 256, (long long)sms * 8));
+	c->fused_blocks_face = (int)std::max<long long>(1, std::min<long long>((c->qnode[kQMax + 1] + 255) / 256,
+	                                                                       (long long)sms * 8));
 	return cudaGetLastError();
 }
 
@@ -333,21 +390,31 @@ cudaError_t bind(dgpu_batch* c)
 	return bind_all<3, 5, kEuler, kLaxFriedrichs>(c);
 }
 
-void free_batch(dgpu_batch* c)
+void drop_graphs(dgpu_batch* c)
 {
 	for (auto& gm : c->graph)
 		for (auto& g : gm)
-			if (g)
+			if (g) {
 				cudaGraphExecDestroy(g);
-	void* ptrs[] = {c->d_ops, c->d_groups, c->d_elf, c->d_fbase, c->gmet, c->inv_wJ, c->fgeo, c->u, c->ug, c->u0,
-	                c->rhs, c->vol_gl, c->traces, c->nnf, c->max_bits, c->err_flag, c->n_corr, c->d_faces_by_q,
-	                c->d_qf_begin, c->d_tiles};
+				g = nullptr;
+			}
+}
+
+void free_batch(dgpu_batch* c)
+{
+	drop_graphs(c);
+	void* ptrs[] = {c->d_ops, c->d_groups, c->d_dgroups, c->d_elf, c->d_fbase, c->d_node_face, c->gmet, c->inv_wJ,
+	                c->fgeo, c->u, c->ug, c->u0, c->rhs, c->vol_gl, c->traces, c->nnf, c->max_bits, c->err_flag,
+	                c->n_corr, c->d_tiles};
 	for (void* p : ptrs)
+		if (p)
+			cudaFree(p);
+	for (void* p : c->dense_bufs)
 		if (p)
 			cudaFree(p);
 	if (c->own_stream && c->stream)
 		cudaStreamDestroy(c->stream);
-	for (int j = 0; j < kQMax; ++j) {
+	for (int j = 0; j < kBranches; ++j) {
 		if (c->aux[j])
 			cudaStreamDestroy(c->aux[j]);
 		if (c->ev_join[j])
@@ -366,8 +433,8 @@ cudaError_t upload_vec(T** dst, const std::vector<T>& src)
 	return cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
 }
 
-// Form 2: the calls of `launch(j, i)` for i in items run on the branch streams, forked from and joined back into
-// the context's stream (under stream capture: parallel branches of the graph).
+// Form 2: the calls launch(i) run on the branch streams, forked from and joined back into the context's stream
+// (under stream capture: parallel branches of the graph).
 template <typename F>
 dgpu_status on_branches(dgpu_batch* c, int n_items, F launch)
 {
@@ -375,7 +442,7 @@ dgpu_status on_branches(dgpu_batch* c, int n_items, F launch)
 	BATCH_CUDA(c, cudaEventRecord(c->ev_fork, main));
 	int j = 0;
 	for (int i = 0; i < n_items; ++i) {
-		cudaStream_t br = c->aux[j];
+		cudaStream_t br = c->aux[j % kBranches];
 		BATCH_CUDA(c, cudaStreamWaitEvent(br, c->ev_fork, 0));
 		c->stream = br;
 		const long long before = c->launches;
@@ -384,36 +451,38 @@ dgpu_status on_branches(dgpu_batch* c, int n_items, F launch)
 		BATCH_CUDA(c, e);
 		if (c->launches == before)   // nothing launched (empty group or face order): no branch
 			continue;
-		BATCH_CUDA(c, cudaEventRecord(c->ev_join[j], br));
-		BATCH_CUDA(c, cudaStreamWaitEvent(main, c->ev_join[j], 0));
+		BATCH_CUDA(c, cudaEventRecord(c->ev_join[j % kBranches], br));
+		BATCH_CUDA(c, cudaStreamWaitEvent(main, c->ev_join[j % kBranches], 0));
 		++j;
 	}
 	return DGPU_OK;
 }
 
-// One residual on GLL coefficients, or one RK stage on GL nodal values.
+// One residual on the coefficients (TP: GLL), or one RK stage on the RK state (TP: GL nodal values).
 dgpu_status enqueue_stage(dgpu_batch* c, bool rhs_mode, double dt, int stage, int want_max)
 {
 	const int lmode = rhs_mode ? kModeRhs : kModeRkGl;
 	if (c->mode == 1) {
 		BATCH_CUDA(c, c->fused_vol(c, rhs_mode));
-		BATCH_CUDA(c, c->fused_face(c));
+		BATCH_CUDA(c, c->face_nodes(c, 0, c->qnode[kQMax + 1], c->fused_blocks_face));
 		BATCH_CUDA(c, c->fused_lift(c, lmode, dt, stage, want_max));
 	} else if (c->mode == 2) {
 		dgpu_status st;
-		if ((st = on_branches(c, c->n_groups, [&](int g) { return c->gl[g].vol(c, g, rhs_mode); })) != DGPU_OK)
+		if ((st = on_branches(c, c->n_all, [&](int g) { return c->gl[g].vol(c, g, rhs_mode); })) != DGPU_OK)
 			return st;
-		if ((st = on_branches(c, kQMax - 1, [&](int i) { return c->face_q(c, i + 2); })) != DGPU_OK)
+		if ((st = on_branches(c, kQMax - 1, [&](int i) {
+			     return c->face_nodes(c, c->qnode[i + 2], c->qnode[i + 3], 0);
+		     })) != DGPU_OK)
 			return st;
-		if ((st = on_branches(c, c->n_groups,
+		if ((st = on_branches(c, c->n_all,
 		                      [&](int g) { return c->gl[g].lift(c, g, lmode, dt, stage, want_max); })) != DGPU_OK)
 			return st;
 	} else {
-		for (int g = 0; g < c->n_groups; ++g)
+		for (int g = 0; g < c->n_all; ++g)
 			BATCH_CUDA(c, c->gl[g].vol(c, g, rhs_mode));
 		for (int qf = 2; qf <= kQMax; ++qf)
-			BATCH_CUDA(c, c->face_q(c, qf));
-		for (int g = 0; g < c->n_groups; ++g)
+			BATCH_CUDA(c, c->face_nodes(c, c->qnode[qf], c->qnode[qf + 1], 0));
+		for (int g = 0; g < c->n_all; ++g)
 			BATCH_CUDA(c, c->gl[g].lift(c, g, lmode, dt, stage, want_max));
 	}
 	return DGPU_OK;
@@ -422,7 +491,7 @@ dgpu_status enqueue_stage(dgpu_batch* c, bool rhs_mode, double dt, int stage, in
 dgpu_status ensure_coef(dgpu_batch* c)
 {
 	if (!c->coef_valid) {
-		for (int g = 0; g < c->n_groups; ++g)
+		for (int g = 0; g < c->n_all; ++g)
 			BATCH_CUDA(c, c->gl[g].conv(c, g, false));
 		c->coef_valid = true;
 	}
@@ -432,7 +501,7 @@ dgpu_status ensure_coef(dgpu_batch* c)
 dgpu_status ensure_gl(dgpu_batch* c)
 {
 	if (!c->gl_valid) {
-		for (int g = 0; g < c->n_groups; ++g)
+		for (int g = 0; g < c->n_all; ++g)
 			BATCH_CUDA(c, c->gl[g].conv(c, g, true));
 		c->gl_valid = true;
 	}
@@ -450,25 +519,40 @@ dgpu_status read_max(dgpu_batch* c, double* max_rhs)
 	return DGPU_OK;
 }
 
-void drop_graphs(dgpu_batch* c)
+dgpu_status upload_group_tiles(dgpu_batch* c)
 {
-	for (auto& gm : c->graph)
-		for (auto& g : gm)
-			if (g) {
-				cudaGraphExecDestroy(g);
-				g = nullptr;
-			}
+	if (!c->hgroups.empty())
+		BATCH_CUDA(c, cudaMemcpyAsync(c->d_groups, c->hgroups.data(), c->hgroups.size() * sizeof(BGroup),
+		                              cudaMemcpyHostToDevice, c->stream));
+	if (!c->hdgroups.empty())
+		BATCH_CUDA(c, cudaMemcpyAsync(c->d_dgroups, c->hdgroups.data(), c->hdgroups.size() * sizeof(DGroup),
+		                              cudaMemcpyHostToDevice, c->stream));
+	BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
 }
 
-}  // namespace
+void set_group_E(dgpu_batch* c, int g, int E)
+{
+	if (c->gl[g].dense)
+		c->hdgroups[c->gl[g].idx].E = E;
+	else
+		c->hgroups[c->gl[g].idx].E = E;
+}
 
-extern "C" {
+int type_faces(int t) { return t == DGPU_TET ? 4 : (t == DGPU_HEX ? 6 : (t == DGPU_QUAD ? 4 : 5)); }
 
-dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu_tp_operators* ops,
-                              const int* vol_group, const dgpu_mesh* mesh, dgpu_batch** out)
+// ---- creation ----
+struct GroupIn {
+	bool dense;
+	const dgpu_tp_operators* tp;
+	const dgpu_dense_operators* dn;
+};
+
+dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gin, const int* vol_group,
+                        const dgpu_mesh* mesh, const int* face_ord, dgpu_batch** out)
 {
 	g_batch_error.clear();
-	if (!phys || n_groups < 1 || !ops || !vol_group || !mesh || !out)
+	if (!phys || gin.empty() || !vol_group || !mesh || !out)
 		return bfail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL argument");
 	*out = nullptr;
 	const int d = phys->d;
@@ -498,191 +582,332 @@ dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu
 	c->positivity = (phys->pde == DGPU_PDE_EULER && phys->positivity) ? 1 : 0;
 	for (int k = 0; k < 3; ++k)
 		c->b_adv[k] = phys->b_adv[k];
-	c->n_groups = n_groups;
 	c->n_vol = mesh->n_volumes;
 	c->n_face = mesh->n_faces;
-	const int nv = c->nv, nV = c->n_vol, nF = c->n_face;
-	auto reject = [&](dgpu_status st, const char* m) {
+	const int nv = c->nv, nV = c->n_vol, nF = c->n_face, nG = (int)gin.size();
+	auto reject = [&](dgpu_status st, const std::string& m) {
+		free_batch(c);
 		delete c;
 		return bfail(nullptr, st, m);
 	};
 
-	// ---- groups and their operators ----
-	c->hgroups.resize(n_groups);
-	c->hops.resize(n_groups);
-	std::vector<std::vector<double>> w(n_groups);
-	for (int g = 0; g < n_groups; ++g) {
-		const dgpu_tp_operators& o = ops[g];
-		if ((d == 2 && o.elem_type != DGPU_QUAD) || (d == 3 && o.elem_type != DGPU_HEX) || o.p < 1 || o.p > kQMax - 1)
-			return reject(DGPU_ERR_UNSUPPORTED, "groups must be QUAD (d=2) or HEX (d=3) with p in 1..4");
-		if (!o.cv0_vs_vc || !o.cv1_vs_vc || !o.cv0_vs_fc || !o.w_vc)
-			return reject(DGPU_ERR_INVALID_ARGUMENT, "NULL operator");
-		if (c->positivity && (!o.ccSB0_vs_vs || !o.ccBS0_vs_vs))
-			return reject(DGPU_ERR_INVALID_ARGUMENT, "positivity needs ccSB0/ccBS0");
-		const int q = o.p + 1;
-		for (int h = 0; h < g; ++h)
-			if (c->hgroups[h].q == q)
-				return reject(DGPU_ERR_INVALID_ARGUMENT, "two groups with the same p");
-		memset(&c->hops[g], 0, sizeof(BatchOps));
-		if (!derive_tp_ops(&o, d, &c->hops[g].t))
-			return reject(DGPU_ERR_INVALID_ARGUMENT, "cv0_vs_vc is singular");
-		// GL(q) Lagrange at GL(qf) nodes for every face order qf >= q
-		double xq[kQMax], xf[kQMax];
-		gauss_legendre_nodes(q, xq);
-		for (int qf = q; qf <= kQMax; ++qf) {
-			gauss_legendre_nodes(qf, xf);
-			for (int i = 0; i < qf; ++i)
-				for (int a = 0; a < q; ++a)
-					c->hops[g].Iup[qf][i][a] = lagrange_value(xq, q, a, xf[i]);
-		}
-		c->hgroups[g].q = q;
-		const int N = (d == 2 ? q * q : q * q * q);
-		w[g].resize(N);
-		for (int n = 0; n < N; ++n) {
-			int r = n;
-			double x = 1.0;
-			for (int k = 0; k < d; ++k) {
-				x *= o.w_vc[r % q];
-				r /= q;
+	// ---- groups: TP first (caller order), then dense (caller order) ----
+	c->caller_to_internal.assign(nG, -1);
+	std::vector<int> internal_to_caller;
+	for (int pass = 0; pass < 2; ++pass)
+		for (int g = 0; g < nG; ++g)
+			if (gin[g].dense == (pass == 1)) {
+				GroupLaunch L;
+				L.dense = gin[g].dense;
+				L.idx = L.dense ? c->n_dense++ : c->n_tp++;
+				c->caller_to_internal[g] = (int)c->gl.size();
+				internal_to_caller.push_back(g);
+				c->gl.push_back(L);
 			}
-			w[g][n] = x;
+	c->n_all = nG;
+	c->hgroups.resize(c->n_tp);
+	c->hops.resize(c->n_tp);
+	c->hdgroups.resize(c->n_dense);
+	std::vector<int> g_q(nG), g_nvs(nG), g_nvc(nG), g_type(nG);   // per internal group
+	std::vector<std::vector<double>> w(nG);                         // volume cubature weights per node
+	std::vector<const dgpu_dense_operators*> dops(c->n_dense);
+	for (int ig = 0; ig < nG; ++ig) {
+		const GroupIn& in = gin[internal_to_caller[ig]];
+		if (!in.dense) {
+			if (!in.tp)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "NULL operator set");
+			const dgpu_tp_operators& o = *in.tp;
+			if ((d == 2 && o.elem_type != DGPU_QUAD) || (d == 3 && o.elem_type != DGPU_HEX) || o.p < 1 ||
+			    o.p > kQMax - 1)
+				return reject(DGPU_ERR_UNSUPPORTED, "TP groups must be QUAD (d=2) or HEX (d=3) with p in 1..4");
+			if (!o.cv0_vs_vc || !o.cv1_vs_vc || !o.cv0_vs_fc || !o.w_vc)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "NULL operator");
+			if (c->positivity && (!o.ccSB0_vs_vs || !o.ccBS0_vs_vs))
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "positivity needs ccSB0/ccBS0");
+			const int q = o.p + 1, t = c->gl[ig].idx;
+			for (int h = 0; h < ig; ++h)
+				if (!c->gl[h].dense && g_q[h] == q)
+					return reject(DGPU_ERR_INVALID_ARGUMENT, "two TP groups with the same p");
+			memset(&c->hops[t], 0, sizeof(BatchOps));
+			if (!derive_tp_ops(&o, d, &c->hops[t].t))
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "cv0_vs_vc is singular");
+			// GL(q) Lagrange at GL(qf) nodes for every face order qf >= q
+			double xq[kQMax], xf[kQMax];
+			gauss_legendre_nodes(q, xq);
+			for (int qf = q; qf <= kQMax; ++qf) {
+				gauss_legendre_nodes(qf, xf);
+				for (int i = 0; i < qf; ++i)
+					for (int a = 0; a < q; ++a)
+						c->hops[t].Iup[qf][i][a] = lagrange_value(xq, q, a, xf[i]);
+			}
+			c->hgroups[t].q = q;
+			const int N = (d == 2 ? q * q : q * q * q);
+			g_q[ig] = q;
+			g_nvs[ig] = g_nvc[ig] = N;
+			g_type[ig] = o.elem_type;
+			w[ig].resize(N);
+			for (int n = 0; n < N; ++n) {
+				int r = n;
+				double x = 1.0;
+				for (int k = 0; k < d; ++k) {
+					x *= o.w_vc[r % q];
+					r /= q;
+				}
+				w[ig][n] = x;
+			}
+		} else {
+			const dgpu_dense_operators* op = in.dn;
+			if (!op)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "NULL operator set");
+			if (d != 3 || (op->elem_type != DGPU_TET && op->elem_type != DGPU_WEDGE && op->elem_type != DGPU_PYR))
+				return reject(DGPU_ERR_UNSUPPORTED, "dense groups must be TET, WEDGE or PYR (d = 3)");
+			if (op->p < 1 || op->p > kQMax - 1 || op->n_vs < 1 || op->n_vc < 1 || op->n_vs > 1024 ||
+			    op->n_vc > 4096 || op->n_lf != type_faces(op->elem_type) || op->n_ord < 1 || op->n_ord > kMaxOrd ||
+			    !op->cv0_vs_vc || !op->cv1_vs_vc || !op->w_vc || !op->n_fc || !op->cv0_vs_fc || !op->w_fc)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "incomplete dense operator set");
+			if (c->positivity)
+				return reject(DGPU_ERR_UNSUPPORTED, "positivity is provided for QUAD/HEX groups only");
+			const int t = c->gl[ig].idx;
+			dops[t] = op;
+			g_q[ig] = op->p + 1;
+			g_nvs[ig] = op->n_vs;
+			g_nvc[ig] = op->n_vc;
+			g_type[ig] = op->elem_type;
+			w[ig].assign(op->w_vc, op->w_vc + op->n_vc);
+			DGroup& G = c->hdgroups[t];
+			memset(&G, 0, sizeof G);
+			G.n_vs = op->n_vs;
+			G.n_vc = op->n_vc;
+			G.n_lf = op->n_lf;
+			G.n_ord = op->n_ord;
+			G.E = std::max(1, 256 / op->n_vc);
+			while (G.E > 1 && (size_t)G.E * DSmem::vol(nv, G.n_vs, G.n_vc) * 8 > 96 * 1024)
+				G.E /= 2;
+			G.E_fused = G.E;
+			if ((size_t)DSmem::vol(nv, G.n_vs, G.n_vc) * 8 > 200 * 1024)
+				return reject(DGPU_ERR_UNSUPPORTED, "dense operator set too large for one volume per CTA");
 		}
 	}
 	// ---- volumes: group-sorted order, offsets ----
-	std::vector<int> count(n_groups, 0);
+	std::vector<int> count(nG, 0), vg(nV);
 	for (int v = 0; v < nV; ++v) {
-		if (vol_group[v] < 0 || vol_group[v] >= n_groups)
+		if (vol_group[v] < 0 || vol_group[v] >= nG)
 			return reject(DGPU_ERR_INVALID_ARGUMENT, "vol_group out of range");
-		count[vol_group[v]]++;
+		vg[v] = c->caller_to_internal[vol_group[v]];
+		count[vg[v]]++;
 	}
 	c->list_off.resize(nV + 1);
 	std::vector<long long> list_vc_off(nV + 1);
 	long long so = 0, vco = 0;
 	for (int v = 0; v < nV; ++v) {
-		const int q = c->hgroups[vol_group[v]].q, N = (d == 2 ? q * q : q * q * q);
 		c->list_off[v] = so;
 		list_vc_off[v] = vco;
-		so += (long long)nv * N;
-		vco += N;
+		so += (long long)nv * g_nvs[vg[v]];
+		vco += g_nvc[vg[v]];
 	}
 	c->list_off[nV] = so;
 	c->ns = (size_t)so;
 	c->order.resize(nV);
 	std::vector<int> sorted_pos(nV);
+	std::vector<long long> g_elem0(nG), g_state(nG), g_gmet(nG), g_wj(nG);
 	{
 		long long elem = 0, st_off = 0, gm_off = 0, wj_off = 0;
-		std::vector<int> next(n_groups);
-		for (int g = 0; g < n_groups; ++g) {
-			const int q = c->hgroups[g].q, N = (d == 2 ? q * q : q * q * q);
-			BGroup& G = c->hgroups[g];
-			G.n_vol = count[g];
-			G.elem0 = elem;
-			G.state_off = st_off;
-			G.gmet_off = gm_off;
-			G.wj_off = wj_off;
-			G.E = std::max(1, 256 / N);
+		std::vector<int> next(nG);
+		for (int g = 0; g < nG; ++g) {   // internal order
+			g_elem0[g] = elem;
+			g_state[g] = st_off;
+			g_gmet[g] = gm_off;
+			g_wj[g] = wj_off;
 			next[g] = (int)elem;
 			elem += count[g];
-			st_off += (long long)count[g] * nv * N;
-			gm_off += (long long)count[g] * d * d * N;
-			wj_off += (long long)count[g] * N;
+			st_off += (long long)count[g] * nv * g_nvs[g];
+			gm_off += (long long)count[g] * d * d * g_nvc[g];
+			if (!c->gl[g].dense)
+				wj_off += (long long)count[g] * g_nvc[g];
 		}
 		for (int v = 0; v < nV; ++v) {
-			const int p = next[vol_group[v]]++;
+			const int p = next[vg[v]]++;
 			c->order[p] = v;
 			sorted_pos[v] = p;
 		}
 	}
+	for (int g = 0; g < nG; ++g) {
+		if (c->gl[g].dense) {
+			DGroup& G = c->hdgroups[c->gl[g].idx];
+			G.n_vol = count[g];
+			G.elem0 = g_elem0[g];
+			G.state_off = g_state[g];
+			G.gmet_off = g_gmet[g];
+		} else {
+			BGroup& G = c->hgroups[c->gl[g].idx];
+			G.n_vol = count[g];
+			G.elem0 = g_elem0[g];
+			G.state_off = g_state[g];
+			G.gmet_off = g_gmet[g];
+			G.wj_off = g_wj[g];
+			G.E = std::max(1, 256 / g_nvs[g]);
+		}
+	}
 	c->sorted_off.resize(nV);
 	std::vector<double> gmet, inv_wJ;
-	for (int g = 0; g < n_groups; ++g) {
-		const int q = c->hgroups[g].q, N = (d == 2 ? q * q : q * q * q);
-		for (int e = 0; e < c->hgroups[g].n_vol; ++e) {
-			const int p = (int)c->hgroups[g].elem0 + e, v = c->order[p];
-			c->sorted_off[p] = c->hgroups[g].state_off + (long long)e * nv * N;
+	std::vector<std::vector<double>> inv_J(c->n_dense);
+	for (int g = 0; g < nG; ++g) {
+		const int N = g_nvc[g];
+		for (int e = 0; e < count[g]; ++e) {
+			const int p = (int)g_elem0[g] + e, v = c->order[p];
+			c->sorted_off[p] = g_state[g] + (long long)e * nv * g_nvs[g];
 			const double* m = mesh->metrics_vc + list_vc_off[v] * d * d;
 			const double* J = mesh->jacobian_det_vc + list_vc_off[v];
 			for (int j = 0; j < d; ++j)
 				for (int i = 0; i < d; ++i)
 					for (int n = 0; n < N; ++n)
 						gmet.push_back(w[g][n] * m[n + (size_t)N * (i + d * j)]);
-			for (int n = 0; n < N; ++n) {
+			for (int n = 0; n < N; ++n)
 				if (!(J[n] > 0.0))
 					return reject(DGPU_ERR_INVALID_ARGUMENT, "non-positive jacobian_det_vc");
-				inv_wJ.push_back(1.0 / (w[g][n] * J[n]));
+			if (c->gl[g].dense) {
+				for (int n = 1; n < N; ++n)
+					if (fabs(J[n] - J[0]) > 1e-12 * J[0])
+						return reject(DGPU_ERR_UNSUPPORTED,
+						              "TET/WEDGE/PYR volumes must be affine (constant jacobian_det_vc)");
+				inv_J[c->gl[g].idx].push_back(1.0 / J[0]);
+			} else {
+				for (int n = 0; n < N; ++n)
+					inv_wJ.push_back(1.0 / (w[g][n] * J[n]));
 			}
 		}
 	}
-	// ---- faces: order p_f = max of the sides, face data at its q_f points ----
-	std::vector<int> face_q(nF);
-	std::vector<long long> fbase(nF + 1);
-	std::vector<int4> elf((size_t)nV * 2 * d, int4{-1, -1, -1, 0});
-	long long fb = 0;
+	// ---- faces: order p_f = max of the sides; internal face ids by increasing q_f ----
+	std::vector<int> face_q(nF), face_nfc(nF);
 	for (int f = 0; f < nF; ++f) {
 		int qf = 0;
 		for (int s = 0; s < 2; ++s) {
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
 			if (v < 0)
 				return reject(DGPU_ERR_UNSUPPORTED, "boundary faces are not supported (periodic meshes)");
-			if (v >= nV || lf < 0 || lf >= 2 * d)
+			if (v >= nV || lf < 0 || lf >= type_faces(g_type[vg[v]]))
 				return reject(DGPU_ERR_INVALID_ARGUMENT, "bad face connectivity");
-			qf = std::max(qf, c->hgroups[vol_group[v]].q);
+			qf = std::max(qf, g_q[vg[v]]);
 		}
 		face_q[f] = qf;
-		fbase[f] = fb;
-		const int nff = (d == 2 ? qf : qf * qf);
-		fb += nff;
+		int nfc = -1;
+		for (int s = 0; s < 2; ++s) {
+			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s], g = vg[v];
+			const int ord = face_ord ? face_ord[2 * f + s] : 0;
+			int n_s;
+			if (c->gl[g].dense) {
+				const dgpu_dense_operators* op = dops[c->gl[g].idx];
+				if (ord < 0 || ord >= op->n_ord)
+					return reject(DGPU_ERR_INVALID_ARGUMENT, "face_ord out of range");
+				const int k = (lf * op->n_ord + ord) * kQMax + (qf - 1);
+				if (!op->cv0_vs_fc[k] || op->n_fc[k] < 1)
+					return reject(DGPU_ERR_INVALID_ARGUMENT, "missing dense face operator");
+				n_s = op->n_fc[k];
+			} else {
+				if (ord != 0)
+					return reject(DGPU_ERR_UNSUPPORTED, "QUAD/HEX volumes must see their faces unpermuted (face_ord 0)");
+				n_s = (d == 2 ? qf : qf * qf);
+			}
+			if (nfc >= 0 && n_s != nfc)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "the two sides of a face have different face node counts");
+			nfc = n_s;
+		}
+		face_nfc[f] = nfc;
+	}
+	std::vector<long long> caller_fc_off(nF + 1);   // the caller's face-node offsets (face-list order)
+	caller_fc_off[0] = 0;
+	for (int f = 0; f < nF; ++f)
+		caller_fc_off[f + 1] = caller_fc_off[f] + face_nfc[f];
+	std::vector<int> by_q(nF);                      // internal face id -> caller face
+	for (int f = 0; f < nF; ++f)
+		by_q[f] = f;
+	std::stable_sort(by_q.begin(), by_q.end(), [&](int a, int b) { return face_q[a] < face_q[b]; });
+	std::vector<int> internal_face(nF);
+	std::vector<long long> fbase(nF + 1);
+	std::vector<int> node_face;
+	long long fb = 0;
+	int cur_q = 0;
+	for (int k = 0; k < nF; ++k) {
+		const int f = by_q[k];
+		internal_face[f] = k;
+		while (cur_q < face_q[f])
+			c->qnode[++cur_q] = fb;
+		fbase[k] = fb;
+		for (int i = 0; i < face_nfc[f]; ++i)
+			node_face.push_back(k);
+		fb += face_nfc[f];
+	}
+	while (cur_q <= kQMax)
+		c->qnode[++cur_q] = fb;
+	fbase[nF] = fb;
+	std::vector<int4> elf((size_t)nV * kMaxLf, int4{-1, -1, -1, 0});
+	for (int f = 0; f < nF; ++f) {
+		if (mesh->nc_fc)
+			for (int i = 0; i < face_nfc[f]; ++i)
+				if (mesh->nc_fc[caller_fc_off[f] + i] != i)
+					return reject(DGPU_ERR_UNSUPPORTED, "the batched path needs face nodes in one canonical order "
+					                                    "(identity nc_fc); orient dense faces with face_ord");
 		for (int s = 0; s < 2; ++s) {
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
-			int4& slot = elf[(size_t)sorted_pos[v] * 2 * d + lf];
+			int4& slot = elf[(size_t)sorted_pos[v] * kMaxLf + lf];
 			if (slot.x != -1)
 				return reject(DGPU_ERR_INVALID_ARGUMENT, "a volume face appears twice in the face list");
-			slot = int4{f, s, qf, 0};
+			slot = int4{internal_face[f], s, face_q[f], face_ord ? face_ord[2 * f + s] : 0};
 		}
-		if (mesh->nc_fc)
-			for (int i = 0; i < nff; ++i)
-				if (mesh->nc_fc[fbase[f] + i] != i)
-					return reject(DGPU_ERR_UNSUPPORTED, "the batched path needs aligned faces (identity nc_fc)");
 	}
-	fbase[nF] = fb;
-	for (size_t i = 0; i < elf.size(); ++i)
-		if (elf[i].x < 0)
-			return reject(DGPU_ERR_INVALID_ARGUMENT, "a volume face is missing from the face list");
-	// face weights: q_f is always the q of one of the groups, whose GL weights the caller gave
+	for (int p = 0; p < nV; ++p)
+		for (int lf = 0; lf < type_faces(g_type[vg[c->order[p]]]); ++lf)
+			if (elf[(size_t)p * kMaxLf + lf].x < 0)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "a volume face is missing from the face list");
+	// face weights at the canonical nodes: the side-0 volume's face rule (TP: GL, the caller's weights when a TP
+	// group of that order exists)
 	double wq[kQMax + 1][kQMax] = {{0}};
-	for (int g = 0; g < n_groups; ++g)
-		for (int a = 0; a < c->hgroups[g].q; ++a)
-			wq[c->hgroups[g].q][a] = ops[g].w_vc[a];
+	bool have_q[kQMax + 1] = {false};
+	for (int g = 0; g < nG; ++g)
+		if (!c->gl[g].dense) {
+			const dgpu_tp_operators* o = gin[internal_to_caller[g]].tp;
+			for (int a = 0; a < g_q[g]; ++a)
+				wq[g_q[g]][a] = o->w_vc[a];
+			have_q[g_q[g]] = true;
+		}
+	for (int q = 1; q <= kQMax; ++q)
+		if (!have_q[q]) {   // GL weights 2 / ((1 - x^2) P_q'(x)^2)
+			double x[kQMax];
+			gauss_legendre_nodes(q, x);
+			for (int a = 0; a < q; ++a) {
+				double pp, dp;
+				legendre(q, x[a], &pp, &dp);
+				wq[q][a] = 2.0 / ((1.0 - x[a] * x[a]) * dp * dp);
+			}
+		}
 	std::vector<double> fgeo((size_t)(d + 1) * fb);
 	for (int f = 0; f < nF; ++f) {
-		const int qf = face_q[f], nff = (d == 2 ? qf : qf * qf);
+		const int qf = face_q[f], nff = face_nfc[f];
+		const long long base = (d + 1) * fbase[internal_face[f]];
+		const int v0 = mesh->face_vol[2 * f], lf0 = mesh->face_lf[2 * f], g0 = vg[v0];
+		const double* wf_dense = nullptr;
+		if (c->gl[g0].dense) {
+			wf_dense = dops[c->gl[g0].idx]->w_fc[lf0 * kQMax + (qf - 1)];
+			if (!wf_dense)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "missing dense face weights");
+		}
 		for (int i = 0; i < nff; ++i) {
-			const double wf = (d == 2 ? wq[qf][i] : wq[qf][i % qf] * wq[qf][i / qf]);
+			const double wf = wf_dense ? wf_dense[i] : (d == 2 ? wq[qf][i] : wq[qf][i % qf] * wq[qf][i / qf]);
 			for (int k = 0; k < d; ++k)
-				fgeo[(d + 1) * fbase[f] + (size_t)k * nff + i] = mesh->normals_fc[(fbase[f] + i) * d + k];
-			fgeo[(d + 1) * fbase[f] + (size_t)d * nff + i] = wf * mesh->jacobian_det_fc[fbase[f] + i];
+				fgeo[base + (size_t)k * nff + i] = mesh->normals_fc[(caller_fc_off[f] + i) * d + k];
+			fgeo[base + (size_t)d * nff + i] = wf * mesh->jacobian_det_fc[caller_fc_off[f] + i];
 		}
 	}
-	std::vector<int> faces_by_q;
-	for (int qf = 0; qf <= kQMax + 1; ++qf)
-		c->qf_begin[qf] = 0;
-	for (int qf = 2; qf <= kQMax; ++qf) {
-		c->qf_begin[qf] = (int)faces_by_q.size();
-		for (int f = 0; f < nF; ++f)
-			if (face_q[f] == qf)
-				faces_by_q.push_back(f);
-	}
-	c->qf_begin[kQMax + 1] = (int)faces_by_q.size();
-	c->n_face_items = 0;
-	for (int qf = 2; qf <= kQMax; ++qf)
-		c->n_face_items += (long long)(c->qf_begin[qf + 1] - c->qf_begin[qf]) * (d == 2 ? qf : qf * qf);
-	// fused tiles: full CTAs of 256 threads per group
+	// fused tiles: full CTAs per group (TP: 256 / q^d volumes; dense: E_fused)
 	std::vector<BTile> tiles;
-	for (int g = 0; g < n_groups; ++g) {
-		const int q = c->hgroups[g].q, N = (d == 2 ? q * q : q * q * q), E = std::max(1, 256 / N);
-		c->hgroups[g].first_tile = (int)tiles.size();
-		for (int e0 = 0; e0 < c->hgroups[g].n_vol; e0 += E)
-			tiles.push_back(BTile{g, e0});
+	for (int g = 0; g < nG; ++g) {
+		const bool dn = c->gl[g].dense;
+		const int E = dn ? c->hdgroups[c->gl[g].idx].E_fused : std::max(1, 256 / g_nvs[g]);
+		if (!dn)
+			c->hgroups[c->gl[g].idx].first_tile = (int)tiles.size();
+		const int tg = dn ? c->n_tp + c->gl[g].idx : c->gl[g].idx;
+		for (int e0 = 0; e0 < count[g]; e0 += E)
+			tiles.push_back(BTile{tg, e0});
 	}
 	c->n_tiles = (int)tiles.size();
 
@@ -690,16 +915,12 @@ dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu
 #define B_TRY(call)                                                                                  \
 	do {                                                                                             \
 		cudaError_t e_ = (call);                                                                     \
-		if (e_ != cudaSuccess) {                                                                     \
-			std::string m_ = std::string(#call) + ": " + cudaGetErrorString(e_);                     \
-			free_batch(c);                                                                           \
-			delete c;                                                                                \
-			return bfail(nullptr, DGPU_ERR_CUDA, m_);                                                \
-		}                                                                                            \
+		if (e_ != cudaSuccess)                                                                       \
+			return reject(DGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
 	} while (0)
 	B_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
 	c->own_stream = true;
-	for (int j = 0; j < kQMax; ++j) {
+	for (int j = 0; j < kBranches; ++j) {
 		B_TRY(cudaStreamCreateWithFlags(&c->aux[j], cudaStreamNonBlocking));
 		B_TRY(cudaEventCreateWithFlags(&c->ev_join[j], cudaEventDisableTiming));
 	}
@@ -721,22 +942,99 @@ dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu
 	B_TRY(cudaMemset(c->max_bits, 0, sizeof(unsigned long long)));
 	B_TRY(cudaMemset(c->err_flag, 0, sizeof(int)));
 	B_TRY(cudaMemset(c->n_corr, 0, sizeof(unsigned long long)));
+	// dense groups: operators, M_ref^-1, face operator table, 1/J
+	for (int t = 0; t < c->n_dense; ++t) {
+		const dgpu_dense_operators* op = dops[t];
+		DGroup& G = c->hdgroups[t];
+		const int nvs = op->n_vs, nvc = op->n_vc;
+		std::vector<double> cv0(op->cv0_vs_vc, op->cv0_vs_vc + (size_t)nvc * nvs);
+		std::vector<double> cv1(op->cv1_vs_vc, op->cv1_vs_vc + (size_t)d * nvc * nvs);
+		std::vector<double> M((size_t)nvs * nvs, 0.0), Minv((size_t)nvs * nvs);
+		for (int a = 0; a < nvs; ++a)
+			for (int b = 0; b < nvs; ++b) {
+				double s = 0.0;
+				for (int r = 0; r < nvc; ++r)
+					s += cv0[(size_t)r * nvs + a] * op->w_vc[r] * cv0[(size_t)r * nvs + b];
+				M[(size_t)a * nvs + b] = s;
+			}
+		if (!host_invert(nvs, M.data(), Minv.data()))
+			return reject(DGPU_ERR_INVALID_ARGUMENT, "singular reference mass matrix of a dense group");
+		std::vector<double> fops;
+		std::vector<long long> foff((size_t)kMaxLf * kMaxOrd * (kQMax + 1), -1);
+		for (int lf = 0; lf < op->n_lf; ++lf)
+			for (int o = 0; o < op->n_ord; ++o)
+				for (int pf = 1; pf < kQMax; ++pf) {
+					const int k = (lf * op->n_ord + o) * kQMax + pf;
+					if (!op->cv0_vs_fc[k] || op->n_fc[k] < 1)
+						continue;
+					foff[(lf * op->n_ord + o) * (kQMax + 1) + pf + 1] = (long long)fops.size();
+					fops.insert(fops.end(), op->cv0_vs_fc[k], op->cv0_vs_fc[k] + (size_t)op->n_fc[k] * nvs);
+				}
+		double *d_cv0 = nullptr, *d_cv1 = nullptr, *d_minv = nullptr, *d_fops = nullptr, *d_ij = nullptr;
+		long long* d_foff = nullptr;
+		B_TRY(upload_vec(&d_cv0, cv0));
+		c->dense_bufs.push_back(d_cv0);
+		B_TRY(upload_vec(&d_cv1, cv1));
+		c->dense_bufs.push_back(d_cv1);
+		B_TRY(upload_vec(&d_minv, Minv));
+		c->dense_bufs.push_back(d_minv);
+		B_TRY(upload_vec(&d_fops, fops));
+		c->dense_bufs.push_back(d_fops);
+		B_TRY(upload_vec(&d_foff, foff));
+		c->dense_bufs.push_back(d_foff);
+		B_TRY(upload_vec(&d_ij, inv_J[t]));
+		c->dense_bufs.push_back(d_ij);
+		G.cv0 = d_cv0;
+		G.cv1 = d_cv1;
+		G.minv = d_minv;
+		G.fops = d_fops;
+		G.fop_off = d_foff;
+		G.inv_J = d_ij;
+	}
 	B_TRY(upload_vec(&c->d_ops, c->hops));
 	B_TRY(upload_vec(&c->d_groups, c->hgroups));
+	B_TRY(upload_vec(&c->d_dgroups, c->hdgroups));
 	B_TRY(upload_vec(&c->d_elf, elf));
 	B_TRY(upload_vec(&c->d_fbase, fbase));
+	B_TRY(upload_vec(&c->d_node_face, node_face));
 	B_TRY(upload_vec(&c->gmet, gmet));
 	B_TRY(upload_vec(&c->inv_wJ, inv_wJ));
 	B_TRY(upload_vec(&c->fgeo, fgeo));
-	B_TRY(upload_vec(&c->d_faces_by_q, faces_by_q));
-	std::vector<int> qb(c->qf_begin, c->qf_begin + kQMax + 2);
-	B_TRY(upload_vec(&c->d_qf_begin, qb));
 	B_TRY(upload_vec(&c->d_tiles, tiles));
-	c->gl.resize(n_groups);
 	B_TRY(bind(c));
 #undef B_TRY
 	*out = c;
 	return DGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu_tp_operators* ops,
+                              const int* vol_group, const dgpu_mesh* mesh, dgpu_batch** out)
+{
+	if (!ops || n_groups < 1)
+		return bfail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+	std::vector<GroupIn> gin(n_groups);
+	for (int g = 0; g < n_groups; ++g)
+		gin[g] = GroupIn{false, &ops[g], nullptr};
+	return create_impl(phys, gin, vol_group, mesh, nullptr, out);
+}
+
+dgpu_status dgpu_batch_create_groups(const dgpu_physics* phys, int n_groups, const dgpu_group* groups,
+                                     const int* vol_group, const dgpu_mesh* mesh, const int* face_ord,
+                                     dgpu_batch** out)
+{
+	if (!groups || n_groups < 1)
+		return bfail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL argument");
+	std::vector<GroupIn> gin(n_groups);
+	for (int g = 0; g < n_groups; ++g) {
+		if ((groups[g].tp == nullptr) == (groups[g].dense == nullptr))
+			return bfail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "each group needs exactly one of tp / dense");
+		gin[g] = GroupIn{groups[g].dense != nullptr, groups[g].tp, groups[g].dense};
+	}
+	return create_impl(phys, gin, vol_group, mesh, face_ord, out);
 }
 
 dgpu_status dgpu_batch_destroy(dgpu_batch* c)
@@ -882,14 +1180,15 @@ dgpu_status dgpu_batch_set_mode(dgpu_batch* c, int form)
 
 dgpu_status dgpu_batch_set_group_tile(dgpu_batch* c, int group, int elements_per_cta)
 {
-	if (!c || group < 0 || group >= c->n_groups || elements_per_cta < 1 || elements_per_cta > c->gl[group].E_max)
+	if (!c || group < 0 || group >= c->n_all)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	c->hgroups[group].E = elements_per_cta;
-	BATCH_CUDA(c, cudaMemcpyAsync(c->d_groups, c->hgroups.data(), c->hgroups.size() * sizeof(BGroup),
-	                              cudaMemcpyHostToDevice, c->stream));
-	BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
+	const int g = c->caller_to_internal[group];
+	if (elements_per_cta < 1 || elements_per_cta > c->gl[g].E_max)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	set_group_E(c, g, elements_per_cta);
+	dgpu_status st = upload_group_tiles(c);
 	drop_graphs(c);
-	return DGPU_OK;
+	return st;
 }
 
 dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report, size_t report_len)
@@ -932,18 +1231,21 @@ dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report
 		return best;
 	};
 	c->mode = 0;
-	for (int g = 0; g < c->n_groups; ++g) {
-		if (c->hgroups[g].n_vol == 0)
+	for (int g = 0; g < c->n_all; ++g) {
+		if (c->group_n_vol(g) == 0)
 			continue;
-		int bestE = c->hgroups[g].E;
+		int bestE = c->group_E(g);
 		float bestT = -1.f;
 		for (int E = c->gl[g].E_max; E >= 1; E /= 2) {
-			c->hgroups[g].E = E;
-			cudaMemcpyAsync(c->d_groups, c->hgroups.data(), c->hgroups.size() * sizeof(BGroup),
-			                cudaMemcpyHostToDevice, c->stream);
+			set_group_E(c, g, E);
+			upload_group_tiles(c);
 			const float t = time_group(g);
-			char line[128];
-			snprintf(line, sizeof line, "group q=%d E=%d: %.4f ms\n", c->hgroups[g].q, E, t);
+			char line[160];
+			if (c->gl[g].dense)
+				snprintf(line, sizeof line, "dense group n_vs=%d n_vc=%d E=%d: %.4f ms\n",
+				         c->hdgroups[c->gl[g].idx].n_vs, c->hdgroups[c->gl[g].idx].n_vc, E, t);
+			else
+				snprintf(line, sizeof line, "group q=%d E=%d: %.4f ms\n", c->hgroups[c->gl[g].idx].q, E, t);
 			rep += line;
 			if (bestT < 0.f || t < bestT) {
 				bestT = t;
@@ -952,10 +1254,12 @@ dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report
 			if (E == 1)
 				break;
 		}
-		c->hgroups[g].E = bestE;
+		set_group_E(c, g, bestE);
 	}
-	BATCH_CUDA(c, cudaMemcpyAsync(c->d_groups, c->hgroups.data(), c->hgroups.size() * sizeof(BGroup),
-	                              cudaMemcpyHostToDevice, c->stream));
+	if ((st = upload_group_tiles(c)) != DGPU_OK) {
+		cudaFree(saved);
+		return st;
+	}
 	drop_graphs(c);
 	// the three forms on RK steps (graph-replayed unless graphs are off)
 	static const char* names[3] = {"plain", "fused", "branches"};
@@ -987,9 +1291,8 @@ dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report
 	cudaEventDestroy(e1);
 	c->coef_valid = coef_was;
 	c->gl_valid = coef_was ? false : gl_was;
-	if (report && report_len) {
+	if (report && report_len)
 		snprintf(report, report_len, "%s", rep.c_str());
-	}
 	return st;
 }
 

@@ -15,6 +15,9 @@
 
 namespace dgpu {
 
+constexpr int kMaxLf = 6;       // element-face slots per volume in elf (HEX has the most faces)
+constexpr int kMaxOrd = 8;      // face orientations (QUAD faces)
+
 struct BatchOps {
 	TPOps t;
 	double Iup[kQMax + 1][kQMax][kQMax];   // Iup[qf][i][a]: GL(q) Lagrange a at GL(qf) node i, qf >= q
@@ -30,13 +33,29 @@ struct BGroup {
 	long long wj_off;         // ... in the 1/(wJ) array
 };
 
+// A non-tensor-product (dense-operator) group: TET, WEDGE or PYR volumes of one p (kernels in dgpu_dense.cuh).
+struct DGroup {
+	int n_vs, n_vc, n_lf, n_ord;
+	int n_vol, E, E_fused;      // volumes; volumes per CTA of the per-group and of the fused kernels
+	long long elem0;            // first element (group-sorted index)
+	long long state_off;        // in state-sized arrays
+	long long gmet_off;         // per element D*D*n_vc doubles of w * metrics, component j*D+i
+	const double* cv0;          // n_vc x n_vs
+	const double* cv1;          // D x n_vc x n_vs
+	const double* minv;         // n_vs x n_vs (M_ref^-1)
+	const double* inv_J;        // per element 1 / J
+	const double* fops;         // face operator table
+	const long long* fop_off;   // [(lf * n_ord + ord) * (kQMax + 1) + q_f] -> offset in fops, -1 if absent
+};
+
 struct BParams {
 	double b_adv[3];
-	int n_groups;
+	int n_groups;             // TP groups; dense groups follow them in the tile list (group >= n_groups)
+	const DGroup* dgroups;
 	const BatchOps* ops;      // [group]
 	const BGroup* groups;     // [group]
-	const int4* elf;          // [element][2D]: (face, side, q_f, 0)
-	const long long* fbase;   // [face]: first face node of the face (prefix sum of q_f^(D-1))
+	const int4* elf;          // [element][kMaxLf]: (face, side, q_f, orientation)
+	const long long* fbase;   // [face + 1]: first face node of the face (faces laid out by increasing q_f)
 	const double* gmet;
 	const double* inv_wJ;
 	const double* fgeo;       // [node][D+1] blocks per face: (D+1) * fbase[f] + k * NF_f + i
@@ -178,7 +197,7 @@ __device__ void bvol_body(const BParams& P, const BatchOps* sops, const BGroup& 
 		// traces at each face's order: copy (q_f == Q) or tangential interpolation Q -> q_f. In 3D the
 		// interpolation is separable: a thread takes one (variable, i0) column, contracts the first tangential
 		// direction once per b (Q^2 FMAs) and reuses the Q partial sums for all q_f outputs i1.
-		const int4* ef = P.elf + v * 2 * D;
+		const int4* ef = P.elf + v * kMaxLf;
 		for (int lf = 0; lf < 2 * D; ++lf) {
 			const int4 fd = ef[lf];
 			const int qf = fd.z;
@@ -229,24 +248,23 @@ __device__ void bvol_body(const BParams& P, const BatchOps* sops, const BGroup& 
 // ---------------------------------------------------------------------------------------------------------------
 // Face numerical flux at q_f points (faces of one q_f in [f_begin, f_end) of the face list)
 // ---------------------------------------------------------------------------------------------------------------
-template <int D, int QF, int NV, int PDE, int FLUX>
-__device__ __forceinline__ void bface_node(const BParams& P, int f, int i)
+template <int D, int NV, int PDE, int FLUX>
+__device__ __forceinline__ void bface_node_rt(const BParams& P, int f, int i, int nff)
 {
-	constexpr int NF = TPShape<D, QF>::NF;
 	const long long fb = P.fbase[f];
 	const double* tL = P.traces + 2 * NV * fb;
-	const double* tR = tL + NV * NF;
+	const double* tR = tL + NV * nff;
 	double WL[NV], WR[NV], n[D];
 #pragma unroll
 	for (int k = 0; k < NV; ++k) {
-		WL[k] = tL[k * NF + i];
-		WR[k] = tR[k * NF + i];
+		WL[k] = tL[k * nff + i];
+		WR[k] = tR[k * nff + i];
 	}
 	const double* fg = P.fgeo + (D + 1) * fb;
 #pragma unroll
 	for (int k = 0; k < D; ++k)
-		n[k] = fg[k * NF + i];
-	const double sc = fg[D * NF + i];
+		n[k] = fg[k * nff + i];
+	const double sc = fg[D * nff + i];
 	double* out = P.nnf + NV * fb;
 	if constexpr (PDE == kEuler) {
 		double nF[NV];
@@ -256,7 +274,7 @@ __device__ __forceinline__ void bface_node(const BParams& P, int f, int i)
 			num_flux_lax_friedrichs<D>(WL, WR, n, nF);
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			out[k * NF + i] = nF[k] * sc;
+			out[k * nff + i] = nF[k] * sc;
 	} else {
 		out[i] = num_flux_upwind<D>(WL[0], WR[0], n, P.b_adv) * sc;
 	}
@@ -287,7 +305,7 @@ __device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup&
 		// face terms at the element's own points: copy (q_f == Q) or transposed interpolation q_f -> Q
 		// (separable in 3D: a thread takes one (variable, a) column, contracts i0 for every i1 once and reuses
 		// the q_f partial sums for all Q outputs b).
-		const int4* ef = P.elf + v * 2 * D;
+		const int4* ef = P.elf + v * kMaxLf;
 		for (int lf = 0; lf < 2 * D; ++lf) {
 			const int4 fd = ef[lf];
 			const int qf = fd.z;
@@ -504,105 +522,6 @@ __global__ void __launch_bounds__(256, 2) blift_group_kernel(const BParams P, in
 	load_batch_ops(sops, &P.ops[g]);
 	__syncthreads();
 	blift_body<D, Q, NV, MODE>(P, sops, G, blockIdx.x * G.E, G.E, rk, smem + sizeof(BatchOps) / 8);
-}
-
-template <int D, int QF, int NV, int PDE, int FLUX>
-__global__ void __launch_bounds__(256) bface_group_kernel(const BParams P, const int* faces, int n)
-{
-	constexpr int NF = TPShape<D, QF>::NF;
-	const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (gid >= (long long)n * NF)
-		return;
-	bface_node<D, QF, NV, PDE, FLUX>(P, faces[gid / NF], (int)(gid % NF));
-}
-
-// Fused persistent kernels: a CTA walks the tile list (grid-stride) and dispatches on the tile's order; the
-// operator set is reloaded into shared memory when the group changes.
-template <int D, int NV, int PDE, bool GLL_IN>
-__global__ void __launch_bounds__(256) bvol_fused_kernel(const BParams P, const BTile* tiles, int n_tiles,
-                                                           const double* __restrict__ u)
-{
-	extern __shared__ double smem[];
-	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
-	double* base = smem + sizeof(BatchOps) / 8;
-	if (blockIdx.x == 0 && threadIdx.x == 0 && P.max_bits)
-		*P.max_bits = 0ull;
-	int cur = -1;
-	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-		const BTile tl = tiles[t];
-		if (tl.group != cur) {
-			__syncthreads();
-			load_batch_ops(sops, &P.ops[tl.group]);
-			cur = tl.group;
-			__syncthreads();
-		}
-		const BGroup G = P.groups[tl.group];
-		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
-		switch (G.q) {
-		case 2: bvol_body<D, 2, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
-		case 3: bvol_body<D, 3, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
-		case 4: bvol_body<D, 4, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
-		default: bvol_body<D, 5, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
-		}
-	}
-}
-
-template <int D, int NV, int MODE>
-__global__ void __launch_bounds__(256, 2) blift_fused_kernel(const BParams P, const BTile* tiles, int n_tiles,
-                                                               const RkArgs rk)
-{
-	extern __shared__ double smem[];
-	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
-	double* base = smem + sizeof(BatchOps) / 8;
-	int cur = -1;
-	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-		const BTile tl = tiles[t];
-		if (tl.group != cur) {
-			__syncthreads();
-			load_batch_ops(sops, &P.ops[tl.group]);
-			cur = tl.group;
-			__syncthreads();
-		}
-		const BGroup G = P.groups[tl.group];
-		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
-		switch (G.q) {
-		case 2: blift_body<D, 2, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
-		case 3: blift_body<D, 3, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
-		case 4: blift_body<D, 4, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
-		default: blift_body<D, 5, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
-		}
-	}
-}
-
-// Faces of all orders: the face list is sorted by q_f; face_q_begin[qf] gives each order's range.
-template <int D, int NV, int PDE, int FLUX>
-__global__ void __launch_bounds__(256) bface_fused_kernel(const BParams P, const int* faces, const int* qf_begin,
-                                                            long long n_items)
-{
-	for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < n_items;
-	     it += (long long)gridDim.x * blockDim.x) {
-		// items are laid out order by order: [qf=2 faces x NF(2)] [qf=3 ...] ...
-		long long off = 0;
-		int qf = 2;
-		for (; qf <= kQMax; ++qf) {
-			const int nf = (D == 2 ? qf : qf * qf);
-			const long long cnt = (long long)(qf_begin[qf + 1] - qf_begin[qf]) * nf;
-			if (it < off + cnt)
-				break;
-			off += cnt;
-		}
-		if (qf > kQMax)
-			return;
-		const int nf = (D == 2 ? qf : qf * qf);
-		const long long local = it - off;
-		const int f = faces[qf_begin[qf] + local / nf], i = (int)(local % nf);
-		switch (qf) {
-		case 2: bface_node<D, 2, NV, PDE, FLUX>(P, f, i); break;
-		case 3: bface_node<D, 3, NV, PDE, FLUX>(P, f, i); break;
-		case 4: bface_node<D, 4, NV, PDE, FLUX>(P, f, i); break;
-		default: bface_node<D, 5, NV, PDE, FLUX>(P, f, i); break;
-		}
-	}
 }
 
 template <int D, int Q, int NV, bool TO_GL>

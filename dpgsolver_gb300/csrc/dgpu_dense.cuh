@@ -1,0 +1,304 @@
+// Dense-operator residual kernels for the non-tensor-product 3D volumes (TET, WEDGE, PYR) of a batched mesh.
+//
+// These volumes carry the caller's dense reference operators, as the reference applies its op_std operators with
+// one small GEMM per volume (operator_T.c:96-156): s_vc = cv0_vs_vc s (constructor_sol_vc_interp,
+// compute_volume_rlhs_T.c:277-285), the contravariant Euler flux at the cubature nodes, rhs = sum_j cv1_j^T
+// (w fr_j) (compute_rhs_v_dg_like_T, compute_volume_rlhs_T.c:166-177), face traces cv0_vs_fc s at the face's
+// canonical nodes, rhs -= cv0_vs_fc^T (w_f J_f F*) per face (compute_rhs_f_dg_like_T, compute_face_rlhs_T.c:
+// 297-310) and M^-1 (scale_rhs_by_m_inv_std, solve_dg.c:265-272). Volumes are affine (constant J), so
+// M^-1 = M_ref^-1 / J with M_ref = cv0^T diag(w) cv0 inverted once on the host.
+//
+// One CTA handles E volumes of one group; every phase maps one thread to one output row of one volume (all
+// variables per thread), reading the operators through the L1 cache (they are shared by every CTA of the group)
+// and the volume's state and fluxes from shared memory. The state stays in coefficient space between stages.
+#pragma once
+
+#include "dgpu_batched.cuh"
+
+namespace dgpu {
+
+struct DSmem {
+	// doubles per element: state (NV n_vs), then fluxes (D NV n_vc) reused by the lift as rhs (NV n_vs)
+	static __host__ __device__ int vol(int nv, int n_vs, int n_vc) { return nv * n_vs + 3 * nv * n_vc; }
+	static __host__ __device__ int lift(int nv, int n_vs) { return 2 * nv * n_vs + 2; }
+};
+
+// ---------------------------------------------------------------------------------------------------------------
+// Volume term (coefficient space) + face traces at the canonical face nodes
+// ---------------------------------------------------------------------------------------------------------------
+template <int D, int NV, int PDE>
+__device__ void dvol_body(const BParams& P, const DGroup& G, int e0, int E, const double* __restrict__ u,
+                          double* smem)
+{
+	const int nvs = G.n_vs, nvc = G.n_vc;
+	const int PER_E = DSmem::vol(NV, nvs, nvc);
+	const int n_here = min(E, G.n_vol - e0);
+	const double* ublk = u + G.state_off + (long long)e0 * NV * nvs;
+	for (int i = threadIdx.x; i < n_here * NV * nvs; i += blockDim.x) {
+		const int e = i / (NV * nvs), r = i % (NV * nvs);
+		smem[e * PER_E + r] = ublk[i];
+	}
+	__syncthreads();
+	const double* __restrict__ cv0 = G.cv0;
+	// phase 1: state at the cubature nodes, contravariant flux, w-weighted (w is folded into the metrics)
+	for (int it = threadIdx.x; it < n_here * nvc; it += blockDim.x) {
+		const int e = it / nvc, r = it % nvc;
+		const double* su = smem + e * PER_E;
+		double* sf = smem + e * PER_E + NV * nvs;   // [j][k][r]
+		double W[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			W[k] = 0.0;
+		const double* row = cv0 + (long long)r * nvs;
+		for (int m = 0; m < nvs; ++m) {
+			const double c = __ldg(row + m);
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				W[k] += c * su[k * nvs + m];
+		}
+		double g[D * D];
+		const double* gm = P.gmet + G.gmet_off + (long long)(e0 + e) * D * D * nvc;
+#pragma unroll
+		for (int c = 0; c < D * D; ++c)
+			g[c] = gm[c * nvc + r];
+		if constexpr (PDE == kEuler) {
+			double fr[D][D + 2];
+			euler_flux_ref<D>(W, g, fr);
+#pragma unroll
+			for (int j = 0; j < D; ++j)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					sf[(j * NV + k) * nvc + r] = fr[j][k];
+		} else {
+#pragma unroll
+			for (int j = 0; j < D; ++j) {
+				double gb = 0.0;
+#pragma unroll
+				for (int i = 0; i < D; ++i)
+					gb += g[j * D + i] * P.b_adv[i];
+				sf[j * nvc + r] = gb * W[0];
+			}
+		}
+	}
+	__syncthreads();
+	// phase 2: rhs_vol[k][m] = sum_j sum_r cv1_j[r][m] sf[j][k][r]
+	const double* __restrict__ cv1 = G.cv1;
+	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
+		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
+		const double* sf = smem + e * PER_E + NV * nvs;
+		double acc = 0.0;
+#pragma unroll
+		for (int j = 0; j < D; ++j) {
+			const double* col = cv1 + (long long)j * nvc * nvs + m;
+			const double* f = sf + (j * NV + k) * nvc;
+			for (int r = 0; r < nvc; ++r)
+				acc += __ldg(col + (long long)r * nvs) * f[r];
+		}
+		P.vol_gl[G.state_off + (long long)(e0 + e) * NV * nvs + k * nvs + m] = acc;
+	}
+	// phase 3: traces at each face's canonical nodes
+	for (int it = threadIdx.x; it < n_here * G.n_lf * kQMax * kQMax; it += blockDim.x) {
+		const int i = it % (kQMax * kQMax), el = it / (kQMax * kQMax), lf = el % G.n_lf, e = el / G.n_lf;
+		const long long v = G.elem0 + e0 + e;
+		const int4 fd = P.elf[v * kMaxLf + lf];
+		const long long fb = P.fbase[fd.x];
+		const int nff = (int)(P.fbase[fd.x + 1] - fb);
+		if (i >= nff)
+			continue;
+		const double* op = G.fops + G.fop_off[(lf * G.n_ord + fd.w) * (kQMax + 1) + fd.z] + (long long)i * nvs;
+		const double* su = smem + e * PER_E;
+		double W[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			W[k] = 0.0;
+		for (int m = 0; m < nvs; ++m) {
+			const double c = __ldg(op + m);
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				W[k] += c * su[k * nvs + m];
+		}
+		double* dst = P.traces + 2 * NV * fb + (long long)fd.y * NV * nff;
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			dst[k * nff + i] = W[k];
+	}
+	__syncthreads();   // shared memory is reused by the next tile
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Lift of the face fluxes, M^-1, then the residual or the RK stage (coefficient space)
+// ---------------------------------------------------------------------------------------------------------------
+template <int NV, int MODE>
+__device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, const RkArgs& rk, double* smem)
+{
+	const int nvs = G.n_vs;
+	const int PER_E = DSmem::lift(NV, nvs);
+	const int n_here = min(E, G.n_vol - e0);
+	// phase 1: rhs = vol - sum_lf sgn cv0_fc^T nnf
+	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
+		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
+		const long long v = G.elem0 + e0 + e;
+		double acc = P.vol_gl[G.state_off + (long long)(e0 + e) * NV * nvs + rem];
+		for (int lf = 0; lf < G.n_lf; ++lf) {
+			const int4 fd = P.elf[v * kMaxLf + lf];
+			const long long fb = P.fbase[fd.x];
+			const int nff = (int)(P.fbase[fd.x + 1] - fb);
+			const double* op = G.fops + G.fop_off[(lf * G.n_ord + fd.w) * (kQMax + 1) + fd.z] + m;
+			const double* src = P.nnf + NV * fb + (long long)k * nff;
+			double s = 0.0;
+			for (int i = 0; i < nff; ++i)
+				s += __ldg(op + (long long)i * nvs) * src[i];
+			acc += (fd.y == 0 ? -s : s);   // side 0: rhs -= ; side 1: rhs -= (-nnf)
+		}
+		smem[e * PER_E + rem] = acc;
+	}
+	__syncthreads();
+	// phase 2: R = M_ref^-1 rhs / J, then the stage
+	const double* __restrict__ minv = G.minv;
+	unsigned long long mx = 0ull;
+	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
+		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
+		const double* sr = smem + e * PER_E + k * nvs;
+		const double* row = minv + (long long)m * nvs;
+		double R = 0.0;
+		for (int a = 0; a < nvs; ++a)
+			R += __ldg(row + a) * sr[a];
+		R *= G.inv_J[e0 + e];
+		const long long o = G.state_off + (long long)(e0 + e) * NV * nvs + rem;
+		if (MODE == kModeRhs || rk.want_max) {
+			const unsigned long long bits = abs_bits(R);
+			mx = bits > mx ? bits : mx;
+		}
+		if constexpr (MODE == kModeRhs) {
+			rk.rhs[o] = R;
+		} else {
+			const double s = rk.u[o];
+			double sn;
+			if (rk.stage == 0) {
+				rk.u0[o] = s;
+				sn = s + rk.dt * R;
+			} else if (rk.stage == 1) {
+				sn = (1.0 / 4.0) * (3.0 * rk.u0[o] + s + rk.dt * R);
+			} else {
+				sn = (1.0 / 3.0) * (rk.u0[o] + 2.0 * s + 2.0 * rk.dt * R);
+			}
+			rk.u[o] = sn;
+		}
+	}
+	if (MODE == kModeRhs || rk.want_max) {
+#pragma unroll
+		for (int off = 16; off > 0; off >>= 1) {
+			const unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, off);
+			mx = o > mx ? o : mx;
+		}
+		if ((threadIdx.x & 31) == 0 && mx && P.max_bits)
+			atomicMax(P.max_bits, mx);
+	}
+	__syncthreads();   // shared memory is reused by the next tile
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Kernels: one launch per dense group, and the bodies the fused kernels dispatch to
+// ---------------------------------------------------------------------------------------------------------------
+template <int D, int NV, int PDE>
+__global__ void __launch_bounds__(256) dvol_group_kernel(const BParams P, int g, const double* __restrict__ u)
+{
+	extern __shared__ double smem[];
+	const DGroup G = P.dgroups[g];
+	if (blockIdx.x == 0 && threadIdx.x == 0 && P.max_bits && G.elem0 == 0)
+		*P.max_bits = 0ull;
+	dvol_body<D, NV, PDE>(P, G, blockIdx.x * G.E, G.E, u, smem);
+}
+
+template <int NV, int MODE>
+__global__ void __launch_bounds__(256) dlift_group_kernel(const BParams P, int g, const RkArgs rk)
+{
+	extern __shared__ double smem[];
+	const DGroup G = P.dgroups[g];
+	dlift_body<NV, MODE>(P, G, blockIdx.x * G.E, G.E, rk, smem);
+}
+
+// Fused persistent kernels: a CTA walks the tile list (grid-stride) and dispatches on the tile's group: a TP
+// group's order (its operator set is reloaded into shared memory when the group changes) or a dense group.
+template <int D, int NV, int PDE, bool GLL_IN>
+__global__ void __launch_bounds__(256) bvol_fused_kernel(const BParams P, const BTile* tiles, int n_tiles,
+                                                           const double* __restrict__ u)
+{
+	extern __shared__ double smem[];
+	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
+	double* base = smem + sizeof(BatchOps) / 8;
+	if (blockIdx.x == 0 && threadIdx.x == 0 && P.max_bits)
+		*P.max_bits = 0ull;
+	int cur = -1;
+	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+		const BTile tl = tiles[t];
+		if (tl.group >= P.n_groups) {
+			if constexpr (D == 3) {
+				const DGroup G = P.dgroups[tl.group - P.n_groups];
+				dvol_body<D, NV, PDE>(P, G, tl.e0, G.E_fused, u, base);
+			}
+			continue;
+		}
+		if (tl.group != cur) {
+			__syncthreads();
+			load_batch_ops(sops, &P.ops[tl.group]);
+			cur = tl.group;
+			__syncthreads();
+		}
+		const BGroup G = P.groups[tl.group];
+		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
+		switch (G.q) {
+		case 2: bvol_body<D, 2, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 3: bvol_body<D, 3, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 4: bvol_body<D, 4, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		default: bvol_body<D, 5, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		}
+	}
+}
+
+template <int D, int NV, int MODE>
+__global__ void __launch_bounds__(256, 2) blift_fused_kernel(const BParams P, const BTile* tiles, int n_tiles,
+                                                               const RkArgs rk)
+{
+	extern __shared__ double smem[];
+	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
+	double* base = smem + sizeof(BatchOps) / 8;
+	int cur = -1;
+	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+		const BTile tl = tiles[t];
+		if (tl.group >= P.n_groups) {
+			const DGroup G = P.dgroups[tl.group - P.n_groups];
+			dlift_body<NV, MODE>(P, G, tl.e0, G.E_fused, rk, base);
+			continue;
+		}
+		if (tl.group != cur) {
+			__syncthreads();
+			load_batch_ops(sops, &P.ops[tl.group]);
+			cur = tl.group;
+			__syncthreads();
+		}
+		const BGroup G = P.groups[tl.group];
+		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
+		switch (G.q) {
+		case 2: blift_body<D, 2, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 3: blift_body<D, 3, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 4: blift_body<D, 4, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		default: blift_body<D, 5, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		}
+	}
+}
+
+// Face numerical flux at every node of the faces in [node_lo, node_hi) of the q_f-sorted face node list.
+template <int D, int NV, int PDE, int FLUX>
+__global__ void __launch_bounds__(256) bface_nodes_kernel(const BParams P, const int* __restrict__ node_face,
+                                                           long long node_lo, long long node_hi)
+{
+	for (long long gid = node_lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; gid < node_hi;
+	     gid += (long long)gridDim.x * blockDim.x) {
+		const int f = node_face[gid];
+		const long long fb = P.fbase[f];
+		bface_node_rt<D, NV, PDE, FLUX>(P, f, (int)(gid - fb), (int)(P.fbase[f + 1] - fb));
+	}
+}
+
+}  // namespace dgpu

@@ -48,6 +48,49 @@ inline bool host_invert_small(int n, const double* A, double* Ainv)
 	return true;
 }
 
+// Gauss-Jordan inverse with partial pivoting of a row-major n x n matrix of any size.
+inline bool host_invert(int n, const double* A, double* Ainv)
+{
+	double* a = new double[(size_t)n * n];
+	for (size_t i = 0; i < (size_t)n * n; ++i)
+		a[i] = A[i];
+	for (int i = 0; i < n; ++i)
+		for (int j = 0; j < n; ++j)
+			Ainv[(size_t)i * n + j] = (i == j) ? 1.0 : 0.0;
+	bool ok = true;
+	for (int col = 0; col < n && ok; ++col) {
+		int piv = col;
+		for (int r = col + 1; r < n; ++r)
+			if (fabs(a[(size_t)r * n + col]) > fabs(a[(size_t)piv * n + col]))
+				piv = r;
+		if (!(fabs(a[(size_t)piv * n + col]) > 1e-300)) {
+			ok = false;
+			break;
+		}
+		if (piv != col)
+			for (int j = 0; j < n; ++j) {
+				double t = a[(size_t)col * n + j]; a[(size_t)col * n + j] = a[(size_t)piv * n + j]; a[(size_t)piv * n + j] = t;
+				t = Ainv[(size_t)col * n + j]; Ainv[(size_t)col * n + j] = Ainv[(size_t)piv * n + j]; Ainv[(size_t)piv * n + j] = t;
+			}
+		const double inv = 1.0 / a[(size_t)col * n + col];
+		for (int j = 0; j < n; ++j) {
+			a[(size_t)col * n + j] *= inv;
+			Ainv[(size_t)col * n + j] *= inv;
+		}
+		for (int r = 0; r < n; ++r) {
+			if (r == col)
+				continue;
+			const double f = a[(size_t)r * n + col];
+			for (int j = 0; j < n; ++j) {
+				a[(size_t)r * n + j] -= f * a[(size_t)col * n + j];
+				Ainv[(size_t)r * n + j] -= f * Ainv[(size_t)col * n + j];
+			}
+		}
+	}
+	delete[] a;
+	return ok;
+}
+
 // Legendre polynomial P_n and its derivative at x (three-term recurrence).
 inline void legendre(int n, double x, double* p, double* dp)
 {

@@ -219,8 +219,13 @@ class BatchSimulation:
         for k in range(3):
             phys.b_adv[k] = float(prob.b_adv[k])
         groups = fl["groups"]
+        dense = any(getattr(o, "dense", False) for o in groups)
         tps = (_lib.TPOperators * len(groups))()
+        dns = (_lib.DenseOperators * len(groups))()
         for g, ops in enumerate(groups):
+            if getattr(ops, "dense", False):
+                self._dense_operators(dns[g], ops, arr, keep)
+                continue
             tps[g].elem_type, tps[g].p = ops.e_type, ops.p
             tps[g].cv0_vs_vc = _dp(arr(ops.cv0_1d))
             tps[g].cv1_vs_vc = _dp(arr(ops.cv1_1d))
@@ -241,8 +246,20 @@ class BatchSimulation:
         m.jacobian_det_fc = _dp(arr(fl["jacobian_det_fc"]))
         vg = arr(fl["vol_group"], np.int32)
         h = ctypes.c_void_p()
-        check(lib.dgpu_batch_create(ctypes.byref(phys), len(groups), tps, _ip(vg), ctypes.byref(m),
-                                    ctypes.byref(h)), None, batch=True)
+        if dense or fl.get("face_ord") is not None:
+            G = (_lib.Group * len(groups))()
+            for g, ops in enumerate(groups):
+                if getattr(ops, "dense", False):
+                    G[g].dense = ctypes.pointer(dns[g])
+                else:
+                    G[g].tp = ctypes.pointer(tps[g])
+            fo = fl.get("face_ord")
+            fop = _ip(arr(fo, np.int32)) if fo is not None else None
+            check(lib.dgpu_batch_create_groups(ctypes.byref(phys), len(groups), G, _ip(vg), ctypes.byref(m), fop,
+                                               ctypes.byref(h)), None, batch=True)
+        else:
+            check(lib.dgpu_batch_create(ctypes.byref(phys), len(groups), tps, _ip(vg), ctypes.byref(m),
+                                        ctypes.byref(h)), None, batch=True)
         self._lib = lib
         self._h = h
         self.prob = prob
@@ -253,6 +270,32 @@ class BatchSimulation:
         if stream is not None:
             check(lib.dgpu_batch_set_stream(h, ctypes.c_void_p(stream)), h, batch=True)
         self.upload_state(prob.sol)
+
+    @staticmethod
+    def _dense_operators(D, ops, arr, keep):
+        """Fill a DenseOperators struct from a DenseOperatorSet: volume operators and the face operator table for
+        every local face, orientation and face order p_f >= p."""
+        from .host import simplex as S
+        n_ord = 8
+        D.elem_type, D.p, D.n_vs, D.n_vc = ops.e_type, ops.p, ops.n_vs, ops.n_vc
+        D.cv0_vs_vc = _dp(arr(ops.cv0_vs_vc()))
+        D.cv1_vs_vc = _dp(arr(np.stack([ops.cv1_vs_vc(k) for k in range(3)])))
+        D.w_vc = _dp(arr(ops.w_vc))
+        D.n_lf, D.n_ord = ops.n_lf, n_ord
+        n_fc = np.zeros(ops.n_lf * n_ord * 5, dtype=np.int32)
+        cv0 = (_lib.c_double_p * (ops.n_lf * n_ord * 5))()
+        w = (_lib.c_double_p * (ops.n_lf * 5))()
+        for lf in range(ops.n_lf):
+            for pf in range(ops.p, 5):
+                w[lf * 5 + pf] = _dp(arr(ops.w_fc(lf, pf + 1)))
+                for o in range(ops.n_ords(lf)):
+                    c = arr(ops.cv0_vs_fc(lf, o, pf + 1))
+                    n_fc[(lf * n_ord + o) * 5 + pf] = c.shape[0]
+                    cv0[(lf * n_ord + o) * 5 + pf] = _dp(c)
+        D.n_fc = _ip(arr(n_fc, np.int32))
+        D.cv0_vs_fc = cv0
+        D.w_fc = w
+        keep.extend([cv0, w])
 
     def _check(self, st):
         check(st, self._h, batch=True)

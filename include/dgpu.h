@@ -47,8 +47,11 @@ typedef int dgpu_status;
 #define DGPU_NUM_FLUX_UPWIND          11
 #define DGPU_NUM_FLUX_ROE_PIKE        31
 #define DGPU_NUM_FLUX_LAX_FRIEDRICHS  32
-#define DGPU_QUAD 3
-#define DGPU_HEX  5
+#define DGPU_QUAD  3
+#define DGPU_TET   4
+#define DGPU_HEX   5
+#define DGPU_WEDGE 6
+#define DGPU_PYR   7
 
 typedef struct dgpu_ctx dgpu_ctx;
 
@@ -207,6 +210,42 @@ const char* dgpu_status_string(dgpu_status st);
 typedef struct dgpu_batch dgpu_batch;
 dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu_tp_operators* ops,
                               const int* vol_group, const dgpu_mesh* mesh, dgpu_batch** out);
+
+/* Dense operator set of one non-tensor-product (TET, WEDGE or PYR, p) group: the reference's op_std operators
+ * (cv0_vs_vc, cv1_vs_vc, cv0_vs_fc: element_operators.c; applied per volume by operator_T.c:96-156) for any
+ * solution basis and cubature the caller uses. Row-major. The volumes must be affine (constant
+ * jacobian_det_vc), so that M^-1 = (cv0^T diag(w_vc) cv0)^-1 / J (constructor_mass_T, volume_solver_T.c:115-145).
+ * Face operators are evaluated at the face's canonical nodes (the node order the face's other side and the face
+ * geometry use) as seen from local face lf under orientation ord (the reference's ind_ord, face.h:47-97):
+ *   cv0_vs_fc[(lf * n_ord + ord) * 5 + p_f]   n_fc x n_vs, NULL where not provided;
+ *   n_fc     [(lf * n_ord + ord) * 5 + p_f]   its number of face nodes (both sides of a face must agree);
+ *   w_fc     [lf * 5 + p_f]                   the face cubature weights at the canonical nodes. */
+typedef struct {
+	int elem_type;                    /* DGPU_TET, DGPU_WEDGE or DGPU_PYR                         */
+	int p;                            /* 1..4                                                      */
+	int n_vs, n_vc;
+	const double* cv0_vs_vc;          /* n_vc x n_vs                                               */
+	const double* cv1_vs_vc;          /* 3 x n_vc x n_vs: d/dr_k of the basis at the vc nodes      */
+	const double* w_vc;               /* n_vc                                                      */
+	int n_lf;                         /* local faces: TET 4, WEDGE 5, PYR 5 (element.c f_ve order) */
+	int n_ord;                        /* orientations per face (at most 8)                         */
+	const int* n_fc;
+	const double* const* cv0_vs_fc;
+	const double* const* w_fc;
+} dgpu_dense_operators;
+
+/* One (type, p) group of a batched mesh: exactly one of tp / dense. */
+typedef struct {
+	const dgpu_tp_operators* tp;
+	const dgpu_dense_operators* dense;
+} dgpu_group;
+
+/* Batched context over TP and dense groups. face_ord (n_faces x 2, may be NULL = all 0) gives each side's
+ * orientation index into its face operator table; QUAD/HEX sides must have orientation 0 (their own face-node
+ * order is the face's canonical order). Positivity is provided for QUAD/HEX groups only. */
+dgpu_status dgpu_batch_create_groups(const dgpu_physics* phys, int n_groups, const dgpu_group* groups,
+                                     const int* vol_group, const dgpu_mesh* mesh, const int* face_ord,
+                                     dgpu_batch** out);
 dgpu_status dgpu_batch_destroy(dgpu_batch* b);
 /* Text of the last error of b (of the last failed dgpu_batch_create when b is NULL). */
 const char* dgpu_batch_last_error(const dgpu_batch* b);

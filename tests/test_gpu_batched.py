@@ -203,3 +203,69 @@ def test_positivity_correction_matches_oracle(gpu_lib):
             ncorr = sim.positivity_corrections()
         assert ncorr == ncorr_ref
         assert rel_err(s, s_ref) <= 1e-10
+
+
+# ---- mixed element types: HEX (TP kernels) with TET / WEDGE / PYR (dense-operator kernels) ------------------------
+
+def _types_case(n, seed, flux=P.NUM_FLUX_ROE_PIKE):
+    from dpgsolver_gb300.host import mixed_types as MT
+    return MT.mixed_types_euler(n, seed=seed, num_flux=flux, perturb=0.3)
+
+
+TYPE_CASES = {
+    "types_roe_4": lambda: _types_case(4, 0),
+    "types_lf_4": lambda: _types_case(4, 1, P.NUM_FLUX_LAX_FRIEDRICHS),
+    "types_roe_6": lambda: _types_case(6, 2),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TYPE_CASES))
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_types_residual_matches_oracle(gpu_lib, name, form):
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = TYPE_CASES[name]()
+    r_ref, mx_ref = oracle.Oracle(prob).compute_rhs(prob.sol)
+    with BatchSimulation(prob) as sim:
+        sim.form = form
+        mx = sim.compute_rhs()
+        r = sim.rhs
+    assert rel_err(r, r_ref) <= TOL
+    assert abs(mx - mx_ref) <= TOL * mx_ref
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_mixed_types_rk3_matches_oracle(gpu_lib, form):
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = TYPE_CASES["types_roe_4"]()
+    ref = oracle.Oracle(prob)
+    s_ref = prob.sol.copy()
+    for _ in range(3):
+        s_ref, mx_ref, _ = ref.ssp_rk3_step(s_ref, prob.dt)
+    with BatchSimulation(prob) as sim:
+        sim.form = form
+        mx = sim.ssp_rk3_steps(prob.dt, 3)
+        s = sim.sol_coef
+    assert rel_err(s, s_ref) <= TOL
+    assert abs(mx - mx_ref) <= 1e-10 * mx_ref
+
+
+def test_mixed_types_forms_and_tiles_agree_bitwise(gpu_lib):
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = TYPE_CASES["types_roe_6"]()
+    out = []
+    with BatchSimulation(prob) as sim:
+        for form, halve in [("plain", False), ("fused", False), ("branches", False), ("plain", True)]:
+            sim.form = form
+            if halve:
+                for g in range(len(prob.groups)):
+                    sim.set_group_tile(g, 1)
+            sim.upload_state(prob.sol)
+            sim.compute_rhs()
+            r = sim.rhs
+            sim.ssp_rk3_steps(prob.dt, 2, want_max=False)
+            out.append((r, sim.sol_coef))
+        rep = sim.autotune(prob.dt, reps=1)
+        assert "dense group" in rep
+    for r, s in out[1:]:
+        assert np.array_equal(r, out[0][0])
+        assert np.array_equal(s, out[0][1])
