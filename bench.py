@@ -52,6 +52,9 @@ WORKLOADS = {
                      desc="2D Euler curved QUAD 64^2 p3 Roe-Pike isentropic vortex"),
     "mixed3d": dict(kind="mixed", n=58, p=None, flux="roe_pike",
                     desc="3D Euler mixed-order HEX 58^3 unit cube, p uniform in {1,2,3,4} (seed 0), Roe-Pike"),
+    "mixed_types": dict(kind="mixed", n=50, p=None, flux="roe_pike",
+                        desc="3D Euler HEX/TET/WEDGE/PYR 50^3 cells unit cube, p uniform in {1,2,3,4} (seed 0), "
+                             "Roe-Pike"),
 }
 
 
@@ -214,7 +217,7 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.set_stream(stream)
         if args.only_rk:
             return mixed_only_rk(torch, stream, args)
-        mx = mixed_measurements(torch, stream, args)
+        mx = mixed_measurements(torch, stream, args, "types" if args.workload == "mixed_types" else "hex")
         best = max(mx["forms"], key=lambda k: mx["forms"][k]["value"])
         return {"metric": "DOF-residual-evals/sec FP64 (batched graph vs plain per-group) at <=1e-12; %HBM peak",
                 "value": mx["forms"][best]["value"], "unit": "DOF-residual-evals/s", "n_gpus": world,
@@ -367,7 +370,8 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_adjoint and prob.pde == 3:
         res["adjoint"] = adjoint_measurements(torch, sim, prob, args)
     if not args.no_mixed:
-        res["mixed"] = mixed_measurements(torch, stream, args)
+        res["mixed_types"] = mixed_measurements(torch, stream, args, "types")
+        res["mixed"] = mixed_measurements(torch, stream, args, "hex")
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, workers=1)
     sim.close()
@@ -400,16 +404,38 @@ def adjoint_measurements(torch, sim, prob, args):
             "note": "forward sweep with checkpoints, segment recomputation, stage recomputation, 3 VJPs per step"}
 
 
-def mixed_measurements(torch, stream, args):
-    """Batched mixed-order workload: periodic unit cube of n^3 HEX volumes (n = 58: 195,112 volumes), p drawn
-    uniformly from {1,2,3,4} with seed 0, Roe-Pike, a seeded smooth sinusoidal state around a Mach 0.5 free stream.
+def _dense_flops(ops, nv=5):
+    """FP64 flops of one RK stage of a dense-operator volume (FMA = 2): interpolation to the cubature nodes, the
+    contravariant flux (~50 per node), the weak derivative, traces and lifts at the volume's own face order, M^-1."""
+    d, nvs, nvc = 3, ops.n_vs, ops.n_vc
+    nfc = sum(len(ops.w_fc(lf, ops.q)) for lf in range(ops.n_lf))
+    fma = nv * nvc * nvs * (1 + d) + 2 * nv * nfc * nvs + nv * nvs * nvs
+    return 2 * fma + 50 * nvc + 3 * nv * nvs
+
+
+def make_mixed(kind, n):
+    if kind == "types":
+        from dpgsolver_gb300.host.mixed_types import mixed_types_euler
+        return mixed_types_euler(n, seed=0)
+    from dpgsolver_gb300.host.mixed import mixed_euler
+    return mixed_euler(3, n, seed=0)
+
+
+def mixed_measurements(torch, stream, args, kind="types"):
+    """Batched mixed workloads, both Roe-Pike with a seeded smooth sinusoidal state around a Mach 0.5 free stream on
+    the periodic unit cube, p drawn uniformly from {1,2,3,4} per volume with seed 0:
+
+    * kind "types" (the configuration with mixed element types): n^3 cells (n = 50) split into HEX, TET, WEDGE
+      and PYR volumes (about 50/25/15/10 %, 207,312 volumes, 41.2 M state values), conforming and straight;
+    * kind "hex": n^3 HEX volumes (n = 58: 195,112 volumes, 54.6 M state values).
+
     SSP-RK3 steps of the whole mesh in five forms: one launch per group and face order from the host (plain),
     the same launches replayed from a CUDA graph, the fused persistent launches replayed from a graph, the
     per-group launches on parallel graph branches, and the autotuned choice (elements per CTA and form)."""
-    from dpgsolver_gb300.host.mixed import mixed_euler
     from dpgsolver_gb300.solver import BatchSimulation
+    n = args.mixed_n if kind == "hex" else args.types_n
     t0 = time.time()
-    prob = mixed_euler(3, args.mixed_n, seed=0)
+    prob = make_mixed(kind, n)
     setup_s = time.time() - t0
     sim = BatchSimulation(prob, stream=stream.cuda_stream)
     ns, dt = prob.n_state, prob.dt
@@ -434,21 +460,32 @@ def mixed_measurements(torch, stream, args):
     report = sim.autotune(dt, reps=3)
     tuned_form = sim.form
     run("autotuned_graph", tuned_form, True)
-    q = np.array([prob.groups[g].q for g in prob.vol_group])
-    flops = sum(flops_per_element(3, int(qq), 5, "roe_pike", coef_io=False) * int(np.sum(q == qq))
-                for qq in np.unique(q))
+    flops = 0
+    for g, ops in enumerate(prob.groups):
+        cnt = int(np.sum(prob.vol_group == g))
+        if getattr(ops, "dense", False):
+            flops += _dense_flops(ops) * cnt
+        else:
+            flops += flops_per_element(3, ops.q, 5, "roe_pike", coef_io=False) * cnt
     best = max(out, key=lambda k: out[k]["value"])
     fp64_peak = ctypes.c_double()
     from dpgsolver_gb300 import _lib
     _lib.check(_lib.load().dgpu_probe_fp64(20000, ctypes.byref(fp64_peak)))
     stage_s = out[best]["ms_per_step"] / 3 * 1e-3
-    bytes_eval = 8 * (2 * ns + int(np.sum((9 + 1) * q ** 3)) + int(np.sum(3 * prob.face_q.astype(np.int64) ** 2)))
+    n_vc = np.array([prob.groups[g].n_vc for g in prob.vol_group], dtype=np.int64)
+    n_fcn = int(np.sum(prob.face_q.astype(np.int64) ** 2))
+    bytes_eval = 8 * (2 * ns + int(np.sum(10 * n_vc)) + 3 * n_fcn)
     peak, peak_kind = hbm_peak()
+    from dpgsolver_gb300.host.element import HEX, PYR, TET, WEDGE
+    tname = {HEX: "HEX", TET: "TET", WEDGE: "WEDGE", PYR: "PYR"}
     res = {
-        "workload": f"3D Euler mixed-order HEX {args.mixed_n}^3 on the unit cube (straight, periodic), p uniform in "
-                    f"{{1,2,3,4}} (seed 0), Roe-Pike, Mach 0.5 seeded sinusoidal state",
-        "elements": prob.n_volumes, "n_state": ns, "groups": {int(g.p): int(np.sum(prob.vol_group == i))
-                                                             for i, g in enumerate(prob.groups)},
+        "workload": (f"3D Euler mixed-type {n}^3 cells on the unit cube (HEX/TET/WEDGE/PYR, straight, conforming, "
+                     f"periodic)" if kind == "types" else f"3D Euler mixed-order HEX {n}^3 on the unit cube "
+                                                          f"(straight, periodic)")
+                    + ", p uniform in {1,2,3,4} (seed 0), Roe-Pike, Mach 0.5 seeded sinusoidal state",
+        "elements": prob.n_volumes, "n_state": ns,
+        "groups": {f"{tname[getattr(o, 'e_type', HEX)]} p{o.p}": int(np.sum(prob.vol_group == i))
+                   for i, o in enumerate(prob.groups)},
         "face_orders": {int(qf) - 1: int(np.sum(prob.face_q == qf)) for qf in np.unique(prob.face_q)},
         "unit": "DOF-residual-evals/s", "steps": n_steps, "dt": dt,
         "forms": out,
@@ -458,21 +495,58 @@ def mixed_measurements(torch, stream, args):
         "autotune": {"form": tuned_form, "report": report},
         "fp64_pipe": {"flops_per_stage": flops, "achieved_tflops": flops / stage_s / 1e12,
                       "peak_tflops": fp64_peak.value, "frac": flops / stage_s / 1e12 / fp64_peak.value,
-                      "form": best, "note": "flops counted per element at its own order (face interpolation to "
+                      "form": best, "note": "flops counted per volume at its own order (face interpolation to "
                                             "p_f not counted)"},
         "eval_hbm": {"bytes_per_eval": bytes_eval, "achieved_gbs": bytes_eval / stage_s / 1e9,
                      "frac": bytes_eval / stage_s / 1e9 / peak, "peak_source": peak_kind},
         "setup_s": setup_s,
     }
+    if kind == "types":
+        res["counts"] = {tname[t]: c for t, c in prob.mesh.counts().items()}
+        if not args.no_cpu_baseline:
+            res["cpu_baseline"] = mixed_cpu_baseline(kind, seconds=min(10.0, args.cpu_seconds))
     sim.close()
     return res
 
 
+def _mixed_oracle_worker(a):
+    kind, n, seconds = a
+    sys.path.insert(0, HERE)
+    import oracle
+    prob = make_mixed(kind, n)
+    o = oracle.Oracle(prob)
+    o.compute_rhs(prob.sol)
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        o.compute_rhs(prob.sol)
+        k += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return prob.n_state * k / el, k, el, prob.n_volumes
+
+
+def mixed_cpu_baseline(kind, seconds, workers=1):
+    n = 8
+    if workers == 1:
+        v, k, el, nvol = _mixed_oracle_worker((kind, n, seconds))
+        vals, ks = [v], k
+    else:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            outs = pool.map(_mixed_oracle_worker, [(kind, n, seconds)] * workers)
+        vals, ks, nvol = [o[0] for o in outs], sum(o[1] for o in outs), outs[0][3]
+    return {"value": float(sum(vals)), "unit": "DOF-residual-evals/s", "cores": workers, "kind": "port",
+            "sample": f"the same generator at n = {n} ({nvol} volumes), {ks} residual evaluations over ~{seconds:.0f} s "
+                      f"per core with the C oracle (dense operators, reference data flow)"}
+
+
 def mixed_only_rk(torch, stream, args):
-    """One form of the mixed-order stages, graph-replayed RK steps only (profiling)."""
-    from dpgsolver_gb300.host.mixed import mixed_euler
+    """One form of the mixed stages, graph-replayed RK steps only (profiling)."""
     from dpgsolver_gb300.solver import BatchSimulation
-    prob = mixed_euler(3, args.mixed_n, seed=0)
+    kind = "types" if args.workload == "mixed_types" else "hex"
+    prob = make_mixed(kind, args.types_n if kind == "types" else args.mixed_n)
     sim = BatchSimulation(prob, stream=stream.cuda_stream)
     sim.form = {"plain": "plain", "per_group_graph": "plain", "fused": "fused",
                 "branches": "branches"}[args.mixed_form]
@@ -539,7 +613,10 @@ def run_reference(args, rank, world):
     # each step: every core evaluates residuals of the sample mesh for a bounded time
     secs = max(1.0, min(10.0, 120.0 / max(1, args.steps + args.warmup)))
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(w, secs, workers=cores)
+        if w["kind"] == "mixed":
+            cb = mixed_cpu_baseline("types" if args.workload == "mixed_types" else "hex", secs, workers=cores)
+        else:
+            cb = cpu_baseline(w, secs, workers=cores)
         if i >= args.warmup:
             per_step.append(cb["value"])
     value = statistics.median(per_step)
@@ -573,7 +650,8 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-budget-gb", type=float, default=4.0)
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched mixed-order measurements")
-    ap.add_argument("--mixed-n", type=int, default=58, help="volumes per direction of the mixed-order mesh")
+    ap.add_argument("--mixed-n", type=int, default=58, help="volumes per direction of the mixed-order HEX mesh")
+    ap.add_argument("--types-n", type=int, default=50, help="cells per direction of the mixed-type mesh (even)")
     ap.add_argument("--mixed-form", choices=["plain", "per_group_graph", "fused", "branches"], default="fused",
                     help="form of the mixed-order stages for --workload mixed3d --only-rk")
     args = ap.parse_args()
