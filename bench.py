@@ -284,10 +284,12 @@ def run_ours(args, rank, world, local_rank):
     n_plain = max(3, min(n_rk, 20))
     sim.ssp_rk3_steps(dt, 1, want_max=False)
     ms_plain = _timed(torch, stream, lambda: sim.ssp_rk3_steps(dt, n_plain, want_max=False), 1)
-    kt = {}
+    kt, kt_total = {}, {}
     for name in ("tp_volume_kernel", "tp_face_kernel", "tp_lift_kernel"):
         tot, cnt = sim.kernel_time(name)
-        kt[name] = tot / max(cnt, 1)
+        if cnt:
+            kt[name] = tot / cnt
+            kt_total[name] = tot
     sim.set_kernel_timing(False)
     plain_value = world * ns * 3 * n_plain / (max_over_ranks(ms_plain) * 1e-3)
 
@@ -318,14 +320,14 @@ def run_ours(args, rank, world, local_rank):
     e2e_ms = max_over_ranks(_timed(torch, stream, e2e_step, n_e2e))
     e2e_value = world * ns * 3 * n_e2e / (e2e_ms * 1e-3)
 
-    dom = max(kt, key=kt.get)
+    dom = max(kt_total, key=kt_total.get)     # the kernel with the largest share of the step
     peak, peak_kind = hbm_peak()
     ab = algorithmic_bytes(prob, dom)
     achieved = ab / (kt[dom] * 1e-3) / 1e9
     fp64_peak = ctypes.c_double()
     _lib.check(lib.dgpu_probe_fp64(20000, ctypes.byref(fp64_peak)))
     stage_flops = flops_per_element(prob.d, prob.ops.q, prob.n_var, w["flux"], coef_io=False) * prob.n_volumes
-    stage_ms = sum(kt.values())
+    stage_ms = ms_per_step / 3.0          # live graph replay (the kernel sum above is serialised and timed eagerly)
     res = {
         "metric": "DOF-residual-evals/sec FP64 (batched graph vs plain per-group) at <=1e-12; %HBM peak",
         "value": value,

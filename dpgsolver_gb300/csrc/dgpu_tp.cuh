@@ -137,28 +137,26 @@ __device__ __forceinline__ void load_ops(TPOps* sops, const TPOps& ops)
 // ---------------------------------------------------------------------------------------------------------------
 // Volume term + traces
 // ---------------------------------------------------------------------------------------------------------------
-template <int D, int Q, int NV, int PDE, bool GLL_IN>
-__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
-tp_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u)
+// Shared memory per element of the bodies below (doubles).
+template <int D, int Q, int NV>
+struct TPSmem {
+	static constexpr int N = TPShape<D, Q>::N;
+	static constexpr int VOL = NV * N * 2 + D * NV * N;   // su, st, sf
+	static constexpr int LIFT = 3 * NV * N + 8;           // sa, sb, sc, per-element scalars
+};
+
+// Volume term of the CTA's E elements; per element PER_E doubles at base (su, st, sf at the start).
+template <int D, int Q, int NV, int PDE, bool GLL_IN, int PER_E>
+__device__ __forceinline__ void tp_volume_body(const TPOps* sops, const TPParams& P, const double* __restrict__ u,
+                                               int v0, int n_here, double* base)
 {
 	using S = TPShape<D, Q>;
-	constexpr int N = S::N, NF = S::NF, E = S::E;
-	extern __shared__ double smem[];
-	TPOps* sops = reinterpret_cast<TPOps*>(smem);
-	double* base = smem + sizeof(TPOps) / 8;
-	// per element: su[NV*N] (state, GL nodal), st[NV*N] (tmp), sf[D*NV*N] (reference flux)
-	constexpr int PER_E = NV * N * 2 + D * NV * N;
-
+	constexpr int N = S::N, NF = S::NF;
 	const int tid = threadIdx.x;
-	load_ops(sops, ops);
-	const int v0 = blockIdx.x * E;
-	const int n_here = min(E, P.n_vol - v0);
 	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {   // coalesced: contiguous element blocks
 		const int e = i / (NV * N), r = i % (NV * N);
 		base[e * PER_E + r] = u[(size_t)v0 * NV * N + i];
 	}
-	if (blockIdx.x == 0 && tid == 0 && P.max_bits)
-		*P.max_bits = 0ull;
 	__syncthreads();
 
 	const int e = tid / N, node = tid % N;
@@ -267,6 +265,21 @@ tp_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u
 			}
 		}
 	}
+}
+
+template <int D, int Q, int NV, int PDE, bool GLL_IN>
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
+tp_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u)
+{
+	using S = TPShape<D, Q>;
+	extern __shared__ double smem[];
+	TPOps* sops = reinterpret_cast<TPOps*>(smem);
+	load_ops(sops, ops);
+	const int v0 = blockIdx.x * S::E;
+	if (blockIdx.x == 0 && threadIdx.x == 0 && P.max_bits)
+		*P.max_bits = 0ull;
+	tp_volume_body<D, Q, NV, PDE, GLL_IN, TPSmem<D, Q, NV>::VOL>(sops, P, u, v0, min(S::E, P.n_vol - v0),
+	                                                                   smem + sizeof(TPOps) / 8);
 }
 
 // ---------------------------------------------------------------------------------------------------------------
@@ -417,21 +430,15 @@ __device__ __noinline__ bool tp_positivity_exact(const double (*toB)[kQMax], con
 // 1e-5 on the pressure bound for its own FP32 arithmetic. Only CTAs holding an element that fails the filter run
 // the exact check, so the decisions are those of the exact FP64 check.
 
-template <int D, int Q, int NV, int MODE>
-__global__ void __launch_bounds__(TPShape<D, Q>::THREADS, 2)
-tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
+// Lift, 1/(wJ), then the residual (V^-1, max|rhs|) or the RK stage + positivity, for the CTA's E elements; per
+// element PER_E doubles at base.
+template <int D, int Q, int NV, int MODE, int PER_E>
+__device__ __forceinline__ void tp_lift_body(const TPOps* sops, const TPParams& P, const RkArgs& rk, int v0,
+                                             int n_here, double* base)
 {
 	using S = TPShape<D, Q>;
-	constexpr int N = S::N, NF = S::NF, E = S::E;
-	extern __shared__ double smem[];
-	TPOps* sops = reinterpret_cast<TPOps*>(smem);
-	double* base = smem + sizeof(TPOps) / 8;
-	constexpr int PER_E = 3 * NV * N + 8;   // sa, sb, sc + per-element scalars
-
+	constexpr int N = S::N, NF = S::NF;
 	const int tid = threadIdx.x;
-	load_ops(sops, ops);
-	const int v0 = blockIdx.x * E;
-	const int n_here = min(E, P.n_vol - v0);
 	const int e = tid / N, node = tid % N;
 	const bool active = e < n_here;
 	const int v = v0 + e;
@@ -596,6 +603,19 @@ tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 				rk.u[o + (size_t)k * N] = snew[k];
 		}
 	}
+}
+
+template <int D, int Q, int NV, int MODE>
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS, 2)
+tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
+{
+	using S = TPShape<D, Q>;
+	extern __shared__ double smem[];
+	TPOps* sops = reinterpret_cast<TPOps*>(smem);
+	load_ops(sops, ops);
+	const int v0 = blockIdx.x * S::E;
+	tp_lift_body<D, Q, NV, MODE, TPSmem<D, Q, NV>::LIFT>(sops, P, rk, v0, min(S::E, P.n_vol - v0),
+	                                                            smem + sizeof(TPOps) / 8);
 }
 
 // ---------------------------------------------------------------------------------------------------------------

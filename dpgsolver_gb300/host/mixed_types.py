@@ -59,94 +59,111 @@ class MixedTypeMesh:
         blk = rng.random((nb, nb, nb)) < c_blocks
         kind[blk[ijk[:, 0] // 2, ijk[:, 1] // 2, ijk[:, 2] // 2]] = 2
 
-        def cell(i, j, k):
-            return (i % n) + n * ((j % n) + n * (k % n))
+        def shifted(a, step):
+            s = ijk.copy()
+            s[:, a] = (s[:, a] + step) % n
+            return s[:, 0] + n * (s[:, 1] + n * s[:, 2])
 
-        def need(c, a, side):
-            """Requirement of cell c on its face normal to axis a (side 0: low, 1: high): 'Q', 'T' or None."""
-            if kind[c] == 0:
-                return "Q"
-            if kind[c] == 1:
-                return "T" if axis[c] == a else "Q"
-            return None
+        nb_hi = [shifted(a, 1) for a in range(3)]
+        nb_lo = [shifted(a, -1) for a in range(3)]
 
-        # resolve H/W conflicts by turning one side into a C cell
-        changed = True
-        while changed:
-            changed = False
-            for c in range(nc):
-                for a in range(3):
-                    nb = cell(*(ijk[c] + np.eye(3, dtype=int)[a]))
-                    ra, rb = need(c, a, 1), need(nb, a, 0)
-                    if ra is not None and rb is not None and ra != rb:
-                        kind[nb if rng.random() < 0.5 else c] = 2
-                        changed = True
-        # face kind of every cell face (a, low corner cell): between two C cells drawn, else the requirement
-        fkind = {}
-        for c in range(nc):
+        def need(a):
+            """Requirement of every cell on its faces normal to axis a: 0 quad, 1 two triangles, -1 none (C)."""
+            return np.where(kind == 0, 0, np.where(kind == 1, (axis == a).astype(np.int64), -1))
+
+        # resolve H/W conflicts by turning one side into a C cell (none arise with z-columns of W cells)
+        while True:
+            bad = False
             for a in range(3):
-                nb = cell(*(ijk[c] + np.eye(3, dtype=int)[a]))
-                r = need(c, a, 1) or need(nb, a, 0)
-                fkind[(c, a)] = r if r is not None else ("T" if rng.random() < p_tri else "Q")
+                r = need(a)
+                r1, r2 = r, r[nb_hi[a]]
+                clash = np.nonzero((r1 >= 0) & (r2 >= 0) & (r1 != r2))[0]
+                if len(clash):
+                    bad = True
+                    flip = rng.random(len(clash)) < 0.5
+                    kind[np.where(flip, nb_hi[a][clash], clash)] = 2
+            if not bad:
+                break
+        # face kind between every cell and its +a neighbour: 1 = two triangles, 0 = quad
+        fk = []
+        for a in range(3):
+            r = need(a)
+            r1, r2 = r, r[nb_hi[a]]
+            free = rng.random(nc) < p_tri
+            fk.append(np.where(r1 >= 0, r1, np.where(r2 >= 0, r2, free.astype(np.int64))))
         self.cell_kind = kind
 
-        # ---- volumes ----
+        # ---- volumes (coordinates in units of h/2: corners even, centres odd) ----
         V = n ** 3   # global vertex ids: corners i + n j + n^2 k (periodic), centres V + cell
-        types, gids, xs = [], [], []
+        types, gids, units = [], [], []
+        kl, il = kind.tolist(), ijk.tolist()
+        fkl = [f.tolist() for f in fk]
+        nbl = [x.tolist() for x in nb_lo]
 
-        def corner(c, off):
-            i, j, k = ijk[c] + np.asarray(off)
-            return cell(i, j, k), (ijk[c] + np.asarray(off)) * self.h
+        def corner(i, j, k):
+            return (i % n) + n * ((j % n) + n * (k % n)), (2 * i, 2 * j, 2 * k)
 
-        def face_corners(c, a, side):
+        def face_corners(i, j, k, a, side):
             """The 4 corners of the cell face normal to a at side 0/1, tensor order in the tangential axes."""
-            t = [x for x in range(3) if x != a]
+            t0, t1 = [x for x in range(3) if x != a]
             out = []
             for dv in (0, 1):
                 for du in (0, 1):
                     off = [0, 0, 0]
                     off[a] = side
-                    off[t[0]] = du
-                    off[t[1]] = dv
-                    out.append(corner(c, off))
+                    off[t0] = du
+                    off[t1] = dv
+                    out.append(corner(i + off[0], j + off[1], k + off[2]))
             return out
 
         def add(t, verts):
-            g = [v[0] for v in verts]
-            x = np.array([v[1] for v in verts], dtype=np.float64)
-            A, b0 = _affine(t, x)
-            if np.linalg.det(A) < 0.0:     # mirror to a positive orientation
-                perm = {TET: [0, 2, 1, 3], WEDGE: [0, 2, 1, 3, 5, 4], PYR: [0, 2, 1, 3, 4],
-                        HEX: [0, 2, 1, 3, 4, 6, 5, 7]}[t]
-                g = [g[m] for m in perm]
-                x = x[perm]
             types.append(t)
-            gids.append(g)
-            xs.append(x)
+            gids.append([v[0] for v in verts])
+            units.append([v[1] for v in verts])
 
         for c in range(nc):
-            if kind[c] == 0:
-                add(HEX, [corner(c, (dx, dy, dz)) for dz in (0, 1) for dy in (0, 1) for dx in (0, 1)])
-            elif kind[c] == 1:
-                a = int(axis[c])
-                lo, hi = face_corners(c, a, 0), face_corners(c, a, 1)
+            i, j, k = il[c]
+            if kl[c] == 0:
+                add(HEX, [corner(i + dx, j + dy, k + dz) for dz in (0, 1) for dy in (0, 1) for dx in (0, 1)])
+            elif kl[c] == 1:
+                lo, hi = face_corners(i, j, k, 2, 0), face_corners(i, j, k, 2, 1)
                 for tri in ((0, 1, 3), (0, 3, 2)):     # triangles of the diagonal (0,0)-(1,1)
                     add(WEDGE, [lo[m] for m in tri] + [hi[m] for m in tri])
             else:
-                centre = (V + c, (ijk[c] + 0.5) * self.h)
+                centre = (V + c, (2 * i + 1, 2 * j + 1, 2 * k + 1))
                 for a in range(3):
                     for side in (0, 1):
-                        fk = fkind[(c, a)] if side == 1 else fkind[(cell(*(ijk[c] - np.eye(3, dtype=int)[a])), a)]
-                        fc = face_corners(c, a, side)
-                        if fk == "Q":
+                        tri_face = fkl[a][c] if side == 1 else fkl[a][nbl[a][c]]
+                        fc = face_corners(i, j, k, a, side)
+                        if not tri_face:
                             add(PYR, fc + [centre])
                         else:
                             for tri in ((0, 1, 3), (0, 3, 2)):
                                 add(TET, [fc[m] for m in tri] + [centre])
         self.types = np.array(types, dtype=np.int32)
         self.n_volumes = len(types)
+        # affine maps per type (batched), mirrored to a positive orientation where needed
+        self.A = np.empty((self.n_volumes, 3, 3))
+        self.b = np.empty((self.n_volumes, 3))
+        self.X = [None] * self.n_volumes
+        mirror = {TET: [0, 2, 1, 3], WEDGE: [0, 2, 1, 3, 5, 4], PYR: [0, 2, 1, 3, 4], HEX: [0, 2, 1, 3, 4, 6, 5, 7]}
+        for t in (HEX, TET, WEDGE, PYR):
+            sel = np.nonzero(self.types == t)[0]
+            if len(sel) == 0:
+                continue
+            X = np.array([units[v] for v in sel], dtype=np.float64) * (0.5 * self.h)
+            A, b0 = _affine_batch(t, X)
+            neg = np.nonzero(np.linalg.det(A) < 0.0)[0]
+            if len(neg):
+                X[neg] = X[neg][:, mirror[t]]
+                for r in neg:
+                    g = gids[sel[r]]
+                    gids[sel[r]] = [g[m] for m in mirror[t]]
+                A[neg], b0[neg] = _affine_batch(t, X[neg])
+            self.A[sel], self.b[sel] = A, b0
+            for r, v in enumerate(sel):
+                self.X[v] = X[r]
         self.gids = gids
-        self.X = xs
         self._faces()
 
     def _faces(self):
@@ -189,6 +206,24 @@ class MixedTypeMesh:
         return {int(t): int(np.sum(self.types == t)) for t in (HEX, TET, WEDGE, PYR)}
 
 
+_AFF_SUB = {TET: [0, 1, 2, 3], WEDGE: [0, 1, 2, 3], PYR: [0, 1, 2, 4], HEX: [0, 1, 2, 4]}
+
+
+def _affine_batch(t, X):
+    """A (n, 3, 3), b (n, 3) with X[:, m] = A r_m + b for the reference vertices r_m of type t (checked on every
+    vertex: the volumes must be affine images of the reference element)."""
+    R = S.VERTS[t]
+    sub = _AFF_SUB[t]
+    Rd = (R[sub[1:]] - R[sub[0]]).T                      # columns r_m - r_0
+    Xd = np.transpose(X[:, sub[1:]] - X[:, [sub[0]]], (0, 2, 1))
+    A = Xd @ np.linalg.inv(Rd)
+    b = X[:, sub[0]] - A @ R[sub[0]]
+    err = np.max(np.abs(np.einsum("vij,mj->vmi", A, R) + b[:, None, :] - X)) if len(X) else 0.0
+    if err > 1e-12 * max(1.0, float(np.max(np.abs(X))) if len(X) else 1.0):
+        raise AssertionError("volume is not an affine image of its reference element")
+    return A, b
+
+
 def _affine(t, x):
     """A, b with x_m = A r_m + b for the reference vertices r_m (affine volumes)."""
     R = S.VERTS[t]
@@ -227,10 +262,7 @@ class MixedTypeProblem:
         self.state_off[1:] = np.cumsum(self.n_var * n_vs)
         self.group_vols = [np.nonzero(self.vol_group == g)[0] for g in range(len(self.groups))]
         # affine geometry per volume: m = J A^-T (m(n,i,j) = J dr_j/dx_i), J = det A
-        self.A = np.empty((nv, 3, 3))
-        self.b = np.empty((nv, 3))
-        for v in range(nv):
-            self.A[v], self.b[v] = _affine(int(mesh.types[v]), mesh.X[v])
+        self.A, self.b = mesh.A, mesh.b
         self.J = np.linalg.det(self.A)
         if np.any(self.J <= 0.0):
             raise AssertionError("non-positive Jacobian")
@@ -245,22 +277,33 @@ class MixedTypeProblem:
         self.dt = 0.0
 
     def _face_geometry(self):
+        """Normals and J_f of the side-0 volume (constant on affine faces) and the side-0 face-rule weights, at the
+        canonical nodes of every face."""
         mesh = self.mesh
-        nfn = int(self.face_off[-1])
-        self.normals_fc = np.empty((nfn, 3))
-        self.jacobian_det_fc = np.empty(nfn)
-        self.w_fc = np.empty(nfn)
-        for f in range(mesh.n_faces):
-            v0, lf0 = mesh.face_vol[f, 0], mesh.face_lf[f, 0]
-            t0 = int(mesh.types[v0])
-            nref = (self.groups[self.vol_group[v0]].normals_ref[lf0])
-            nun = self.m[v0] @ nref
-            jn = np.linalg.norm(nun)
-            o, e = self.face_off[f], self.face_off[f + 1]
-            self.normals_fc[o:e] = nun / jn
-            self.jacobian_det_fc[o:e] = jn
-            ft = S.TRI if len(S.F_VE[t0][lf0]) == 3 else S.QUAD
-            self.w_fc[o:e] = S.face_rule(ft, int(self.face_q[f]))[1]
+        v0, lf0 = mesh.face_vol[:, 0], mesh.face_lf[:, 0]
+        nref = np.zeros((mesh.n_faces, 3))
+        ftype = np.zeros(mesh.n_faces, dtype=np.int32)
+        for t in (HEX, TET, WEDGE, PYR):
+            sel = np.nonzero(mesh.types[v0] == t)[0]
+            if len(sel) == 0:
+                continue
+            nr = S.reference_normals_3d(t) if t != HEX else TPOperatorSet(HEX, 1).normals_ref
+            nref[sel] = nr[lf0[sel]]
+            ftype[sel] = np.array([len(fv) for fv in S.F_VE[t]])[lf0[sel]]
+        nun = np.einsum("fij,fj->fi", self.m[v0], nref)
+        jn = np.linalg.norm(nun, axis=1)
+        nfc = np.diff(self.face_off)
+        self.normals_fc = np.repeat(nun / jn[:, None], nfc, axis=0)
+        self.jacobian_det_fc = np.repeat(jn, nfc)
+        self.w_fc = np.empty(int(self.face_off[-1]))
+        for nvert, ft in ((3, S.TRI), (4, S.QUAD)):
+            for qf in np.unique(self.face_q):
+                sel = np.nonzero((ftype == nvert) & (self.face_q == qf))[0]
+                if len(sel) == 0:
+                    continue
+                wr = S.face_rule(ft, int(qf))[1]
+                idx = (self.face_off[sel][:, None] + np.arange(len(wr))[None, :]).ravel()
+                self.w_fc[idx] = np.tile(wr, len(sel))
 
     # ---- layout helpers (as MixedTPProblem) ----
     @property
@@ -301,13 +344,22 @@ class MixedTypeProblem:
         return np.concatenate([np.arange(n, dtype=np.int32) for n in np.diff(self.face_off)])
 
     def flat(self) -> dict:
-        nv = self.mesh.n_volumes
-        mvc, jvc = [None] * nv, [None] * nv
+        n_vc = np.array([self.groups[g].n_vc for g in self.vol_group], dtype=np.int64)
+        vc_off = np.zeros(len(n_vc) + 1, dtype=np.int64)
+        vc_off[1:] = np.cumsum(n_vc)
+        mflat = np.empty(int(vc_off[-1]) * 9)
+        jflat = np.empty(int(vc_off[-1]))
         for g, vols in enumerate(self.group_vols):
-            n_vc = self.groups[g].n_vc
-            for v in vols:
-                mvc[v] = np.repeat(self.m[v].T.reshape(9, 1), n_vc, axis=1).ravel()   # [j][i][n]
-                jvc[v] = np.full(n_vc, self.J[v])
+            if len(vols) == 0:
+                continue
+            nq = self.groups[g].n_vc
+            mt = np.transpose(self.m[vols], (0, 2, 1)).reshape(len(vols), 9)      # [j][i] per volume
+            blk = np.repeat(mt[:, :, None], nq, axis=2).reshape(len(vols), 9 * nq)
+            idx = (9 * vc_off[vols])[:, None] + np.arange(9 * nq)[None, :]
+            mflat[idx] = blk
+            jidx = vc_off[vols][:, None] + np.arange(nq)[None, :]
+            jflat[jidx] = np.repeat(self.J[vols][:, None], nq, axis=1)
+        mvc, jvc = [mflat], [jflat]
         return {
             "groups": self.groups,
             "vol_group": self.vol_group,
@@ -333,8 +385,8 @@ class MixedTypeProblem:
                 x = self.vc_xyz(g)
                 U = fn(x.reshape(-1, 3)).reshape(len(vols), ops.n_vc, self.n_var)
                 # orthonormal basis, affine volume: coef = M_ref^-1 cv0^T diag(w) U
-                Minv = np.linalg.inv(ops.mass())
-                coef = np.einsum("ab,nb,n,vnk->vka", Minv, ops.cv0_vs_vc(), ops.w_vc, U)
+                Pm = np.linalg.inv(ops.mass()) @ (ops.cv0_vs_vc().T * ops.w_vc[None, :])   # (n_vs, n_vc)
+                coef = np.transpose(U, (0, 2, 1)) @ Pm.T                                   # (v, k, a)
             else:
                 xs = tp_nodes(ops.x_vs, 3)
                 x = np.einsum("vij,nj->vni", self.A[vols], xs) + self.b[vols][:, None, :]

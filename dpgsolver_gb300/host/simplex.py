@@ -201,8 +201,18 @@ def quad_rule(q: int):
     return np.stack([np.tile(x1, q), np.repeat(x1, q)], axis=1), np.tile(w1, q) * np.repeat(w1, q)
 
 
+_FACE_RULES = {}
+
+
 def face_rule(ftype: int, q: int):
-    return tri_rule(q) if ftype == TRI else quad_rule(q)
+    """Cached (nodes, weights) of the face reference element (read-only arrays)."""
+    key = (ftype, q)
+    if key not in _FACE_RULES:
+        x, w = tri_rule(q) if ftype == TRI else quad_rule(q)
+        x.setflags(write=False)
+        w.setflags(write=False)
+        _FACE_RULES[key] = (x, w)
+    return _FACE_RULES[key]
 
 
 def volume_rule(e_type: int, q: int):
