@@ -231,8 +231,12 @@ cudaError_t launch_lift_rk_t(dgpu_ctx* c, double dt, int stage, int want_max)
 	rk.positivity = c->positivity;
 	rk.want_max = want_max;
 	record_start(c, "tp_lift_kernel");
-	tp_lift_kernel<D, Q, NV, kModeRkGl><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
-		c->ops, c->params(), rk);
+	if (want_max)
+		tp_lift_kernel<D, Q, NV, kModeRkGl><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
+			c->ops, c->params(), rk);
+	else
+		tp_lift_kernel<D, Q, NV, kModeRkGlNoMax><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
+			c->ops, c->params(), rk);
 	record_stop(c);
 	c->launches++;
 	return cudaGetLastError();
@@ -340,6 +344,8 @@ cudaError_t bind(dgpu_ctx* c)
 	if ((e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRhs>, smem, (int)lift_smem_bytes<D, Q, NV>())))
 		return e;
 	if ((e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRkGl>, smem, (int)lift_smem_bytes<D, Q, NV>())))
+		return e;
+	if ((e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRkGlNoMax>, smem, (int)lift_smem_bytes<D, Q, NV>())))
 		return e;
 	if ((e = cudaFuncSetAttribute(tp_convert_kernel<D, Q, NV, true>, smem, (int)convert_smem_bytes<D, Q, NV>())))
 		return e;

@@ -327,7 +327,9 @@ tp_face_kernel(const TPParams P)
 // ---------------------------------------------------------------------------------------------------------------
 // Lift + M^-1 + (residual | RK stage + positivity)
 // ---------------------------------------------------------------------------------------------------------------
-enum LiftMode { kModeRhs = 0, kModeRkGl = 1 };
+// kModeRkGl reads rk.want_max at run time; kModeRkGlNoMax is the RK stage compiled without the max |rhs| path
+// (fewer registers for the common graph-replayed stage).
+enum LiftMode { kModeRhs = 0, kModeRkGl = 1, kModeRkGlNoMax = 2 };
 
 struct RkArgs {
 	double* u;         // kModeRkGl: state as GL nodal values (ug), updated in place
@@ -482,10 +484,10 @@ __device__ __forceinline__ void tp_lift_body(const TPOps* sops, const TPParams& 
 			Rg[k] *= iw;
 	}
 
-	const bool need_coef = (MODE == kModeRhs) || rk.want_max;   // uniform across the grid
+	const bool need_coef = (MODE == kModeRhs) || (MODE == kModeRkGl && rk.want_max);   // uniform across the grid
 	unsigned long long mx = 0ull;
 	double R[NV];
-	if (need_coef) {
+	if (MODE != kModeRkGlNoMax && need_coef) {
 		// R = V^-1 R_gl (GLL coefficients): D passes of Binv
 		if (active)
 #pragma unroll
@@ -605,8 +607,12 @@ __device__ __forceinline__ void tp_lift_body(const TPOps* sops, const TPParams& 
 	}
 }
 
+// Minimum CTAs per SM of the lift kernel (caps its registers): 3 for the plain RK stage, 2 otherwise.
+template <int MODE>
+struct LiftOccupancy { static constexpr int value = (MODE == kModeRkGlNoMax) ? 3 : 2; };
+
 template <int D, int Q, int NV, int MODE>
-__global__ void __launch_bounds__(TPShape<D, Q>::THREADS, 2)
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS, LiftOccupancy<MODE>::value)
 tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 {
 	using S = TPShape<D, Q>;
