@@ -609,7 +609,7 @@ __device__ __forceinline__ void tp_lift_body(const TPOps* sops, const TPParams& 
 
 // Minimum CTAs per SM of the lift kernel (caps its registers): 3 for the plain RK stage, 2 otherwise.
 template <int MODE>
-struct LiftOccupancy { static constexpr int value = (MODE == kModeRkGlNoMax) ? 3 : 2; };
+struct LiftOccupancy { static constexpr int value = (MODE == kModeRkGlNoMax) ? 4 : 2; };
 
 template <int D, int Q, int NV, int MODE>
 __global__ void __launch_bounds__(TPShape<D, Q>::THREADS, LiftOccupancy<MODE>::value)
