@@ -408,10 +408,20 @@ def adjoint_measurements(torch, sim, prob, args):
 
 def _dense_flops(ops, nv=5):
     """FP64 flops of one RK stage of a dense-operator volume (FMA = 2): interpolation to the cubature nodes, the
-    contravariant flux (~50 per node), the weak derivative, traces and lifts at the volume's own face order, M^-1."""
+    contravariant flux (~50 per node), the weak derivative, traces and lifts at the volume's own face order and
+    the stage update. WEDGE volume terms are counted sum-factorised (TRI x LINE), as the kernel applies them;
+    M^-1 is 1/J for these orthonormal bases."""
     d, nvs, nvc = 3, ops.n_vs, ops.n_vc
     nfc = sum(len(ops.w_fc(lf, ops.q)) for lf in range(ops.n_lf))
-    fma = nv * nvc * nvs * (1 + d) + 2 * nv * nfc * nvs + nv * nvs * nvs
+    if getattr(ops, "e_type", None) == 6:     # WEDGE: TRI x LINE factors
+        t0, _, l0, _ = ops.prism_factors()
+        ntc, ntv = t0.shape
+        nlc, nlv = l0.shape
+        vol = nv * (nlv * ntc * ntv + nvc * nlv) \
+            + nv * (2 * nlv * ntc * nlc + nlc * ntv * ntc + nvs * (2 * ntc + nlc))
+    else:
+        vol = nv * nvc * nvs * (1 + d)
+    fma = vol + 2 * nv * nfc * nvs
     return 2 * fma + 50 * nvc + 3 * nv * nvs
 
 

@@ -79,7 +79,10 @@ class DenseOperators(ctypes.Structure):
     _fields_ = [("elem_type", ctypes.c_int), ("p", ctypes.c_int), ("n_vs", ctypes.c_int), ("n_vc", ctypes.c_int),
                 ("cv0_vs_vc", c_double_p), ("cv1_vs_vc", c_double_p), ("w_vc", c_double_p),
                 ("n_lf", ctypes.c_int), ("n_ord", ctypes.c_int), ("n_fc", c_int_p),
-                ("cv0_vs_fc", ctypes.POINTER(c_double_p)), ("w_fc", ctypes.POINTER(c_double_p))]
+                ("cv0_vs_fc", ctypes.POINTER(c_double_p)), ("w_fc", ctypes.POINTER(c_double_p)),
+                ("n_tri_vs", ctypes.c_int), ("n_tri_vc", ctypes.c_int), ("n_line_vs", ctypes.c_int),
+                ("n_line_vc", ctypes.c_int), ("tri_cv0", c_double_p), ("tri_cv1", c_double_p),
+                ("line_cv0", c_double_p), ("line_cv1", c_double_p)]
 
 
 class Group(ctypes.Structure):

@@ -135,8 +135,8 @@ template <int D, int Q, int NV>
 size_t blift_smem(int E) { return sizeof(BatchOps) + (size_t)E * BSmem<D, Q, NV>::LIFT * sizeof(double); }
 template <int D, int Q, int NV>
 size_t bconv_smem(int E) { return sizeof(BatchOps) + (size_t)E * 3 * NV * TPShape<D, Q>::N * sizeof(double); }
-size_t dvol_smem(int nv, const DGroup& G, int E) { return (size_t)E * DSmem::vol(nv, G.n_vs, G.n_vc) * sizeof(double); }
-size_t dlift_smem(int nv, const DGroup& G, int E) { return (size_t)E * DSmem::lift(nv, G.n_vs) * sizeof(double); }
+size_t dvol_smem(int, const DGroup& G, int E) { return (size_t)E * G.vol_per_e * sizeof(double); }
+size_t dlift_smem(int, const DGroup& G, int E) { return (size_t)E * G.lift_per_e * sizeof(double); }
 
 int threads_for(int E, int N) { return ((E * N + 31) / 32) * 32; }
 
@@ -680,11 +680,47 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 			G.n_vc = op->n_vc;
 			G.n_lf = op->n_lf;
 			G.n_ord = op->n_ord;
+			G.vol_per_e = DSmem::vol(nv, G.n_vs, G.n_vc);
+			G.lift_per_e = DSmem::lift(nv, G.n_vs);
+			if (op->elem_type == DGPU_WEDGE && op->tri_cv0 && op->tri_cv1 && op->line_cv0 && op->line_cv1) {
+				const int ntv = op->n_tri_vs, ntc = op->n_tri_vc, nlv = op->n_line_vs, nlc = op->n_line_vc;
+				if (ntv < 1 || ntc < 1 || nlv < 1 || nlc < 1 || ntv * nlv != op->n_vs || ntc * nlc != op->n_vc)
+					return reject(DGPU_ERR_INVALID_ARGUMENT, "WEDGE factor sizes do not match n_vs / n_vc");
+				// the factors must reproduce the dense operators
+				double scale = 0.0, diff = 0.0;
+				for (int rz = 0; rz < nlc; ++rz)
+					for (int rt = 0; rt < ntc; ++rt)
+						for (int c0 = 0; c0 < nlv; ++c0)
+							for (int t = 0; t < ntv; ++t) {
+								const size_t rr = (size_t)rz * ntc + rt, cc = (size_t)c0 * ntv + t;
+								const size_t ti = (size_t)rt * ntv + t, li = (size_t)rz * nlv + c0;
+								const double ref[4] = {op->cv0_vs_vc[rr * op->n_vs + cc],
+								                       op->cv1_vs_vc[(0 * (size_t)op->n_vc + rr) * op->n_vs + cc],
+								                       op->cv1_vs_vc[(1 * (size_t)op->n_vc + rr) * op->n_vs + cc],
+								                       op->cv1_vs_vc[(2 * (size_t)op->n_vc + rr) * op->n_vs + cc]};
+								const double fac[4] = {op->line_cv0[li] * op->tri_cv0[ti],
+								                       op->line_cv0[li] * op->tri_cv1[ti],
+								                       op->line_cv0[li] * op->tri_cv1[(size_t)ntc * ntv + ti],
+								                       op->line_cv1[li] * op->tri_cv0[ti]};
+								for (int k = 0; k < 4; ++k) {
+									scale = std::max(scale, fabs(ref[k]));
+									diff = std::max(diff, fabs(ref[k] - fac[k]));
+								}
+							}
+				if (!(diff <= 1e-12 * scale))
+					return reject(DGPU_ERR_INVALID_ARGUMENT, "the WEDGE factors do not reproduce the dense operators");
+				G.prism = 1;
+				G.n_tvs = ntv;
+				G.n_tvc = ntc;
+				G.n_lvs = nlv;
+				G.n_lvc = nlc;
+				G.vol_per_e += DSmem::prism_tmp(nv, ntv, ntc, nlv, nlc);
+			}
 			G.E = std::max(1, 256 / op->n_vc);
-			while (G.E > 1 && (size_t)G.E * DSmem::vol(nv, G.n_vs, G.n_vc) * 8 > 96 * 1024)
+			while (G.E > 1 && (size_t)G.E * G.vol_per_e * 8 > 96 * 1024)
 				G.E /= 2;
 			G.E_fused = G.E;
-			if ((size_t)DSmem::vol(nv, G.n_vs, G.n_vc) * 8 > 200 * 1024)
+			if ((size_t)G.vol_per_e * 8 > 200 * 1024)
 				return reject(DGPU_ERR_UNSUPPORTED, "dense operator set too large for one volume per CTA");
 		}
 	}
@@ -959,6 +995,28 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 			}
 		if (!host_invert(nvs, M.data(), Minv.data()))
 			return reject(DGPU_ERR_INVALID_ARGUMENT, "singular reference mass matrix of a dense group");
+		// an orthonormal basis: M_ref = I to rounding, so M^-1 = 1/J without the n_vs^2 product
+		double off_id = 0.0;
+		for (int a = 0; a < nvs; ++a)
+			for (int b = 0; b < nvs; ++b)
+				off_id = std::max(off_id, fabs(M[(size_t)a * nvs + b] - (a == b ? 1.0 : 0.0)));
+		G.minv_identity = off_id <= 1e-13 ? 1 : 0;
+		if (G.prism) {
+			double *d_t0 = nullptr, *d_t1 = nullptr, *d_l0 = nullptr, *d_l1 = nullptr;
+			const size_t nt = (size_t)G.n_tvc * G.n_tvs, nl = (size_t)G.n_lvc * G.n_lvs;
+			B_TRY(upload_vec(&d_t0, std::vector<double>(op->tri_cv0, op->tri_cv0 + nt)));
+			c->dense_bufs.push_back(d_t0);
+			B_TRY(upload_vec(&d_t1, std::vector<double>(op->tri_cv1, op->tri_cv1 + 2 * nt)));
+			c->dense_bufs.push_back(d_t1);
+			B_TRY(upload_vec(&d_l0, std::vector<double>(op->line_cv0, op->line_cv0 + nl)));
+			c->dense_bufs.push_back(d_l0);
+			B_TRY(upload_vec(&d_l1, std::vector<double>(op->line_cv1, op->line_cv1 + nl)));
+			c->dense_bufs.push_back(d_l1);
+			G.tri0 = d_t0;
+			G.tri1 = d_t1;
+			G.line0 = d_l0;
+			G.line1 = d_l1;
+		}
 		std::vector<double> fops;
 		std::vector<long long> foff((size_t)kMaxLf * kMaxOrd * (kQMax + 1), -1);
 		for (int lf = 0; lf < op->n_lf; ++lf)

@@ -46,6 +46,14 @@ struct DGroup {
 	const double* inv_J;        // per element 1 / J
 	const double* fops;         // face operator table
 	const long long* fop_off;   // [(lf * n_ord + ord) * (kQMax + 1) + q_f] -> offset in fops, -1 if absent
+	int vol_per_e, lift_per_e;  // shared memory per volume (doubles) of the volume and lift bodies
+	int minv_identity;          // M_ref is the identity to rounding (orthonormal basis): M^-1 = 1/J
+	int prism;                  // WEDGE with TRI x LINE factors: sum-factorised volume term
+	int n_tvs, n_tvc, n_lvs, n_lvc;
+	const double* tri0;         // n_tvc x n_tvs
+	const double* tri1;         // 2 x n_tvc x n_tvs
+	const double* line0;        // n_lvc x n_lvs
+	const double* line1;        // n_lvc x n_lvs
 };
 
 struct BParams {

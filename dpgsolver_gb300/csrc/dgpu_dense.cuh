@@ -18,10 +18,152 @@
 namespace dgpu {
 
 struct DSmem {
-	// doubles per element: state (NV n_vs), then fluxes (D NV n_vc) reused by the lift as rhs (NV n_vs)
+	// doubles per element: state (NV n_vs), fluxes (D NV n_vc) and, for a factorised WEDGE, the partial sums of
+	// the sum-factorised contractions; the lift keeps its rhs (NV n_vs)
 	static __host__ __device__ int vol(int nv, int n_vs, int n_vc) { return nv * n_vs + 3 * nv * n_vc; }
+	static __host__ __device__ int prism_tmp(int nv, int n_tvs, int n_tvc, int n_lvs, int n_lvc)
+	{
+		return nv * (2 * n_lvs * n_tvc + n_lvc * n_tvs);
+	}
 	static __host__ __device__ int lift(int nv, int n_vs) { return 2 * nv * n_vs + 2; }
 };
+
+// Traces of the CTA's volumes (state in shared memory) at each face's canonical nodes.
+template <int NV>
+__device__ void dtraces(const BParams& P, const DGroup& G, int e0, int n_here, const double* smem, int PER_E)
+{
+	const int nvs = G.n_vs;
+	for (int it = threadIdx.x; it < n_here * G.n_lf * kQMax * kQMax; it += blockDim.x) {
+		const int i = it % (kQMax * kQMax), el = it / (kQMax * kQMax), lf = el % G.n_lf, e = el / G.n_lf;
+		const long long v = G.elem0 + e0 + e;
+		const int4 fd = P.elf[v * kMaxLf + lf];
+		const long long fb = P.fbase[fd.x];
+		const int nff = (int)(P.fbase[fd.x + 1] - fb);
+		if (i >= nff)
+			continue;
+		const double* op = G.fops + G.fop_off[(lf * G.n_ord + fd.w) * (kQMax + 1) + fd.z] + (long long)i * nvs;
+		const double* su = smem + e * PER_E;
+		double W[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			W[k] = 0.0;
+		for (int m = 0; m < nvs; ++m) {
+			const double c = __ldg(op + m);
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				W[k] += c * su[k * nvs + m];
+		}
+		double* dst = P.traces + 2 * NV * fb + (long long)fd.y * NV * nff;
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			dst[k * nff + i] = W[k];
+	}
+}
+
+// Sum-factorised volume term of a WEDGE volume whose operators are Kronecker products of TRI and LINE factors
+// (basis index c * n_tvs + t, node index rz * n_tvc + rt): s_vc in two passes (TRI, then LINE), the flux, then
+// sum_j cv1_j^T (w fr_j) as LINE then TRI passes for x and y and TRI then LINE for z. Fills sf and vol_gl.
+template <int D, int NV, int PDE>
+__device__ void dvol_prism_phases(const BParams& P, const DGroup& G, int e0, int n_here, double* smem, int PER_E)
+{
+	const int nvs = G.n_vs, nvc = G.n_vc, ntv = G.n_tvs, ntc = G.n_tvc, nlv = G.n_lvs, nlc = G.n_lvc;
+	const double* __restrict__ T0 = G.tri0;
+	const double* __restrict__ T1 = G.tri1;
+	const double* __restrict__ L0 = G.line0;
+	const double* __restrict__ L1 = G.line1;
+	// 1a: v[k][c][rt] = sum_t T0[rt][t] s[k][c][t]
+	for (int it = threadIdx.x; it < n_here * NV * nlv * ntc; it += blockDim.x) {
+		const int e = it / (NV * nlv * ntc), rem = it % (NV * nlv * ntc);
+		const int k = rem / (nlv * ntc), c = (rem / ntc) % nlv, rt = rem % ntc;
+		const double* su = smem + e * PER_E + k * nvs + c * ntv;
+		const double* row = T0 + (long long)rt * ntv;
+		double acc = 0.0;
+		for (int t = 0; t < ntv; ++t)
+			acc += __ldg(row + t) * su[t];
+		smem[e * PER_E + NV * nvs + 3 * NV * nvc + rem] = acc;
+	}
+	__syncthreads();
+	// 1b: W[k] at (rz, rt) = sum_c L0[rz][c] v[k][c][rt]; the flux there
+	for (int it = threadIdx.x; it < n_here * nvc; it += blockDim.x) {
+		const int e = it / nvc, r = it % nvc, rz = r / ntc, rt = r % ntc;
+		const double* v = smem + e * PER_E + NV * nvs + 3 * NV * nvc;
+		double* sf = smem + e * PER_E + NV * nvs;
+		double W[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			double acc = 0.0;
+			for (int c = 0; c < nlv; ++c)
+				acc += __ldg(L0 + rz * nlv + c) * v[(k * nlv + c) * ntc + rt];
+			W[k] = acc;
+		}
+		double g[D * D];
+		const double* gm = P.gmet + G.gmet_off + (long long)(e0 + e) * D * D * nvc;
+#pragma unroll
+		for (int cc = 0; cc < D * D; ++cc)
+			g[cc] = gm[cc * nvc + r];
+		if constexpr (PDE == kEuler) {
+			double fr[D][D + 2];
+			euler_flux_ref<D>(W, g, fr);
+#pragma unroll
+			for (int j = 0; j < D; ++j)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					sf[(j * NV + k) * nvc + r] = fr[j][k];
+		} else {
+#pragma unroll
+			for (int j = 0; j < D; ++j) {
+				double gb = 0.0;
+#pragma unroll
+				for (int i = 0; i < D; ++i)
+					gb += g[j * D + i] * P.b_adv[i];
+				sf[j * nvc + r] = gb * W[0];
+			}
+		}
+	}
+	__syncthreads();
+	// 2a: gx, gy[k][c][rt] = sum_rz L0[rz][c] f_x,y[k][rz][rt];  h[k][rz][t] = sum_rt T0[rt][t] f_z[k][rz][rt]
+	const int gsz = NV * nlv * ntc;
+	for (int it = threadIdx.x; it < n_here * gsz; it += blockDim.x) {
+		const int e = it / gsz, rem = it % gsz;
+		const int k = rem / (nlv * ntc), c = (rem / ntc) % nlv, rt = rem % ntc;
+		const double* sf = smem + e * PER_E + NV * nvs;
+		double* tmp = smem + e * PER_E + NV * nvs + 3 * NV * nvc;
+		double ax = 0.0, ay = 0.0;
+		for (int rz = 0; rz < nlc; ++rz) {
+			const double l = __ldg(L0 + rz * nlv + c);
+			ax += l * sf[(0 * NV + k) * nvc + rz * ntc + rt];
+			ay += l * sf[(1 * NV + k) * nvc + rz * ntc + rt];
+		}
+		tmp[rem] = ax;
+		tmp[gsz + rem] = ay;
+	}
+	const int hsz = NV * nlc * ntv;
+	for (int it = threadIdx.x; it < n_here * hsz; it += blockDim.x) {
+		const int e = it / hsz, rem = it % hsz;
+		const int k = rem / (nlc * ntv), rz = (rem / ntv) % nlc, t = rem % ntv;
+		const double* fz = smem + e * PER_E + NV * nvs + (2 * NV + k) * nvc + rz * ntc;
+		double* h = smem + e * PER_E + NV * nvs + 3 * NV * nvc + 2 * gsz;
+		double acc = 0.0;
+		for (int rt = 0; rt < ntc; ++rt)
+			acc += __ldg(T0 + (long long)rt * ntv + t) * fz[rt];
+		h[rem] = acc;
+	}
+	__syncthreads();
+	// 2b: vol[k][c][t] = sum_rt (T1x[rt][t] gx[k][c][rt] + T1y[rt][t] gy[k][c][rt]) + sum_rz L1[rz][c] h[k][rz][t]
+	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
+		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, c = (rem % nvs) / ntv, t = rem % ntv;
+		const double* tmp = smem + e * PER_E + NV * nvs + 3 * NV * nvc;
+		const double* gx = tmp + (k * nlv + c) * ntc;
+		const double* gy = gx + gsz;
+		const double* h = tmp + 2 * gsz + k * nlc * ntv + t;
+		double acc = 0.0;
+		for (int rt = 0; rt < ntc; ++rt)
+			acc += __ldg(T1 + (long long)rt * ntv + t) * gx[rt] + __ldg(T1 + (long long)(ntc + rt) * ntv + t) * gy[rt];
+		for (int rz = 0; rz < nlc; ++rz)
+			acc += __ldg(L1 + rz * nlv + c) * h[rz * ntv];
+		P.vol_gl[G.state_off + (long long)(e0 + e) * NV * nvs + rem] = acc;
+	}
+}
 
 // ---------------------------------------------------------------------------------------------------------------
 // Volume term (coefficient space) + face traces at the canonical face nodes
@@ -31,7 +173,7 @@ __device__ void dvol_body(const BParams& P, const DGroup& G, int e0, int E, cons
                           double* smem)
 {
 	const int nvs = G.n_vs, nvc = G.n_vc;
-	const int PER_E = DSmem::vol(NV, nvs, nvc);
+	const int PER_E = G.vol_per_e;
 	const int n_here = min(E, G.n_vol - e0);
 	const double* ublk = u + G.state_off + (long long)e0 * NV * nvs;
 	for (int i = threadIdx.x; i < n_here * NV * nvs; i += blockDim.x) {
@@ -39,6 +181,12 @@ __device__ void dvol_body(const BParams& P, const DGroup& G, int e0, int E, cons
 		smem[e * PER_E + r] = ublk[i];
 	}
 	__syncthreads();
+	if (G.prism) {
+		dvol_prism_phases<D, NV, PDE>(P, G, e0, n_here, smem, PER_E);
+		dtraces<NV>(P, G, e0, n_here, smem, PER_E);
+		__syncthreads();   // shared memory is reused by the next tile
+		return;
+	}
 	const double* __restrict__ cv0 = G.cv0;
 	// phase 1: state at the cubature nodes, contravariant flux, w-weighted (w is folded into the metrics)
 	for (int it = threadIdx.x; it < n_here * nvc; it += blockDim.x) {
@@ -96,32 +244,7 @@ __device__ void dvol_body(const BParams& P, const DGroup& G, int e0, int E, cons
 		}
 		P.vol_gl[G.state_off + (long long)(e0 + e) * NV * nvs + k * nvs + m] = acc;
 	}
-	// phase 3: traces at each face's canonical nodes
-	for (int it = threadIdx.x; it < n_here * G.n_lf * kQMax * kQMax; it += blockDim.x) {
-		const int i = it % (kQMax * kQMax), el = it / (kQMax * kQMax), lf = el % G.n_lf, e = el / G.n_lf;
-		const long long v = G.elem0 + e0 + e;
-		const int4 fd = P.elf[v * kMaxLf + lf];
-		const long long fb = P.fbase[fd.x];
-		const int nff = (int)(P.fbase[fd.x + 1] - fb);
-		if (i >= nff)
-			continue;
-		const double* op = G.fops + G.fop_off[(lf * G.n_ord + fd.w) * (kQMax + 1) + fd.z] + (long long)i * nvs;
-		const double* su = smem + e * PER_E;
-		double W[NV];
-#pragma unroll
-		for (int k = 0; k < NV; ++k)
-			W[k] = 0.0;
-		for (int m = 0; m < nvs; ++m) {
-			const double c = __ldg(op + m);
-#pragma unroll
-			for (int k = 0; k < NV; ++k)
-				W[k] += c * su[k * nvs + m];
-		}
-		double* dst = P.traces + 2 * NV * fb + (long long)fd.y * NV * nff;
-#pragma unroll
-		for (int k = 0; k < NV; ++k)
-			dst[k * nff + i] = W[k];
-	}
+	dtraces<NV>(P, G, e0, n_here, smem, PER_E);
 	__syncthreads();   // shared memory is reused by the next tile
 }
 
@@ -132,7 +255,7 @@ template <int NV, int MODE>
 __device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, const RkArgs& rk, double* smem)
 {
 	const int nvs = G.n_vs;
-	const int PER_E = DSmem::lift(NV, nvs);
+	const int PER_E = G.lift_per_e;
 	const int n_here = min(E, G.n_vol - e0);
 	// phase 1: rhs = vol - sum_lf sgn cv0_fc^T nnf
 	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
@@ -159,10 +282,15 @@ __device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, con
 	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
 		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
 		const double* sr = smem + e * PER_E + k * nvs;
-		const double* row = minv + (long long)m * nvs;
-		double R = 0.0;
-		for (int a = 0; a < nvs; ++a)
-			R += __ldg(row + a) * sr[a];
+		double R;
+		if (G.minv_identity) {
+			R = sr[m];
+		} else {
+			const double* row = minv + (long long)m * nvs;
+			R = 0.0;
+			for (int a = 0; a < nvs; ++a)
+				R += __ldg(row + a) * sr[a];
+		}
 		R *= G.inv_J[e0 + e];
 		const long long o = G.state_off + (long long)(e0 + e) * NV * nvs + rem;
 		if (MODE == kModeRhs || rk.want_max) {

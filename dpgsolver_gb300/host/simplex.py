@@ -314,6 +314,27 @@ def _raw_basis(e_type: int, p: int, x: np.ndarray):
     return V, G
 
 
+def _raw_tri(p: int, x: np.ndarray):
+    """P_a(x) P_b(y), a + b <= p, in the order of the WEDGE's inner index: values (n, m), gradients (2, n, m)."""
+    cols, gx, gy = [], [], []
+    for tot in range(p + 1):
+        for a in range(tot, -1, -1):
+            b = tot - a
+            (pa, da), (pb, db) = _leg(a, x[:, 0]), _leg(b, x[:, 1])
+            cols.append(pa * pb)
+            gx.append(da * pb)
+            gy.append(pa * db)
+    return np.stack(cols, axis=1), np.stack([np.stack(gx, axis=1), np.stack(gy, axis=1)])
+
+
+def _orthonormaliser(V: np.ndarray, w: np.ndarray) -> np.ndarray:
+    """C with (V C)^T diag(w) (V C) = I (QR, then one re-orthogonalisation pass)."""
+    _, R = np.linalg.qr(np.sqrt(w)[:, None] * V)
+    Cm = np.linalg.inv(R)
+    _, R2 = np.linalg.qr(np.sqrt(w)[:, None] * (V @ Cm))
+    return Cm @ np.linalg.inv(R2)
+
+
 def n_basis(e_type: int, p: int) -> int:
     if e_type == TET:
         return (p + 1) * (p + 2) * (p + 3) // 6
@@ -343,16 +364,21 @@ class DenseOperatorSet:
         self.n_vc = len(self.w_vc)
         self.n_lf = len(F_VE[e_type])
         self.normals_ref = reference_normals_3d(e_type)
-        # orthonormalise the spanning functions with a rule exact for their products
-        xg, wg = volume_rule(e_type, p + 2)
-        Vg, _ = _raw_basis(e_type, p, xg)
-        if Vg.shape[1] != self.n_vs:
-            raise AssertionError("basis dimension")
-        Q, R = np.linalg.qr(np.sqrt(wg)[:, None] * Vg)
-        Cm = np.linalg.inv(R)
-        # second pass (re-orthogonalisation) for the last ulps
-        Q2, R2 = np.linalg.qr(np.sqrt(wg)[:, None] * (Vg @ Cm))
-        self._C = Cm @ np.linalg.inv(R2)
+        if e_type == WEDGE:
+            # the product of an orthonormal TRI basis and the normalised Legendre polynomials, so that every
+            # volume operator is a Kronecker product (prism_factors)
+            xt, wt = tri_rule(p + 2)
+            Vt, _ = _raw_tri(p, xt)
+            self._Ct = _orthonormaliser(Vt, wt)
+            self._Cl = np.diag([math.sqrt(0.5 * (2 * c + 1)) for c in range(p + 1)])
+            self._C = np.kron(self._Cl, self._Ct)
+        else:
+            # orthonormalise the spanning functions with a rule exact for their products
+            xg, wg = volume_rule(e_type, p + 2)
+            Vg, _ = _raw_basis(e_type, p, xg)
+            if Vg.shape[1] != self.n_vs:
+                raise AssertionError("basis dimension")
+            self._C = _orthonormaliser(Vg, wg)
         self._cache = {}
         V, G = self.basis(self.x_vc)
         self._cv0 = V
@@ -361,6 +387,20 @@ class DenseOperatorSet:
     def basis(self, x):
         V, G = _raw_basis(self.e_type, self.p, np.asarray(x, dtype=np.float64))
         return V @ self._C, np.stack([G[k] @ self._C for k in range(3)])
+
+    def prism_factors(self):
+        """WEDGE only: (tri_cv0 (n_tvc x n_tvs), tri_cv1 (2 x n_tvc x n_tvs), line_cv0, line_cv1 (q x q)) with
+        cv0_vs_vc = kron(line_cv0, tri_cv0), cv1_vs_vc[0/1] = kron(line_cv0, tri_cv1[0/1]) and
+        cv1_vs_vc[2] = kron(line_cv1, tri_cv0) (basis index c * n_tvs + t, node index rz * n_tvc + rt)."""
+        if self.e_type != WEDGE:
+            raise ValueError("WEDGE only")
+        q = self.q
+        xt, _ = tri_rule(q)
+        Vt, Gt = _raw_tri(self.p, xt)
+        xz, _ = gauss_legendre(q)
+        Vl = np.stack([jacobi_p(c, 0.0, 0.0, xz) for c in range(q)], axis=1)
+        Dl = np.stack([jacobi_dp(c, 0.0, 0.0, xz) for c in range(q)], axis=1)
+        return (Vt @ self._Ct, np.stack([Gt[0] @ self._Ct, Gt[1] @ self._Ct]), Vl @ self._Cl, Dl @ self._Cl)
 
     def cv0_vs_vc(self):
         return self._cv0

@@ -200,7 +200,9 @@ class BatchSimulation:
     """One batched dgpu context for a mixed-order TP mesh (dpgsolver_gb300.host.mixed.MixedTPProblem, or a uniform
     DGProblem as a one-group mesh). States are flat arrays in volume-list order (the problem's layout)."""
 
-    def __init__(self, prob, stream=None):
+    def __init__(self, prob, stream=None, factorised: bool = True):
+        """factorised: pass the TRI x LINE factors of WEDGE groups (sum-factorised volume term); False runs every
+        TET/WEDGE/PYR group through the dense per-volume products."""
         from .host.problem import flat_arrays
 
         lib = _lib.load()
@@ -224,7 +226,7 @@ class BatchSimulation:
         dns = (_lib.DenseOperators * len(groups))()
         for g, ops in enumerate(groups):
             if getattr(ops, "dense", False):
-                self._dense_operators(dns[g], ops, arr, keep)
+                self._dense_operators(dns[g], ops, arr, keep, factorised)
                 continue
             tps[g].elem_type, tps[g].p = ops.e_type, ops.p
             tps[g].cv0_vs_vc = _dp(arr(ops.cv0_1d))
@@ -272,7 +274,7 @@ class BatchSimulation:
         self.upload_state(prob.sol)
 
     @staticmethod
-    def _dense_operators(D, ops, arr, keep):
+    def _dense_operators(D, ops, arr, keep, factorised=True):
         """Fill a DenseOperators struct from a DenseOperatorSet: volume operators and the face operator table for
         every local face, orientation and face order p_f >= p."""
         from .host import simplex as S
@@ -296,6 +298,12 @@ class BatchSimulation:
         D.cv0_vs_fc = cv0
         D.w_fc = w
         keep.extend([cv0, w])
+        if ops.e_type == S.WEDGE and factorised:
+            t0, t1, l0, l1 = ops.prism_factors()
+            D.n_tri_vs, D.n_tri_vc = t0.shape[1], t0.shape[0]
+            D.n_line_vs, D.n_line_vc = l0.shape[1], l0.shape[0]
+            D.tri_cv0, D.tri_cv1 = _dp(arr(t0)), _dp(arr(t1))
+            D.line_cv0, D.line_cv1 = _dp(arr(l0)), _dp(arr(l1))
 
     def _check(self, st):
         check(st, self._h, batch=True)

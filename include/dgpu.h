@@ -232,6 +232,15 @@ typedef struct {
 	const int* n_fc;
 	const double* const* cv0_vs_fc;
 	const double* const* w_fc;
+	/* Optional (WEDGE; NULL / 0 otherwise): the TRI x LINE factors of the volume operators, applied sum-factorised
+	 * (the reference keeps such factors in Operator::ops_tp, operator.h:40-44): with basis index c * n_tri_vs + t
+	 * and node index rz * n_tri_vc + rt, cv0_vs_vc = line_cv0 (x) tri_cv0, cv1_vs_vc[0/1] = line_cv0 (x)
+	 * tri_cv1[0/1], cv1_vs_vc[2] = line_cv1 (x) tri_cv0. Checked against the dense operators at creation. */
+	int n_tri_vs, n_tri_vc, n_line_vs, n_line_vc;
+	const double* tri_cv0;            /* n_tri_vc x n_tri_vs                                       */
+	const double* tri_cv1;            /* 2 x n_tri_vc x n_tri_vs                                   */
+	const double* line_cv0;           /* n_line_vc x n_line_vs                                     */
+	const double* line_cv1;           /* n_line_vc x n_line_vs                                     */
 } dgpu_dense_operators;
 
 /* One (type, p) group of a batched mesh: exactly one of tp / dense. */

@@ -269,3 +269,18 @@ def test_mixed_types_forms_and_tiles_agree_bitwise(gpu_lib):
     for r, s in out[1:]:
         assert np.array_equal(r, out[0][0])
         assert np.array_equal(s, out[0][1])
+
+
+def test_wedge_factorised_equals_dense(gpu_lib):
+    """The sum-factorised WEDGE volume term (TRI x LINE factors) gives the dense per-volume products' residual."""
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = TYPE_CASES["types_roe_6"]()
+    r_ref, _ = oracle.Oracle(prob).compute_rhs(prob.sol)
+    out = []
+    for fac in (True, False):
+        with BatchSimulation(prob, factorised=fac) as sim:
+            sim.compute_rhs()
+            out.append(sim.rhs)
+    assert rel_err(out[0], r_ref) <= TOL
+    assert rel_err(out[1], r_ref) <= TOL
+    assert rel_err(out[0], out[1]) <= 1e-13

@@ -154,12 +154,28 @@ def test_mixed_type_oracle_free_stream_and_conservation():
 
 
 def test_mixed_type_complex_step():
+    """Complex step = central differences on the mixed-type mesh. The additive perturbation (1e-2) keeps the two
+    traces of every face node apart, away from the kinks of the numerical fluxes (max of the two sides' wave
+    speeds, Roe's entropy fix), where the two linearisations legitimately differ."""
     prob = MT.mixed_types_euler(4, seed=1)
     o = oracle.Oracle(prob)
     rng = np.random.default_rng(2)
-    base = prob.sol + 1e-3 * rng.standard_normal(prob.sol.shape)
+    base = prob.sol + 1e-2 * rng.standard_normal(prob.sol.shape)
     dirn = rng.standard_normal(prob.sol.shape)
     _, ri = o.compute_rhs_cmplx(base, 1e-30 * dirn)
     eps = 1e-6
     fd = (o.compute_rhs(base + eps * dirn)[0] - o.compute_rhs(base - eps * dirn)[0]) / (2 * eps)
     assert np.max(np.abs(ri / 1e-30 - fd)) <= 1e-6 * np.max(np.abs(fd))
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_wedge_operators_are_kronecker_products(p):
+    """The WEDGE basis is the product of an orthonormal TRI basis and normalised Legendre polynomials, so its volume
+    operators are Kronecker products of the TRI and LINE factors (what the sum-factorised kernel applies)."""
+    o = S.DenseOperatorSet(WEDGE, p)
+    t0, t1, l0, l1 = o.prism_factors()
+    scale = max(np.abs(o.cv1_vs_vc(k)).max() for k in range(3))
+    assert np.abs(np.kron(l0, t0) - o.cv0_vs_vc()).max() <= 1e-13 * scale
+    assert np.abs(np.kron(l0, t1[0]) - o.cv1_vs_vc(0)).max() <= 1e-13 * scale
+    assert np.abs(np.kron(l0, t1[1]) - o.cv1_vs_vc(1)).max() <= 1e-13 * scale
+    assert np.abs(np.kron(l1, t0) - o.cv1_vs_vc(2)).max() <= 1e-13 * scale
