@@ -182,6 +182,20 @@ def algorithmic_bytes(prob, kernel):
     raise KeyError(kernel)
 
 
+# DRAM bytes per element of one tp_volume_kernel launch (GL state in) measured by ncu on curved HEX 24^3, p = 3,
+# 5 variables: 99.5 MB read + 42.4 MB written over 13,824 elements (writes stay below the algorithmic vol_gl +
+# traces because L2 holds part of them until the face kernel reads them).
+_VOLUME_DRAM_BYTES_PER_ELEMENT_HEX_P3 = (99.5e6 + 42.4e6) / 13824
+
+
+def volume_traffic(prob, kernel):
+    """Measured DRAM traffic per launch of the dominant kernel, where an ncu capture of the same kernel and order
+    exists (the curved HEX p = 3 Euler volume kernel); None otherwise."""
+    if kernel == "tp_volume_kernel" and prob.d == 3 and prob.ops.q == 4 and prob.n_var == 5:
+        return _VOLUME_DRAM_BYTES_PER_ELEMENT_HEX_P3 * prob.n_volumes
+    return None
+
+
 def eval_bytes(prob):
     """Algorithmic bytes of one residual evaluation: state read + residual written + metric terms and J at the
     cubature nodes + face normals x J_f (the compulsory traffic, reference-element operators excluded)."""
@@ -356,7 +370,10 @@ def run_ours(args, rank, world, local_rank):
                 "note": "per step: dgpu_upload_state + dgpu_ssp_rk3_step + dgpu_download_state from pinned memory"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": f"{peak_kind} (MEASURED_PEAKS hbm_gbs)",
+                     "frac": achieved / peak, "traffic": volume_traffic(prob, dom),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of tp_volume_kernel on the "
+                                       "24^3 p3 case (profiles/tp_rk3_stage_hex24_p3_lf_full.md), scaled per element",
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS hbm_gbs)",
                      "algorithmic_bytes_per_launch": ab, "kernel_ms": kt},
         "fp64_pipe": {"achieved_tflops": stage_flops / (stage_ms * 1e-3) / 1e12,
                       "peak_tflops": fp64_peak.value, "peak_source": "measured (dgpu_probe_fp64 DFMA loop)",
