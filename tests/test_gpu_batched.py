@@ -284,3 +284,82 @@ def test_wedge_factorised_equals_dense(gpu_lib):
     assert rel_err(out[0], r_ref) <= TOL
     assert rel_err(out[1], r_ref) <= TOL
     assert rel_err(out[0], out[1]) <= 1e-13
+
+
+# ---- argument checking of dgpu_batch_create_groups (host-side validation, before any kernel) ---------------------
+
+def _create_error(prob, **kw):
+    from dpgsolver_gb300.solver import BatchSimulation, DGPUError
+    with pytest.raises(DGPUError) as ei:
+        BatchSimulation(prob, **kw)
+    return ei.value
+
+
+def test_create_rejects_positivity_on_dense_groups(gpu_lib):
+    prob = TYPE_CASES["types_roe_4"]()
+    prob.positivity = True
+    e = _create_error(prob)
+    assert e.status == 2 and "positivity" in str(e)
+
+
+def test_create_rejects_non_affine_dense_volumes(gpu_lib):
+    prob = TYPE_CASES["types_roe_4"]()
+    flat = prob.flat
+
+    def bent():
+        fl = flat()
+        v = int(prob.group_vols[[getattr(o, "dense", False) for o in prob.groups].index(True)][0])
+        n_vc = np.array([prob.groups[g].n_vc for g in prob.vol_group])
+        off = int(np.sum(n_vc[:v]))
+        fl["jacobian_det_vc"] = fl["jacobian_det_vc"].copy()
+        fl["jacobian_det_vc"][off + 1] *= 1.01
+        return fl
+    prob.flat = bent
+    e = _create_error(prob)
+    assert e.status == 2 and "affine" in str(e)
+
+
+def test_create_rejects_bad_orientation(gpu_lib):
+    prob = TYPE_CASES["types_roe_4"]()
+    flat = prob.flat
+
+    def bad():
+        fl = flat()
+        fo = fl["face_ord"].copy()
+        hexes = np.nonzero(np.array([not getattr(prob.groups[g], "dense", False) for g in prob.vol_group]))[0]
+        f = int(np.nonzero(np.isin(prob.mesh.face_vol[:, 0], hexes))[0][0])
+        fo[f, 0] = 3                       # a HEX side must see its face unpermuted
+        fl["face_ord"] = fo
+        return fl
+    prob.flat = bad
+    e = _create_error(prob)
+    assert e.status == 2 and "face_ord 0" in str(e)
+    prob.flat = flat
+
+    def out_of_range():
+        fl = flat()
+        fo = fl["face_ord"].copy()
+        dense = np.nonzero(np.array([getattr(prob.groups[g], "dense", False) for g in prob.vol_group]))[0]
+        f = int(np.nonzero(np.isin(prob.mesh.face_vol[:, 1], dense))[0][0])
+        fo[f, 1] = 9
+        fl["face_ord"] = fo
+        return fl
+    prob.flat = out_of_range
+    e = _create_error(prob)
+    assert e.status == 1 and "face_ord" in str(e)
+
+
+def test_create_rejects_wedge_factors_that_do_not_match(gpu_lib):
+    prob = TYPE_CASES["types_roe_4"]()
+    from dpgsolver_gb300.host.element import WEDGE
+    g = [getattr(o, "e_type", None) for o in prob.groups].index(WEDGE)
+    ops = prob.groups[g]
+    good = ops.prism_factors
+
+    def scaled():
+        t0, t1, l0, l1 = good()
+        return t0 * 1.001, t1, l0, l1
+    ops.prism_factors = scaled
+    e = _create_error(prob)
+    assert e.status == 1 and "WEDGE factors" in str(e)
+    ops.prism_factors = good

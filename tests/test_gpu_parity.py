@@ -165,3 +165,22 @@ def test_state_round_trips_between_rk_and_residual(gpu_lib):
     assert abs(mx - mx_ref) <= 1e-10 * mx_ref
     assert rel_err(r, r_ref) <= TOL
     assert abs(rmx - rmx_ref) <= 1e-10 * rmx_ref
+
+
+def test_entropy_error_after_rk_steps_matches_oracle(gpu_lib):
+    """Config 2's reported quantity: the L2 entropy error (compute_error_euler.c:135-180) after SSP-RK3 steps of the
+    isentropic vortex, from the GPU state and from the oracle's."""
+    from dpgsolver_gb300.host.errors import l2_entropy_error
+    from dpgsolver_gb300.solver import Simulation
+    prob = P.euler_vortex_2d(16, 3)
+    ref = oracle.Oracle(prob)
+    s_ref = prob.sol.copy()
+    for _ in range(50):
+        s_ref, _, _ = ref.ssp_rk3_step(s_ref, prob.dt)
+    with Simulation(prob) as sim:
+        sim.ssp_rk3_steps(prob.dt, 50, want_max=False)
+        s = sim.sol_coef
+    e_gpu, e_ref = l2_entropy_error(prob, s), l2_entropy_error(prob, s_ref)
+    # the states agree to ~1e-13; the entropy error (~4e-5) is a norm of O(1)-cancelling log terms, so it carries
+    # that absolute agreement as ~1e-9 relative at most
+    assert abs(e_gpu - e_ref) <= 1e-7 * e_ref

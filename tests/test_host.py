@@ -68,3 +68,15 @@ def test_problem_sizes_match_workloads():
     a = P.advection_2d()
     assert a.n_state == 2304 and a.mesh.n_faces == 512
     assert abs(a.dt - 0.1 * 0.125 / np.hypot(1.0, 0.5)) < 1e-15
+
+
+def test_entropy_error_functional():
+    """compute_error_euler.c's entropy error: zero for an isentropic constant state, and at the interpolation-error
+    level for the projected isentropic vortex."""
+    from dpgsolver_gb300.host.errors import l2_entropy_error
+    prob = P.euler_vortex_2d(8, 3)
+    s = P.constant_state(prob, [1.3, 0.3, -0.2, 1.3 ** 1.4 / 0.4 + 0.5 * (0.3 ** 2 + 0.2 ** 2) / 1.3])
+    assert l2_entropy_error(prob, s) < 1e-14
+    e0 = l2_entropy_error(prob, prob.sol)
+    assert 0.0 < e0 < 1e-2
+    assert l2_entropy_error(P.euler_vortex_2d(16, 3), P.euler_vortex_2d(16, 3).sol) < e0
