@@ -411,6 +411,12 @@ def adjoint_measurements(torch, sim, prob, args):
     for _ in range(reps):
         sim.vjp_backward(v)
     vjp_s = (time.perf_counter() - t0) / reps
+    d = rng.standard_normal(prob.sol.shape)
+    sim.jvp(prob.sol, d)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sim.jvp(prob.sol, d)
+    jvp_s = (time.perf_counter() - t0) / reps
     sim.set_objective_faces(prob.faces_on_plane(2))
     n_adj = args.adjoint_steps
     budget = int(args.adjoint_budget_gb * 2**30)
@@ -420,6 +426,7 @@ def adjoint_measurements(torch, sim, prob, args):
     return {"vjp_backward_s": vjp_s,
             "vjp_dof_per_s": prob.n_state / vjp_s,
             "vjp_note": "host cotangent in, host gradient out (84 MB each way included)",
+            "jvp_s": jvp_s, "jvp_note": "dgpu_jvp: host state and direction in, R and (dR/du) d out (dual numbers)",
             "rk3_adjoint_steps": n_adj, "rk3_adjoint_s": adj_s, "segment_steps": K,
             "budget_bytes": budget, "J": J, "grad_norm": float(np.linalg.norm(g)),
             "note": "forward sweep with checkpoints, segment recomputation, stage recomputation, 3 VJPs per step"}

@@ -15,7 +15,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 LIB_PATH = os.path.join(PKG_DIR, "libdgpu.so")
 SOURCES = ["dgpu.cu", "dgpu_batched.cu"]
 HEADERS = ["dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
-           "dgpu_host_ops.h"]
+           "dgpu_dense.cuh", "dgpu_jvp.cuh", "dgpu_host_ops.h"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
               "-Xcompiler", "-fPIC"]
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
@@ -117,6 +117,7 @@ EXPORTS = {
                                         ctypes.POINTER(ctypes.c_longlong)]),
     "dgpu_probe_fp64": (ctypes.c_int, [ctypes.c_int, c_double_p]),
     "dgpu_vjp_forward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
+    "dgpu_jvp": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_vjp_backward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
     "dgpu_set_objective_faces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_int_p]),
     "dgpu_objective": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),

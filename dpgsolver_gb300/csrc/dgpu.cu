@@ -15,6 +15,7 @@
 #include "../../include/dgpu.h"
 #include "dgpu_tp.cuh"
 #include "dgpu_adjoint.cuh"
+#include "dgpu_jvp.cuh"
 #include "dgpu_host_ops.h"
 
 using namespace dgpu;
@@ -46,6 +47,8 @@ struct dgpu_ctx {
 	int* obj_faces = nullptr;             // faces of the objective J (side 0), see dgpu_set_objective_faces
 	int n_obj = 0;
 	double* obj_contrib = nullptr;        // per objective face node: w_f J_f p
+	// forward-mode linearisation (allocated on first use): tangent state, volume term, traces, face fluxes, product
+	double *jv_du = nullptr, *jv_vol = nullptr, *jv_traces = nullptr, *jv_nnf = nullptr, *jv_out = nullptr;
 	bool coef_valid = true, gl_valid = false;   // which of u / ug holds the current state
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
@@ -70,6 +73,7 @@ struct dgpu_ctx {
 	cudaError_t (*launch_convert)(dgpu_ctx*, bool to_gl) = nullptr;
 	cudaError_t (*launch_adjoint)(dgpu_ctx*, const double* u, const double* rbar, double* ubar) = nullptr;
 	cudaError_t (*launch_objective)(dgpu_ctx*, double* ubar) = nullptr;   // needs traces of the state
+	cudaError_t (*launch_jvp)(dgpu_ctx*) = nullptr;   // R(u) into rhs and (dR/du) jv_du into jv_out
 	// optional per-kernel timing (eager launches only)
 	bool timing = false;
 	std::vector<KernelTimer> timers;
@@ -324,11 +328,54 @@ cudaError_t launch_objective_t(dgpu_ctx* c, double* ubar)
 	return cudaGetLastError();
 }
 
+template <int D, int Q, int NV>
+size_t jvp_volume_smem_bytes()
+{
+	using S = TPShape<D, Q>;
+	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * 2 * TPSmem<D, Q, NV>::VOL * sizeof(double);
+}
+
+// R(u) and the directional derivative along jv_du: tangent-carrying volume and face kernels, then the residual-mode
+// lift on the primal buffers and on the tangent buffers (the lift is linear).
+template <int D, int Q, int NV, int PDE, int FLUX>
+cudaError_t launch_jvp_t(dgpu_ctx* c)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	const TPParams P = c->params();
+	TPParams Pd = P;
+	Pd.vol_gl = c->jv_vol;
+	Pd.traces = c->jv_traces;
+	Pd.nnf = c->jv_nnf;
+	Pd.max_bits = nullptr;
+	cudaError_t e = cudaMemsetAsync(c->max_bits, 0, sizeof(unsigned long long), c->stream);
+	if (e != cudaSuccess)
+		return e;
+	tp_jvp_volume_kernel<D, Q, NV, PDE><<<blocks, S::THREADS, jvp_volume_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, P, Pd, c->u, c->jv_du);
+	const long long nf = (long long)c->n_face * S::NF;
+	tp_jvp_face_kernel<D, Q, NV, PDE, FLUX><<<(unsigned)((nf + 255) / 256), 256, 0, c->stream>>>(P, Pd);
+	RkArgs rk;
+	rk.u = c->u;
+	rk.u0 = c->u0;
+	rk.rhs = c->rhs;
+	rk.dt = 0.0;
+	rk.stage = 0;
+	rk.positivity = 0;
+	rk.want_max = 1;
+	tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, P, rk);
+	rk.rhs = c->jv_out;
+	tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, Pd, rk);
+	c->launches += 4;
+	return cudaGetLastError();
+}
+
 template <int D, int Q, int NV, int PDE, int FLUX>
 cudaError_t bind(dgpu_ctx* c)
 {
 	c->launch_adjoint = launch_adjoint_t<D, Q, NV, PDE, FLUX>;
 	c->launch_objective = launch_objective_t<D, Q, NV>;
+	c->launch_jvp = launch_jvp_t<D, Q, NV, PDE, FLUX>;
 	c->launch_volume = launch_volume_t<D, Q, NV, PDE, true>;
 	c->launch_volume_gl = launch_volume_t<D, Q, NV, PDE, false>;
 	c->launch_face = launch_face_t<D, Q, NV, PDE, FLUX>;
@@ -352,6 +399,8 @@ cudaError_t bind(dgpu_ctx* c)
 	if ((e = cudaFuncSetAttribute(tp_adj_volume_kernel<D, Q, NV, PDE>, smem, (int)adj_volume_smem_bytes<D, Q, NV>())))
 		return e;
 	if ((e = cudaFuncSetAttribute(tp_adj_lift_kernel<D, Q, NV>, smem, (int)convert_smem_bytes<D, Q, NV>())))
+		return e;
+	if ((e = cudaFuncSetAttribute(tp_jvp_volume_kernel<D, Q, NV, PDE>, smem, (int)jvp_volume_smem_bytes<D, Q, NV>())))
 		return e;
 	return cudaFuncSetAttribute(tp_convert_kernel<D, Q, NV, false>, smem, (int)convert_smem_bytes<D, Q, NV>());
 }
@@ -389,7 +438,7 @@ void free_all(dgpu_ctx* c)
 		cudaEventDestroy(t.stop);
 	}
 	c->timers.clear();
-	void* ptrs[] = {c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
+	void* ptrs[] = {c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
 	                c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -1321,6 +1370,32 @@ dgpu_status ensure_adjoint_buffers(dgpu_ctx* c)
 }
 
 }  // namespace
+
+extern "C" dgpu_status dgpu_jvp(dgpu_ctx* c, const double* sol, const double* dir, double* rhs, double* jv)
+{
+	if (!c || !sol || !dir || !jv)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	const size_t ns = state_size(c);
+	const size_t nt = (size_t)c->n_face * 2 * c->nv * c->NF;
+	if (!c->jv_du) {
+		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_du, ns * sizeof(double)));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_vol, ns * sizeof(double)));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_out, ns * sizeof(double)));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_traces, nt * sizeof(double)));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_nnf, nt / 2 * sizeof(double)));
+	}
+	const size_t bytes = ns * sizeof(double);
+	DGPU_CUDA(c, cudaMemcpyAsync(c->u, sol, bytes, cudaMemcpyHostToDevice, c->stream));
+	DGPU_CUDA(c, cudaMemcpyAsync(c->jv_du, dir, bytes, cudaMemcpyHostToDevice, c->stream));
+	c->coef_valid = true;
+	c->gl_valid = false;
+	DGPU_CUDA(c, c->launch_jvp(c));
+	if (rhs)
+		DGPU_CUDA(c, cudaMemcpyAsync(rhs, c->rhs, bytes, cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaMemcpyAsync(jv, c->jv_out, bytes, cudaMemcpyDeviceToHost, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
 
 extern "C" dgpu_status dgpu_vjp_forward(dgpu_ctx* c, const double* sol, double* rhs, double* max_rhs)
 {

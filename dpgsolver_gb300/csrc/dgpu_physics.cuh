@@ -45,23 +45,23 @@ __device__ __forceinline__ T max_abs_real(const T& a, const T& b)
 // and g the metric terms (pre-multiplied by the cubature weight) of constructor_flux_ref_piece_T
 // (compute_rlhs_T.c:71-110). The contraction is regrouped through the contravariant velocity
 // U_j = sum_i g[j*D+i] u_i, which is the same sum with fewer FP64 operations.
-template <int D>
-__device__ __forceinline__ void euler_flux_ref(const double* W, const double* g, double (*fr)[D + 2])
+template <int D, typename T = double>
+__device__ __forceinline__ void euler_flux_ref(const T* W, const double* g, T (*fr)[D + 2])
 {
-	const double rho = W[0], E = W[D + 1];
-	const double rho_inv = 1.0 / rho;
-	double u[D];
-	double V2 = 0.0;
+	const T rho = W[0], E = W[D + 1];
+	const T rho_inv = 1.0 / rho;
+	T u[D];
+	T V2 = 0.0;
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
 		u[k] = rho_inv * W[1 + k];
 		V2 += u[k] * u[k];
 	}
-	const double p = kGm1 * (E - 0.5 * rho * V2);
-	const double Ep = E + p;
+	const T p = kGm1 * (E - 0.5 * rho * V2);
+	const T Ep = E + p;
 #pragma unroll
 	for (int j = 0; j < D; ++j) {
-		double U = 0.0;
+		T U = 0.0;
 #pragma unroll
 		for (int i = 0; i < D; ++i)
 			U += g[j * D + i] * u[i];

@@ -142,6 +142,17 @@ class Simulation:
         check(self._lib.dgpu_vjp_forward(self._h, _dp(s), _dp(r), ctypes.byref(mx)), self._h)
         return r, mx.value
 
+    def jvp(self, sol, direction):
+        """(R(sol), (dR/dsol) direction) by forward mode (dual numbers through the flux routines)."""
+        s = np.ascontiguousarray(sol, dtype=np.float64)
+        d = np.ascontiguousarray(direction, dtype=np.float64)
+        if s.shape != self.shape or d.shape != self.shape:
+            raise ValueError(f"state shape {s.shape} / {d.shape} != {self.shape}")
+        r = np.empty(self.shape)
+        jv = np.empty(self.shape)
+        check(self._lib.dgpu_jvp(self._h, _dp(s), _dp(d), _dp(r), _dp(jv)), self._h)
+        return r, jv
+
     def vjp_backward(self, cotangent):
         """(dR/dsol)^T cotangent at the state kept by vjp_forward."""
         v = np.ascontiguousarray(cotangent, dtype=np.float64)

@@ -146,6 +146,14 @@ dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const dgpu_tp_ope
 dgpu_status dgpu_vjp_forward(dgpu_ctx* ctx, const double* sol, double* rhs, double* max_rhs);
 dgpu_status dgpu_vjp_backward(dgpu_ctx* ctx, const double* cotangent, double* grad_sol);
 
+/* Forward-mode linearisation (the matrix-free Jacobian-vector product of an implicit solver): rhs = R(sol) (may be
+ * NULL) and jv = (dR/dsol) dir, host buffers in the state layout; the context's state becomes sol. The reference
+ * forms the same product by complex step (compute_lhs_cmplx_step_dg, src/testing/support/simulation/solvers/dg/
+ * test_support_solve_dg.c:83-110) and assembles the Jacobian itself for its implicit solver (compute_rlhs_dg,
+ * src/simulation/solvers/dg/solve_dg.c:138-145); here the flux routines run on dual numbers, which gives the
+ * product without a step size. Kinks of the fluxes take the derivative of the branch the value takes. */
+dgpu_status dgpu_jvp(dgpu_ctx* ctx, const double* sol, const double* dir, double* rhs, double* jv);
+
 /* Output functional for the adjoint: J(sol) = sum over the listed faces of the integral of pressure on side 0
  * (sum over face cubature nodes of w_fc J_fc p(W_L)), e.g. the faces of the plane z = 0. Euler only. The
  * reference computes such integrals as error functionals (src/simulation/test_case/compute_error/) but has no
