@@ -52,6 +52,9 @@ struct dgpu_ctx {
 	bool coef_valid = true, gl_valid = false;   // which of u / ug holds the current state
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
+	int n_bnd = 0;                        // boundary faces (face_vol[2f+1] < 0)
+	int *bnd = nullptr, *bc_code = nullptr;
+	double* bc_ext = nullptr;
 	double *traces = nullptr, *nnf = nullptr, *vol_gl = nullptr;
 	unsigned long long* max_bits = nullptr;
 	int* err_flag = nullptr;
@@ -98,6 +101,9 @@ struct dgpu_ctx {
 		P.max_bits = max_bits;
 		P.err_flag = err_flag;
 		P.n_corr = n_corr;
+		P.bnd = bnd;
+		P.bc_code = bc_code;
+		P.bc_ext = bc_ext;
 		return P;
 	}
 };
@@ -439,7 +445,7 @@ void free_all(dgpu_ctx* c)
 	}
 	c->timers.clear();
 	void* ptrs[] = {c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
-	                c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
+	                c->bnd, c->bc_code, c->bc_ext, c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
 			cudaFree(p);
@@ -658,25 +664,43 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		nc.assign(mesh->nc_fc, mesh->nc_fc + nF * NF);
 		nc_inv.assign(nF * NF, -1);
 	}
+	// boundary faces: side 1 absent; their BC code and exterior state, compacted to the boundary list
+	std::vector<int> bnd(nF, -1), bc_code;
+	std::vector<double> bc_ext;
 	for (size_t f = 0; f < nF; ++f) {
-		for (int s = 0; s < 2; ++s) {
+		const bool boundary = mesh->face_vol[2 * f + 1] < 0;
+		for (int s = 0; s < (boundary ? 1 : 2); ++s) {
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
-			if (v < 0) {
-				delete c;
-				return fail(nullptr, DGPU_ERR_UNSUPPORTED, "boundary faces are not supported (periodic meshes)");
-			}
-			if (v >= c->n_vol || lf < 0 || lf >= 2 * d || vol_face[(size_t)v * 2 * d + lf] != -1) {
+			if (v < 0 || v >= c->n_vol || lf < 0 || lf >= 2 * d || vol_face[(size_t)v * 2 * d + lf] != -1) {
 				delete c;
 				return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "bad face connectivity");
 			}
 			vol_face[(size_t)v * 2 * d + lf] = (int)(2 * f + s);
+		}
+		if (boundary) {
+			if (!mesh->bc_fc || !mesh->bc_state_fc) {
+				delete c;
+				return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "boundary faces need bc_fc and bc_state_fc");
+			}
+			const int code = mesh->bc_fc[f] % kBcStepSC;
+			if (code < 0 || (c->pde == DGPU_PDE_EULER ? !bc_is_euler(code) : !bc_is_advection_upwind(code))) {
+				delete c;
+				return fail(nullptr, DGPU_ERR_UNSUPPORTED,
+				            "BC code " + std::to_string(mesh->bc_fc[f]) + " is not provided for this pde");
+			}
+			bnd[f] = (int)bc_code.size();
+			bc_code.push_back(code);
+			const double* e = mesh->bc_state_fc + f * (size_t)NF * c->nv;
+			for (int k = 0; k < c->nv; ++k)
+				for (int i = 0; i < NF; ++i)
+					bc_ext.push_back(e[(size_t)i * c->nv + k]);
 		}
 		for (int i = 0; i < NF; ++i) {
 			for (int k = 0; k < d; ++k)
 				fgeo[(f * (d + 1) + k) * NF + i] = mesh->normals_fc[(f * NF + i) * d + k];
 			fgeo[(f * (d + 1) + d) * NF + i] = wf[i] * mesh->jacobian_det_fc[f * NF + i];
 		}
-		if (mesh->nc_fc) {
+		if (mesh->nc_fc && !boundary) {
 			for (int i = 0; i < NF; ++i) {
 				const int t = nc[f * NF + i];
 				if (t < 0 || t >= NF || nc_inv[f * NF + t] != -1) {
@@ -730,8 +754,18 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 	DG_TRY(upload(&c->fgeo, fgeo));
 	DG_TRY(upload(&c->vol_face, vol_face));
 	if (any_perm) {
+		for (size_t f = 0; f < nF; ++f)   // boundary faces: unused entries, kept a permutation
+			if (bnd[f] >= 0)
+				for (int i = 0; i < NF; ++i)
+					nc[f * NF + i] = nc_inv[f * NF + i] = i;
 		DG_TRY(upload(&c->nc, nc));
 		DG_TRY(upload(&c->nc_inv, nc_inv));
+	}
+	c->n_bnd = (int)bc_code.size();
+	if (c->n_bnd > 0) {
+		DG_TRY(upload(&c->bnd, bnd));
+		DG_TRY(upload(&c->bc_code, bc_code));
+		DG_TRY(upload(&c->bc_ext, bc_ext));
 	}
 	cudaError_t be = (d == 2 ? bind_q<2>(c) : bind_q<3>(c));
 	if (be != cudaSuccess) {
@@ -1195,6 +1229,8 @@ extern "C" dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const 
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL operator");
 	if (d_mesh->n_volumes < 1 || d_mesh->n_faces < 1)
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "empty mesh");
+	if (d_mesh->bc_fc || d_mesh->bc_state_fc)
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "boundary faces are not supported here (use dgpu_create)");
 	if (!is_device_pointer(d_sol) || !is_device_pointer(d_rhs) || !is_device_pointer(d_mesh->metrics_vc) ||
 	    !is_device_pointer(d_mesh->jacobian_det_vc) || !is_device_pointer(d_mesh->face_vol) ||
 	    !is_device_pointer(d_mesh->face_lf) || !is_device_pointer(d_mesh->normals_fc) ||

@@ -122,6 +122,33 @@ __device__ __forceinline__ void num_flux_vjp_side(const double* WL, const double
 	}
 }
 
+// (d/dW_L F*(W_L, W_b(W_L)))^T Fbar at a boundary face node, W_b the boundary value of its BC (the exterior state
+// is data and carries no derivative).
+template <int D, int NV, int FLUX>
+__device__ __forceinline__ void num_flux_vjp_boundary(const TPParams& P, int b, int i, int NF, const double* WL,
+                                                      const double* n, const double* Fbar, double* Wbar)
+{
+	Dual<NV> L[NV], R[NV], F[NV];
+#pragma unroll
+	for (int k = 0; k < NV; ++k) {
+		L[k] = Dual<NV>(WL[k]);
+		L[k].d[k] = 1.0;
+	}
+	boundary_value<D, NV, kEuler, Dual<NV>>(P, b, i, NF, L, n, R);
+	if constexpr (FLUX == kRoePike)
+		num_flux_roe_pike<D, Dual<NV>>(L, R, n, F);
+	else
+		num_flux_lax_friedrichs<D, Dual<NV>>(L, R, n, F);
+#pragma unroll
+	for (int k = 0; k < NV; ++k) {
+		double s = 0.0;
+#pragma unroll
+		for (int eq = 0; eq < NV; ++eq)
+			s += Fbar[eq] * F[eq].d[k];
+		Wbar[k] = s;
+	}
+}
+
 // ---------------------------------------------------------------------------------------------------------------
 template <int D, int Q, int NV, int PDE>
 __global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
@@ -256,14 +283,42 @@ tp_adj_face_kernel(const TPParams P, const AdjArgs A)
 	if (gid >= P.n_face * NF)
 		return;
 	const int f = gid / NF, i = gid % NF;
-	const int iR = P.nc ? P.nc[(size_t)f * NF + i] : i;
+	const int b = P.bnd ? P.bnd[f] : -1;
 	const double* tL = P.traces + (size_t)(2 * f) * NV * NF;
-	const double* tR = P.traces + (size_t)(2 * f + 1) * NV * NF;
 	const double* aL = A.atraces + (size_t)(2 * f) * NV * NF;
-	const double* aR = A.atraces + (size_t)(2 * f + 1) * NV * NF;
 	const double* fg = P.fgeo + (size_t)f * (D + 1) * NF;
 	double WL[NV], WR[NV], Fb[NV], n[D];
 	const double sc = fg[D * NF + i];
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		n[k] = fg[k * NF + i];
+	double* wL = A.wbar + (size_t)(2 * f) * NV * NF;
+	if (b >= 0) {
+		// boundary face: R_L -= E_L^T S F*(W_L, W_b(W_L)) only, so Fbar = -S E_L xbar_L
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			WL[k] = tL[k * NF + i];
+			Fb[k] = -sc * aL[k * NF + i];
+		}
+		if constexpr (PDE == kEuler) {
+			double WbL[NV];
+			num_flux_vjp_boundary<D, NV, FLUX>(P, b, i, NF, WL, n, Fb, WbL);
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				wL[k * NF + i] = WbL[k];
+		} else {
+			double b_dot_n = 0.0;
+#pragma unroll
+			for (int k = 0; k < D; ++k)
+				b_dot_n += P.b_adv[k] * n[k];
+			// outflow (b.n > 0): the flux is b.n u_L on either branch of the upwind flux; inflow: the exterior
+			wL[i] = b_dot_n > 0.0 ? b_dot_n * Fb[0] : 0.0;
+		}
+		return;
+	}
+	const int iR = P.nc ? P.nc[(size_t)f * NF + i] : i;
+	const double* tR = P.traces + (size_t)(2 * f + 1) * NV * NF;
+	const double* aR = A.atraces + (size_t)(2 * f + 1) * NV * NF;
 #pragma unroll
 	for (int k = 0; k < NV; ++k) {
 		WL[k] = tL[k * NF + i];
@@ -271,10 +326,6 @@ tp_adj_face_kernel(const TPParams P, const AdjArgs A)
 		// R_L -= E_L^T S F*, R_R += E_R^T S F* (right in its own node order): Fbar = S (E_R xbar_R - E_L xbar_L)
 		Fb[k] = sc * (aR[k * NF + iR] - aL[k * NF + i]);
 	}
-#pragma unroll
-	for (int k = 0; k < D; ++k)
-		n[k] = fg[k * NF + i];
-	double* wL = A.wbar + (size_t)(2 * f) * NV * NF;
 	double* wR = A.wbar + (size_t)(2 * f + 1) * NV * NF;
 	if constexpr (PDE == kEuler) {
 		double WbL[NV], WbR[NV];

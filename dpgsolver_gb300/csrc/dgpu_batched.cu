@@ -820,7 +820,7 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 		for (int s = 0; s < 2; ++s) {
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
 			if (v < 0)
-				return reject(DGPU_ERR_UNSUPPORTED, "boundary faces are not supported (periodic meshes)");
+				return reject(DGPU_ERR_UNSUPPORTED, "boundary faces are supported by dgpu_create only");
 			if (v >= nV || lf < 0 || lf >= type_faces(g_type[vg[v]]))
 				return reject(DGPU_ERR_INVALID_ARGUMENT, "bad face connectivity");
 			qf = std::max(qf, g_q[vg[v]]);

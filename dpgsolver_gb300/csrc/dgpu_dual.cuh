@@ -138,4 +138,17 @@ __device__ __forceinline__ Dual<K> sqrt(const Dual<K>& a)
 template <int K>
 __device__ __forceinline__ Dual<K> fabs(const Dual<K>& a) { return a.v < 0.0 ? -a : a; }
 
+// a^b for a constant exponent (the boundary values' pow_T): derivative b a^(b-1) = b a^b / a, for a > 0.
+template <int K>
+__device__ __forceinline__ Dual<K> pow(const Dual<K>& a, double b)
+{
+	Dual<K> r;
+	r.v = ::pow(a.v, b);
+	const double s = b * r.v / a.v;
+#pragma unroll
+	for (int k = 0; k < K; ++k)
+		r.d[k] = a.d[k] * s;
+	return r;
+}
+
 }  // namespace dgpu

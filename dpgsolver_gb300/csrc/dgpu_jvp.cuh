@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(256) tp_jvp_face_kernel(const TPParams P, cons
 	if (gid >= P.n_face * NF)
 		return;
 	const int f = gid / NF, i = gid % NF;
+	const int b = P.bnd ? P.bnd[f] : -1;
 	const int iR = P.nc ? P.nc[(size_t)f * NF + i] : i;
 	const size_t oL = (size_t)(2 * f) * NV * NF, oR = (size_t)(2 * f + 1) * NV * NF;
 	double n[D];
@@ -174,8 +175,15 @@ __global__ void __launch_bounds__(256) tp_jvp_face_kernel(const TPParams P, cons
 		for (int k = 0; k < NV; ++k) {
 			WL[k].v = P.traces[oL + k * NF + i];
 			WL[k].d[0] = Pd.traces[oL + k * NF + i];
-			WR[k].v = P.traces[oR + k * NF + iR];
-			WR[k].d[0] = Pd.traces[oR + k * NF + iR];
+		}
+		if (b < 0) {
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				WR[k].v = P.traces[oR + k * NF + iR];
+				WR[k].d[0] = Pd.traces[oR + k * NF + iR];
+			}
+		} else {
+			boundary_value<D, NV, PDE, Dual<1>>(P, b, i, NF, WL, n, WR);
 		}
 		if constexpr (FLUX == kRoePike)
 			num_flux_roe_pike<D, Dual<1>>(WL, WR, n, nF);
@@ -187,9 +195,22 @@ __global__ void __launch_bounds__(256) tp_jvp_face_kernel(const TPParams P, cons
 			dout[k * NF + i] = nF[k].d[0] * sc;
 		}
 	} else {
-		// upwind: linear in the traces, the branch set by b.n alone
-		out[i] = num_flux_upwind<D>(P.traces[oL + i], P.traces[oR + iR], n, P.b_adv) * sc;
-		dout[i] = num_flux_upwind<D>(Pd.traces[oL + i], Pd.traces[oR + iR], n, P.b_adv) * sc;
+		// upwind: linear in the traces, the branch set by b.n alone; the boundary value is the interior trace
+		// (derivative: its tangent) or the fixed exterior state (derivative 0)
+		double uR = 0.0, duR = 0.0;
+		if (b < 0) {
+			uR = P.traces[oR + iR];
+			duR = Pd.traces[oR + iR];
+		} else {
+			Dual<1> uL, r;
+			uL.v = P.traces[oL + i];
+			uL.d[0] = Pd.traces[oL + i];
+			boundary_value<D, NV, PDE, Dual<1>>(P, b, i, NF, &uL, n, &r);
+			uR = r.v;
+			duR = r.d[0];
+		}
+		out[i] = num_flux_upwind<D>(P.traces[oL + i], uR, n, P.b_adv) * sc;
+		dout[i] = num_flux_upwind<D>(Pd.traces[oL + i], duR, n, P.b_adv) * sc;
 	}
 }
 

@@ -15,6 +15,7 @@
 namespace dgpu {
 
 using ::fabs;
+using ::pow;
 using ::sqrt;
 
 constexpr double kGamma = 1.4;          // definitions_physics.h:23
@@ -173,6 +174,139 @@ __device__ __forceinline__ double num_flux_upwind(double uL, double uR, const do
 	for (int k = 0; k < D; ++k)
 		b_dot_n += b[k] * n[k];
 	return (b_dot_n > kEps ? b_dot_n * uL : b_dot_n * uR);
+}
+
+// ---- boundary values ----------------------------------------------------------------------------------------------
+// BC codes after taking them modulo BC_STEP_SC (definitions_bc.h:33-64); set_function_pointers_num_flux_bc_advection
+// and _euler (face_solver_T.c:203-275) select the boundary value by these.
+constexpr int kBcStepSC = 10000;
+enum BcCode { kBcRiemann = 101, kBcSlipWall = 102, kBcSupersonicIn = 105, kBcSupersonicOut = 106 };
+
+// True for the advection codes that take the upwind boundary value (inflow 1-3, outflow 11-13, upwind 41-46).
+__host__ __device__ __forceinline__ bool bc_is_advection_upwind(int bc)
+{
+	return (bc >= 1 && bc <= 3) || (bc >= 11 && bc <= 13) || (bc >= 41 && bc <= 46);
+}
+__host__ __device__ __forceinline__ bool bc_is_euler(int bc)
+{
+	return bc == kBcRiemann || bc == kBcSlipWall || bc == kBcSupersonicIn || bc == kBcSupersonicOut;
+}
+
+// Exterior state WR of an Euler boundary face node from the interior trace WL, the test case's solution at the node
+// (ext, conserved: constructor_sol_bv) and the unit normal n (outward from the interior volume). bc is already
+// reduced modulo kBcStepSC and is one of the four codes (the context validates them on creation).
+//   kBcRiemann       constructor_Boundary_Value_T_euler_riemann (boundary_euler_T.c:99-180): the outgoing
+//                    invariant Vn + 2c/(gamma-1) of the interior and the incoming one of the exterior give the
+//                    normal velocity and speed of sound; entropy and tangential velocity come from the upwind side;
+//                    supersonic faces take the upwind state whole;
+//   kBcSlipWall      ..._euler_slipwall (:494-533): density and energy kept, momentum mirrored about the face;
+//   kBcSupersonicIn  ..._euler_supersonic_inflow (:657-692): the exterior state;
+//   kBcSupersonicOut ..._euler_supersonic_outflow (:705-745): the interior state.
+template <int D, typename T>
+__device__ __forceinline__ void euler_boundary_state(int bc, const T* WL, const double* ext, const double* n, T* WR)
+{
+	constexpr int NV = D + 2;
+	if (bc == kBcSlipWall) {
+		T rhoVn = 0.0;
+#pragma unroll
+		for (int k = 0; k < D; ++k)
+			rhoVn += n[k] * WL[1 + k];
+		WR[0] = WL[0];
+#pragma unroll
+		for (int k = 0; k < D; ++k)
+			WR[1 + k] = WL[1 + k] - 2.0 * rhoVn * n[k];
+		WR[D + 1] = WL[D + 1];
+		return;
+	}
+	if (bc == kBcSupersonicIn) {
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			WR[k] = ext[k];
+		return;
+	}
+	if (bc != kBcRiemann) {   // supersonic outflow
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			WR[k] = WL[k];
+		return;
+	}
+	// Riemann: primitive variables of both sides
+	const T rho_l = WL[0], rho_l_inv = 1.0 / rho_l;
+	T u_l[D], V2_l = 0.0, Vn_l = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		u_l[k] = WL[1 + k] * rho_l_inv;
+		V2_l += u_l[k] * u_l[k];
+		Vn_l += n[k] * u_l[k];
+	}
+	const T p_l = kGm1 * (WL[D + 1] - 0.5 * rho_l * V2_l);
+	const double rho_r = ext[0];
+	double u_r[D], V2_r = 0.0, Vn_r = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		u_r[k] = ext[1 + k] / rho_r;
+		V2_r += u_r[k] * u_r[k];
+		Vn_r += n[k] * u_r[k];
+	}
+	const double p_r = kGm1 * (ext[D + 1] - 0.5 * rho_r * V2_r);
+	const T c_l = sqrt(kGamma * p_l * rho_l_inv);
+	const double c_r = ::sqrt(kGamma * p_r / rho_r);
+	const T R_l = Vn_l + (2.0 / kGm1) * c_l;   // outgoing
+	const T R_r = Vn_r - (2.0 / kGm1) * c_r;   // incoming
+	const T Vn = 0.5 * (R_l + R_r), cc = 0.25 * kGm1 * (R_l - R_r);
+	T rho, p, uvw[D];
+	if (!(fabs(Vn) < fabs(cc))) {   // supersonic: the upwind side's state
+		if (Vn < 0.0) {
+			rho = rho_r;
+			p = p_r;
+#pragma unroll
+			for (int k = 0; k < D; ++k)
+				uvw[k] = u_r[k];
+		} else {
+			rho = rho_l;
+			p = p_l;
+#pragma unroll
+			for (int k = 0; k < D; ++k)
+				uvw[k] = u_l[k];
+		}
+	} else {                        // subsonic: entropy and tangential velocity from the upwind side
+		const T c2g = (1.0 / kGamma) * cc * cc;
+		if (Vn < 0.0) {
+			const double s_r = p_r / ::pow(rho_r, kGamma);
+			rho = pow(c2g / s_r, 1.0 / kGm1);
+#pragma unroll
+			for (int k = 0; k < D; ++k)
+				uvw[k] = Vn * n[k] + (u_r[k] - Vn_r * n[k]);
+		} else {
+			const T s_l = p_l / pow(rho_l, kGamma);
+			rho = pow(c2g / s_l, 1.0 / kGm1);
+#pragma unroll
+			for (int k = 0; k < D; ++k)
+				uvw[k] = Vn * n[k] + (u_l[k] - Vn_l * n[k]);
+		}
+		p = c2g * rho;
+	}
+	T V2 = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		V2 += uvw[k] * uvw[k];
+	WR[0] = rho;
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		WR[1 + k] = rho * uvw[k];
+	WR[D + 1] = p * (1.0 / kGm1) + 0.5 * rho * V2;
+}
+
+// Exterior value of an advection boundary node (constructor_Boundary_Value_T_advection_upwind,
+// boundary_advection_T.c:40-77): the exterior solution where b.n <= 0 (inflow), else the interior trace.
+template <int D, typename T>
+__device__ __forceinline__ T advection_boundary_value(const T& uL, double ext, const double* n, const double* b)
+{
+	double b_dot_n = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		b_dot_n += b[k] * n[k];
+	return b_dot_n <= 0.0 ? T(ext) : uL;
 }
 
 }  // namespace dgpu

@@ -63,7 +63,28 @@ struct TPParams {
 	unsigned long long* max_bits;  // max |rhs| as the bit pattern of a non-negative double
 	int* err_flag;             // positivity failure flag
 	unsigned long long* n_corr;    // positivity corrections applied
+	// Boundary faces (no side-1 volume), or all three nullptr on a mesh without any:
+	const int* bnd;            // [f] index b of the face in the boundary list, -1 for an interior face
+	const int* bc_code;        // [b] BC code modulo BC_STEP_SC
+	const double* bc_ext;      // [b][NV][NF] exterior (test case) conserved state at the face nodes
 };
+
+// Right-hand state of face node i of boundary face b: the boundary value of its BC from the interior trace WL.
+template <int D, int NV, int PDE, typename T>
+__device__ __forceinline__ void boundary_value(const TPParams& P, int b, int i, int NF, const T* WL, const double* n,
+                                               T* WR)
+{
+	const double* ext = P.bc_ext + (size_t)b * NV * NF;
+	if constexpr (PDE == kEuler) {
+		double e[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			e[k] = ext[k * NF + i];
+		euler_boundary_state<D, T>(P.bc_code[b], WL, e, n, WR);
+	} else {
+		WR[0] = advection_boundary_value<D, T>(WL[0], ext[i], n, P.b_adv);
+	}
+}
 
 template <int D, int Q>
 struct TPShape {
@@ -295,19 +316,25 @@ tp_face_kernel(const TPParams P)
 	if (gid >= P.n_face * NF)
 		return;
 	const int f = gid / NF, i = gid % NF;
-	const int iR = P.nc ? P.nc[(size_t)f * NF + i] : i;
+	const int b = P.bnd ? P.bnd[f] : -1;
 	const double* tL = P.traces + (size_t)(2 * f) * NV * NF;
-	const double* tR = P.traces + (size_t)(2 * f + 1) * NV * NF;
 	double WL[NV], WR[NV], n[D];
 #pragma unroll
-	for (int k = 0; k < NV; ++k) {
+	for (int k = 0; k < NV; ++k)
 		WL[k] = tL[k * NF + i];
-		WR[k] = tR[k * NF + iR];
-	}
 	const double* fg = P.fgeo + (size_t)f * (D + 1) * NF;
 #pragma unroll
 	for (int k = 0; k < D; ++k)
 		n[k] = fg[k * NF + i];
+	if (b < 0) {
+		const int iR = P.nc ? P.nc[(size_t)f * NF + i] : i;
+		const double* tR = P.traces + (size_t)(2 * f + 1) * NV * NF;
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			WR[k] = tR[k * NF + iR];
+	} else {
+		boundary_value<D, NV, PDE, double>(P, b, i, NF, WL, n, WR);
+	}
 	const double sc = fg[D * NF + i];
 	double* out = P.nnf + (size_t)f * NV * NF;
 	if constexpr (PDE == kEuler) {

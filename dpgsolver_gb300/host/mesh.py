@@ -1,4 +1,4 @@
-"""Structured periodic QUAD/HEX meshes and the reference's face list.
+"""Structured QUAD/HEX meshes (periodic, or bounded in chosen directions) and the reference's face list.
 
 The reference reads gmsh files and builds its connectivity in src/simulation/mesh; the
 face list itself is built by computational_elements/face.c:86-160: volumes are visited in
@@ -19,7 +19,8 @@ from .element import QUAD, HEX
 
 
 class StructuredMesh:
-    """Periodic n_x x n_y (x n_z) mesh of [lo, hi]^d.
+    """n_x x n_y (x n_z) mesh of [lo, hi]^d, periodic in the directions `periodic` selects (all by default); the
+    ends of the other directions are boundary faces with face_vol[f, 1] = face_lf[f, 1] = -1.
 
     Attributes
     ----------
@@ -33,7 +34,7 @@ class StructuredMesh:
     vol_side : (n_volumes, 2d) which side (0/1) the volume is on for that face
     """
 
-    def __init__(self, d: int, n, lo, hi):
+    def __init__(self, d: int, n, lo, hi, periodic=True):
         if d not in (2, 3):
             raise ValueError("d must be 2 or 3")
         n = [int(v) for v in (n if np.ndim(n) else [n] * d)]
@@ -57,6 +58,8 @@ class StructuredMesh:
         self.ijk = np.stack(ijk, axis=1)
         self.vertices_lo = lo[None, :] + self.ijk * self.h[None, :]
 
+        per = [bool(x) for x in (periodic if np.ndim(periodic) else [periodic] * d)]
+        self.periodic = per
         n_lf = 2 * d
         vol_faces = -np.ones((nv, n_lf), dtype=np.int64)
         vol_side = -np.ones((nv, n_lf), dtype=np.int64)
@@ -67,7 +70,16 @@ class StructuredMesh:
                     continue
                 dim, side = lf // 2, lf % 2
                 nb = self.ijk[v].copy()
-                nb[dim] = (nb[dim] + (1 if side == 1 else -1)) % n[dim]
+                step = nb[dim] + (1 if side == 1 else -1)
+                if not per[dim] and (step < 0 or step >= n[dim]):
+                    # boundary face: the volume is side 0, no side 1 (face.c:86-160 for a face with one neighbour)
+                    f = len(face_vol)
+                    face_vol.append((v, -1))
+                    face_lf.append((lf, -1))
+                    vol_faces[v, lf] = f
+                    vol_side[v, lf] = 0
+                    continue
+                nb[dim] = step % n[dim]
                 vn = self._index(nb)
                 lf_n = lf ^ 1
                 f = len(face_vol)

@@ -46,6 +46,8 @@ class DGProblem:
     dt: float
     n_steps: int
     meta: dict = field(default_factory=dict)
+    bc: np.ndarray | None = None          # (n_faces,) BC code of each face (definitions_bc.h), 0 on interior faces
+    bc_state: np.ndarray | None = None    # (n_faces, n_fc, n_var) exterior conserved state at the face nodes
 
     @property
     def n_var(self) -> int:
@@ -93,6 +95,8 @@ def flat_arrays(prob) -> dict:
         "jacobian_det_fc": np.ascontiguousarray(g.jacobian_det_fc).ravel(),
         "nc_fc": prob.nc_fc().ravel(),
         "sol": np.ascontiguousarray(prob.sol).ravel(),
+        "bc_fc": None if prob.bc is None else np.ascontiguousarray(prob.bc, dtype=np.int32),
+        "bc_state_fc": None if prob.bc_state is None else np.ascontiguousarray(prob.bc_state).ravel(),
     }
 
 
@@ -192,3 +196,116 @@ def constant_state(prob: DGProblem, values) -> np.ndarray:
     for k, val in enumerate(values):
         s[:, k, :] = val
     return s
+
+
+# ---- bounded domains: the reference's BC codes (test_case/boundary/definitions_bc.h) ----------------------------
+BC_UPWIND = 41
+BC_RIEMANN = 101
+BC_SLIPWALL = 102
+BC_SUPERSONIC_IN = 105
+BC_SUPERSONIC_OUT = 106
+
+
+def _set_boundaries(prob: DGProblem, side_bc: dict, exterior) -> DGProblem:
+    """bc per face from {(dim, side): code} and the exterior state exterior(xyz (m, d)) -> (m, n_var) at every face
+    node (the test case's constructor_sol_bv)."""
+    mesh = prob.mesh
+    bc = np.zeros(mesh.n_faces, dtype=np.int32)
+    bnd = np.nonzero(mesh.face_vol[:, 1] < 0)[0]
+    for f in bnd:
+        lf = int(mesh.face_lf[f, 0])
+        bc[f] = side_bc[(lf // 2, lf % 2)]
+    xyz = prob.geom.xyz_fc                                   # (n_faces, n_fc, d)
+    ext = exterior(xyz.reshape(-1, prob.d)).reshape(mesh.n_faces, -1, prob.n_var)
+    ext[mesh.face_vol[:, 1] >= 0] = 0.0
+    prob.bc, prob.bc_state = bc, np.ascontiguousarray(ext)
+    return prob
+
+
+def _uniform_flow(d, rho, vel, p):
+    def f(x):
+        vv = np.broadcast_to(np.asarray(vel, dtype=np.float64)[:, None], (d, len(x)))
+        U = primitive_to_conserved(d, np.full(len(x), rho), vv, np.full(len(x), p))
+        return U.T
+    return f
+
+
+def euler_channel_2d(n: int = 8, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, amplitude: float = 0.05) -> DGProblem:
+    """The curved isentropic-vortex mesh and state of euler_vortex_2d, periodic in x and bounded in y by slip walls
+    (BC_SLIPWALL); the walls stay straight under the sinusoidal mapping."""
+    L = 10.0
+    mesh = StructuredMesh(2, n, 0.0, L, periodic=(True, False))
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_2d(amplitude, L), curved=True)
+    prob = DGProblem("euler_channel_2d", 2, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, 4, ops.n_vs)), dt=0.0, n_steps=100)
+    xyz = prob.solution_node_xyz()
+    rho, u, v, pr = isentropic_vortex(xyz, 5.0, 5.0, 5.0)
+    prob.sol = _pack_state(primitive_to_conserved(2, rho, np.stack([u, v]), pr))
+    prob.dt = stable_dt(prob)
+    return _set_boundaries(prob, {(1, 0): BC_SLIPWALL, (1, 1): BC_SLIPWALL}, _uniform_flow(2, 1.0, (1.0, 1.0), 1.0))
+
+
+def euler_riemann_2d(n: int = 8, p: int = 3, num_flux: int = NUM_FLUX_LAX_FRIEDRICHS,
+                     amplitude: float = 0.05) -> DGProblem:
+    """The vortex mesh and state with characteristic (BC_RIEMANN) boundaries on all four sides, the exterior being
+    the free stream (rho, u, v, p) = (1, 1, 1, 1)."""
+    L = 10.0
+    mesh = StructuredMesh(2, n, 0.0, L, periodic=(False, False))
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_2d(amplitude, L), curved=True)
+    prob = DGProblem("euler_riemann_2d", 2, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, 4, ops.n_vs)), dt=0.0, n_steps=100)
+    xyz = prob.solution_node_xyz()
+    rho, u, v, pr = isentropic_vortex(xyz, 5.0, 5.0, 5.0)
+    prob.sol = _pack_state(primitive_to_conserved(2, rho, np.stack([u, v]), pr))
+    prob.dt = stable_dt(prob)
+    sides = {(dd, s): BC_RIEMANN for dd in range(2) for s in range(2)}
+    return _set_boundaries(prob, sides, _uniform_flow(2, 1.0, (1.0, 1.0), 1.0))
+
+
+def euler_duct_3d(n: int = 4, p: int = 2, num_flux: int = NUM_FLUX_ROE_PIKE, amplitude: float = 0.03,
+                  mach: float = 2.0, seed: int = 0, perturb: float = 0.02) -> DGProblem:
+    """Curved HEX box [0,10]^3 with a Mach `mach` stream along x: supersonic inflow at x = 0 (BC_SUPERSONIC_IN),
+    supersonic outflow at x = 10 (BC_SUPERSONIC_OUT), slip walls in y (BC_SLIPWALL), characteristic boundaries in z
+    (BC_RIEMANN); the state is the stream with seeded smooth perturbations."""
+    L = 10.0
+    mesh = StructuredMesh(3, n, 0.0, L, periodic=(False, False, False))
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_3d(amplitude, L), curved=True)
+    prob = DGProblem("euler_duct_3d", 3, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, 5, ops.n_vs)), dt=0.0, n_steps=100)
+    xyz = prob.solution_node_xyz()
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0.0, 2.0 * math.pi, size=(5, 3))
+
+    def wave(k):
+        s = np.ones(xyz.shape[:2])
+        for j in range(3):
+            s = s * np.sin(2.0 * math.pi * xyz[..., j] / L + ph[k, j])
+        return s
+    u0 = mach * math.sqrt(GAMMA)
+    vel = np.stack([u0 * (1.0 + perturb * wave(2)), u0 * perturb * wave(3), u0 * perturb * wave(4)])
+    prob.sol = _pack_state(primitive_to_conserved(3, 1.0 + perturb * wave(0), vel, 1.0 + perturb * wave(1)))
+    prob.dt = stable_dt(prob)
+    sides = {(0, 0): BC_SUPERSONIC_IN, (0, 1): BC_SUPERSONIC_OUT, (1, 0): BC_SLIPWALL, (1, 1): BC_SLIPWALL,
+             (2, 0): BC_RIEMANN, (2, 1): BC_RIEMANN}
+    return _set_boundaries(prob, sides, _uniform_flow(3, 1.0, (u0, 0.0, 0.0), 1.0))
+
+
+def advection_box_2d(n: int = 8, p: int = 2, b=(1.0, 0.5)) -> DGProblem:
+    """advection_2d's state on [-1,1]^2 without periodicity: upwind boundaries (BC_UPWIND) whose exterior state is
+    the initial solution sin(pi x) sin(pi y) at the face nodes (inflow sides take it, outflow sides the interior)."""
+    mesh = StructuredMesh(2, n, -1.0, 1.0, periodic=(False, False))
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops)
+    prob = DGProblem("advection_box_2d", 2, PDE_ADVECTION, NUM_FLUX_UPWIND, False, np.array([b[0], b[1], 0.0]), ops,
+                     mesh, geom, sol=np.zeros((mesh.n_volumes, 1, ops.n_vs)), dt=0.0, n_steps=100)
+    xyz = prob.solution_node_xyz()
+    prob.sol = (np.sin(np.pi * xyz[..., 0]) * np.sin(np.pi * xyz[..., 1]))[:, None, :]
+    prob.dt = 0.1 * float(np.min(mesh.h)) / ((2 * p + 1) * float(np.hypot(*b)))
+
+    def ext(x):
+        return (np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1]))[:, None]
+    sides = {(dd, s): BC_UPWIND for dd in range(2) for s in range(2)}
+    return _set_boundaries(prob, sides, ext)

@@ -64,6 +64,11 @@ class Simulation:
         m.nc_fc = _ip(arr("nc", nc, np.int32))
         m.normals_fc = _dp(arr("nrm", geom.normals_fc))
         m.jacobian_det_fc = _dp(arr("Jf", geom.jacobian_det_fc))
+        if getattr(prob, "bc", None) is not None:
+            if np.size(prob.bc) != mesh.n_faces or np.size(prob.bc_state) != mesh.n_faces * ops.n_fc * prob.n_var:
+                raise ValueError("bc needs one code per face and bc_state (n_faces, n_fc, n_var) values")
+            m.bc_fc = _ip(arr("bc", prob.bc, np.int32))
+            m.bc_state_fc = _dp(arr("bcs", prob.bc_state))
         h = ctypes.c_void_p()
         st = lib.dgpu_create(ctypes.byref(phys), ctypes.byref(tp), ctypes.byref(m), ctypes.byref(h))
         check(st, None)

@@ -40,6 +40,7 @@ class _Problem(ctypes.Structure):
         ("jacobian_det_vc", _c_double_p),
         ("n_faces", ctypes.c_int), ("face_vol", _c_int_p), ("face_lf", _c_int_p), ("face_ops_idx", _c_int_p),
         ("nc_fc", _c_int_p), ("normals_fc", _c_double_p), ("jacobian_det_fc", _c_double_p),
+        ("bc_fc", _c_int_p), ("bc_state_fc", _c_double_p),
     ]
 
 
@@ -125,7 +126,8 @@ class Oracle:
         for f in range(mesh.n_faces):
             for s in range(2):
                 o = int(face_ord[f, s]) if face_ord is not None else 0
-                key = (int(vol_group[mesh.face_vol[f, s]]), int(face_q[f]), o)
+                v = mesh.face_vol[f, s] if mesh.face_vol[f, s] >= 0 else mesh.face_vol[f, 0]   # boundary: unused
+                key = (int(vol_group[v]), int(face_q[f]), o)
                 if key not in pairs:
                     pairs[key] = len(pairs)
                 idx[f, s] = pairs[key]
@@ -169,6 +171,12 @@ class Oracle:
         P.nc_fc = _ip(arr(fl["nc_fc"], np.int32))
         P.normals_fc = _dp(arr(fl["normals_fc"]))
         P.jacobian_det_fc = _dp(arr(fl["jacobian_det_fc"]))
+        if fl.get("bc_fc") is not None:
+            n_fc_total = int(sum(FO[idx[f, 0]].n_fc for f in range(mesh.n_faces)))
+            if np.size(fl["bc_fc"]) != mesh.n_faces or np.size(fl["bc_state_fc"]) != n_fc_total * prob.n_var:
+                raise ValueError("bc_fc needs one code per face and bc_state_fc n_var values per face node")
+            P.bc_fc = _ip(arr(fl["bc_fc"], np.int32))
+            P.bc_state_fc = _dp(arr(fl["bc_state_fc"]))
         self._keep = (keep, G, FO, P)
         h = ctypes.c_void_p()
         st = lib.oracle_create(ctypes.byref(P), ctypes.byref(h))

@@ -42,12 +42,14 @@ struct oracle_ctx {
 #define REAL_T(x) (x)
 #define ABS_T(x) fabs(x)
 #define SQRT_T(x) sqrt(x)
+#define POW_T(x, y) pow(x, y)
 #include "dg_oracle_T.h"
 #undef Type
 #undef SUF
 #undef REAL_T
 #undef ABS_T
 #undef SQRT_T
+#undef POW_T
 
 /* ---- double complex instantiation ---- */
 #define Type double complex
@@ -55,12 +57,14 @@ struct oracle_ctx {
 #define REAL_T(x) creal(x)
 #define ABS_T(x) cabs(x)
 #define SQRT_T(x) csqrt(x)
+#define POW_T(x, y) cpow(x, y)
 #include "dg_oracle_T.h"
 #undef Type
 #undef SUF
 #undef REAL_T
 #undef ABS_T
 #undef SQRT_T
+#undef POW_T
 
 /* Inverse by Gauss-Jordan elimination with partial pivoting (the reference solves with the identity as
  * right-hand side through LAPACKE, matrix_constructors_T.c constructor_inverse_const_Matrix_T). */
@@ -151,7 +155,8 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 	for (size_t f = 0; f < nF; ++f) {
 		const struct oracle_face_ops* FL = &in->face_ops[in->face_ops_idx[2 * f]];
 		const struct oracle_face_ops* FR = &in->face_ops[in->face_ops_idx[2 * f + 1]];
-		if (FL->n_fc != FR->n_fc) {
+		const int boundary = in->face_vol[2 * f + 1] < 0;
+		if ((!boundary && FL->n_fc != FR->n_fc) || (boundary && (!in->bc_fc || !in->bc_state_fc))) {
 			oracle_destroy(c);
 			return ORACLE_ERR_ARG;
 		}

@@ -57,6 +57,11 @@ struct oracle_problem {
 	const int* nc_fc;              /* per face n_fc: right trace gathered as sR[i] = sR_own[nc_fc[i]] */
 	const double* normals_fc;      /* per face (n_fc x d) row-major */
 	const double* jacobian_det_fc; /* per face n_fc */
+	/* Boundary faces have face_vol[2f+1] < 0. bc_fc: per face the reference's BC code (definitions_bc.h; 0 or any
+	 * value on interior faces); bc_state_fc: per face (n_fc x n_var) row-major exterior conserved state
+	 * (constructor_sol_bv at the face nodes). Both may be NULL on meshes without boundary faces. */
+	const int* bc_fc;
+	const double* bc_state_fc;
 };
 
 struct oracle_ctx;

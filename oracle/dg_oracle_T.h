@@ -41,6 +41,123 @@ static void SUF(mm_acc)(const int m, const int k, const int nc, const double alp
 	}
 }
 
+/* Exterior ("right") state of a boundary face node from the interior state WL, the exterior state ext (the test
+ * case's solution at the node, constructor_sol_bv) and the unit normal, by BC code (definitions_bc.h):
+ *   BC_RIEMANN 101         constructor_Boundary_Value_T_euler_riemann        (boundary_euler_T.c:99-290)
+ *   BC_SLIPWALL 102        constructor_Boundary_Value_T_euler_slipwall       (boundary_euler_T.c:494-545)
+ *   BC_SUPERSONIC_IN 105   constructor_Boundary_Value_T_euler_supersonic_inflow  (:657-703)
+ *   BC_SUPERSONIC_OUT 106  constructor_Boundary_Value_T_euler_supersonic_outflow (:705-770)
+ *   advection (1-3, 11-13, 41-46)  constructor_Boundary_Value_T_advection_upwind (boundary_advection_T.c:40-95)
+ * The code is taken modulo BC_STEP_SC = 10000 (straight/curved variants) as set_function_pointers_num_flux_bc_*
+ * do (face_solver_T.c:203-275).
+ * Returns 0, or -1 for a BC code this oracle does not provide. */
+static int SUF(boundary_state)(const struct oracle_problem* P, const int bc, const Type* WL, const double* ext,
+                               const double* n, Type* WR)
+{
+	const int d = P->d, nv = P->n_var;
+	if (P->pde == ORACLE_PDE_ADVECTION) {
+		/* every advection code (inflow 1-3, outflow 11-13, upwind 41-46) takes the upwind boundary value
+		 * (set_function_pointers_num_flux_bc_advection, face_solver_T.c:203-226) */
+		const int a = bc % 10000;
+		if (!((a >= 1 && a <= 3) || (a >= 11 && a <= 13) || (a >= 41 && a <= 46)))
+			return -1;
+		double b_dot_n = 0.0;
+		for (int k = 0; k < d; ++k)
+			b_dot_n += P->b_adv[k] * n[k];
+		WR[0] = (b_dot_n <= 0.0 ? (Type)ext[0] : WL[0]);   /* inflow: exterior; outflow: interior */
+		return 0;
+	}
+	switch (bc % 10000) {
+	case 102: {   /* slip wall: rho and E kept, momentum reflected about the face */
+		Type rhoVn = 0.0;
+		for (int k = 0; k < d; ++k)
+			rhoVn += n[k] * WL[1 + k];
+		WR[0] = WL[0];
+		for (int k = 0; k < d; ++k)
+			WR[1 + k] = WL[1 + k] - 2.0 * rhoVn * n[k];
+		WR[d + 1] = WL[d + 1];
+		return 0;
+	}
+	case 105:
+		for (int k = 0; k < nv; ++k)
+			WR[k] = ext[k];
+		return 0;
+	case 106:
+		for (int k = 0; k < nv; ++k)
+			WR[k] = WL[k];
+		return 0;
+	case 101: {
+		/* primitive variables of both sides (convert_variables 'c' -> 'p') */
+		const Type rho_l = WL[0];
+		Type u_l[3] = {0.0, 0.0, 0.0}, V2_l = 0.0;
+		for (int k = 0; k < d; ++k) {
+			u_l[k] = WL[1 + k] / rho_l;
+			V2_l += u_l[k] * u_l[k];
+		}
+		const Type p_l = GM1 * (WL[d + 1] - 0.5 * rho_l * V2_l);
+		const double rho_r = ext[0];
+		double u_r[3] = {0.0, 0.0, 0.0}, V2_r = 0.0;
+		for (int k = 0; k < d; ++k) {
+			u_r[k] = ext[1 + k] / rho_r;
+			V2_r += u_r[k] * u_r[k];
+		}
+		const double p_r = GM1 * (ext[d + 1] - 0.5 * rho_r * V2_r);
+		const Type c_l = SQRT_T(GAMMA * p_l / rho_l);
+		const double c_r = sqrt(GAMMA * p_r / rho_r);
+		Type Vn_l = 0.0;
+		double Vn_r = 0.0;
+		for (int k = 0; k < d; ++k) {
+			Vn_l += n[k] * u_l[k];
+			Vn_r += n[k] * u_r[k];
+		}
+		const Type R_l = Vn_l + 2.0 / GM1 * c_l;   /* outgoing Riemann invariant */
+		const Type R_r = Vn_r - 2.0 / GM1 * c_r;   /* incoming */
+		const Type Vn = 0.5 * (R_l + R_r), cc = 0.25 * GM1 * (R_l - R_r);
+		Type rho, p, uvw[3] = {0.0, 0.0, 0.0};
+		if (ABS_T(Vn) >= ABS_T(cc)) {   /* supersonic */
+			if (REAL_T(Vn) < 0.0) {     /* inlet */
+				rho = rho_r;
+				for (int k = 0; k < d; ++k)
+					uvw[k] = u_r[k];
+				p = p_r;
+			} else {                    /* outlet */
+				rho = rho_l;
+				for (int k = 0; k < d; ++k)
+					uvw[k] = u_l[k];
+				p = p_l;
+			}
+		} else {                        /* subsonic */
+			Type uvw_t[3] = {0.0, 0.0, 0.0};
+			if (REAL_T(Vn) < 0.0) {
+				const double s_r = p_r / pow(rho_r, GAMMA);
+				rho = POW_T(1.0 / GAMMA * cc * cc / s_r, 1.0 / GM1);
+				for (int k = 0; k < d; ++k)
+					uvw_t[k] = u_r[k] - Vn_r * n[k];
+			} else {
+				const Type s_l = p_l / POW_T(rho_l, GAMMA);
+				rho = POW_T(1.0 / GAMMA * cc * cc / s_l, 1.0 / GM1);
+				for (int k = 0; k < d; ++k)
+					uvw_t[k] = u_l[k] - Vn_l * n[k];
+			}
+			for (int k = 0; k < d; ++k)
+				uvw[k] = Vn * n[k] + uvw_t[k];
+			p = 1.0 / GAMMA * cc * cc * rho;
+		}
+		/* back to conserved variables (convert_variables 'p' -> 'c') */
+		Type V2 = 0.0;
+		for (int k = 0; k < d; ++k)
+			V2 += uvw[k] * uvw[k];
+		WR[0] = rho;
+		for (int k = 0; k < d; ++k)
+			WR[1 + k] = rho * uvw[k];
+		WR[d + 1] = p / GM1 + 0.5 * rho * V2;
+		return 0;
+	}
+	default:
+		return -1;
+	}
+}
+
 /* Physical Euler flux at one node, f[dim + d*eq]: compute_Flux_T_euler + compute_Flux_euler_0
  * (src/simulation/test_case/flux/flux_euler_T.c:71-143, 259-298). */
 static void SUF(flux_euler)(const int d, const Type* W, Type* f)
@@ -153,6 +270,47 @@ static void SUF(num_flux_roe)(const int d, const Type* WL, const Type* WR, const
  * compute_volume_rlhs_dg (compute_volume_rlhs_dg_T.c:53-72 -> compute_volume_rlhs_T.c:145-177,
  * compute_rlhs_T.c:71-110) and compute_face_rlhs_dg (compute_face_rlhs_dg_T.c:88-114 ->
  * boundary_T.c:42-145, compute_face_rlhs_T.c:297-359). sol/rhs: per volume (n_vs x n_var) column-major. */
+/* A boundary face (no right volume): the interior trace, the exterior state of its BC at every node, the numerical
+ * flux with the interior normal, and the lift into the interior volume only (compute_face_rlhs_T.c:297-310 with
+ * Solver_Face_T::constructor_Boundary_Value_fcl, face_solver_T.c:246-274). */
+static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Type* sol, Type* rhs, Type* sL, Type* nnf)
+{
+	const struct oracle_problem* P = &c->P;
+	const int d = P->d, nv = P->n_var, neq = P->n_var;
+	const int vL = P->face_vol[2 * f], lfL = P->face_lf[2 * f];
+	const struct oracle_face_ops* FL = &P->face_ops[P->face_ops_idx[2 * f]];
+	const int n_fc = FL->n_fc;
+	const double* nrm = &P->normals_fc[c->fc_off[f] * d];
+	const double* jf = &P->jacobian_det_fc[c->fc_off[f]];
+	const double* ext = &P->bc_state_fc[c->fc_off[f] * nv];
+	for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
+		sL[i] = 0.0;
+	SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], &sol[c->state_off[vL]], sL);
+	for (int i = 0; i < n_fc; ++i) {
+		Type WL[5], WR[5], nF[5];
+		for (int k = 0; k < nv; ++k)
+			WL[k] = sL[i + (size_t)n_fc * k];
+		const double* ni = &nrm[(size_t)i * d];
+		if (SUF(boundary_state)(P, P->bc_fc[f], WL, &ext[(size_t)i * nv], ni, WR) != 0)
+			return -1;
+		if (P->pde == ORACLE_PDE_EULER) {
+			if (P->num_flux == ORACLE_NUM_FLUX_ROE_PIKE)
+				SUF(num_flux_roe)(d, WL, WR, ni, nF);
+			else
+				SUF(num_flux_lf)(d, WL, WR, ni, nF);
+		} else {
+			double b_dot_n = 0.0;
+			for (int k = 0; k < d; ++k)
+				b_dot_n += P->b_adv[k] * ni[k];
+			nF[0] = (b_dot_n > ORACLE_EPS ? b_dot_n * WL[0] : b_dot_n * WR[0]);
+		}
+		for (int k = 0; k < neq; ++k)
+			nnf[i + (size_t)n_fc * k] = nF[k] * jf[i];
+	}
+	SUF(mm_acc)(FL->n_vs, n_fc, neq, -1.0, &FL->tw0_vt_fc[(size_t)lfL * FL->n_vs * n_fc], nnf, &rhs[c->state_off[vL]]);
+	return 0;
+}
+
 static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* rhs)
 {
 	const struct oracle_problem* P = &c->P;
@@ -207,6 +365,13 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 	/* ---- face term ---- */
 	for (int f = 0; f < P->n_faces; ++f) {
 		const int vL = P->face_vol[2 * f], vR = P->face_vol[2 * f + 1];
+		if (vR < 0) {
+			if (SUF(boundary_face)(c, f, sol, rhs, sL, nnf) != 0) {
+				free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);
+				return ORACLE_ERR_ARG;
+			}
+			continue;
+		}
 		const int lfL = P->face_lf[2 * f], lfR = P->face_lf[2 * f + 1];
 		const struct oracle_face_ops* FL = &P->face_ops[P->face_ops_idx[2 * f]];
 		const struct oracle_face_ops* FR = &P->face_ops[P->face_ops_idx[2 * f + 1]];
