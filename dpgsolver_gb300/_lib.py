@@ -93,7 +93,7 @@ class Mesh(ctypes.Structure):
     _fields_ = [("n_volumes", ctypes.c_int), ("metrics_vc", c_double_p), ("jacobian_det_vc", c_double_p),
                 ("n_faces", ctypes.c_int), ("face_vol", c_int_p), ("face_lf", c_int_p), ("nc_fc", c_int_p),
                 ("normals_fc", c_double_p), ("jacobian_det_fc", c_double_p), ("bc_fc", c_int_p),
-                ("bc_state_fc", c_double_p)]
+                ("bc_state_fc", c_double_p), ("bc_data", c_double_p)]
 
 
 EXPORTS = {

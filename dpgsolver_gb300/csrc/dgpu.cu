@@ -55,6 +55,7 @@ struct dgpu_ctx {
 	int n_bnd = 0;                        // boundary faces (face_vol[2f+1] < 0)
 	int *bnd = nullptr, *bc_code = nullptr;
 	double* bc_ext = nullptr;
+	BcData bc_data = {0.0, 0.0, 0.0, 0.0};
 	double *traces = nullptr, *nnf = nullptr, *vol_gl = nullptr;
 	unsigned long long* max_bits = nullptr;
 	int* err_flag = nullptr;
@@ -104,6 +105,7 @@ struct dgpu_ctx {
 		P.bnd = bnd;
 		P.bc_code = bc_code;
 		P.bc_ext = bc_ext;
+		P.bc_data = bc_data;
 		return P;
 	}
 };
@@ -688,6 +690,10 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 				return fail(nullptr, DGPU_ERR_UNSUPPORTED,
 				            "BC code " + std::to_string(mesh->bc_fc[f]) + " is not provided for this pde");
 			}
+			if ((code == kBcBackPressure || code == kBcTotalTP) && !mesh->bc_data) {
+				delete c;
+				return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "back pressure / total TP faces need bc_data");
+			}
 			bnd[f] = (int)bc_code.size();
 			bc_code.push_back(code);
 			const double* e = mesh->bc_state_fc + f * (size_t)NF * c->nv;
@@ -762,6 +768,8 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		DG_TRY(upload(&c->nc_inv, nc_inv));
 	}
 	c->n_bnd = (int)bc_code.size();
+	if (mesh->bc_data)
+		c->bc_data = BcData{mesh->bc_data[0], mesh->bc_data[1], mesh->bc_data[2], mesh->bc_data[3]};
 	if (c->n_bnd > 0) {
 		DG_TRY(upload(&c->bnd, bnd));
 		DG_TRY(upload(&c->bc_code, bc_code));
@@ -1229,7 +1237,7 @@ extern "C" dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const 
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL operator");
 	if (d_mesh->n_volumes < 1 || d_mesh->n_faces < 1)
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "empty mesh");
-	if (d_mesh->bc_fc || d_mesh->bc_state_fc)
+	if (d_mesh->bc_fc || d_mesh->bc_state_fc || d_mesh->bc_data)
 		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "boundary faces are not supported here (use dgpu_create)");
 	if (!is_device_pointer(d_sol) || !is_device_pointer(d_rhs) || !is_device_pointer(d_mesh->metrics_vc) ||
 	    !is_device_pointer(d_mesh->jacobian_det_vc) || !is_device_pointer(d_mesh->face_vol) ||

@@ -180,7 +180,18 @@ __device__ __forceinline__ double num_flux_upwind(double uL, double uR, const do
 // BC codes after taking them modulo BC_STEP_SC (definitions_bc.h:33-64); set_function_pointers_num_flux_bc_advection
 // and _euler (face_solver_T.c:203-275) select the boundary value by these.
 constexpr int kBcStepSC = 10000;
-enum BcCode { kBcRiemann = 101, kBcSlipWall = 102, kBcSupersonicIn = 105, kBcSupersonicOut = 106 };
+enum BcCode {
+	kBcRiemann = 101, kBcSlipWall = 102, kBcBackPressure = 103, kBcTotalTP = 104, kBcSupersonicIn = 105,
+	kBcSupersonicOut = 106
+};
+
+// BC_Data (boundary_euler_T.c:44-49): the scalars the reference reads from the test case's input file.
+struct BcData {
+	double p_back;   // BC_BACKPRESSURE
+	double t_total;  // BC_TOTAL_TP: total temperature, total pressure, specific gas constant
+	double p_total;
+	double r_s;
+};
 
 // True for the advection codes that take the upwind boundary value (inflow 1-3, outflow 11-13, upwind 41-46).
 __host__ __device__ __forceinline__ bool bc_is_advection_upwind(int bc)
@@ -189,7 +200,7 @@ __host__ __device__ __forceinline__ bool bc_is_advection_upwind(int bc)
 }
 __host__ __device__ __forceinline__ bool bc_is_euler(int bc)
 {
-	return bc == kBcRiemann || bc == kBcSlipWall || bc == kBcSupersonicIn || bc == kBcSupersonicOut;
+	return bc >= kBcRiemann && bc <= kBcSupersonicOut;
 }
 
 // Exterior state WR of an Euler boundary face node from the interior trace WL, the test case's solution at the node
@@ -201,11 +212,66 @@ __host__ __device__ __forceinline__ bool bc_is_euler(int bc)
 //                    supersonic faces take the upwind state whole;
 //   kBcSlipWall      ..._euler_slipwall (:494-533): density and energy kept, momentum mirrored about the face;
 //   kBcSupersonicIn  ..._euler_supersonic_inflow (:657-692): the exterior state;
-//   kBcSupersonicOut ..._euler_supersonic_outflow (:705-745): the interior state.
+//   kBcSupersonicOut ..._euler_supersonic_outflow (:705-745): the interior state;
+//   kBcBackPressure  ..._euler_back_pressure (:772-866): the interior state where |V| >= c, else the interior
+//                    velocity at pressure p_back and density gamma p_back / c^2;
+//   kBcTotalTP       ..._euler_total_tp (:991-1120): the speed of sound from the interior's outgoing invariant and
+//                    total enthalpy (the larger root of a quadratic), flow along the normal, temperature and
+//                    pressure from the total values by the isentropic relations, density by the gas law.
 template <int D, typename T>
-__device__ __forceinline__ void euler_boundary_state(int bc, const T* WL, const double* ext, const double* n, T* WR)
+__device__ __forceinline__ void euler_boundary_state(int bc, const T* WL, const double* ext, const double* n, T* WR,
+                                                     const BcData& bd)
 {
 	constexpr int NV = D + 2;
+	if (bc == kBcBackPressure || bc == kBcTotalTP) {
+		const T rho_l = WL[0], rho_l_inv = 1.0 / rho_l;
+		T u_l[D], V2_l = 0.0, Vn_l = 0.0;
+#pragma unroll
+		for (int k = 0; k < D; ++k) {
+			u_l[k] = WL[1 + k] * rho_l_inv;
+			V2_l += u_l[k] * u_l[k];
+			Vn_l += n[k] * u_l[k];
+		}
+		const T p_l = kGm1 * (WL[D + 1] - 0.5 * rho_l * V2_l);
+		const T c2_l = kGamma * p_l * rho_l_inv;
+		if (bc == kBcBackPressure) {
+			if (!(sqrt(V2_l) < sqrt(c2_l))) {
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					WR[k] = WL[k];
+			} else {
+				const T rho_b = (kGamma * bd.p_back) / c2_l;
+				WR[0] = rho_b;
+#pragma unroll
+				for (int k = 0; k < D; ++k)
+					WR[1 + k] = u_l[k] * rho_b;
+				WR[D + 1] = bd.p_back * (1.0 / kGm1) + 0.5 * rho_b * V2_l;
+			}
+			return;
+		}
+		const T H_l = (WL[D + 1] + p_l) * rho_l_inv;
+		const T R_l = Vn_l + (2.0 / kGm1) * sqrt(c2_l);
+		constexpr double aQ = 1.0 + 2.0 / kGm1;
+		const T bQ = -2.0 * R_l, cQ = 0.5 * kGm1 * (R_l * R_l - 2.0 * H_l);
+		const T t1 = bQ * (-0.5 / aQ), t2 = sqrt(bQ * bQ - 4.0 * aQ * cQ) * (0.5 / aQ);
+		const T cM = t1 - t2, cP = t1 + t2;
+		const T c = (cM > cP ? cM : cP);
+		const T Vn = R_l - (2.0 / kGm1) * c;
+		const T M = Vn / c;
+		const T Tb = bd.t_total / (1.0 + 0.5 * kGm1 * M * M);
+		const T p = bd.p_total * pow(Tb * (1.0 / bd.t_total), kGamma / kGm1);
+		const T rho = p / (bd.r_s * Tb);
+		T V2 = 0.0;
+		WR[0] = rho;
+#pragma unroll
+		for (int k = 0; k < D; ++k) {
+			const T uk = Vn * n[k];
+			V2 += uk * uk;
+			WR[1 + k] = rho * uk;
+		}
+		WR[D + 1] = p * (1.0 / kGm1) + 0.5 * rho * V2;
+		return;
+	}
 	if (bc == kBcSlipWall) {
 		T rhoVn = 0.0;
 #pragma unroll

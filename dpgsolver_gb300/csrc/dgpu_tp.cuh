@@ -67,6 +67,7 @@ struct TPParams {
 	const int* bnd;            // [f] index b of the face in the boundary list, -1 for an interior face
 	const int* bc_code;        // [b] BC code modulo BC_STEP_SC
 	const double* bc_ext;      // [b][NV][NF] exterior (test case) conserved state at the face nodes
+	BcData bc_data;            // back pressure / total temperature and pressure data
 };
 
 // Right-hand state of face node i of boundary face b: the boundary value of its BC from the interior trace WL.
@@ -80,7 +81,7 @@ __device__ __forceinline__ void boundary_value(const TPParams& P, int b, int i, 
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
 			e[k] = ext[k * NF + i];
-		euler_boundary_state<D, T>(P.bc_code[b], WL, e, n, WR);
+		euler_boundary_state<D, T>(P.bc_code[b], WL, e, n, WR, P.bc_data);
 	} else {
 		WR[0] = advection_boundary_value<D, T>(WL[0], ext[i], n, P.b_adv);
 	}

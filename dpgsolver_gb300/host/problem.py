@@ -48,6 +48,7 @@ class DGProblem:
     meta: dict = field(default_factory=dict)
     bc: np.ndarray | None = None          # (n_faces,) BC code of each face (definitions_bc.h), 0 on interior faces
     bc_state: np.ndarray | None = None    # (n_faces, n_fc, n_var) exterior conserved state at the face nodes
+    bc_data: tuple | None = None          # (p_back, t_total, p_total, r_s): BC_Data of boundary_euler_T.c:44-49
 
     @property
     def n_var(self) -> int:
@@ -97,6 +98,7 @@ def flat_arrays(prob) -> dict:
         "sol": np.ascontiguousarray(prob.sol).ravel(),
         "bc_fc": None if prob.bc is None else np.ascontiguousarray(prob.bc, dtype=np.int32),
         "bc_state_fc": None if prob.bc_state is None else np.ascontiguousarray(prob.bc_state).ravel(),
+        "bc_data": prob.bc_data,
     }
 
 
@@ -202,6 +204,8 @@ def constant_state(prob: DGProblem, values) -> np.ndarray:
 BC_UPWIND = 41
 BC_RIEMANN = 101
 BC_SLIPWALL = 102
+BC_BACKPRESSURE = 103
+BC_TOTAL_TP = 104
 BC_SUPERSONIC_IN = 105
 BC_SUPERSONIC_OUT = 106
 
@@ -309,3 +313,36 @@ def advection_box_2d(n: int = 8, p: int = 2, b=(1.0, 0.5)) -> DGProblem:
         return (np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1]))[:, None]
     sides = {(dd, s): BC_UPWIND for dd in range(2) for s in range(2)}
     return _set_boundaries(prob, sides, ext)
+
+
+def euler_subsonic_duct(d: int = 2, n: int = 6, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, mach: float = 0.4,
+                        amplitude: float = 0.03, seed: int = 0, perturb: float = 0.02) -> DGProblem:
+    """Curved QUAD/HEX box [0,10]^d with a subsonic stream along x: total temperature and pressure inflow at x = 0
+    (BC_TOTAL_TP), back pressure outflow at x = 10 (BC_BACKPRESSURE), slip walls on the other sides. The BC data
+    (p_back, t_total, p_total, r_s) are those of the unperturbed stream (rho, p) = (1, 1), r_s = 1 (T = p / rho), so
+    that stream is a steady state; the state is the stream with seeded smooth perturbations."""
+    L = 10.0
+    mesh = StructuredMesh(d, n, 0.0, L, periodic=(False,) * d)
+    ops = TPOperatorSet(mesh.e_type, p)
+    deform = sinusoidal_deform_2d(amplitude, L) if d == 2 else sinusoidal_deform_3d(amplitude, L)
+    geom = TPGeometry(mesh, ops, deform=deform, curved=True)
+    prob = DGProblem(f"euler_subsonic_duct_{d}d", d, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, d + 2, ops.n_vs)), dt=0.0, n_steps=100)
+    xyz = prob.solution_node_xyz()
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0.0, 2.0 * math.pi, size=(d + 2, d))
+
+    def wave(k):
+        s = np.ones(xyz.shape[:2])
+        for j in range(d):
+            s = s * np.sin(2.0 * math.pi * xyz[..., j] / L + ph[k, j])
+        return s
+    u0 = mach * math.sqrt(GAMMA)
+    vel = np.stack([u0 * (1.0 + perturb * wave(2))] + [u0 * perturb * wave(3 + j) for j in range(d - 1)])
+    prob.sol = _pack_state(primitive_to_conserved(d, 1.0 + perturb * wave(0), vel, 1.0 + perturb * wave(1)))
+    prob.dt = stable_dt(prob)
+    T_tot = 1.0 + 0.5 * GM1 * mach * mach
+    prob.bc_data = (1.0, T_tot, T_tot ** (GAMMA / GM1), 1.0)
+    sides = {(0, 0): BC_TOTAL_TP, (0, 1): BC_BACKPRESSURE}
+    sides.update({(k, s): BC_SLIPWALL for k in range(1, d) for s in range(2)})
+    return _set_boundaries(prob, sides, _uniform_flow(d, 1.0, (u0,) + (0.0,) * (d - 1), 1.0))

@@ -69,6 +69,8 @@ class Simulation:
                 raise ValueError("bc needs one code per face and bc_state (n_faces, n_fc, n_var) values")
             m.bc_fc = _ip(arr("bc", prob.bc, np.int32))
             m.bc_state_fc = _dp(arr("bcs", prob.bc_state))
+            if getattr(prob, "bc_data", None) is not None:
+                m.bc_data = _dp(arr("bcd", np.asarray(prob.bc_data, dtype=np.float64).reshape(4)))
         h = ctypes.c_void_p()
         st = lib.dgpu_create(ctypes.byref(phys), ctypes.byref(tp), ctypes.byref(m), ctypes.byref(h))
         check(st, None)

@@ -95,15 +95,19 @@ typedef struct {
 	/* Boundary faces: face_vol[2f+1] = -1 (no neighbour; the face belongs to its side-0 volume, normals_fc
 	 * outward from it). Both arrays may be NULL when no face is a boundary face.
 	 * bc_fc: n_faces: Face::bc, the reference's BC code (definitions_bc.h), read on boundary faces only and
-	 *   taken modulo BC_STEP_SC = 10000. Euler: BC_RIEMANN 101, BC_SLIPWALL 102, BC_SUPERSONIC_IN 105,
-	 *   BC_SUPERSONIC_OUT 106 (boundary_euler_T.c); advection: inflow/outflow/upwind 1-3, 11-13, 41-46, all the
-	 *   upwind boundary value (boundary_advection_T.c:40-77). Other codes: DGPU_ERR_UNSUPPORTED.
+	 *   taken modulo BC_STEP_SC = 10000. Euler: BC_RIEMANN 101, BC_SLIPWALL 102, BC_BACKPRESSURE 103,
+	 *   BC_TOTAL_TP 104, BC_SUPERSONIC_IN 105, BC_SUPERSONIC_OUT 106 (boundary_euler_T.c); advection:
+	 *   inflow/outflow/upwind 1-3, 11-13, 41-46, all the upwind boundary value (boundary_advection_T.c:40-77).
+	 *   Other codes: DGPU_ERR_UNSUPPORTED.
 	 * bc_state_fc: n_faces x (n_fc x n_var) row-major: the test case's conserved solution at the face's
 	 *   cubature nodes (constructor_sol_bv(xyz_fc)), the exterior data of Riemann, supersonic inflow and
 	 *   upwind inflow boundaries; read on boundary faces only.
 	 * dgpu_create only: the no-allocation entry and the batched context return DGPU_ERR_UNSUPPORTED. */
 	const int* bc_fc;
 	const double* bc_state_fc;
+	/* bc_data: 4 doubles {p_back, t_total, p_total, r_s}, the reference's BC_Data (boundary_euler_T.c:44-49, read
+	 * from the test case's input file there) for BC_BACKPRESSURE and BC_TOTAL_TP faces; NULL when none. */
+	const double* bc_data;
 } dgpu_mesh;
 
 /* Create a context on the current CUDA device and copy everything it needs; the caller may free its arrays

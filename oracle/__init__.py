@@ -40,7 +40,7 @@ class _Problem(ctypes.Structure):
         ("jacobian_det_vc", _c_double_p),
         ("n_faces", ctypes.c_int), ("face_vol", _c_int_p), ("face_lf", _c_int_p), ("face_ops_idx", _c_int_p),
         ("nc_fc", _c_int_p), ("normals_fc", _c_double_p), ("jacobian_det_fc", _c_double_p),
-        ("bc_fc", _c_int_p), ("bc_state_fc", _c_double_p),
+        ("bc_fc", _c_int_p), ("bc_state_fc", _c_double_p), ("bc_data", ctypes.c_double * 4),
     ]
 
 
@@ -177,6 +177,8 @@ class Oracle:
                 raise ValueError("bc_fc needs one code per face and bc_state_fc n_var values per face node")
             P.bc_fc = _ip(arr(fl["bc_fc"], np.int32))
             P.bc_state_fc = _dp(arr(fl["bc_state_fc"]))
+            for k, x in enumerate(fl.get("bc_data") or (0.0, 0.0, 0.0, 0.0)):
+                P.bc_data[k] = float(x)
         self._keep = (keep, G, FO, P)
         h = ctypes.c_void_p()
         st = lib.oracle_create(ctypes.byref(P), ctypes.byref(h))

@@ -62,6 +62,9 @@ struct oracle_problem {
 	 * (constructor_sol_bv at the face nodes). Both may be NULL on meshes without boundary faces. */
 	const int* bc_fc;
 	const double* bc_state_fc;
+	/* BC_Data of boundary_euler_T.c:44-49, read from the test case's input by the reference: p_back (BC_BACKPRESSURE
+	 * 103), t_total, p_total, r_s (BC_TOTAL_TP 104). */
+	double bc_data[4];
 };
 
 struct oracle_ctx;

@@ -47,6 +47,9 @@ static void SUF(mm_acc)(const int m, const int k, const int nc, const double alp
  *   BC_SLIPWALL 102        constructor_Boundary_Value_T_euler_slipwall       (boundary_euler_T.c:494-545)
  *   BC_SUPERSONIC_IN 105   constructor_Boundary_Value_T_euler_supersonic_inflow  (:657-703)
  *   BC_SUPERSONIC_OUT 106  constructor_Boundary_Value_T_euler_supersonic_outflow (:705-770)
+ *   BC_BACKPRESSURE 103    constructor_Boundary_Value_T_euler_back_pressure  (:772-866), p_back = bc_data[0]
+ *   BC_TOTAL_TP 104        constructor_Boundary_Value_T_euler_total_tp       (:991-1120), bc_data[1..3] =
+ *                          (t_total, p_total, r_s)
  *   advection (1-3, 11-13, 41-46)  constructor_Boundary_Value_T_advection_upwind (boundary_advection_T.c:40-95)
  * The code is taken modulo BC_STEP_SC = 10000 (straight/curved variants) as set_function_pointers_num_flux_bc_*
  * do (face_solver_T.c:203-275).
@@ -82,6 +85,60 @@ static int SUF(boundary_state)(const struct oracle_problem* P, const int bc, con
 		for (int k = 0; k < nv; ++k)
 			WR[k] = ext[k];
 		return 0;
+	case 103: {   /* back pressure: supersonic (|V| >= c) keeps the interior state, else p = p_back */
+		const double p_back = P->bc_data[0];
+		const Type rho_l = WL[0];
+		Type u_l[3] = {0.0, 0.0, 0.0}, V2_l = 0.0;
+		for (int k = 0; k < d; ++k) {
+			u_l[k] = WL[1 + k] / rho_l;
+			V2_l += u_l[k] * u_l[k];
+		}
+		const Type p_l = GM1 * (WL[d + 1] - 0.5 * rho_l * V2_l);
+		const Type c2_l = GAMMA * p_l / rho_l;
+		if (ABS_T(SQRT_T(V2_l)) >= ABS_T(SQRT_T(c2_l))) {
+			for (int k = 0; k < nv; ++k)
+				WR[k] = WL[k];
+		} else {
+			const Type rho_b = GAMMA * p_back / c2_l;
+			WR[0] = rho_b;
+			for (int k = 0; k < d; ++k)
+				WR[1 + k] = u_l[k] * rho_b;
+			WR[d + 1] = p_back / GM1 + 0.5 * rho_b * V2_l;
+		}
+		return 0;
+	}
+	case 104: {   /* total temperature and pressure: outgoing invariant + total enthalpy give c, flow along n */
+		const double T_tot = P->bc_data[1], p_tot = P->bc_data[2], r_s = P->bc_data[3];
+		const Type rho_l = WL[0];
+		Type u_l[3] = {0.0, 0.0, 0.0}, V2_l = 0.0, Vn_l = 0.0;
+		for (int k = 0; k < d; ++k) {
+			u_l[k] = WL[1 + k] / rho_l;
+			V2_l += u_l[k] * u_l[k];
+			Vn_l += n[k] * u_l[k];
+		}
+		const Type p_l = GM1 * (WL[d + 1] - 0.5 * rho_l * V2_l);
+		const Type c_l = SQRT_T(GAMMA * p_l / rho_l);
+		const Type H_l = (WL[d + 1] + p_l) / rho_l;
+		const Type R_l = Vn_l + 2.0 / GM1 * c_l;
+		const double aQ = 1.0 + 2.0 / GM1;
+		const Type bQ = -2.0 * R_l, cQ = 0.5 * GM1 * (R_l * R_l - 2.0 * H_l);
+		const Type t1 = -bQ / (2.0 * aQ), t2 = SQRT_T(bQ * bQ - 4.0 * aQ * cQ) / (2.0 * aQ);
+		const Type cM = t1 - t2, cP = t1 + t2;
+		const Type c = (REAL_T(cM) > REAL_T(cP) ? cM : cP);
+		const Type Vn = R_l - 2.0 / GM1 * c;
+		const Type M = Vn / c;
+		const Type T = T_tot / (1.0 + 0.5 * GM1 * M * M);
+		const Type p = p_tot * POW_T(T / T_tot, GAMMA / GM1);
+		const Type rho = p / (r_s * T);
+		Type V2 = 0.0;
+		for (int k = 0; k < d; ++k)
+			V2 += (Vn * n[k]) * (Vn * n[k]);
+		WR[0] = rho;
+		for (int k = 0; k < d; ++k)
+			WR[1 + k] = rho * (Vn * n[k]);
+		WR[d + 1] = p / GM1 + 0.5 * rho * V2;
+		return 0;
+	}
 	case 106:
 		for (int k = 0; k < nv; ++k)
 			WR[k] = WL[k];

@@ -1,8 +1,8 @@
 """Boundary faces on the CUDA path (dgpu_create with bc_fc / bc_state_fc) against the CPU oracle.
 
 The residual, SSP-RK3 steps, the forward linearisation (against the oracle's complex step) and the adjoint (the
-transpose of the forward one) on bounded meshes: slip walls, Riemann, supersonic inflow/outflow and upwind
-advection boundaries (the reference's boundary values, test_case/boundary/boundary_euler_T.c and
+transpose of the forward one) on bounded meshes: slip walls, Riemann, supersonic inflow/outflow, back pressure,
+total temperature/pressure and upwind advection boundaries (the reference's boundary values, test_case/boundary/boundary_euler_T.c and
 boundary_advection_T.c). Tolerances as in test_gpu_parity.py: <= 1e-12 normwise relative.
 """
 import ctypes
@@ -27,6 +27,9 @@ CASES = {
     "duct3d_roe_p1_6": lambda: P.euler_duct_3d(6, 1),
     "advbox2d_p2_8": lambda: P.advection_box_2d(8, 2),
     "advbox2d_p4_4": lambda: P.advection_box_2d(4, 4, b=(-0.6, 1.1)),
+    "subduct2d_roe_p3_8": lambda: P.euler_subsonic_duct(2, 8, 3),
+    "subduct3d_lf_p2_4": lambda: P.euler_subsonic_duct(3, 4, 2, num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
+    "subduct3d_roe_p3_4": lambda: P.euler_subsonic_duct(3, 4, 3),
     # many CTAs: boundary and interior faces interleaved across the whole grid
     "duct3d_roe_p3_12": lambda: P.euler_duct_3d(12, 3),
 }
@@ -48,7 +51,8 @@ def test_bc_residual_matches_oracle(gpu_lib, name):
     assert abs(mx - mx_ref) <= TOL * mx_ref
 
 
-@pytest.mark.parametrize("name", ["channel2d_roe_p3_8", "riemann2d_lf_p3_8", "duct3d_roe_p2_4", "advbox2d_p2_8"])
+@pytest.mark.parametrize("name", ["channel2d_roe_p3_8", "riemann2d_lf_p3_8", "duct3d_roe_p2_4", "advbox2d_p2_8",
+                                  "subduct3d_roe_p3_4"])
 def test_bc_rk3_steps_match_oracle(gpu_lib, name):
     from dpgsolver_gb300.solver import Simulation
     prob = CASES[name]()
@@ -65,16 +69,18 @@ def test_bc_rk3_steps_match_oracle(gpu_lib, name):
 
 def test_bc_free_stream_preserved_on_gpu(gpu_lib):
     """Streams that satisfy every boundary condition are steady: Riemann sides with the free stream as exterior,
-    slip walls with a tangential stream, the supersonic duct with its Mach 2 stream."""
+    slip walls with a tangential stream, the supersonic duct with its Mach 2 stream, the subsonic duct (total
+    temperature/pressure inflow, back-pressure outflow) with the stream its BC data come from."""
     from dpgsolver_gb300.solver import Simulation
 
     def stream(prob, rho, vel, p):
         vel = np.asarray(vel, dtype=np.float64)
         return P.constant_state(prob, [rho] + list(rho * vel) + [p / P.GM1 + 0.5 * rho * float(vel @ vel)])
-    u0 = 2.0 * np.sqrt(P.GAMMA)
+    u0, u1 = 2.0 * np.sqrt(P.GAMMA), 0.4 * np.sqrt(P.GAMMA)
     for prob, st in ((P.euler_riemann_2d(8, 3), (1.0, (1.0, 1.0), 1.0)),
                      (P.euler_channel_2d(8, 3), (1.0, (0.8, 0.0), 1.0)),
-                     (P.euler_duct_3d(4, 3), (1.0, (u0, 0.0, 0.0), 1.0))):
+                     (P.euler_duct_3d(4, 3), (1.0, (u0, 0.0, 0.0), 1.0)),
+                     (P.euler_subsonic_duct(3, 4, 3), (1.0, (u1, 0.0, 0.0), 1.0))):
         with Simulation(prob) as sim:
             sim.upload_state(stream(prob, *st))
             assert sim.compute_rhs() < 1e-10
@@ -86,7 +92,7 @@ def _perturbed(prob, seed):
 
 
 @pytest.mark.parametrize("name", ["channel2d_roe_p3_8", "riemann2d_roe_p4_5", "duct3d_lf_p3_4", "duct3d_roe_p2_4",
-                                  "advbox2d_p2_8"])
+                                  "advbox2d_p2_8", "subduct2d_roe_p3_8", "subduct3d_lf_p2_4"])
 def test_bc_jvp_matches_complex_step(gpu_lib, name):
     """The dual-number boundary values against the oracle's complex-step ones (the reference's linearisation)."""
     from dpgsolver_gb300.solver import Simulation
@@ -99,7 +105,8 @@ def test_bc_jvp_matches_complex_step(gpu_lib, name):
     assert rel_err(jv, ri / 1e-30) <= TOL
 
 
-@pytest.mark.parametrize("name", ["channel2d_roe_p3_8", "riemann2d_lf_p3_8", "duct3d_roe_p2_4", "advbox2d_p2_8"])
+@pytest.mark.parametrize("name", ["channel2d_roe_p3_8", "riemann2d_lf_p3_8", "duct3d_roe_p2_4", "advbox2d_p2_8",
+                                  "subduct2d_roe_p3_8"])
 def test_bc_vjp_is_the_transpose_of_the_jvp(gpu_lib, name):
     from dpgsolver_gb300.solver import Simulation
     prob = CASES[name]()
@@ -122,11 +129,15 @@ def test_bc_create_errors(gpu_lib):
     with pytest.raises(_lib.DGPUError) as e:
         Simulation(prob)
     assert e.value.status == 1
-    for code in (103, 104, 41, 999):      # back pressure, total TP (not provided); advection code on Euler; junk
+    for code in (111, 113, 41, 999):      # no-slip walls (Navier-Stokes); an advection code on Euler; junk
         prob.bc, prob.bc_state = np.where(bc > 0, code, 0).astype(np.int32), bcs
         with pytest.raises(_lib.DGPUError) as e:
             Simulation(prob)
         assert e.value.status == 2
+    prob.bc = np.where(bc > 0, 103, 0).astype(np.int32)            # back pressure without its BC data
+    with pytest.raises(_lib.DGPUError) as e:
+        Simulation(prob)
+    assert e.value.status == 1
     prob.bc = np.where(bc > 0, 20000 + 102, 0).astype(np.int32)   # curved slip wall: the same boundary value
     with Simulation(prob) as sim:
         mx = sim.compute_rhs()

@@ -125,7 +125,7 @@ def test_boundary_face_needs_bc_arrays():
 
 def test_unknown_bc_code_is_an_error():
     prob = P.euler_channel_2d(3, 2)
-    prob.bc = np.where(prob.bc > 0, 103, 0).astype(np.int32)   # BC_BACKPRESSURE: not provided
+    prob.bc = np.where(prob.bc > 0, 111, 0).astype(np.int32)   # BC_NOSLIP_ADIABATIC: Navier-Stokes only
     with pytest.raises(Exception):
         oracle.Oracle(prob).compute_rhs(prob.sol)
 
@@ -149,3 +149,37 @@ def test_boundary_layout(mk, sides):
     assert prob.bc_state.shape == (m.n_faces, prob.ops.n_fc, prob.n_var)
     assert set(map(tuple, np.unique(np.stack([m.face_lf[bnd, 0] // 2, m.face_lf[bnd, 0] % 2], 1), axis=0))) \
         == set(sides)
+
+
+@pytest.mark.parametrize("d,flux", [(2, P.NUM_FLUX_ROE_PIKE), (2, P.NUM_FLUX_LAX_FRIEDRICHS), (3, P.NUM_FLUX_ROE_PIKE)])
+def test_total_tp_and_back_pressure_preserve_their_stream(d, flux):
+    """Total temperature/pressure inflow and back-pressure outflow whose data come from a subsonic stream along x
+    (slip walls elsewhere): that stream is steady."""
+    prob = P.euler_subsonic_duct(d, 3, 2, num_flux=flux)
+    u0 = 0.4 * np.sqrt(P.GAMMA)
+    _, mx = oracle.Oracle(prob).compute_rhs(_stream(prob, 1.0, (u0,) + (0.0,) * (d - 1), 1.0))
+    assert mx < 1e-10
+
+
+def test_back_pressure_sets_the_outflow_pressure():
+    """Raising p_back changes the residual only in the elements at the outflow end x = 10."""
+    prob = P.euler_subsonic_duct(2, 4, 2)
+    r0, _ = oracle.Oracle(prob).compute_rhs(prob.sol)
+    prob.bc_data = (1.2,) + tuple(prob.bc_data[1:])
+    r1, _ = oracle.Oracle(prob).compute_rhs(prob.sol)
+    changed = np.abs(r1 - r0).max(axis=(1, 2)) > 1e-12
+    assert np.array_equal(changed, prob.mesh.ijk[:, 0] == 3)
+
+
+def test_total_tp_and_back_pressure_complex_step():
+    prob = P.euler_subsonic_duct(2, 3, 2)
+    o = oracle.Oracle(prob)
+    rng = np.random.default_rng(5)
+    base = prob.sol + 1e-2 * rng.standard_normal(prob.sol.shape)
+    dirn = rng.standard_normal(prob.sol.shape)
+    _, ri = o.compute_rhs_cmplx(base, 1e-30 * dirn)
+    eps = 1e-6
+    rp, _ = o.compute_rhs(base + eps * dirn)
+    rm, _ = o.compute_rhs(base - eps * dirn)
+    jv = ri / 1e-30
+    assert np.max(np.abs(jv - (rp - rm) / (2 * eps))) <= 1e-6 * np.max(np.abs(jv))
