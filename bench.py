@@ -386,6 +386,8 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "setup_s": setup_s,
     }
+    if prob.d == 3:
+        res["geometry"] = geometry_measurements(torch, prob, stream)
     if not args.no_adjoint and prob.pde == 3:
         res["adjoint"] = adjoint_measurements(torch, sim, prob, args)
     if not args.no_vortex:
@@ -397,6 +399,35 @@ def run_ours(args, rank, world, local_rank):
         res["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, workers=1)
     sim.close()
     return res
+
+
+def geometry_measurements(torch, prob, stream):
+    """Geometry precompute of the workload's mesh: the host restatement (numpy, TPGeometry) against the device
+    (dgpu_compute_geometry: coefficients in, the five factor arrays out, copies included), and context creation from
+    the host's factors against creation from the geometry coefficients alone."""
+    from dpgsolver_gb300.host.geometry import TPGeometry, sinusoidal_deform_3d
+    from dpgsolver_gb300.solver import Simulation, compute_geometry
+    t0 = time.perf_counter()
+    TPGeometry(prob.mesh, prob.ops, deform=sinusoidal_deform_3d(0.03, 10.0), curved=True)
+    host_s = time.perf_counter() - t0
+    compute_geometry(prob)                       # warm-up (module load, first launches)
+    t0 = time.perf_counter()
+    dev = compute_geometry(prob)
+    dev_s = time.perf_counter() - t0
+    g = prob.geom
+    diff = max(float(np.max(np.abs(dev[k] - getattr(g, k))) / np.max(np.abs(getattr(g, k))))
+               for k in ("metrics_vc", "jacobian_det_vc", "normals_fc", "jacobian_det_fc", "xyz_fc"))
+    times = {}
+    for name, flag in (("create_from_factors_s", False), ("create_from_geom_coef_s", True)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s = Simulation(prob, stream=stream.cuda_stream, device_geometry=flag)
+        torch.cuda.synchronize()
+        times[name] = time.perf_counter() - t0
+        s.close()
+    return {"host_numpy_s": host_s, "device_s": dev_s, "speedup": host_s / dev_s, "max_rel_diff": diff, **times,
+            "note": "host: TPGeometry of the same mesh (vectorised numpy, metric terms + faces); device: "
+                    "dgpu_compute_geometry incl. host<->device copies of coefficients and results"}
 
 
 def adjoint_measurements(torch, sim, prob, args):

@@ -14,7 +14,7 @@ REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 LIB_PATH = os.path.join(PKG_DIR, "libdgpu.so")
 SOURCES = ["dgpu.cu", "dgpu_batched.cu"]
-HEADERS = ["dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
+HEADERS = ["dgpu_geometry.cuh", "dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
            "dgpu_dense.cuh", "dgpu_jvp.cuh", "dgpu_host_ops.h"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
               "-Xcompiler", "-fPIC"]
@@ -93,7 +93,8 @@ class Mesh(ctypes.Structure):
     _fields_ = [("n_volumes", ctypes.c_int), ("metrics_vc", c_double_p), ("jacobian_det_vc", c_double_p),
                 ("n_faces", ctypes.c_int), ("face_vol", c_int_p), ("face_lf", c_int_p), ("nc_fc", c_int_p),
                 ("normals_fc", c_double_p), ("jacobian_det_fc", c_double_p), ("bc_fc", c_int_p),
-                ("bc_state_fc", c_double_p), ("bc_data", c_double_p)]
+                ("bc_state_fc", c_double_p), ("bc_data", c_double_p), ("p_g", ctypes.c_int),
+                ("geom_coef", c_double_p)]
 
 
 EXPORTS = {
@@ -101,6 +102,8 @@ EXPORTS = {
     "dgpu_create": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.POINTER(TPOperators), ctypes.POINTER(Mesh),
                                    ctypes.POINTER(ctypes.c_void_p)]),
     "dgpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dgpu_compute_geometry": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(TPOperators), ctypes.POINTER(Mesh),
+                                             c_double_p, c_double_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_state_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
     "dgpu_upload_state": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dgpu_download_state": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),

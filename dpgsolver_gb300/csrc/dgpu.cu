@@ -15,6 +15,7 @@
 #include "../../include/dgpu.h"
 #include "dgpu_tp.cuh"
 #include "dgpu_adjoint.cuh"
+#include "dgpu_geometry.cuh"
 #include "dgpu_jvp.cuh"
 #include "dgpu_host_ops.h"
 
@@ -466,6 +467,126 @@ cudaError_t upload(T** dst, const std::vector<T>& src)
 
 size_t state_size(const dgpu_ctx* c) { return (size_t)c->n_vol * c->nv * c->N; }
 
+// The geometry operators of a QUAD/HEX element of order p with geometry order p_g (the TP factors of the
+// reference's cv1_vg_vm, cv1_vg_vc, vv0_vm_vc and vv0_vm_fc), derived from their GLL and GL node sets, and the
+// reference normals of its local faces (element.c:708-780, with the same cos/sin round-off).
+void build_geo_ops(int d, int q, int p_g, const double* w_vc, GeoOps* G)
+{
+	memset(G, 0, sizeof *G);
+	G->d = d;
+	G->qg = p_g + 1;
+	G->q = q;
+	double xg[kQMax], xc[kQMax];
+	gauss_lobatto_nodes(G->qg, xg);
+	gauss_legendre_nodes(q, xc);
+	for (int a = 0; a < G->qg; ++a) {
+		for (int m = 0; m < G->qg; ++m)
+			G->Dgg[m][a] = lagrange_derivative(xg, G->qg, a, xg[m]);
+		for (int c = 0; c < q; ++c) {
+			G->Lgc[c][a] = lagrange_value(xg, G->qg, a, xc[c]);
+			G->Dgc[c][a] = lagrange_derivative(xg, G->qg, a, xc[c]);
+		}
+		G->Lgb[0][a] = lagrange_value(xg, G->qg, a, -1.0);
+		G->Lgb[1][a] = lagrange_value(xg, G->qg, a, 1.0);
+	}
+	const double t_z[6] = {M_PI, 0.0, 1.5 * M_PI, 0.5 * M_PI, 0.0, M_PI};
+	const double t_e[6] = {0.0, 0.0, 0.0, 0.0, 0.5 * M_PI, 1.5 * M_PI};
+	for (int lf = 0; lf < 2 * d; ++lf) {
+		G->nref[lf][0] = cos(t_e[lf]) * cos(t_z[lf]);
+		G->nref[lf][1] = cos(t_e[lf]) * sin(t_z[lf]);
+		G->nref[lf][2] = (d == 3 ? -sin(t_e[lf]) : 0.0);
+	}
+	for (int c = 0; c < q; ++c)
+		G->w[c] = w_vc[c];
+}
+
+// Volume then face geometry on the stream; out.metrics_vm and out.err must be device buffers (n_vol d^2 n_g doubles,
+// one int set to 0).
+cudaError_t run_geometry(const GeoOps& G, int n_vol, int n_face, const double* geom_coef, const int* face_vol,
+                         const int* face_lf, const GeoOut& out, cudaStream_t st)
+{
+	const size_t smem = kGeoSmem * sizeof(double);
+	cudaError_t e = cudaFuncSetAttribute(geo_volume_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e != cudaSuccess)
+		return e;
+	geo_volume_kernel<<<(unsigned)n_vol, 128, smem, st>>>(G, n_vol, geom_coef, out);
+	if ((e = cudaGetLastError()) != cudaSuccess)
+		return e;
+	const int nf = (G.d == 2 ? G.q : G.q * G.q);
+	const long long n_nodes = (long long)n_face * nf;
+	if (n_nodes > 0)
+		geo_face_kernel<<<(unsigned)((n_nodes + 127) / 128), 128, 0, st>>>(G, n_face, face_vol, face_lf, geom_coef,
+		                                                                   out);
+	return cudaGetLastError();
+}
+
+// Device buffers of one geometry computation: the coefficients and side-0 connectivity copied in, the vm metric
+// scratch and the error flag. The connectivity must have been checked on the host (side 0 in range).
+struct GeoBuffers {
+	double* geom = nullptr;
+	double* mvm = nullptr;
+	int* fv = nullptr;
+	int* flf = nullptr;
+	int* err = nullptr;
+	~GeoBuffers()
+	{
+		void* ptrs[] = {geom, mvm, fv, flf, err};
+		for (void* p : ptrs)
+			if (p)
+				cudaFree(p);
+	}
+	cudaError_t init(const dgpu_mesh* m, int d, cudaStream_t st)
+	{
+		const int qg = m->p_g + 1;
+		const size_t ng = (d == 2 ? qg * qg : qg * qg * qg), nv = (size_t)m->n_volumes, nf = (size_t)m->n_faces;
+		cudaError_t e;
+		if ((e = cudaMalloc((void**)&geom, nv * ng * d * sizeof(double))) ||
+		    (e = cudaMalloc((void**)&mvm, nv * ng * d * d * sizeof(double))) ||
+		    (e = cudaMalloc((void**)&fv, (nf > 0 ? nf : 1) * 2 * sizeof(int))) ||
+		    (e = cudaMalloc((void**)&flf, (nf > 0 ? nf : 1) * 2 * sizeof(int))) ||
+		    (e = cudaMalloc((void**)&err, sizeof(int))))
+			return e;
+		if ((e = cudaMemcpyAsync(geom, m->geom_coef, nv * ng * d * sizeof(double), cudaMemcpyHostToDevice, st)) ||
+		    (nf > 0 && (e = cudaMemcpyAsync(fv, m->face_vol, nf * 2 * sizeof(int), cudaMemcpyHostToDevice, st))) ||
+		    (nf > 0 && (e = cudaMemcpyAsync(flf, m->face_lf, nf * 2 * sizeof(int), cudaMemcpyHostToDevice, st))))
+			return e;
+		return cudaMemsetAsync(err, 0, sizeof(int), st);
+	}
+	// Runs the kernels into `out` (whose metrics_vm and err are set here) and returns the error flag.
+	cudaError_t run(const GeoOps& G, const dgpu_mesh* m, GeoOut out, cudaStream_t st, int* h_err)
+	{
+		out.metrics_vm = mvm;
+		out.err = err;
+		cudaError_t e = run_geometry(G, m->n_volumes, m->n_faces, geom, fv, flf, out, st);
+		if (e != cudaSuccess)
+			return e;
+		if ((e = cudaMemcpyAsync(h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+			return e;
+		return cudaStreamSynchronize(st);
+	}
+};
+
+// The context's gmet, inv_wJ and fgeo from the mesh's geometry coefficients.
+dgpu_status device_geometry(dgpu_ctx* c, const dgpu_tp_operators* ops, const dgpu_mesh* mesh)
+{
+	GeoOps G;
+	build_geo_ops(c->d, c->q, mesh->p_g, ops->w_vc, &G);
+	GeoBuffers B;
+	GeoOut out = {};
+	out.gmet = c->gmet;
+	out.inv_wJ = c->inv_wJ;
+	out.fgeo = c->fgeo;
+	int h_err = 0;
+	cudaError_t e = B.init(mesh, c->d, c->stream);
+	if (e == cudaSuccess)
+		e = B.run(G, mesh, out, c->stream, &h_err);
+	if (e != cudaSuccess)
+		return cuda_fail(nullptr, e, "device geometry");
+	if (h_err)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "non-positive Jacobian determinant (device geometry)");
+	return DGPU_OK;
+}
+
 // One residual (volume, face, lift) on the stream.
 dgpu_status enqueue_rhs(dgpu_ctx* c)
 {
@@ -582,9 +703,15 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL operator");
 	if (phys->pde == DGPU_PDE_EULER && phys->positivity && (!ops->ccSB0_vs_vs || !ops->ccBS0_vs_vs))
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "positivity needs ccSB0/ccBS0");
-	if (mesh->n_volumes < 1 || mesh->n_faces < 1 || !mesh->metrics_vc || !mesh->jacobian_det_vc ||
-	    !mesh->face_vol || !mesh->face_lf || !mesh->normals_fc || !mesh->jacobian_det_fc)
-		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "incomplete mesh");
+	// geometry: the geometric factors, or the geometry coefficients from which the device computes them
+	const bool dev_geo = mesh->geom_coef != nullptr;
+	const bool host_geo = mesh->metrics_vc && mesh->jacobian_det_vc && mesh->normals_fc && mesh->jacobian_det_fc;
+	if (mesh->n_volumes < 1 || mesh->n_faces < 1 || !mesh->face_vol || !mesh->face_lf || dev_geo == host_geo ||
+	    (dev_geo && (mesh->metrics_vc || mesh->jacobian_det_vc || mesh->normals_fc || mesh->jacobian_det_fc)))
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT,
+		            "incomplete mesh (give either the four geometric factor arrays or geom_coef)");
+	if (dev_geo && (mesh->p_g < 1 || mesh->p_g > kQMax - 1))
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "p_g must be in 1..4");
 
 	int dev = 0, n_dev = 0;
 	if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1)
@@ -639,8 +766,8 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 
 	// ---- volume geometry ----
 	const size_t nV = (size_t)c->n_vol;
-	std::vector<double> gmet(nV * d * d * N), inv_wJ(nV * N);
-	for (size_t v = 0; v < nV; ++v) {
+	std::vector<double> gmet(dev_geo ? 0 : nV * d * d * N), inv_wJ(dev_geo ? 0 : nV * N);
+	for (size_t v = 0; v < (dev_geo ? 0 : nV); ++v) {
 		const double* m = mesh->metrics_vc + v * (size_t)N * d * d;
 		const double* J = mesh->jacobian_det_vc + v * (size_t)N;
 		for (int j = 0; j < d; ++j)
@@ -658,7 +785,7 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 
 	// ---- faces ----
 	const size_t nF = (size_t)c->n_face;
-	std::vector<double> fgeo(nF * (d + 1) * NF);
+	std::vector<double> fgeo(dev_geo ? 0 : nF * (d + 1) * NF);
 	std::vector<int> vol_face(nV * 2 * d, -1);
 	bool any_perm = false;
 	std::vector<int> nc, nc_inv;
@@ -701,7 +828,7 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 				for (int i = 0; i < NF; ++i)
 					bc_ext.push_back(e[(size_t)i * c->nv + k]);
 		}
-		for (int i = 0; i < NF; ++i) {
+		for (int i = 0; i < (dev_geo ? 0 : NF); ++i) {
 			for (int k = 0; k < d; ++k)
 				fgeo[(f * (d + 1) + k) * NF + i] = mesh->normals_fc[(f * NF + i) * d + k];
 			fgeo[(f * (d + 1) + d) * NF + i] = wf[i] * mesh->jacobian_det_fc[f * NF + i];
@@ -755,9 +882,21 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 	DG_TRY(cudaMemset(c->max_bits, 0, sizeof(unsigned long long)));
 	DG_TRY(cudaMemset(c->err_flag, 0, sizeof(int)));
 	DG_TRY(cudaMemset(c->n_corr, 0, sizeof(unsigned long long)));
-	DG_TRY(upload(&c->gmet, gmet));
-	DG_TRY(upload(&c->inv_wJ, inv_wJ));
-	DG_TRY(upload(&c->fgeo, fgeo));
+	if (dev_geo) {
+		DG_TRY(cudaMalloc((void**)&c->gmet, nV * d * d * N * sizeof(double)));
+		DG_TRY(cudaMalloc((void**)&c->inv_wJ, nV * N * sizeof(double)));
+		DG_TRY(cudaMalloc((void**)&c->fgeo, nF * (d + 1) * NF * sizeof(double)));
+		const dgpu_status gs = device_geometry(c, ops, mesh);
+		if (gs != DGPU_OK) {
+			free_all(c);
+			delete c;
+			return gs;
+		}
+	} else {
+		DG_TRY(upload(&c->gmet, gmet));
+		DG_TRY(upload(&c->inv_wJ, inv_wJ));
+		DG_TRY(upload(&c->fgeo, fgeo));
+	}
 	DG_TRY(upload(&c->vol_face, vol_face));
 	if (any_perm) {
 		for (size_t f = 0; f < nF; ++f)   // boundary faces: unused entries, kept a permutation
@@ -1676,5 +1815,73 @@ extern "C" dgpu_status dgpu_adjoint_ssp_rk3(dgpu_ctx* c, double dt, int n_steps,
 	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
 	if (segment_out)
 		*segment_out = K;
+	return DGPU_OK;
+}
+
+extern "C" dgpu_status dgpu_compute_geometry(int d, const dgpu_tp_operators* ops, const dgpu_mesh* mesh,
+                                             double* metrics_vc, double* jacobian_det_vc, double* normals_fc,
+                                             double* jacobian_det_fc, double* xyz_fc)
+{
+	g_create_error.clear();
+	if (!ops || !mesh || !mesh->geom_coef || !ops->w_vc)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL argument (geom_coef and w_vc are needed)");
+	if ((d == 2 && ops->elem_type != DGPU_QUAD) || (d == 3 && ops->elem_type != DGPU_HEX) || (d != 2 && d != 3))
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "element type must be QUAD (d=2) or HEX (d=3)");
+	if (ops->p < 1 || ops->p > kQMax - 1 || mesh->p_g < 1 || mesh->p_g > kQMax - 1)
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "p and p_g must be in 1..4");
+	if (mesh->n_volumes < 1 || mesh->n_faces < 0 || (mesh->n_faces > 0 && (!mesh->face_vol || !mesh->face_lf)))
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "incomplete mesh");
+	for (int f = 0; f < mesh->n_faces; ++f)
+		if (mesh->face_vol[2 * f] < 0 || mesh->face_vol[2 * f] >= mesh->n_volumes || mesh->face_lf[2 * f] < 0 ||
+		    mesh->face_lf[2 * f] >= 2 * d)
+			return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "bad face connectivity (side 0)");
+	int n_dev = 0;
+	if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1)
+		return fail(nullptr, DGPU_ERR_NO_DEVICE, "no CUDA device");
+
+	const int q = ops->p + 1;
+	const size_t nv = (size_t)mesh->n_volumes, nf = (size_t)mesh->n_faces;
+	const size_t nc = (d == 2 ? q * q : q * q * q), nfc = (d == 2 ? q : q * q);
+	GeoOps G;
+	build_geo_ops(d, q, mesh->p_g, ops->w_vc, &G);
+	GeoBuffers B;
+	struct Result {
+		double* host;
+		size_t n;
+		double* dev;
+	} res[5] = {{metrics_vc, nv * d * d * nc, nullptr}, {jacobian_det_vc, nv * nc, nullptr},
+	            {normals_fc, nf * nfc * d, nullptr}, {jacobian_det_fc, nf * nfc, nullptr},
+	            {xyz_fc, nf * nfc * d, nullptr}};
+	cudaStream_t st = nullptr;
+	cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+	for (auto& r : res)
+		if (e == cudaSuccess && r.host && r.n > 0)
+			e = cudaMalloc((void**)&r.dev, r.n * sizeof(double));
+	if (e == cudaSuccess)
+		e = B.init(mesh, d, st);
+	int h_err = 0;
+	if (e == cudaSuccess) {
+		GeoOut out = {};
+		out.metrics_vc = res[0].dev;
+		out.jacobian_det_vc = res[1].dev;
+		out.normals_fc = res[2].dev;
+		out.jacobian_det_fc = res[3].dev;
+		out.xyz_fc = res[4].dev;
+		e = B.run(G, mesh, out, st, &h_err);
+	}
+	for (auto& r : res)
+		if (e == cudaSuccess && r.dev)
+			e = cudaMemcpyAsync(r.host, r.dev, r.n * sizeof(double), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(st);
+	for (auto& r : res)
+		if (r.dev)
+			cudaFree(r.dev);
+	if (st)
+		cudaStreamDestroy(st);
+	if (e != cudaSuccess)
+		return cuda_fail(nullptr, e, "dgpu_compute_geometry");
+	if (h_err)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "non-positive Jacobian determinant");
 	return DGPU_OK;
 }

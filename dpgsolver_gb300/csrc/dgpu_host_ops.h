@@ -145,6 +145,55 @@ inline double lagrange_value(const double* xn, int q, int i, double x)
 	return num / den;
 }
 
+// Derivative of the i-th Lagrange polynomial on nodes xn (q of them) at x.
+inline double lagrange_derivative(const double* xn, int q, int i, double x)
+{
+	double den = 1.0, s = 0.0;
+	for (int k = 0; k < q; ++k)
+		if (k != i)
+			den *= xn[i] - xn[k];
+	for (int j = 0; j < q; ++j) {
+		if (j == i)
+			continue;
+		double t = 1.0;
+		for (int k = 0; k < q; ++k)
+			if (k != i && k != j)
+				t *= x - xn[k];
+		s += t;
+	}
+	return s / den;
+}
+
+// Gauss-Lobatto-Legendre nodes (ascending, q >= 2): the end points and the roots of P_{q-1}', by Newton iteration on
+// (1 - x^2) P_n'(x), whose derivative is -n (n + 1) P_n(x), from the Chebyshev-Gauss-Lobatto points.
+inline void gauss_lobatto_nodes(int q, double* x)
+{
+	const int n = q - 1;
+	for (int i = 0; i < q; ++i)
+		x[i] = -cos(M_PI * i / n);
+	for (int i = 1; i < n; ++i) {
+		double z = x[i];
+		for (int it = 0; it < 100; ++it) {
+			double p, dp;
+			legendre(n, z, &p, &dp);
+			const double dz = ((1.0 - z * z) * dp) / (-n * (n + 1) * p);
+			z -= dz;
+			if (fabs(dz) < 1e-17)
+				break;
+		}
+		x[i] = z;
+	}
+	x[0] = -1.0;
+	x[n] = 1.0;
+	for (int i = 0; i < q / 2; ++i) {   // exact symmetry
+		const double s = 0.5 * (x[q - 1 - i] - x[i]);
+		x[i] = -s;
+		x[q - 1 - i] = s;
+	}
+	if (q % 2)
+		x[q / 2] = 0.0;
+}
+
 // B, B^-1, Dgl, l_gl(+-1), Bezier maps, positivity constants, transposes: see TPOps.
 inline bool derive_tp_ops(const dgpu_tp_operators* ops, int d, TPOps* out)
 {

@@ -26,10 +26,45 @@ def _ip(a):
     return a.ctypes.data_as(_lib.c_int_p)
 
 
-class Simulation:
-    """One dgpu context for a TP DGProblem (dpgsolver_gb300.host.problem)."""
+def _geom_coef(prob):
+    """Solver_Volume_T::geom_coef of every volume, (n_volumes, d, n_g): per volume the (n_g x d) column-major
+    block of the coordinates at the GLL geometry nodes."""
+    return np.ascontiguousarray(np.transpose(prob.geom.X_geom, (0, 2, 1)))
 
-    def __init__(self, prob, stream=None):
+
+def compute_geometry(prob):
+    """The geometric factors of a TP DGProblem computed on the device from its geometry coefficients
+    (dgpu_compute_geometry), in the layouts of prob.geom: metrics_vc (n_volumes, n_vc, d, d), jacobian_det_vc
+    (n_volumes, n_vc), normals_fc (n_faces, n_fc, d), jacobian_det_fc (n_faces, n_fc), xyz_fc (n_faces, n_fc, d)."""
+    lib = _lib.load()
+    ops, mesh, d = prob.ops, prob.mesh, prob.d
+    w = np.ascontiguousarray(ops.w_vc_1d, dtype=np.float64)
+    tp = _lib.TPOperators()
+    tp.elem_type, tp.p, tp.w_vc = ops.e_type, ops.p, _dp(w)
+    gc = _geom_coef(prob)
+    fv = np.ascontiguousarray(mesh.face_vol, dtype=np.int32)
+    flf = np.ascontiguousarray(mesh.face_lf, dtype=np.int32)
+    m = _lib.Mesh()
+    m.n_volumes, m.n_faces = mesh.n_volumes, mesh.n_faces
+    m.face_vol, m.face_lf = _ip(fv), _ip(flf)
+    m.p_g, m.geom_coef = prob.geom.p_g, _dp(gc)
+    nv, nf, nc, nfc = mesh.n_volumes, mesh.n_faces, ops.n_vc, ops.n_fc
+    met = np.empty((nv, d, d, nc))          # [v][j][i][c]: column-major (n_vc, d, d)
+    jac = np.empty((nv, nc))
+    nrm = np.empty((nf, nfc, d))
+    jf = np.empty((nf, nfc))
+    xyz = np.empty((nf, nfc, d))
+    check(lib.dgpu_compute_geometry(d, ctypes.byref(tp), ctypes.byref(m), _dp(met), _dp(jac), _dp(nrm), _dp(jf),
+                                    _dp(xyz)), None)
+    return {"metrics_vc": np.transpose(met, (0, 3, 2, 1)), "jacobian_det_vc": jac, "normals_fc": nrm,
+            "jacobian_det_fc": jf, "xyz_fc": xyz}
+
+
+class Simulation:
+    """One dgpu context for a TP DGProblem (dpgsolver_gb300.host.problem). device_geometry=True hands the library
+    the geometry coefficients instead of the host's geometric factors, and the device computes them."""
+
+    def __init__(self, prob, stream=None, device_geometry=False):
         lib = _lib.load()
         ops, mesh, geom = prob.ops, prob.mesh, prob.geom
         d = prob.d
@@ -55,15 +90,20 @@ class Simulation:
         tp.ccBS0_vs_vs = _dp(arr("bs", ops.ccBS0_1d))
         m = _lib.Mesh()
         m.n_volumes = mesh.n_volumes
-        m.metrics_vc = _dp(arr("m", np.transpose(geom.metrics_vc, (0, 3, 2, 1))))
-        m.jacobian_det_vc = _dp(arr("J", geom.jacobian_det_vc))
+        if device_geometry:
+            m.p_g = geom.p_g
+            m.geom_coef = _dp(arr("gc", _geom_coef(prob)))
+        else:
+            m.metrics_vc = _dp(arr("m", np.transpose(geom.metrics_vc, (0, 3, 2, 1))))
+            m.jacobian_det_vc = _dp(arr("J", geom.jacobian_det_vc))
         m.n_faces = mesh.n_faces
         m.face_vol = _ip(arr("fv", mesh.face_vol, np.int32))
         m.face_lf = _ip(arr("flf", mesh.face_lf, np.int32))
         nc = prob.nc_fc()
         m.nc_fc = _ip(arr("nc", nc, np.int32))
-        m.normals_fc = _dp(arr("nrm", geom.normals_fc))
-        m.jacobian_det_fc = _dp(arr("Jf", geom.jacobian_det_fc))
+        if not device_geometry:
+            m.normals_fc = _dp(arr("nrm", geom.normals_fc))
+            m.jacobian_det_fc = _dp(arr("Jf", geom.jacobian_det_fc))
         if getattr(prob, "bc", None) is not None:
             if np.size(prob.bc) != mesh.n_faces or np.size(prob.bc_state) != mesh.n_faces * ops.n_fc * prob.n_var:
                 raise ValueError("bc needs one code per face and bc_state (n_faces, n_fc, n_var) values")

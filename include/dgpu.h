@@ -108,6 +108,13 @@ typedef struct {
 	/* bc_data: 4 doubles {p_back, t_total, p_total, r_s}, the reference's BC_Data (boundary_euler_T.c:44-49, read
 	 * from the test case's input file there) for BC_BACKPRESSURE and BC_TOTAL_TP faces; NULL when none. */
 	const double* bc_data;
+	/* Geometry coefficients instead of the four geometric factor arrays (metrics_vc, jacobian_det_vc, normals_fc,
+	 * jacobian_det_fc all NULL): the device computes the factors (set_up_solver_geometry_T, geometry_T.c:165-185).
+	 * geom_coef: n_volumes x (n_g x d) column-major, Solver_Volume_T::geom_coef: the coordinates at the GLL nodes
+	 * of order p_g (n_g = (p_g+1)^d, first direction fastest); p_g = p for curved volumes, 1 for straight ones
+	 * (geometry_T.c:740-742). NULL when the factors are given. dgpu_create only. */
+	int p_g;
+	const double* geom_coef;
 } dgpu_mesh;
 
 /* Create a context on the current CUDA device and copy everything it needs; the caller may free its arrays
@@ -116,6 +123,21 @@ typedef struct {
 dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, const dgpu_mesh* mesh,
                         dgpu_ctx** out);
 dgpu_status dgpu_destroy(dgpu_ctx* ctx);
+
+/* Geometry precompute on the device, results in host buffers in dgpu_mesh's layouts (any output may be NULL):
+ * set_up_solver_geometry_T (geometry_T.c:165-185) for QUAD (d = 2) / HEX (d = 3) volumes of order ops->p from
+ * mesh->geom_coef and mesh->p_g, with the faces' side 0 (mesh->face_vol, face_lf) and their cubature nodes:
+ *   metrics_vc      n_volumes x (n_vc, d, d) column-major: the vm metric terms (2D cofactors, compute_cofactors_T
+ *                   geometry_T.c:546-590; 3D the conservative curl form) interpolated to the GL nodes (:734-801);
+ *   jacobian_det_vc n_volumes x n_vc: det of the Jacobian evaluated at the GL nodes;
+ *   normals_fc      n_faces x (n_fc x d) row-major, jacobian_det_fc n_faces x n_fc: side 0's vm metric terms at
+ *                   the face nodes times the reference normal, normalised / its length (:274-325, :412-445);
+ *   xyz_fc          n_faces x (n_fc x d) row-major: the face cubature nodes' coordinates (for constructor_sol_bv).
+ * Synchronous. DGPU_ERR_INVALID_ARGUMENT when a Jacobian determinant is not positive. Of ops only elem_type, p and
+ * w_vc are read. */
+dgpu_status dgpu_compute_geometry(int d, const dgpu_tp_operators* ops, const dgpu_mesh* mesh, double* metrics_vc,
+                                  double* jacobian_det_vc, double* normals_fc, double* jacobian_det_fc,
+                                  double* xyz_fc);
 
 dgpu_status dgpu_state_size(const dgpu_ctx* ctx, size_t* n_doubles);
 dgpu_status dgpu_upload_state(dgpu_ctx* ctx, const double* sol);      /* host -> device, synchronous */
