@@ -388,6 +388,8 @@ def run_ours(args, rank, world, local_rank):
     }
     if prob.d == 3:
         res["geometry"] = geometry_measurements(torch, prob, stream)
+    if prob.d == 3 and not args.no_jacobian:
+        res["jacobian"] = jacobian_measurements(torch, stream, args)
     if not args.no_adjoint and prob.pde == 3:
         res["adjoint"] = adjoint_measurements(torch, sim, prob, args)
     if not args.no_vortex:
@@ -428,6 +430,45 @@ def geometry_measurements(torch, prob, stream):
     return {"host_numpy_s": host_s, "device_s": dev_s, "speedup": host_s / dev_s, "max_rel_diff": diff, **times,
             "note": "host: TPGeometry of the same mesh (vectorised numpy, metric terms + faces); device: "
                     "dgpu_compute_geometry incl. host<->device copies of coefficients and results"}
+
+
+def jacobian_measurements(torch, stream, args):
+    """Block-sparse Jacobian assembly (dgpu_jacobian_bsr, raw residual = the reference's lhs) on the 8^3 HEX p3
+    Euler mesh into device memory, against the oracle's complex-step Jacobian, whose cost is one complex residual per
+    column: that rate is sampled and extrapolated to every column (the full CPU run would take hours)."""
+    import oracle
+    from dpgsolver_gb300.host import problem as P
+    from dpgsolver_gb300.solver import Simulation
+    prob = P.euler_hex_3d(8, 3)
+    base = prob.sol
+    with Simulation(prob, stream=stream.cuda_stream) as sim:
+        nb, nnz, n_col = sim.jacobian_structure()
+        dev = torch.empty((nnz, nb, nb), dtype=torch.float64, device="cuda")
+        sim.jacobian(base, raw=True, values_ptr=dev.data_ptr())      # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.jacobian(base, raw=True, values_ptr=dev.data_ptr())
+        torch.cuda.synchronize()
+        gpu_s = time.perf_counter() - t0
+        del dev
+    res = {"workload": "3D Euler curved HEX 8^3 p3 Lax-Friedrichs, raw residual (the reference's lhs)",
+           "block_size": nb, "n_blocks": nnz, "n_colours": n_col, "directional_derivatives": n_col * nb,
+           "bytes": nnz * nb * nb * 8, "gpu_s": gpu_s, "blocks_per_s": nnz / gpu_s}
+    if not args.no_cpu_baseline:
+        o = oracle.Oracle(prob)
+        e = np.zeros(prob.sol.shape)
+        e.flat[0] = 1e-30
+        o.compute_rhs_cmplx(base, e)
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < 5.0:
+            o.compute_rhs_cmplx(base, e)
+            k += 1
+        per_col = (time.perf_counter() - t0) / k
+        res["cpu_complex_step"] = {"s_per_column": per_col, "columns": prob.n_state,
+                                   "extrapolated_s": per_col * prob.n_state, "cores": 1, "kind": "port",
+                                   "sample": f"{k} complex residual evaluations of the oracle on the same mesh"}
+    return res
 
 
 def adjoint_measurements(torch, sim, prob, args):
@@ -738,6 +779,7 @@ def main():
                     help="time compute_rhs_dg only (device-resident; profiling)")
     ap.add_argument("--only-rk", action="store_true", help="time graph-replayed SSP-RK3 steps only (profiling)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurements")
+    ap.add_argument("--no-jacobian", action="store_true", help="skip the block-sparse Jacobian assembly")
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-budget-gb", type=float, default=4.0)
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched mixed-order measurements")

@@ -14,7 +14,7 @@ REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 LIB_PATH = os.path.join(PKG_DIR, "libdgpu.so")
 SOURCES = ["dgpu.cu", "dgpu_batched.cu"]
-HEADERS = ["dgpu_geometry.cuh", "dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
+HEADERS = ["dgpu_geometry.cuh", "dgpu_jacobian.cuh", "dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
            "dgpu_dense.cuh", "dgpu_jvp.cuh", "dgpu_host_ops.h"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
               "-Xcompiler", "-fPIC"]
@@ -102,6 +102,10 @@ EXPORTS = {
     "dgpu_create": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.POINTER(TPOperators), ctypes.POINTER(Mesh),
                                    ctypes.POINTER(ctypes.c_void_p)]),
     "dgpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dgpu_jacobian_structure": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                               ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)]),
+    "dgpu_jacobian_bsr": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int, c_int_p, c_int_p,
+                                         ctypes.c_void_p]),
     "dgpu_compute_geometry": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(TPOperators), ctypes.POINTER(Mesh),
                                              c_double_p, c_double_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_state_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),

@@ -9,6 +9,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -16,6 +17,7 @@
 #include "dgpu_tp.cuh"
 #include "dgpu_adjoint.cuh"
 #include "dgpu_geometry.cuh"
+#include "dgpu_jacobian.cuh"
 #include "dgpu_jvp.cuh"
 #include "dgpu_host_ops.h"
 
@@ -50,6 +52,11 @@ struct dgpu_ctx {
 	double* obj_contrib = nullptr;        // per objective face node: w_f J_f p
 	// forward-mode linearisation (allocated on first use): tangent state, volume term, traces, face fluxes, product
 	double *jv_du = nullptr, *jv_vol = nullptr, *jv_traces = nullptr, *jv_nnf = nullptr, *jv_out = nullptr;
+	// block-sparse Jacobian (built on first use): block rows, colouring, block slot of (volume, colour)
+	std::vector<int> h_face_vol;          // host copy of face_vol
+	int jac_colours = 0;
+	std::vector<int> jac_row_ptr, jac_col_idx, jac_members_off;
+	int *jac_slot = nullptr, *jac_members = nullptr;
 	bool coef_valid = true, gl_valid = false;   // which of u / ug holds the current state
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
@@ -79,6 +86,8 @@ struct dgpu_ctx {
 	cudaError_t (*launch_adjoint)(dgpu_ctx*, const double* u, const double* rbar, double* ubar) = nullptr;
 	cudaError_t (*launch_objective)(dgpu_ctx*, double* ubar) = nullptr;   // needs traces of the state
 	cudaError_t (*launch_jvp)(dgpu_ctx*) = nullptr;   // R(u) into rhs and (dR/du) jv_du into jv_out
+	cudaError_t (*launch_jvp_tangent)(dgpu_ctx*) = nullptr;   // (dR/du) jv_du into jv_out only
+	cudaError_t (*launch_mass)(dgpu_ctx*, const double* in, double* out) = nullptr;   // out = M in per volume
 	// optional per-kernel timing (eager launches only)
 	bool timing = false;
 	std::vector<KernelTimer> timers;
@@ -346,7 +355,9 @@ size_t jvp_volume_smem_bytes()
 
 // R(u) and the directional derivative along jv_du: tangent-carrying volume and face kernels, then the residual-mode
 // lift on the primal buffers and on the tangent buffers (the lift is linear).
-template <int D, int Q, int NV, int PDE, int FLUX>
+// PRIMAL = false: the derivative only (the primal volume and face quantities are still formed, the primal lift is
+// skipped and rhs is left as it was).
+template <int D, int Q, int NV, int PDE, int FLUX, bool PRIMAL>
 cudaError_t launch_jvp_t(dgpu_ctx* c)
 {
 	using S = TPShape<D, Q>;
@@ -357,7 +368,7 @@ cudaError_t launch_jvp_t(dgpu_ctx* c)
 	Pd.traces = c->jv_traces;
 	Pd.nnf = c->jv_nnf;
 	Pd.max_bits = nullptr;
-	cudaError_t e = cudaMemsetAsync(c->max_bits, 0, sizeof(unsigned long long), c->stream);
+	cudaError_t e = PRIMAL ? cudaMemsetAsync(c->max_bits, 0, sizeof(unsigned long long), c->stream) : cudaSuccess;
 	if (e != cudaSuccess)
 		return e;
 	tp_jvp_volume_kernel<D, Q, NV, PDE><<<blocks, S::THREADS, jvp_volume_smem_bytes<D, Q, NV>(), c->stream>>>(
@@ -372,10 +383,23 @@ cudaError_t launch_jvp_t(dgpu_ctx* c)
 	rk.stage = 0;
 	rk.positivity = 0;
 	rk.want_max = 1;
-	tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, P, rk);
+	if (PRIMAL)
+		tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, P,
+		                                                                                                   rk);
 	rk.rhs = c->jv_out;
 	tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, Pd, rk);
-	c->launches += 4;
+	c->launches += PRIMAL ? 4 : 3;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV>
+cudaError_t launch_mass_t(dgpu_ctx* c, const double* in, double* out)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	tp_mass_kernel<D, Q, NV><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, c->params(), in,
+	                                                                                       out);
+	c->launches++;
 	return cudaGetLastError();
 }
 
@@ -384,7 +408,9 @@ cudaError_t bind(dgpu_ctx* c)
 {
 	c->launch_adjoint = launch_adjoint_t<D, Q, NV, PDE, FLUX>;
 	c->launch_objective = launch_objective_t<D, Q, NV>;
-	c->launch_jvp = launch_jvp_t<D, Q, NV, PDE, FLUX>;
+	c->launch_jvp = launch_jvp_t<D, Q, NV, PDE, FLUX, true>;
+	c->launch_jvp_tangent = launch_jvp_t<D, Q, NV, PDE, FLUX, false>;
+	c->launch_mass = launch_mass_t<D, Q, NV>;
 	c->launch_volume = launch_volume_t<D, Q, NV, PDE, true>;
 	c->launch_volume_gl = launch_volume_t<D, Q, NV, PDE, false>;
 	c->launch_face = launch_face_t<D, Q, NV, PDE, FLUX>;
@@ -408,6 +434,8 @@ cudaError_t bind(dgpu_ctx* c)
 	if ((e = cudaFuncSetAttribute(tp_adj_volume_kernel<D, Q, NV, PDE>, smem, (int)adj_volume_smem_bytes<D, Q, NV>())))
 		return e;
 	if ((e = cudaFuncSetAttribute(tp_adj_lift_kernel<D, Q, NV>, smem, (int)convert_smem_bytes<D, Q, NV>())))
+		return e;
+	if ((e = cudaFuncSetAttribute(tp_mass_kernel<D, Q, NV>, smem, (int)lift_smem_bytes<D, Q, NV>())))
 		return e;
 	if ((e = cudaFuncSetAttribute(tp_jvp_volume_kernel<D, Q, NV, PDE>, smem, (int)jvp_volume_smem_bytes<D, Q, NV>())))
 		return e;
@@ -448,6 +476,7 @@ void free_all(dgpu_ctx* c)
 	}
 	c->timers.clear();
 	void* ptrs[] = {c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
+	                c->jac_slot, c->jac_members,
 	                c->bnd, c->bc_code, c->bc_ext, c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -846,6 +875,7 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 			}
 		}
 	}
+	c->h_face_vol.assign(mesh->face_vol, mesh->face_vol + 2 * nF);
 	for (size_t i = 0; i < vol_face.size(); ++i)
 		if (vol_face[i] < 0) {
 			delete c;
@@ -1554,10 +1584,10 @@ dgpu_status ensure_adjoint_buffers(dgpu_ctx* c)
 
 }  // namespace
 
-extern "C" dgpu_status dgpu_jvp(dgpu_ctx* c, const double* sol, const double* dir, double* rhs, double* jv)
+namespace {
+
+dgpu_status ensure_jvp_buffers(dgpu_ctx* c)
 {
-	if (!c || !sol || !dir || !jv)
-		return DGPU_ERR_INVALID_ARGUMENT;
 	const size_t ns = state_size(c);
 	const size_t nt = (size_t)c->n_face * 2 * c->nv * c->NF;
 	if (!c->jv_du) {
@@ -1566,6 +1596,172 @@ extern "C" dgpu_status dgpu_jvp(dgpu_ctx* c, const double* sol, const double* di
 		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_out, ns * sizeof(double)));
 		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_traces, nt * sizeof(double)));
 		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_nnf, nt / 2 * sizeof(double)));
+	}
+	return DGPU_OK;
+}
+
+// Block rows (volume v: itself and its face neighbours, ascending, each once), a greedy distance-2 colouring (no
+// block row holds two volumes of one colour) and, per (volume, colour), the slot of the block whose column volume
+// has that colour (-1 when none).
+dgpu_status jacobian_setup(dgpu_ctx* c)
+{
+	if (c->jac_colours > 0)
+		return DGPU_OK;
+	const int nV = c->n_vol;
+	std::vector<std::vector<int>> cols(nV);
+	for (int v = 0; v < nV; ++v)
+		cols[v].push_back(v);
+	for (int f = 0; f < c->n_face; ++f) {
+		const int a = c->h_face_vol[2 * f], b = c->h_face_vol[2 * f + 1];
+		if (b < 0)
+			continue;   // boundary face: no coupling
+		cols[a].push_back(b);
+		cols[b].push_back(a);
+	}
+	c->jac_row_ptr.assign(nV + 1, 0);
+	c->jac_col_idx.clear();
+	for (int v = 0; v < nV; ++v) {
+		std::sort(cols[v].begin(), cols[v].end());
+		cols[v].erase(std::unique(cols[v].begin(), cols[v].end()), cols[v].end());
+		c->jac_row_ptr[v + 1] = c->jac_row_ptr[v] + (int)cols[v].size();
+		c->jac_col_idx.insert(c->jac_col_idx.end(), cols[v].begin(), cols[v].end());
+	}
+	std::vector<int> colour(nV, -1), stamp;
+	int n_col = 0;
+	for (int v = 0; v < nV; ++v) {
+		for (int r : cols[v])          // the rows that hold v ...
+			for (int y : cols[r])      // ... and every volume in them
+				if (colour[y] >= 0)
+					stamp[colour[y]] = v + 1;
+		int k = 0;
+		while (k < n_col && stamp[k] == v + 1)
+			++k;
+		if (k == n_col) {
+			++n_col;
+			stamp.push_back(0);
+		}
+		colour[v] = k;
+	}
+	std::vector<int> slot((size_t)nV * n_col, -1);
+	for (int v = 0; v < nV; ++v)
+		for (int j = c->jac_row_ptr[v]; j < c->jac_row_ptr[v + 1]; ++j) {
+			int& s = slot[(size_t)v * n_col + colour[c->jac_col_idx[j]]];
+			if (s != -1)
+				return fail(c, DGPU_ERR_INVALID_ARGUMENT, "internal: colouring is not distance-2");
+			s = j;
+		}
+	c->jac_members_off.assign(n_col + 1, 0);
+	for (int v = 0; v < nV; ++v)
+		++c->jac_members_off[colour[v] + 1];
+	for (int k = 0; k < n_col; ++k)
+		c->jac_members_off[k + 1] += c->jac_members_off[k];
+	std::vector<int> members(nV), fill(c->jac_members_off.begin(), c->jac_members_off.end() - 1);
+	for (int v = 0; v < nV; ++v)
+		members[fill[colour[v]]++] = v;
+	DGPU_CUDA(c, upload(&c->jac_slot, slot));
+	DGPU_CUDA(c, upload(&c->jac_members, members));
+	c->jac_colours = n_col;
+	return DGPU_OK;
+}
+
+}  // namespace
+
+extern "C" dgpu_status dgpu_jacobian_structure(dgpu_ctx* c, int* block_size, long long* n_blocks, int* n_colours)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	const dgpu_status st = jacobian_setup(c);
+	if (st != DGPU_OK)
+		return st;
+	if (block_size)
+		*block_size = c->nv * c->N;
+	if (n_blocks)
+		*n_blocks = (long long)c->jac_col_idx.size();
+	if (n_colours)
+		*n_colours = c->jac_colours;
+	return DGPU_OK;
+}
+
+extern "C" dgpu_status dgpu_jacobian_bsr(dgpu_ctx* c, const double* sol, int raw, int* row_ptr, int* col_idx,
+                                         double* values)
+{
+	if (!c || !sol)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	dgpu_status st = jacobian_setup(c);
+	if (st == DGPU_OK)
+		st = ensure_jvp_buffers(c);
+	if (st != DGPU_OK)
+		return st;
+	if (row_ptr)
+		memcpy(row_ptr, c->jac_row_ptr.data(), c->jac_row_ptr.size() * sizeof(int));
+	if (col_idx)
+		memcpy(col_idx, c->jac_col_idx.data(), c->jac_col_idx.size() * sizeof(int));
+	if (!values)
+		return DGPU_OK;
+	const int nb = c->nv * c->N, n_col = c->jac_colours;
+	const size_t n_vals = c->jac_col_idx.size() * (size_t)nb * nb, ns = state_size(c);
+	cudaPointerAttributes pa;
+	bool dev_out = false;
+	if (cudaPointerGetAttributes(&pa, values) == cudaSuccess)
+		dev_out = (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged);
+	else
+		cudaGetLastError();
+	double* vals = values;
+	double* mass_out = nullptr;
+	if (!dev_out) {
+		cudaError_t e = cudaMalloc((void**)&vals, n_vals * sizeof(double));
+		if (e != cudaSuccess)
+			return fail(c, DGPU_ERR_CUDA, "dgpu_jacobian_bsr: no device memory for the staging copy of " +
+			                                  std::to_string(n_vals * sizeof(double)) + " bytes of blocks");
+	}
+	cudaError_t e = raw ? cudaMalloc((void**)&mass_out, ns * sizeof(double)) : cudaSuccess;
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(c->u, sol, ns * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+	if (e == cudaSuccess)
+		e = cudaMemsetAsync(c->jv_du, 0, ns * sizeof(double), c->stream);
+	c->coef_valid = true;
+	c->gl_valid = false;
+	const long long nrows = (long long)c->n_vol * nb;
+	for (int col = 0; col < n_col && e == cudaSuccess; ++col) {
+		const int m0 = c->jac_members_off[col], nm = c->jac_members_off[col + 1] - m0;
+		const unsigned gs = (unsigned)((nm + 255) / 256), gr = (unsigned)((nrows + 255) / 256);
+		for (int k = 0; k < nb && e == cudaSuccess; ++k) {
+			jac_seed_kernel<<<gs, 256, 0, c->stream>>>(c->jv_du, c->jac_members + m0, nm, nb, k, 1.0);
+			e = c->launch_jvp_tangent(c);
+			const double* jv = c->jv_out;
+			if (e == cudaSuccess && raw) {
+				e = c->launch_mass(c, c->jv_out, mass_out);
+				jv = mass_out;
+			}
+			jac_scatter_kernel<<<gr, 256, 0, c->stream>>>(jv, c->jac_slot, n_col, col, c->n_vol, nb, k, vals);
+			jac_seed_kernel<<<gs, 256, 0, c->stream>>>(c->jv_du, c->jac_members + m0, nm, nb, k, 0.0);
+			c->launches += 3;
+			if (e == cudaSuccess)
+				e = cudaGetLastError();
+		}
+	}
+	if (e == cudaSuccess && !dev_out)
+		e = cudaMemcpyAsync(values, vals, n_vals * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(c->stream);
+	if (!dev_out)
+		cudaFree(vals);
+	if (mass_out)
+		cudaFree(mass_out);
+	if (e != cudaSuccess)
+		return cuda_fail(c, e, "dgpu_jacobian_bsr");
+	return DGPU_OK;
+}
+
+extern "C" dgpu_status dgpu_jvp(dgpu_ctx* c, const double* sol, const double* dir, double* rhs, double* jv)
+{
+	if (!c || !sol || !dir || !jv)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	const size_t ns = state_size(c);
+	{
+		const dgpu_status st = ensure_jvp_buffers(c);
+		if (st != DGPU_OK)
+			return st;
 	}
 	const size_t bytes = ns * sizeof(double);
 	DGPU_CUDA(c, cudaMemcpyAsync(c->u, sol, bytes, cudaMemcpyHostToDevice, c->stream));

@@ -200,6 +200,30 @@ class Simulation:
         check(self._lib.dgpu_jvp(self._h, _dp(s), _dp(d), _dp(r), _dp(jv)), self._h)
         return r, jv
 
+    def jacobian_structure(self):
+        """(block_size, n_blocks, n_colours) of the block-sparse Jacobian (dgpu_jacobian_structure)."""
+        nb, nnz, nc = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_int()
+        check(self._lib.dgpu_jacobian_structure(self._h, ctypes.byref(nb), ctypes.byref(nnz), ctypes.byref(nc)),
+              self._h)
+        return nb.value, nnz.value, nc.value
+
+    def jacobian(self, sol, raw=True, values_ptr=None):
+        """Block-sparse Jacobian at sol (dgpu_jacobian_bsr): (row_ptr, col_idx, values) with values
+        (n_blocks, block_size, block_size), row-major blocks in the reference's lhs layout. raw: of the residual
+        before M^-1 (the reference's lhs) or of the explicit right-hand side. values_ptr: a device address of
+        n_blocks * block_size^2 doubles to write the blocks to instead (values is then None)."""
+        s = np.ascontiguousarray(sol, dtype=np.float64)
+        if s.shape != self.shape:
+            raise ValueError(f"state shape {s.shape} != {self.shape}")
+        nb, nnz, _ = self.jacobian_structure()
+        row_ptr = np.empty(self.prob.n_volumes + 1, dtype=np.int32)
+        col_idx = np.empty(nnz, dtype=np.int32)
+        vals = None if values_ptr is not None else np.empty((nnz, nb, nb))
+        ptr = ctypes.c_void_p(values_ptr) if values_ptr is not None else vals.ctypes.data_as(ctypes.c_void_p)
+        check(self._lib.dgpu_jacobian_bsr(self._h, _dp(s), 1 if raw else 0, _ip(row_ptr), _ip(col_idx), ptr),
+              self._h)
+        return row_ptr, col_idx, vals
+
     def vjp_backward(self, cotangent):
         """(dR/dsol)^T cotangent at the state kept by vjp_forward."""
         v = np.ascontiguousarray(cotangent, dtype=np.float64)

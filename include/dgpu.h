@@ -192,6 +192,25 @@ dgpu_status dgpu_vjp_backward(dgpu_ctx* ctx, const double* cotangent, double* gr
  * product without a step size. Kinks of the fluxes take the derivative of the branch the value takes. */
 dgpu_status dgpu_jvp(dgpu_ctx* ctx, const double* sol, const double* dir, double* rhs, double* jv);
 
+/* Block-sparse Jacobian of the residual at sol, the matrix the reference assembles for its implicit solver block by
+ * block (constructor_lhs_v_1_T, compute_volume_rlhs_T.c:179-220; constructor_lhs_f_1_T, compute_face_rlhs_T.c:163-220)
+ * and adds to PETSc (add_to_petsc_Mat, solve.c:321-338). Block row v = volume v; its blocks are the volume itself
+ * and its face neighbours, ascending, each once (boundary faces couple nothing). A block is block_size x block_size,
+ * block_size = n_var * n_vs, row-major, row eq * n_vs + i (residual of equation eq at basis function i), column
+ * var * n_vs + j: the reference's lhs layout. raw = 1: the derivative of the residual before M^-1 (the reference's
+ * lhs, whose right-hand side compute_rlhs_dg leaves unscaled); raw = 0: of the explicit right-hand side
+ * (M^-1 applied, the operator of dgpu_compute_rhs and dgpu_jvp).
+ * dgpu_jacobian_structure: block_size, the number of blocks and of colours (any output may be NULL); the structure
+ *   and the colouring are built on the first call of either entry and kept.
+ * dgpu_jacobian_bsr: sol (host, state layout) becomes the context's state; row_ptr (n_volumes + 1), col_idx
+ *   (n_blocks) are host buffers and may be NULL; values (n_blocks * block_size^2 doubles) may be NULL (structure only),
+ *   device memory of the context's device (written in place) or host memory (staged through a device buffer of the
+ *   same size for the call). Computed as n_colours * block_size directional derivatives of the JVP kernels, one per
+ *   (colour, local unknown), each giving one column of every block whose column volume has that colour. */
+dgpu_status dgpu_jacobian_structure(dgpu_ctx* ctx, int* block_size, long long* n_blocks, int* n_colours);
+dgpu_status dgpu_jacobian_bsr(dgpu_ctx* ctx, const double* sol, int raw, int* row_ptr, int* col_idx,
+                              double* values);
+
 /* Output functional for the adjoint: J(sol) = sum over the listed faces of the integral of pressure on side 0
  * (sum over face cubature nodes of w_fc J_fc p(W_L)), e.g. the faces of the plane z = 0. Euler only. The
  * reference computes such integrals as error functionals (src/simulation/test_case/compute_error/) but has no
