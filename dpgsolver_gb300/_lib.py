@@ -13,7 +13,7 @@ PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 LIB_PATH = os.path.join(PKG_DIR, "libdgpu.so")
-SOURCES = ["dgpu.cu", "dgpu_batched.cu"]
+SOURCES = ["dgpu.cu", "dgpu_batched.cu", "dgpu_mesh_io.cpp"]
 HEADERS = ["dgpu_geometry.cuh", "dgpu_jacobian.cuh", "dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
            "dgpu_dense.cuh", "dgpu_jvp.cuh", "dgpu_host_ops.h"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
@@ -32,7 +32,8 @@ def _stale() -> bool:
     if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(REPO_DIR, "include", "dgpu.h")]
+    deps = [os.path.join(CSRC, f) for f in SOURCES + HEADERS] + [os.path.join(REPO_DIR, "include", h)
+                                                                           for h in ("dgpu.h", "dgpu_mesh.h")]
     return any(os.path.getmtime(p) > t for p in deps)
 
 
@@ -89,6 +90,11 @@ class Group(ctypes.Structure):
     _fields_ = [("tp", ctypes.POINTER(TPOperators)), ("dense", ctypes.POINTER(DenseOperators))]
 
 
+class GmshSizes(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("d", "n_nodes", "n_elements", "n_node_nums", "n_periodic", "n_volumes",
+                                             "n_volume_faces", "n_ve_bc", "n_faces", "has_periodic")]
+
+
 class Mesh(ctypes.Structure):
     _fields_ = [("n_volumes", ctypes.c_int), ("metrics_vc", c_double_p), ("jacobian_det_vc", c_double_p),
                 ("n_faces", ctypes.c_int), ("face_vol", c_int_p), ("face_lf", c_int_p), ("nc_fc", c_int_p),
@@ -102,6 +108,15 @@ EXPORTS = {
     "dgpu_create": (ctypes.c_int, [ctypes.POINTER(Physics), ctypes.POINTER(TPOperators), ctypes.POINTER(Mesh),
                                    ctypes.POINTER(ctypes.c_void_p)]),
     "dgpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dgpu_gmsh_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "dgpu_gmsh_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dgpu_gmsh_last_error": (ctypes.c_char_p, []),
+    "dgpu_gmsh_get_sizes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GmshSizes)]),
+    "dgpu_gmsh_data": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p,
+                                      c_int_p]),
+    "dgpu_gmsh_connectivity": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p]),
+    "dgpu_gmsh_vertices": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p]),
+    "dgpu_gmsh_faces": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     "dgpu_jacobian_structure": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
                                                ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)]),
     "dgpu_jacobian_bsr": (ctypes.c_int, [ctypes.c_void_p, c_double_p, ctypes.c_int, c_int_p, c_int_p,

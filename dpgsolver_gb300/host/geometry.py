@@ -34,10 +34,13 @@ def apply_nodes(op: np.ndarray, x: np.ndarray) -> np.ndarray:
 
 
 class TPGeometry:
-    def __init__(self, mesh, ops: TPOperatorSet, deform=None, curved: bool | None = None, vols=None):
+    def __init__(self, mesh, ops: TPOperatorSet, deform=None, curved: bool | None = None, vols=None, coef=None):
         """deform: callable (m, d) physical -> (m, d) physical applied to the affine element map, or None.
         vols: indices of the volumes to compute (all volumes and their faces when None; the volume terms only
-        otherwise, as for one (type, p) group of a mixed-order mesh)."""
+        otherwise, as for one (type, p) group of a mixed-order mesh).
+        coef: the geometry coefficients themselves, (n_volumes, n_g, d) coordinates at the GLL nodes of order p_g
+        (p when curved, else 1; for straight volumes the vertices in the reference's order), instead of the affine
+        box map and deform (Solver_Volume_T::geom_coef of a mesh read from a file)."""
         d = mesh.d
         self.d = d
         if curved is None:
@@ -47,15 +50,23 @@ class TPGeometry:
         self.p_g = p_g
         x_g, _ = gauss_lobatto(p_g + 1)
         xi_g = tp_nodes(x_g, d)                      # geometry == metric nodes (p_m = p_g)
-        lo = mesh.vertices_lo if vols is None else mesh.vertices_lo[np.asarray(vols)]
-        nv = len(lo)
         n_g = len(xi_g)
         self.x_g = x_g
 
         # geometry node coordinates (nv, n_g, d)
-        X = lo[:, None, :] + 0.5 * (xi_g[None, :, :] + 1.0) * mesh.h[None, None, :]
-        if deform is not None:
-            X = deform(X.reshape(-1, d)).reshape(nv, n_g, d)
+        if coef is not None:
+            X = np.asarray(coef, dtype=np.float64)
+            if vols is not None:
+                X = X[np.asarray(vols)]
+            if X.shape[1:] != (n_g, d):
+                raise ValueError(f"geometry coefficients of shape {X.shape[1:]}, expected {(n_g, d)}")
+            nv = len(X)
+        else:
+            lo = mesh.vertices_lo if vols is None else mesh.vertices_lo[np.asarray(vols)]
+            nv = len(lo)
+            X = lo[:, None, :] + 0.5 * (xi_g[None, :, :] + 1.0) * mesh.h[None, None, :]
+            if deform is not None:
+                X = deform(X.reshape(-1, d)).reshape(nv, n_g, d)
         self.X_geom = X
 
         L_gg = lagrange_matrix(x_g, x_g)

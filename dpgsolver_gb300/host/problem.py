@@ -63,7 +63,10 @@ class DGProblem:
         return int(self.sol.size)
 
     def nc_fc(self) -> np.ndarray:
-        """Right-trace gather permutation per face (identity for these aligned structured meshes)."""
+        """Right-trace gather permutation per face: the mesh's own (a mesh read from a file, whose neighbouring
+        volumes may see a face in different orientations), else the identity (aligned structured meshes)."""
+        if hasattr(self.mesh, "nc_fc"):
+            return self.mesh.nc_fc(self.ops.q)
         return np.tile(np.arange(self.ops.n_fc, dtype=np.int32), (self.mesh.n_faces, 1))
 
     def faces_on_plane(self, axis: int = 2) -> np.ndarray:

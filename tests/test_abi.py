@@ -1,4 +1,4 @@
-"""The C-ABI library builds for sm_103a, loads without a GPU and exports every symbol include/dgpu.h declares."""
+"""The C-ABI library builds for sm_103a, loads without a GPU and exports every symbol include/*.h declares."""
 import ctypes
 import os
 import re
@@ -8,11 +8,11 @@ import pytest
 import dpgsolver_gb300
 from dpgsolver_gb300 import _lib
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "dgpu.h")
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
 
 
 def declared_functions():
-    text = open(HEADER).read()
+    text = "".join(open(os.path.join(INCLUDE, h)).read() for h in sorted(os.listdir(INCLUDE)) if h.endswith(".h"))
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(dgpu_[a-z0-9_]+)\s*\(", text)))
 
