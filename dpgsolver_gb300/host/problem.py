@@ -24,6 +24,9 @@ from .mesh import StructuredMesh
 
 PDE_ADVECTION = 1
 PDE_EULER = 3
+PDE_NAVIER_STOKES = 4
+VISCOSITY_CONSTANT = 101
+VISCOSITY_SUTHERLAND = 102
 NUM_FLUX_UPWIND = 11
 NUM_FLUX_ROE_PIKE = 31
 NUM_FLUX_LAX_FRIEDRICHS = 32
@@ -49,6 +52,7 @@ class DGProblem:
     bc: np.ndarray | None = None          # (n_faces,) BC code of each face (definitions_bc.h), 0 on interior faces
     bc_state: np.ndarray | None = None    # (n_faces, n_fc, n_var) exterior conserved state at the face nodes
     bc_data: tuple | None = None          # (p_back, t_total, p_total, r_s): BC_Data of boundary_euler_T.c:44-49
+    ns: dict | None = None                # Navier-Stokes: {"viscosity": 101|102, "mu", "Pr", "r_s"}
 
     @property
     def n_var(self) -> int:
@@ -349,3 +353,68 @@ def euler_subsonic_duct(d: int = 2, n: int = 6, p: int = 3, num_flux: int = NUM_
     sides = {(0, 0): BC_TOTAL_TP, (0, 1): BC_BACKPRESSURE}
     sides.update({(k, s): BC_SLIPWALL for k in range(1, d) for s in range(2)})
     return _set_boundaries(prob, sides, _uniform_flow(d, 1.0, (u0,) + (0.0,) * (d - 1), 1.0))
+
+
+# ---- Navier-Stokes (pde 4: Euler inviscid flux + viscous flux, BR2 second-order numerical flux) ----------------------
+def _ns_params(mu, Pr=0.72, viscosity=VISCOSITY_CONSTANT, r_s=1.0):
+    return {"viscosity": int(viscosity), "mu": float(mu), "Pr": float(Pr), "r_s": float(r_s)}
+
+
+def ns_taylor_green(n: int = 8, p: int = 3, Re: float = 1600.0, mach: float = 0.1,
+                    num_flux: int = NUM_FLUX_ROE_PIKE, amplitude: float = 0.0, viscosity=VISCOSITY_CONSTANT,
+                    dt: float | None = None, n_steps: int = 200) -> DGProblem:
+    """The Taylor-Green vortex, the standard viscous DG benchmark: periodic HEX box [0, 2 pi]^3, rho = 1,
+    u = sin x cos y cos z, v = -cos x sin y cos z, w = 0, p = 1 / (gamma Ma^2) + (cos 2x + cos 2y)(cos 2z + 2) / 16,
+    mu = 1 / Re (unit length and velocity), Pr = 0.72 (Brachet et al., 1983; the published case, not a reference
+    input file). amplitude > 0 curves the mesh with the sinusoidal interior mapping."""
+    L = 2.0 * math.pi
+    mesh = StructuredMesh(3, n, 0.0, L)
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_3d(amplitude, L) if amplitude > 0 else None,
+                      curved=amplitude > 0)
+    prob = DGProblem("ns_taylor_green", 3, PDE_NAVIER_STOKES, num_flux, True, np.zeros(3), ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, 5, ops.n_vs)), dt=0.0, n_steps=n_steps,
+                     ns=_ns_params(1.0 / Re, viscosity=viscosity))
+    x = prob.solution_node_xyz()
+    X, Y, Z = x[..., 0], x[..., 1], x[..., 2]
+    rho = np.ones_like(X)
+    vel = np.stack([np.sin(X) * np.cos(Y) * np.cos(Z), -np.cos(X) * np.sin(Y) * np.cos(Z), np.zeros_like(X)])
+    pr = 1.0 / (GAMMA * mach * mach) + (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0) / 16.0
+    prob.sol = _pack_state(primitive_to_conserved(3, rho, vel, pr))
+    prob.dt = stable_dt(prob) if dt is None else dt
+    prob.meta.update(n=n, p=p, Re=Re, mach=mach)
+    return prob
+
+
+def ns_vortex_2d(n: int = 8, p: int = 3, mu: float = 0.01, num_flux: int = NUM_FLUX_ROE_PIKE,
+                 amplitude: float = 0.05, viscosity=VISCOSITY_CONSTANT) -> DGProblem:
+    """The curved periodic 2D vortex of euler_vortex_2d with viscosity mu (Pr = 0.72)."""
+    prob = euler_vortex_2d(n, p, num_flux=num_flux, amplitude=amplitude)
+    prob.name = "ns_vortex_2d"
+    prob.pde = PDE_NAVIER_STOKES
+    prob.ns = _ns_params(mu, viscosity=viscosity)
+    return prob
+
+
+def ns_periodic_field_2d(n: int = 4, p: int = 3, mu: float = 0.05, viscosity=VISCOSITY_CONSTANT) -> DGProblem:
+    """Straight periodic QUAD box [0, 2 pi]^2 with a smooth non-uniform state (density, velocity and pressure
+    waves); a test field for the viscous operator's consistency."""
+    L = 2.0 * math.pi
+    mesh = StructuredMesh(2, n, 0.0, L)
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops)
+    prob = DGProblem("ns_periodic_field_2d", 2, PDE_NAVIER_STOKES, NUM_FLUX_ROE_PIKE, True, np.zeros(3), ops, mesh,
+                     geom, sol=np.zeros((mesh.n_volumes, 4, ops.n_vs)), dt=0.0, n_steps=10,
+                     ns=_ns_params(mu, viscosity=viscosity))
+    x = prob.solution_node_xyz()
+    prob.sol = _pack_state(ns_field_2d(x[..., 0], x[..., 1]))
+    prob.dt = stable_dt(prob)
+    return prob
+
+
+def ns_field_2d(X, Y):
+    """Conserved variables (4, ...) of the smooth periodic test field of ns_periodic_field_2d."""
+    rho = 1.0 + 0.2 * np.sin(X) * np.cos(Y)
+    vel = np.stack([0.3 + 0.2 * np.cos(X + Y), -0.1 + 0.15 * np.sin(2 * X - Y)])
+    pr = 1.0 + 0.1 * np.cos(X) * np.sin(2 * Y)
+    return primitive_to_conserved(2, rho, vel, pr)

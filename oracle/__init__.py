@@ -22,7 +22,8 @@ _c_int_p = ctypes.POINTER(ctypes.c_int)
 
 class _Group(ctypes.Structure):
     _fields_ = [("n_vs", ctypes.c_int), ("n_vc", ctypes.c_int), ("cv0_vs_vc", _c_double_p),
-                ("tw1_vt_vc", _c_double_p), ("w_vc", _c_double_p), ("ccSB0", _c_double_p), ("ccBS0", _c_double_p)]
+                ("tw1_vt_vc", _c_double_p), ("w_vc", _c_double_p), ("ccSB0", _c_double_p), ("ccBS0", _c_double_p),
+                ("cv1_vs_vc", _c_double_p)]
 
 
 class _FaceOps(ctypes.Structure):
@@ -41,6 +42,7 @@ class _Problem(ctypes.Structure):
         ("n_faces", ctypes.c_int), ("face_vol", _c_int_p), ("face_lf", _c_int_p), ("face_ops_idx", _c_int_p),
         ("nc_fc", _c_int_p), ("normals_fc", _c_double_p), ("jacobian_det_fc", _c_double_p),
         ("bc_fc", _c_int_p), ("bc_state_fc", _c_double_p), ("bc_data", ctypes.c_double * 4),
+        ("viscosity", ctypes.c_int), ("mu", ctypes.c_double), ("Pr", ctypes.c_double), ("r_s", ctypes.c_double),
     ]
 
 
@@ -116,6 +118,7 @@ class Oracle:
             if not getattr(ops, "dense", False):    # Bezier maps exist for the TP groups only
                 G[gi].ccSB0 = _dp(arr(ops.ccSB0_vs_vs()))
                 G[gi].ccBS0 = _dp(arr(ops.ccBS0_vs_vs()))
+                G[gi].cv1_vs_vc = _dp(arr(np.stack([ops.cv1_vs_vc(k) for k in range(d)])))
         # face operator sets: one per (group, face order, orientation) that occurs, stacked over local faces
         vol_group = fl["vol_group"]
         face_q = fl["face_q"]
@@ -179,6 +182,9 @@ class Oracle:
             P.bc_state_fc = _dp(arr(fl["bc_state_fc"]))
             for k, x in enumerate(fl.get("bc_data") or (0.0, 0.0, 0.0, 0.0)):
                 P.bc_data[k] = float(x)
+        ns = getattr(prob, "ns", None)
+        if ns is not None:
+            P.viscosity, P.mu, P.Pr, P.r_s = int(ns["viscosity"]), float(ns["mu"]), float(ns["Pr"]), float(ns["r_s"])
         self._keep = (keep, G, FO, P)
         h = ctypes.c_void_p()
         st = lib.oracle_create(ctypes.byref(P), ctypes.byref(h))

@@ -117,10 +117,21 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 		return ORACLE_ERR_ARG;
 	if (in->d < 2 || in->d > 3 || in->n_volumes < 1 || in->n_groups < 1 || in->n_face_ops < 1)
 		return ORACLE_ERR_ARG;
-	if (in->pde == ORACLE_PDE_EULER && in->n_var != in->d + 2)
+	if ((in->pde == ORACLE_PDE_EULER || in->pde == ORACLE_PDE_NAVIER_STOKES) && in->n_var != in->d + 2)
 		return ORACLE_ERR_ARG;
 	if (in->pde == ORACLE_PDE_ADVECTION && in->n_var != 1)
 		return ORACLE_ERR_ARG;
+	if (in->pde == ORACLE_PDE_NAVIER_STOKES) {   /* gradients need the basis derivatives; no boundary values yet */
+		if ((in->viscosity != ORACLE_VISCOSITY_CONSTANT && in->viscosity != ORACLE_VISCOSITY_SUTHERLAND) ||
+		    !(in->Pr > 0.0) || !(in->mu >= 0.0))
+			return ORACLE_ERR_ARG;
+		for (int g = 0; g < in->n_groups; ++g)
+			if (!in->groups[g].cv1_vs_vc)
+				return ORACLE_ERR_ARG;
+		for (int f = 0; f < in->n_faces; ++f)
+			if (in->face_vol[2 * f + 1] < 0)
+				return ORACLE_ERR_ARG;
+	}
 	if (in->positivity)   /* the limiter needs every group's Bezier maps */
 		for (int g = 0; g < in->n_groups; ++g)
 			if (!in->groups[g].ccSB0 || !in->groups[g].ccBS0)

@@ -15,7 +15,8 @@ enum {
 	ORACLE_ERR_POSITIVITY = -3,
 };
 
-enum { ORACLE_PDE_ADVECTION = 1, ORACLE_PDE_EULER = 3 };                  /* definitions_test_case.h */
+enum { ORACLE_PDE_ADVECTION = 1, ORACLE_PDE_EULER = 3, ORACLE_PDE_NAVIER_STOKES = 4 };   /* definitions_test_case.h */
+enum { ORACLE_VISCOSITY_CONSTANT = 101, ORACLE_VISCOSITY_SUTHERLAND = 102 };  /* definitions_physics.h:34-36 */
 enum { ORACLE_NUM_FLUX_UPWIND = 11, ORACLE_NUM_FLUX_ROE_PIKE = 31, ORACLE_NUM_FLUX_LAX_FRIEDRICHS = 32 };
 
 /* One (element type, p): the reference's dense (op_std) volume operators. Row-major. */
@@ -26,6 +27,7 @@ struct oracle_group {
 	const double* w_vc;        /* n_vc */
 	const double* ccSB0;       /* n_vs x n_vs  Lagrange -> Bezier coefficients */
 	const double* ccBS0;       /* n_vs x n_vs  Bezier -> Lagrange coefficients */
+	const double* cv1_vs_vc;   /* d x (n_vc x n_vs): basis derivatives at the volume cubature nodes (Navier-Stokes) */
 };
 
 /* Face operators of a volume of one group at one face cubature order p_f (cv0_vs_fc[lf][p_f][p_v],
@@ -65,6 +67,13 @@ struct oracle_problem {
 	/* BC_Data of boundary_euler_T.c:44-49, read from the test case's input by the reference: p_back (BC_BACKPRESSURE
 	 * 103), t_total, p_total, r_s (BC_TOTAL_TP 104). */
 	double bc_data[4];
+	/* Navier-Stokes (pde 4): viscosity model (VISCOSITY_CONSTANT 101 / VISCOSITY_SUTHERLAND 102), mu (the constant
+	 * viscosity, or the reference value Sutherland's law scales), Prandtl number, specific gas constant (Sutherland's
+	 * temperature), read from the test case's input by the reference (solution_navier_stokes_T.c:188-255,
+	 * flux_navier_stokes_T.c:461-482). The second-order numerical flux is BR2 (NUM_FLUX_BR2_STABLE), the only
+	 * explicit option the reference's DG solver provides. */
+	int viscosity;
+	double mu, Pr, r_s;
 };
 
 struct oracle_ctx;

@@ -237,6 +237,52 @@ static void SUF(flux_euler)(const int d, const Type* W, Type* f)
 		f[ind++] = (E + p) * uvw[k];
 }
 
+/* Viscous part of the Navier-Stokes flux at one node, subtracted from f[dim + d*eq] (the reference adds the negated
+ * viscous flux to the Euler flux, compute_Flux_12_T with compute_Flux_T_navier_stokes, flux_navier_stokes_T.c:175-
+ * 284, 1005-1040). W: conserved state; G[dx + d*var]: its gradient. Velocity gradients (compute_duvw :708-720),
+ * stress tau = mu (grad u + grad u^T - 2/3 div u I) (compute_tau :776-799), scaled temperature gradient
+ * dTs = grad(E/rho) - 1/2 grad |u|^2 (compute_dTs :905-927), heat flux gamma/Pr mu dTs; mu constant or Sutherland's
+ * law mu = c1 sqrt(T) / (1 + c2 / T), c1 = 0.08 mu, c2 = 112, T = p / (rho r_s) (compute_mu_sutherland_T,
+ * solution_navier_stokes_T.c:246-256, solution_navier_stokes.h:31-32). */
+static void SUF(flux_ns_sub)(const struct oracle_problem* P, const Type* W, const Type* G, Type* f)
+{
+	const int d = P->d;
+	const Type rho = W[0], E = W[d + 1], rho_inv = 1.0 / rho;
+	Type u[3] = {0.0, 0.0, 0.0}, du[3][3], V2 = 0.0;
+	for (int k = 0; k < d; ++k) {
+		u[k] = W[1 + k] * rho_inv;
+		V2 += u[k] * u[k];
+	}
+	for (int s = 0; s < d; ++s)
+		for (int x = 0; x < d; ++x)
+			du[s][x] = rho_inv * (G[x + d * (1 + s)] - G[x + d * 0] * u[s]);
+	Type mu = P->mu;
+	if (P->viscosity == ORACLE_VISCOSITY_SUTHERLAND) {
+		const Type p = GM1 * (E - 0.5 * rho * V2), T = p / (rho * P->r_s);
+		mu = 0.08 * P->mu / (1.0 + 112.0 / T) * SQRT_T(T);
+	}
+	Type div = 0.0;
+	for (int k = 0; k < d; ++k)
+		div += du[k][k];
+	Type tau[3][3];
+	for (int a = 0; a < d; ++a)
+		for (int b = 0; b < d; ++b)
+			tau[a][b] = (a == b) ? mu * 2.0 * (du[a][a] - div / 3.0) : mu * (du[b][a] + du[a][b]);
+	for (int x = 0; x < d; ++x) {
+		const Type dE_o_rho = rho_inv * rho_inv * (G[x + d * (d + 1)] * rho - E * G[x + d * 0]);
+		Type dV2 = 0.0;
+		for (int k = 0; k < d; ++k)
+			dV2 += 2.0 * u[k] * du[k][x];
+		const Type dTs = dE_o_rho - 0.5 * dV2;
+		Type ut = 0.0;
+		for (int k = 0; k < d; ++k)
+			ut += u[k] * tau[x][k];
+		for (int k = 0; k < d; ++k)
+			f[x + d * (1 + k)] -= tau[k][x];
+		f[x + d * (d + 1)] -= GAMMA / P->Pr * mu * dTs + ut;
+	}
+}
+
 /* Lax-Friedrichs: numerical_flux_euler_T.c:60-327. WL/WR are per-node state vectors, n is the node's
  * unit normal; writes nF[eq]. */
 static void SUF(num_flux_lf)(const int d, const Type* WL, const Type* WR, const double* n, Type* nF)
@@ -350,7 +396,7 @@ static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Typ
 		const double* ni = &nrm[(size_t)i * d];
 		if (SUF(boundary_state)(P, P->bc_fc[f], WL, &ext[(size_t)i * nv], ni, WR) != 0)
 			return -1;
-		if (P->pde == ORACLE_PDE_EULER) {
+		if (P->pde != ORACLE_PDE_ADVECTION) {
 			if (P->num_flux == ORACLE_NUM_FLUX_ROE_PIKE)
 				SUF(num_flux_roe)(d, WL, WR, ni, nF);
 			else
@@ -368,6 +414,98 @@ static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Typ
 	return 0;
 }
 
+/* BR2 gradients of the Navier-Stokes residual (compute_grad_coef_dg_T, compute_grad_coef_dg_T.c:60-316) for
+ * interior faces and the explicit, non-collocated case:
+ *   volume:  grad_coef_v[dir] = M^-1 tw0_vt_vc (sum_k m(., dir, k) cv1_vs_vc[k]) sol   (:168-214, 342-358);
+ *   faces:   grad_coef_f[side][dir] = M^-1 tw0_vt_fc (J_f n_dir (s_num - s_side)), the central numerical
+ *            solution s_num = (s_L + s_R) / 2 (get_sol_scale :674-686), side 1 in its own face-node order
+ *            (:216-316, 424-440);
+ *   total:   grad_coef = grad_coef_v + sum over the volume's faces of grad_coef_f (:503-525).
+ * gv, gt: d x n_state ([dir][state]); gf: per face side (2f + s) d x (max_vs x n_var). */
+static void SUF(ns_gradients)(const struct oracle_ctx* c, const Type* sol, Type* gv, Type* gf, Type* gt)
+{
+	const struct oracle_problem* P = &c->P;
+	const int d = P->d, nv = P->n_var;
+	const size_t ns = c->n_state, fstride = (size_t)c->max_vs * nv;
+	Type* dr = malloc(sizeof(Type) * (size_t)c->max_vc * nv * d);
+	Type* t = malloc(sizeof(Type) * (size_t)c->max_vc * nv);
+	Type* y = malloc(sizeof(Type) * fstride);
+	for (size_t i = 0; i < ns * d; ++i)
+		gv[i] = gt[i] = 0.0;
+	for (size_t i = 0; i < (size_t)P->n_faces * 2 * d * fstride; ++i)
+		gf[i] = 0.0;
+	for (int v = 0; v < P->n_volumes; ++v) {
+		const struct oracle_group* G = &P->groups[P->vol_group[v]];
+		const int n_vs = G->n_vs, n_vc = G->n_vc;
+		const Type* s = &sol[c->state_off[v]];
+		const double* m = &P->metrics_vc[c->vc_off[v] * d * d];
+		for (size_t i = 0; i < (size_t)n_vc * nv * d; ++i)
+			dr[i] = 0.0;
+		for (int k = 0; k < d; ++k)
+			SUF(mm_acc)(n_vc, n_vs, nv, 1.0, &G->cv1_vs_vc[(size_t)k * n_vc * n_vs], s, &dr[(size_t)k * n_vc * nv]);
+		for (int dir = 0; dir < d; ++dir) {
+			for (int var = 0; var < nv; ++var)
+				for (int n = 0; n < n_vc; ++n) {
+					Type a = 0.0;
+					for (int k = 0; k < d; ++k)
+						a += m[n + (size_t)n_vc * (dir + d * k)] * dr[(size_t)k * n_vc * nv + n + (size_t)n_vc * var];
+					t[n + (size_t)n_vc * var] = G->w_vc[n] * a;   /* tw0_vt_vc = cv0^T diag(w_vc) */
+				}
+			for (int var = 0; var < nv; ++var)
+				for (int i = 0; i < n_vs; ++i) {
+					Type a = 0.0;
+					for (int n = 0; n < n_vc; ++n)
+						a += G->cv0_vs_vc[(size_t)n * n_vs + i] * t[n + (size_t)n_vc * var];
+					y[i + (size_t)n_vs * var] = a;
+				}
+			SUF(mm_acc)(n_vs, n_vs, nv, 1.0, &c->m_inv[c->minv_off[v]], y, &gv[ns * dir + c->state_off[v]]);
+		}
+	}
+	Type* sL = malloc(sizeof(Type) * (size_t)c->max_fc * nv);
+	Type* sR0 = malloc(sizeof(Type) * (size_t)c->max_fc * nv);
+	Type* X = malloc(sizeof(Type) * (size_t)c->max_fc * nv);
+	Type* XR = malloc(sizeof(Type) * (size_t)c->max_fc * nv);
+	for (int f = 0; f < P->n_faces; ++f) {
+		const int vL = P->face_vol[2 * f], vR = P->face_vol[2 * f + 1];
+		const int lfL = P->face_lf[2 * f], lfR = P->face_lf[2 * f + 1];
+		const struct oracle_face_ops* FL = &P->face_ops[P->face_ops_idx[2 * f]];
+		const struct oracle_face_ops* FR = &P->face_ops[P->face_ops_idx[2 * f + 1]];
+		const int n_fc = FL->n_fc;
+		const int* nc = &P->nc_fc[c->fc_off[f]];
+		const double* nrm = &P->normals_fc[c->fc_off[f] * d];
+		const double* jf = &P->jacobian_det_fc[c->fc_off[f]];
+		for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
+			sL[i] = sR0[i] = 0.0;
+		SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], &sol[c->state_off[vL]], sL);
+		SUF(mm_acc)(n_fc, FR->n_vs, nv, 1.0, &FR->cv0_vs_fc[(size_t)lfR * n_fc * FR->n_vs], &sol[c->state_off[vR]], sR0);
+		for (int dir = 0; dir < d; ++dir) {
+			for (int var = 0; var < nv; ++var)
+				for (int i = 0; i < n_fc; ++i) {
+					const size_t o = i + (size_t)n_fc * var;
+					X[o] = jf[i] * nrm[(size_t)i * d + dir] * 0.5 * (sR0[nc[i] + (size_t)n_fc * var] - sL[o]);
+					XR[nc[i] + (size_t)n_fc * var] = X[o];   /* side 1: J_f (-n) (s_num - s_R) = the same values */
+				}
+			Type* gL = &gf[((size_t)(2 * f) * d + dir) * fstride];
+			Type* gR = &gf[((size_t)(2 * f + 1) * d + dir) * fstride];
+			for (size_t i = 0; i < fstride; ++i)
+				y[i] = 0.0;
+			SUF(mm_acc)(FL->n_vs, n_fc, nv, 1.0, &FL->tw0_vt_fc[(size_t)lfL * FL->n_vs * n_fc], X, y);
+			SUF(mm_acc)(FL->n_vs, FL->n_vs, nv, 1.0, &c->m_inv[c->minv_off[vL]], y, gL);
+			for (size_t i = 0; i < fstride; ++i)
+				y[i] = 0.0;
+			SUF(mm_acc)(FR->n_vs, n_fc, nv, 1.0, &FR->tw0_vt_fc[(size_t)lfR * FR->n_vs * n_fc], XR, y);
+			SUF(mm_acc)(FR->n_vs, FR->n_vs, nv, 1.0, &c->m_inv[c->minv_off[vR]], y, gR);
+			for (size_t i = 0; i < (size_t)FL->n_vs * nv; ++i)
+				gt[ns * dir + c->state_off[vL] + i] += gL[i];
+			for (size_t i = 0; i < (size_t)FR->n_vs * nv; ++i)
+				gt[ns * dir + c->state_off[vR] + i] += gR[i];
+		}
+	}
+	for (size_t i = 0; i < ns * d; ++i)
+		gt[i] += gv[i];
+	free(dr); free(t); free(y); free(sL); free(sR0); free(X); free(XR);
+}
+
 static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* rhs)
 {
 	const struct oracle_problem* P = &c->P;
@@ -383,6 +521,23 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 	Type* sR = malloc(sizeof(Type) * (size_t)c->max_fc * nv);
 	Type* nnf = malloc(sizeof(Type) * (size_t)c->max_fc * neq);
 	Type* nnfR = malloc(sizeof(Type) * (size_t)c->max_fc * neq);
+	const int ns_pde = P->pde == ORACLE_PDE_NAVIER_STOKES;
+	const size_t fstride = (size_t)c->max_vs * nv;
+	Type *gv = NULL, *gf = NULL, *gt = NULL, *g_vc = NULL, *gpL = NULL, *gpR0 = NULL, *gpR = NULL, *tmp = NULL;
+	if (ns_pde) {
+		gv = malloc(sizeof(Type) * c->n_state * d);
+		gt = malloc(sizeof(Type) * c->n_state * d);
+		gf = malloc(sizeof(Type) * (size_t)(P->n_faces > 0 ? P->n_faces : 1) * 2 * d * fstride);
+		g_vc = malloc(sizeof(Type) * (size_t)c->max_vc * nv * d);
+		gpL = malloc(sizeof(Type) * (size_t)c->max_fc * nv * d);
+		gpR0 = malloc(sizeof(Type) * (size_t)c->max_fc * nv * d);
+		gpR = malloc(sizeof(Type) * (size_t)c->max_fc * nv * d);
+		tmp = malloc(sizeof(Type) * fstride);
+		SUF(ns_gradients)(c, sol, gv, gf, gt);
+	}
+	/* BR2's scaling of a face's own lifting in the face gradient: PENALTY_SCALING * NFMAX
+	 * (compute_face_rlhs_dg_T.c:273-295, NFMAX = 2 DIM for the TP elements, definitions_elements.h:60-76) */
+	const double eta = 1.01 * 2 * d;
 
 	/* ---- volume term ---- */
 	for (int v = 0; v < P->n_volumes; ++v) {
@@ -394,14 +549,28 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 		for (size_t i = 0; i < (size_t)n_vc * nv; ++i)
 			s_vc[i] = 0.0;
 		SUF(mm_acc)(n_vc, n_vs, nv, 1.0, G->cv0_vs_vc, s, s_vc);
+		if (ns_pde) {   /* the gradient at the cubature nodes: cv0_vr_vc grad_coef */
+			for (size_t i = 0; i < (size_t)n_vc * nv * d; ++i)
+				g_vc[i] = 0.0;
+			for (int dir = 0; dir < d; ++dir)
+				SUF(mm_acc)(n_vc, n_vs, nv, 1.0, G->cv0_vs_vc, &gt[c->n_state * dir + c->state_off[v]],
+				            &g_vc[(size_t)dir * n_vc * nv]);
+		}
 		for (size_t i = 0; i < (size_t)n_vc * neq * d; ++i)
 			fr[i] = 0.0;
 		for (int n = 0; n < n_vc; ++n) {
 			Type W[5], f[15];
 			for (int k = 0; k < nv; ++k)
 				W[k] = s_vc[n + (size_t)n_vc * k];
-			if (P->pde == ORACLE_PDE_EULER) {
+			if (P->pde != ORACLE_PDE_ADVECTION) {
 				SUF(flux_euler)(d, W, f);
+				if (ns_pde) {
+					Type Gn[15];
+					for (int var = 0; var < nv; ++var)
+						for (int x = 0; x < d; ++x)
+							Gn[x + d * var] = g_vc[(size_t)x * n_vc * nv + n + (size_t)n_vc * var];
+					SUF(flux_ns_sub)(P, W, Gn, f);
+				}
 			} else {
 				for (int k = 0; k < d; ++k)
 					f[k] = P->b_adv[k] * W[0];
@@ -425,6 +594,7 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 		if (vR < 0) {
 			if (SUF(boundary_face)(c, f, sol, rhs, sL, nnf) != 0) {
 				free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);
+				free(gv); free(gf); free(gt); free(g_vc); free(gpL); free(gpR0); free(gpR); free(tmp);
 				return ORACLE_ERR_ARG;
 			}
 			continue;
@@ -444,6 +614,29 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 		for (int k = 0; k < nv; ++k)
 			for (int i = 0; i < n_fc; ++i)
 				sR[i + (size_t)n_fc * k] = sR0[nc[i] + (size_t)n_fc * k];
+		if (ns_pde) {
+			/* each side's partially corrected gradient at the face nodes: cv0_vr_fc (grad_coef_v + eta
+			 * grad_coef_f of this face) (constructor_partial_grad_fc_interp, compute_face_rlhs_dg_T.c:239-262),
+			 * the right side's in the left's node order */
+			for (size_t i = 0; i < (size_t)n_fc * nv * d; ++i)
+				gpL[i] = gpR0[i] = 0.0;
+			for (int dir = 0; dir < d; ++dir) {
+				const Type* gfL = &gf[((size_t)(2 * f) * d + dir) * fstride];
+				const Type* gfR = &gf[((size_t)(2 * f + 1) * d + dir) * fstride];
+				for (size_t i = 0; i < (size_t)FL->n_vs * nv; ++i)
+					tmp[i] = gv[c->n_state * dir + c->state_off[vL] + i] + eta * gfL[i];
+				SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], tmp,
+				            &gpL[(size_t)dir * n_fc * nv]);
+				for (size_t i = 0; i < (size_t)FR->n_vs * nv; ++i)
+					tmp[i] = gv[c->n_state * dir + c->state_off[vR] + i] + eta * gfR[i];
+				SUF(mm_acc)(n_fc, FR->n_vs, nv, 1.0, &FR->cv0_vs_fc[(size_t)lfR * n_fc * FR->n_vs], tmp,
+				            &gpR0[(size_t)dir * n_fc * nv]);
+				for (int k = 0; k < nv; ++k)
+					for (int i = 0; i < n_fc; ++i)
+						gpR[(size_t)dir * n_fc * nv + i + (size_t)n_fc * k] =
+							gpR0[(size_t)dir * n_fc * nv + nc[i] + (size_t)n_fc * k];
+			}
+		}
 		for (int i = 0; i < n_fc; ++i) {
 			Type WL[5], WR[5], nF[5];
 			for (int k = 0; k < nv; ++k) {
@@ -451,7 +644,7 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 				WR[k] = sR[i + (size_t)n_fc * k];
 			}
 			const double* ni = &nrm[(size_t)i * d];
-			if (P->pde == ORACLE_PDE_EULER) {
+			if (P->pde != ORACLE_PDE_ADVECTION) {
 				if (P->num_flux == ORACLE_NUM_FLUX_ROE_PIKE)
 					SUF(num_flux_roe)(d, WL, WR, ni, nF);
 				else
@@ -462,6 +655,21 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 				for (int k = 0; k < d; ++k)
 					b_dot_n += P->b_adv[k] * ni[k];
 				nF[0] = (b_dot_n > ORACLE_EPS ? b_dot_n * WL[0] : b_dot_n * WR[0]);
+			}
+			if (ns_pde) {   /* + the central viscous flux (compute_Numerical_Flux_T_central, numerical_flux_central_T.c) */
+				Type GL[15], GR[15], fL[15], fR[15];
+				for (int var = 0; var < nv; ++var)
+					for (int x = 0; x < d; ++x) {
+						GL[x + d * var] = gpL[(size_t)x * n_fc * nv + i + (size_t)n_fc * var];
+						GR[x + d * var] = gpR[(size_t)x * n_fc * nv + i + (size_t)n_fc * var];
+					}
+				for (int k = 0; k < d * neq; ++k)
+					fL[k] = fR[k] = 0.0;
+				SUF(flux_ns_sub)(P, WL, GL, fL);
+				SUF(flux_ns_sub)(P, WR, GR, fR);
+				for (int eq = 0; eq < neq; ++eq)
+					for (int x = 0; x < d; ++x)
+						nF[eq] += 0.5 * ni[x] * (fL[x + d * eq] + fR[x + d * eq]);
 			}
 			/* scale_by_Jacobian_e_T (compute_face_rlhs_T.c:337-342) */
 			for (int k = 0; k < neq; ++k)
@@ -479,6 +687,7 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 	}
 
 	free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);
+	free(gv); free(gf); free(gt); free(g_vc); free(gpL); free(gpR0); free(gpR); free(tmp);
 	return ORACLE_OK;
 }
 
