@@ -14,7 +14,7 @@ REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 LIB_PATH = os.path.join(PKG_DIR, "libdgpu.so")
 SOURCES = ["dgpu.cu", "dgpu_batched.cu", "dgpu_mesh_io.cpp"]
-HEADERS = ["dgpu_geometry.cuh", "dgpu_jacobian.cuh", "dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
+HEADERS = ["dgpu_ns.cuh", "dgpu_geometry.cuh", "dgpu_jacobian.cuh", "dgpu_tp.cuh", "dgpu_physics.cuh", "dgpu_dual.cuh", "dgpu_adjoint.cuh", "dgpu_batched.cuh",
            "dgpu_dense.cuh", "dgpu_jvp.cuh", "dgpu_host_ops.h"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
               "-Xcompiler", "-fPIC"]
@@ -67,7 +67,8 @@ c_int_p = ctypes.POINTER(ctypes.c_int)
 
 class Physics(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int), ("pde", ctypes.c_int), ("num_flux", ctypes.c_int),
-                ("positivity", ctypes.c_int), ("b_adv", ctypes.c_double * 3)]
+                ("positivity", ctypes.c_int), ("b_adv", ctypes.c_double * 3), ("viscosity", ctypes.c_int),
+                ("mu", ctypes.c_double), ("Pr", ctypes.c_double), ("r_s", ctypes.c_double)]
 
 
 class TPOperators(ctypes.Structure):

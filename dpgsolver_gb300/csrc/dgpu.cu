@@ -18,6 +18,7 @@
 #include "dgpu_adjoint.cuh"
 #include "dgpu_geometry.cuh"
 #include "dgpu_jacobian.cuh"
+#include "dgpu_ns.cuh"
 #include "dgpu_jvp.cuh"
 #include "dgpu_host_ops.h"
 
@@ -27,7 +28,6 @@ namespace {
 
 thread_local std::string g_create_error;
 
-constexpr int kRkStepLaunches = 9;   // kernels of one SSP-RK3 step (enqueue_rk_step)
 
 struct KernelTimer {
 	const char* name;
@@ -60,6 +60,10 @@ struct dgpu_ctx {
 	bool coef_valid = true, gl_valid = false;   // which of u / ug holds the current state
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
+	bool ns = false;                      // Navier-Stokes: BR2 gradient buffers and the four-kernel stage
+	NsPhys ns_phys = {0.0, 1.0, 1.0, 101};
+	double *ns_gtr = nullptr, *ns_lam = nullptr, *ns_X = nullptr;
+	int stage_launches = 3;               // kernels per residual evaluation / RK stage
 	int n_bnd = 0;                        // boundary faces (face_vol[2f+1] < 0)
 	int *bnd = nullptr, *bc_code = nullptr;
 	double* bc_ext = nullptr;
@@ -116,6 +120,11 @@ struct dgpu_ctx {
 		P.bc_code = bc_code;
 		P.bc_ext = bc_ext;
 		P.bc_data = bc_data;
+		P.ns_gtr = ns_gtr;
+		P.ns_lam = ns_lam;
+		P.ns_X = ns_X;
+		P.ns = ns_phys;
+		P.ns_eta = 1.01 * 2 * d;   // PENALTY_SCALING * NFMAX (compute_face_rlhs_dg_T.c:273-295)
 		return P;
 	}
 };
@@ -442,9 +451,68 @@ cudaError_t bind(dgpu_ctx* c)
 	return cudaFuncSetAttribute(tp_convert_kernel<D, Q, NV, false>, smem, (int)convert_smem_bytes<D, Q, NV>());
 }
 
+template <int D, int Q, int NV>
+size_t ns_smem_bytes()
+{
+	using S = TPShape<D, Q>;
+	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * NsSmem<D, Q, NV>::PER_E * sizeof(double);
+}
+
+// Navier-Stokes volume and face work of one residual: gradients and traces, face fluxes, volume flux (the lift that
+// follows is the ordinary one).
+template <int D, int Q, int FLUX, bool GLL_IN>
+cudaError_t launch_ns_t(dgpu_ctx* c)
+{
+	using S = TPShape<D, Q>;
+	constexpr int NV = D + 2;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	const TPParams P = c->params();
+	const double* u = GLL_IN ? c->u : c->ug;
+	record_start(c, "tp_ns_grad_kernel");
+	tp_ns_grad_kernel<D, Q, NV, GLL_IN><<<blocks, S::THREADS, ns_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, P, u);
+	record_stop(c);
+	const long long nf = (long long)c->n_face * S::NF;
+	record_start(c, "tp_ns_face_kernel");
+	tp_ns_face_kernel<D, Q, FLUX><<<(unsigned)((nf + 127) / 128), 128, 0, c->stream>>>(P);
+	record_stop(c);
+	record_start(c, "tp_ns_volume_kernel");
+	tp_ns_volume_kernel<D, Q, NV, GLL_IN><<<blocks, S::THREADS, ns_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, P, u);
+	record_stop(c);
+	c->launches += 3;
+	return cudaGetLastError();
+}
+
+cudaError_t launch_nothing(dgpu_ctx*) { return cudaSuccess; }
+
+template <int D, int Q, int FLUX>
+cudaError_t bind_ns(dgpu_ctx* c)
+{
+	constexpr int NV = D + 2;
+	cudaError_t e = bind<D, Q, NV, kEuler, FLUX>(c);   // lift, convert, positivity: as for Euler
+	if (e != cudaSuccess)
+		return e;
+	c->launch_volume = launch_ns_t<D, Q, FLUX, true>;
+	c->launch_volume_gl = launch_ns_t<D, Q, FLUX, false>;
+	c->launch_face = launch_nothing;
+	c->launch_adjoint = nullptr;
+	c->launch_objective = nullptr;
+	c->launch_jvp = nullptr;
+	c->launch_jvp_tangent = nullptr;
+	const cudaFuncAttribute smem = cudaFuncAttributeMaxDynamicSharedMemorySize;
+	const int bytes = (int)ns_smem_bytes<D, Q, NV>();
+	if ((e = cudaFuncSetAttribute(tp_ns_grad_kernel<D, Q, NV, true>, smem, bytes)) ||
+	    (e = cudaFuncSetAttribute(tp_ns_grad_kernel<D, Q, NV, false>, smem, bytes)) ||
+	    (e = cudaFuncSetAttribute(tp_ns_volume_kernel<D, Q, NV, true>, smem, bytes)) ||
+	    (e = cudaFuncSetAttribute(tp_ns_volume_kernel<D, Q, NV, false>, smem, bytes)))
+		return e;
+	return cudaSuccess;
+}
+
 template <int D, int Q>
 cudaError_t bind_pde(dgpu_ctx* c)
 {
+	if (c->pde == DGPU_PDE_NAVIER_STOKES)
+		return c->flux == DGPU_NUM_FLUX_ROE_PIKE ? bind_ns<D, Q, kRoePike>(c) : bind_ns<D, Q, kLaxFriedrichs>(c);
 	if (c->pde == DGPU_PDE_ADVECTION)
 		return bind<D, Q, 1, kAdvection, kUpwind>(c);
 	if (c->flux == DGPU_NUM_FLUX_ROE_PIKE)
@@ -476,7 +544,7 @@ void free_all(dgpu_ctx* c)
 	}
 	c->timers.clear();
 	void* ptrs[] = {c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
-	                c->jac_slot, c->jac_members,
+	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X,
 	                c->bnd, c->bc_code, c->bc_ext, c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -722,15 +790,21 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 	if (phys->pde == DGPU_PDE_ADVECTION) {
 		if (phys->num_flux != DGPU_NUM_FLUX_UPWIND)
 			return fail(nullptr, DGPU_ERR_UNSUPPORTED, "advection supports the upwind flux");
-	} else if (phys->pde == DGPU_PDE_EULER) {
+	} else if (phys->pde == DGPU_PDE_EULER || phys->pde == DGPU_PDE_NAVIER_STOKES) {
 		if (phys->num_flux != DGPU_NUM_FLUX_ROE_PIKE && phys->num_flux != DGPU_NUM_FLUX_LAX_FRIEDRICHS)
 			return fail(nullptr, DGPU_ERR_UNSUPPORTED, "Euler supports Roe-Pike and Lax-Friedrichs");
+		if (phys->pde == DGPU_PDE_NAVIER_STOKES &&
+		    ((phys->viscosity != DGPU_VISCOSITY_CONSTANT && phys->viscosity != DGPU_VISCOSITY_SUTHERLAND) ||
+		     !(phys->mu >= 0.0) || !(phys->Pr > 0.0) ||
+		     (phys->viscosity == DGPU_VISCOSITY_SUTHERLAND && !(phys->r_s > 0.0))))
+			return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "Navier-Stokes needs a viscosity model, mu >= 0, Pr > 0"
+			                                               " (and r_s > 0 for Sutherland's law)");
 	} else {
-		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "pde must be advection or Euler");
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "pde must be advection, Euler or Navier-Stokes");
 	}
 	if (!ops->cv0_vs_vc || !ops->cv1_vs_vc || !ops->cv0_vs_fc || !ops->w_vc)
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL operator");
-	if (phys->pde == DGPU_PDE_EULER && phys->positivity && (!ops->ccSB0_vs_vs || !ops->ccBS0_vs_vs))
+	if (phys->pde != DGPU_PDE_ADVECTION && phys->positivity && (!ops->ccSB0_vs_vs || !ops->ccBS0_vs_vs))
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "positivity needs ccSB0/ccBS0");
 	// geometry: the geometric factors, or the geometry coefficients from which the device computes them
 	const bool dev_geo = mesh->geom_coef != nullptr;
@@ -758,8 +832,13 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 	c->NF = (d == 2 ? q : q * q);
 	c->pde = phys->pde;
 	c->flux = phys->num_flux;
-	c->nv = (phys->pde == DGPU_PDE_EULER ? d + 2 : 1);
-	c->positivity = (phys->pde == DGPU_PDE_EULER && phys->positivity) ? 1 : 0;
+	c->nv = (phys->pde != DGPU_PDE_ADVECTION ? d + 2 : 1);
+	c->positivity = (phys->pde != DGPU_PDE_ADVECTION && phys->positivity) ? 1 : 0;
+	c->ns = phys->pde == DGPU_PDE_NAVIER_STOKES;
+	if (c->ns) {
+		c->ns_phys = NsPhys{phys->mu, phys->Pr, phys->r_s, phys->viscosity};
+		c->stage_launches = 4;
+	}
 	c->n_vol = mesh->n_volumes;
 	c->n_face = mesh->n_faces;
 	for (int k = 0; k < 3; ++k)
@@ -841,6 +920,10 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 				return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "boundary faces need bc_fc and bc_state_fc");
 			}
 			const int code = mesh->bc_fc[f] % kBcStepSC;
+			if (c->ns) {
+				delete c;
+				return fail(nullptr, DGPU_ERR_UNSUPPORTED, "boundary faces are not provided for Navier-Stokes");
+			}
 			if (code < 0 || (c->pde == DGPU_PDE_EULER ? !bc_is_euler(code) : !bc_is_advection_upwind(code))) {
 				delete c;
 				return fail(nullptr, DGPU_ERR_UNSUPPORTED,
@@ -943,6 +1026,25 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		DG_TRY(upload(&c->bnd, bnd));
 		DG_TRY(upload(&c->bc_code, bc_code));
 		DG_TRY(upload(&c->bc_ext, bc_ext));
+	}
+	if (c->ns) {   // BR2 buffers and the faces' own lifting diagonal
+		DG_TRY(cudaMalloc((void**)&c->ns_gtr, nF * 2 * d * c->nv * NF * sizeof(double)));
+		DG_TRY(cudaMalloc((void**)&c->ns_lam, nF * 2 * NF * sizeof(double)));
+		DG_TRY(cudaMalloc((void**)&c->ns_X, nF * d * c->nv * NF * sizeof(double)));
+		const long long n_lam = (long long)nV * 2 * d * NF;
+		const unsigned g = (unsigned)((n_lam + 255) / 256);
+		switch ((d == 2 ? 10 : 20) + q) {
+		case 12: tp_ns_lambda_kernel<2, 2><<<g, 256, 0, c->stream>>>(c->ops, c->params(), c->ns_lam); break;
+		case 13: tp_ns_lambda_kernel<2, 3><<<g, 256, 0, c->stream>>>(c->ops, c->params(), c->ns_lam); break;
+		case 14: tp_ns_lambda_kernel<2, 4><<<g, 256, 0, c->stream>>>(c->ops, c->params(), c->ns_lam); break;
+		case 15: tp_ns_lambda_kernel<2, 5><<<g, 256, 0, c->stream>>>(c->ops, c->params(), c->ns_lam); break;
+		case 22: tp_ns_lambda_kernel<3, 2><<<g, 256, 0, c->stream>>>(c->ops, c->params(), c->ns_lam); break;
+		case 23: tp_ns_lambda_kernel<3, 3><<<g, 256, 0, c->stream>>>(c->ops, c->params(), c->ns_lam); break;
+		case 24: tp_ns_lambda_kernel<3, 4><<<g, 256, 0, c->stream>>>(c->ops, c->params(), c->ns_lam); break;
+		default: tp_ns_lambda_kernel<3, 5><<<g, 256, 0, c->stream>>>(c->ops, c->params(), c->ns_lam); break;
+		}
+		DG_TRY(cudaGetLastError());
+		DG_TRY(cudaStreamSynchronize(c->stream));
 	}
 	cudaError_t be = (d == 2 ? bind_q<2>(c) : bind_q<3>(c));
 	if (be != cudaSuccess) {
@@ -1086,11 +1188,11 @@ dgpu_status dgpu_ssp_rk3_steps(dgpu_ctx* c, double dt, int n_steps, double* max_
 			return st;
 		for (int s = 0; s < plain; ++s) {
 			DGPU_CUDA(c, cudaGraphLaunch(c->rk_graph, c->stream));
-			c->launches += kRkStepLaunches;
+			c->launches += 3 * c->stage_launches;
 		}
 		if (want_max && n_steps > 0) {
 			DGPU_CUDA(c, cudaGraphLaunch(c->rk_graph_max, c->stream));
-			c->launches += kRkStepLaunches;
+			c->launches += 3 * c->stage_launches;
 		}
 	}
 	if (n_steps > 0)
@@ -1670,6 +1772,8 @@ extern "C" dgpu_status dgpu_jacobian_structure(dgpu_ctx* c, int* block_size, lon
 {
 	if (!c)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_jacobian_structure is not provided for Navier-Stokes");
 	const dgpu_status st = jacobian_setup(c);
 	if (st != DGPU_OK)
 		return st;
@@ -1687,6 +1791,8 @@ extern "C" dgpu_status dgpu_jacobian_bsr(dgpu_ctx* c, const double* sol, int raw
 {
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_jacobian_bsr is not provided for Navier-Stokes");
 	dgpu_status st = jacobian_setup(c);
 	if (st == DGPU_OK)
 		st = ensure_jvp_buffers(c);
@@ -1757,6 +1863,8 @@ extern "C" dgpu_status dgpu_jvp(dgpu_ctx* c, const double* sol, const double* di
 {
 	if (!c || !sol || !dir || !jv)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_jvp is not provided for Navier-Stokes");
 	const size_t ns = state_size(c);
 	{
 		const dgpu_status st = ensure_jvp_buffers(c);
@@ -1780,6 +1888,8 @@ extern "C" dgpu_status dgpu_vjp_forward(dgpu_ctx* c, const double* sol, double* 
 {
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_vjp_forward is not provided for Navier-Stokes");
 	dgpu_status st = ensure_adjoint_buffers(c);
 	if (st != DGPU_OK)
 		return st;
@@ -1803,6 +1913,8 @@ extern "C" dgpu_status dgpu_vjp_backward(dgpu_ctx* c, const double* cotangent, d
 {
 	if (!c || !cotangent || !grad_sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_vjp_backward is not provided for Navier-Stokes");
 	if (!c->u_saved)
 		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "dgpu_vjp_backward needs a preceding dgpu_vjp_forward");
 	const size_t bytes = state_size(c) * sizeof(double);
@@ -1820,6 +1932,8 @@ extern "C" dgpu_status dgpu_set_objective_faces(dgpu_ctx* c, int n_faces, const 
 {
 	if (!c || n_faces < 1 || !faces)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_set_objective_faces is not provided for Navier-Stokes");
 	if (c->pde != DGPU_PDE_EULER)
 		return fail(c, DGPU_ERR_UNSUPPORTED, "the pressure objective needs the Euler equations");
 	for (int i = 0; i < n_faces; ++i)
@@ -1908,6 +2022,8 @@ extern "C" dgpu_status dgpu_objective(dgpu_ctx* c, const double* sol, double* J,
 {
 	if (!c || !sol || !J)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_objective is not provided for Navier-Stokes");
 	if (!c->obj_faces)
 		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "no objective faces: call dgpu_set_objective_faces");
 	const size_t bytes = state_size(c) * sizeof(double);
@@ -1925,6 +2041,8 @@ extern "C" dgpu_status dgpu_adjoint_ssp_rk3(dgpu_ctx* c, double dt, int n_steps,
 {
 	if (!c || n_steps < 1 || !sol0 || !J || !dJ_dsol0 || !(dt == dt))
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_adjoint_ssp_rk3 is not provided for Navier-Stokes");
 	if (!c->obj_faces)
 		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "no objective faces: call dgpu_set_objective_faces");
 	const size_t ns = state_size(c), sb = ns * sizeof(double);

@@ -1,0 +1,324 @@
+// Navier-Stokes residual on the TP path: the Euler flux plus the viscous flux, with the BR2 gradients of the
+// reference's explicit DG solver (compute_grad_coef_dg_T, src/simulation/solvers/dg/compute_grad_coef_dg_T.c:60-316;
+// constructor_partial_grad_fc_interp, compute_face_rlhs_dg_T.c:239-295) in GL nodal space.
+//
+// In GL space with the GLL basis and the GL cubature of the same size, V (GLL -> GL) is square and invertible, so the
+// reference's operators reduce as follows (M = V^T diag(w J) V, E = GL -> face interpolation along the normal):
+//   grad_coef_v = M^-1 tw0_vt_vc (sum_k m(., dir, k) cv1_vs_vc[k]) u  ->  V grad_coef_v = (1/J) sum_k m(dir, k) d_r_k u_gl,
+//       the physical gradient of the solution at the GL nodes (d_r_k: GL collocation derivative);
+//   grad_coef_f = M^-1 tw0_vt_fc (J_f n (s_num - s))                 ->  diag(1/(w J)) E^T X,
+//       X = w_f J_f n (s_R - s_L) / 2 at the face nodes (the same values seen from either side);
+//   cv0_vr_fc grad_coef_f (the face's own lifting at its nodes)      ->  lambda X, lambda(t) = sum_m lb[m]^2 / (w J)(t, m):
+//       diagonal in the face nodes because E^T puts a face node's value on one line of volume nodes.
+// Per stage: tp_ns_grad_kernel (state and gradient traces), tp_ns_face_kernel (X, the partial face gradients
+// g_tr + eta lambda X, Roe-Pike / Lax-Friedrichs plus the central viscous flux), tp_ns_volume_kernel (gradient + lifting
+// of X from every face, the Euler and viscous contravariant flux, Dgl^T contraction), then the ordinary lift kernel.
+#pragma once
+
+#include "dgpu_tp.cuh"
+
+namespace dgpu {
+
+// Start index and stride of the line of volume nodes under face node t of local face lf (normal direction nd).
+template <int D, int Q>
+__device__ __forceinline__ void face_line(int nd, int t, int* base, int* stride)
+{
+	const int t0 = (D == 2 ? t : t % Q), t1 = (D == 2 ? 0 : t / Q);
+	if (D == 2) {
+		*stride = (nd == 0 ? 1 : Q);
+		*base = (nd == 0 ? t0 * Q : t0);
+	} else {
+		*stride = (nd == 0 ? 1 : (nd == 1 ? Q : Q * Q));
+		*base = (nd == 0 ? t0 * Q + t1 * Q * Q : (nd == 1 ? t0 + t1 * Q * Q : t0 + t1 * Q));
+	}
+}
+
+// Face node index of volume node `node` on a face with normal direction nd (tangential directions ascending).
+template <int D, int Q>
+__device__ __forceinline__ int face_node_of(int node, int nd)
+{
+	const int c0 = node_coord<Q>(node, 0), c1 = node_coord<Q>(node, 1), c2 = (D == 3 ? node_coord<Q>(node, 2) : 0);
+	if (D == 2)
+		return nd == 0 ? c1 : c0;
+	return nd == 0 ? c1 + Q * c2 : (nd == 1 ? c0 + Q * c2 : c0 + Q * c1);
+}
+
+// lambda(t) of every face side at its own nodes (setup).
+template <int D, int Q>
+__global__ void __launch_bounds__(256) tp_ns_lambda_kernel(const TPOps ops, const TPParams P, double* lam)
+{
+	using S = TPShape<D, Q>;
+	constexpr int NF = S::NF, N = S::N;
+	const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= (long long)P.n_vol * 2 * D * NF)
+		return;
+	const int v = (int)(gid / (2 * D * NF)), r = (int)(gid % (2 * D * NF));
+	const int lf = r / NF, t = r % NF, nd = lf >> 1, side = lf & 1;
+	int base, stride;
+	face_line<D, Q>(nd, t, &base, &stride);
+	double s = 0.0;
+	for (int m = 0; m < Q; ++m) {
+		const double l = ops.lb[side][m];
+		s += l * l * P.inv_wJ[(size_t)v * N + base + m * stride];
+	}
+	lam[(size_t)P.vol_face[(size_t)v * 2 * D + lf] * NF + t] = s;
+}
+
+// Shared memory per element of the two NS element kernels (doubles): the state and D gradient components.
+template <int D, int Q, int NV>
+struct NsSmem {
+	static constexpr int PER_E = (1 + D) * NV * TPShape<D, Q>::N;
+};
+
+// GL values of the element into su (from GLL coefficients when GLL_IN), the GL collocation derivatives into sd and
+// the physical volume gradient at this thread's node into g. All threads call it (it synchronises).
+template <int D, int Q, int NV, bool GLL_IN>
+__device__ __forceinline__ void ns_element_gradient(const TPOps* sops, const TPParams& P, int v, int node, bool active,
+                                                    double* su, double* sd, double (*g)[NV])
+{
+	constexpr int N = TPShape<D, Q>::N;
+	if (GLL_IN) {
+		tp_apply<D, Q, NV>(su, sd, sd + NV * N, sops->B, node, active);
+		if (active)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				su[k * N + node] = sd[k * N + node];
+		__syncthreads();
+	}
+	if (active)
+#pragma unroll
+		for (int k = 0; k < D; ++k)
+			tp_pass<D, Q, NV>(su, sd + k * NV * N, sops->Dgl, k, node);
+	__syncthreads();
+	if (active) {
+		const double iwJ = P.inv_wJ[(size_t)v * N + node];
+		double gm[D * D];
+#pragma unroll
+		for (int c = 0; c < D * D; ++c)
+			gm[c] = P.gmet[((size_t)v * D * D + c) * N + node];
+#pragma unroll
+		for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+			for (int var = 0; var < NV; ++var) {
+				double a = 0.0;
+#pragma unroll
+				for (int k = 0; k < D; ++k)
+					a += gm[k * D + dir] * sd[(k * NV + var) * N + node];   // w J dr_k/dx_dir d_r_k u
+				g[dir][var] = iwJ * a;
+			}
+	}
+	__syncthreads();
+}
+
+template <int D, int Q, int NV, bool GLL_IN>
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
+tp_ns_grad_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u)
+{
+	using S = TPShape<D, Q>;
+	constexpr int N = S::N, NF = S::NF, E = S::E, PER_E = NsSmem<D, Q, NV>::PER_E;
+	extern __shared__ double smem[];
+	TPOps* sops = reinterpret_cast<TPOps*>(smem);
+	double* base = smem + sizeof(TPOps) / 8;
+	load_ops(sops, ops);
+	const int tid = threadIdx.x, v0 = blockIdx.x * E, n_here = min(E, P.n_vol - v0);
+	for (int i = tid; i < n_here * NV * N; i += blockDim.x)
+		base[(i / (NV * N)) * PER_E + i % (NV * N)] = u[(size_t)v0 * NV * N + i];
+	__syncthreads();
+	const int e = tid / N, node = tid % N;
+	const bool active = e < n_here;
+	double* su = base + e * PER_E;
+	double* sd = su + NV * N;
+	const int v = v0 + e;
+	double g[D][NV];
+	ns_element_gradient<D, Q, NV, GLL_IN>(sops, P, v, node, active, su, sd, g);
+	if (active)
+#pragma unroll
+		for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+			for (int var = 0; var < NV; ++var)
+				sd[(dir * NV + var) * N + node] = g[dir][var];
+	__syncthreads();
+	if (!active)
+		return;
+	// traces of the state and of the volume gradient on the 2D local faces
+	for (int it = node; it < 2 * D * NF; it += N) {
+		const int lf = it / NF, t = it % NF, nd = lf >> 1, side = lf & 1;
+		int b, stride;
+		face_line<D, Q>(nd, t, &b, &stride);
+		const int fs = P.vol_face[(size_t)v * 2 * D + lf];
+		double* ds = P.traces + (size_t)fs * NV * NF;
+		double* dg = P.ns_gtr + (size_t)fs * D * NV * NF;
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			double s = 0.0;
+#pragma unroll
+			for (int m = 0; m < Q; ++m)
+				s += sops->lb[side][m] * su[k * N + b + m * stride];
+			ds[k * NF + t] = s;
+		}
+		for (int c = 0; c < D * NV; ++c) {
+			double s = 0.0;
+#pragma unroll
+			for (int m = 0; m < Q; ++m)
+				s += sops->lb[side][m] * sd[c * N + b + m * stride];
+			dg[c * NF + t] = s;
+		}
+	}
+}
+
+template <int D, int Q, int FLUX>
+__global__ void __launch_bounds__(128) tp_ns_face_kernel(const TPParams P)
+{
+	using S = TPShape<D, Q>;
+	constexpr int NF = S::NF, NV = D + 2;
+	const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= P.n_face * NF)
+		return;
+	const int f = gid / NF, t = gid % NF;
+	const int tR = P.nc ? P.nc[(size_t)f * NF + t] : t;
+	const double* fg = P.fgeo + (size_t)f * (D + 1) * NF;
+	double n[D], WL[NV], WR[NV];
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		n[k] = fg[k * NF + t];
+	const double sc = fg[D * NF + t];
+#pragma unroll
+	for (int k = 0; k < NV; ++k) {
+		WL[k] = P.traces[(size_t)(2 * f) * NV * NF + k * NF + t];
+		WR[k] = P.traces[(size_t)(2 * f + 1) * NV * NF + k * NF + tR];
+	}
+	const double lamL = P.ns_lam[(size_t)(2 * f) * NF + t], lamR = P.ns_lam[(size_t)(2 * f + 1) * NF + tR];
+	const double* gL = P.ns_gtr + (size_t)(2 * f) * D * NV * NF;
+	const double* gR = P.ns_gtr + (size_t)(2 * f + 1) * D * NV * NF;
+	double GL[D][NV], GR[D][NV];
+#pragma unroll
+	for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			const double X = 0.5 * sc * n[dir] * (WR[k] - WL[k]);
+			P.ns_X[((size_t)f * D * NV + dir * NV + k) * NF + t] = X;
+			GL[dir][k] = gL[(dir * NV + k) * NF + t] + P.ns_eta * lamL * X;
+			GR[dir][k] = gR[(dir * NV + k) * NF + tR] + P.ns_eta * lamR * X;
+		}
+	double nF[NV];
+	if constexpr (FLUX == kRoePike)
+		num_flux_roe_pike<D>(WL, WR, n, nF);
+	else
+		num_flux_lax_friedrichs<D>(WL, WR, n, nF);
+	double FL[D][NV], FR[D][NV];
+#pragma unroll
+	for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			FL[dir][k] = FR[dir][k] = 0.0;
+	ns_viscous_sub<D, double>(WL, GL, P.ns, FL);
+	ns_viscous_sub<D, double>(WR, GR, P.ns, FR);
+	double* out = P.nnf + (size_t)f * NV * NF;
+#pragma unroll
+	for (int k = 0; k < NV; ++k) {
+		double s = 0.0;
+#pragma unroll
+		for (int dir = 0; dir < D; ++dir)
+			s += n[dir] * (FL[dir][k] + FR[dir][k]);
+		out[k * NF + t] = (nF[k] + 0.5 * s) * sc;
+	}
+}
+
+template <int D, int Q, int NV, bool GLL_IN>
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
+tp_ns_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict__ u)
+{
+	using S = TPShape<D, Q>;
+	constexpr int N = S::N, NF = S::NF, E = S::E, PER_E = NsSmem<D, Q, NV>::PER_E;
+	extern __shared__ double smem[];
+	TPOps* sops = reinterpret_cast<TPOps*>(smem);
+	double* base = smem + sizeof(TPOps) / 8;
+	load_ops(sops, ops);
+	const int tid = threadIdx.x, v0 = blockIdx.x * E, n_here = min(E, P.n_vol - v0);
+	for (int i = tid; i < n_here * NV * N; i += blockDim.x)
+		base[(i / (NV * N)) * PER_E + i % (NV * N)] = u[(size_t)v0 * NV * N + i];
+	__syncthreads();
+	const int e = tid / N, node = tid % N;
+	const bool active = e < n_here;
+	double* su = base + e * PER_E;
+	double* sf = su + NV * N;
+	const int v = v0 + e;
+	double g[D][NV];
+	ns_element_gradient<D, Q, NV, GLL_IN>(sops, P, v, node, active, su, sf, g);
+	double fr[D][NV];
+	if (active) {
+		// + the lifting of every face's X (BR2 total gradient): inv_wJ lb[side][m] X at this node
+		const double iwJ = P.inv_wJ[(size_t)v * N + node];
+#pragma unroll
+		for (int lf = 0; lf < 2 * D; ++lf) {
+			const int nd = lf >> 1, side = lf & 1;
+			const int tf = face_node_of<D, Q>(node, nd);
+			const int fs = P.vol_face[(size_t)v * 2 * D + lf], f = fs >> 1;
+			const int tX = ((fs & 1) && P.nc_inv) ? P.nc_inv[(size_t)f * NF + tf] : tf;
+			const double c = iwJ * sops->lb[side][node_coord<Q>(node, nd)];
+			const double* X = P.ns_X + (size_t)f * D * NV * NF + tX;
+#pragma unroll
+			for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					g[dir][k] += c * X[(dir * NV + k) * NF];
+		}
+		double W[NV], gm[D * D];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			W[k] = su[k * N + node];
+#pragma unroll
+		for (int c = 0; c < D * D; ++c)
+			gm[c] = P.gmet[((size_t)v * D * D + c) * N + node];
+		euler_flux_ref<D>(W, gm, fr);
+		double Fv[D][NV];
+#pragma unroll
+		for (int i = 0; i < D; ++i)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				Fv[i][k] = 0.0;
+		ns_viscous_sub<D, double>(W, g, P.ns, Fv);
+#pragma unroll
+		for (int j = 0; j < D; ++j)
+#pragma unroll
+			for (int k = 0; k < NV; ++k) {
+				double a = 0.0;
+#pragma unroll
+				for (int i = 0; i < D; ++i)
+					a += gm[j * D + i] * Fv[i][k];
+				fr[j][k] += a;
+			}
+	}
+	__syncthreads();   // everyone is done with sf's derivatives
+	if (active)
+#pragma unroll
+		for (int j = 0; j < D; ++j)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				sf[(j * NV + k) * N + node] = fr[j][k];
+	__syncthreads();
+	if (!active)
+		return;
+	double acc[NV];
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+		acc[k] = 0.0;
+#pragma unroll
+	for (int j = 0; j < D; ++j) {
+		const int stride = (j == 0 ? 1 : (j == 1 ? Q : Q * Q));
+		const int a = node_coord<Q>(node, j);
+		const int b0 = node - a * stride;
+#pragma unroll
+		for (int m = 0; m < Q; ++m) {
+			const double w = sops->Dgl[m][a];
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				acc[k] += w * sf[(j * NV + k) * N + b0 + m * stride];
+		}
+	}
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+		P.vol_gl[((size_t)v * NV + k) * N + node] = acc[k];
+}
+
+}  // namespace dgpu

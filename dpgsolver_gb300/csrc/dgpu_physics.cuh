@@ -23,7 +23,8 @@ constexpr double kGm1 = 0.4;            // definitions_physics.h:24
 constexpr double kEpsPhys = 1.0e-13;    // definitions_physics.h:30
 constexpr double kEps = 1.0e-15;        // definitions_tol.h:23
 
-enum Pde { kAdvection = 1, kEuler = 3 };
+enum Pde { kAdvection = 1, kEuler = 3, kNavierStokes = 4 };
+enum Viscosity { kViscosityConstant = 101, kViscositySutherland = 102 };   // definitions_physics.h:34-36
 enum NumFlux { kUpwind = 11, kRoePike = 31, kLaxFriedrichs = 32 };
 
 // min_abs_real_T / max_abs_real_T (general/math_functions_T.c:222-236); T = double, or Dual for Jacobians.
@@ -373,6 +374,67 @@ __device__ __forceinline__ T advection_boundary_value(const T& uL, double ext, c
 	for (int k = 0; k < D; ++k)
 		b_dot_n += b[k] * n[k];
 	return b_dot_n <= 0.0 ? T(ext) : uL;
+}
+
+// ---- Navier-Stokes viscous flux -----------------------------------------------------------------------------------
+// Viscous part of the Navier-Stokes flux at one node, subtracted from F[dir][eq] (the reference adds the negated
+// viscous flux to the Euler flux: compute_Flux_12_T with compute_Flux_T_navier_stokes, flux_navier_stokes_T.c:175-284,
+// 1005-1040). W: conserved state; G[dir][var]: its gradient. Velocity gradients (compute_duvw :708-720), stress
+// tau = mu (grad u + grad u^T - 2/3 div u I) (compute_tau :776-799), scaled temperature gradient
+// dTs = grad(E/rho) - 1/2 grad |u|^2 (compute_dTs :905-927), heat flux gamma/Pr mu dTs. mu: constant, or
+// Sutherland's law mu = 0.08 mu_ref sqrt(T) / (1 + 112 / T), T = p / (rho r_s) (compute_mu_sutherland_T,
+// solution_navier_stokes_T.c:246-256, solution_navier_stokes.h:31-32).
+struct NsPhys {
+	double mu, Pr, r_s;
+	int viscosity;
+};
+
+template <int D, typename T>
+__device__ __forceinline__ void ns_viscous_sub(const T* W, const T (*G)[D + 2], const NsPhys& ph, T (*F)[D + 2])
+{
+	const T rho = W[0], E = W[D + 1], rho_inv = 1.0 / rho;
+	T u[D], du[D][D], V2 = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k) {
+		u[k] = W[1 + k] * rho_inv;
+		V2 += u[k] * u[k];
+	}
+#pragma unroll
+	for (int s = 0; s < D; ++s)
+#pragma unroll
+		for (int x = 0; x < D; ++x)
+			du[s][x] = rho_inv * (G[x][1 + s] - G[x][0] * u[s]);
+	T mu = ph.mu;
+	if (ph.viscosity == kViscositySutherland) {
+		const T p = kGm1 * (E - 0.5 * rho * V2), Tt = p / (rho * ph.r_s);
+		mu = 0.08 * ph.mu / (1.0 + 112.0 / Tt) * sqrt(Tt);
+	}
+	T div = 0.0;
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		div += du[k][k];
+	T tau[D][D];
+#pragma unroll
+	for (int a = 0; a < D; ++a)
+#pragma unroll
+		for (int b = 0; b < D; ++b)
+			tau[a][b] = (a == b) ? mu * 2.0 * (du[a][a] - div * (1.0 / 3.0)) : mu * (du[b][a] + du[a][b]);
+	const T kappa = (kGamma / ph.Pr) * mu;
+#pragma unroll
+	for (int x = 0; x < D; ++x) {
+		const T dE_o_rho = rho_inv * rho_inv * (G[x][D + 1] * rho - E * G[x][0]);
+		T dV2 = 0.0, ut = 0.0;
+#pragma unroll
+		for (int k = 0; k < D; ++k) {
+			dV2 += 2.0 * u[k] * du[k][x];
+			ut += u[k] * tau[x][k];
+		}
+		const T dTs = dE_o_rho - 0.5 * dV2;
+#pragma unroll
+		for (int k = 0; k < D; ++k)
+			F[x][1 + k] = F[x][1 + k] - tau[k][x];
+		F[x][D + 1] = F[x][D + 1] - (kappa * dTs + ut);
+	}
 }
 
 }  // namespace dgpu

@@ -68,6 +68,12 @@ struct TPParams {
 	const int* bc_code;        // [b] BC code modulo BC_STEP_SC
 	const double* bc_ext;      // [b][NV][NF] exterior (test case) conserved state at the face nodes
 	BcData bc_data;            // back pressure / total temperature and pressure data
+	// Navier-Stokes (BR2 second-order terms), all nullptr otherwise:
+	double* ns_gtr;            // [face side][D][NV][NF] traces of the volume gradient
+	const double* ns_lam;      // [face side][NF] diagonal of the face's own lifting at its nodes
+	double* ns_X;              // [f][D][NV][NF] w_f J_f n (s_R - s_L) / 2, side-0 node order
+	NsPhys ns;                 // viscosity model and constants
+	double ns_eta;             // BR2 scaling of a face's own lifting in its face gradient
 };
 
 // Right-hand state of face node i of boundary face b: the boundary value of its BC from the interior trace WL.

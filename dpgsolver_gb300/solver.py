@@ -79,6 +79,9 @@ class Simulation:
         phys.positivity = 1 if prob.positivity else 0
         for k in range(3):
             phys.b_adv[k] = float(prob.b_adv[k])
+        ns = getattr(prob, "ns", None)
+        if ns is not None:
+            phys.viscosity, phys.mu, phys.Pr, phys.r_s = int(ns["viscosity"]), ns["mu"], ns["Pr"], ns["r_s"]
         tp = _lib.TPOperators()
         tp.elem_type = ops.e_type
         tp.p = ops.p

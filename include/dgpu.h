@@ -44,6 +44,9 @@ typedef int dgpu_status;
  *  definitions_numerical_flux.h, src/element/definitions_elements.h). */
 #define DGPU_PDE_ADVECTION 1
 #define DGPU_PDE_EULER     3
+#define DGPU_PDE_NAVIER_STOKES 4   /* Euler flux + viscous flux, BR2 second-order terms (dgpu_create only) */
+#define DGPU_VISCOSITY_CONSTANT   101   /* definitions_physics.h:34-36 */
+#define DGPU_VISCOSITY_SUTHERLAND 102
 #define DGPU_NUM_FLUX_UPWIND          11
 #define DGPU_NUM_FLUX_ROE_PIKE        31
 #define DGPU_NUM_FLUX_LAX_FRIEDRICHS  32
@@ -63,6 +66,14 @@ typedef struct {
 	int num_flux;       /* DGPU_NUM_FLUX_*                                                  */
 	int positivity;     /* 1: enforce_positivity_highorder after every RK stage (Euler)     */
 	double b_adv[3];    /* advection velocity (advection only)                              */
+	/* Navier-Stokes only, the test case's constants the reference reads from its input file
+	 * (solution_navier_stokes_T.c:188-255, flux_navier_stokes_T.c:461-482): the viscosity model
+	 * (DGPU_VISCOSITY_CONSTANT: mu; DGPU_VISCOSITY_SUTHERLAND: 0.08 mu sqrt(T) / (1 + 112 / T), T = p / (rho r_s)),
+	 * mu, the Prandtl number and the specific gas constant. The inviscid numerical flux is num_flux; the second-order
+	 * one is BR2 (NUM_FLUX_BR2_STABLE: central flux of the partially corrected gradients, scaling 1.01 * 2d), the only
+	 * explicit DG option of the reference. */
+	int viscosity;
+	double mu, Pr, r_s;
 } dgpu_physics;
 
 /* Tensor-product operator set of one (element type, p): the 1D factors of the reference's Operator::ops_tp

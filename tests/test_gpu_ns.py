@@ -1,0 +1,131 @@
+"""Navier-Stokes on the CUDA path (Euler flux + viscous flux with BR2 gradients in GL nodal space) against the
+oracle's restatement of the reference's data flow (compute_grad_coef_dg_T, constructor_partial_grad_fc_interp,
+the central viscous numerical flux), at <= 1e-12 normwise relative as in test_gpu_parity.py.
+
+On the Taylor-Green vortex the residual (0.5 to 3 here, smaller the finer the mesh) is what remains after terms
+of the size of the background pressure 1 / (gamma Ma^2) (7.9 at Mach 0.3, 71 at Mach 0.1) cancel, so its rounding
+noise relative to max|R| is far above the other cases': the oracle's own response to one-ulp perturbations of its
+input (the noise floor, measured per case) reaches 1.2e-11 on 12^3 p = 3. Those cases are held to
+max(1e-12, 4 x floor); at Mach 0.3 and p <= 2 the floor is below 1e-12 and the plain bound applies.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from dpgsolver_gb300 import _lib
+from dpgsolver_gb300.host import problem as P
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+CASES = {
+    "vortex2d_roe_p3_8": lambda: P.ns_vortex_2d(8, 3, mu=0.01),
+    "vortex2d_lf_p2_6": lambda: P.ns_vortex_2d(6, 2, mu=0.05, num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
+    "vortex2d_suth_p4_4": lambda: P.ns_vortex_2d(4, 4, mu=0.05, viscosity=P.VISCOSITY_SUTHERLAND),
+    "field2d_p3_8": lambda: P.ns_periodic_field_2d(8, 3, mu=0.05),
+    "tgv_p3_4_curved": lambda: P.ns_taylor_green(4, 3, Re=100.0, mach=0.3, amplitude=0.1),
+    "tgv_p2_6": lambda: P.ns_taylor_green(6, 2, Re=400.0, mach=0.3),
+    "tgv_p4_2_lf": lambda: P.ns_taylor_green(2, 4, Re=50.0, mach=0.3, num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
+    "tgv_p1_4_suth": lambda: P.ns_taylor_green(4, 1, Re=200.0, mach=0.3, viscosity=P.VISCOSITY_SUTHERLAND),
+    # many CTAs
+    "tgv_p3_12": lambda: P.ns_taylor_green(12, 3, Re=1600.0, mach=0.3),
+}
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+def noise_floor(o, sol, r_ref, seeds=3):
+    """max over seeds of rel(R(sol (1 +- 2^-52)), R(sol)): the oracle's response to one-ulp input noise."""
+    out = 0.0
+    for seed in range(seeds):
+        noisy = sol * (1.0 + np.random.default_rng(seed).choice([-1.0, 1.0], sol.shape) * 2.0 ** -52)
+        out = max(out, rel(o.compute_rhs(noisy)[0], r_ref))
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_ns_residual_matches_oracle(gpu_lib, name):
+    from dpgsolver_gb300.solver import Simulation
+    prob = CASES[name]()
+    o = oracle.Oracle(prob)
+    r_ref, mx_ref = o.compute_rhs(prob.sol)
+    tol = max(TOL, 4.0 * noise_floor(o, prob.sol, r_ref)) if name.startswith("tgv") else TOL
+    with Simulation(prob) as sim:
+        mx = sim.compute_rhs()
+        r = sim.rhs
+    assert rel(r, r_ref) <= tol
+    assert abs(mx - mx_ref) <= tol * mx_ref
+
+
+def test_ns_mach01_taylor_green_within_the_oracle_noise_floor(gpu_lib):
+    from dpgsolver_gb300.solver import Simulation
+    prob = P.ns_taylor_green(6, 2, Re=1600.0, mach=0.1)
+    o = oracle.Oracle(prob)
+    r_ref, _ = o.compute_rhs(prob.sol)
+    floor = noise_floor(o, prob.sol, r_ref)
+    with Simulation(prob) as sim:
+        sim.compute_rhs()
+        r = sim.rhs
+    assert rel(r, r_ref) <= 4.0 * floor
+
+
+@pytest.mark.parametrize("name", ["vortex2d_roe_p3_8", "tgv_p3_4_curved", "tgv_p2_6"])
+def test_ns_rk3_steps_match_oracle(gpu_lib, name):
+    from dpgsolver_gb300.solver import Simulation
+    prob = CASES[name]()
+    ref = oracle.Oracle(prob)
+    s_ref = prob.sol.copy()
+    for _ in range(4):
+        s_ref, mx_ref, _ = ref.ssp_rk3_step(s_ref, prob.dt)
+    with Simulation(prob) as sim:
+        mx = sim.ssp_rk3_steps(prob.dt, 4)
+        s = sim.sol_coef
+    assert rel(s, s_ref) <= TOL   # the state itself is O(1): no cancellation
+    assert abs(mx - mx_ref) <= 1e-10 * mx_ref
+
+
+def test_ns_zero_viscosity_is_the_euler_path(gpu_lib):
+    """mu = 0: the four-kernel Navier-Stokes stage gives the three-kernel Euler stage's residual (the two are
+    compiled separately, so they may differ by rounding: held to the oracle's noise floor of the Euler case)."""
+    from dpgsolver_gb300.solver import Simulation
+    pn, pe = P.ns_vortex_2d(8, 3, mu=0.0), P.euler_vortex_2d(8, 3)
+    with Simulation(pn) as a, Simulation(pe) as b:
+        a.compute_rhs()
+        b.compute_rhs()
+        ra, rb = a.rhs, b.rhs
+    o = oracle.Oracle(pe)
+    r_ref, _ = o.compute_rhs(pe.sol)
+    assert rel(ra, rb) <= max(TOL, 4.0 * noise_floor(o, pe.sol, r_ref))
+
+
+def test_ns_free_stream(gpu_lib):
+    from dpgsolver_gb300.solver import Simulation
+    for prob in (P.ns_vortex_2d(8, 3), P.ns_taylor_green(4, 3, amplitude=0.1)):
+        vals = [1.0, 0.3, -0.2] + ([0.1] if prob.d == 3 else []) + [2.5]
+        with Simulation(prob) as sim:
+            sim.upload_state(P.constant_state(prob, vals))
+            assert sim.compute_rhs() < 1e-11
+
+
+def test_ns_refusals(gpu_lib):
+    from dpgsolver_gb300.solver import BatchSimulation, Simulation
+    prob = P.ns_vortex_2d(4, 2)
+    with Simulation(prob) as sim:
+        with pytest.raises(_lib.DGPUError) as e:
+            sim.jvp(prob.sol, prob.sol)
+        assert e.value.status == 2
+    with pytest.raises(_lib.DGPUError) as e:
+        BatchSimulation(prob)
+    assert e.value.status == 2
+    bounded = P.euler_channel_2d(4, 2)
+    bounded.pde, bounded.ns = P.PDE_NAVIER_STOKES, {"viscosity": 101, "mu": 0.01, "Pr": 0.72, "r_s": 1.0}
+    with pytest.raises(_lib.DGPUError) as e:
+        Simulation(bounded)
+    assert e.value.status == 2
+    bad = P.ns_vortex_2d(4, 2)
+    bad.ns["Pr"] = 0.0
+    with pytest.raises(_lib.DGPUError) as e:
+        Simulation(bad)
+    assert e.value.status == 1
