@@ -394,6 +394,8 @@ def run_ours(args, rank, world, local_rank):
         res["adjoint"] = adjoint_measurements(torch, sim, prob, args)
     if not args.no_vortex:
         res["vortex2d"] = vortex2d_measurements(torch, stream, args)
+    if prob.d == 3 and not args.no_ns:
+        res["navier_stokes"] = ns_measurements(torch, stream, args)
     if not args.no_mixed:
         res["mixed_types"] = mixed_measurements(torch, stream, args, "types")
         res["mixed"] = mixed_measurements(torch, stream, args, "hex")
@@ -691,6 +693,45 @@ def vortex2d_measurements(torch, stream, args):
     return res
 
 
+def ns_measurements(torch, stream, args):
+    """Navier-Stokes: the Taylor-Green vortex at Re = 1600, Mach 0.1 on HEX 32^3, p = 3 (Roe-Pike + BR2), graph-
+    replayed SSP-RK3 steps and plain residuals; the kinetic energy before and after (it must decay); the CPU oracle
+    on a 6^3 sample of the same element work."""
+    import oracle
+    from dpgsolver_gb300.host.errors import kinetic_energy
+    from dpgsolver_gb300.host.problem import ns_taylor_green
+    from dpgsolver_gb300.solver import Simulation
+    prob = ns_taylor_green(32, 3, Re=1600.0, mach=0.1)
+    sim = Simulation(prob, stream=stream.cuda_stream)
+    n = args.ns_steps
+    sim.ssp_rk3_steps(prob.dt, 1, want_max=False)     # capture the step graph
+    sim.upload_state(prob.sol)
+    ms = _timed(torch, stream, lambda: sim.ssp_rk3_steps(prob.dt, n, want_max=False), 1)
+    final = sim.sol_coef
+    sim.upload_state(prob.sol)
+    k = 20
+    ms_rhs = _timed(torch, stream, lambda: [sim.compute_rhs(want_max=False) for _ in range(k)], 1) / k
+    sim.close()
+    res = {"workload": "3D Navier-Stokes Taylor-Green vortex, Re 1600, Mach 0.1, HEX 32^3 p3, Roe-Pike + BR2",
+           "n_state": prob.n_state, "steps": n, "dt": prob.dt,
+           "value": 3 * prob.n_state * n / (ms * 1e-3), "unit": "DOF-residual-evals/s", "ms_per_step": ms / n,
+           "rhs_value": prob.n_state / (ms_rhs * 1e-3), "rhs_ms": ms_rhs,
+           "kinetic_energy": {"initial": kinetic_energy(prob, prob.sol), "final": kinetic_energy(prob, final)},
+           "launches_per_stage": 4}
+    if not args.no_cpu_baseline:
+        sample = ns_taylor_green(6, 3, Re=1600.0, mach=0.1)
+        o = oracle.Oracle(sample)
+        o.compute_rhs(sample.sol)
+        t0, cnt = time.perf_counter(), 0
+        while time.perf_counter() - t0 < 5.0:
+            o.compute_rhs(sample.sol)
+            cnt += 1
+        el = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": sample.n_state * cnt / el, "unit": "DOF-residual-evals/s", "cores": 1,
+                               "kind": "port", "sample": f"HEX 6^3 p3 Taylor-Green, {cnt} oracle residuals in {el:.1f} s"}
+    return res
+
+
 def _oracle_worker(args):
     """Time the CPU oracle on the sample mesh; returns (DOF-evals/s, n_evals, seconds)."""
     wname, n, seconds = args
@@ -780,6 +821,8 @@ def main():
     ap.add_argument("--only-rk", action="store_true", help="time graph-replayed SSP-RK3 steps only (profiling)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurements")
     ap.add_argument("--no-jacobian", action="store_true", help="skip the block-sparse Jacobian assembly")
+    ap.add_argument("--no-ns", action="store_true", help="skip the Navier-Stokes Taylor-Green measurements")
+    ap.add_argument("--ns-steps", type=int, default=100, help="timed SSP-RK3 steps of the Taylor-Green run")
     ap.add_argument("--adjoint-steps", type=int, default=200)
     ap.add_argument("--adjoint-budget-gb", type=float, default=4.0)
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched mixed-order measurements")

@@ -29,3 +29,14 @@ def l2_entropy_error(prob, sol, s_exact: float = 0.0) -> float:
     s = entropy_at_cubature(prob, sol)
     wJ = prob.ops.w_vc[None, :] * prob.geom.jacobian_det_vc
     return float(np.sqrt(np.sum(wJ * (s - s_exact) ** 2) / np.sum(wJ)))
+
+
+def kinetic_energy(prob, sol) -> float:
+    """Volume-averaged kinetic energy (1/|Omega|) int rho |u|^2 / 2 (the Taylor-Green vortex's dissipation
+    diagnostic), by the volume cubature of a uniform TP problem."""
+    V = prob.ops.cv0_vs_vc()
+    W = np.einsum("cn,vkn->vkc", V, np.asarray(sol))
+    d = prob.d
+    ek = 0.5 * np.sum(W[:, 1:1 + d] ** 2, axis=1) / W[:, 0]
+    wJ = prob.ops.w_vc[None, :] * prob.geom.jacobian_det_vc
+    return float(np.sum(wJ * ek) / np.sum(wJ))
