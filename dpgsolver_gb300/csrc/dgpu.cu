@@ -62,7 +62,7 @@ struct dgpu_ctx {
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
 	bool ns = false;                      // Navier-Stokes: BR2 gradient buffers and the four-kernel stage
 	NsPhys ns_phys = {0.0, 1.0, 1.0, 101};
-	double *ns_gtr = nullptr, *ns_lam = nullptr, *ns_X = nullptr;
+	double *ns_gtr = nullptr, *ns_lam = nullptr, *ns_X = nullptr, *ns_gv = nullptr;
 	int stage_launches = 3;               // kernels per residual evaluation / RK stage
 	int n_bnd = 0;                        // boundary faces (face_vol[2f+1] < 0)
 	int *bnd = nullptr, *bc_code = nullptr;
@@ -123,6 +123,7 @@ struct dgpu_ctx {
 		P.ns_gtr = ns_gtr;
 		P.ns_lam = ns_lam;
 		P.ns_X = ns_X;
+		P.ns_gv = ns_gv;
 		P.ns = ns_phys;
 		P.ns_eta = 1.01 * 2 * d;   // PENALTY_SCALING * NFMAX (compute_face_rlhs_dg_T.c:273-295)
 		return P;
@@ -544,7 +545,7 @@ void free_all(dgpu_ctx* c)
 	}
 	c->timers.clear();
 	void* ptrs[] = {c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
-	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X,
+	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X, c->ns_gv,
 	                c->bnd, c->bc_code, c->bc_ext, c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -1031,6 +1032,7 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		DG_TRY(cudaMalloc((void**)&c->ns_gtr, nF * 2 * d * c->nv * NF * sizeof(double)));
 		DG_TRY(cudaMalloc((void**)&c->ns_lam, nF * 2 * NF * sizeof(double)));
 		DG_TRY(cudaMalloc((void**)&c->ns_X, nF * d * c->nv * NF * sizeof(double)));
+		DG_TRY(cudaMalloc((void**)&c->ns_gv, nV * d * c->nv * N * sizeof(double)));
 		const long long n_lam = (long long)nV * 2 * d * NF;
 		const unsigned g = (unsigned)((n_lam + 255) / 256);
 		switch ((d == 2 ? 10 : 20) + q) {

@@ -10,9 +10,11 @@
 //       X = w_f J_f n (s_R - s_L) / 2 at the face nodes (the same values seen from either side);
 //   cv0_vr_fc grad_coef_f (the face's own lifting at its nodes)      ->  lambda X, lambda(t) = sum_m lb[m]^2 / (w J)(t, m):
 //       diagonal in the face nodes because E^T puts a face node's value on one line of volume nodes.
-// Per stage: tp_ns_grad_kernel (state and gradient traces), tp_ns_face_kernel (X, the partial face gradients
-// g_tr + eta lambda X, Roe-Pike / Lax-Friedrichs plus the central viscous flux), tp_ns_volume_kernel (gradient + lifting
-// of X from every face, the Euler and viscous contravariant flux, Dgl^T contraction), then the ordinary lift kernel.
+// Per stage: tp_ns_grad_kernel (the volume gradient, kept, and the state and gradient traces), tp_ns_face_kernel (X,
+// the partial face gradients g_tr + eta lambda X, Roe-Pike / Lax-Friedrichs plus the central viscous flux),
+// tp_ns_volume_kernel (the kept gradient + the lifting of X from every face, the Euler and viscous contravariant flux,
+// Dgl^T contraction), then the ordinary lift kernel. All three are bound by the FP64 issue rate, so the volume
+// kernel reads the gradient (D NV doubles a node) rather than forming it again (about D (NV Q + NV D) FMAs a node).
 #pragma once
 
 #include "dgpu_tp.cuh"
@@ -135,8 +137,10 @@ tp_ns_grad_kernel(const TPOps ops, const TPParams P, const double* __restrict__ 
 #pragma unroll
 		for (int dir = 0; dir < D; ++dir)
 #pragma unroll
-			for (int var = 0; var < NV; ++var)
+			for (int var = 0; var < NV; ++var) {
 				sd[(dir * NV + var) * N + node] = g[dir][var];
+				P.ns_gv[(((size_t)v * D + dir) * NV + var) * N + node] = g[dir][var];
+			}
 	__syncthreads();
 	if (!active)
 		return;
@@ -243,8 +247,21 @@ tp_ns_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict_
 	double* su = base + e * PER_E;
 	double* sf = su + NV * N;
 	const int v = v0 + e;
+	if (GLL_IN) {   // GL values of the state
+		tp_apply<D, Q, NV>(su, sf, sf + NV * N, sops->B, node, active);
+		if (active)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				su[k * N + node] = sf[k * N + node];
+		__syncthreads();
+	}
 	double g[D][NV];
-	ns_element_gradient<D, Q, NV, GLL_IN>(sops, P, v, node, active, su, sf, g);
+	if (active)
+#pragma unroll
+		for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+			for (int var = 0; var < NV; ++var)
+				g[dir][var] = P.ns_gv[(((size_t)v * D + dir) * NV + var) * N + node];
 	double fr[D][NV];
 	if (active) {
 		// + the lifting of every face's X (BR2 total gradient): inv_wJ lb[side][m] X at this node

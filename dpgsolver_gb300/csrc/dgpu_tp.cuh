@@ -72,6 +72,7 @@ struct TPParams {
 	double* ns_gtr;            // [face side][D][NV][NF] traces of the volume gradient
 	const double* ns_lam;      // [face side][NF] diagonal of the face's own lifting at its nodes
 	double* ns_X;              // [f][D][NV][NF] w_f J_f n (s_R - s_L) / 2, side-0 node order
+	double* ns_gv;             // [v][D][NV][N] volume gradient (physical, at the GL nodes)
 	NsPhys ns;                 // viscosity model and constants
 	double ns_eta;             // BR2 scaling of a face's own lifting in its face gradient
 };
