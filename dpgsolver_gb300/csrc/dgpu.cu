@@ -921,11 +921,8 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 				return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "boundary faces need bc_fc and bc_state_fc");
 			}
 			const int code = mesh->bc_fc[f] % kBcStepSC;
-			if (c->ns) {
-				delete c;
-				return fail(nullptr, DGPU_ERR_UNSUPPORTED, "boundary faces are not provided for Navier-Stokes");
-			}
-			if (code < 0 || (c->pde == DGPU_PDE_EULER ? !bc_is_euler(code) : !bc_is_advection_upwind(code))) {
+			if (code < 0 || (c->ns ? !bc_is_navier_stokes(code)
+			                       : (c->pde == DGPU_PDE_EULER ? !bc_is_euler(code) : !bc_is_advection_upwind(code)))) {
 				delete c;
 				return fail(nullptr, DGPU_ERR_UNSUPPORTED,
 				            "BC code " + std::to_string(mesh->bc_fc[f]) + " is not provided for this pde");

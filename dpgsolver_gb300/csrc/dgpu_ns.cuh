@@ -179,7 +179,8 @@ __global__ void __launch_bounds__(128) tp_ns_face_kernel(const TPParams P)
 	if (gid >= P.n_face * NF)
 		return;
 	const int f = gid / NF, t = gid % NF;
-	const int tR = P.nc ? P.nc[(size_t)f * NF + t] : t;
+	const int b = P.bnd ? P.bnd[f] : -1;   // boundary face: its index in the boundary list
+	const int tR = (b < 0 && P.nc) ? P.nc[(size_t)f * NF + t] : t;
 	const double* fg = P.fgeo + (size_t)f * (D + 1) * NF;
 	double n[D], WL[NV], WR[NV];
 #pragma unroll
@@ -187,13 +188,32 @@ __global__ void __launch_bounds__(128) tp_ns_face_kernel(const TPParams P)
 		n[k] = fg[k * NF + t];
 	const double sc = fg[D * NF + t];
 #pragma unroll
-	for (int k = 0; k < NV; ++k) {
+	for (int k = 0; k < NV; ++k)
 		WL[k] = P.traces[(size_t)(2 * f) * NV * NF + k * NF + t];
-		WR[k] = P.traces[(size_t)(2 * f + 1) * NV * NF + k * NF + tR];
+	int code = 0;
+	if (b < 0) {
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			WR[k] = P.traces[(size_t)(2 * f + 1) * NV * NF + k * NF + tR];
+	} else {
+		// the reference's Navier-Stokes boundary values (set_function_pointers_num_flux_bc_navier_stokes,
+		// face_solver_T.c:277-300): Riemann and supersonic in/outflow as for Euler; the no-slip adiabatic wall keeps
+		// rho and E and mirrors the momentum (boundary_navier_stokes_T.c:258-304)
+		code = P.bc_code[b];
+		if (code == kBcNoSlipAdiabatic) {
+			WR[0] = WL[0];
+#pragma unroll
+			for (int k = 0; k < D; ++k)
+				WR[1 + k] = -WL[1 + k];
+			WR[D + 1] = WL[D + 1];
+		} else {
+			boundary_value<D, NV, kEuler, double>(P, b, t, NF, WL, n, WR);
+		}
 	}
-	const double lamL = P.ns_lam[(size_t)(2 * f) * NF + t], lamR = P.ns_lam[(size_t)(2 * f + 1) * NF + tR];
+	const double lamL = P.ns_lam[(size_t)(2 * f) * NF + t];
+	const double lamR = b < 0 ? P.ns_lam[(size_t)(2 * f + 1) * NF + tR] : lamL;
 	const double* gL = P.ns_gtr + (size_t)(2 * f) * D * NV * NF;
-	const double* gR = P.ns_gtr + (size_t)(2 * f + 1) * D * NV * NF;
+	const double* gR = b < 0 ? P.ns_gtr + (size_t)(2 * f + 1) * D * NV * NF : gL;
 	double GL[D][NV], GR[D][NV];
 #pragma unroll
 	for (int dir = 0; dir < D; ++dir)
@@ -202,7 +222,8 @@ __global__ void __launch_bounds__(128) tp_ns_face_kernel(const TPParams P)
 			const double X = 0.5 * sc * n[dir] * (WR[k] - WL[k]);
 			P.ns_X[((size_t)f * D * NV + dir * NV + k) * NF + t] = X;
 			GL[dir][k] = gL[(dir * NV + k) * NF + t] + P.ns_eta * lamL * X;
-			GR[dir][k] = gR[(dir * NV + k) * NF + tR] + P.ns_eta * lamR * X;
+			// on a boundary face the exterior gradient is the interior one (grad_from_internal; the walls copy it)
+			GR[dir][k] = b < 0 ? gR[(dir * NV + k) * NF + tR] + P.ns_eta * lamR * X : GL[dir][k];
 		}
 	double nF[NV];
 	if constexpr (FLUX == kRoePike)
@@ -224,7 +245,9 @@ __global__ void __launch_bounds__(128) tp_ns_face_kernel(const TPParams P)
 #pragma unroll
 		for (int dir = 0; dir < D; ++dir)
 			s += n[dir] * (FL[dir][k] + FR[dir][k]);
-		out[k * NF + t] = (nF[k] + 0.5 * s) * sc;
+		// an adiabatic wall sets the total normal energy flux to nf_E = 0 (set_provided_Numerical_Flux_members,
+		// numerical_flux_central_T.c:222-231)
+		out[k * NF + t] = (k == D + 1 && code == kBcNoSlipAdiabatic) ? 0.0 : (nF[k] + 0.5 * s) * sc;
 	}
 }
 

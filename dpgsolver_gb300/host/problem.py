@@ -215,6 +215,7 @@ BC_BACKPRESSURE = 103
 BC_TOTAL_TP = 104
 BC_SUPERSONIC_IN = 105
 BC_SUPERSONIC_OUT = 106
+BC_NOSLIP_ADIABATIC = 111
 
 
 def _set_boundaries(prob: DGProblem, side_bc: dict, exterior) -> DGProblem:
@@ -418,3 +419,38 @@ def ns_field_2d(X, Y):
     vel = np.stack([0.3 + 0.2 * np.cos(X + Y), -0.1 + 0.15 * np.sin(2 * X - Y)])
     pr = 1.0 + 0.1 * np.cos(X) * np.sin(2 * Y)
     return primitive_to_conserved(2, rho, vel, pr)
+
+
+def ns_channel(d: int = 2, n: int = 6, p: int = 3, mu: float = 0.01, mach: float = 0.3,
+               num_flux: int = NUM_FLUX_ROE_PIKE, amplitude: float = 0.0, perturb: float = 0.1) -> DGProblem:
+    """Navier-Stokes between no-slip adiabatic walls (BC_NOSLIP_ADIABATIC) at y = 0 and y = 2 pi, periodic in the
+    other directions: rho = 1, p = 1 / (gamma Ma^2), u = sin(y / 2) (1 + perturb cos x), v = perturb sin x sin(y / 2)
+    (zero on the walls), w = 0."""
+    L = 2.0 * math.pi
+    per = tuple(k != 1 for k in range(d))
+    mesh = StructuredMesh(d, n, 0.0, L, periodic=per)
+    ops = TPOperatorSet(mesh.e_type, p)
+    deform = None
+    if amplitude > 0:
+        deform = sinusoidal_deform_2d(amplitude, L) if d == 2 else sinusoidal_deform_3d(amplitude, L)
+    geom = TPGeometry(mesh, ops, deform=deform, curved=amplitude > 0)
+    prob = DGProblem(f"ns_channel_{d}d", d, PDE_NAVIER_STOKES, num_flux, True, np.zeros(3), ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, d + 2, ops.n_vs)), dt=0.0, n_steps=100, ns=_ns_params(mu))
+    x = prob.solution_node_xyz()
+    X, Y = x[..., 0], x[..., 1]
+    wall = np.sin(0.5 * Y)
+    vel = [wall * (1.0 + perturb * np.cos(X)), perturb * np.sin(X) * wall] + ([np.zeros_like(X)] if d == 3 else [])
+    pr = np.full_like(X, 1.0 / (GAMMA * mach * mach))
+    prob.sol = _pack_state(primitive_to_conserved(d, np.ones_like(X), np.stack(vel), pr))
+    prob.dt = stable_dt(prob)
+    sides = {(1, 0): BC_NOSLIP_ADIABATIC, (1, 1): BC_NOSLIP_ADIABATIC}
+    return _set_boundaries(prob, sides, _uniform_flow(d, 1.0, (0.0,) * d, 1.0 / (GAMMA * mach * mach)))
+
+
+def ns_riemann_vortex_2d(n: int = 6, p: int = 3, mu: float = 0.01, num_flux: int = NUM_FLUX_ROE_PIKE) -> DGProblem:
+    """euler_riemann_2d (the curved vortex box with characteristic boundaries on every side) with viscosity mu."""
+    prob = euler_riemann_2d(n, p, num_flux=num_flux)
+    prob.name = "ns_riemann_vortex_2d"
+    prob.pde = PDE_NAVIER_STOKES
+    prob.ns = _ns_params(mu)
+    return prob

@@ -108,7 +108,9 @@ typedef struct {
 	 * bc_fc: n_faces: Face::bc, the reference's BC code (definitions_bc.h), read on boundary faces only and
 	 *   taken modulo BC_STEP_SC = 10000. Euler: BC_RIEMANN 101, BC_SLIPWALL 102, BC_BACKPRESSURE 103,
 	 *   BC_TOTAL_TP 104, BC_SUPERSONIC_IN 105, BC_SUPERSONIC_OUT 106 (boundary_euler_T.c); advection:
-	 *   inflow/outflow/upwind 1-3, 11-13, 41-46, all the upwind boundary value (boundary_advection_T.c:40-77).
+	 *   inflow/outflow/upwind 1-3, 11-13, 41-46, all the upwind boundary value (boundary_advection_T.c:40-77);
+	 *   Navier-Stokes: BC_RIEMANN, BC_SUPERSONIC_IN, BC_SUPERSONIC_OUT (with the interior gradient) and
+	 *   BC_NOSLIP_ADIABATIC 111 (static wall, boundary_navier_stokes_T.c:130-141, 258-304).
 	 *   Other codes: DGPU_ERR_UNSUPPORTED.
 	 * bc_state_fc: n_faces x (n_fc x n_var) row-major: the test case's conserved solution at the face's
 	 *   cubature nodes (constructor_sol_bv(xyz_fc)), the exterior data of Riemann, supersonic inflow and

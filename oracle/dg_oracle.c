@@ -128,9 +128,6 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 		for (int g = 0; g < in->n_groups; ++g)
 			if (!in->groups[g].cv1_vs_vc)
 				return ORACLE_ERR_ARG;
-		for (int f = 0; f < in->n_faces; ++f)
-			if (in->face_vol[2 * f + 1] < 0)
-				return ORACLE_ERR_ARG;
 	}
 	if (in->positivity)   /* the limiter needs every group's Bezier maps */
 		for (int g = 0; g < in->n_groups; ++g)

@@ -70,6 +70,22 @@ static int SUF(boundary_state)(const struct oracle_problem* P, const int bc, con
 		WR[0] = (b_dot_n <= 0.0 ? (Type)ext[0] : WL[0]);   /* inflow: exterior; outflow: interior */
 		return 0;
 	}
+	if (P->pde == ORACLE_PDE_NAVIER_STOKES) {
+		/* set_function_pointers_num_flux_bc_navier_stokes (face_solver_T.c:277-300): Riemann and supersonic
+		 * in/outflow as for Euler, and the no-slip walls; BC_NOSLIP_ADIABATIC 111 (static wall, u_ex = 0):
+		 * rho and E kept, momentum -rhouvw_l + 2 rho u_ex (constructor_Boundary_Value_T_navier_stokes_no_slip_flux_
+		 * general, boundary_navier_stokes_T.c:258-304) */
+		const int b = bc % 10000;
+		if (b == 111) {
+			WR[0] = WL[0];
+			for (int k = 0; k < d; ++k)
+				WR[1 + k] = -WL[1 + k];
+			WR[d + 1] = WL[d + 1];
+			return 0;
+		}
+		if (b != 101 && b != 105 && b != 106)
+			return -1;
+	}
 	switch (bc % 10000) {
 	case 102: {   /* slip wall: rho and E kept, momentum reflected about the face */
 		Type rhoVn = 0.0;
@@ -376,7 +392,13 @@ static void SUF(num_flux_roe)(const int d, const Type* WL, const Type* WR, const
 /* A boundary face (no right volume): the interior trace, the exterior state of its BC at every node, the numerical
  * flux with the interior normal, and the lift into the interior volume only (compute_face_rlhs_T.c:297-310 with
  * Solver_Face_T::constructor_Boundary_Value_fcl, face_solver_T.c:246-274). */
-static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Type* sol, Type* rhs, Type* sL, Type* nnf)
+/* Navier-Stokes: the partially corrected gradient of the interior side (gv + eta gf of this face, cv0_vs_fc) is
+ * also the boundary gradient (constructor_Boundary_Value_T_grad_from_internal; the no-slip walls copy the density and
+ * momentum gradients, boundary_navier_stokes_T.c:306-352), the central viscous flux is added, and on a no-slip
+ * adiabatic wall the total normal energy flux is set to nf_E = 0 (nf_E_provided, set_provided_Numerical_Flux_members,
+ * numerical_flux_central_T.c:222-231; DIABATIC_FLUX_CONSTANT_ZERO). gv, gf: as ns_gradients writes them, else NULL. */
+static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Type* sol, Type* rhs, Type* sL, Type* nnf,
+                              const Type* gv, const Type* gf)
 {
 	const struct oracle_problem* P = &c->P;
 	const int d = P->d, nv = P->n_var, neq = P->n_var;
@@ -389,13 +411,29 @@ static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Typ
 	for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
 		sL[i] = 0.0;
 	SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], &sol[c->state_off[vL]], sL);
+	Type* gp = NULL;
+	if (gv) {
+		const size_t fstride = (size_t)c->max_vs * nv;
+		gp = calloc((size_t)n_fc * nv * d, sizeof(Type));
+		Type* tmp = malloc(sizeof(Type) * fstride);
+		for (int dir = 0; dir < d; ++dir) {
+			const Type* gfL = &gf[((size_t)(2 * f) * d + dir) * fstride];
+			for (size_t i = 0; i < (size_t)FL->n_vs * nv; ++i)
+				tmp[i] = gv[c->n_state * dir + c->state_off[vL] + i] + 1.01 * 2 * d * gfL[i];
+			SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], tmp,
+			            &gp[(size_t)dir * n_fc * nv]);
+		}
+		free(tmp);
+	}
 	for (int i = 0; i < n_fc; ++i) {
 		Type WL[5], WR[5], nF[5];
 		for (int k = 0; k < nv; ++k)
 			WL[k] = sL[i + (size_t)n_fc * k];
 		const double* ni = &nrm[(size_t)i * d];
-		if (SUF(boundary_state)(P, P->bc_fc[f], WL, &ext[(size_t)i * nv], ni, WR) != 0)
+		if (SUF(boundary_state)(P, P->bc_fc[f], WL, &ext[(size_t)i * nv], ni, WR) != 0) {
+			free(gp);
 			return -1;
+		}
 		if (P->pde != ORACLE_PDE_ADVECTION) {
 			if (P->num_flux == ORACLE_NUM_FLUX_ROE_PIKE)
 				SUF(num_flux_roe)(d, WL, WR, ni, nF);
@@ -407,15 +445,31 @@ static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Typ
 				b_dot_n += P->b_adv[k] * ni[k];
 			nF[0] = (b_dot_n > ORACLE_EPS ? b_dot_n * WL[0] : b_dot_n * WR[0]);
 		}
+		if (gp) {
+			Type G[15], FvL[15], FvR[15];
+			for (int var = 0; var < nv; ++var)
+				for (int x = 0; x < d; ++x)
+					G[x + d * var] = gp[(size_t)x * n_fc * nv + i + (size_t)n_fc * var];
+			for (int k = 0; k < d * neq; ++k)
+				FvL[k] = FvR[k] = 0.0;
+			SUF(flux_ns_sub)(P, WL, G, FvL);
+			SUF(flux_ns_sub)(P, WR, G, FvR);
+			for (int eq = 0; eq < neq; ++eq)
+				for (int x = 0; x < d; ++x)
+					nF[eq] += 0.5 * ni[x] * (FvL[x + d * eq] + FvR[x + d * eq]);
+			if (P->bc_fc[f] % 10000 == 111)
+				nF[d + 1] = 0.0;
+		}
 		for (int k = 0; k < neq; ++k)
 			nnf[i + (size_t)n_fc * k] = nF[k] * jf[i];
 	}
+	free(gp);
 	SUF(mm_acc)(FL->n_vs, n_fc, neq, -1.0, &FL->tw0_vt_fc[(size_t)lfL * FL->n_vs * n_fc], nnf, &rhs[c->state_off[vL]]);
 	return 0;
 }
 
-/* BR2 gradients of the Navier-Stokes residual (compute_grad_coef_dg_T, compute_grad_coef_dg_T.c:60-316) for
- * interior faces and the explicit, non-collocated case:
+/* BR2 gradients of the Navier-Stokes residual (compute_grad_coef_dg_T, compute_grad_coef_dg_T.c:60-316) for the
+ * explicit, non-collocated case:
  *   volume:  grad_coef_v[dir] = M^-1 tw0_vt_vc (sum_k m(., dir, k) cv1_vs_vc[k]) sol   (:168-214, 342-358);
  *   faces:   grad_coef_f[side][dir] = M^-1 tw0_vt_fc (J_f n_dir (s_num - s_side)), the central numerical
  *            solution s_num = (s_L + s_R) / 2 (get_sol_scale :674-686), side 1 in its own face-node order
@@ -474,6 +528,37 @@ static void SUF(ns_gradients)(const struct oracle_ctx* c, const Type* sol, Type*
 		const int* nc = &P->nc_fc[c->fc_off[f]];
 		const double* nrm = &P->normals_fc[c->fc_off[f] * d];
 		const double* jf = &P->jacobian_det_fc[c->fc_off[f]];
+		if (vR < 0) {   /* boundary face: s_num = (s_L + s_b) / 2 with s_b its boundary value
+		                 * (compute_g_coef_related_boundary, compute_grad_coef_dg_T.c:527-640) */
+			const double* ext = &P->bc_state_fc[c->fc_off[f] * nv];
+			for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
+				sL[i] = 0.0;
+			SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], &sol[c->state_off[vL]],
+			            sL);
+			for (int i = 0; i < n_fc; ++i) {
+				Type WL[5], WB[5];
+				for (int k = 0; k < nv; ++k)
+					WL[k] = sL[i + (size_t)n_fc * k];
+				SUF(boundary_state)(P, P->bc_fc[f], WL, &ext[(size_t)i * nv], &nrm[(size_t)i * d], WB);
+				for (int k = 0; k < nv; ++k)
+					sR0[i + (size_t)n_fc * k] = WB[k];
+			}
+			for (int dir = 0; dir < d; ++dir) {
+				for (int var = 0; var < nv; ++var)
+					for (int i = 0; i < n_fc; ++i) {
+						const size_t o = i + (size_t)n_fc * var;
+						X[o] = jf[i] * nrm[(size_t)i * d + dir] * 0.5 * (sR0[o] - sL[o]);
+					}
+				Type* gL = &gf[((size_t)(2 * f) * d + dir) * fstride];
+				for (size_t i = 0; i < fstride; ++i)
+					y[i] = 0.0;
+				SUF(mm_acc)(FL->n_vs, n_fc, nv, 1.0, &FL->tw0_vt_fc[(size_t)lfL * FL->n_vs * n_fc], X, y);
+				SUF(mm_acc)(FL->n_vs, FL->n_vs, nv, 1.0, &c->m_inv[c->minv_off[vL]], y, gL);
+				for (size_t i = 0; i < (size_t)FL->n_vs * nv; ++i)
+					gt[ns * dir + c->state_off[vL] + i] += gL[i];
+			}
+			continue;
+		}
 		for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
 			sL[i] = sR0[i] = 0.0;
 		SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], &sol[c->state_off[vL]], sL);
@@ -592,7 +677,7 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 	for (int f = 0; f < P->n_faces; ++f) {
 		const int vL = P->face_vol[2 * f], vR = P->face_vol[2 * f + 1];
 		if (vR < 0) {
-			if (SUF(boundary_face)(c, f, sol, rhs, sL, nnf) != 0) {
+			if (SUF(boundary_face)(c, f, sol, rhs, sL, nnf, gv, gf) != 0) {
 				free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);
 				free(gv); free(gf); free(gt); free(g_vc); free(gpL); free(gpR0); free(gpR); free(tmp);
 				return ORACLE_ERR_ARG;

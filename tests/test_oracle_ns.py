@@ -109,3 +109,57 @@ def test_viscous_operator_converges_to_the_divergence_of_the_viscous_flux():
         exact = np.transpose(_exact_viscous_divergence(x[..., 0], x[..., 1], mu), (1, 0, 2))
         errs.append(np.max(np.abs(r1 - r0 - exact)))
     assert errs[1] < errs[0] / 3.5      # h^(p-1) = h^2 for p = 3 (observed ratio 4.65)
+
+
+# ---- boundaries: no-slip adiabatic walls and the Euler boundary values with the interior gradient ----------------
+def _at_rest(prob, p):
+    return P.constant_state(prob, [1.0] + [0.0] * prob.d + [p / P.GM1])
+
+
+@pytest.mark.parametrize("d,flux", [(2, P.NUM_FLUX_ROE_PIKE), (3, P.NUM_FLUX_LAX_FRIEDRICHS)])
+def test_fluid_at_rest_between_no_slip_walls_is_steady(d, flux):
+    prob = P.ns_channel(d, 3, 2, num_flux=flux, amplitude=0.05)
+    assert oracle.Oracle(prob).compute_rhs(_at_rest(prob, 2.0))[1] < 1e-11
+
+
+def test_no_slip_walls_conserve_mass():
+    """Lax-Friedrichs with the mirrored momentum and no viscous mass flux: nothing crosses the walls."""
+    prob = P.ns_channel(2, 4, 3, num_flux=P.NUM_FLUX_LAX_FRIEDRICHS)
+    raw = oracle.Oracle(prob).compute_rhs_raw(prob.sol)
+    assert abs(raw[:, 0].sum()) <= 1e-13 * np.abs(raw[:, 0]).sum()
+
+
+def test_adiabatic_walls_conserve_energy():
+    """The wall's normal energy flux is set to zero, so total energy only moves between volumes."""
+    prob = P.ns_channel(2, 4, 3, num_flux=P.NUM_FLUX_ROE_PIKE)
+    raw = oracle.Oracle(prob).compute_rhs_raw(prob.sol)
+    assert abs(raw[:, 3].sum()) <= 1e-12 * np.abs(raw[:, 3]).sum()
+
+
+def test_riemann_boundaries_keep_the_free_stream():
+    prob = P.ns_riemann_vortex_2d(4, 3)
+    vals = [1.0, 1.0, 1.0, 1.0 / P.GM1 + 1.0]   # the exterior stream (1, 1, 1, 1)
+    assert oracle.Oracle(prob).compute_rhs(P.constant_state(prob, vals))[1] < 1e-11
+
+
+@pytest.mark.parametrize("mk", [lambda: P.ns_channel(2, 3, 2, mu=0.05), lambda: P.ns_riemann_vortex_2d(3, 2, mu=0.05),
+                                lambda: P.ns_channel(3, 2, 2, mu=0.05)])
+def test_boundary_complex_step(mk):
+    prob = mk()
+    o = oracle.Oracle(prob)
+    rng = np.random.default_rng(4)
+    base = prob.sol + 1e-2 * rng.standard_normal(prob.sol.shape)
+    dirn = rng.standard_normal(prob.sol.shape)
+    _, ri = o.compute_rhs_cmplx(base, 1e-30 * dirn)
+    jv = ri / 1e-30
+    eps = 1e-6
+    rp, _ = o.compute_rhs(base + eps * dirn)
+    rm, _ = o.compute_rhs(base - eps * dirn)
+    assert np.max(np.abs(jv - (rp - rm) / (2 * eps))) <= 1e-6 * np.max(np.abs(jv))
+
+
+def test_ns_refuses_euler_only_boundaries():
+    prob = P.euler_channel_2d(3, 2)              # slip walls: an Euler boundary the reference's NS does not take
+    prob.pde, prob.ns = P.PDE_NAVIER_STOKES, {"viscosity": 101, "mu": 0.01, "Pr": 0.72, "r_s": 1.0}
+    with pytest.raises(Exception):
+        oracle.Oracle(prob).compute_rhs(prob.sol)
