@@ -63,6 +63,7 @@ struct dgpu_ctx {
 	bool ns = false;                      // Navier-Stokes: BR2 gradient buffers and the four-kernel stage
 	NsPhys ns_phys = {0.0, 1.0, 1.0, 101};
 	double *ns_gtr = nullptr, *ns_lam = nullptr, *ns_X = nullptr, *ns_gv = nullptr;
+	double *ns_gtr_d = nullptr, *ns_X_d = nullptr, *ns_gv_d = nullptr;   // their tangents (linearisations)
 	int stage_launches = 3;               // kernels per residual evaluation / RK stage
 	int n_bnd = 0;                        // boundary faces (face_vol[2f+1] < 0)
 	int *bnd = nullptr, *bc_code = nullptr;
@@ -483,6 +484,57 @@ cudaError_t launch_ns_t(dgpu_ctx* c)
 	return cudaGetLastError();
 }
 
+template <int D, int Q, int NV>
+size_t ns_jvp_smem_bytes()
+{
+	using S = TPShape<D, Q>;
+	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * NsJvpSmem<D, Q, NV>::PER_E * sizeof(double);
+}
+
+// Navier-Stokes R(u) (when PRIMAL) and (dR/du) jv_du: the gradient kernel on u and on du (it is linear), the face and
+// volume kernels on dual numbers, the residual-mode lift on the primal and the tangent buffers.
+template <int D, int Q, int FLUX, bool PRIMAL>
+cudaError_t launch_ns_jvp_t(dgpu_ctx* c)
+{
+	using S = TPShape<D, Q>;
+	constexpr int NV = D + 2;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	const TPParams P = c->params();
+	TPParams Pd = P;
+	Pd.vol_gl = c->jv_vol;
+	Pd.traces = c->jv_traces;
+	Pd.nnf = c->jv_nnf;
+	Pd.ns_gtr = c->ns_gtr_d;
+	Pd.ns_X = c->ns_X_d;
+	Pd.ns_gv = c->ns_gv_d;
+	Pd.max_bits = nullptr;
+	cudaError_t e = PRIMAL ? cudaMemsetAsync(c->max_bits, 0, sizeof(unsigned long long), c->stream) : cudaSuccess;
+	if (e != cudaSuccess)
+		return e;
+	tp_ns_grad_kernel<D, Q, NV, true><<<blocks, S::THREADS, ns_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, P, c->u);
+	tp_ns_grad_kernel<D, Q, NV, true><<<blocks, S::THREADS, ns_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, Pd,
+	                                                                                               c->jv_du);
+	const long long nf = (long long)c->n_face * S::NF;
+	tp_ns_jvp_face_kernel<D, Q, FLUX><<<(unsigned)((nf + 127) / 128), 128, 0, c->stream>>>(P, Pd);
+	tp_ns_jvp_volume_kernel<D, Q, NV><<<blocks, S::THREADS, ns_jvp_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, P, Pd, c->u, c->jv_du);
+	RkArgs rk;
+	rk.u = c->u;
+	rk.u0 = c->u0;
+	rk.rhs = c->rhs;
+	rk.dt = 0.0;
+	rk.stage = 0;
+	rk.positivity = 0;
+	rk.want_max = 1;
+	if (PRIMAL)
+		tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, P,
+		                                                                                                   rk);
+	rk.rhs = c->jv_out;
+	tp_lift_kernel<D, Q, NV, kModeRhs><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, Pd, rk);
+	c->launches += PRIMAL ? 6 : 5;
+	return cudaGetLastError();
+}
+
 cudaError_t launch_nothing(dgpu_ctx*) { return cudaSuccess; }
 
 template <int D, int Q, int FLUX>
@@ -497,9 +549,11 @@ cudaError_t bind_ns(dgpu_ctx* c)
 	c->launch_face = launch_nothing;
 	c->launch_adjoint = nullptr;
 	c->launch_objective = nullptr;
-	c->launch_jvp = nullptr;
-	c->launch_jvp_tangent = nullptr;
+	c->launch_jvp = launch_ns_jvp_t<D, Q, FLUX, true>;
+	c->launch_jvp_tangent = launch_ns_jvp_t<D, Q, FLUX, false>;
 	const cudaFuncAttribute smem = cudaFuncAttributeMaxDynamicSharedMemorySize;
+	if ((e = cudaFuncSetAttribute(tp_ns_jvp_volume_kernel<D, Q, NV>, smem, (int)ns_jvp_smem_bytes<D, Q, NV>())))
+		return e;
 	const int bytes = (int)ns_smem_bytes<D, Q, NV>();
 	if ((e = cudaFuncSetAttribute(tp_ns_grad_kernel<D, Q, NV, true>, smem, bytes)) ||
 	    (e = cudaFuncSetAttribute(tp_ns_grad_kernel<D, Q, NV, false>, smem, bytes)) ||
@@ -545,7 +599,7 @@ void free_all(dgpu_ctx* c)
 	}
 	c->timers.clear();
 	void* ptrs[] = {c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
-	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X, c->ns_gv,
+	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X, c->ns_gv, c->ns_gtr_d, c->ns_X_d, c->ns_gv_d,
 	                c->bnd, c->bc_code, c->bc_ext, c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -1698,6 +1752,11 @@ dgpu_status ensure_jvp_buffers(dgpu_ctx* c)
 		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_traces, nt * sizeof(double)));
 		DGPU_CUDA(c, cudaMalloc((void**)&c->jv_nnf, nt / 2 * sizeof(double)));
 	}
+	if (c->ns && !c->ns_gv_d) {
+		DGPU_CUDA(c, cudaMalloc((void**)&c->ns_gtr_d, nt * c->d * sizeof(double)));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->ns_X_d, nt / 2 * c->d * sizeof(double)));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->ns_gv_d, ns * c->d * sizeof(double)));
+	}
 	return DGPU_OK;
 }
 
@@ -1771,8 +1830,6 @@ extern "C" dgpu_status dgpu_jacobian_structure(dgpu_ctx* c, int* block_size, lon
 {
 	if (!c)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	if (c->ns)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_jacobian_structure is not provided for Navier-Stokes");
 	const dgpu_status st = jacobian_setup(c);
 	if (st != DGPU_OK)
 		return st;
@@ -1790,8 +1847,6 @@ extern "C" dgpu_status dgpu_jacobian_bsr(dgpu_ctx* c, const double* sol, int raw
 {
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	if (c->ns)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_jacobian_bsr is not provided for Navier-Stokes");
 	dgpu_status st = jacobian_setup(c);
 	if (st == DGPU_OK)
 		st = ensure_jvp_buffers(c);
@@ -1862,8 +1917,6 @@ extern "C" dgpu_status dgpu_jvp(dgpu_ctx* c, const double* sol, const double* di
 {
 	if (!c || !sol || !dir || !jv)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	if (c->ns)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_jvp is not provided for Navier-Stokes");
 	const size_t ns = state_size(c);
 	{
 		const dgpu_status st = ensure_jvp_buffers(c);

@@ -17,6 +17,8 @@
 // kernel reads the gradient (D NV doubles a node) rather than forming it again (about D (NV Q + NV D) FMAs a node).
 #pragma once
 
+#include <type_traits>
+
 #include "dgpu_tp.cuh"
 
 namespace dgpu {
@@ -170,31 +172,44 @@ tp_ns_grad_kernel(const TPOps ops, const TPParams P, const double* __restrict__ 
 	}
 }
 
-template <int D, int Q, int FLUX>
-__global__ void __launch_bounds__(128) tp_ns_face_kernel(const TPParams P)
+// Scalar helpers of the face and volume bodies below: T = double (the residual) or Dual<1> (the residual and its
+// directional derivative, the tangent quantities read from and written to a second parameter set Pd).
+__device__ __forceinline__ void ns_set(double& x, double v, double) { x = v; }
+__device__ __forceinline__ void ns_set(Dual<1>& x, double v, double d)
 {
-	using S = TPShape<D, Q>;
-	constexpr int NF = S::NF, NV = D + 2;
-	const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-	if (gid >= P.n_face * NF)
-		return;
-	const int f = gid / NF, t = gid % NF;
+	x.v = v;
+	x.d[0] = d;
+}
+__device__ __forceinline__ double ns_val(const double& x) { return x; }
+__device__ __forceinline__ double ns_val(const Dual<1>& x) { return x.v; }
+__device__ __forceinline__ double ns_der(const double&) { return 0.0; }
+__device__ __forceinline__ double ns_der(const Dual<1>& x) { return x.d[0]; }
+
+// One face node: the boundary value or right trace, X, the partial face gradients, Roe-Pike / Lax-Friedrichs plus
+// the central viscous flux, times w_f J_f. With T = Dual<1> the tangent traces, gradient traces and outputs are Pd's.
+template <int D, int Q, int FLUX, typename T>
+__device__ __forceinline__ void ns_face_node(const TPParams& P, const TPParams& Pd, int f, int t)
+{
+	constexpr int NF = TPShape<D, Q>::NF, NV = D + 2;
+	constexpr bool TAN = !std::is_same<T, double>::value;
 	const int b = P.bnd ? P.bnd[f] : -1;   // boundary face: its index in the boundary list
 	const int tR = (b < 0 && P.nc) ? P.nc[(size_t)f * NF + t] : t;
 	const double* fg = P.fgeo + (size_t)f * (D + 1) * NF;
-	double n[D], WL[NV], WR[NV];
+	double n[D];
+	T WL[NV], WR[NV];
 #pragma unroll
 	for (int k = 0; k < D; ++k)
 		n[k] = fg[k * NF + t];
 	const double sc = fg[D * NF + t];
+	const size_t oL = (size_t)(2 * f) * NV * NF, oR = (size_t)(2 * f + 1) * NV * NF;
 #pragma unroll
 	for (int k = 0; k < NV; ++k)
-		WL[k] = P.traces[(size_t)(2 * f) * NV * NF + k * NF + t];
+		ns_set(WL[k], P.traces[oL + k * NF + t], TAN ? Pd.traces[oL + k * NF + t] : 0.0);
 	int code = 0;
 	if (b < 0) {
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			WR[k] = P.traces[(size_t)(2 * f + 1) * NV * NF + k * NF + tR];
+			ns_set(WR[k], P.traces[oR + k * NF + tR], TAN ? Pd.traces[oR + k * NF + tR] : 0.0);
 	} else {
 		// the reference's Navier-Stokes boundary values (set_function_pointers_num_flux_bc_navier_stokes,
 		// face_solver_T.c:277-300): Riemann and supersonic in/outflow as for Euler; the no-slip adiabatic wall keeps
@@ -207,48 +222,82 @@ __global__ void __launch_bounds__(128) tp_ns_face_kernel(const TPParams P)
 				WR[1 + k] = -WL[1 + k];
 			WR[D + 1] = WL[D + 1];
 		} else {
-			boundary_value<D, NV, kEuler, double>(P, b, t, NF, WL, n, WR);
+			boundary_value<D, NV, kEuler, T>(P, b, t, NF, WL, n, WR);
 		}
 	}
 	const double lamL = P.ns_lam[(size_t)(2 * f) * NF + t];
 	const double lamR = b < 0 ? P.ns_lam[(size_t)(2 * f + 1) * NF + tR] : lamL;
-	const double* gL = P.ns_gtr + (size_t)(2 * f) * D * NV * NF;
-	const double* gR = b < 0 ? P.ns_gtr + (size_t)(2 * f + 1) * D * NV * NF : gL;
-	double GL[D][NV], GR[D][NV];
+	const size_t gL = (size_t)(2 * f) * D * NV * NF, gR = (size_t)(2 * f + 1) * D * NV * NF;
+	T GL[D][NV], GR[D][NV];
 #pragma unroll
 	for (int dir = 0; dir < D; ++dir)
 #pragma unroll
 		for (int k = 0; k < NV; ++k) {
-			const double X = 0.5 * sc * n[dir] * (WR[k] - WL[k]);
-			P.ns_X[((size_t)f * D * NV + dir * NV + k) * NF + t] = X;
-			GL[dir][k] = gL[(dir * NV + k) * NF + t] + P.ns_eta * lamL * X;
+			const T X = (0.5 * sc * n[dir]) * (WR[k] - WL[k]);
+			const size_t ox = ((size_t)f * D * NV + dir * NV + k) * NF + t;
+			P.ns_X[ox] = ns_val(X);
+			if (TAN)
+				Pd.ns_X[ox] = ns_der(X);
+			const size_t cl = gL + (dir * NV + k) * NF + t;
+			T g;
+			ns_set(g, P.ns_gtr[cl], TAN ? Pd.ns_gtr[cl] : 0.0);
+			GL[dir][k] = g + (P.ns_eta * lamL) * X;
 			// on a boundary face the exterior gradient is the interior one (grad_from_internal; the walls copy it)
-			GR[dir][k] = b < 0 ? gR[(dir * NV + k) * NF + tR] + P.ns_eta * lamR * X : GL[dir][k];
+			if (b < 0) {
+				const size_t cr = gR + (dir * NV + k) * NF + tR;
+				ns_set(g, P.ns_gtr[cr], TAN ? Pd.ns_gtr[cr] : 0.0);
+				GR[dir][k] = g + (P.ns_eta * lamR) * X;
+			} else {
+				GR[dir][k] = GL[dir][k];
+			}
 		}
-	double nF[NV];
+	T nF[NV];
 	if constexpr (FLUX == kRoePike)
-		num_flux_roe_pike<D>(WL, WR, n, nF);
+		num_flux_roe_pike<D, T>(WL, WR, n, nF);
 	else
-		num_flux_lax_friedrichs<D>(WL, WR, n, nF);
-	double FL[D][NV], FR[D][NV];
+		num_flux_lax_friedrichs<D, T>(WL, WR, n, nF);
+	T FL[D][NV], FR[D][NV];
 #pragma unroll
 	for (int dir = 0; dir < D; ++dir)
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			FL[dir][k] = FR[dir][k] = 0.0;
-	ns_viscous_sub<D, double>(WL, GL, P.ns, FL);
-	ns_viscous_sub<D, double>(WR, GR, P.ns, FR);
-	double* out = P.nnf + (size_t)f * NV * NF;
+			FL[dir][k] = FR[dir][k] = T(0.0);
+	ns_viscous_sub<D, T>(WL, GL, P.ns, FL);
+	ns_viscous_sub<D, T>(WR, GR, P.ns, FR);
+	const size_t on = (size_t)f * NV * NF + t;
 #pragma unroll
 	for (int k = 0; k < NV; ++k) {
-		double s = 0.0;
+		T s = T(0.0);
 #pragma unroll
 		for (int dir = 0; dir < D; ++dir)
-			s += n[dir] * (FL[dir][k] + FR[dir][k]);
+			s = s + n[dir] * (FL[dir][k] + FR[dir][k]);
 		// an adiabatic wall sets the total normal energy flux to nf_E = 0 (set_provided_Numerical_Flux_members,
 		// numerical_flux_central_T.c:222-231)
-		out[k * NF + t] = (k == D + 1 && code == kBcNoSlipAdiabatic) ? 0.0 : (nF[k] + 0.5 * s) * sc;
+		const bool wall_E = (k == D + 1 && code == kBcNoSlipAdiabatic);
+		const T o = (nF[k] + 0.5 * s) * sc;
+		P.nnf[on + k * NF] = wall_E ? 0.0 : ns_val(o);
+		if (TAN)
+			Pd.nnf[on + k * NF] = wall_E ? 0.0 : ns_der(o);
 	}
+}
+
+template <int D, int Q, int FLUX>
+__global__ void __launch_bounds__(128) tp_ns_face_kernel(const TPParams P)
+{
+	constexpr int NF = TPShape<D, Q>::NF;
+	const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid < P.n_face * NF)
+		ns_face_node<D, Q, FLUX, double>(P, P, gid / NF, gid % NF);
+}
+
+// The face kernel on dual numbers: primal outputs to P, tangent outputs to Pd (forward-mode linearisation).
+template <int D, int Q, int FLUX>
+__global__ void __launch_bounds__(128) tp_ns_jvp_face_kernel(const TPParams P, const TPParams Pd)
+{
+	constexpr int NF = TPShape<D, Q>::NF;
+	const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid < P.n_face * NF)
+		ns_face_node<D, Q, FLUX, Dual<1>>(P, Pd, gid / NF, gid % NF);
 }
 
 template <int D, int Q, int NV, bool GLL_IN>
@@ -359,6 +408,136 @@ tp_ns_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict_
 #pragma unroll
 	for (int k = 0; k < NV; ++k)
 		P.vol_gl[((size_t)v * NV + k) * N + node] = acc[k];
+}
+
+// Volume term on dual numbers (forward-mode linearisation): the state and its direction from GLL coefficients u, du;
+// the kept gradients (P.ns_gv, Pd.ns_gv) plus the liftings of X and its tangent; the Euler and viscous contravariant
+// flux on Dual<1>; the Dgl^T contraction of the value into P.vol_gl, then of the derivative into Pd.vol_gl.
+template <int D, int Q, int NV>
+struct NsJvpSmem {
+	static constexpr int PER_E = (2 + D) * NV * TPShape<D, Q>::N;   // su, sud, sf (also V's temporaries)
+};
+
+template <int D, int Q, int NV>
+__global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
+tp_ns_jvp_volume_kernel(const TPOps ops, const TPParams P, const TPParams Pd, const double* __restrict__ u,
+                        const double* __restrict__ du)
+{
+	using S = TPShape<D, Q>;
+	constexpr int N = S::N, NF = S::NF, E = S::E, PER_E = NsJvpSmem<D, Q, NV>::PER_E;
+	extern __shared__ double smem[];
+	TPOps* sops = reinterpret_cast<TPOps*>(smem);
+	double* base = smem + sizeof(TPOps) / 8;
+	load_ops(sops, ops);
+	const int tid = threadIdx.x, v0 = blockIdx.x * E, n_here = min(E, P.n_vol - v0);
+	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {
+		const int e = i / (NV * N), r = i % (NV * N);
+		base[e * PER_E + r] = u[(size_t)v0 * NV * N + i];
+		base[e * PER_E + NV * N + r] = du[(size_t)v0 * NV * N + i];
+	}
+	__syncthreads();
+	const int e = tid / N, node = tid % N;
+	const bool active = e < n_here;
+	double* su = base + e * PER_E;
+	double* sud = su + NV * N;
+	double* sf = sud + NV * N;
+	tp_apply<D, Q, NV>(su, sf, sf + NV * N, sops->B, node, active);
+	if (active)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			su[k * N + node] = sf[k * N + node];
+	__syncthreads();
+	tp_apply<D, Q, NV>(sud, sf, sf + NV * N, sops->B, node, active);
+	if (active)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			sud[k * N + node] = sf[k * N + node];
+	__syncthreads();
+	const int v = v0 + e;
+	Dual<1> fr[D][NV];
+	if (active) {
+		Dual<1> g[D][NV], W[NV];
+#pragma unroll
+		for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+			for (int var = 0; var < NV; ++var) {
+				const size_t o = (((size_t)v * D + dir) * NV + var) * N + node;
+				ns_set(g[dir][var], P.ns_gv[o], Pd.ns_gv[o]);
+			}
+		const double iwJ = P.inv_wJ[(size_t)v * N + node];
+#pragma unroll
+		for (int lf = 0; lf < 2 * D; ++lf) {
+			const int nd = lf >> 1, side = lf & 1;
+			const int tf = face_node_of<D, Q>(node, nd);
+			const int fs = P.vol_face[(size_t)v * 2 * D + lf], f = fs >> 1;
+			const int tX = ((fs & 1) && P.nc_inv) ? P.nc_inv[(size_t)f * NF + tf] : tf;
+			const double c = iwJ * sops->lb[side][node_coord<Q>(node, nd)];
+			const size_t ox = (size_t)f * D * NV * NF + tX;
+#pragma unroll
+			for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+				for (int k = 0; k < NV; ++k) {
+					g[dir][k].v += c * P.ns_X[ox + (dir * NV + k) * NF];
+					g[dir][k].d[0] += c * Pd.ns_X[ox + (dir * NV + k) * NF];
+				}
+		}
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			ns_set(W[k], su[k * N + node], sud[k * N + node]);
+		double gm[D * D];
+#pragma unroll
+		for (int c = 0; c < D * D; ++c)
+			gm[c] = P.gmet[((size_t)v * D * D + c) * N + node];
+		euler_flux_ref<D, Dual<1>>(W, gm, fr);
+		Dual<1> Fv[D][NV];
+#pragma unroll
+		for (int i = 0; i < D; ++i)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				Fv[i][k] = Dual<1>(0.0);
+		ns_viscous_sub<D, Dual<1>>(W, g, P.ns, Fv);
+#pragma unroll
+		for (int j = 0; j < D; ++j)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+#pragma unroll
+				for (int i = 0; i < D; ++i)
+					fr[j][k] = fr[j][k] + gm[j * D + i] * Fv[i][k];
+	}
+	// contraction of the value, then of the derivative, through the same shared buffer
+	for (int pass = 0; pass < 2; ++pass) {
+		__syncthreads();
+		if (active)
+#pragma unroll
+			for (int j = 0; j < D; ++j)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					sf[(j * NV + k) * N + node] = pass == 0 ? fr[j][k].v : fr[j][k].d[0];
+		__syncthreads();
+		if (active) {
+			double acc[NV];
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				acc[k] = 0.0;
+#pragma unroll
+			for (int j = 0; j < D; ++j) {
+				const int stride = (j == 0 ? 1 : (j == 1 ? Q : Q * Q));
+				const int a = node_coord<Q>(node, j);
+				const int b0 = node - a * stride;
+#pragma unroll
+				for (int m = 0; m < Q; ++m) {
+					const double w = sops->Dgl[m][a];
+#pragma unroll
+					for (int k = 0; k < NV; ++k)
+						acc[k] += w * sf[(j * NV + k) * N + b0 + m * stride];
+				}
+			}
+			double* out = pass == 0 ? P.vol_gl : Pd.vol_gl;
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				out[((size_t)v * NV + k) * N + node] = acc[k];
+		}
+	}
 }
 
 }  // namespace dgpu

@@ -193,7 +193,8 @@ dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const dgpu_tp_ope
  * has no adjoint: it linearises the same residual by complex step (compute_lhs_cmplx_step_dg,
  * src/testing/support/simulation/solvers/dg/test_support_solve_dg.c:83-110) and assembles its Jacobian for the
  * implicit solver (compute_rlhs_dg, src/simulation/solvers/dg/solve_dg.c:138-145); grad is that Jacobian's
- * transpose applied to the cotangent. Kinks of the fluxes take the derivative of the branch the value takes. */
+ * transpose applied to the cotangent. Kinks of the fluxes take the derivative of the branch the value takes.
+ * Advection and Euler: a Navier-Stokes context returns DGPU_ERR_UNSUPPORTED. */
 dgpu_status dgpu_vjp_forward(dgpu_ctx* ctx, const double* sol, double* rhs, double* max_rhs);
 dgpu_status dgpu_vjp_backward(dgpu_ctx* ctx, const double* cotangent, double* grad_sol);
 
@@ -202,7 +203,8 @@ dgpu_status dgpu_vjp_backward(dgpu_ctx* ctx, const double* cotangent, double* gr
  * forms the same product by complex step (compute_lhs_cmplx_step_dg, src/testing/support/simulation/solvers/dg/
  * test_support_solve_dg.c:83-110) and assembles the Jacobian itself for its implicit solver (compute_rlhs_dg,
  * src/simulation/solvers/dg/solve_dg.c:138-145); here the flux routines run on dual numbers, which gives the
- * product without a step size. Kinks of the fluxes take the derivative of the branch the value takes. */
+ * product without a step size. Kinks of the fluxes take the derivative of the branch the value takes. Every PDE,
+ * Navier-Stokes included (its gradients, liftings and viscous flux are linearised with the rest). */
 dgpu_status dgpu_jvp(dgpu_ctx* ctx, const double* sol, const double* dir, double* rhs, double* jv);
 
 /* Block-sparse Jacobian of the residual at sol, the matrix the reference assembles for its implicit solver block by
