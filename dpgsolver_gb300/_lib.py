@@ -6,6 +6,7 @@ or no GB300 is present, every call raises.
 from __future__ import annotations
 
 import ctypes
+import fcntl
 import os
 import subprocess
 
@@ -38,10 +39,19 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile libdgpu.so for sm_103a (nvcc cross-compiles without a GPU)."""
+    """Compile libdgpu.so for sm_103a (nvcc cross-compiles without a GPU). Processes that build at the same time
+    (a test run and a benchmark started together) serialise on a lock file; the later one finds the library fresh."""
     if not force and not _stale():
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
+    with open(os.path.join(BUILD_DIR, "build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and not _stale():
+            return LIB_PATH
+        return _build_locked(verbose)
+
+
+def _build_locked(verbose: bool) -> str:
     objs, procs = [], []
     for src in SOURCES:   # translation units compile in parallel, then one link
         obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
@@ -53,7 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for cmd, pr in procs:
         if pr.wait() != 0:
             raise subprocess.CalledProcessError(pr.returncode, cmd)
-    tmp = LIB_PATH + ".tmp"
+    tmp = f"{LIB_PATH}.{os.getpid()}.tmp"
     subprocess.run([nvcc_path(), "-shared", "-o", tmp] + objs, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -140,6 +150,7 @@ EXPORTS = {
     "dgpu_kernel_time": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, c_double_p,
                                         ctypes.POINTER(ctypes.c_longlong)]),
     "dgpu_probe_fp64": (ctypes.c_int, [ctypes.c_int, c_double_p]),
+    "dgpu_probe_fp64_mma": (ctypes.c_int, [ctypes.c_int, c_double_p]),
     "dgpu_vjp_forward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_jvp": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_vjp_backward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),

@@ -1365,9 +1365,31 @@ __global__ void fp64_fma_probe_kernel(double* out, int iters, double a, double b
 	out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-}  // namespace
+// FP64 tensor-core throughput probe: 8 independent m8n8k4 accumulators per warp (2 * 8 * 8 * 4 flops each).
+__global__ void fp64_mma_probe_kernel(double* out, int iters, double a, double b)
+{
+	const double av = a * (threadIdx.x + 1), bv = b;
+	double d[8][2];
+#pragma unroll
+	for (int k = 0; k < 8; ++k) {
+		d[k][0] = k;
+		d[k][1] = -k;
+	}
+	for (int i = 0; i < iters; ++i) {
+#pragma unroll
+		for (int k = 0; k < 8; ++k)
+			asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+			             : "+d"(d[k][0]), "+d"(d[k][1])
+			             : "d"(av), "d"(bv));
+	}
+	double s = 0.0;
+#pragma unroll
+	for (int k = 0; k < 8; ++k)
+		s += d[k][0] + d[k][1];
+	out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 
-extern "C" dgpu_status dgpu_probe_fp64(int iters, double* tflops)
+dgpu_status probe_fp64_rate(int iters, double* tflops, bool mma)
 {
 	if (iters < 1 || !tflops)
 		return DGPU_ERR_INVALID_ARGUMENT;
@@ -1381,9 +1403,10 @@ extern "C" dgpu_status dgpu_probe_fp64(int iters, double* tflops)
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
-	fp64_fma_probe_kernel<<<blocks, threads>>>(out, 16, 0.999999, 1e-7);  // warm-up
+	auto* kern = mma ? fp64_mma_probe_kernel : fp64_fma_probe_kernel;
+	kern<<<blocks, threads>>>(out, 16, mma ? 1e-9 : 0.999999, mma ? 0.5 : 1e-7);  // warm-up
 	cudaEventRecord(e0);
-	fp64_fma_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+	kern<<<blocks, threads>>>(out, iters, mma ? 1e-9 : 0.999999, mma ? 0.5 : 1e-7);
 	cudaEventRecord(e1);
 	cudaError_t e = cudaEventSynchronize(e1);
 	float ms = 0.f;
@@ -1393,10 +1416,17 @@ extern "C" dgpu_status dgpu_probe_fp64(int iters, double* tflops)
 	cudaFree(out);
 	if (e != cudaSuccess)
 		return DGPU_ERR_CUDA;
-	const double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+	// per thread and iteration: 8 FMAs (FMA probe) or 8 / 32 of a warp's 8 m8n8k4 products of 512 flops
+	const double flops = (mma ? 8.0 * 512.0 / 32.0 : 2.0 * 8.0) * (double)iters * threads * blocks;
 	*tflops = flops / (ms * 1e-3) / 1e12;
 	return DGPU_OK;
 }
+
+}  // namespace
+
+extern "C" dgpu_status dgpu_probe_fp64(int iters, double* tflops) { return probe_fp64_rate(iters, tflops, false); }
+
+extern "C" dgpu_status dgpu_probe_fp64_mma(int iters, double* tflops) { return probe_fp64_rate(iters, tflops, true); }
 
 // ---------------------------------------------------------------------------------------------------------------
 // Residual evaluation without any device allocation (dgpu_compute_rhs_noalloc).

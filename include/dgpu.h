@@ -263,6 +263,10 @@ const char* dgpu_last_error(const dgpu_ctx* ctx);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (8 independent chains per thread, `iters`
  * iterations): the denominator of the FP64-pipe roofline. Measurement aid; no reference counterpart. */
 dgpu_status dgpu_probe_fp64(int iters, double* tflops);
+/* Measured FP64 tensor-core throughput (mma.sync m8n8k4 f64, 8 independent accumulators per warp) in TFLOP/s:
+ * the evidence for or against routing the small contractions through DMMA. Measurement aid; no reference
+ * counterpart. */
+dgpu_status dgpu_probe_fp64_mma(int iters, double* tflops);
 const char* dgpu_status_string(dgpu_status st);
 
 /* ---- Batched residual over a mixed-order mesh ------------------------------------------------------------------

@@ -7,6 +7,7 @@ timed CPU baseline, never as the product.
 from __future__ import annotations
 
 import ctypes
+import fcntl
 import os
 import subprocess
 
@@ -46,12 +47,19 @@ class _Problem(ctypes.Structure):
     ]
 
 
+def _stale() -> bool:
+    return not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < max(
+        os.path.getmtime(os.path.join(_HERE, f)) for f in ("dg_oracle.c", "dg_oracle_T.h", "dg_oracle.h"))
+
+
 def build(force: bool = False) -> str:
-    """Compile liboracle.so with the committed Makefile."""
-    if force or not os.path.exists(_LIB_PATH) or \
-            os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(os.path.join(_HERE, f))
-                                               for f in ("dg_oracle.c", "dg_oracle_T.h", "dg_oracle.h")):
-        subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    """Compile liboracle.so with the committed Makefile (processes building at the same time serialise on a lock
+    file; the Makefile links to a temporary name and renames, so a loader never sees a partial library)."""
+    if force or _stale():
+        with open(os.path.join(_HERE, ".build.lock"), "w") as lock:
+            fcntl.flock(lock, fcntl.LOCK_EX)
+            if force or _stale():
+                subprocess.run(["make", "-s", "-B" if force else "-s", "-C", _HERE, "liboracle.so"], check=True)
     return _LIB_PATH
 
 
