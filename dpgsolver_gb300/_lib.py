@@ -78,7 +78,8 @@ c_int_p = ctypes.POINTER(ctypes.c_int)
 class Physics(ctypes.Structure):
     _fields_ = [("d", ctypes.c_int), ("pde", ctypes.c_int), ("num_flux", ctypes.c_int),
                 ("positivity", ctypes.c_int), ("b_adv", ctypes.c_double * 3), ("viscosity", ctypes.c_int),
-                ("mu", ctypes.c_double), ("Pr", ctypes.c_double), ("r_s", ctypes.c_double)]
+                ("mu", ctypes.c_double), ("Pr", ctypes.c_double), ("r_s", ctypes.c_double),
+                ("dTdn", ctypes.c_double)]
 
 
 class TPOperators(ctypes.Structure):

@@ -61,7 +61,7 @@ struct dgpu_ctx {
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	int *vol_face = nullptr, *nc = nullptr, *nc_inv = nullptr;
 	bool ns = false;                      // Navier-Stokes: BR2 gradient buffers and the four-kernel stage
-	NsPhys ns_phys = {0.0, 1.0, 1.0, 101};
+	NsPhys ns_phys = {0.0, 1.0, 1.0, 101, 0.0};
 	double *ns_gtr = nullptr, *ns_lam = nullptr, *ns_X = nullptr, *ns_gv = nullptr;
 	double *ns_gtr_d = nullptr, *ns_X_d = nullptr, *ns_gv_d = nullptr;   // their tangents (linearisations)
 	int stage_launches = 3;               // kernels per residual evaluation / RK stage
@@ -854,6 +854,8 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		     (phys->viscosity == DGPU_VISCOSITY_SUTHERLAND && !(phys->r_s > 0.0))))
 			return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "Navier-Stokes needs a viscosity model, mu >= 0, Pr > 0"
 			                                               " (and r_s > 0 for Sutherland's law)");
+		if (phys->pde == DGPU_PDE_NAVIER_STOKES && phys->dTdn != 0.0 && phys->viscosity != DGPU_VISCOSITY_CONSTANT)
+			return fail(nullptr, DGPU_ERR_UNSUPPORTED, "a diabatic wall flux (dTdn != 0) needs constant viscosity");
 	} else {
 		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "pde must be advection, Euler or Navier-Stokes");
 	}
@@ -891,7 +893,8 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 	c->positivity = (phys->pde != DGPU_PDE_ADVECTION && phys->positivity) ? 1 : 0;
 	c->ns = phys->pde == DGPU_PDE_NAVIER_STOKES;
 	if (c->ns) {
-		c->ns_phys = NsPhys{phys->mu, phys->Pr, phys->r_s, phys->viscosity};
+		c->ns_phys = NsPhys{phys->mu, phys->Pr, phys->r_s, phys->viscosity,
+		                    -phys->mu * (kGamma / kGm1 * phys->r_s) / phys->Pr * phys->dTdn};
 		c->stage_launches = 4;
 	}
 	c->n_vol = mesh->n_volumes;

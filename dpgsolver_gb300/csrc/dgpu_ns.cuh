@@ -212,15 +212,21 @@ __device__ __forceinline__ void ns_face_node(const TPParams& P, const TPParams& 
 			ns_set(WR[k], P.traces[oR + k * NF + tR], TAN ? Pd.traces[oR + k * NF + tR] : 0.0);
 	} else {
 		// the reference's Navier-Stokes boundary values (set_function_pointers_num_flux_bc_navier_stokes,
-		// face_solver_T.c:277-300): Riemann and supersonic in/outflow as for Euler; the no-slip adiabatic wall keeps
-		// rho and E and mirrors the momentum (boundary_navier_stokes_T.c:258-304)
+		// face_solver_T.c:277-300): Riemann and supersonic in/outflow as for Euler; the static no-slip walls keep
+		// rho and E and mirror the momentum (boundary_navier_stokes_T.c:258-304); the rotating wall takes
+		// 2 s_ex - s_l for every variable, s_ex = (rho_b, rho_b u_wall, E_b) given as the exterior state (:196-244)
 		code = P.bc_code[b];
-		if (code == kBcNoSlipAdiabatic) {
+		if (code == kBcNoSlipAdiabatic || code == kBcNoSlipDiabatic) {
 			WR[0] = WL[0];
 #pragma unroll
 			for (int k = 0; k < D; ++k)
 				WR[1 + k] = -WL[1 + k];
 			WR[D + 1] = WL[D + 1];
+		} else if (code == kBcNoSlipAllRotating) {
+			const double* ext = P.bc_ext + (size_t)b * NV * NF + t;
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				WR[k] = 2.0 * ext[k * NF] - WL[k];
 		} else {
 			boundary_value<D, NV, kEuler, T>(P, b, t, NF, WL, n, WR);
 		}
@@ -271,11 +277,12 @@ __device__ __forceinline__ void ns_face_node(const TPParams& P, const TPParams& 
 #pragma unroll
 		for (int dir = 0; dir < D; ++dir)
 			s = s + n[dir] * (FL[dir][k] + FR[dir][k]);
-		// an adiabatic wall sets the total normal energy flux to nf_E = 0 (set_provided_Numerical_Flux_members,
-		// numerical_flux_central_T.c:222-231)
-		const bool wall_E = (k == D + 1 && code == kBcNoSlipAdiabatic);
+		// a static wall sets the total normal energy flux to nf_E: 0 when adiabatic, -mu Cp / Pr dTdn when
+		// diabatic (set_provided_Numerical_Flux_members, numerical_flux_central_T.c:222-231)
+		const bool wall_E = (k == D + 1 && (code == kBcNoSlipAdiabatic || code == kBcNoSlipDiabatic));
+		const double nf_E = code == kBcNoSlipDiabatic ? P.ns.wall_nf_E * sc : 0.0;
 		const T o = (nF[k] + 0.5 * s) * sc;
-		P.nnf[on + k * NF] = wall_E ? 0.0 : ns_val(o);
+		P.nnf[on + k * NF] = wall_E ? nf_E : ns_val(o);
 		if (TAN)
 			Pd.nnf[on + k * NF] = wall_E ? 0.0 : ns_der(o);
 	}

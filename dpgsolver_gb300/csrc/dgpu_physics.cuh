@@ -183,7 +183,7 @@ __device__ __forceinline__ double num_flux_upwind(double uL, double uR, const do
 constexpr int kBcStepSC = 10000;
 enum BcCode {
 	kBcRiemann = 101, kBcSlipWall = 102, kBcBackPressure = 103, kBcTotalTP = 104, kBcSupersonicIn = 105,
-	kBcSupersonicOut = 106, kBcNoSlipAdiabatic = 111
+	kBcSupersonicOut = 106, kBcNoSlipAdiabatic = 111, kBcNoSlipDiabatic = 112, kBcNoSlipAllRotating = 113
 };
 
 // BC_Data (boundary_euler_T.c:44-49): the scalars the reference reads from the test case's input file.
@@ -203,11 +203,11 @@ __host__ __device__ __forceinline__ bool bc_is_euler(int bc)
 {
 	return bc >= kBcRiemann && bc <= kBcSupersonicOut;
 }
-// The boundary values the reference's Navier-Stokes takes (face_solver_T.c:277-300), less the rotating and diabatic
-// walls.
+// The boundary values the reference's Navier-Stokes takes (face_solver_T.c:277-300).
 __host__ __device__ __forceinline__ bool bc_is_navier_stokes(int bc)
 {
-	return bc == kBcRiemann || bc == kBcSupersonicIn || bc == kBcSupersonicOut || bc == kBcNoSlipAdiabatic;
+	return bc == kBcRiemann || bc == kBcSupersonicIn || bc == kBcSupersonicOut || bc == kBcNoSlipAdiabatic ||
+	       bc == kBcNoSlipDiabatic || bc == kBcNoSlipAllRotating;
 }
 
 // Exterior state WR of an Euler boundary face node from the interior trace WL, the test case's solution at the node
@@ -393,6 +393,7 @@ __device__ __forceinline__ T advection_boundary_value(const T& uL, double ext, c
 struct NsPhys {
 	double mu, Pr, r_s;
 	int viscosity;
+	double wall_nf_E;   // BC_NOSLIP_DIABATIC: the wall's normal energy flux -mu Cp / Pr dTdn
 };
 
 template <int D, typename T>

@@ -109,8 +109,10 @@ def flat_arrays(prob) -> dict:
     }
 
 
-def stable_dt(prob: "DGProblem", cfl: float = 0.1) -> float:
-    """dt = cfl * h / ((2p + 1) * max(|V| + c)) over the solution nodes of the current state."""
+def stable_dt(prob: "DGProblem", cfl: float = 0.1, h: float | None = None) -> float:
+    """dt = cfl * h / ((2p + 1) * max(|V| + c)) over the solution nodes of the current state; with viscosity also
+    at most cfl * h^2 / ((2p + 1)^2 * max(gamma mu / (Pr rho))) (the heat-flux diffusivity bounds the momentum one
+    for Pr < gamma). h: the smallest physical volume size (the structured mesh's own spacing by default)."""
     d = prob.d
     U = prob.sol
     rho = U[:, 0]
@@ -118,8 +120,16 @@ def stable_dt(prob: "DGProblem", cfl: float = 0.1) -> float:
     V2 = np.sum(vel * vel, axis=1)
     p = GM1 * (U[:, d + 1] - 0.5 * rho * V2)
     lam = float(np.max(np.sqrt(V2) + np.sqrt(GAMMA * p / rho)))
-    h = float(np.min(prob.mesh.h))
-    return cfl * h / ((2 * prob.ops.p + 1) * lam)
+    h = float(np.min(prob.mesh.h)) if h is None else float(h)
+    k = 2 * prob.ops.p + 1
+    dt = cfl * h / (k * lam)
+    if prob.ns is not None and prob.ns["mu"] > 0.0:
+        mu = prob.ns["mu"]
+        if prob.ns["viscosity"] == VISCOSITY_SUTHERLAND:   # 0.08 mu sqrt(T) / (1 + 112 / T) <= 0.08 mu sqrt(T)
+            mu *= 0.08 * float(np.sqrt(np.max(p / (rho * prob.ns["r_s"]))))
+        nu = GAMMA * mu / (prob.ns["Pr"] * float(np.min(rho)))
+        dt = min(dt, cfl * h * h / (k * k * nu))
+    return dt
 
 
 def primitive_to_conserved(d, rho, vel, p):
@@ -216,6 +226,8 @@ BC_TOTAL_TP = 104
 BC_SUPERSONIC_IN = 105
 BC_SUPERSONIC_OUT = 106
 BC_NOSLIP_ADIABATIC = 111
+BC_NOSLIP_DIABATIC = 112
+BC_NOSLIP_ALL_ROTATING = 113
 
 
 def _set_boundaries(prob: DGProblem, side_bc: dict, exterior) -> DGProblem:
@@ -454,3 +466,66 @@ def ns_riemann_vortex_2d(n: int = 6, p: int = 3, mu: float = 0.01, num_flux: int
     prob.pde = PDE_NAVIER_STOKES
     prob.ns = _ns_params(mu)
     return prob
+
+
+def annulus_deform(r_i: float, r_o: float):
+    """Maps the unit square onto the annulus r_i <= r <= r_o: x -> r = r_i + (r_o - r_i) x, y -> theta = 2 pi y."""
+    def f(x):
+        r = r_i + (r_o - r_i) * x[:, 0]
+        th = 2.0 * math.pi * x[:, 1]
+        return np.stack([r * np.cos(th), r * np.sin(th)], axis=1)
+    return f
+
+
+def taylor_couette_state(x, y, r_i, r_o, omega, mu, Pr, r_s, t_b, p_b, dTdn):
+    """The reference's Taylor-Couette solution (solution_taylor_couette_T.c:136-179, after Illingworth 1950):
+    azimuthal velocity c (1/r - r/r_o^2), c = omega / (1/r_i^2 - 1/r_o^2), the temperature of the viscous heating
+    with conductivity kappa = mu Cp / Pr and the outer wall's gradient dTdn, uniform pressure p_b, rho = p / (r_s T).
+    Returns the conserved variables (4, ...)."""
+    r, th = np.sqrt(x * x + y * y), np.arctan2(y, x)
+    c = omega / (1.0 / r_i ** 2 - 1.0 / r_o ** 2)
+    kappa = mu * (GAMMA / GM1 * r_s) / Pr
+    vt = c * (1.0 / r - r / r_o ** 2)
+    t = (t_b - 2.0 * c * c / r_o ** 2 * mu / kappa * np.log(r / r_i) - c * c * mu / kappa * (1.0 / r ** 2 - 1.0 / r_i ** 2)
+         + dTdn * r_o * np.log(r / r_i))
+    pr = np.full_like(r, p_b)
+    return primitive_to_conserved(2, pr / (r_s * t), np.stack([-np.sin(th) * vt, np.cos(th) * vt]), pr)
+
+
+def ns_taylor_couette(n: int = 8, p: int = 3, mu: float = 1e-3, omega: float = 1.0, diabatic: bool = False,
+                      dTdn: float = 1.0, num_flux: int = NUM_FLUX_ROE_PIKE, perturb: float = 0.0) -> DGProblem:
+    """The reference's Navier-Stokes Taylor-Couette case (input_files/navier_stokes/steady/taylor_couette, mesh
+    meshes/n-cylinder_hollow/2d.geo) on a curved QUAD annulus, n x n volumes, r_i = 0.5, r_o = 1, periodic in theta:
+    the inner cylinder rotates at omega (BC_NOSLIP_ALL_ROTATING with rho_b = 1, E_b = p_b / (gamma - 1) +
+    rho_b (omega r_i)^2 / 2), the outer one is a static adiabatic wall (BC_NOSLIP_ADIABATIC), or a diabatic one
+    with the normal temperature gradient dTdn (BC_NOSLIP_DIABATIC, solution_diabatic.data). Pr = 0.72, r_s = 1,
+    p_b = t_b = 1; the state is the reference's Taylor-Couette solution, its density scaled by
+    1 + perturb sin(3 theta) sin(pi (r - r_i) / (r_o - r_i))."""
+    r_i, r_o, Pr, r_s, p_b, t_b = 0.5, 1.0, 0.72, 1.0, 1.0, 1.0
+    mesh = StructuredMesh(2, n, 0.0, 1.0, periodic=(False, True))
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops, deform=annulus_deform(r_i, r_o), curved=True)
+    ns = _ns_params(mu, Pr=Pr, r_s=r_s)
+    ns["dTdn"] = float(dTdn) if diabatic else 0.0
+    prob = DGProblem("ns_taylor_couette", 2, PDE_NAVIER_STOKES, num_flux, True, np.zeros(3), ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, 4, ops.n_vs)), dt=0.0, n_steps=100, ns=ns)
+    x = prob.solution_node_xyz()
+    X, Y = x[..., 0], x[..., 1]
+    U = taylor_couette_state(X, Y, r_i, r_o, omega, mu, Pr, r_s, t_b, p_b, ns["dTdn"])
+    if perturb:
+        R, TH = np.sqrt(X * X + Y * Y), np.arctan2(Y, X)
+        U = U * (1.0 + perturb * np.sin(3.0 * TH) * np.sin(math.pi * (R - r_i) / (r_o - r_i)))[None]
+    prob.sol = _pack_state(U)
+    prob.dt = stable_dt(prob, h=(r_o - r_i) / n)
+    rho_b = 1.0
+    E_b = p_b / GM1 + 0.5 * rho_b * (omega * r_i) ** 2
+
+    def wall_state(xyz):
+        # compute_uvw_ex_rotating (boundary_navier_stokes_T.c:507-523): the wall's velocity omega r e_theta
+        r, th = np.sqrt(xyz[:, 0] ** 2 + xyz[:, 1] ** 2), np.arctan2(xyz[:, 1], xyz[:, 0])
+        vt = omega * r
+        return np.stack([np.full(len(r), rho_b), -rho_b * np.sin(th) * vt, rho_b * np.cos(th) * vt,
+                         np.full(len(r), E_b)], axis=1)
+    outer = BC_NOSLIP_DIABATIC if diabatic else BC_NOSLIP_ADIABATIC
+    prob.meta.update(n=n, p=p, omega=omega, r_i=r_i, r_o=r_o)
+    return _set_boundaries(prob, {(0, 0): BC_NOSLIP_ALL_ROTATING, (0, 1): outer}, wall_state)

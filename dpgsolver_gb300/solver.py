@@ -82,6 +82,7 @@ class Simulation:
         ns = getattr(prob, "ns", None)
         if ns is not None:
             phys.viscosity, phys.mu, phys.Pr, phys.r_s = int(ns["viscosity"]), ns["mu"], ns["Pr"], ns["r_s"]
+            phys.dTdn = float(ns.get("dTdn", 0.0))
         tp = _lib.TPOperators()
         tp.elem_type = ops.e_type
         tp.p = ops.p

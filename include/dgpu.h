@@ -74,6 +74,10 @@ typedef struct {
 	 * explicit DG option of the reference. */
 	int viscosity;
 	double mu, Pr, r_s;
+	/* BC_NOSLIP_DIABATIC walls: the normal temperature gradient dTdn of the input (diabatic_flux_type constant;
+	 * 0 for constant_zero). The wall's normal energy flux is -mu Cp / Pr dTdn, Cp = gamma / (gamma - 1) r_s
+	 * (get_normal_flux_Energy, solution_navier_stokes.c:93-150); a non-zero dTdn needs constant viscosity. */
+	double dTdn;
 } dgpu_physics;
 
 /* Tensor-product operator set of one (element type, p): the 1D factors of the reference's Operator::ops_tp
@@ -109,12 +113,15 @@ typedef struct {
 	 *   taken modulo BC_STEP_SC = 10000. Euler: BC_RIEMANN 101, BC_SLIPWALL 102, BC_BACKPRESSURE 103,
 	 *   BC_TOTAL_TP 104, BC_SUPERSONIC_IN 105, BC_SUPERSONIC_OUT 106 (boundary_euler_T.c); advection:
 	 *   inflow/outflow/upwind 1-3, 11-13, 41-46, all the upwind boundary value (boundary_advection_T.c:40-77);
-	 *   Navier-Stokes: BC_RIEMANN, BC_SUPERSONIC_IN, BC_SUPERSONIC_OUT (with the interior gradient) and
-	 *   BC_NOSLIP_ADIABATIC 111 (static wall, boundary_navier_stokes_T.c:130-141, 258-304).
+	 *   Navier-Stokes: BC_RIEMANN, BC_SUPERSONIC_IN, BC_SUPERSONIC_OUT (with the interior gradient),
+	 *   BC_NOSLIP_ADIABATIC 111 and BC_NOSLIP_DIABATIC 112 (static walls, boundary_navier_stokes_T.c:130-156,
+	 *   258-304) and BC_NOSLIP_ALL_ROTATING 113 (boundary_navier_stokes_T.c:117-128, 196-244).
 	 *   Other codes: DGPU_ERR_UNSUPPORTED.
 	 * bc_state_fc: n_faces x (n_fc x n_var) row-major: the test case's conserved solution at the face's
 	 *   cubature nodes (constructor_sol_bv(xyz_fc)), the exterior data of Riemann, supersonic inflow and
-	 *   upwind inflow boundaries; read on boundary faces only.
+	 *   upwind inflow boundaries; on BC_NOSLIP_ALL_ROTATING faces the wall state (rho_b, rho_b u_wall, E_b) with
+	 *   the wall's velocity at the node (compute_uvw_ex_rotating: omega about the z axis); read on boundary
+	 *   faces only.
 	 * dgpu_create only: the no-allocation entry and the batched context return DGPU_ERR_UNSUPPORTED. */
 	const int* bc_fc;
 	const double* bc_state_fc;

@@ -125,6 +125,9 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 		if ((in->viscosity != ORACLE_VISCOSITY_CONSTANT && in->viscosity != ORACLE_VISCOSITY_SUTHERLAND) ||
 		    !(in->Pr > 0.0) || !(in->mu >= 0.0))
 			return ORACLE_ERR_ARG;
+		/* a non-zero wall heat flux needs constant viscosity (the assertion of get_normal_flux_Energy) */
+		if (in->dTdn != 0.0 && in->viscosity != ORACLE_VISCOSITY_CONSTANT)
+			return ORACLE_ERR_ARG;
 		for (int g = 0; g < in->n_groups; ++g)
 			if (!in->groups[g].cv1_vs_vc)
 				return ORACLE_ERR_ARG;

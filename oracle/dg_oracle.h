@@ -74,6 +74,10 @@ struct oracle_problem {
 	 * explicit option the reference's DG solver provides. */
 	int viscosity;
 	double mu, Pr, r_s;
+	/* BC_NOSLIP_DIABATIC 112: the wall's normal temperature gradient dTdn (diabatic_flux_type constant; 0 for
+	 * constant_zero), which sets the wall's normal energy flux nf_E = -mu Cp / Pr dTdn (get_normal_flux_Energy,
+	 * solution_navier_stokes.c:93-150). */
+	double dTdn;
 };
 
 struct oracle_ctx;

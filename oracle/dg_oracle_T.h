@@ -72,15 +72,23 @@ static int SUF(boundary_state)(const struct oracle_problem* P, const int bc, con
 	}
 	if (P->pde == ORACLE_PDE_NAVIER_STOKES) {
 		/* set_function_pointers_num_flux_bc_navier_stokes (face_solver_T.c:277-300): Riemann and supersonic
-		 * in/outflow as for Euler, and the no-slip walls; BC_NOSLIP_ADIABATIC 111 (static wall, u_ex = 0):
-		 * rho and E kept, momentum -rhouvw_l + 2 rho u_ex (constructor_Boundary_Value_T_navier_stokes_no_slip_flux_
-		 * general, boundary_navier_stokes_T.c:258-304) */
+		 * in/outflow as for Euler, and the no-slip walls. BC_NOSLIP_ADIABATIC 111 and BC_NOSLIP_DIABATIC 112
+		 * (static wall, u_ex = 0): rho and E kept, momentum -rhouvw_l + 2 rho u_ex
+		 * (constructor_Boundary_Value_T_navier_stokes_no_slip_flux_general, boundary_navier_stokes_T.c:258-304).
+		 * BC_NOSLIP_ALL_ROTATING 113: every variable 2 s_ex - s_l, s_ex = (rho_b, rho_b u_ex, E_b) with the wall's
+		 * velocity u_ex (compute_uvw_ex_rotating, omega about the z axis), which the caller supplies as the exterior
+		 * state (constructor_Boundary_Value_T_navier_stokes_no_slip_all_general, :196-244). */
 		const int b = bc % 10000;
-		if (b == 111) {
+		if (b == 111 || b == 112) {
 			WR[0] = WL[0];
 			for (int k = 0; k < d; ++k)
 				WR[1 + k] = -WL[1 + k];
 			WR[d + 1] = WL[d + 1];
+			return 0;
+		}
+		if (b == 113) {
+			for (int k = 0; k < nv; ++k)
+				WR[k] = -WL[k] + 2.0 * ext[k];
 			return 0;
 		}
 		if (b != 101 && b != 105 && b != 106)
@@ -396,7 +404,8 @@ static void SUF(num_flux_roe)(const int d, const Type* WL, const Type* WR, const
  * also the boundary gradient (constructor_Boundary_Value_T_grad_from_internal; the no-slip walls copy the density and
  * momentum gradients, boundary_navier_stokes_T.c:306-352), the central viscous flux is added, and on a no-slip
  * adiabatic wall the total normal energy flux is set to nf_E = 0 (nf_E_provided, set_provided_Numerical_Flux_members,
- * numerical_flux_central_T.c:222-231; DIABATIC_FLUX_CONSTANT_ZERO). gv, gf: as ns_gradients writes them, else NULL. */
+ * numerical_flux_central_T.c:222-231; DIABATIC_FLUX_CONSTANT_ZERO), on a diabatic one to nf_E = -mu Cp / Pr dTdn
+ * (DIABATIC_FLUX_CONSTANT). gv, gf: as ns_gradients writes them, else NULL. */
 static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Type* sol, Type* rhs, Type* sL, Type* nnf,
                               const Type* gv, const Type* gf)
 {
@@ -459,6 +468,8 @@ static int SUF(boundary_face)(const struct oracle_ctx* c, const int f, const Typ
 					nF[eq] += 0.5 * ni[x] * (FvL[x + d * eq] + FvR[x + d * eq]);
 			if (P->bc_fc[f] % 10000 == 111)
 				nF[d + 1] = 0.0;
+			else if (P->bc_fc[f] % 10000 == 112)   /* -mu Cp / Pr dTdn, Cp = gamma / (gamma - 1) r_s */
+				nF[d + 1] = -P->mu * (GAMMA / GM1 * P->r_s) / P->Pr * P->dTdn;
 		}
 		for (int k = 0; k < neq; ++k)
 			nnf[i + (size_t)n_fc * k] = nF[k] * jf[i];

@@ -8,6 +8,11 @@ noise relative to max|R| is far above the other cases': the oracle's own respons
 input (the noise floor, measured per case) reaches 1.2e-11 on 12^3 p = 3; the Mach 0.3 channel (background
 pressure 7.9) sits at 1e-12. Every residual case is therefore held to max(1e-12, 4 x its measured floor): where the
 floor is low (the vortex cases, below 3e-13) the plain bound is the one that applies.
+
+The Taylor-Couette cases (the reference's navier_stokes/steady/taylor_couette on a curved annulus) cover the
+rotating wall (BC_NOSLIP_ALL_ROTATING: 2 s_wall - s_l) and the diabatic wall (BC_NOSLIP_DIABATIC: the energy flux
+-mu Cp / Pr dTdn). Their volumes are stretched (aspect ratio up to 12) and the oracle's noise floor there is about
+7e-12, so the same max(1e-12, 4 x floor) rule applies.
 """
 import numpy as np
 import pytest
@@ -35,6 +40,11 @@ CASES = {
     "channel3d_lf_p2_4": lambda: P.ns_channel(3, 4, 2, mu=0.02, num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
     "channel3d_roe_p3_4": lambda: P.ns_channel(3, 4, 3, mu=0.01, amplitude=0.05),
     "riemann2d_roe_p3_6": lambda: P.ns_riemann_vortex_2d(6, 3, mu=0.02),
+    # the Taylor-Couette annulus: rotating inner wall, adiabatic or diabatic outer wall
+    "couette_roe_p3_6": lambda: P.ns_taylor_couette(6, 3, mu=0.02, perturb=0.2),
+    "couette_diab_lf_p2_8": lambda: P.ns_taylor_couette(8, 2, mu=0.02, diabatic=True, perturb=0.2,
+                                                         num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
+    "couette_diab_roe_p4_4": lambda: P.ns_taylor_couette(4, 4, mu=0.01, diabatic=True, perturb=0.2),
 }
 
 
@@ -78,7 +88,7 @@ def test_ns_mach01_taylor_green_within_the_oracle_noise_floor(gpu_lib):
 
 
 @pytest.mark.parametrize("name", ["vortex2d_roe_p3_8", "tgv_p3_4_curved", "tgv_p2_6", "channel3d_roe_p3_4",
-                                  "riemann2d_roe_p3_6"])
+                                  "riemann2d_roe_p3_6", "couette_diab_lf_p2_8"])
 def test_ns_rk3_steps_match_oracle(gpu_lib, name):
     from dpgsolver_gb300.solver import Simulation
     prob = CASES[name]()
@@ -116,7 +126,8 @@ def test_ns_free_stream(gpu_lib):
             assert sim.compute_rhs() < 1e-11
     # fluid at rest between no-slip walls; the exterior stream inside Riemann sides
     for prob, vals in ((P.ns_channel(3, 4, 3, amplitude=0.05), [1.0, 0.0, 0.0, 0.0, 2.0 / P.GM1]),
-                       (P.ns_riemann_vortex_2d(6, 3), [1.0, 1.0, 1.0, 1.0 / P.GM1 + 1.0])):
+                       (P.ns_riemann_vortex_2d(6, 3), [1.0, 1.0, 1.0, 1.0 / P.GM1 + 1.0]),
+                       (P.ns_taylor_couette(6, 3, omega=0.0), [1.0, 0.0, 0.0, 1.0 / P.GM1])):
         with Simulation(prob) as sim:
             sim.upload_state(P.constant_state(prob, vals))
             assert sim.compute_rhs() < 1e-11
@@ -124,7 +135,8 @@ def test_ns_free_stream(gpu_lib):
 
 # ---- forward-mode linearisation and the block-sparse Jacobian ------------------------------------------------------
 JVP_CASES = ["vortex2d_roe_p3_8", "vortex2d_lf_p2_6", "vortex2d_suth_p4_4", "tgv_p3_4_curved", "tgv_p1_4_suth",
-             "tgv_p4_2_lf", "channel2d_roe_p3_6", "channel3d_lf_p2_4", "riemann2d_roe_p3_6"]
+             "tgv_p4_2_lf", "channel2d_roe_p3_6", "channel3d_lf_p2_4", "riemann2d_roe_p3_6", "couette_roe_p3_6",
+             "couette_diab_lf_p2_8"]
 
 
 def _inputs(prob, seed):
@@ -178,6 +190,9 @@ JAC_CASES = {
     "channel2d_roe_p2_3": lambda: P.ns_channel(2, 3, 2, mu=0.05, amplitude=0.05),
     "channel3d_lf_p1_2": lambda: P.ns_channel(3, 2, 1, mu=0.05, num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
     "riemann2d_roe_p2_3": lambda: P.ns_riemann_vortex_2d(3, 2, mu=0.05),
+    "couette_roe_p2_3": lambda: P.ns_taylor_couette(3, 2, mu=0.05, perturb=0.05),
+    "couette_diab_lf_p1_4": lambda: P.ns_taylor_couette(4, 1, mu=0.05, diabatic=True, perturb=0.05,
+                                                         num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
 }
 
 
@@ -221,3 +236,8 @@ def test_ns_refusals(gpu_lib):
     with pytest.raises(_lib.DGPUError) as e:
         Simulation(bad)
     assert e.value.status == 1
+    hot = P.ns_taylor_couette(3, 2, diabatic=True)   # a wall heat flux with Sutherland's law: the reference asserts
+    hot.ns["viscosity"] = P.VISCOSITY_SUTHERLAND
+    with pytest.raises(_lib.DGPUError) as e:
+        Simulation(hot)
+    assert e.value.status == 2

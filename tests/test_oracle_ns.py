@@ -163,3 +163,55 @@ def test_ns_refuses_euler_only_boundaries():
     prob.pde, prob.ns = P.PDE_NAVIER_STOKES, {"viscosity": 101, "mu": 0.01, "Pr": 0.72, "r_s": 1.0}
     with pytest.raises(Exception):
         oracle.Oracle(prob).compute_rhs(prob.sol)
+
+
+# ---- the rotating and diabatic walls of the Taylor-Couette case ----------------------------------------------------
+def test_taylor_couette_at_rest_is_steady():
+    """omega = 0: the rotating wall's state (rho_b, 0, E_b) equals the interior's, the outer wall is adiabatic."""
+    prob = P.ns_taylor_couette(4, 3, mu=0.02, omega=0.0)
+    assert oracle.Oracle(prob).compute_rhs(_at_rest(prob, 1.0))[1] < 1e-11
+
+
+def test_diabatic_wall_without_heat_flux_is_the_adiabatic_wall():
+    pa = P.ns_taylor_couette(4, 3, mu=0.02, perturb=0.05)
+    pd = P.ns_taylor_couette(4, 3, mu=0.02, perturb=0.05, diabatic=True, dTdn=0.0)
+    assert np.array_equal(oracle.Oracle(pa).compute_rhs(pa.sol)[0], oracle.Oracle(pd).compute_rhs(pd.sol)[0])
+
+
+def test_diabatic_wall_adds_its_heat_flux():
+    """The wall's energy flux nf_E = -mu Cp / Pr dTdn replaces the computed one, so switching dTdn on (same state)
+    adds mu Cp / Pr dTdn times the wall's length to the total energy, and nothing else changes. The length is the
+    face quadrature of the curved wall (sum of w_f J_f), within 1e-6 of 2 pi r_o at 8 volumes around."""
+    mu, dTdn = 0.02, 1.0
+    p1 = P.ns_taylor_couette(8, 3, mu=mu, diabatic=True, dTdn=dTdn, perturb=0.05)
+    p0 = P.ns_taylor_couette(8, 3, mu=mu, diabatic=True, dTdn=dTdn, perturb=0.05)
+    p0.ns["dTdn"] = 0.0
+    d = oracle.Oracle(p1).compute_rhs_raw(p1.sol) - oracle.Oracle(p0).compute_rhs_raw(p0.sol)
+    q = mu * (P.GAMMA / P.GM1) / 0.72 * dTdn
+    wall = p1.bc == P.BC_NOSLIP_DIABATIC
+    length = float((p1.geom.jacobian_det_fc[wall] * p1.ops.w_fc[None, :]).sum())
+    assert abs(length - 2.0 * np.pi) <= 1e-6 * 2.0 * np.pi
+    assert abs(d[:, 3].sum() - q * length) <= 1e-12 * q * length
+    assert np.max(np.abs(d[:, :3])) == 0.0
+
+
+@pytest.mark.parametrize("diabatic", [False, True])
+def test_taylor_couette_complex_step(diabatic):
+    prob = P.ns_taylor_couette(3, 2, mu=0.05, diabatic=diabatic, perturb=0.05)
+    o = oracle.Oracle(prob)
+    rng = np.random.default_rng(5)
+    base = prob.sol + 1e-2 * rng.standard_normal(prob.sol.shape)
+    dirn = rng.standard_normal(prob.sol.shape)
+    _, ri = o.compute_rhs_cmplx(base, 1e-30 * dirn)
+    jv = ri / 1e-30
+    eps = 1e-6
+    rp, _ = o.compute_rhs(base + eps * dirn)
+    rm, _ = o.compute_rhs(base - eps * dirn)
+    assert np.max(np.abs(jv - (rp - rm) / (2 * eps))) <= 1e-6 * np.max(np.abs(jv))
+
+
+def test_diabatic_heat_flux_needs_constant_viscosity():
+    prob = P.ns_taylor_couette(3, 2, diabatic=True)
+    prob.ns["viscosity"] = P.VISCOSITY_SUTHERLAND
+    with pytest.raises(Exception):
+        oracle.Oracle(prob).compute_rhs(prob.sol)
