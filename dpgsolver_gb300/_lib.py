@@ -152,6 +152,7 @@ EXPORTS = {
                                         ctypes.POINTER(ctypes.c_longlong)]),
     "dgpu_probe_fp64": (ctypes.c_int, [ctypes.c_int, c_double_p]),
     "dgpu_probe_fp64_mma": (ctypes.c_int, [ctypes.c_int, c_double_p]),
+    "dgpu_blend_geometry": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_int_p, c_double_p]),
     "dgpu_vjp_forward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_jvp": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_vjp_backward": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),

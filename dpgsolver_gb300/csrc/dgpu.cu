@@ -2284,3 +2284,56 @@ extern "C" dgpu_status dgpu_compute_geometry(int d, const dgpu_tp_operators* ops
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "non-positive Jacobian determinant");
 	return DGPU_OK;
 }
+
+extern "C" dgpu_status dgpu_blend_geometry(int d, int p_g, int n_volumes, const double* xyz_ve, const int* face_curved,
+                                           double* geom_coef)
+{
+	g_create_error.clear();
+	if (!xyz_ve || !face_curved || !geom_coef || n_volumes < 1)
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "NULL argument or no volumes");
+	if (d != 2)
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "blended geometry is provided for QUAD volumes (d = 2) only");
+	if (p_g < 1 || p_g > kQMax - 1)
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "p_g must be in 1..4");
+	int n_dev = 0;
+	if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1)
+		return fail(nullptr, DGPU_ERR_NO_DEVICE, "no CUDA device");
+	BlendArgs A = {};
+	A.n_vol = n_volumes;
+	A.qg = p_g + 1;
+	gauss_lobatto_nodes(A.qg, A.x);
+	const size_t nv = (size_t)n_volumes, n_g = (size_t)A.qg * A.qg;
+	cudaStream_t st = nullptr;
+	double *d_ve = nullptr, *d_out = nullptr;
+	int* d_fc = nullptr;
+	cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+	if (e == cudaSuccess)
+		e = cudaMalloc((void**)&d_ve, nv * 8 * sizeof(double));
+	if (e == cudaSuccess)
+		e = cudaMalloc((void**)&d_fc, nv * 4 * sizeof(int));
+	if (e == cudaSuccess)
+		e = cudaMalloc((void**)&d_out, nv * 2 * n_g * sizeof(double));
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(d_ve, xyz_ve, nv * 8 * sizeof(double), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(d_fc, face_curved, nv * 4 * sizeof(int), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) {
+		A.xyz_ve = d_ve;
+		A.face_curved = d_fc;
+		A.geom_coef = d_out;
+		blend_quad_kernel<<<(unsigned)((nv + 127) / 128), 128, 0, st>>>(A);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(geom_coef, d_out, nv * 2 * n_g * sizeof(double), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(st);
+	cudaFree(d_ve);
+	cudaFree(d_fc);
+	cudaFree(d_out);
+	if (st)
+		cudaStreamDestroy(st);
+	if (e != cudaSuccess)
+		return cuda_fail(nullptr, e, "dgpu_blend_geometry");
+	return DGPU_OK;
+}

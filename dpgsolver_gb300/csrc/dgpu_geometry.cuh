@@ -271,4 +271,84 @@ __global__ void __launch_bounds__(128) geo_face_kernel(const GeoOps G, int n_fac
 	}
 }
 
+
+// ---- blended geometry of curved QUAD volumes -------------------------------------------------------------------
+// compute_geom_coef_blended_T (geometry_T.c:845-855) with constructor_xyz_blended_ce (geometry_blended_T.c:286-315)
+// for tensor-product volumes (Gordon-Hall blending, compute_p_base_min :320-335) on the reference's blended domains,
+// the n-cylinder meshes with the radial projection (constructor_xyz_surface_cylinder_radial_proj_T,
+// geometry_surface_T.c:103-147). Per volume, starting from the straight (bilinear) map at the GLL geometry nodes of
+// order p_g, each curved local face b in turn:
+//   surface   the face's straight nodes (its two vertices interpolated at the face's GLL nodes) projected radially
+//             onto the circle through its first vertex: r (cos theta, sin theta), theta = atan2(y, x);
+//   diff      surface - the current coordinates at the face's nodes, extended along the volume's lines normal to
+//             the face (vv0_fgc_vgc: the face node with the same tangential coordinate);
+//   blend     the sum of the face's two vertex basis functions at the node (constructor_blend_values :337-351),
+//             i.e. the linear hat that is 1 on face b and 0 on the opposite face;
+//   xyz += blend * diff.
+// The reference has no 3D TP blending (its edge step stops with EXIT_ADD_SUPPORT), so this is 2D only.
+struct BlendArgs {
+	int n_vol;
+	int qg;                  // geometry nodes per direction, p_g + 1
+	double x[kQMax];         // GLL nodes of order p_g on [-1, 1]
+	const double* xyz_ve;    // [v][c][vertex]: the straight volume's vertices (the p_g = 1 geom_coef layout)
+	const int* face_curved;  // [v][lf]: 1 for a curved boundary face (Face::bc > BC_CURVED_START)
+	double* geom_coef;       // [v][c][node]
+};
+
+__global__ void __launch_bounds__(128) blend_quad_kernel(const BlendArgs A)
+{
+	const int v = blockIdx.x * blockDim.x + threadIdx.x;
+	if (v >= A.n_vol)
+		return;
+	const int q = A.qg, n_g = q * q;
+	// local faces of a QUAD and their vertices (element.c f_ve, TP vertex order v = a + 2 b)
+	const int f_ve[4][2] = {{0, 2}, {1, 3}, {0, 1}, {2, 3}};
+	double ve[2][4];
+	for (int c = 0; c < 2; ++c)
+		for (int k = 0; k < 4; ++k)
+			ve[c][k] = A.xyz_ve[((size_t)v * 2 + c) * 4 + k];
+	double X[2][kQMax * kQMax];
+	for (int j = 0; j < q; ++j)
+		for (int i = 0; i < q; ++i) {
+			double phi[4];
+			for (int k = 0; k < 4; ++k)
+				phi[k] = 0.5 * ((k & 1) ? 1.0 + A.x[i] : 1.0 - A.x[i]) * 0.5 * ((k & 2) ? 1.0 + A.x[j] : 1.0 - A.x[j]);
+			for (int c = 0; c < 2; ++c) {
+				double s = 0.0;
+				for (int k = 0; k < 4; ++k)
+					s += phi[k] * ve[c][k];
+				X[c][i + q * j] = s;
+			}
+		}
+	for (int b = 0; b < 4; ++b) {
+		if (!A.face_curved[(size_t)v * 4 + b])
+			continue;
+		const int va = f_ve[b][0], vb = f_ve[b][1];
+		const double r = sqrt(ve[0][va] * ve[0][va] + ve[1][va] * ve[1][va]);
+		double diff[2][kQMax];
+		for (int k = 0; k < q; ++k) {
+			const double la = 0.5 * (1.0 - A.x[k]), lb = 0.5 * (1.0 + A.x[k]);
+			const double sx = la * ve[0][va] + lb * ve[0][vb], sy = la * ve[1][va] + lb * ve[1][vb];
+			const double th = atan2(sy, sx);
+			const int n = (b < 2) ? (b == 0 ? 0 : q - 1) + q * k : k + q * (b == 2 ? 0 : q - 1);
+			diff[0][k] = r * cos(th) - X[0][n];
+			diff[1][k] = r * sin(th) - X[1][n];
+		}
+		for (int j = 0; j < q; ++j)
+			for (int i = 0; i < q; ++i) {
+				double blend = 0.0;
+				for (int e = 0; e < 2; ++e) {
+					const int k = f_ve[b][e];
+					blend += 0.5 * ((k & 1) ? 1.0 + A.x[i] : 1.0 - A.x[i]) * 0.5 * ((k & 2) ? 1.0 + A.x[j] : 1.0 - A.x[j]);
+				}
+				const int t = (b < 2) ? j : i;
+				X[0][i + q * j] += blend * diff[0][t];
+				X[1][i + q * j] += blend * diff[1][t];
+			}
+	}
+	for (int c = 0; c < 2; ++c)
+		for (int n = 0; n < n_g; ++n)
+			A.geom_coef[((size_t)v * 2 + c) * n_g + n] = X[c][n];
+}
+
 }  // namespace dgpu

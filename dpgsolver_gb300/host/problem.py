@@ -484,27 +484,55 @@ def taylor_couette_state(x, y, r_i, r_o, omega, mu, Pr, r_s, t_b, p_b, dTdn):
     Returns the conserved variables (4, ...)."""
     r, th = np.sqrt(x * x + y * y), np.arctan2(y, x)
     c = omega / (1.0 / r_i ** 2 - 1.0 / r_o ** 2)
-    kappa = mu * (GAMMA / GM1 * r_s) / Pr
+    mu_kappa = Pr / (GAMMA / GM1 * r_s)                    # mu / kappa, kappa = mu Cp / Pr (also for mu = 0)
     vt = c * (1.0 / r - r / r_o ** 2)
-    t = (t_b - 2.0 * c * c / r_o ** 2 * mu / kappa * np.log(r / r_i) - c * c * mu / kappa * (1.0 / r ** 2 - 1.0 / r_i ** 2)
+    t = (t_b - 2.0 * c * c / r_o ** 2 * mu_kappa * np.log(r / r_i) - c * c * mu_kappa * (1.0 / r ** 2 - 1.0 / r_i ** 2)
          + dTdn * r_o * np.log(r / r_i))
     pr = np.full_like(r, p_b)
     return primitive_to_conserved(2, pr / (r_s * t), np.stack([-np.sin(th) * vt, np.cos(th) * vt]), pr)
 
 
-def ns_taylor_couette(n: int = 8, p: int = 3, mu: float = 1e-3, omega: float = 1.0, diabatic: bool = False,
-                      dTdn: float = 1.0, num_flux: int = NUM_FLUX_ROE_PIKE, perturb: float = 0.0) -> DGProblem:
+def annulus_vertices(n, r_i: float = 0.5, r_o: float = 1.0, rotate: float = 0.0):
+    """The straight QUAD mesh of the annulus r_i <= r <= r_o with n = n_r or (n_r, n_theta) volumes: volume (i, j) of
+    StructuredMesh(2, (n_r, n_theta), 0, 1, periodic=(False, True)) has its vertices on the circles
+    r_i + (r_o - r_i) (i + {0, 1}) / n_r at the angles 2 pi (j + {0, 1}) / n_theta + rotate. Returns xyz_ve
+    (n_volumes, 2, 4) in the TP vertex order and face_curved (n_volumes, 4), 1 on the faces on r_i (local face 0)
+    and r_o (local face 1), the reference's curved boundaries."""
+    n_r, n_t = (n, n) if np.ndim(n) == 0 else (int(n[0]), int(n[1]))
+    mesh = StructuredMesh(2, (n_r, n_t), 0.0, 1.0, periodic=(False, True))
+    ve = np.empty((mesh.n_volumes, 2, 4))
+    fc = np.zeros((mesh.n_volumes, 4), dtype=np.int32)
+    for v in range(mesh.n_volumes):
+        i, j = (int(k) for k in mesh.ijk[v][:2])
+        for k in range(4):
+            r = r_i + (r_o - r_i) * (i + (k & 1)) / n_r
+            th = 2.0 * math.pi * (j + (k >> 1)) / n_t + rotate
+            ve[v, :, k] = (r * math.cos(th), r * math.sin(th))
+        fc[v, 0] = 1 if i == 0 else 0
+        fc[v, 1] = 1 if i == n_r - 1 else 0
+    return ve, fc
+
+
+def ns_taylor_couette(n=8, p: int = 3, mu: float = 1e-3, omega: float = 1.0, diabatic: bool = False,
+                      dTdn: float = 1.0, num_flux: int = NUM_FLUX_ROE_PIKE, perturb: float = 0.0,
+                      geom_coef=None) -> DGProblem:
     """The reference's Navier-Stokes Taylor-Couette case (input_files/navier_stokes/steady/taylor_couette, mesh
-    meshes/n-cylinder_hollow/2d.geo) on a curved QUAD annulus, n x n volumes, r_i = 0.5, r_o = 1, periodic in theta:
+    meshes/n-cylinder_hollow/2d.geo) on a curved QUAD annulus, n = n_r or (n_r, n_theta) volumes, r_i = 0.5,
+    r_o = 1, periodic in theta:
     the inner cylinder rotates at omega (BC_NOSLIP_ALL_ROTATING with rho_b = 1, E_b = p_b / (gamma - 1) +
     rho_b (omega r_i)^2 / 2), the outer one is a static adiabatic wall (BC_NOSLIP_ADIABATIC), or a diabatic one
     with the normal temperature gradient dTdn (BC_NOSLIP_DIABATIC, solution_diabatic.data). Pr = 0.72, r_s = 1,
     p_b = t_b = 1; the state is the reference's Taylor-Couette solution, its density scaled by
-    1 + perturb sin(3 theta) sin(pi (r - r_i) / (r_o - r_i))."""
+    1 + perturb sin(3 theta) sin(pi (r - r_i) / (r_o - r_i)). The geometry is the exact polar map, or geom_coef
+    ((n_volumes, (p+1)^2, 2) at the GLL nodes of order p, e.g. the blended geometry of annulus_vertices(n))."""
     r_i, r_o, Pr, r_s, p_b, t_b = 0.5, 1.0, 0.72, 1.0, 1.0, 1.0
-    mesh = StructuredMesh(2, n, 0.0, 1.0, periodic=(False, True))
+    n_r, n_t = (n, n) if np.ndim(n) == 0 else (int(n[0]), int(n[1]))
+    mesh = StructuredMesh(2, (n_r, n_t), 0.0, 1.0, periodic=(False, True))
     ops = TPOperatorSet(mesh.e_type, p)
-    geom = TPGeometry(mesh, ops, deform=annulus_deform(r_i, r_o), curved=True)
+    if geom_coef is None:
+        geom = TPGeometry(mesh, ops, deform=annulus_deform(r_i, r_o), curved=True)
+    else:
+        geom = TPGeometry(mesh, ops, curved=True, coef=geom_coef)
     ns = _ns_params(mu, Pr=Pr, r_s=r_s)
     ns["dTdn"] = float(dTdn) if diabatic else 0.0
     prob = DGProblem("ns_taylor_couette", 2, PDE_NAVIER_STOKES, num_flux, True, np.zeros(3), ops, mesh, geom,
@@ -516,7 +544,7 @@ def ns_taylor_couette(n: int = 8, p: int = 3, mu: float = 1e-3, omega: float = 1
         R, TH = np.sqrt(X * X + Y * Y), np.arctan2(Y, X)
         U = U * (1.0 + perturb * np.sin(3.0 * TH) * np.sin(math.pi * (R - r_i) / (r_o - r_i)))[None]
     prob.sol = _pack_state(U)
-    prob.dt = stable_dt(prob, h=(r_o - r_i) / n)
+    prob.dt = stable_dt(prob, h=min((r_o - r_i) / n_r, 2.0 * math.pi * r_i / n_t))
     rho_b = 1.0
     E_b = p_b / GM1 + 0.5 * rho_b * (omega * r_i) ** 2
 
@@ -527,5 +555,5 @@ def ns_taylor_couette(n: int = 8, p: int = 3, mu: float = 1e-3, omega: float = 1
         return np.stack([np.full(len(r), rho_b), -rho_b * np.sin(th) * vt, rho_b * np.cos(th) * vt,
                          np.full(len(r), E_b)], axis=1)
     outer = BC_NOSLIP_DIABATIC if diabatic else BC_NOSLIP_ADIABATIC
-    prob.meta.update(n=n, p=p, omega=omega, r_i=r_i, r_o=r_o)
+    prob.meta.update(n=(n_r, n_t), p=p, omega=omega, r_i=r_i, r_o=r_o)
     return _set_boundaries(prob, {(0, 0): BC_NOSLIP_ALL_ROTATING, (0, 1): outer}, wall_state)

@@ -32,6 +32,21 @@ def _geom_coef(prob):
     return np.ascontiguousarray(np.transpose(prob.geom.X_geom, (0, 2, 1)))
 
 
+def blend_geometry(xyz_ve, face_curved, p_g: int):
+    """Blended geometry coefficients of curved QUAD volumes computed on the device (dgpu_blend_geometry): xyz_ve
+    (n_volumes, 2, 4) straight vertices, face_curved (n_volumes, 4) -> (n_volumes, (p_g+1)^2, 2), the coordinates at
+    the GLL nodes of order p_g (the layout of TPGeometry's coef)."""
+    lib = _lib.load()
+    ve = np.ascontiguousarray(xyz_ve, dtype=np.float64)
+    fc = np.ascontiguousarray(face_curved, dtype=np.int32)
+    nv, n_g = ve.shape[0], (p_g + 1) ** 2
+    if ve.shape != (nv, 2, 4) or fc.shape != (nv, 4):
+        raise ValueError("xyz_ve must be (n_volumes, 2, 4) and face_curved (n_volumes, 4)")
+    out = np.empty((nv, 2, n_g))
+    check(lib.dgpu_blend_geometry(2, p_g, nv, _dp(ve), _ip(fc), _dp(out)), None)
+    return np.ascontiguousarray(np.transpose(out, (0, 2, 1)))
+
+
 def compute_geometry(prob):
     """The geometric factors of a TP DGProblem computed on the device from its geometry coefficients
     (dgpu_compute_geometry), in the layouts of prob.geom: metrics_vc (n_volumes, n_vc, d, d), jacobian_det_vc

@@ -155,6 +155,21 @@ dgpu_status dgpu_destroy(dgpu_ctx* ctx);
  *   xyz_fc          n_faces x (n_fc x d) row-major: the face cubature nodes' coordinates (for constructor_sol_bv).
  * Synchronous. DGPU_ERR_INVALID_ARGUMENT when a Jacobian determinant is not positive. Of ops only elem_type, p and
  * w_vc are read. */
+/* Blended geometry coefficients of curved QUAD volumes on the device, host buffers in and out (synchronous): the
+ * reference's compute_geom_coef_blended_T (geometry_T.c:845-855, constructor_xyz_blended_ce
+ * geometry_blended_T.c:286-315) with TP Gordon-Hall blending and the radial projection of its blended n-cylinder
+ * domains (constructor_xyz_surface_cylinder_radial_proj_T, geometry_surface_T.c:103-147: each curved face's straight
+ * nodes moved to the circle about the origin through the face's first vertex).
+ *   xyz_ve      n_volumes x (4 x 2) column-major: the straight volume's vertices (Volume::xyz_ve, TP order; the
+ *               p_g = 1 geom_coef layout);
+ *   face_curved n_volumes x 4: 1 where local face lf (element.c order) is a curved boundary face
+ *               (Face::bc > BC_CURVED_START = 20000, is_face_bc_curved), else 0;
+ *   geom_coef   out, n_volumes x ((p_g+1)^2 x 2) column-major: the coordinates at the GLL nodes of order p_g, the
+ *               layout of dgpu_mesh.geom_coef.
+ * d = 2 only: the reference's 3D TP blending stops with EXIT_ADD_SUPPORT, and its other parametrizations
+ * (arc_length, normal_proj) are EXIT_ADD_SUPPORT too. Volumes without a curved face get the bilinear map. */
+dgpu_status dgpu_blend_geometry(int d, int p_g, int n_volumes, const double* xyz_ve, const int* face_curved,
+                                double* geom_coef);
 dgpu_status dgpu_compute_geometry(int d, const dgpu_tp_operators* ops, const dgpu_mesh* mesh, double* metrics_vc,
                                   double* jacobian_det_vc, double* normals_fc, double* jacobian_det_fc,
                                   double* xyz_fc);

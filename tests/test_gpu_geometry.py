@@ -118,3 +118,58 @@ def test_geometry_errors(gpu_lib):
     h = ctypes.c_void_p()
     st = gpu_lib.dgpu_create(ctypes.byref(phys), ctypes.byref(tp), ctypes.byref(m), ctypes.byref(h))
     assert st == 1 and b"geom_coef" in gpu_lib.dgpu_last_error(None)
+
+
+# ---- blended geometry of curved QUAD volumes (dgpu_blend_geometry) ------------------------------------------------
+@pytest.mark.parametrize("p_g", [1, 2, 3, 4])
+def test_blend_geometry_matches_oracle(gpu_lib, p_g):
+    """The device's blend against the oracle's dense-operator restatement (oracle/blend.py) on the annulus, and on
+    the same vertices with random curved-face flags (several curved faces per volume, blended one after another)."""
+    from oracle import blend as B
+    from dpgsolver_gb300.solver import blend_geometry
+    for n, seed in (((3, 16), None), ((6, 6), None), ((4, 8), 3)):
+        ve, fc = P.annulus_vertices(n, rotate=0.3)
+        if seed is not None:
+            fc = np.random.default_rng(seed).integers(0, 2, fc.shape).astype(np.int32)
+        ref = np.transpose(B.blend_quad(ve, fc, p_g), (0, 2, 1))
+        got = blend_geometry(ve, fc, p_g)
+        assert np.max(np.abs(got - ref)) <= 1e-14
+
+
+def test_taylor_couette_on_the_device_blended_geometry(gpu_lib):
+    """The reference's Taylor-Couette set-up end to end on the device: straight annulus -> dgpu_blend_geometry ->
+    dgpu_create from the geometry coefficients -> residual and RK steps, against the oracle on the same
+    coefficients (the host's geometric factors)."""
+    from dpgsolver_gb300.solver import Simulation, blend_geometry
+    ve, fc = P.annulus_vertices((3, 16))
+    coef = blend_geometry(ve, fc, 3)
+    prob = P.ns_taylor_couette((3, 16), 3, mu=0.02, perturb=0.2, geom_coef=coef)
+    o = oracle.Oracle(prob)
+    r_ref, _ = o.compute_rhs(prob.sol)
+    floor = 0.0
+    for seed in range(3):
+        noisy = prob.sol * (1.0 + np.random.default_rng(seed).choice([-1.0, 1.0], prob.sol.shape) * 2.0 ** -52)
+        floor = max(floor, rel(o.compute_rhs(noisy)[0], r_ref))
+    s_ref = prob.sol.copy()
+    for _ in range(3):
+        s_ref, _, _ = o.ssp_rk3_step(s_ref, prob.dt)
+    with Simulation(prob, device_geometry=True) as sim:
+        sim.compute_rhs()
+        r = sim.rhs
+        sim.ssp_rk3_steps(prob.dt, 3)
+        s = sim.sol_coef
+    assert rel(r, r_ref) <= max(TOL, 4.0 * floor)
+    assert rel(s, s_ref) <= TOL
+
+
+def test_blend_geometry_refusals(gpu_lib):
+    lib = _lib.load()
+    ve = np.zeros((1, 2, 4))
+    fc = np.zeros((1, 4), dtype=np.int32)
+    out = np.zeros((1, 2, 16))
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    args = (ve.ctypes.data_as(dp), fc.ctypes.data_as(ip), out.ctypes.data_as(dp))
+    assert lib.dgpu_blend_geometry(3, 3, 1, *args) == 2    # no 3D TP blending in the reference
+    assert lib.dgpu_blend_geometry(2, 5, 1, *args) == 2
+    assert lib.dgpu_blend_geometry(2, 3, 0, *args) == 1
