@@ -369,7 +369,8 @@ def run_ours(args, rank, world, local_rank):
                            "note": "residual on the reference's GLL coefficients (V u and V^-1 R included)"},
         "e2e": {"value": e2e_value, "unit": "DOF-residual-evals/s", "h2d_bytes_per_step": int(ns * 8),
                 "d2h_bytes_per_step": int(ns * 8),
-                "note": "per step: dgpu_upload_state + dgpu_ssp_rk3_step + dgpu_download_state from pinned memory"},
+                "note": "per step: dgpu_upload_state + dgpu_ssp_rk3_step + dgpu_download_state from pinned memory "
+                        "(the basis-change kernel reads and writes the pinned buffers directly over the host link)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": volume_traffic(prob, dom),

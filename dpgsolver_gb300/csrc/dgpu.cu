@@ -87,7 +87,9 @@ struct dgpu_ctx {
 	cudaError_t (*launch_face)(dgpu_ctx*) = nullptr;
 	cudaError_t (*launch_lift_rhs)(dgpu_ctx*) = nullptr;
 	cudaError_t (*launch_lift_rk)(dgpu_ctx*, double dt, int stage, int want_max) = nullptr;
-	cudaError_t (*launch_convert)(dgpu_ctx*, bool to_gl) = nullptr;
+	// basis change of a whole state between GLL coefficients and GL values; in_copy / out_copy may be null
+	cudaError_t (*launch_convert)(dgpu_ctx*, bool to_gl, const double* in, double* out, double* in_copy,
+	                              double* out_copy) = nullptr;
 	cudaError_t (*launch_adjoint)(dgpu_ctx*, const double* u, const double* rbar, double* ubar) = nullptr;
 	cudaError_t (*launch_objective)(dgpu_ctx*, double* ubar) = nullptr;   // needs traces of the state
 	cudaError_t (*launch_jvp)(dgpu_ctx*) = nullptr;   // R(u) into rhs and (dR/du) jv_du into jv_out
@@ -276,17 +278,18 @@ cudaError_t launch_lift_rk_t(dgpu_ctx* c, double dt, int stage, int want_max)
 }
 
 template <int D, int Q, int NV>
-cudaError_t launch_convert_t(dgpu_ctx* c, bool to_gl)
+cudaError_t launch_convert_t(dgpu_ctx* c, bool to_gl, const double* in, double* out, double* in_copy,
+                             double* out_copy)
 {
 	using S = TPShape<D, Q>;
 	const int blocks = (c->n_vol + S::E - 1) / S::E;
 	record_start(c, "tp_convert_kernel");
 	if (to_gl)
 		tp_convert_kernel<D, Q, NV, true><<<blocks, S::THREADS, convert_smem_bytes<D, Q, NV>(), c->stream>>>(
-			c->ops, c->n_vol, c->u, c->ug);
+			c->ops, c->n_vol, in, out, in_copy, out_copy);
 	else
 		tp_convert_kernel<D, Q, NV, false><<<blocks, S::THREADS, convert_smem_bytes<D, Q, NV>(), c->stream>>>(
-			c->ops, c->n_vol, c->ug, c->u);
+			c->ops, c->n_vol, in, out, in_copy, out_copy);
 	record_stop(c);
 	c->launches++;
 	return cudaGetLastError();
@@ -765,7 +768,7 @@ dgpu_status enqueue_rk_step(dgpu_ctx* c, double dt, bool want_max)
 dgpu_status ensure_coef(dgpu_ctx* c)
 {
 	if (!c->coef_valid) {
-		DGPU_CUDA(c, c->launch_convert(c, false));
+		DGPU_CUDA(c, c->launch_convert(c, false, c->ug, c->u, nullptr, nullptr));
 		c->coef_valid = true;
 	}
 	return DGPU_OK;
@@ -775,7 +778,7 @@ dgpu_status ensure_coef(dgpu_ctx* c)
 dgpu_status ensure_gl(dgpu_ctx* c)
 {
 	if (!c->gl_valid) {
-		DGPU_CUDA(c, c->launch_convert(c, true));
+		DGPU_CUDA(c, c->launch_convert(c, true, c->u, c->ug, nullptr, nullptr));
 		c->gl_valid = true;
 	}
 	return DGPU_OK;
@@ -1133,10 +1136,30 @@ dgpu_status dgpu_state_size(const dgpu_ctx* ctx, size_t* n)
 	return DGPU_OK;
 }
 
+// The device address of a caller's page-locked host buffer (cudaHostAlloc / cudaHostRegister), which kernels may
+// read and write directly over the host link; null for any other pointer (pageable or device memory).
+double* pinned_device_view(const void* host)
+{
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	return a.type == cudaMemoryTypeHost ? static_cast<double*>(a.devicePointer) : nullptr;
+}
+
 dgpu_status dgpu_upload_state(dgpu_ctx* c, const double* sol)
 {
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (double* dv = c->launch_convert ? pinned_device_view(sol) : nullptr) {
+		// a pinned buffer: one pass reads it over the host link, keeps the coefficients and forms the GL values
+		DGPU_CUDA(c, c->launch_convert(c, true, dv, c->ug, c->u, nullptr));
+		DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+		c->coef_valid = true;
+		c->gl_valid = true;
+		return DGPU_OK;
+	}
 	DGPU_CUDA(c, cudaMemcpyAsync(c->u, sol, state_size(c) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
 	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
 	c->coef_valid = true;
@@ -1148,6 +1171,15 @@ dgpu_status dgpu_download_state(dgpu_ctx* c, double* sol)
 {
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (!c->coef_valid && c->launch_convert) {
+		if (double* dv = pinned_device_view(sol)) {
+			// the coefficients are stale: V^-1 of the GL values written to the device copy and the pinned buffer
+			DGPU_CUDA(c, c->launch_convert(c, false, c->ug, c->u, nullptr, dv));
+			DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+			c->coef_valid = true;
+			return DGPU_OK;
+		}
+	}
 	dgpu_status st = ensure_coef(c);
 	if (st != DGPU_OK)
 		return st;

@@ -662,9 +662,12 @@ tp_lift_kernel(const TPOps ops, const TPParams P, const RkArgs rk)
 // ---------------------------------------------------------------------------------------------------------------
 // u (GLL coefficients) <-> ug (GL nodal values)
 // ---------------------------------------------------------------------------------------------------------------
+// in_copy / out_copy (either may be null): also write the input / the result there, so that one pass both moves a
+// state between a caller's pinned host buffer and the device and changes its basis.
 template <int D, int Q, int NV, bool TO_GL>
 __global__ void __launch_bounds__(TPShape<D, Q>::THREADS)
-tp_convert_kernel(const TPOps ops, int n_vol, const double* __restrict__ in, double* __restrict__ out)
+tp_convert_kernel(const TPOps ops, int n_vol, const double* __restrict__ in, double* __restrict__ out,
+                  double* __restrict__ in_copy, double* __restrict__ out_copy)
 {
 	using S = TPShape<D, Q>;
 	constexpr int N = S::N, E = S::E;
@@ -678,7 +681,10 @@ tp_convert_kernel(const TPOps ops, int n_vol, const double* __restrict__ in, dou
 	const int n_here = min(E, n_vol - v0);
 	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {
 		const int e = i / (NV * N), r = i % (NV * N);
-		base[e * PER_E + r] = in[(size_t)v0 * NV * N + i];
+		const double x = in[(size_t)v0 * NV * N + i];
+		base[e * PER_E + r] = x;
+		if (in_copy)
+			in_copy[(size_t)v0 * NV * N + i] = x;
 	}
 	__syncthreads();
 	const int e = tid / N, node = tid % N;
@@ -689,8 +695,12 @@ tp_convert_kernel(const TPOps ops, int n_vol, const double* __restrict__ in, dou
 	tp_apply<D, Q, NV>(sa, sb, sc, TO_GL ? sops->B : sops->Binv, node, active);
 	if (active)
 #pragma unroll
-		for (int k = 0; k < NV; ++k)
-			out[((size_t)(v0 + e) * NV + k) * N + node] = sb[k * N + node];
+		for (int k = 0; k < NV; ++k) {
+			const size_t o = ((size_t)(v0 + e) * NV + k) * N + node;
+			out[o] = sb[k * N + node];
+			if (out_copy)
+				out_copy[o] = sb[k * N + node];
+		}
 }
 
 }  // namespace dgpu
