@@ -11,8 +11,8 @@ by its stage update and positivity check (time_step_ssp_rk_33), replayed from a 
   value           device-resident state, CUDA events on the library's stream, max over ranks.
   plain_launches  the same stages launched kernel by kernel (the per-group form without the graph).
   compute_rhs_dg  the residual entry alone on the reference's GLL coefficients.
-  e2e             every step through the C ABI from pinned host memory: upload sol_coef, one RK3 step,
-                  download sol_coef (84 MB each way per step inside the timed region).
+  e2e             every step through the C ABI on pinned host memory: dgpu_ssp_rk3_step_host, the drop-in for
+                  time_step_ssp_rk_33 on the host's sol_coef (84 MB each way per step inside the timed region).
 Inputs are larger than L2 (state 84 MB + metric terms 151 MB + face data 50 MB per evaluation), so no flush.
 
 --impl reference times the reference's algorithm on the host cores. The reference itself cannot be built here
@@ -323,9 +323,7 @@ def run_ours(args, rank, world, local_rank):
     op = ctypes.cast(out_h.data_ptr(), c_dp)
 
     def e2e_step():
-        _lib.check(lib.dgpu_upload_state(sim.handle, sp), sim.handle)
-        _lib.check(lib.dgpu_ssp_rk3_step(sim.handle, ctypes.c_double(dt), None), sim.handle)
-        _lib.check(lib.dgpu_download_state(sim.handle, op), sim.handle)
+        _lib.check(lib.dgpu_ssp_rk3_step_host(sim.handle, ctypes.c_double(dt), sp, op, None), sim.handle)
 
     for _ in range(2):
         e2e_step()
@@ -369,8 +367,9 @@ def run_ours(args, rank, world, local_rank):
                            "note": "residual on the reference's GLL coefficients (V u and V^-1 R included)"},
         "e2e": {"value": e2e_value, "unit": "DOF-residual-evals/s", "h2d_bytes_per_step": int(ns * 8),
                 "d2h_bytes_per_step": int(ns * 8),
-                "note": "per step: dgpu_upload_state + dgpu_ssp_rk3_step + dgpu_download_state from pinned memory "
-                        "(the basis-change kernel reads and writes the pinned buffers directly over the host link)"},
+                "note": "per step: dgpu_ssp_rk3_step_host (time_step_ssp_rk_33 on host sol_coef) from and to "
+                        "pinned memory; the first volume kernel reads and the last lift writes the host buffers "
+                        "over the host link, overlapped with their arithmetic"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": volume_traffic(prob, dom),

@@ -143,6 +143,7 @@ EXPORTS = {
     "dgpu_compute_rhs_host": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
     "dgpu_ssp_rk3_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, c_double_p]),
     "dgpu_ssp_rk3_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, c_double_p]),
+    "dgpu_ssp_rk3_step_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, c_double_p, c_double_p, c_double_p]),
     "dgpu_positivity_corrections": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "dgpu_kernel_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "dgpu_synchronize": (ctypes.c_int, [ctypes.c_void_p]),

@@ -79,6 +79,12 @@ struct dgpu_ctx {
 	cudaGraphExec_t rk_graph = nullptr;       // one SSP-RK3 step
 	cudaGraphExec_t rk_graph_max = nullptr;   // the same step reducing max|rhs| in its last stage
 	double rk_graph_dt = 0.0, rk_graph_max_dt = 0.0;
+	// dgpu_ssp_rk3_step_host: a step that reads and writes caller buffers, captured for one (dt, in, out, max)
+	cudaGraphExec_t host_graph = nullptr;
+	double host_graph_dt = 0.0;
+	const double* host_graph_in = nullptr;
+	double* host_graph_out = nullptr;
+	bool host_graph_max = false;
 	long long launches = 0;
 	std::string err;
 	// launchers for the instantiated (D, Q, NV, PDE, FLUX)
@@ -87,6 +93,10 @@ struct dgpu_ctx {
 	cudaError_t (*launch_face)(dgpu_ctx*) = nullptr;
 	cudaError_t (*launch_lift_rhs)(dgpu_ctx*) = nullptr;
 	cudaError_t (*launch_lift_rk)(dgpu_ctx*, double dt, int stage, int want_max) = nullptr;
+	// the first volume term of a step on GLL coefficients `in`, keeping them (keep_coef, may be null) and ug; the
+	// last lift also writing the new coefficients to u and out_host (may be null). Null for Navier-Stokes.
+	cudaError_t (*launch_volume_in)(dgpu_ctx*, const double* in, double* keep_coef) = nullptr;
+	cudaError_t (*launch_lift_out)(dgpu_ctx*, double dt, int want_max, double* out_host) = nullptr;
 	// basis change of a whole state between GLL coefficients and GL values; in_copy / out_copy may be null
 	cudaError_t (*launch_convert)(dgpu_ctx*, bool to_gl, const double* in, double* out, double* in_copy,
 	                              double* out_copy) = nullptr;
@@ -277,6 +287,41 @@ cudaError_t launch_lift_rk_t(dgpu_ctx* c, double dt, int stage, int want_max)
 	return cudaGetLastError();
 }
 
+template <int D, int Q, int NV, int PDE>
+cudaError_t launch_volume_in_t(dgpu_ctx* c, const double* in, double* keep_coef)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	TPParams P = c->params();
+	P.keep_coef = keep_coef;
+	P.keep_gl = c->ug;
+	tp_volume_kernel<D, Q, NV, PDE, true><<<blocks, S::THREADS, volume_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops,
+	                                                                                                      P, in);
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV>
+cudaError_t launch_lift_out_t(dgpu_ctx* c, double dt, int want_max, double* out_host)
+{
+	using S = TPShape<D, Q>;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	RkArgs rk;
+	rk.u = c->ug;
+	rk.u0 = c->u0;
+	rk.rhs = c->rhs;
+	rk.dt = dt;
+	rk.stage = 2;
+	rk.positivity = c->positivity;
+	rk.want_max = want_max;
+	rk.out_coef = c->u;
+	rk.out_host = out_host;
+	tp_lift_kernel<D, Q, NV, kModeRkGlOut><<<blocks, S::THREADS, lift_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, c->params(), rk);
+	c->launches++;
+	return cudaGetLastError();
+}
+
 template <int D, int Q, int NV>
 cudaError_t launch_convert_t(dgpu_ctx* c, bool to_gl, const double* in, double* out, double* in_copy,
                              double* out_copy)
@@ -431,8 +476,12 @@ cudaError_t bind(dgpu_ctx* c)
 	c->launch_lift_rhs = launch_lift_rhs_t<D, Q, NV>;
 	c->launch_lift_rk = launch_lift_rk_t<D, Q, NV>;
 	c->launch_convert = launch_convert_t<D, Q, NV>;
+	c->launch_volume_in = launch_volume_in_t<D, Q, NV, PDE>;
+	c->launch_lift_out = launch_lift_out_t<D, Q, NV>;
 	const cudaFuncAttribute smem = cudaFuncAttributeMaxDynamicSharedMemorySize;
 	cudaError_t e;
+	if ((e = cudaFuncSetAttribute(tp_lift_kernel<D, Q, NV, kModeRkGlOut>, smem, (int)lift_smem_bytes<D, Q, NV>())))
+		return e;
 	if ((e = cudaFuncSetAttribute(tp_volume_kernel<D, Q, NV, PDE, true>, smem, (int)volume_smem_bytes<D, Q, NV>())))
 		return e;
 	if ((e = cudaFuncSetAttribute(tp_volume_kernel<D, Q, NV, PDE, false>, smem, (int)volume_smem_bytes<D, Q, NV>())))
@@ -545,6 +594,8 @@ cudaError_t bind_ns(dgpu_ctx* c)
 {
 	constexpr int NV = D + 2;
 	cudaError_t e = bind<D, Q, NV, kEuler, FLUX>(c);   // lift, convert, positivity: as for Euler
+	c->launch_volume_in = nullptr;   // the fused host step is Euler / advection only
+	c->launch_lift_out = nullptr;
 	if (e != cudaSuccess)
 		return e;
 	c->launch_volume = launch_ns_t<D, Q, FLUX, true>;
@@ -596,6 +647,8 @@ void free_all(dgpu_ctx* c)
 		cudaGraphExecDestroy(c->rk_graph);
 	if (c->rk_graph_max)
 		cudaGraphExecDestroy(c->rk_graph_max);
+	if (c->host_graph)
+		cudaGraphExecDestroy(c->host_graph);
 	for (auto& t : c->timers) {
 		cudaEventDestroy(t.start);
 		cudaEventDestroy(t.stop);
@@ -1296,6 +1349,85 @@ dgpu_status dgpu_ssp_rk3_step(dgpu_ctx* c, double dt, double* max_rhs)
 	return dgpu_ssp_rk3_steps(c, dt, 1, max_rhs);
 }
 
+// One SSP-RK3 step from GLL coefficients `in` (device-readable) to ug and u, the new coefficients also into `out`
+// (a device view of the caller's pinned buffer, or null): the first volume term keeps the coefficients (keep,
+// null when they are already in u) and forms ug; the last lift writes V^-1 of the new state.
+static dgpu_status enqueue_rk_step_host(dgpu_ctx* c, double dt, bool want_max, const double* in, double* keep,
+                                        double* out)
+{
+	DGPU_CUDA(c, c->launch_volume_in(c, in, keep));
+	DGPU_CUDA(c, c->launch_face(c));
+	DGPU_CUDA(c, c->launch_lift_rk(c, dt, 0, 0));
+	DGPU_CUDA(c, c->launch_volume_gl(c));
+	DGPU_CUDA(c, c->launch_face(c));
+	DGPU_CUDA(c, c->launch_lift_rk(c, dt, 1, 0));
+	DGPU_CUDA(c, c->launch_volume_gl(c));
+	DGPU_CUDA(c, c->launch_face(c));
+	DGPU_CUDA(c, c->launch_lift_out(c, dt, want_max ? 1 : 0, out));
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_ssp_rk3_step_host(dgpu_ctx* c, double dt, const double* sol_in, double* sol_out, double* max_rhs)
+{
+	if (!c || !sol_in || !sol_out || !(dt == dt))
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (!c->launch_volume_in || !c->launch_lift_out || c->timing) {   // Navier-Stokes, or per-kernel timing
+		dgpu_status st = dgpu_upload_state(c, sol_in);
+		if (st == DGPU_OK)
+			st = dgpu_ssp_rk3_step(c, dt, max_rhs);
+		if (st == DGPU_OK)
+			st = dgpu_download_state(c, sol_out);
+		return st;
+	}
+	const size_t bytes = state_size(c) * sizeof(double);
+	const double* in = pinned_device_view(sol_in);
+	double* keep = c->u;
+	if (!in) {   // pageable: copy to u first
+		DGPU_CUDA(c, cudaMemcpyAsync(c->u, sol_in, bytes, cudaMemcpyHostToDevice, c->stream));
+		in = c->u;
+		keep = nullptr;
+	}
+	double* out = pinned_device_view(sol_out);
+	const bool want_max = (max_rhs != nullptr);
+	if (!(c->host_graph && c->host_graph_dt == dt && c->host_graph_in == in && c->host_graph_out == out &&
+	      c->host_graph_max == want_max)) {
+		if (c->host_graph) {
+			cudaGraphExecDestroy(c->host_graph);
+			c->host_graph = nullptr;
+		}
+		cudaGraph_t g;
+		DGPU_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+		const long long before = c->launches;
+		dgpu_status st = enqueue_rk_step_host(c, dt, want_max, in, keep, out);
+		c->launches = before;   // captured, not launched
+		cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+		if (st != DGPU_OK)
+			return st;
+		DGPU_CUDA(c, ec);
+		cudaError_t ei = cudaGraphInstantiate(&c->host_graph, g, 0);
+		cudaGraphDestroy(g);
+		DGPU_CUDA(c, ei);
+		c->host_graph_dt = dt;
+		c->host_graph_in = in;
+		c->host_graph_out = out;
+		c->host_graph_max = want_max;
+	}
+	DGPU_CUDA(c, cudaGraphLaunch(c->host_graph, c->stream));
+	c->launches += 9;
+	c->coef_valid = true;
+	c->gl_valid = true;
+	if (!out)
+		DGPU_CUDA(c, cudaMemcpyAsync(sol_out, c->u, bytes, cudaMemcpyDeviceToHost, c->stream));
+	dgpu_status st = check_positivity_flag(c);
+	if (st != DGPU_OK)
+		return st;
+	st = read_max(c, max_rhs);
+	if (st != DGPU_OK)
+		return st;
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}
+
 dgpu_status dgpu_positivity_corrections(dgpu_ctx* c, long long* n)
 {
 	if (!c || !n)
@@ -1339,6 +1471,10 @@ dgpu_status dgpu_set_stream(dgpu_ctx* c, void* stream)
 	if (c->rk_graph_max) {
 		cudaGraphExecDestroy(c->rk_graph_max);
 		c->rk_graph_max = nullptr;
+	}
+	if (c->host_graph) {
+		cudaGraphExecDestroy(c->host_graph);
+		c->host_graph = nullptr;
 	}
 	return DGPU_OK;
 }

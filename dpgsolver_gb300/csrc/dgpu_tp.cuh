@@ -75,6 +75,10 @@ struct TPParams {
 	double* ns_gv;             // [v][D][NV][N] volume gradient (physical, at the GL nodes)
 	NsPhys ns;                 // viscosity model and constants
 	double ns_eta;             // BR2 scaling of a face's own lifting in its face gradient
+	// Volume kernel on GLL coefficients only (may be null): also keep the coefficients it read and the GL values it
+	// formed, so that one pass over a caller's host buffer both uploads the state and starts the RK step.
+	double* keep_coef = nullptr;   // [v][NV][N]
+	double* keep_gl = nullptr;     // [v][NV][N]
 };
 
 // Right-hand state of face node i of boundary face b: the boundary value of its BC from the interior trace WL.
@@ -184,7 +188,10 @@ __device__ __forceinline__ void tp_volume_body(const TPOps* sops, const TPParams
 	const int tid = threadIdx.x;
 	for (int i = tid; i < n_here * NV * N; i += blockDim.x) {   // coalesced: contiguous element blocks
 		const int e = i / (NV * N), r = i % (NV * N);
-		base[e * PER_E + r] = u[(size_t)v0 * NV * N + i];
+		const double x = u[(size_t)v0 * NV * N + i];
+		base[e * PER_E + r] = x;
+		if (GLL_IN && P.keep_coef)
+			P.keep_coef[(size_t)v0 * NV * N + i] = x;
 	}
 	__syncthreads();
 
@@ -199,8 +206,11 @@ __device__ __forceinline__ void tp_volume_body(const TPOps* sops, const TPParams
 		tp_apply<D, Q, NV>(su, st, sf, sops->B, node, active);
 		if (active)
 #pragma unroll
-			for (int k = 0; k < NV; ++k)
+			for (int k = 0; k < NV; ++k) {
 				su[k * N + node] = st[k * N + node];
+				if (P.keep_gl)
+					P.keep_gl[((size_t)(v0 + e) * NV + k) * N + node] = st[k * N + node];
+			}
 		__syncthreads();
 	}
 
@@ -364,7 +374,9 @@ tp_face_kernel(const TPParams P)
 // ---------------------------------------------------------------------------------------------------------------
 // kModeRkGl reads rk.want_max at run time; kModeRkGlNoMax is the RK stage compiled without the max |rhs| path
 // (fewer registers for the common graph-replayed stage).
-enum LiftMode { kModeRhs = 0, kModeRkGl = 1, kModeRkGlNoMax = 2 };
+// kModeRkGlOut is kModeRkGl that also writes the new state's GLL coefficients (the last stage of a step whose result
+// goes back to the caller).
+enum LiftMode { kModeRhs = 0, kModeRkGl = 1, kModeRkGlNoMax = 2, kModeRkGlOut = 3 };
 
 struct RkArgs {
 	double* u;         // kModeRkGl: state as GL nodal values (ug), updated in place
@@ -374,6 +386,8 @@ struct RkArgs {
 	int stage;         // 0, 1, 2
 	int positivity;
 	int want_max;      // kModeRkGl: also reduce max |rhs| (needs V^-1 of the GL residual)
+	double* out_coef = nullptr;   // kModeRkGlOut: V^-1 of the new state (GLL coefficients)
+	double* out_host = nullptr;   // kModeRkGlOut: the same into a caller's pinned host buffer, or null
 };
 
 // enforce_positivity_highorder (solve.c:187-233) on one element held in shared memory.
@@ -519,7 +533,7 @@ __device__ __forceinline__ void tp_lift_body(const TPOps* sops, const TPParams& 
 			Rg[k] *= iw;
 	}
 
-	const bool need_coef = (MODE == kModeRhs) || (MODE == kModeRkGl && rk.want_max);   // uniform across the grid
+	const bool need_coef = (MODE == kModeRhs) || ((MODE == kModeRkGl || MODE == kModeRkGlOut) && rk.want_max);
 	unsigned long long mx = 0ull;
 	double R[NV];
 	if (MODE != kModeRkGlNoMax && need_coef) {
@@ -639,12 +653,30 @@ __device__ __forceinline__ void tp_lift_body(const TPOps* sops, const TPParams& 
 			for (int k = 0; k < NV; ++k)
 				rk.u[o + (size_t)k * N] = snew[k];
 		}
+		if constexpr (MODE == kModeRkGlOut) {
+			// the new state's GLL coefficients: V^-1 of the GL values (D passes of Binv)
+			__syncthreads();   // sa/sb/sc are free again
+			if (active)
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					sa[k * N + node] = snew[k];
+			__syncthreads();
+			tp_apply<D, Q, NV>(sa, sb, sc, sops->Binv, node, active);
+			if (active)
+#pragma unroll
+				for (int k = 0; k < NV; ++k) {
+					const size_t o = ((size_t)v * NV + k) * N + node;
+					rk.out_coef[o] = sb[k * N + node];
+					if (rk.out_host)
+						rk.out_host[o] = sb[k * N + node];
+				}
+		}
 	}
 }
 
 // Minimum CTAs per SM of the lift kernel (caps its registers): 3 for the plain RK stage, 2 otherwise.
 template <int MODE>
-struct LiftOccupancy { static constexpr int value = (MODE == kModeRkGlNoMax) ? 4 : 2; };
+struct LiftOccupancy { static constexpr int value = (MODE == kModeRkGlNoMax) ? 4 : 2; };   // Out: as RkGl
 
 template <int D, int Q, int NV, int MODE>
 __global__ void __launch_bounds__(TPShape<D, Q>::THREADS, LiftOccupancy<MODE>::value)

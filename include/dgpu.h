@@ -189,6 +189,14 @@ dgpu_status dgpu_compute_rhs_host(dgpu_ctx* ctx, const double* sol, double* rhs,
  * graph captured on first use for each dt. max_rhs: as for dgpu_compute_rhs (last stage's residual). */
 dgpu_status dgpu_ssp_rk3_step(dgpu_ctx* ctx, double dt, double* max_rhs);
 dgpu_status dgpu_ssp_rk3_steps(dgpu_ctx* ctx, double dt, int n_steps, double* max_rhs);
+/* time_step_ssp_rk_33 (solve_explicit.c:252-301) on host state: sol_in (host, the sol_coef blocks) -> one SSP-RK3
+ * step -> sol_out (host; may equal sol_in), synchronous; the device state becomes the new state. The same result,
+ * bit for bit, as dgpu_upload_state + dgpu_ssp_rk3_step + dgpu_download_state. For page-locked buffers
+ * (cudaHostAlloc / cudaHostRegister) the transfers happen inside the step's first volume kernel and last lift
+ * kernel, overlapped with their arithmetic; pageable buffers are copied. Replayed from a CUDA graph captured for
+ * each (dt, buffers, max_rhs requested); Navier-Stokes contexts run the three calls above. */
+dgpu_status dgpu_ssp_rk3_step_host(dgpu_ctx* ctx, double dt, const double* sol_in, double* sol_out,
+                                   double* max_rhs);
 
 /* Residual without any device allocation. No counterpart in the reference (its residual is host code).
  *

@@ -49,3 +49,57 @@ def test_pinned_and_pageable_transfers_agree(gpu_lib, mk):
     assert np.array_equal(o0, o1)
     assert m0 == m1
     assert np.array_equal(r0, r1)
+
+
+def _step_host(lib, h, dt, src, dst, want_max):
+    mx = ctypes.c_double()
+    _lib.check(lib.dgpu_ssp_rk3_step_host(h, ctypes.c_double(dt), src, dst, ctypes.byref(mx) if want_max else None),
+               h)
+    return mx.value
+
+
+@pytest.mark.parametrize("mk", [lambda: P.euler_hex_3d(4, 3), lambda: P.euler_channel_2d(6, 2),
+                                lambda: P.advection_2d(8, 2), lambda: P.ns_channel(2, 4, 2)])
+def test_step_on_host_buffers_is_the_composed_step(gpu_lib, mk):
+    """dgpu_ssp_rk3_step_host == upload + step + download, bit for bit: pinned and pageable buffers, the output
+    aliasing the input, two steps on one graph, then a new dt (a new capture); the device state follows."""
+    import torch
+    from dpgsolver_gb300.solver import Simulation
+    prob = mk()
+    lib = _lib.load()
+    dp = ctypes.POINTER(ctypes.c_double)
+    base = prob.sol + 1e-3 * np.random.default_rng(5).standard_normal(prob.sol.shape)
+    dts = (prob.dt, prob.dt, 0.5 * prob.dt)
+    ref, ref_mx = [], []
+    with Simulation(prob) as sim:
+        h, s = sim.handle, np.ascontiguousarray(base).copy()
+        for k, dt in enumerate(dts):
+            _lib.check(lib.dgpu_upload_state(h, s.ctypes.data_as(dp)), h)
+            mx = ctypes.c_double()
+            _lib.check(lib.dgpu_ssp_rk3_step(h, ctypes.c_double(dt), ctypes.byref(mx) if k != 1 else None), h)
+            _lib.check(lib.dgpu_download_state(h, s.ctypes.data_as(dp)), h)
+            ref.append(s.copy())
+            ref_mx.append(mx.value)
+    for mode in ("pinned", "pageable", "pinned_alias"):
+        with Simulation(prob) as sim:
+            h = sim.handle
+            if mode == "pageable":
+                a, b = np.ascontiguousarray(base).copy(), np.empty_like(base)
+                pa, pb = a.ctypes.data_as(dp), b.ctypes.data_as(dp)
+                get = lambda: b.copy()   # noqa: E731
+            else:
+                ta = torch.from_numpy(base.copy()).pin_memory()
+                tb = ta if mode == "pinned_alias" else torch.zeros(base.shape, dtype=torch.float64).pin_memory()
+                pa, pb = ctypes.cast(ta.data_ptr(), dp), ctypes.cast(tb.data_ptr(), dp)
+                get = lambda: tb.numpy().copy()   # noqa: E731
+            for k, dt in enumerate(dts):
+                mx = _step_host(lib, h, dt, pa, pb, k != 1)
+                out = get()
+                assert np.array_equal(out, ref[k]), (mode, k)
+                if k != 1:
+                    assert mx == ref_mx[k]
+                if mode == "pageable":
+                    a[...] = out
+                elif mode == "pinned":
+                    ta.copy_(tb)
+            assert np.array_equal(sim.sol_coef, ref[-1])
