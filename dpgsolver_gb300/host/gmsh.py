@@ -12,6 +12,8 @@ from __future__ import annotations
 
 import ctypes
 
+import math
+
 import numpy as np
 
 from .. import _lib
@@ -190,6 +192,47 @@ def write_box_msh(path, d: int, n, lo=0.0, hi=1.0, periodic=True, codes=None, ro
             fh.write("$EndPeriodic\n")
 
 
+def write_annulus_msh(path, n_r: int, n_t: int, r_i: float = 0.5, r_o: float = 1.0, inner: int = 20113,
+                      outer: int = 20111, rotate_seed=None):
+    """Write the QUAD annulus r_i <= r <= r_o (n_r volumes across, n_t around, vertices on the circles) as a gmsh 2.2
+    file the way the reference's n-cylinder_hollow meshes come: the boundary lines on r_i and r_o carry the codes
+    inner and outer (BC_CURVED_START + code: curved, e.g. 20113 for the rotating wall), then the volumes. The mesh is
+    conforming round the circle (no periodic section). rotate_seed: random local frames, as in write_box_msh."""
+    def node(i, j):
+        return i + (n_r + 1) * (j % n_t)
+
+    pts = []
+    for j in range(n_t):
+        th = 2.0 * math.pi * j / n_t
+        for i in range(n_r + 1):
+            r = r_i + (r_o - r_i) * i / n_r
+            pts.append((r * math.cos(th), r * math.sin(th)))
+    rots = _rotations(2)
+    rng = np.random.default_rng(rotate_seed) if rotate_seed is not None else None
+    corners = np.array([[v & 1, (v >> 1) & 1] for v in range(4)])
+    lines = []
+    for j in range(n_t):
+        lines.append((LINE, (inner, 1001), [node(0, j), node(0, j + 1)]))
+    for j in range(n_t):
+        lines.append((LINE, (outer, 1002), [node(n_r, j), node(n_r, j + 1)]))
+    for j in range(n_t):
+        for i in range(n_r):
+            R = rots[int(rng.integers(len(rots)))] if rng is not None else np.eye(2, dtype=int)
+            ref = []
+            for c in corners:
+                rc = (R @ (2 * c - 1) + 1) // 2
+                ref.append(node(i + int(rc[0]), j + int(rc[1])))
+            lines.append((QUAD, (9401, 4001), [ref[k] for k in _GMSH_FROM_TP[2]]))
+    with open(path, "w") as fh:
+        fh.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % len(pts))
+        for k, (x, y) in enumerate(pts):
+            fh.write("%d %.17g %.17g 0\n" % (k + 1, x, y))
+        fh.write("$EndNodes\n$Elements\n%d\n" % len(lines))
+        for k, (t, tags, verts) in enumerate(lines):
+            fh.write("%d %d 2 %d %d %s\n" % (k + 1, t, tags[0], tags[1], " ".join(str(v + 1) for v in verts)))
+        fh.write("$EndElements\n")
+
+
 # ---- a TP problem on a mesh read from a file ------------------------------------------------------------------------
 def tp_face_permutation(match, q: int, d: int) -> np.ndarray:
     """The right-trace gather permutation nc (sR[i] = sR_own[nc[i]]) of a TP face's q^(d-1) GL nodes from the
@@ -246,25 +289,44 @@ class GmshTPMesh:
         return nc
 
 
+BC_CURVED_START = 20000   # definitions_bc.h:34: codes above it mark curved boundary faces
+
+
+def curved_faces(mesh) -> np.ndarray:
+    """(n_volumes, 2d): 1 where a volume's local face is a curved boundary face (face_bc > BC_CURVED_START,
+    is_face_bc_curved), the faces a blended domain moves onto its surface."""
+    fc = np.zeros((mesh.n_volumes, 2 * mesh.d), dtype=np.int32)
+    for f in np.nonzero((mesh.face_vol[:, 1] < 0) & (mesh.face_bc > BC_CURVED_START))[0]:
+        fc[mesh.face_vol[f, 0], mesh.face_lf[f, 0]] = 1
+    return fc
+
+
 def gmsh_tp_problem(path, d: int, p: int, pde: int, num_flux: int, state, b_adv=(1.0, 0.5, 0.0), exterior=None,
-                    bc_data=None, cfl: float = 0.1, name: str | None = None):
-    """A DGProblem on the straight QUAD/HEX mesh in a gmsh file: geometry coefficients = the volumes' vertices (p_g =
-    1), state(xyz (m, d)) -> (m, n_var) the conserved initial state at the solution nodes, exterior(xyz) likewise the
-    exterior state of the boundary faces (their BC codes come from the file), bc_data the BC_Data scalars."""
+                    bc_data=None, cfl: float = 0.1, name: str | None = None, ns=None, blend=None):
+    """A DGProblem on the QUAD/HEX mesh in a gmsh file: geometry coefficients = the volumes' vertices (p_g = 1),
+    state(xyz (m, d)) -> (m, n_var) the conserved initial state at the solution nodes, exterior(xyz) likewise the
+    exterior state of the boundary faces (their BC codes come from the file), bc_data the BC_Data scalars, ns the
+    Navier-Stokes constants (pde 4). blend(xyz_ve (n_volumes, 2, 4), face_curved, p) -> (n_volumes, (p+1)^2, 2):
+    the blended domain's geometry coefficients at order p for the volumes with curved faces (2D; e.g.
+    solver.blend_geometry on the device)."""
     from .element import TPOperatorSet
     from .geometry import TPGeometry
-    from .problem import DGProblem, PDE_EULER, stable_dt
+    from .problem import DGProblem, PDE_ADVECTION, stable_dt
     gm = GmshMesh(path, d)
     mesh = GmshTPMesh(gm)
     ops = TPOperatorSet(mesh.e_type, p)
-    geom = TPGeometry(mesh, ops, curved=False, coef=mesh.vertices)
-    n_var = d + 2 if pde == PDE_EULER else 1
-    prob = DGProblem(name or f"gmsh_{d}d", d, pde, num_flux, pde == PDE_EULER, np.asarray(b_adv, dtype=np.float64),
-                     ops, mesh, geom, sol=np.zeros((mesh.n_volumes, n_var, ops.n_vs)), dt=0.0, n_steps=100)
+    if blend is not None:
+        coef = blend(np.ascontiguousarray(np.transpose(mesh.vertices, (0, 2, 1))), curved_faces(mesh), p)
+        geom = TPGeometry(mesh, ops, curved=True, coef=coef)
+    else:
+        geom = TPGeometry(mesh, ops, curved=False, coef=mesh.vertices)
+    n_var = 1 if pde == PDE_ADVECTION else d + 2
+    prob = DGProblem(name or f"gmsh_{d}d", d, pde, num_flux, pde != PDE_ADVECTION, np.asarray(b_adv, dtype=np.float64),
+                     ops, mesh, geom, sol=np.zeros((mesh.n_volumes, n_var, ops.n_vs)), dt=0.0, n_steps=100, ns=ns)
     xyz = prob.solution_node_xyz()
     U = np.asarray(state(xyz.reshape(-1, d)), dtype=np.float64).reshape(mesh.n_volumes, ops.n_vs, n_var)
     prob.sol = np.ascontiguousarray(np.transpose(U, (0, 2, 1)))
-    if pde == PDE_EULER:
+    if pde != PDE_ADVECTION:
         prob.dt = stable_dt(prob, cfl)
     else:
         prob.dt = cfl * float(np.min(mesh.h)) / ((2 * p + 1) * float(np.linalg.norm(prob.b_adv)))

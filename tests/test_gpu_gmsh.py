@@ -86,3 +86,40 @@ def test_gmsh_advection_upwind_box(gpu_lib, tmp_path):
         sim.compute_rhs()
         r = sim.rhs
     assert rel(r, r_ref) <= TOL
+
+
+def test_taylor_couette_from_a_gmsh_file_on_the_device(gpu_lib, tmp_path):
+    """The reference's curved-boundary workflow on the device: a gmsh annulus with curved codes (20113 rotating
+    wall inside, 20112 diabatic wall outside) and random local frames -> reader and connectivity -> the blended
+    geometry of its curved faces (dgpu_blend_geometry) -> a Navier-Stokes context from the geometry coefficients:
+    residual and RK steps against the oracle on the same problem (noise-floor rule of test_gpu_ns.py)."""
+    from dpgsolver_gb300.solver import Simulation, blend_geometry
+    path = tmp_path / "annulus.msh"
+    G.write_annulus_msh(path, 3, 16, outer=20112, rotate_seed=9)
+
+    def state(x):
+        U = P.taylor_couette_state(x[:, 0], x[:, 1], 0.5, 1.0, 1.0, 0.02, 0.72, 1.0, 1.0, 1.0, 0.5).T
+        return U * (1.0 + 0.1 * np.sin(3.0 * np.arctan2(x[:, 1], x[:, 0])))[:, None]
+
+    def wall(x):
+        r, th = np.hypot(x[:, 0], x[:, 1]), np.arctan2(x[:, 1], x[:, 0])
+        return np.stack([np.ones_like(r), -np.sin(th) * r, np.cos(th) * r, np.full_like(r, 1.0 / P.GM1 + 0.125)], 1)
+    ns = {"viscosity": P.VISCOSITY_CONSTANT, "mu": 0.02, "Pr": 0.72, "r_s": 1.0, "dTdn": 0.5}
+    prob = G.gmsh_tp_problem(path, 2, 3, P.PDE_NAVIER_STOKES, P.NUM_FLUX_ROE_PIKE, state, exterior=wall, ns=ns,
+                             blend=blend_geometry)
+    o = oracle.Oracle(prob)
+    r_ref, _ = o.compute_rhs(prob.sol)
+    floor = 0.0
+    for seed in range(3):
+        noisy = prob.sol * (1.0 + np.random.default_rng(seed).choice([-1.0, 1.0], prob.sol.shape) * 2.0 ** -52)
+        floor = max(floor, rel(o.compute_rhs(noisy)[0], r_ref))
+    s_ref = prob.sol.copy()
+    for _ in range(3):
+        s_ref, _, _ = o.ssp_rk3_step(s_ref, prob.dt)
+    with Simulation(prob, device_geometry=True) as sim:
+        sim.compute_rhs()
+        r = sim.rhs
+        sim.ssp_rk3_steps(prob.dt, 3)
+        s = sim.sol_coef
+    assert rel(r, r_ref) <= max(TOL, 4.0 * floor)
+    assert rel(s, s_ref) <= TOL

@@ -134,3 +134,45 @@ def test_free_stream_on_perturbed_rotated_mesh(tmp_path):
         prob = _box_problem(tmp_path, d, n, 3, 7)
         cs = P.constant_state(prob, [1.0, 0.3, -0.2] + ([0.1] if d == 3 else []) + [2.5])
         assert oracle.Oracle(prob).compute_rhs(cs)[1] < 1e-11
+
+
+# ---- the reference's curved-boundary workflow: a blended annulus read from a file ----------------------------------
+def _couette_fns(omega=1.0):
+    def state(x):
+        return P.taylor_couette_state(x[:, 0], x[:, 1], 0.5, 1.0, omega, 0.02, 0.72, 1.0, 1.0, 1.0, 0.0).T
+
+    def wall(x):
+        r, th = np.hypot(x[:, 0], x[:, 1]), np.arctan2(x[:, 1], x[:, 0])
+        e_b = 1.0 / P.GM1 + 0.5 * (omega * 0.5) ** 2
+        return np.stack([np.ones_like(r), -np.sin(th) * omega * r, np.cos(th) * omega * r, np.full_like(r, e_b)], 1)
+    return state, wall
+
+
+def _oracle_blend(ve, fc, p):
+    from oracle import blend as B
+    return np.transpose(B.blend_quad(ve, fc, p), (0, 2, 1))
+
+
+def test_blended_annulus_from_a_file(tmp_path):
+    """gmsh annulus (codes 20113 inside, 20111 outside, random local frames) -> reader -> curved faces from the codes
+    -> blend: the same domain as the structured annulus (area), and the fluid at rest is steady on it."""
+    from dpgsolver_gb300.host.element import TPOperatorSet
+    from dpgsolver_gb300.host.geometry import TPGeometry
+    from dpgsolver_gb300.host.mesh import StructuredMesh
+    path = tmp_path / "annulus.msh"
+    G.write_annulus_msh(path, 3, 16, rotate_seed=4)
+    state, wall = _couette_fns(omega=0.0)
+    ns = {"viscosity": P.VISCOSITY_CONSTANT, "mu": 0.02, "Pr": 0.72, "r_s": 1.0}
+    prob = G.gmsh_tp_problem(path, 2, 3, P.PDE_NAVIER_STOKES, P.NUM_FLUX_ROE_PIKE, state, exterior=wall, ns=ns,
+                             blend=_oracle_blend)
+    assert sorted(set(prob.bc[prob.mesh.face_vol[:, 1] < 0].tolist())) == [20111, 20113]
+    assert int(G.curved_faces(prob.mesh).sum()) == 32
+    area = float((prob.geom.jacobian_det_vc * prob.ops.w_vc[None, :]).sum())
+    ve, fc = P.annulus_vertices((3, 16))
+    mesh = StructuredMesh(2, (3, 16), 0.0, 1.0, periodic=(False, True))
+    ops = TPOperatorSet(mesh.e_type, 3)
+    ref = TPGeometry(mesh, ops, curved=True, coef=_oracle_blend(ve, fc, 3))
+    assert abs(area - float((ref.jacobian_det_vc * ops.w_vc[None, :]).sum())) <= 1e-13
+    rest = P.constant_state(prob, [1.0, 0.0, 0.0, 1.0 / P.GM1])
+    o = oracle.Oracle(prob)
+    assert np.max(np.abs(o.compute_rhs_raw(rest))) < 1e-14
