@@ -61,6 +61,9 @@ struct dgpu_batch {
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	double *u = nullptr, *ug = nullptr, *u0 = nullptr, *rhs = nullptr, *vol_gl = nullptr;
 	double *traces = nullptr, *nnf = nullptr;
+	int* d_fbc = nullptr;                  // boundary faces (null without any): code per internal face, -1 inside
+	double* d_fext = nullptr;              // their exterior state, [NV][NF_f] at NV fbase[f]
+	BcData bc_data = {0.0, 0.0, 0.0, 0.0};
 	unsigned long long* max_bits = nullptr;
 	int* err_flag = nullptr;
 	unsigned long long* n_corr = nullptr;
@@ -105,6 +108,9 @@ struct dgpu_batch {
 		P.max_bits = max_bits;
 		P.err_flag = err_flag;
 		P.n_corr = n_corr;
+		P.fbc = d_fbc;
+		P.fext = d_fext;
+		P.bc_data = bc_data;
 		return P;
 	}
 	int group_n_vol(int g) const { return gl[g].dense ? hdgroups[gl[g].idx].n_vol : hgroups[gl[g].idx].n_vol; }
@@ -405,7 +411,7 @@ void free_batch(dgpu_batch* c)
 	drop_graphs(c);
 	void* ptrs[] = {c->d_ops, c->d_groups, c->d_dgroups, c->d_elf, c->d_fbase, c->d_node_face, c->gmet, c->inv_wJ,
 	                c->fgeo, c->u, c->ug, c->u0, c->rhs, c->vol_gl, c->traces, c->nnf, c->max_bits, c->err_flag,
-	                c->n_corr, c->d_tiles};
+	                c->n_corr, c->d_tiles, c->d_fbc, c->d_fext};
 	for (void* p : ptrs)
 		if (p)
 			cudaFree(p);
@@ -815,19 +821,30 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	}
 	// ---- faces: order p_f = max of the sides; internal face ids by increasing q_f ----
 	std::vector<int> face_q(nF), face_nfc(nF);
+	int n_bnd = 0;
 	for (int f = 0; f < nF; ++f) {
 		int qf = 0;
-		for (int s = 0; s < 2; ++s) {
+		const int ns_f = (mesh->face_vol[2 * f + 1] < 0) ? 1 : 2;   // a boundary face has side 0 only
+		if (ns_f == 1) {
+			if (!mesh->bc_fc || !mesh->bc_state_fc)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "boundary faces need bc_fc and bc_state_fc");
+			const int code = mesh->bc_fc[f] % kBcStepSC;
+			if (code < 0 || (c->pde == DGPU_PDE_EULER ? !bc_is_euler(code) : !bc_is_advection_upwind(code)))
+				return reject(DGPU_ERR_UNSUPPORTED,
+				              "BC code " + std::to_string(mesh->bc_fc[f]) + " is not provided for this pde");
+			if ((code == kBcBackPressure || code == kBcTotalTP) && !mesh->bc_data)
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "back pressure / total TP faces need bc_data");
+			++n_bnd;
+		}
+		for (int s = 0; s < ns_f; ++s) {
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
-			if (v < 0)
-				return reject(DGPU_ERR_UNSUPPORTED, "boundary faces are supported by dgpu_create only");
-			if (v >= nV || lf < 0 || lf >= type_faces(g_type[vg[v]]))
+			if (v < 0 || v >= nV || lf < 0 || lf >= type_faces(g_type[vg[v]]))
 				return reject(DGPU_ERR_INVALID_ARGUMENT, "bad face connectivity");
 			qf = std::max(qf, g_q[vg[v]]);
 		}
 		face_q[f] = qf;
 		int nfc = -1;
-		for (int s = 0; s < 2; ++s) {
+		for (int s = 0; s < ns_f; ++s) {
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s], g = vg[v];
 			const int ord = face_ord ? face_ord[2 * f + s] : 0;
 			int n_s;
@@ -878,12 +895,13 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	fbase[nF] = fb;
 	std::vector<int4> elf((size_t)nV * kMaxLf, int4{-1, -1, -1, 0});
 	for (int f = 0; f < nF; ++f) {
-		if (mesh->nc_fc)
+		const int ns_f = (mesh->face_vol[2 * f + 1] < 0) ? 1 : 2;
+		if (mesh->nc_fc && ns_f == 2)
 			for (int i = 0; i < face_nfc[f]; ++i)
 				if (mesh->nc_fc[caller_fc_off[f] + i] != i)
 					return reject(DGPU_ERR_UNSUPPORTED, "the batched path needs face nodes in one canonical order "
 					                                    "(identity nc_fc); orient dense faces with face_ord");
-		for (int s = 0; s < 2; ++s) {
+		for (int s = 0; s < ns_f; ++s) {
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
 			int4& slot = elf[(size_t)sorted_pos[v] * kMaxLf + lf];
 			if (slot.x != -1)
@@ -933,6 +951,25 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 				fgeo[base + (size_t)k * nff + i] = mesh->normals_fc[(caller_fc_off[f] + i) * d + k];
 			fgeo[base + (size_t)d * nff + i] = wf * mesh->jacobian_det_fc[caller_fc_off[f] + i];
 		}
+	}
+	// boundary faces: code per internal face and the exterior state in the internal face-node layout
+	std::vector<int> fbc;
+	std::vector<double> fext;
+	if (n_bnd > 0) {
+		fbc.assign(nF, -1);
+		fext.assign((size_t)nv * fb, 0.0);
+		for (int f = 0; f < nF; ++f) {
+			if (mesh->face_vol[2 * f + 1] >= 0)
+				continue;
+			const int k = internal_face[f], nff = face_nfc[f];
+			fbc[k] = mesh->bc_fc[f] % kBcStepSC;
+			for (int i = 0; i < nff; ++i)
+				for (int var = 0; var < nv; ++var)
+					fext[(size_t)nv * fbase[k] + (size_t)var * nff + i] =
+						mesh->bc_state_fc[(caller_fc_off[f] + i) * nv + var];
+		}
+		if (mesh->bc_data)
+			c->bc_data = BcData{mesh->bc_data[0], mesh->bc_data[1], mesh->bc_data[2], mesh->bc_data[3]};
 	}
 	// fused tiles: full CTAs per group (TP: 256 / q^d volumes; dense: E_fused)
 	std::vector<BTile> tiles;
@@ -1059,6 +1096,10 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	B_TRY(upload_vec(&c->inv_wJ, inv_wJ));
 	B_TRY(upload_vec(&c->fgeo, fgeo));
 	B_TRY(upload_vec(&c->d_tiles, tiles));
+	if (n_bnd > 0) {
+		B_TRY(upload_vec(&c->d_fbc, fbc));
+		B_TRY(upload_vec(&c->d_fext, fext));
+	}
 	B_TRY(bind(c));
 #undef B_TRY
 	*out = c;

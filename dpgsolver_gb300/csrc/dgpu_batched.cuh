@@ -73,6 +73,10 @@ struct BParams {
 	unsigned long long* max_bits;
 	int* err_flag;
 	unsigned long long* n_corr;
+	// boundary faces (no side-1 volume), all null on a mesh without any:
+	const int* fbc;           // [face]: BC code modulo BC_STEP_SC, -1 on interior faces
+	const double* fext;       // per face: NV NF_f at NV fbase[f]: [NV][NF_f] exterior state at the face nodes
+	BcData bc_data;
 };
 
 // Fused tile list entry: group and first element within the group.
@@ -263,15 +267,31 @@ __device__ __forceinline__ void bface_node_rt(const BParams& P, int f, int i, in
 	const double* tL = P.traces + 2 * NV * fb;
 	const double* tR = tL + NV * nff;
 	double WL[NV], WR[NV], n[D];
-#pragma unroll
-	for (int k = 0; k < NV; ++k) {
-		WL[k] = tL[k * nff + i];
-		WR[k] = tR[k * nff + i];
-	}
 	const double* fg = P.fgeo + (D + 1) * fb;
 #pragma unroll
 	for (int k = 0; k < D; ++k)
 		n[k] = fg[k * nff + i];
+	const int code = P.fbc ? P.fbc[f] : -1;
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+		WL[k] = tL[k * nff + i];
+	if (code < 0) {
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			WR[k] = tR[k * nff + i];
+	} else {
+		// a boundary face: the boundary value of its BC from the interior trace (face_solver_T.c:203-275)
+		const double* ext = P.fext + NV * fb + i;
+		if constexpr (PDE == kEuler) {
+			double e[NV];
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				e[k] = ext[k * nff];
+			euler_boundary_state<D, double>(code, WL, e, n, WR, P.bc_data);
+		} else {
+			WR[0] = advection_boundary_value<D, double>(WL[0], ext[0], n, P.b_adv);
+		}
+	}
 	const double sc = fg[D * nff + i];
 	double* out = P.nnf + NV * fb;
 	if constexpr (PDE == kEuler) {

@@ -61,18 +61,24 @@ class MixedTPProblem:
         self._face_geometry()
         self.sol = np.zeros(int(self.state_off[-1]))
         self.dt = 0.0
+        self.bc = None          # (n_faces,) BC code per face (0 inside) when the mesh has boundary faces
+        self.bc_state = None    # (face nodes, n_var): exterior state at every face node, face blocks in face order
+        self.bc_data = None
 
     # ---- faces at p_f = max(p_L, p_R) ---------------------------------------------------------------------------
     def _face_geometry(self):
         mesh, d = self.mesh, self.d
         qv = np.array([self.groups[g].q for g in self.vol_group], dtype=np.int64)
-        self.face_q = np.maximum(qv[mesh.face_vol[:, 0]], qv[mesh.face_vol[:, 1]]).astype(np.int32)
+        v1 = mesh.face_vol[:, 1]
+        q1 = np.where(v1 >= 0, qv[np.maximum(v1, 0)], 0)          # a boundary face has side 0 only
+        self.face_q = np.maximum(qv[mesh.face_vol[:, 0]], q1).astype(np.int32)
         n_fc = self.face_q.astype(np.int64) ** (d - 1)
         self.face_off = np.zeros(mesh.n_faces + 1, dtype=np.int64)
         self.face_off[1:] = np.cumsum(n_fc)
         nfn = int(self.face_off[-1])
         self.normals_fc = np.empty((nfn, d))
         self.jacobian_det_fc = np.empty(nfn)
+        self.xyz_fc = np.empty((nfn, d))
         pos_in_group = np.empty(mesh.n_volumes, dtype=np.int64)
         for g, vols in enumerate(self.group_vols):
             pos_in_group[vols] = np.arange(len(vols))
@@ -100,6 +106,7 @@ class MixedTPProblem:
                     rows = (self.face_off[sel][:, None] + np.arange(nff)[None, :]).ravel()
                     self.normals_fc[rows] = (nun / nrm[..., None]).reshape(-1, d)
                     self.jacobian_det_fc[rows] = nrm.ravel()
+                    self.xyz_fc[rows] = apply_nodes(I_mf, geom.X_geom[pos_in_group[v0[sel]]]).reshape(-1, d)
 
     # ---- layout helpers -------------------------------------------------------------------------------------------
     @property
@@ -161,7 +168,23 @@ class MixedTPProblem:
             "jacobian_det_fc": np.ascontiguousarray(self.jacobian_det_fc),
             "nc_fc": self.nc_fc(),
             "sol": self.sol,
+            "bc_fc": None if self.bc is None else np.ascontiguousarray(self.bc, dtype=np.int32),
+            "bc_state_fc": None if self.bc_state is None else np.ascontiguousarray(self.bc_state).ravel(),
+            "bc_data": self.bc_data,
         }
+
+    def set_boundaries(self, side_bc: dict, exterior):
+        """BC code per boundary face from {(dim, side): code} and the exterior state exterior(xyz (m, d)) ->
+        (m, n_var) at every face node (the test case's constructor_sol_bv); interior faces get code 0."""
+        mesh = self.mesh
+        self.bc = np.zeros(mesh.n_faces, dtype=np.int32)
+        for f in np.nonzero(mesh.face_vol[:, 1] < 0)[0]:
+            lf = int(mesh.face_lf[f, 0])
+            self.bc[f] = side_bc[(lf // 2, lf % 2)]
+        ext = np.asarray(exterior(self.xyz_fc), dtype=np.float64).reshape(len(self.xyz_fc), self.n_var)
+        inner = np.repeat(mesh.face_vol[:, 1] >= 0, np.diff(self.face_off))
+        ext[inner] = 0.0
+        self.bc_state = np.ascontiguousarray(ext)
 
     def stable_dt(self, cfl: float = 0.1) -> float:
         """dt = cfl * h / ((2 p_max + 1) * max(|V| + c)) over the solution nodes."""
@@ -190,12 +213,14 @@ def _seeded_p(n_volumes, p_set, seed):
 
 def mixed_euler(d: int = 3, n: int = 58, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE, seed: int = 0,
                 curved: bool = False, amplitude: float = 0.03, mach: float = 0.5, perturb: float = 0.05,
-                positivity: bool = True) -> MixedTPProblem:
-    """Periodic unit square/cube, per-volume p drawn uniformly from p_set (seeded), smooth seeded sinusoidal state
+                positivity: bool = True, periodic=True, codes=None) -> MixedTPProblem:
+    """Unit square/cube, per-volume p drawn uniformly from p_set (seeded), smooth seeded sinusoidal state
     around a free stream of Mach `mach`: rho = 1 + perturb * prod sin(2 pi x_k + phi_k), p = 1 + perturb * ...,
-    velocity Mach * c along a fixed oblique direction with perturbations of the same form."""
+    velocity Mach * c along a fixed oblique direction with perturbations of the same form. periodic: per direction
+    (all by default); codes: {(dim, side): BC code} for the ends of the other directions, whose exterior state is
+    the unperturbed free stream."""
     L = 1.0
-    mesh = StructuredMesh(d, n, 0.0, L)
+    mesh = StructuredMesh(d, n, 0.0, L, periodic=periodic)
     deform = None
     if curved:
         deform = sinusoidal_deform_2d(amplitude, L) if d == 2 else sinusoidal_deform_3d(amplitude, L)
@@ -223,6 +248,14 @@ def mixed_euler(d: int = 3, n: int = 58, p_set=(1, 2, 3, 4), num_flux: int = NUM
         prob.set_group(prob.sol, g, np.transpose(U, (1, 0, 2)))
     prob.dt = prob.stable_dt()
     prob.meta.update(n=n, p_set=tuple(p_set), seed=seed, curved=curved)
+    if np.any(mesh.face_vol[:, 1] < 0):
+        vel0 = mach * c0 * dirn
+
+        def stream(x):
+            U = primitive_to_conserved(d, np.ones(len(x)), np.broadcast_to(vel0[:, None], (d, len(x))),
+                                       np.ones(len(x)))
+            return U.T
+        prob.set_boundaries(codes, stream)
     return prob
 
 

@@ -347,6 +347,11 @@ class BatchSimulation:
         m.nc_fc = _ip(arr(fl["nc_fc"], np.int32))
         m.normals_fc = _dp(arr(fl["normals_fc"]))
         m.jacobian_det_fc = _dp(arr(fl["jacobian_det_fc"]))
+        if fl.get("bc_fc") is not None:
+            m.bc_fc = _ip(arr(fl["bc_fc"], np.int32))
+            m.bc_state_fc = _dp(arr(fl["bc_state_fc"]))
+            if fl.get("bc_data") is not None:
+                m.bc_data = _dp(arr(np.asarray(fl["bc_data"], dtype=np.float64).reshape(4)))
         vg = arr(fl["vol_group"], np.int32)
         h = ctypes.c_void_p()
         if dense or fl.get("face_ord") is not None:

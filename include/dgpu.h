@@ -122,7 +122,8 @@ typedef struct {
 	 *   upwind inflow boundaries; on BC_NOSLIP_ALL_ROTATING faces the wall state (rho_b, rho_b u_wall, E_b) with
 	 *   the wall's velocity at the node (compute_uvw_ex_rotating: omega about the z axis); read on boundary
 	 *   faces only.
-	 * dgpu_create only: the no-allocation entry and the batched context return DGPU_ERR_UNSUPPORTED. */
+	 * dgpu_create and the batched context (Euler and advection codes; there the boundary face's nodes are those of
+	 *   its side-0 volume's order); the no-allocation entry returns DGPU_ERR_UNSUPPORTED. */
 	const int* bc_fc;
 	const double* bc_state_fc;
 	/* bc_data: 4 doubles {p_back, t_total, p_total, r_s}, the reference's BC_Data (boundary_euler_T.c:44-49, read
@@ -310,9 +311,10 @@ const char* dgpu_status_string(dgpu_status st);
  *   ops[g]            the TP operator set of group g (distinct p per group)
  *   vol_group[v]      group of volume v
  *   mesh              as for dgpu_create with ragged blocks: volume v holds n_vc(v) = q(v)^d nodes, face f
- *                     holds n_fc(f) = q_f^(d-1) nodes with q_f = max(q(L), q(R)); every array concatenates the
- *                     blocks in list order. nc_fc must be NULL or the identity (aligned faces); periodic meshes
- *                     only (no boundary faces).
+ *                     holds n_fc(f) = q_f^(d-1) nodes with q_f = max(q(L), q(R)) (q(L) on a boundary face);
+ *                     every array concatenates the blocks in list order. nc_fc must be NULL or the identity
+ *                     (aligned faces). Boundary faces take bc_fc / bc_state_fc / bc_data as for dgpu_create
+ *                     (Euler: BC_RIEMANN .. BC_SUPERSONIC_OUT; advection: the upwind codes).
  *
  * The state is the volumes' (n_vs(v) x n_var) column-major sol_coef blocks concatenated in volume-list order.
  * On the device the volumes are stored group by group; uploads and downloads permute. Each RK stage runs in one

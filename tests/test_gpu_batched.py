@@ -74,6 +74,55 @@ def test_rk3_steps_match_oracle(gpu_lib, name, n_steps, form):
     assert abs(mx - mx_ref) <= 1e-10 * mx_ref
 
 
+# boundary faces (the reference's BCs on the ends of the non-periodic directions, exterior = the free stream)
+BC_CASES = {
+    "hex_roe_wall_riemann_4": lambda: M.mixed_euler(3, 4, seed=1, perturb=0.3, periodic=(True, False, True),
+                                                    codes={(1, 0): 10102, (1, 1): 10101}),
+    "hex_lf_supersonic_curved_3": lambda: M.mixed_euler(3, 3, seed=2, curved=True, perturb=0.3,
+                                                        num_flux=P.NUM_FLUX_LAX_FRIEDRICHS,
+                                                        periodic=(False, True, True),
+                                                        codes={(0, 0): 10105, (0, 1): 10106}),
+    "quad_roe_box_8": lambda: M.mixed_euler(2, 8, seed=3, perturb=0.3, periodic=False,
+                                            codes={(0, 0): 10101, (0, 1): 10101, (1, 0): 10102, (1, 1): 10102}),
+}
+
+
+@pytest.mark.parametrize("name", sorted(BC_CASES))
+@pytest.mark.parametrize("form", FORMS)
+def test_boundaries_match_oracle(gpu_lib, name, form):
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = BC_CASES[name]()
+    ref = oracle.Oracle(prob)
+    r_ref, mx_ref = ref.compute_rhs(prob.sol)
+    s_ref = prob.sol.copy()
+    for _ in range(2):
+        s_ref, _, _ = ref.ssp_rk3_step(s_ref, prob.dt)
+    with BatchSimulation(prob) as sim:
+        sim.form = form
+        mx = sim.compute_rhs()
+        r = sim.rhs
+        sim.ssp_rk3_steps(prob.dt, 2)
+        s = sim.sol_coef
+    assert rel_err(r, r_ref) <= TOL
+    assert abs(mx - mx_ref) <= TOL * mx_ref
+    assert rel_err(s, s_ref) <= TOL
+
+
+def test_boundaries_keep_the_free_stream(gpu_lib):
+    from dpgsolver_gb300.solver import BatchSimulation
+    for name in ("hex_roe_wall_riemann_4", "quad_roe_box_8"):
+        prob = BC_CASES[name]()
+        d = prob.d
+        vel = 0.5 * np.sqrt(P.GAMMA) * np.array([1.0, 0.5, 0.25][:d]) / np.linalg.norm([1.0, 0.5, 0.25][:d])
+        vel[1] = 0.0     # no flow through the slip walls (y = const)
+        U = P.primitive_to_conserved(d, np.ones(1), vel[:, None], np.ones(1))[:, 0]
+        s = np.concatenate([np.repeat(U, n) for n in prob.n_vs])
+        prob.bc_state[:] = U
+        with BatchSimulation(prob) as sim:
+            sim.upload_state(s)
+            assert sim.compute_rhs() < 1e-11
+
+
 def test_ill_conditioned_case_within_rounding_noise(gpu_lib):
     """With small volumes and a small perturbation of the free stream, the residual is a small difference of
     large flux terms: h = 0.1 and 5 % perturbations make max|R| about 30 p^2 times smaller than the terms. Rounding

@@ -146,12 +146,16 @@ def test_bc_create_errors(gpu_lib):
     assert abs(mx - mx_ref) <= TOL * mx_ref
 
 
-def test_bc_refused_by_batched_and_noalloc(gpu_lib):
+def test_bc_in_batched_context_and_refused_by_noalloc(gpu_lib):
+    """The batched context takes boundary faces (a uniform mesh as one group matches the oracle); the
+    no-allocation entry refuses them."""
     from dpgsolver_gb300.solver import BatchSimulation
     prob = P.euler_channel_2d(4, 2)
-    with pytest.raises(_lib.DGPUError) as e:
-        BatchSimulation(prob)
-    assert e.value.status == 2
+    r_ref, _ = oracle.Oracle(prob).compute_rhs(prob.sol)
+    with BatchSimulation(prob) as sim:
+        sim.compute_rhs()
+        r = sim.rhs
+    assert np.max(np.abs(np.reshape(r, r_ref.shape) - r_ref)) <= TOL * np.max(np.abs(r_ref))
     phys = _lib.Physics()
     phys.d, phys.pde, phys.num_flux = 2, prob.pde, prob.num_flux
     tp = _lib.TPOperators()
