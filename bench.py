@@ -165,6 +165,26 @@ def flops_per_element(d, q, nv, flux, coef_io):
     return total
 
 
+# FP64 thread-instructions (DFMA + DMUL + DADD) per element of one RK stage, from ncu
+# (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on of the volume, face and lift kernels on the 24^3 case,
+# profiles/tp_rk3_stage_hex24_p3_lf_full.md): 8.84 k + 5.67 k + 2.94 k.
+FP64_INSTR_PER_ELEMENT = {(3, 3, "lf"): 17450}
+
+
+def fp64_issue(prob, w, stage_ms, peak_tflops):
+    """Fraction of the FP64 pipe's issue slots the live stage uses: every FP64 instruction (a division or square root
+    is several) against 2 per cycle per SM, i.e. the DFMA probe's rate / 2. Known for the workloads ncu counted."""
+    from dpgsolver_gb300.host import problem as P
+    key = (prob.d, prob.ops.p, "lf" if prob.num_flux == P.NUM_FLUX_LAX_FRIEDRICHS else "roe")
+    n = FP64_INSTR_PER_ELEMENT.get(key)
+    if n is None:
+        return {}
+    rate = n * prob.n_volumes / (stage_ms * 1e-3)
+    return {"instr_per_element": n, "issue_frac": rate / (peak_tflops * 1e12 / 2.0),
+            "issue_source": "ncu FP64 instruction counts per element (profiles/tp_rk3_stage_hex24_p3_lf_full.md) x "
+                            "elements / live stage time, against the DFMA probe's instruction rate"}
+
+
 def algorithmic_bytes(prob, kernel):
     """Compulsory DRAM bytes of one launch of `kernel` (each array read or written once)."""
     d, q, nv = prob.d, prob.ops.q, prob.n_var
@@ -381,6 +401,7 @@ def run_ours(args, rank, world, local_rank):
                       "peak_tflops": fp64_peak.value, "peak_source": "measured (dgpu_probe_fp64 DFMA loop)",
                       "frac": stage_flops / (stage_ms * 1e-3) / 1e12 / fp64_peak.value,
                       "flops_per_stage": stage_flops,
+                      **fp64_issue(prob, w, stage_ms, fp64_peak.value),
                       "dmma_tflops": mma_peak.value,
                       "dmma_source": "measured (dgpu_probe_fp64_mma: mma.sync m8n8k4 f64 loop)",
                       "note": "binding roof: FP64 issue rate, not HBM; the FP64 tensor cores (dmma_tflops) run at "
