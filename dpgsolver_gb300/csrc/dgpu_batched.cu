@@ -545,7 +545,10 @@ void set_group_E(dgpu_batch* c, int g, int E)
 		c->hgroups[c->gl[g].idx].E = E;
 }
 
-int type_faces(int t) { return t == DGPU_TET ? 4 : (t == DGPU_HEX ? 6 : (t == DGPU_QUAD ? 4 : 5)); }
+int type_faces(int t)
+{
+	return t == DGPU_TRI ? 3 : (t == DGPU_TET ? 4 : (t == DGPU_HEX ? 6 : (t == DGPU_QUAD ? 4 : 5)));
+}
 
 // ---- creation ----
 struct GroupIn {
@@ -665,8 +668,9 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 			const dgpu_dense_operators* op = in.dn;
 			if (!op)
 				return reject(DGPU_ERR_INVALID_ARGUMENT, "NULL operator set");
-			if (d != 3 || (op->elem_type != DGPU_TET && op->elem_type != DGPU_WEDGE && op->elem_type != DGPU_PYR))
-				return reject(DGPU_ERR_UNSUPPORTED, "dense groups must be TET, WEDGE or PYR (d = 3)");
+			if (d == 2 ? op->elem_type != DGPU_TRI
+			           : (op->elem_type != DGPU_TET && op->elem_type != DGPU_WEDGE && op->elem_type != DGPU_PYR))
+				return reject(DGPU_ERR_UNSUPPORTED, "dense groups must be TRI (d = 2) or TET, WEDGE, PYR (d = 3)");
 			if (op->p < 1 || op->p > kQMax - 1 || op->n_vs < 1 || op->n_vc < 1 || op->n_vs > 1024 ||
 			    op->n_vc > 4096 || op->n_lf != type_faces(op->elem_type) || op->n_ord < 1 || op->n_ord > kMaxOrd ||
 			    !op->cv0_vs_vc || !op->cv1_vs_vc || !op->w_vc || !op->n_fc || !op->cv0_vs_fc || !op->w_fc)

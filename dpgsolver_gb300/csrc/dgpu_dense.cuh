@@ -361,10 +361,8 @@ __global__ void __launch_bounds__(256) bvol_fused_kernel(const BParams P, const 
 	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
 		const BTile tl = tiles[t];
 		if (tl.group >= P.n_groups) {
-			if constexpr (D == 3) {
-				const DGroup G = P.dgroups[tl.group - P.n_groups];
-				dvol_body<D, NV, PDE>(P, G, tl.e0, G.E_fused, u, base);
-			}
+			const DGroup G = P.dgroups[tl.group - P.n_groups];
+			dvol_body<D, NV, PDE>(P, G, tl.e0, G.E_fused, u, base);
 			continue;
 		}
 		if (tl.group != cur) {

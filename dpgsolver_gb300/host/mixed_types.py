@@ -27,7 +27,7 @@ import math
 
 import numpy as np
 
-from .element import HEX, PYR, QUAD, TET, TRI, WEDGE, TPOperatorSet
+from .element import HEX, LINE, PYR, QUAD, TET, TRI, WEDGE, TPOperatorSet
 from .problem import (GAMMA, GM1, NUM_FLUX_LAX_FRIEDRICHS, NUM_FLUX_ROE_PIKE, PDE_EULER,
                       primitive_to_conserved)
 from . import simplex as S
@@ -188,12 +188,13 @@ class MixedTypeMesh:
         self.n_faces = len(fv)
         self.face_ord = np.zeros((self.n_faces, 2), dtype=np.int32)
         self.face_canon = np.zeros(self.n_faces, dtype=np.int32)    # side whose local order is canonical
+        tp = getattr(self, "tp_type", HEX)
         for f in range(self.n_faces):
             vs = self.face_vol[f]
-            cs = 1 if (self.types[vs[1]] == HEX and self.types[vs[0]] != HEX) else 0
+            cs = 1 if (self.types[vs[1]] == tp and self.types[vs[0]] != tp) else 0
             self.face_canon[f] = cs
             canon = [self.gids[vs[cs]][m] for m in S.F_VE[self.types[vs[cs]]][self.face_lf[f, cs]]]
-            ft = S.TRI if len(canon) == 3 else S.QUAD
+            ft = {2: LINE, 3: S.TRI, 4: S.QUAD}[len(canon)]
             for s in range(2):
                 loc = [self.gids[vs[s]][m] for m in S.F_VE[self.types[vs[s]]][self.face_lf[f, s]]]
                 perm = tuple(loc.index(g) for g in canon)
@@ -206,7 +207,56 @@ class MixedTypeMesh:
         return {int(t): int(np.sum(self.types == t)) for t in (HEX, TET, WEDGE, PYR)}
 
 
-_AFF_SUB = {TET: [0, 1, 2, 3], WEDGE: [0, 1, 2, 3], PYR: [0, 1, 2, 4], HEX: [0, 1, 2, 4]}
+_AFF_SUB = {TET: [0, 1, 2, 3], WEDGE: [0, 1, 2, 3], PYR: [0, 1, 2, 4], HEX: [0, 1, 2, 4], TRI: [0, 1, 2],
+            QUAD: [0, 1, 2]}
+
+
+class MixedTriQuadMesh(MixedTypeMesh):
+    """The 2D counterpart: the periodic unit square in n^2 cells, each (seeded, probability p_tri) one QUAD or two
+    TRIs split along the diagonal (0,0)-(1,1) of the cell, both counter-clockwise. Conforming by construction; faces
+    (edges) follow the same rule as the 3D mesh: the QUAD's own order when a QUAD is on the face, else side 0's,
+    and face_ord indexes simplex.LINE_ORDS."""
+
+    tp_type = QUAD
+
+    def __init__(self, n: int, seed: int = 0, p_tri: float = 0.5):
+        if n < 2:
+            raise ValueError("n >= 2")
+        self.d, self.n = 2, n
+        self.h = 1.0 / n
+        rng = np.random.default_rng(seed)
+        types, gids, X = [], [], []
+
+        def vid(i, j):
+            return (i % n) + n * (j % n)
+        for j in range(n):
+            for i in range(n):
+                c = [(i, j), (i + 1, j), (i, j + 1), (i + 1, j + 1)]     # TP corner order
+                if rng.random() < p_tri:
+                    for tri in ((0, 1, 3), (0, 3, 2)):
+                        types.append(TRI)
+                        gids.append([vid(*c[m]) for m in tri])
+                        X.append([c[m] for m in tri])
+                else:
+                    types.append(QUAD)
+                    gids.append([vid(*cc) for cc in c])
+                    X.append(c)
+        self.types = np.array(types, dtype=np.int32)
+        self.n_volumes = len(types)
+        self.gids = gids
+        self.A = np.empty((self.n_volumes, 2, 2))
+        self.b = np.empty((self.n_volumes, 2))
+        self.X = [np.asarray(x, dtype=np.float64) * self.h for x in X]
+        for t in (QUAD, TRI):
+            sel = np.nonzero(self.types == t)[0]
+            if len(sel) == 0:
+                continue
+            A, b0 = _affine_batch(t, np.array([self.X[v] for v in sel]))
+            self.A[sel], self.b[sel] = A, b0
+        self._faces()
+
+    def counts(self):
+        return {int(t): int(np.sum(self.types == t)) for t in (QUAD, TRI)}
 
 
 def _affine_batch(t, X):
@@ -240,17 +290,18 @@ class MixedTypeProblem:
 
     def __init__(self, mesh: MixedTypeMesh, p_vol, pde=PDE_EULER, num_flux=NUM_FLUX_ROE_PIKE):
         self.mesh = mesh
-        self.d = 3
+        self.d = d = getattr(mesh, "d", 3)
+        tp = QUAD if d == 2 else HEX
         self.pde = pde
         self.num_flux = num_flux
         self.positivity = False
         self.b_adv = np.zeros(3)
-        self.n_var = 5
+        self.n_var = d + 2
         self.name = "mixed_types"
         self.meta = {}
         p_vol = np.asarray(p_vol, dtype=np.int32)
-        keys = sorted(set((int(t), int(p)) for t, p in zip(mesh.types, p_vol)), key=lambda k: (k[0] != HEX, k))
-        self.groups = [TPOperatorSet(HEX, p) if t == HEX else S.DenseOperatorSet(t, p) for t, p in keys]
+        keys = sorted(set((int(t), int(p)) for t, p in zip(mesh.types, p_vol)), key=lambda k: (k[0] != tp, k))
+        self.groups = [TPOperatorSet(tp, p) if t == tp else S.DenseOperatorSet(t, p) for t, p in keys]
         self.group_key = keys
         gidx = {k: g for g, k in enumerate(keys)}
         self.vol_group = np.array([gidx[(int(t), int(p))] for t, p in zip(mesh.types, p_vol)], dtype=np.int32)
@@ -267,11 +318,11 @@ class MixedTypeProblem:
         if np.any(self.J <= 0.0):
             raise AssertionError("non-positive Jacobian")
         self.m = self.J[:, None, None] * np.transpose(np.linalg.inv(self.A), (0, 2, 1))
-        # faces at p_f = max(p_L, p_R): q_f^2 nodes on triangles (collapsed rule) and quads (GL)
+        # faces at p_f = max(p_L, p_R): q_f^2 nodes on triangles (collapsed rule) and quads (GL), q_f on lines
         q = p_vol.astype(np.int64) + 1
         self.face_q = np.maximum(q[mesh.face_vol[:, 0]], q[mesh.face_vol[:, 1]]).astype(np.int32)
         self.face_off = np.zeros(mesh.n_faces + 1, dtype=np.int64)
-        self.face_off[1:] = np.cumsum(self.face_q.astype(np.int64) ** 2)
+        self.face_off[1:] = np.cumsum(self.face_q.astype(np.int64) ** (d - 1))
         self._face_geometry()
         self.sol = np.zeros(int(self.state_off[-1]))
         self.dt = 0.0
@@ -279,15 +330,18 @@ class MixedTypeProblem:
     def _face_geometry(self):
         """Normals and J_f of the side-0 volume (constant on affine faces) and the side-0 face-rule weights, at the
         canonical nodes of every face."""
-        mesh = self.mesh
+        mesh, d = self.mesh, self.d
         v0, lf0 = mesh.face_vol[:, 0], mesh.face_lf[:, 0]
-        nref = np.zeros((mesh.n_faces, 3))
+        nref = np.zeros((mesh.n_faces, d))
         ftype = np.zeros(mesh.n_faces, dtype=np.int32)
-        for t in (HEX, TET, WEDGE, PYR):
+        for t in ((QUAD, TRI) if d == 2 else (HEX, TET, WEDGE, PYR)):
             sel = np.nonzero(mesh.types[v0] == t)[0]
             if len(sel) == 0:
                 continue
-            nr = S.reference_normals_3d(t) if t != HEX else TPOperatorSet(HEX, 1).normals_ref
+            if t in (HEX, QUAD):
+                nr = TPOperatorSet(t, 1).normals_ref
+            else:
+                nr = S.reference_normals_2d(t) if d == 2 else S.reference_normals_3d(t)
             nref[sel] = nr[lf0[sel]]
             ftype[sel] = np.array([len(fv) for fv in S.F_VE[t]])[lf0[sel]]
         nun = np.einsum("fij,fj->fi", self.m[v0], nref)
@@ -296,7 +350,7 @@ class MixedTypeProblem:
         self.normals_fc = np.repeat(nun / jn[:, None], nfc, axis=0)
         self.jacobian_det_fc = np.repeat(jn, nfc)
         self.w_fc = np.empty(int(self.face_off[-1]))
-        for nvert, ft in ((3, S.TRI), (4, S.QUAD)):
+        for nvert, ft in ((2, LINE), (3, S.TRI), (4, S.QUAD)):
             for qf in np.unique(self.face_q):
                 sel = np.nonzero((ftype == nvert) & (self.face_q == qf))[0]
                 if len(sel) == 0:
@@ -330,14 +384,14 @@ class MixedTypeProblem:
         state[idx] = np.asarray(blocks).reshape(len(vols), n)
 
     def vc_xyz(self, g):
-        """Physical coordinates of group g's volume cubature nodes (n_vols_g, n_vc, 3)."""
+        """Physical coordinates of group g's volume cubature nodes (n_vols_g, n_vc, d)."""
         ops = self.groups[g]
         vols = self.group_vols[g]
         if getattr(ops, "dense", False):
             xr = ops.x_vc
         else:
             from .element import tp_nodes
-            xr = tp_nodes(ops.x_vc, 3)
+            xr = tp_nodes(ops.x_vc, self.d)
         return np.einsum("vij,nj->vni", self.A[vols], xr) + self.b[vols][:, None, :]
 
     def nc_fc(self) -> np.ndarray:
@@ -347,15 +401,16 @@ class MixedTypeProblem:
         n_vc = np.array([self.groups[g].n_vc for g in self.vol_group], dtype=np.int64)
         vc_off = np.zeros(len(n_vc) + 1, dtype=np.int64)
         vc_off[1:] = np.cumsum(n_vc)
-        mflat = np.empty(int(vc_off[-1]) * 9)
+        dd = self.d * self.d
+        mflat = np.empty(int(vc_off[-1]) * dd)
         jflat = np.empty(int(vc_off[-1]))
         for g, vols in enumerate(self.group_vols):
             if len(vols) == 0:
                 continue
             nq = self.groups[g].n_vc
-            mt = np.transpose(self.m[vols], (0, 2, 1)).reshape(len(vols), 9)      # [j][i] per volume
-            blk = np.repeat(mt[:, :, None], nq, axis=2).reshape(len(vols), 9 * nq)
-            idx = (9 * vc_off[vols])[:, None] + np.arange(9 * nq)[None, :]
+            mt = np.transpose(self.m[vols], (0, 2, 1)).reshape(len(vols), dd)     # [j][i] per volume
+            blk = np.repeat(mt[:, :, None], nq, axis=2).reshape(len(vols), dd * nq)
+            idx = (dd * vc_off[vols])[:, None] + np.arange(dd * nq)[None, :]
             mflat[idx] = blk
             jidx = vc_off[vols][:, None] + np.arange(nq)[None, :]
             jflat[jidx] = np.repeat(self.J[vols][:, None], nq, axis=1)
@@ -383,14 +438,14 @@ class MixedTypeProblem:
                 continue
             if getattr(ops, "dense", False):
                 x = self.vc_xyz(g)
-                U = fn(x.reshape(-1, 3)).reshape(len(vols), ops.n_vc, self.n_var)
+                U = fn(x.reshape(-1, self.d)).reshape(len(vols), ops.n_vc, self.n_var)
                 # orthonormal basis, affine volume: coef = M_ref^-1 cv0^T diag(w) U
                 Pm = np.linalg.inv(ops.mass()) @ (ops.cv0_vs_vc().T * ops.w_vc[None, :])   # (n_vs, n_vc)
                 coef = np.transpose(U, (0, 2, 1)) @ Pm.T                                   # (v, k, a)
             else:
-                xs = tp_nodes(ops.x_vs, 3)
+                xs = tp_nodes(ops.x_vs, self.d)
                 x = np.einsum("vij,nj->vni", self.A[vols], xs) + self.b[vols][:, None, :]
-                coef = np.transpose(fn(x.reshape(-1, 3)).reshape(len(vols), ops.n_vs, self.n_var), (0, 2, 1))
+                coef = np.transpose(fn(x.reshape(-1, self.d)).reshape(len(vols), ops.n_vs, self.n_var), (0, 2, 1))
             self.set_group(self.sol, g, coef)
 
     def stable_dt(self, cfl: float = 0.1, lam: float = 1.0) -> float:
@@ -423,6 +478,34 @@ def mixed_types_euler(n: int = 12, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: 
         pr = 1.0 + perturb * wave(1)
         vel = np.stack([mach * c0 * dirn[j] * (1.0 + perturb * wave(2 + j)) for j in range(3)])
         return primitive_to_conserved(3, rho, vel, pr).T
+
+    prob.project(state)
+    lam = mach * c0 * (1.0 + perturb) + c0 * math.sqrt((1.0 + perturb) / (1.0 - perturb))
+    prob.dt = prob.stable_dt(lam=lam)
+    prob.meta.update(n=n, seed=seed, p_set=tuple(p_set), counts=mesh.counts())
+    return prob
+
+
+def mixed_tri_quad_euler(n: int = 16, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE,
+                         mach: float = 0.5, perturb: float = 0.3, p_tri: float = 0.5) -> MixedTypeProblem:
+    """Mixed QUAD/TRI mesh of the periodic unit square (n^2 cells, MixedTriQuadMesh), p uniform in p_set per volume
+    (seeded), Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed_types_euler)."""
+    mesh = MixedTriQuadMesh(n, seed=seed, p_tri=p_tri)
+    rng = np.random.default_rng(seed + 17)
+    p_vol = rng.choice(np.asarray(p_set, dtype=np.int32), size=mesh.n_volumes)
+    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux)
+    rng2 = np.random.default_rng(seed + 1)
+    ph = rng2.uniform(0.0, 2.0 * math.pi, size=(4, 2))
+    c0 = math.sqrt(GAMMA)
+    dirn = np.array([1.0, 0.5]) / math.sqrt(1.25)
+
+    def state(x):
+        def wave(k):
+            return np.sin(2.0 * math.pi * x[:, 0] + ph[k, 0]) * np.sin(2.0 * math.pi * x[:, 1] + ph[k, 1])
+        rho = 1.0 + perturb * wave(0)
+        pr = 1.0 + perturb * wave(1)
+        vel = np.stack([mach * c0 * dirn[j] * (1.0 + perturb * wave(2 + j)) for j in range(2)])
+        return primitive_to_conserved(2, rho, vel, pr).T
 
     prob.project(state)
     lam = mach * c0 * (1.0 + perturb) + c0 * math.sqrt((1.0 + perturb) / (1.0 - perturb))

@@ -36,7 +36,7 @@ import math
 
 import numpy as np
 
-from .element import HEX, PYR, QUAD, TET, TRI, WEDGE, gauss_legendre
+from .element import HEX, LINE, PYR, QUAD, TET, TRI, WEDGE, gauss_legendre
 
 SQ2, SQ3, SQ6 = math.sqrt(2.0), math.sqrt(3.0), math.sqrt(6.0)
 
@@ -51,6 +51,8 @@ VERTS = {
     PYR: np.array([[-1.0, -1.0, -SQ2 / 5.0], [1.0, -1.0, -SQ2 / 5.0], [-1.0, 1.0, -SQ2 / 5.0],
                    [1.0, 1.0, -SQ2 / 5.0], [0.0, 0.0, 4.0 * SQ2 / 5.0]]),
     HEX: np.array([[x, y, z] for z in (-1.0, 1.0) for y in (-1.0, 1.0) for x in (-1.0, 1.0)]),
+    TRI: TRI_VERTS,
+    QUAD: QUAD_VERTS,
 }
 
 F_VE = {
@@ -58,6 +60,8 @@ F_VE = {
     WEDGE: [[1, 2, 4, 5], [0, 2, 3, 5], [0, 1, 3, 4], [0, 1, 2], [3, 4, 5]],
     PYR: [[0, 2, 4], [1, 3, 4], [0, 1, 4], [2, 3, 4], [0, 1, 2, 3]],
     HEX: [[0, 2, 4, 6], [1, 3, 5, 7], [0, 1, 4, 5], [2, 3, 6, 7], [0, 1, 2, 3], [4, 5, 6, 7]],
+    TRI: [[1, 2], [0, 2], [0, 1]],
+    QUAD: [[0, 2], [1, 3], [0, 1], [2, 3]],
 }
 
 # face orientations: vertex permutations perm with canonical face vertex m <-> local face vertex perm[m]
@@ -79,14 +83,24 @@ def _quad_ords():
 
 
 QUAD_ORDS = _quad_ords()          # QUAD_ORDS[0] is the identity
+LINE_ORDS = [(0, 1), (1, 0)]      # the faces of 2D volumes: as is, reversed
 
 
 def face_type(e_type: int, lf: int) -> int:
-    return TRI if len(F_VE[e_type][lf]) == 3 else QUAD
+    nv = len(F_VE[e_type][lf])
+    return LINE if nv == 2 else (TRI if nv == 3 else QUAD)
 
 
 def face_ords(ftype: int):
-    return TRI_ORDS if ftype == TRI else QUAD_ORDS
+    return LINE_ORDS if ftype == LINE else (TRI_ORDS if ftype == TRI else QUAD_ORDS)
+
+
+def reference_normals_2d(e_type: int) -> np.ndarray:
+    """Outward unit normals of the reference TRI per local face, in the angle form of element.c (pi/6, 5 pi/6,
+    3 pi/2)."""
+    if e_type != TRI:
+        raise ValueError("TRI")
+    return np.array([[math.cos(t), math.sin(t)] for t in (math.pi / 6.0, 5.0 * math.pi / 6.0, 1.5 * math.pi)])
 
 
 def reference_normals_3d(e_type: int) -> np.ndarray:
@@ -208,7 +222,11 @@ def face_rule(ftype: int, q: int):
     """Cached (nodes, weights) of the face reference element (read-only arrays)."""
     key = (ftype, q)
     if key not in _FACE_RULES:
-        x, w = tri_rule(q) if ftype == TRI else quad_rule(q)
+        if ftype == LINE:
+            x1, w = gauss_legendre(q)
+            x = x1[:, None].copy()
+        else:
+            x, w = tri_rule(q) if ftype == TRI else quad_rule(q)
         x.setflags(write=False)
         w.setflags(write=False)
         _FACE_RULES[key] = (x, w)
@@ -216,7 +234,9 @@ def face_rule(ftype: int, q: int):
 
 
 def volume_rule(e_type: int, q: int):
-    """Nodes (n, 3) and weights on the reference element, exact to degree 2q-1 (conical products)."""
+    """Nodes (n, d) and weights on the reference element, exact to degree 2q-1 (conical products)."""
+    if e_type == TRI:
+        return tri_rule(q)
     if e_type == TET:
         xa, wa = gauss_legendre(q)
         xb, wb = gauss_jacobi(q, 1.0)
@@ -268,6 +288,8 @@ def _raw_basis(e_type: int, p: int, x: np.ndarray):
     """Unnormalised spanning functions of the solution space at points x (n, 3): values (n, m), gradients
     (3, n, m)."""
     cols, grads = [], []
+    if e_type == TRI:
+        return _raw_tri(p, x)
     if e_type == TET:
         for tot in range(p + 1):
             for a in range(tot, -1, -1):
@@ -336,6 +358,8 @@ def _orthonormaliser(V: np.ndarray, w: np.ndarray) -> np.ndarray:
 
 
 def n_basis(e_type: int, p: int) -> int:
+    if e_type == TRI:
+        return (p + 1) * (p + 2) // 2
     if e_type == TET:
         return (p + 1) * (p + 2) * (p + 3) // 6
     if e_type == WEDGE:
@@ -354,16 +378,16 @@ class DenseOperatorSet:
     dense = True
 
     def __init__(self, e_type: int, p: int):
-        if e_type not in (TET, WEDGE, PYR):
-            raise ValueError("TET, WEDGE or PYR")
+        if e_type not in (TRI, TET, WEDGE, PYR):
+            raise ValueError("TRI, TET, WEDGE or PYR")
         if not 1 <= p <= 4:
             raise ValueError("p in 1..4")
-        self.e_type, self.p, self.d, self.q = e_type, p, 3, p + 1
+        self.e_type, self.p, self.d, self.q = e_type, p, (2 if e_type == TRI else 3), p + 1
         self.n_vs = n_basis(e_type, p)
         self.x_vc, self.w_vc = volume_rule(e_type, p + 1)
         self.n_vc = len(self.w_vc)
         self.n_lf = len(F_VE[e_type])
-        self.normals_ref = reference_normals_3d(e_type)
+        self.normals_ref = reference_normals_2d(e_type) if e_type == TRI else reference_normals_3d(e_type)
         if e_type == WEDGE:
             # the product of an orthonormal TRI basis and the normalised Legendre polynomials, so that every
             # volume operator is a Kronecker product (prism_factors)
@@ -386,7 +410,7 @@ class DenseOperatorSet:
 
     def basis(self, x):
         V, G = _raw_basis(self.e_type, self.p, np.asarray(x, dtype=np.float64))
-        return V @ self._C, np.stack([G[k] @ self._C for k in range(3)])
+        return V @ self._C, np.stack([G[k] @ self._C for k in range(self.d)])
 
     def prism_factors(self):
         """WEDGE only: (tri_cv0 (n_tvc x n_tvs), tri_cv1 (2 x n_tvc x n_tvs), line_cv0, line_cv1 (q x q)) with
@@ -440,7 +464,10 @@ class DenseOperatorSet:
 
 def face_shape(ftype: int, xi: np.ndarray) -> np.ndarray:
     """(n, n_vertices) shape functions of the face reference element at xi: barycentric coordinates on the TRI,
-    bilinear in tensor vertex order on the QUAD."""
+    bilinear in tensor vertex order on the QUAD, linear on the LINE."""
+    if ftype == LINE:
+        t = xi[:, 0]
+        return np.stack([0.5 * (1.0 - t), 0.5 * (1.0 + t)], axis=1)
     if ftype == TRI:
         T = np.vstack([TRI_VERTS.T, np.ones(3)])
         lam = np.linalg.solve(T, np.vstack([xi.T, np.ones(len(xi))]))

@@ -387,7 +387,7 @@ class BatchSimulation:
         n_ord = 8
         D.elem_type, D.p, D.n_vs, D.n_vc = ops.e_type, ops.p, ops.n_vs, ops.n_vc
         D.cv0_vs_vc = _dp(arr(ops.cv0_vs_vc()))
-        D.cv1_vs_vc = _dp(arr(np.stack([ops.cv1_vs_vc(k) for k in range(3)])))
+        D.cv1_vs_vc = _dp(arr(np.stack([ops.cv1_vs_vc(k) for k in range(ops.d)])))
         D.w_vc = _dp(arr(ops.w_vc))
         D.n_lf, D.n_ord = ops.n_lf, n_ord
         n_fc = np.zeros(ops.n_lf * n_ord * 5, dtype=np.int32)

@@ -50,6 +50,7 @@ typedef int dgpu_status;
 #define DGPU_NUM_FLUX_UPWIND          11
 #define DGPU_NUM_FLUX_ROE_PIKE        31
 #define DGPU_NUM_FLUX_LAX_FRIEDRICHS  32
+#define DGPU_TRI   2
 #define DGPU_QUAD  3
 #define DGPU_TET   4
 #define DGPU_HEX   5
@@ -337,11 +338,11 @@ dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu
  *   n_fc     [(lf * n_ord + ord) * 5 + p_f]   its number of face nodes (both sides of a face must agree);
  *   w_fc     [lf * 5 + p_f]                   the face cubature weights at the canonical nodes. */
 typedef struct {
-	int elem_type;                    /* DGPU_TET, DGPU_WEDGE or DGPU_PYR                         */
+	int elem_type;                    /* DGPU_TRI (d = 2), DGPU_TET, DGPU_WEDGE or DGPU_PYR (d = 3) */
 	int p;                            /* 1..4                                                      */
 	int n_vs, n_vc;
 	const double* cv0_vs_vc;          /* n_vc x n_vs                                               */
-	const double* cv1_vs_vc;          /* 3 x n_vc x n_vs: d/dr_k of the basis at the vc nodes      */
+	const double* cv1_vs_vc;          /* d x n_vc x n_vs: d/dr_k of the basis at the vc nodes      */
 	const double* w_vc;               /* n_vc                                                      */
 	int n_lf;                         /* local faces: TET 4, WEDGE 5, PYR 5 (element.c f_ve order) */
 	int n_ord;                        /* orientations per face (at most 8)                         */

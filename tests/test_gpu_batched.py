@@ -412,3 +412,35 @@ def test_create_rejects_wedge_factors_that_do_not_match(gpu_lib):
     e = _create_error(prob)
     assert e.status == 1 and "WEDGE factors" in str(e)
     ops.prism_factors = good
+
+
+# ---- 2D: QUAD and TRI volumes (dense TRI groups, LINE faces in two orientations) -------------------------------
+TRI_CASES = {
+    "tri_quad_roe_6": lambda: __import__("dpgsolver_gb300.host.mixed_types", fromlist=["x"]).mixed_tri_quad_euler(
+        6, seed=1),
+    "tri_quad_lf_p13_8": lambda: __import__("dpgsolver_gb300.host.mixed_types", fromlist=["x"]).mixed_tri_quad_euler(
+        8, seed=2, p_set=(1, 3), num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
+    "tri_only_roe_5": lambda: __import__("dpgsolver_gb300.host.mixed_types", fromlist=["x"]).mixed_tri_quad_euler(
+        5, seed=3, p_tri=1.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TRI_CASES))
+@pytest.mark.parametrize("form", FORMS)
+def test_tri_quad_matches_oracle(gpu_lib, name, form):
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = TRI_CASES[name]()
+    ref = oracle.Oracle(prob)
+    r_ref, mx_ref = ref.compute_rhs(prob.sol)
+    s_ref = prob.sol.copy()
+    for _ in range(2):
+        s_ref, _, _ = ref.ssp_rk3_step(s_ref, prob.dt)
+    with BatchSimulation(prob) as sim:
+        sim.form = form
+        mx = sim.compute_rhs()
+        r = sim.rhs
+        sim.ssp_rk3_steps(prob.dt, 2)
+        s = sim.sol_coef
+    assert rel_err(r, r_ref) <= TOL
+    assert abs(mx - mx_ref) <= TOL * mx_ref
+    assert rel_err(s, s_ref) <= TOL

@@ -179,3 +179,82 @@ def test_wedge_operators_are_kronecker_products(p):
     assert np.abs(np.kron(l0, t1[0]) - o.cv1_vs_vc(0)).max() <= 1e-13 * scale
     assert np.abs(np.kron(l0, t1[1]) - o.cv1_vs_vc(1)).max() <= 1e-13 * scale
     assert np.abs(np.kron(l1, t0) - o.cv1_vs_vc(2)).max() <= 1e-13 * scale
+
+
+# ---- 2D: TRI volumes and the mixed QUAD/TRI mesh ---------------------------------------------------------------------
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_tri_basis_rule_and_faces(p):
+    """Orthonormal P_p on the reference TRI (element.c vertices), finite-difference gradients, face nodes on the
+    face lines, face weights summing to the edge length 2, outward normals."""
+    from dpgsolver_gb300.host.element import TRI
+    o = S.DenseOperatorSet(TRI, p)
+    assert o.n_vs == (p + 1) * (p + 2) // 2 and o.d == 2
+    assert np.abs(o.mass() - np.eye(o.n_vs)).max() < 1e-12
+    x0 = o.x_vc[::3]
+    _, G = o.basis(x0)
+    for k in range(2):
+        dx = np.zeros(2)
+        dx[k] = 1e-6
+        fd = (o.basis(x0 + dx)[0] - o.basis(x0 - dx)[0]) / 2e-6
+        assert np.abs(fd - G[k]).max() < 1e-6 * max(1.0, np.abs(G[k]).max())
+    V = S.VERTS[TRI]
+    for lf, fv in enumerate(S.F_VE[TRI]):
+        P = V[fv]
+        assert abs(o.w_fc(lf, 3).sum() - np.linalg.norm(P[1] - P[0])) < 1e-14
+        t = (P[1] - P[0]) / np.linalg.norm(P[1] - P[0])
+        n = np.array([t[1], -t[0]])
+        if np.dot(n, P[0] - V.mean(0)) < 0:
+            n = -n                                                 # outward
+        assert np.abs(n - o.normals_ref[lf]).max() < 1e-14
+        for ord_ in range(o.n_ords(lf)):
+            assert np.abs((o.face_points(lf, ord_, 3) - P[0]) @ n).max() < 1e-14
+
+
+def test_tri_quad_mesh_faces_match():
+    """Both sides of every edge evaluate at the same physical points (LINE orientations), QUAD sides unpermuted."""
+    from dpgsolver_gb300.host.element import QUAD, TRI, gauss_legendre
+    prob = MT.mixed_tri_quad_euler(5, seed=2)
+    mesh = prob.mesh
+    assert mesh.counts()[TRI] > 0 and mesh.counts()[QUAD] > 0
+    assert set(mesh.face_ord.ravel().tolist()) == {0, 1}
+    for f in range(mesh.n_faces):
+        pts = []
+        for s in range(2):
+            v = mesh.face_vol[f, s]
+            ops = prob.groups[prob.vol_group[v]]
+            lf, o = mesh.face_lf[f, s], mesh.face_ord[f, s]
+            if getattr(ops, "dense", False):
+                xr = ops.face_points(lf, o, int(prob.face_q[f]))
+            else:
+                assert o == 0
+                xq, _ = gauss_legendre(int(prob.face_q[f]))
+                nd, side = lf // 2, lf % 2
+                xr = np.zeros((len(xq), 2))
+                xr[:, nd] = -1.0 if side == 0 else 1.0
+                xr[:, 1 - nd] = xq
+            pts.append(xr @ prob.A[v].T + prob.b[v])
+        dd = pts[0] - pts[1]
+        dd -= np.round(dd)          # periodic images
+        assert np.abs(dd).max() < 1e-13
+
+
+def test_tri_quad_oracle_free_stream_conservation_and_complex_step():
+    prob = MT.mixed_tri_quad_euler(4, seed=0)
+    o = oracle.Oracle(prob)
+    raw = o.compute_rhs_raw(prob.sol)
+    tot, scale = np.zeros(4), np.zeros(4)
+    for g, ops in enumerate(prob.groups):
+        one = _one_coefficients(ops)
+        B = prob.group_view(raw, g)
+        tot += np.einsum("vka,a->k", B, one)
+        scale += np.einsum("vka,a->k", np.abs(B), np.abs(one))
+    assert np.all(np.abs(tot) <= 1e-13 * scale.max())
+    rng = np.random.default_rng(3)
+    base = prob.sol + 1e-2 * rng.standard_normal(prob.sol.shape)
+    dirn = rng.standard_normal(prob.sol.shape)
+    _, ri = o.compute_rhs_cmplx(base, 1e-30 * dirn)
+    fd = (o.compute_rhs(base + 1e-6 * dirn)[0] - o.compute_rhs(base - 1e-6 * dirn)[0]) / 2e-6
+    assert np.max(np.abs(ri / 1e-30 - fd)) <= 1e-6 * np.max(np.abs(fd))
+    vals = np.array([1.0, 0.3, -0.2, 2.5])
+    prob.project(lambda x: np.tile(vals, (len(x), 1)))
+    assert o.compute_rhs(prob.sol)[1] < 1e-11
