@@ -425,6 +425,7 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_mixed:
         res["mixed_types"] = mixed_measurements(torch, stream, args, "types")
         res["mixed"] = mixed_measurements(torch, stream, args, "hex")
+        res["tri_quad_2d"] = tri_quad_measurements(torch, stream, args)
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, workers=1)
     sim.close()
@@ -559,6 +560,59 @@ def make_mixed(kind, n):
     return mixed_euler(3, n, seed=0)
 
 
+def _batched_forms(torch, stream, args, sim, prob, n_steps, autotune=True):
+    """SSP-RK3 steps of a batched context in its forms: plain per-group launches, the same from a graph, the fused
+    persistent launches and the parallel branches from graphs, then (autotune) the autotuned choice."""
+    ns, dt = prob.n_state, prob.dt
+    out = {}
+
+    def run(label, form, graphs):
+        sim.form = form
+        sim.set_graphs(graphs)
+        sim.upload_state(prob.sol)
+        sim.ssp_rk3_steps(dt, max(args.warmup, 3), want_max=False)
+        l0 = sim.kernel_launches()
+        ms = _timed(torch, stream, lambda: sim.ssp_rk3_steps(dt, n_steps, want_max=False), 1)
+        out[label] = {"value": 3 * ns * n_steps / (ms * 1e-3), "ms_per_step": ms / n_steps,
+                      "launches_per_step": (sim.kernel_launches() - l0) / n_steps}
+
+    run("plain_per_group", "plain", False)
+    run("per_group_graph", "plain", True)
+    run("fused_graph", "fused", True)
+    run("branches_graph", "branches", True)
+    report, tuned_form = None, None
+    if autotune:
+        sim.upload_state(prob.sol)
+        report = sim.autotune(dt, reps=3)
+        tuned_form = sim.form
+        run("autotuned_graph", tuned_form, True)
+    return out, report, tuned_form
+
+
+def tri_quad_measurements(torch, stream, args):
+    """2D Euler on the mixed QUAD/TRI mesh of the periodic unit square (mixed_tri_quad_euler: n^2 cells, half of
+    them split into two TRIs, p uniform in {1,2,3,4} with seed 0, Roe-Pike, Mach 0.5 seeded sinusoidal state with
+    5 % perturbations): SSP-RK3 steps in the batched context's four forms, the TRI groups on the dense kernels."""
+    from dpgsolver_gb300.host.element import QUAD, TRI
+    from dpgsolver_gb300.host.mixed_types import mixed_tri_quad_euler
+    from dpgsolver_gb300.solver import BatchSimulation
+    n = args.tri_n
+    t0 = time.time()
+    prob = mixed_tri_quad_euler(n, seed=0, perturb=0.05)
+    setup_s = time.time() - t0
+    n_steps = max(3, min(args.steps, 20))
+    with BatchSimulation(prob, stream=stream.cuda_stream) as sim:
+        out, _, _ = _batched_forms(torch, stream, args, sim, prob, n_steps, autotune=False)
+    tname = {QUAD: "QUAD", TRI: "TRI"}
+    return {"workload": f"2D Euler mixed QUAD/TRI {n}^2 cells on the unit square (half split into TRIs, straight, "
+                        "conforming, periodic), p uniform in {1,2,3,4} (seed 0), Roe-Pike, Mach 0.5 seeded "
+                        "sinusoidal state",
+            "elements": prob.n_volumes, "n_state": prob.n_state,
+            "groups": {f"{tname[getattr(o, 'e_type', QUAD)]} p{o.p}": int(np.sum(prob.vol_group == i))
+                       for i, o in enumerate(prob.groups)},
+            "unit": "DOF-residual-evals/s", "steps": n_steps, "forms": out, "setup_s": setup_s}
+
+
 def mixed_measurements(torch, stream, args, kind="types"):
     """Batched mixed workloads, both Roe-Pike with a seeded smooth sinusoidal state around a Mach 0.5 free stream on
     the periodic unit cube, p drawn uniformly from {1,2,3,4} per volume with seed 0:
@@ -578,26 +632,7 @@ def mixed_measurements(torch, stream, args, kind="types"):
     sim = BatchSimulation(prob, stream=stream.cuda_stream)
     ns, dt = prob.n_state, prob.dt
     n_steps = max(3, min(args.steps, 20))
-    out = {}
-
-    def run(label, form, graphs):
-        sim.form = form
-        sim.set_graphs(graphs)
-        sim.upload_state(prob.sol)
-        sim.ssp_rk3_steps(dt, max(args.warmup, 3), want_max=False)
-        l0 = sim.kernel_launches()
-        ms = _timed(torch, stream, lambda: sim.ssp_rk3_steps(dt, n_steps, want_max=False), 1)
-        out[label] = {"value": 3 * ns * n_steps / (ms * 1e-3), "ms_per_step": ms / n_steps,
-                      "launches_per_step": (sim.kernel_launches() - l0) / n_steps}
-
-    run("plain_per_group", "plain", False)
-    run("per_group_graph", "plain", True)
-    run("fused_graph", "fused", True)
-    run("branches_graph", "branches", True)
-    sim.upload_state(prob.sol)
-    report = sim.autotune(dt, reps=3)
-    tuned_form = sim.form
-    run("autotuned_graph", tuned_form, True)
+    out, report, tuned_form = _batched_forms(torch, stream, args, sim, prob, n_steps)
     flops = 0
     for g, ops in enumerate(prob.groups):
         cnt = int(np.sum(prob.vol_group == g))
@@ -856,6 +891,7 @@ def main():
     ap.add_argument("--vortex-steps", type=int, default=1000)
     ap.add_argument("--mixed-n", type=int, default=58, help="volumes per direction of the mixed-order HEX mesh")
     ap.add_argument("--types-n", type=int, default=50, help="cells per direction of the mixed-type mesh (even)")
+    ap.add_argument("--tri-n", type=int, default=384, help="cells per direction of the 2D QUAD/TRI mesh")
     ap.add_argument("--mixed-form", choices=["plain", "per_group_graph", "fused", "branches"], default="fused",
                     help="form of the mixed-order stages for --workload mixed3d --only-rk")
     args = ap.parse_args()
