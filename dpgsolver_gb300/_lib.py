@@ -95,7 +95,8 @@ class DenseOperators(ctypes.Structure):
                 ("cv0_vs_fc", ctypes.POINTER(c_double_p)), ("w_fc", ctypes.POINTER(c_double_p)),
                 ("n_tri_vs", ctypes.c_int), ("n_tri_vc", ctypes.c_int), ("n_line_vs", ctypes.c_int),
                 ("n_line_vc", ctypes.c_int), ("tri_cv0", c_double_p), ("tri_cv1", c_double_p),
-                ("line_cv0", c_double_p), ("line_cv1", c_double_p)]
+                ("line_cv0", c_double_p), ("line_cv1", c_double_p),
+                ("ccSB0_vs_vs", c_double_p), ("ccBS0_vs_vs", c_double_p)]
 
 
 class Group(ctypes.Structure):

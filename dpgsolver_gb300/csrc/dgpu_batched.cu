@@ -675,8 +675,8 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 			    op->n_vc > 4096 || op->n_lf != type_faces(op->elem_type) || op->n_ord < 1 || op->n_ord > kMaxOrd ||
 			    !op->cv0_vs_vc || !op->cv1_vs_vc || !op->w_vc || !op->n_fc || !op->cv0_vs_fc || !op->w_fc)
 				return reject(DGPU_ERR_INVALID_ARGUMENT, "incomplete dense operator set");
-			if (c->positivity)
-				return reject(DGPU_ERR_UNSUPPORTED, "positivity is provided for QUAD/HEX groups only");
+			if (c->positivity && (!op->ccSB0_vs_vs || !op->ccBS0_vs_vs))
+				return reject(DGPU_ERR_INVALID_ARGUMENT, "positivity needs the Bezier maps of every dense group");
 			const int t = c->gl[ig].idx;
 			dops[t] = op;
 			g_q[ig] = op->p + 1;
@@ -1083,6 +1083,15 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 		c->dense_bufs.push_back(d_foff);
 		B_TRY(upload_vec(&d_ij, inv_J[t]));
 		c->dense_bufs.push_back(d_ij);
+		if (c->positivity) {
+			double *d_sb = nullptr, *d_bs = nullptr;
+			B_TRY(upload_vec(&d_sb, std::vector<double>(op->ccSB0_vs_vs, op->ccSB0_vs_vs + (size_t)nvs * nvs)));
+			c->dense_bufs.push_back(d_sb);
+			B_TRY(upload_vec(&d_bs, std::vector<double>(op->ccBS0_vs_vs, op->ccBS0_vs_vs + (size_t)nvs * nvs)));
+			c->dense_bufs.push_back(d_bs);
+			G.ccSB0 = d_sb;
+			G.ccBS0 = d_bs;
+		}
 		G.cv0 = d_cv0;
 		G.cv1 = d_cv1;
 		G.minv = d_minv;

@@ -54,6 +54,8 @@ struct DGroup {
 	const double* tri1;         // 2 x n_tvc x n_tvs
 	const double* line0;        // n_lvc x n_lvs
 	const double* line1;        // n_lvc x n_lvs
+	const double* ccSB0;        // n_vs x n_vs: coefficients -> Bezier coefficients (positivity), or null
+	const double* ccBS0;        // n_vs x n_vs: Bezier -> coefficients
 };
 
 struct BParams {

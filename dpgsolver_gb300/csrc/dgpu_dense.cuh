@@ -251,6 +251,110 @@ __device__ void dvol_body(const BParams& P, const DGroup& G, int e0, int E, cons
 // ---------------------------------------------------------------------------------------------------------------
 // Lift of the face fluxes, M^-1, then the residual or the RK stage (coefficient space)
 // ---------------------------------------------------------------------------------------------------------------
+// enforce_positivity_highorder (solve.c:187-233) on the new states of the CTA's elements (kept at NV n_vs of
+// each element's block): Bezier coefficients b = ccSB0 s per variable; one thread per element converts them to
+// primitive variables, checks the average (error flag below EPS_PHYS) and minimum of the density, then of the
+// pressure, and when a minimum is below EPS_PHYS blends every variable toward its average (correct_coef,
+// :356-374) before the pressure check; corrected elements get s = ccBS0 b back in conserved variables. Elements
+// that need no correction keep s (the reference's round trip is the identity up to rounding).
+template <int NV>
+__device__ void dense_positivity(const BParams& P, const DGroup& G, int e0, int n_here, const RkArgs& rk,
+                                 double* smem, int PER_E)
+{
+	constexpr double kEpsPhys = 1e-13;   // definitions_tol.h EPS_PHYS
+	constexpr int D = NV - 2;
+	const int nvs = G.n_vs;
+	__syncthreads();
+	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
+		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
+		const double* sv = smem + e * PER_E + NV * nvs + k * nvs;
+		const double* row = G.ccSB0 + (long long)m * nvs;
+		double b = 0.0;
+		for (int a = 0; a < nvs; ++a)
+			b += __ldg(row + a) * sv[a];
+		smem[e * PER_E + rem] = b;
+	}
+	__syncthreads();
+	// conserved -> primitive (rho, u, p) at every Bezier node (convert_variables 'c' -> 'p'), node-parallel
+	for (int it = threadIdx.x; it < n_here * nvs; it += blockDim.x) {
+		const int e = it / nvs, m = it % nvs;
+		double* b = smem + e * PER_E;
+		const double rho = b[m];
+		double V2 = 0.0;
+#pragma unroll
+		for (int d = 0; d < D; ++d) {
+			const double u = b[(1 + d) * nvs + m] / rho;
+			b[(1 + d) * nvs + m] = u;
+			V2 += u * u;
+		}
+		b[(D + 1) * nvs + m] = kGm1 * (b[(D + 1) * nvs + m] - 0.5 * rho * V2);
+	}
+	__syncthreads();
+	// per element: the rhs half of its block now holds b, the other half s; the flag takes a spare scalar slot
+	for (int e = threadIdx.x; e < n_here; e += blockDim.x) {
+		double* b = smem + e * PER_E;
+		bool corrected = false;
+		for (int vr = 0; vr < NV; vr += NV - 1) {
+			double avg = 0.0, mn = b[vr * nvs];
+			for (int m = 0; m < nvs; ++m) {
+				avg += b[vr * nvs + m];
+				mn = fmin(mn, b[vr * nvs + m]);
+			}
+			avg /= nvs;
+			if (!(avg >= kEpsPhys)) {
+				atomicExch(P.err_flag, 1);
+				break;
+			}
+			if (mn < kEpsPhys) {
+				const double th = fmax(0.0, fmin(1.0, (avg - kEpsPhys) / (avg - mn)));
+				for (int k = 0; k < NV; ++k) {
+					double a = 0.0;
+					for (int m = 0; m < nvs; ++m)
+						a += b[k * nvs + m];
+					a /= nvs;
+					if ((k == 0 || k == NV - 1) && a < kEpsPhys)
+						a = kEpsPhys;
+					for (int m = 0; m < nvs; ++m)
+						b[k * nvs + m] = th * b[k * nvs + m] + (1.0 - th) * a;
+				}
+				corrected = true;
+			}
+		}
+		if (corrected)
+			atomicAdd(P.n_corr, 1ull);
+		smem[e * PER_E + 2 * NV * nvs] = corrected ? 1.0 : 0.0;
+	}
+	__syncthreads();
+	// primitive -> conserved on the corrected elements, node-parallel
+	for (int it = threadIdx.x; it < n_here * nvs; it += blockDim.x) {
+		const int e = it / nvs, m = it % nvs;
+		if (smem[e * PER_E + 2 * NV * nvs] == 0.0)
+			continue;
+		double* b = smem + e * PER_E;
+		const double rho = b[m];
+		double V2 = 0.0;
+#pragma unroll
+		for (int d = 0; d < D; ++d) {
+			const double u = b[(1 + d) * nvs + m];
+			V2 += u * u;
+			b[(1 + d) * nvs + m] = rho * u;
+		}
+		b[(D + 1) * nvs + m] = b[(D + 1) * nvs + m] / kGm1 + 0.5 * rho * V2;
+	}
+	__syncthreads();
+	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
+		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
+		if (smem[e * PER_E + 2 * NV * nvs] == 0.0)
+			continue;
+		const double* bv = smem + e * PER_E + k * nvs;
+		const double* row = G.ccBS0 + (long long)m * nvs;
+		double s = 0.0;
+		for (int a = 0; a < nvs; ++a)
+			s += __ldg(row + a) * bv[a];
+		rk.u[G.state_off + (long long)(e0 + e) * NV * nvs + rem] = s;
+	}
+}
+
 template <int NV, int MODE>
 __device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, const RkArgs& rk, double* smem)
 {
@@ -311,7 +415,12 @@ __device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, con
 				sn = (1.0 / 3.0) * (rk.u0[o] + 2.0 * s + 2.0 * rk.dt * R);
 			}
 			rk.u[o] = sn;
+			smem[e * PER_E + NV * nvs + rem] = sn;   // kept for the positivity check
 		}
+	}
+	if constexpr (MODE != kModeRhs) {
+		if (rk.positivity && G.ccSB0)
+			dense_positivity<NV>(P, G, e0, n_here, rk, smem, PER_E);
 	}
 	if (MODE == kModeRhs || rk.want_max) {
 #pragma unroll

@@ -288,13 +288,13 @@ class MixedTypeProblem:
     """Mixed-type mesh + per-volume p + per-(type, p) operators + affine geometry + state (flat layout as
     MixedTPProblem: per volume the (n_var x n_vs(v)) block, volume-list order)."""
 
-    def __init__(self, mesh: MixedTypeMesh, p_vol, pde=PDE_EULER, num_flux=NUM_FLUX_ROE_PIKE):
+    def __init__(self, mesh: MixedTypeMesh, p_vol, pde=PDE_EULER, num_flux=NUM_FLUX_ROE_PIKE, positivity=False):
         self.mesh = mesh
         self.d = d = getattr(mesh, "d", 3)
         tp = QUAD if d == 2 else HEX
         self.pde = pde
         self.num_flux = num_flux
-        self.positivity = False
+        self.positivity = bool(positivity)
         self.b_adv = np.zeros(3)
         self.n_var = d + 2
         self.name = "mixed_types"
@@ -455,13 +455,15 @@ class MixedTypeProblem:
 
 def mixed_types_euler(n: int = 12, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE,
                       mach: float = 0.5, perturb: float = 0.05, c_blocks: float = 0.06, w_columns: float = 0.15,
-                      p_tri: float = 1.0) -> MixedTypeProblem:
+                      p_tri: float = 1.0, positivity: bool = True) -> MixedTypeProblem:
     """Mixed HEX/TET/WEDGE/PYR mesh of the periodic unit cube (n^3 cells), p uniform in p_set per volume (seeded),
-    Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed.mixed_euler)."""
+    Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed.mixed_euler). The
+    positivity limiter is on by default, as the reference applies it to every Euler stage
+    (test_case_requires_positivity)."""
     mesh = MixedTypeMesh(n, seed=seed, c_blocks=c_blocks, w_columns=w_columns, p_tri=p_tri)
     rng = np.random.default_rng(seed + 17)
     p_vol = rng.choice(np.asarray(p_set, dtype=np.int32), size=mesh.n_volumes)
-    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux)
+    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux, positivity=positivity)
     rng2 = np.random.default_rng(seed + 1)
     ph = rng2.uniform(0.0, 2.0 * math.pi, size=(5, 3))
     c0 = math.sqrt(GAMMA)
@@ -487,13 +489,15 @@ def mixed_types_euler(n: int = 12, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: 
 
 
 def mixed_tri_quad_euler(n: int = 16, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE,
-                         mach: float = 0.5, perturb: float = 0.3, p_tri: float = 0.5) -> MixedTypeProblem:
+                         mach: float = 0.5, perturb: float = 0.3, p_tri: float = 0.5,
+                         positivity: bool = True) -> MixedTypeProblem:
     """Mixed QUAD/TRI mesh of the periodic unit square (n^2 cells, MixedTriQuadMesh), p uniform in p_set per volume
-    (seeded), Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed_types_euler)."""
+    (seeded), Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed_types_euler),
+    positivity limiter on by default."""
     mesh = MixedTriQuadMesh(n, seed=seed, p_tri=p_tri)
     rng = np.random.default_rng(seed + 17)
     p_vol = rng.choice(np.asarray(p_set, dtype=np.int32), size=mesh.n_volumes)
-    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux)
+    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux, positivity=positivity)
     rng2 = np.random.default_rng(seed + 1)
     ph = rng2.uniform(0.0, 2.0 * math.pi, size=(4, 2))
     c0 = math.sqrt(GAMMA)

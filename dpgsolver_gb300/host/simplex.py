@@ -426,6 +426,27 @@ class DenseOperatorSet:
         Dl = np.stack([jacobi_dp(c, 0.0, 0.0, xz) for c in range(q)], axis=1)
         return (Vt @ self._Ct, np.stack([Gt[0] @ self._Ct, Gt[1] @ self._Ct]), Vl @ self._Cl, Dl @ self._Cl)
 
+    def _bezier_maps(self):
+        if "bez" not in self._cache:
+            x, w = volume_rule(self.e_type, self.p + 2)
+            B = bezier_basis(self.e_type, self.p, x)
+            if B.shape[1] != self.n_vs:
+                raise AssertionError("Bezier basis dimension")
+            S_ = self.basis(x)[0]
+            sb = np.linalg.lstsq(B, S_, rcond=None)[0]          # solution basis in the Bezier basis: S = B sb
+            if np.abs(B @ sb - S_).max() > 1e-10 * max(1.0, np.abs(S_).max()):
+                raise AssertionError("the Bezier functions do not span the solution space")
+            self._cache["bez"] = (sb, np.linalg.inv(sb))
+        return self._cache["bez"]
+
+    def ccSB0_vs_vs(self):
+        """Solution-basis coefficients -> Bezier coefficients (the reference's ccSB0_vs_vs)."""
+        return self._bezier_maps()[0]
+
+    def ccBS0_vs_vs(self):
+        """Bezier coefficients -> solution-basis coefficients (ccBS0_vs_vs)."""
+        return self._bezier_maps()[1]
+
     def cv0_vs_vc(self):
         return self._cv0
 
@@ -460,6 +481,52 @@ class DenseOperatorSet:
 
     def w_fc(self, lf: int, q_f: int):
         return face_rule(self.face_type(lf), q_f)[1]
+
+
+def _bern(n: int, k: int, x):
+    """1D Bernstein polynomial C(n, k) ((1 + x) / 2)^k ((1 - x) / 2)^(n - k) on [-1, 1]."""
+    return math.comb(n, k) * (0.5 * (1.0 + x)) ** k * (0.5 * (1.0 - x)) ** (n - k)
+
+
+def bezier_basis(e_type: int, p: int, x: np.ndarray) -> np.ndarray:
+    """The reference's Bezier basis at points x (n, d) (bases.c:570-760): the Bernstein polynomials of the
+    barycentric coordinates on TRI and TET (constructor_basis_si_bezier writes the same functions in collapsed
+    coordinates), the TRI x LINE product on WEDGE, and on PYR the products B^{p-k}_i(a) B^{p-k}_j(b) B^p_k(c) of the
+    collapsed coordinates (constructor_basis_pyr_bezier). The limiter only uses their set, not their order."""
+    x = np.asarray(x, dtype=np.float64)
+    cols = []
+    if e_type in (TRI, TET):
+        V = VERTS[e_type]
+        d = V.shape[1]
+        T = np.vstack([V.T, np.ones(d + 1)])
+        lam = np.linalg.solve(T, np.vstack([x.T, np.ones(len(x))])).T          # barycentric coordinates
+        import itertools
+        for alpha in itertools.product(range(p + 1), repeat=d + 1):
+            if sum(alpha) != p:
+                continue
+            c = math.factorial(p)
+            val = np.ones(len(x))
+            for m, a in enumerate(alpha):
+                c //= math.factorial(a)
+                val = val * lam[:, m] ** a
+            cols.append(c * val)
+    elif e_type == WEDGE:
+        tri = bezier_basis(TRI, p, x[:, :2])
+        for k in range(p + 1):
+            lk = _bern(p, k, x[:, 2])
+            for t in range(tri.shape[1]):
+                cols.append(tri[:, t] * lk)
+    elif e_type == PYR:
+        xs, ys, zs = _pyr_ref_to_std(x)
+        om = 1.0 - zs
+        a, b = 2.0 * xs / om, 2.0 * ys / om
+        for i in range(p + 1):
+            for j in range(p + 1):
+                for k in range(p - max(i, j) + 1):
+                    cols.append(_bern(p - k, i, a) * _bern(p - k, j, b) * _bern(p, k, zs))
+    else:
+        raise ValueError("TRI, TET, WEDGE or PYR")
+    return np.stack(cols, axis=1)
 
 
 def face_shape(ftype: int, xi: np.ndarray) -> np.ndarray:

@@ -404,6 +404,8 @@ class BatchSimulation:
         D.cv0_vs_fc = cv0
         D.w_fc = w
         keep.extend([cv0, w])
+        D.ccSB0_vs_vs = _dp(arr(ops.ccSB0_vs_vs()))
+        D.ccBS0_vs_vs = _dp(arr(ops.ccBS0_vs_vs()))
         if ops.e_type == S.WEDGE and factorised:
             t0, t1, l0, l1 = ops.prism_factors()
             D.n_tri_vs, D.n_tri_vc = t0.shape[1], t0.shape[0]

@@ -358,6 +358,10 @@ typedef struct {
 	const double* tri_cv1;            /* 2 x n_tri_vc x n_tri_vs                                   */
 	const double* line_cv0;           /* n_line_vc x n_line_vs                                     */
 	const double* line_cv1;           /* n_line_vc x n_line_vs                                     */
+	/* Needed with positivity (NULL otherwise): solution-basis <-> Bezier coefficients, n_vs x n_vs row-major each
+	 * (the element's ccSB0_vs_vs / ccBS0_vs_vs of enforce_positivity_highorder, solve.c:187-233). */
+	const double* ccSB0_vs_vs;
+	const double* ccBS0_vs_vs;
 } dgpu_dense_operators;
 
 /* One (type, p) group of a batched mesh: exactly one of tp / dense. */
@@ -368,7 +372,7 @@ typedef struct {
 
 /* Batched context over TP and dense groups. face_ord (n_faces x 2, may be NULL = all 0) gives each side's
  * orientation index into its face operator table; QUAD/HEX sides must have orientation 0 (their own face-node
- * order is the face's canonical order). Positivity is provided for QUAD/HEX groups only. */
+ * order is the face's canonical order). With positivity every dense group must give its Bezier maps. */
 dgpu_status dgpu_batch_create_groups(const dgpu_physics* phys, int n_groups, const dgpu_group* groups,
                                      const int* vol_group, const dgpu_mesh* mesh, const int* face_ord,
                                      dgpu_batch** out);

@@ -124,9 +124,9 @@ class Oracle:
             G[gi].cv0_vs_vc = _dp(arr(ops.cv0_vs_vc()))
             G[gi].tw1_vt_vc = _dp(arr(np.stack([ops.tw1_vt_vc(k) for k in range(d)])))
             G[gi].w_vc = _dp(arr(ops.w_vc))
-            if not getattr(ops, "dense", False):    # Bezier maps exist for the TP groups only
-                G[gi].ccSB0 = _dp(arr(ops.ccSB0_vs_vs()))
-                G[gi].ccBS0 = _dp(arr(ops.ccBS0_vs_vs()))
+            G[gi].ccSB0 = _dp(arr(ops.ccSB0_vs_vs()))      # Bezier maps (enforce_positivity_highorder)
+            G[gi].ccBS0 = _dp(arr(ops.ccBS0_vs_vs()))
+            if not getattr(ops, "dense", False):
                 G[gi].cv1_vs_vc = _dp(arr(np.stack([ops.cv1_vs_vc(k) for k in range(d)])))
         # face operator sets: one per (group, face order, orientation) that occurs, stacked over local faces
         vol_group = fl["vol_group"]

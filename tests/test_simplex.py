@@ -258,3 +258,18 @@ def test_tri_quad_oracle_free_stream_conservation_and_complex_step():
     vals = np.array([1.0, 0.3, -0.2, 2.5])
     prob.project(lambda x: np.tile(vals, (len(x), 1)))
     assert o.compute_rhs(prob.sol)[1] < 1e-11
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_bezier_maps(p):
+    """The reference's Bezier bases (bases.c:570-760) span each solution space: partition of unity, non-negative,
+    the constant function has equal Bezier coefficients, and ccBS0 ccSB0 = I."""
+    from dpgsolver_gb300.host.element import TRI
+    for e in (TRI, TET, WEDGE, PYR):
+        o = S.DenseOperatorSet(e, p)
+        B = S.bezier_basis(e, p, o.x_vc)
+        assert np.abs(B.sum(axis=1) - 1.0).max() < 1e-14 and B.min() >= 0.0
+        sb, bs = o.ccSB0_vs_vs(), o.ccBS0_vs_vs()
+        assert np.abs(bs @ sb - np.eye(o.n_vs)).max() < 1e-11
+        b1 = sb @ _one_coefficients(o)
+        assert np.abs(b1 - 1.0).max() < 1e-12
