@@ -1091,6 +1091,23 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 			c->dense_bufs.push_back(d_bs);
 			G.ccSB0 = d_sb;
 			G.ccBS0 = d_bs;
+			// FP32 pre-filter: the map in FP32 and its rounding bound, (n_vs + 2) 2^-23 max_m sum_a |ccSB0[m][a]|
+			// (inputs and map entries rounded to FP32, n_vs-term FP32 sums), doubled
+			std::vector<float> sbf((size_t)nvs * nvs);
+			double row_max = 0.0;
+			for (int m = 0; m < nvs; ++m) {
+				double r = 0.0;
+				for (int a = 0; a < nvs; ++a) {
+					sbf[(size_t)m * nvs + a] = (float)op->ccSB0_vs_vs[(size_t)m * nvs + a];
+					r += fabs(op->ccSB0_vs_vs[(size_t)m * nvs + a]);
+				}
+				row_max = std::max(row_max, r);
+			}
+			float* d_sbf = nullptr;
+			B_TRY(upload_vec(&d_sbf, sbf));
+			c->dense_bufs.push_back(d_sbf);
+			G.ccSB0f = d_sbf;
+			G.pos_err = (float)(2.0 * (nvs + 2) * ldexp(1.0, -23) * row_max);
 		}
 		G.cv0 = d_cv0;
 		G.cv1 = d_cv1;

@@ -56,6 +56,8 @@ struct DGroup {
 	const double* line1;        // n_lvc x n_lvs
 	const double* ccSB0;        // n_vs x n_vs: coefficients -> Bezier coefficients (positivity), or null
 	const double* ccBS0;        // n_vs x n_vs: Bezier -> coefficients
+	const float* ccSB0f;        // ccSB0 in FP32 (the limiter's pre-filter)
+	float pos_err;              // bound on |b_fp32 - b| / max |s| of the pre-filter's Bezier coefficients
 };
 
 struct BParams {

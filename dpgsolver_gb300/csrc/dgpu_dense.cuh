@@ -265,8 +265,61 @@ __device__ void dense_positivity(const BParams& P, const DGroup& G, int e0, int 
 	constexpr int D = NV - 2;
 	const int nvs = G.n_vs;
 	__syncthreads();
+	// FP32 pre-filter: per element the scales S_k = max |s_k| (into the free rhs half), then every Bezier node's
+	// density and pressure lower bounds from FP32 coefficients and their rounding bound pos_err S_k; an element
+	// whose bounds all clear the thresholds (which lie far above EPS_PHYS) needs no correction and is skipped
+	// the state in FP32 once (after the NV scales in the free rhs half), so the n_vs^2 products run on FP32 only
+	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
+		const int e = it / (NV * nvs), rem = it % (NV * nvs);
+		reinterpret_cast<float*>(smem + e * PER_E + NV)[rem] = (float)smem[e * PER_E + NV * nvs + rem];
+	}
+	for (int e = threadIdx.x; e < n_here; e += blockDim.x) {
+		const double* sv = smem + e * PER_E + NV * nvs;
+		for (int k = 0; k < NV; ++k) {
+			double mx = 0.0;
+			for (int a = 0; a < nvs; ++a)
+				mx = fmax(mx, fabs(sv[k * nvs + a]));
+			smem[e * PER_E + k] = mx;
+		}
+		smem[e * PER_E + 2 * NV * nvs + 1] = 0.0;   // unsafe flag
+	}
+	__syncthreads();
+	for (int it = threadIdx.x; it < n_here * nvs; it += blockDim.x) {
+		const int e = it / nvs, m = it % nvs;
+		const float* sf = reinterpret_cast<const float*>(smem + e * PER_E + NV);
+		const float* row = G.ccSB0f + (long long)m * nvs;
+		float bk[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			float acc = 0.f;
+			for (int a = 0; a < nvs; ++a)
+				acc += __ldg(row + a) * sf[k * nvs + a];
+			bk[k] = acc;
+		}
+		const float err = G.pos_err;
+		const float s_rho = (float)smem[e * PER_E];
+		const float rho_lo = bk[0] - err * s_rho;
+		bool safe = rho_lo > 1e-6f * s_rho + 1e-12f;
+		if (safe) {
+			float m2 = 0.f;
+#pragma unroll
+			for (int d = 0; d < D; ++d) {
+				const float mk = fabsf(bk[1 + d]) + err * (float)smem[e * PER_E + 1 + d];
+				m2 += mk * mk;
+			}
+			const float E_lo = bk[D + 1] - err * (float)smem[e * PER_E + D + 1];
+			const float ke = 0.5f * m2 / rho_lo;
+			const float p_lo = 0.4f * (E_lo - ke);
+			safe = p_lo > 1e-5f * (fabsf(E_lo) + ke) + 1e-12f;   // NaN/Inf fail this test and go to the exact path
+		}
+		if (!safe)
+			smem[e * PER_E + 2 * NV * nvs + 1] = 1.0;
+	}
+	__syncthreads();
 	for (int it = threadIdx.x; it < n_here * NV * nvs; it += blockDim.x) {
 		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
+		if (smem[e * PER_E + 2 * NV * nvs + 1] == 0.0)
+			continue;
 		const double* sv = smem + e * PER_E + NV * nvs + k * nvs;
 		const double* row = G.ccSB0 + (long long)m * nvs;
 		double b = 0.0;
@@ -278,6 +331,8 @@ __device__ void dense_positivity(const BParams& P, const DGroup& G, int e0, int 
 	// conserved -> primitive (rho, u, p) at every Bezier node (convert_variables 'c' -> 'p'), node-parallel
 	for (int it = threadIdx.x; it < n_here * nvs; it += blockDim.x) {
 		const int e = it / nvs, m = it % nvs;
+		if (smem[e * PER_E + 2 * NV * nvs + 1] == 0.0)
+			continue;
 		double* b = smem + e * PER_E;
 		const double rho = b[m];
 		double V2 = 0.0;
@@ -294,6 +349,10 @@ __device__ void dense_positivity(const BParams& P, const DGroup& G, int e0, int 
 	for (int e = threadIdx.x; e < n_here; e += blockDim.x) {
 		double* b = smem + e * PER_E;
 		bool corrected = false;
+		if (smem[e * PER_E + 2 * NV * nvs + 1] == 0.0) {   // cleared by the pre-filter
+			smem[e * PER_E + 2 * NV * nvs] = 0.0;
+			continue;
+		}
 		for (int vr = 0; vr < NV; vr += NV - 1) {
 			double avg = 0.0, mn = b[vr * nvs];
 			for (int m = 0; m < nvs; ++m) {
