@@ -11,6 +11,7 @@ import pytest
 
 import oracle
 from dpgsolver_gb300.host import mixed as M
+from dpgsolver_gb300.host import mixed_types as MT
 from dpgsolver_gb300.host import problem as P
 
 pytestmark = pytest.mark.gpu
@@ -409,12 +410,10 @@ def test_create_rejects_wedge_factors_that_do_not_match(gpu_lib):
 
 # ---- 2D: QUAD and TRI volumes (dense TRI groups, LINE faces in two orientations) -------------------------------
 TRI_CASES = {
-    "tri_quad_roe_6": lambda: __import__("dpgsolver_gb300.host.mixed_types", fromlist=["x"]).mixed_tri_quad_euler(
-        6, seed=1),
-    "tri_quad_lf_p13_8": lambda: __import__("dpgsolver_gb300.host.mixed_types", fromlist=["x"]).mixed_tri_quad_euler(
-        8, seed=2, p_set=(1, 3), num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
-    "tri_only_roe_5": lambda: __import__("dpgsolver_gb300.host.mixed_types", fromlist=["x"]).mixed_tri_quad_euler(
-        5, seed=3, p_tri=1.0),
+    "tri_quad_roe_6": lambda: MT.mixed_tri_quad_euler(6, seed=1),
+    "tri_quad_lf_p13_8": lambda: MT.mixed_tri_quad_euler(8, seed=2, p_set=(1, 3),
+                                                         num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
+    "tri_only_roe_5": lambda: MT.mixed_tri_quad_euler(5, seed=3, p_tri=1.0),
 }
 
 
@@ -439,10 +438,8 @@ def test_tri_quad_matches_oracle(gpu_lib, name, form):
     assert rel_err(s, s_ref) <= TOL
 
 
-@pytest.mark.parametrize("make", [lambda: __import__("dpgsolver_gb300.host.mixed_types", fromlist=["x"]).mixed_types_euler(
-                                      4, seed=0, perturb=0.9),
-                                  lambda: __import__("dpgsolver_gb300.host.mixed_types", fromlist=["x"]).mixed_tri_quad_euler(
-                                      5, seed=4, perturb=0.97)])
+@pytest.mark.parametrize("make", [lambda: MT.mixed_types_euler(4, seed=0, perturb=0.9),
+                                  lambda: MT.mixed_tri_quad_euler(5, seed=4, perturb=0.97)])
 def test_dense_positivity_matches_oracle(gpu_lib, make):
     """enforce_positivity_highorder on TRI/TET/WEDGE/PYR groups (their Bezier maps, simplex.bezier_basis): strong
     density and pressure dips trigger corrections; two RK steps in every form against the oracle, the same number
