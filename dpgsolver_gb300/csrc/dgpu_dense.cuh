@@ -273,15 +273,15 @@ __device__ void dense_positivity(const BParams& P, const DGroup& G, int e0, int 
 		const int e = it / (NV * nvs), rem = it % (NV * nvs);
 		reinterpret_cast<float*>(smem + e * PER_E + NV)[rem] = (float)smem[e * PER_E + NV * nvs + rem];
 	}
-	for (int e = threadIdx.x; e < n_here; e += blockDim.x) {
-		const double* sv = smem + e * PER_E + NV * nvs;
-		for (int k = 0; k < NV; ++k) {
-			double mx = 0.0;
-			for (int a = 0; a < nvs; ++a)
-				mx = fmax(mx, fabs(sv[k * nvs + a]));
-			smem[e * PER_E + k] = mx;
-		}
-		smem[e * PER_E + 2 * NV * nvs + 1] = 0.0;   // unsafe flag
+	for (int it = threadIdx.x; it < n_here * NV; it += blockDim.x) {   // one thread per (volume, variable)
+		const int e = it / NV, k = it % NV;
+		const double* sv = smem + e * PER_E + NV * nvs + k * nvs;
+		double mx = 0.0;
+		for (int a = 0; a < nvs; ++a)
+			mx = fmax(mx, fabs(sv[a]));
+		smem[e * PER_E + k] = mx;
+		if (k == 0)
+			smem[e * PER_E + 2 * NV * nvs + 1] = 0.0;   // unsafe flag
 	}
 	__syncthreads();
 	for (int it = threadIdx.x; it < n_here * nvs; it += blockDim.x) {
