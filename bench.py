@@ -166,8 +166,8 @@ def flops_per_element(d, q, nv, flux, coef_io):
 
 
 # FP64 thread-instructions (DFMA + DMUL + DADD) per element of one RK stage, from ncu
-# (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on of the volume, face and lift kernels on the 24^3 case,
-# profiles/tp_rk3_stage_hex24_p3_lf_full.md): 8.84 k + 5.67 k + 2.94 k.
+# (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on of the volume, face and lift kernels on the 24^3 p3
+# Lax-Friedrichs case, the --set full capture of one stage): 8.84 k + 5.67 k + 2.94 k.
 FP64_INSTR_PER_ELEMENT = {(3, 3, "lf"): 17450}
 
 
@@ -181,7 +181,7 @@ def fp64_issue(prob, w, stage_ms, peak_tflops):
         return {}
     rate = n * prob.n_volumes / (stage_ms * 1e-3)
     return {"instr_per_element": n, "issue_frac": rate / (peak_tflops * 1e12 / 2.0),
-            "issue_source": "ncu FP64 instruction counts per element (profiles/tp_rk3_stage_hex24_p3_lf_full.md) x "
+            "issue_source": "ncu FP64 instruction counts per element (the --set full capture of one 24^3 p3 stage) x "
                             "elements / live stage time, against the DFMA probe's instruction rate"}
 
 
@@ -394,7 +394,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": volume_traffic(prob, dom),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of tp_volume_kernel on the "
-                                       "24^3 p3 case (profiles/tp_rk3_stage_hex24_p3_lf_full.md), scaled per element",
+                                       "24^3 p3 case (the --set full capture of one stage), scaled per element",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS hbm_gbs)",
                      "algorithmic_bytes_per_launch": ab, "kernel_ms": kt},
         "fp64_pipe": {"achieved_tflops": stage_flops / (stage_ms * 1e-3) / 1e12,
