@@ -260,9 +260,10 @@ def mixed_euler(d: int = 3, n: int = 58, p_set=(1, 2, 3, 4), num_flux: int = NUM
 
 
 def mixed_advection_2d(n: int = 8, p_set=(1, 2, 3, 4), seed: int = 0, b=(1.0, 0.5), curved: bool = False,
-                       amplitude: float = 0.03) -> MixedTPProblem:
-    """Periodic [-1,1]^2, per-volume p from p_set (seeded), u0 = sin(pi x) sin(pi y), upwind flux."""
-    mesh = StructuredMesh(2, n, -1.0, 1.0)
+                       amplitude: float = 0.03, periodic=True, codes=None) -> MixedTPProblem:
+    """[-1,1]^2, per-volume p from p_set (seeded), u0 = sin(pi x) sin(pi y), upwind flux; periodic per direction
+    (all by default), codes {(dim, side): BC code} on the other ends with the exterior state u0 itself."""
+    mesh = StructuredMesh(2, n, -1.0, 1.0, periodic=periodic)
     deform = sinusoidal_deform_2d(amplitude, 2.0) if curved else None
     prob = MixedTPProblem("mixed_advection_2d", 2, PDE_ADVECTION, NUM_FLUX_UPWIND, False,
                           np.array([b[0], b[1], 0.0]), mesh, _seeded_p(mesh.n_volumes, p_set, seed),
@@ -275,6 +276,8 @@ def mixed_advection_2d(n: int = 8, p_set=(1, 2, 3, 4), seed: int = 0, b=(1.0, 0.
         prob.set_group(prob.sol, g, u[:, None, :])
     prob.dt = prob.stable_dt()
     prob.meta.update(n=n, p_set=tuple(p_set), seed=seed, curved=curved)
+    if np.any(mesh.face_vol[:, 1] < 0):
+        prob.set_boundaries(codes, lambda x: (np.sin(math.pi * x[:, 0]) * np.sin(math.pi * x[:, 1]))[:, None])
     return prob
 
 

@@ -85,6 +85,10 @@ BC_CASES = {
                                                         codes={(0, 0): 10105, (0, 1): 10106}),
     "quad_roe_box_8": lambda: M.mixed_euler(2, 8, seed=3, perturb=0.3, periodic=False,
                                             codes={(0, 0): 10101, (0, 1): 10101, (1, 0): 10102, (1, 1): 10102}),
+    # advection: inflow (b.n < 0) takes the exterior value, outflow the interior one
+    "adv_upwind_box_8": lambda: M.mixed_advection_2d(8, seed=2, curved=True, periodic=False,
+                                                     codes={(0, 0): 10041, (0, 1): 10041, (1, 0): 10001,
+                                                            (1, 1): 10011}),
 }
 
 
