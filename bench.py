@@ -772,11 +772,26 @@ def ns_measurements(torch, stream, args):
     sim.upload_state(prob.sol)
     k = 20
     ms_rhs = _timed(torch, stream, lambda: [sim.compute_rhs(want_max=False) for _ in range(k)], 1) / k
+    # end to end: dgpu_ssp_rk3_step_host on pinned buffers (a Navier-Stokes context runs upload + step + download)
+    from dpgsolver_gb300 import _lib
+    lib = _lib.load()
+    sol_h = torch.from_numpy(np.ascontiguousarray(prob.sol)).pin_memory()
+    out_h = torch.empty_like(sol_h).pin_memory()
+    sp, op = (ctypes.cast(t.data_ptr(), _lib.c_double_p) for t in (sol_h, out_h))
+
+    def e2e_step():
+        _lib.check(lib.dgpu_ssp_rk3_step_host(sim.handle, ctypes.c_double(prob.dt), sp, op, None), sim.handle)
+    e2e_step()
+    n_e2e = 10
+    ms_e2e = _timed(torch, stream, lambda: [e2e_step() for _ in range(n_e2e)], 1) / n_e2e
     sim.close()
     res = {"workload": "3D Navier-Stokes Taylor-Green vortex, Re 1600, Mach 0.1, HEX 32^3 p3, Roe-Pike + BR2",
            "n_state": prob.n_state, "steps": n, "dt": prob.dt,
            "value": 3 * prob.n_state * n / (ms * 1e-3), "unit": "DOF-residual-evals/s", "ms_per_step": ms / n,
            "rhs_value": prob.n_state / (ms_rhs * 1e-3), "rhs_ms": ms_rhs,
+           "e2e": {"value": 3 * prob.n_state / (ms_e2e * 1e-3), "unit": "DOF-residual-evals/s", "ms_per_step": ms_e2e,
+                   "h2d_bytes_per_step": int(prob.n_state * 8), "d2h_bytes_per_step": int(prob.n_state * 8),
+                   "note": "dgpu_ssp_rk3_step_host on pinned buffers (upload, graph-replayed step, download)"},
            "kinetic_energy": {"initial": kinetic_energy(prob, prob.sol), "final": kinetic_energy(prob, final)},
            "launches_per_stage": 4}
     if not args.no_cpu_baseline:
