@@ -171,6 +171,21 @@ def flops_per_element(d, q, nv, flux, coef_io):
 FP64_INSTR_PER_ELEMENT = {(3, 3, "lf"): 17450}
 
 
+def ranks_barrier(torch, world):
+    """The barrier on both sides of a timed region (replicas: the only collective of a run)."""
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def ranks_max(torch, world, ms, device):
+    """The maximum of a time over the ranks (the job's time is its slowest replica's)."""
+    if world > 1:
+        t = torch.tensor([float(ms)], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+    return ms
+
+
 def fp64_issue(prob, w, stage_ms, peak_tflops):
     """Fraction of the FP64 pipe's issue slots the live stage uses: every FP64 instruction (a division or square root
     is several) against 2 per cycle per SM, i.e. the DFMA probe's rate / 2. Known for the workloads ncu counted."""
@@ -273,15 +288,10 @@ def run_ours(args, rank, world, local_rank):
     n_rk = max(1, args.steps)
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+        ranks_barrier(torch, world)
 
     def max_over_ranks(ms):
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return ms
+        return ranks_max(torch, world, ms, "cuda")
 
     if args.only_residual:
         for _ in range(max(args.warmup, 3)):
