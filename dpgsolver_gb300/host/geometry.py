@@ -33,9 +33,47 @@ def apply_nodes(op: np.ndarray, x: np.ndarray) -> np.ndarray:
     return y.reshape((sh[0], op.shape[0]) + sh[2:])
 
 
+_QUAD_F_VE = ((0, 2), (1, 3), (0, 1), (2, 3))   # QUAD local faces -> vertices (element.c f_ve), v = a + 2 b
+
+
+def parametric_quad_nodes(X_straight: np.ndarray, x_g: np.ndarray, deform) -> np.ndarray:
+    """Geometry nodes of QUAD volumes of a parametric domain, the way the reference builds them.
+
+    compute_geom_coef_parametric_T (geometry_T.c:857-874) maps every geometry node with the domain's map, then
+    correct_internal_xyz_blended_T (geometry_blended_T.c:77-96) rebuilds the volume from its straight nodes and its
+    faces: constructor_xyz_blended_ce (:277-318) with use_existing_as_surf treats every local face b in order,
+        xyz += blend_b * (E_b (surf_b - R_b xyz)),
+    where surf_b is the mapped geometry on face b (the face's straight GLL nodes, mapped), R_b restricts volume
+    nodes to the face's nodes, E_b extends a face function constantly across the volume and blend_b is the sum of
+    face b's bilinear vertex functions (constructor_blend_values, :359-377). Each face sees the coordinates the
+    faces before it left, so the corners end on the mapped vertices.
+
+    X_straight: (nv, q^2, 2) straight (bilinear) positions at the GLL nodes x_g, first direction fastest.
+    """
+    q = len(x_g)
+    rr, ss = np.tile(x_g, q), np.repeat(x_g, q)
+    h = lambda t: np.stack([0.5 * (1.0 - t), 0.5 * (1.0 + t)], axis=1)
+    V = np.stack([h(rr)[:, v & 1] * h(ss)[:, v >> 1] for v in range(4)], axis=1)    # vertex basis at the nodes
+    X = np.array(X_straight, dtype=np.float64, copy=True)
+    nv = X.shape[0]
+    idx = np.arange(q)
+    for b in range(4):
+        # face b's nodes among the volume's: r = -1 / +1 (b = 0 / 1) or s = -1 / +1 (b = 2 / 3)
+        on_face = (idx * q + (0 if b == 0 else q - 1)) if b < 2 else ((0 if b == 2 else q - 1) * q + idx)
+        tang = ss if b < 2 else rr                          # the face coordinate of every volume node
+        E = lagrange_matrix(x_g, tang)                      # (q^2, q)
+        blend = V[:, _QUAD_F_VE[b][0]] + V[:, _QUAD_F_VE[b][1]]
+        surf = deform(X_straight[:, on_face, :].reshape(-1, 2)).reshape(nv, q, 2)
+        X = X + blend[None, :, None] * np.matmul(E, surf - X[:, on_face, :])
+    return X
+
+
 class TPGeometry:
-    def __init__(self, mesh, ops: TPOperatorSet, deform=None, curved: bool | None = None, vols=None, coef=None):
+    def __init__(self, mesh, ops: TPOperatorSet, deform=None, curved: bool | None = None, vols=None, coef=None,
+                 parametric: bool = False):
         """deform: callable (m, d) physical -> (m, d) physical applied to the affine element map, or None.
+        parametric (2D): build the mapped volumes as the reference does for a parametric domain (the map on the
+        faces, blended into the volume: parametric_quad_nodes) instead of mapping every geometry node.
         vols: indices of the volumes to compute (all volumes and their faces when None; the volume terms only
         otherwise, as for one (type, p) group of a mixed-order mesh).
         coef: the geometry coefficients themselves, (n_volumes, n_g, d) coordinates at the GLL nodes of order p_g
@@ -65,7 +103,11 @@ class TPGeometry:
             lo = mesh.vertices_lo if vols is None else mesh.vertices_lo[np.asarray(vols)]
             nv = len(lo)
             X = lo[:, None, :] + 0.5 * (xi_g[None, :, :] + 1.0) * mesh.h[None, None, :]
-            if deform is not None:
+            if deform is not None and parametric:
+                if d != 2:
+                    raise ValueError("parametric blending is built for QUAD volumes")
+                X = parametric_quad_nodes(X, x_g, deform)
+            elif deform is not None:
                 X = deform(X.reshape(-1, d)).reshape(nv, n_g, d)
         self.X_geom = X
 

@@ -173,11 +173,13 @@ def advection_2d(n: int = 16, p: int = 2, b=(1.0, 0.5), cfl: float = 0.1, n_step
 
 
 def euler_vortex_2d(n: int = 64, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, amplitude: float = 0.05,
-                    dt: float | None = None, n_steps: int = 1000) -> DGProblem:
+                    dt: float | None = None, n_steps: int = 1000, parametric: bool = True) -> DGProblem:
+    """The curved 2D vortex. parametric: the domain map applied the way the reference applies it to a parametric
+    domain (mapped faces blended into the volumes, geometry_T.c:857-874), else to every geometry node."""
     L = 10.0
     mesh = StructuredMesh(2, n, 0.0, L)
     ops = TPOperatorSet(mesh.e_type, p)
-    geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_2d(amplitude, L), curved=True)
+    geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_2d(amplitude, L), curved=True, parametric=parametric)
     prob = DGProblem("euler_vortex_2d", 2, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
                      sol=np.zeros((mesh.n_volumes, 4, ops.n_vs)), dt=0.0, n_steps=n_steps)
     xyz = prob.solution_node_xyz()

@@ -1,0 +1,272 @@
+"""The reference's own 2D explicit-DG code, compiled into ``oracle/_ref`` by ``oracle/ref/Makefile`` (TEST
+INFRASTRUCTURE ONLY: it pins the oracle and the kernels to residuals the reference itself computes; nothing on the
+product path imports it).
+
+``build(ref_dir)`` compiles the reference's ``src/`` tree where it lies, with the stand-ins of ``oracle/ref/shim``;
+``run_case(...)`` writes a control file, the test case's ``test_case.data`` / ``solution.data`` and a gmsh 2.2 mesh
+under ``oracle/_ref/run/input`` (the input directory compiled into the build), runs ``dpg_ref_harness`` and reads
+back what it wrote: the volume and face lists in the reference's own order with their geometry, and, given a state,
+``compute_rhs`` and the SSP-RK3 steps of ``time_step_ssp_rk_33``.
+
+The reference cannot travel to the GPU machine (it is built here, for this host, from the reference's sources), so the
+GPU tests use fixtures generated from it by ``tests/golden/make_ref_golden.py``.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+REF_OUT = os.path.join(_HERE, "_ref")
+HARNESS = os.path.join(REF_OUT, "dpg_ref_harness")
+RUN_DIR = os.path.join(REF_OUT, "run")
+INPUT_DIR = os.path.join(RUN_DIR, "input")
+
+
+def available() -> bool:
+    return os.path.exists(HARNESS)
+
+
+def build(ref_dir: str, jobs: int | None = None) -> str:
+    """Compile oracle/_ref/dpg_ref_harness from the reference checkout at ref_dir."""
+    jobs = jobs or max(1, os.cpu_count() or 1)
+    subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "ref"), f"REF={ref_dir}", f"-j{jobs}"], check=True)
+    return HARNESS
+
+
+_CTRL = """pde_name  {pde_name}
+pde_spec  {pde_spec}
+
+geom_name n-cube
+geom_spec NONE
+
+dimension 2
+
+mesh_generator   n-cube/2d.geo
+mesh_format      gmsh
+mesh_domain      {domain}
+mesh_type        quad
+mesh_level       0 0
+mesh_path        {mesh}
+
+interp_tp  GLL
+interp_si  AO
+interp_pyr GLL
+
+basis_geom  bezier
+basis_sol   lagrange
+
+geom_representation  isoparametric
+geom_blending_tp     gordon_hall
+geom_blending_si     szabo_babuska_gen
+
+p_ref    {p} {p}
+
+fe_method 1
+"""
+
+_TEST_CASE = """solver_proc   explicit
+solver_type_e ssp_rk_33
+
+num_flux_1st {num_flux}
+
+time_step  {dt!r}
+time_final {t_final!r}
+
+display_progress 0
+"""
+
+# The reference's own spelling of the numerical fluxes in test_case.data (test_case_T.c:277 converts them).
+NUM_FLUX_NAMES = {11: "upwind", 31: "Roe-Pike", 32: "Lax-Friedrichs"}
+
+
+def _write(path: str, text: str) -> None:
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "w") as fh:
+        fh.write(text)
+
+
+def _read_bin(path: str) -> np.ndarray:
+    return np.fromfile(path, dtype=np.float64)
+
+
+def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux: int, state_fn=None,
+             steps: int = 0, dt: float = 0.0, map_amplitude: float = 0.0, b_adv=(1.0, 0.5)) -> dict:
+    """Set up a periodic n x n QUAD mesh of [lo, hi]^2 at order p in the reference and run it.
+
+    pde: "advection" (upwind, b_adv) or "euler". map_amplitude > 0 makes the domain parametric with the map
+    x, y += A sin(2 pi x / (hi - lo)) sin(2 pi y / (hi - lo)). state_fn(xyz_vs) -> (n_vs, n_var) gives the initial
+    nodal state of a volume from its solution-node coordinates (GLL Lagrange coefficients are nodal values); with
+    it the reference's compute_rhs and ``steps`` SSP-RK3 steps of size dt are run.
+    """
+    from dpgsolver_gb300.host.gmsh import write_box_msh
+
+    if not available():
+        raise RuntimeError("oracle/_ref is not built")
+    ctrl_name = f"TEST_ref_{name}"
+    case_dir = os.path.join(RUN_DIR, name)
+    os.makedirs(case_dir, exist_ok=True)
+    mesh = os.path.join(case_dir, "mesh.msh")
+    write_box_msh(mesh, 2, n, lo=lo, hi=hi, periodic=True)
+    if pde == "advection":
+        pde_spec = "steady/free_stream"
+        solution = f"advection_type constant\nb_adv   {b_adv[0]!r} {b_adv[1]!r} 0.0\n"
+    elif pde == "euler":
+        pde_spec = "periodic/periodic_vortex"
+        solution = ("r_v   0.165\ntheta 0.7853981633974483\nV_inf 0.5916079783099616\np_inf 1.0\nt_inf 1.0\n"
+                    "Rg    1.0\n\np_frac 0.05\n")
+    else:
+        raise ValueError(pde)
+    domain = "parametric" if map_amplitude else "straight"
+    _write(os.path.join(INPUT_DIR, "testing", "control_files", ctrl_name + ".ctrl"),
+           _CTRL.format(pde_name=pde, pde_spec=pde_spec, domain=domain, mesh=mesh, p=p))
+    data_dir = os.path.join(INPUT_DIR, "input_files", pde, pde_spec)
+    _write(os.path.join(data_dir, "test_case.data"),
+           _TEST_CASE.format(num_flux=NUM_FLUX_NAMES[num_flux], dt=float(dt or 1e-3),
+                             t_final=float((dt or 1e-3) * max(steps, 1))))
+    _write(os.path.join(data_dir, "solution.data"), solution)
+
+    args = [HARNESS, ctrl_name, case_dir]
+    if map_amplitude:
+        args += ["--map", repr(float(map_amplitude)), repr(float(hi - lo))]
+    subprocess.run(args, check=True, cwd=case_dir, stdout=subprocess.DEVNULL)
+    out = _read_outputs(case_dir)
+    if state_fn is not None:
+        sol = np.concatenate([np.asarray(state_fn(x), dtype=np.float64).reshape(x.shape[0], -1).T.ravel()
+                              for x in out["xyz_vs"]])
+        sol.tofile(os.path.join(case_dir, "sol_in.bin"))
+        args += ["--state", os.path.join(case_dir, "sol_in.bin")]
+        if steps:
+            args += ["--steps", str(int(steps)), "--dt", repr(float(dt))]
+        subprocess.run(args, check=True, cwd=case_dir, stdout=subprocess.DEVNULL)
+        out.update(_read_outputs(case_dir))
+        out["sol_in"] = sol
+        n_var = sol.size // sum(x.shape[0] for x in out["xyz_vs"])
+        out["n_var"] = n_var
+        out["rhs"] = _read_bin(os.path.join(case_dir, "rhs.bin"))
+        mx = np.loadtxt(os.path.join(case_dir, "max_rhs.txt"), ndmin=1)
+        out["max_rhs"] = float(mx[0])
+        if steps:
+            out["max_rhs_steps"] = mx[1:]
+            out["sol_steps"] = _read_bin(os.path.join(case_dir, "sol_steps.bin"))
+    return out
+
+
+def _read_outputs(case_dir: str) -> dict:
+    vols = np.loadtxt(os.path.join(case_dir, "volumes.txt"), dtype=np.int64, ndmin=2)
+    faces = np.loadtxt(os.path.join(case_dir, "faces.txt"), dtype=np.int64, ndmin=2)
+    d = 2
+    n_vs, n_vc, n_ve = vols[:, 4], vols[:, 5], vols[:, 6]
+
+    def split(arr, sizes):
+        return np.split(arr, np.cumsum(sizes)[:-1])
+
+    def cols(blocks, sizes, k):
+        # column-major (n, k) blocks -> list of (n, k) arrays
+        return [b.reshape(k, n).T for b, n in zip(blocks, sizes)]
+
+    xyz_ve = cols(split(_read_bin(os.path.join(case_dir, "xyz_ve.bin")), n_ve * d), n_ve, d)
+    xyz_vs = cols(split(_read_bin(os.path.join(case_dir, "xyz_vs.bin")), n_vs * d), n_vs, d)
+    met = split(_read_bin(os.path.join(case_dir, "metrics_vc.bin")), n_vc * d * d)
+    # metrics_vc (n_vc, d, d) column-major: entry (n, i, j) at n + n_vc (i + d j)
+    metrics = [m.reshape(d, d, nc).transpose(2, 1, 0) for m, nc in zip(met, n_vc)]
+    jac = split(_read_bin(os.path.join(case_dir, "jacobian_det_vc.bin")), n_vc)
+    n_fc = faces[:, 3]
+    # normals_fc is the reference's one row-major ('R') face multiarray (face_solver_T.h:56)
+    normals = [b.reshape(nf, d) for b, nf in zip(split(_read_bin(os.path.join(case_dir, "normals_fc.bin")), n_fc * d),
+                                                  n_fc)]
+    jac_f = split(_read_bin(os.path.join(case_dir, "jacobian_det_fc.bin")), n_fc)
+    xyz_fc = cols(split(_read_bin(os.path.join(case_dir, "xyz_fc.bin")), n_fc * d), n_fc, d)
+    return dict(volumes=vols, faces=faces, xyz_ve=xyz_ve, xyz_vs=xyz_vs, metrics_vc=metrics, jacobian_det_vc=jac,
+                normals_fc=normals, jacobian_det_fc=jac_f, xyz_fc=xyz_fc)
+
+
+# ------------------------------------------------------------------------------------------------------------------
+# The parity cases run through the reference, and their counterparts built by the repo's own host set-up.
+
+def _advection_state(x):
+    return np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1])
+
+
+def _vortex_state(x):
+    from dpgsolver_gb300.host.problem import isentropic_vortex, primitive_to_conserved
+    rho, u, v, pr = isentropic_vortex(x, 5.0, 5.0, 5.0)
+    return np.asarray(primitive_to_conserved(2, rho, np.stack([u, v]), pr)).T
+
+
+# name -> (pde, n, p, numerical flux, RK steps). "c1" is the linear-advection configuration at its stated size
+# (QUAD 16^2 on [-1,1]^2, p = 2, b = (1, 0.5), upwind, u0 = sin(pi x) sin(pi y), dt = 0.1 h / |b|, 100 steps);
+# the "c2*" cases are the curved isentropic-vortex configuration (QUAD on [0,10]^2 mapped by
+# 0.05 sin(pi x/5) sin(pi y/5), vortex strength 5 at (5,5) on (1,1,1,1)) on smaller meshes and other fluxes and
+# orders; "c2" itself (64^2, p = 3, Roe) is run live by the CPU tests.
+CASES = {
+    "c1": ("advection", 16, 2, 11, 100),
+    "c2_n8": ("euler", 8, 3, 31, 1000),
+    "c2_lf_n8": ("euler", 8, 3, 32, 20),
+    "c2_p1_n8": ("euler", 8, 1, 32, 20),
+    "c2_p4_n4": ("euler", 4, 4, 31, 20),
+    "c2": ("euler", 64, 3, 31, 10),
+}
+
+
+def host_problem(name: str):
+    """The repo's own host set-up of a case (mesh, operators, geometry, state, dt)."""
+    from dpgsolver_gb300.host import problem as P
+    pde, n, p, flux, steps = CASES[name]
+    if pde == "advection":
+        return P.advection_2d(n, p)
+    return P.euler_vortex_2d(n=n, p=p, num_flux=flux)
+
+
+def run_named(name: str) -> dict:
+    """Run a case through the reference with the host problem's dt; returns run_case's dictionary."""
+    pde, n, p, flux, steps = CASES[name]
+    prob = host_problem(name)
+    if pde == "advection":
+        return run_case(name, pde, n, p, -1.0, 1.0, flux, state_fn=_advection_state, steps=steps, dt=prob.dt)
+    return run_case(name, pde, n, p, 0.0, 10.0, flux, state_fn=_vortex_state, steps=steps, dt=prob.dt,
+                    map_amplitude=0.05)
+
+
+def to_arrays(out: dict) -> dict:
+    """The reference's run in the host problem's layouts (what the golden fixtures store)."""
+    nv = len(out["xyz_vs"])
+    n_var = out.get("n_var", 1)
+    res = dict(
+        xyz_vs=np.stack(out["xyz_vs"]),
+        metrics_vc=np.stack(out["metrics_vc"]),
+        jacobian_det_vc=np.stack(out["jacobian_det_vc"]),
+        normals_fc=np.stack(out["normals_fc"]),
+        jacobian_det_fc=np.stack(out["jacobian_det_fc"]),
+        face_vol=out["faces"][:, [4, 7]].astype(np.int32),
+        face_lf=out["faces"][:, [5, 8]].astype(np.int32),
+        face_ord=out["faces"][:, [6, 9]].astype(np.int32),
+    )
+    if "sol_in" in out:
+        res.update(sol_in=out["sol_in"].reshape(nv, n_var, -1), rhs=out["rhs"].reshape(nv, n_var, -1),
+                   max_rhs=np.float64(out["max_rhs"]))
+    if "sol_steps" in out:
+        res.update(sol_steps=out["sol_steps"].reshape(nv, n_var, -1), max_rhs_steps=out["max_rhs_steps"])
+    return res
+
+
+def with_reference_inputs(prob, ref: dict):
+    """Give the host problem the reference's own geometry and initial state: what a caller packing the reference's
+    Solver_Volume / Solver_Face lists would pass. Checks first that both list the same volumes (solution nodes within
+    1e-12) and faces (volumes and local faces per side, identity face-node orders) in the same order."""
+    xyz = prob.solution_node_xyz()
+    if np.abs(xyz - ref["xyz_vs"]).max() > 1e-12:
+        raise AssertionError("volume lists differ")
+    if not (np.array_equal(prob.mesh.face_vol, ref["face_vol"]) and np.array_equal(prob.mesh.face_lf, ref["face_lf"])
+            and not np.any(ref["face_ord"])):
+        raise AssertionError("face lists differ")
+    g = prob.geom
+    g.metrics_vc = np.array(ref["metrics_vc"], dtype=np.float64)
+    g.jacobian_det_vc = np.array(ref["jacobian_det_vc"], dtype=np.float64)
+    g.normals_fc = np.array(ref["normals_fc"], dtype=np.float64)
+    g.jacobian_det_fc = np.array(ref["jacobian_det_fc"], dtype=np.float64)
+    if "sol_in" in ref:
+        prob.sol = np.array(ref["sol_in"], dtype=np.float64)
+    return prob

@@ -2,7 +2,7 @@
 
 Run once where the reference tree is mounted (it is not needed afterwards):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the reference checkout>
 
 Sources (read as text, values copied verbatim):
   input/testing/unit/operators/operators_tp.data  -- test_unit_operators_tp.c:56-170 (TP op_std assembly and
@@ -134,4 +134,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])

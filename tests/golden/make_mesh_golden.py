@@ -2,7 +2,7 @@
 
 Run once where the reference tree is mounted (it is not needed afterwards):
 
-    python tests/golden/make_mesh_golden.py /root/reference
+    python tests/golden/make_mesh_golden.py <path of the reference checkout>
 
 Sources (read as text, values copied verbatim): input/testing/integration/mesh/<name>.msh, the gmsh files the
 reference's test_integration_mesh.c reads, and <name>.msh.data, the Mesh_Data, Mesh_Connectivity and
@@ -71,4 +71,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])

@@ -1,0 +1,138 @@
+"""The oracle and the host set-up against outputs of the reference itself (its own compute_rhs and
+time_step_ssp_rk_33, compiled from its sources into oracle/_ref).
+
+* Golden fixtures (tests/golden/reference_*.npz, made by tests/golden/make_ref_golden.py) hold the reference's
+  residual and RK states on the 2D configurations: the advection case at its stated size (QUAD 16^2, p = 2, 100
+  steps) and the curved Euler vortex on 8^2 / 4^2 meshes (Roe and Lax-Friedrichs, p = 1, 3, 4; 1000 Roe steps).
+  The oracle, given the reference's geometry and state, must reproduce them to 1e-12; the repo's own geometry must
+  reproduce the reference's to 1e-13.
+* Where oracle/_ref is built (the reference tree is present), the full-size vortex (QUAD 64^2, p = 3, Roe) is run
+  live: residual, ten RK steps and geometry.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import oracle.reference as R
+
+FIXTURE_CASES = [c for c in R.CASES if c != "c2"]
+
+
+def _fixture(name):
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", f"reference_{name}.npz")
+    return dict(np.load(path))
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("name", FIXTURE_CASES)
+def test_oracle_residual_matches_reference_fixture(name):
+    ref = _fixture(name)
+    prob = R.with_reference_inputs(R.host_problem(name), ref)
+    r, mx = oracle.Oracle(prob).compute_rhs(prob.sol)
+    assert _rel(r, ref["rhs"]) <= 1e-12
+    assert abs(mx - float(ref["max_rhs"])) <= 1e-12 * float(ref["max_rhs"])
+
+
+@pytest.mark.parametrize("name", FIXTURE_CASES)
+def test_oracle_rk3_steps_match_reference_fixture(name):
+    ref = _fixture(name)
+    prob = R.with_reference_inputs(R.host_problem(name), ref)
+    assert float(ref["dt"]) == prob.dt
+    o = oracle.Oracle(prob)
+    s = prob.sol.copy()
+    mxs = []
+    for _ in range(int(ref["steps"])):
+        s, mx, _ = o.ssp_rk3_step(s, prob.dt)
+        mxs.append(mx)
+    assert _rel(s, ref["sol_steps"]) <= 1e-12
+    assert np.max(np.abs(np.array(mxs) - ref["max_rhs_steps"]) / ref["max_rhs_steps"]) <= 1e-10
+
+
+@pytest.mark.parametrize("name", FIXTURE_CASES)
+def test_host_geometry_matches_reference_fixture(name):
+    """The repo's own set-up (mesh order, node coordinates, metric terms, normals, Jacobians) is the reference's."""
+    ref = _fixture(name)
+    prob = R.host_problem(name)
+    g = prob.geom
+    assert np.array_equal(prob.mesh.face_vol, ref["face_vol"]) and np.array_equal(prob.mesh.face_lf, ref["face_lf"])
+    assert np.max(np.abs(prob.solution_node_xyz() - ref["xyz_vs"])) <= 1e-13 * np.max(np.abs(ref["xyz_vs"]))
+    for key in ("metrics_vc", "jacobian_det_vc", "normals_fc", "jacobian_det_fc"):
+        assert _rel(getattr(g, key), ref[key]) <= 1e-13, key
+
+
+def test_reference_fixture_state_is_the_host_state():
+    """The fixtures' initial states are the host problems' own states (the same formula at the same nodes)."""
+    for name in FIXTURE_CASES:
+        ref = _fixture(name)
+        prob = R.host_problem(name)
+        assert _rel(prob.sol, ref["sol_in"]) <= 1e-13, name
+
+
+live = pytest.mark.skipif(not R.available(), reason="oracle/_ref is built only where the reference tree is present")
+
+
+@pytest.fixture(scope="module")
+def c2_live():
+    return R.to_arrays(R.run_named("c2"))
+
+
+@live
+def test_live_c1_at_stated_size():
+    """The advection configuration: residual and the state after its 100 SSP-RK3 steps."""
+    ref = R.to_arrays(R.run_named("c1"))
+    prob = R.with_reference_inputs(R.host_problem("c1"), ref)
+    o = oracle.Oracle(prob)
+    r, _ = o.compute_rhs(prob.sol)
+    assert _rel(r, ref["rhs"]) <= 1e-12
+    s = prob.sol.copy()
+    for _ in range(100):
+        s, _, _ = o.ssp_rk3_step(s, prob.dt)
+    assert _rel(s, ref["sol_steps"]) <= 1e-12
+
+
+@live
+def test_live_c2_residual_at_stated_size(c2_live):
+    """Curved vortex, QUAD 64^2, p = 3, Roe-Pike. At this size the residual is the difference of flux terms about
+    10^3 times larger, and the reference's own residual moves by about 1e-12 (normwise) when its input state moves
+    by one ulp. The bar is therefore 1e-12 or twice that floor, measured here on the reference itself."""
+    ref = c2_live
+    prob = R.with_reference_inputs(R.host_problem("c2"), ref)
+    r, mx = oracle.Oracle(prob).compute_rhs(prob.sol)
+    rng = np.random.default_rng(1)
+
+    def state_ulp(x):
+        s = R._vortex_state(x)
+        return s * (1.0 + 2.0 ** -52 * rng.choice([-1.0, 1.0], size=s.shape))
+    pde, n, p, flux, _ = R.CASES["c2"]
+    ref_ulp = R.run_case("c2_ulp", pde, n, p, 0.0, 10.0, flux, state_fn=state_ulp, map_amplitude=0.05)
+    floor = _rel(ref_ulp["rhs"].reshape(ref["rhs"].shape), ref["rhs"])
+    err = _rel(r, ref["rhs"])
+    assert err <= max(1e-12, 2.0 * floor), (err, floor)
+    assert abs(mx - float(ref["max_rhs"])) <= 1e-12 * float(ref["max_rhs"])
+
+
+@live
+def test_live_c2_rk3_steps_at_stated_size(c2_live):
+    ref = c2_live
+    prob = R.with_reference_inputs(R.host_problem("c2"), ref)
+    o = oracle.Oracle(prob)
+    s = prob.sol.copy()
+    for _ in range(R.CASES["c2"][4]):
+        s, _, _ = o.ssp_rk3_step(s, prob.dt)
+    assert _rel(s, ref["sol_steps"]) <= 1e-12
+
+
+@live
+def test_live_c2_host_geometry_at_stated_size(c2_live):
+    """The metric terms are derivatives of coordinates up to 10 over volumes 0.16 wide: one ulp of a coordinate is
+    3e-14 of a metric term, so the bar for them is 1e-12 here (node coordinates stay at 1e-13)."""
+    ref = c2_live
+    prob = R.host_problem("c2")
+    g = prob.geom
+    assert np.max(np.abs(prob.solution_node_xyz() - ref["xyz_vs"])) <= 1e-13 * np.max(np.abs(ref["xyz_vs"]))
+    for key in ("metrics_vc", "jacobian_det_vc", "normals_fc", "jacobian_det_fc"):
+        assert _rel(getattr(g, key), ref[key]) <= 1e-12, key
