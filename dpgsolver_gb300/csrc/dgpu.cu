@@ -54,6 +54,12 @@ struct dgpu_ctx {
 	double *jv_du = nullptr, *jv_vol = nullptr, *jv_traces = nullptr, *jv_nnf = nullptr, *jv_out = nullptr;
 	// block-sparse Jacobian (built on first use): block rows, colouring, block slot of (volume, colour)
 	std::vector<int> h_face_vol;          // host copy of face_vol
+	// element partition (face sides of other ranks' volumes, DGPU_REMOTE_VOLUME): the halo plan of dgpu_halo_setup
+	int n_remote = 0;                     // face sides whose volume belongs to another rank
+	int n_halo = 0;                       // trace slots exchanged per stage
+	int *halo_send = nullptr, *halo_recv = nullptr;   // slots 2f+s: the local side of a cut face / its remote side
+	double *halo_sbuf = nullptr, *halo_rbuf = nullptr;   // n_halo x (nv x NF): what is sent / what arrives
+	bool halo_recv_ready = false;
 	int jac_colours = 0;
 	std::vector<int> jac_row_ptr, jac_col_idx, jac_members_off;
 	int *jac_slot = nullptr, *jac_members = nullptr;
@@ -654,7 +660,7 @@ void free_all(dgpu_ctx* c)
 		cudaEventDestroy(t.stop);
 	}
 	c->timers.clear();
-	void* ptrs[] = {c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
+	void* ptrs[] = {c->halo_send, c->halo_recv, c->halo_sbuf, c->halo_rbuf, c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
 	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X, c->ns_gv, c->ns_gtr_d, c->ns_X_d, c->ns_gv_d,
 	                c->bnd, c->bc_code, c->bc_ext, c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
@@ -850,6 +856,45 @@ dgpu_status read_max(dgpu_ctx* c, double* max_rhs)
 	return DGPU_OK;
 }
 
+// Entry points that evaluate the whole mesh refuse a partitioned context: its remote traces come only from the
+// dgpu_halo_* calls.
+#define DGPU_WHOLE_MESH(c)                                                                                        \
+	do {                                                                                                          \
+		if ((c) && (c)->n_remote > 0)                                                                             \
+			return fail((c), DGPU_ERR_INVALID_ARGUMENT,                                                           \
+			            "partitioned context: evaluate it with dgpu_halo_stage_begin / dgpu_halo_stage_end");       \
+	} while (0)
+
+// Copies trace slots between the trace array and a halo buffer: pack reads traces[slot] into buf[i], unpack writes
+// buf[i] into traces[slot]. One thread per double; a slot is nv x NF contiguous doubles of [f][side][var][node].
+__global__ void halo_copy_kernel(double* __restrict__ traces, double* __restrict__ buf, const int* __restrict__ slots,
+                                 int n, int slot_doubles, int pack)
+{
+	const long long total = (long long)n * slot_doubles;
+	for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+	     idx += (long long)gridDim.x * blockDim.x) {
+		const long long i = idx / slot_doubles;
+		const long long t = (long long)slots[i] * slot_doubles + (idx - i * slot_doubles);
+		if (pack)
+			buf[idx] = traces[t];
+		else
+			traces[t] = buf[idx];
+	}
+}
+
+cudaError_t launch_halo_copy(dgpu_ctx* c, bool pack)
+{
+	if (c->n_halo == 0)
+		return cudaSuccess;
+	const int slot = c->nv * c->NF;
+	const long long total = (long long)c->n_halo * slot;
+	const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 8);
+	halo_copy_kernel<<<blocks, 256, 0, c->stream>>>(c->traces, pack ? c->halo_sbuf : c->halo_rbuf,
+	                                                 pack ? c->halo_send : c->halo_recv, c->n_halo, slot, pack ? 1 : 0);
+	c->launches++;
+	return cudaGetLastError();
+}
+
 dgpu_status check_positivity_flag(dgpu_ctx* c)
 {
 	if (!c->positivity)
@@ -1018,9 +1063,20 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 	// boundary faces: side 1 absent; their BC code and exterior state, compacted to the boundary list
 	std::vector<int> bnd(nF, -1), bc_code;
 	std::vector<double> bc_ext;
+	int n_remote = 0;
 	for (size_t f = 0; f < nF; ++f) {
-		const bool boundary = mesh->face_vol[2 * f + 1] < 0;
+		const bool rem0 = mesh->face_vol[2 * f] == DGPU_REMOTE_VOLUME;
+		const bool rem1 = mesh->face_vol[2 * f + 1] == DGPU_REMOTE_VOLUME;
+		if (rem0 && rem1) {
+			delete c;
+			return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "a face with both sides on other ranks");
+		}
+		const bool boundary = mesh->face_vol[2 * f + 1] < 0 && !rem1;
 		for (int s = 0; s < (boundary ? 1 : 2); ++s) {
+			if ((s == 0 && rem0) || (s == 1 && rem1)) {   // the other rank's side: its trace arrives by exchange
+				++n_remote;
+				continue;
+			}
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
 			if (v < 0 || v >= c->n_vol || lf < 0 || lf >= 2 * d || vol_face[(size_t)v * 2 * d + lf] != -1) {
 				delete c;
@@ -1070,6 +1126,11 @@ dgpu_status dgpu_create(const dgpu_physics* phys, const dgpu_tp_operators* ops, 
 		}
 	}
 	c->h_face_vol.assign(mesh->face_vol, mesh->face_vol + 2 * nF);
+	c->n_remote = n_remote;
+	if (n_remote > 0 && c->ns) {
+		delete c;
+		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "partitioned meshes: Euler and advection only");
+	}
 	for (size_t i = 0; i < vol_face.size(); ++i)
 		if (vol_face[i] < 0) {
 			delete c;
@@ -1252,6 +1313,7 @@ dgpu_status dgpu_download_rhs(dgpu_ctx* c, double* rhs)
 
 dgpu_status dgpu_compute_rhs(dgpu_ctx* c, double* max_rhs)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	dgpu_status st = ensure_coef(c);
@@ -1265,6 +1327,7 @@ dgpu_status dgpu_compute_rhs(dgpu_ctx* c, double* max_rhs)
 
 dgpu_status dgpu_compute_rhs_host(dgpu_ctx* c, const double* sol, double* rhs, double* max_rhs)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || !sol || !rhs)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	const size_t bytes = state_size(c) * sizeof(double);
@@ -1308,6 +1371,7 @@ static dgpu_status capture_step(dgpu_ctx* c, double dt, bool want_max, cudaGraph
 
 dgpu_status dgpu_ssp_rk3_steps(dgpu_ctx* c, double dt, int n_steps, double* max_rhs)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || n_steps < 0 || !(dt == dt))
 		return DGPU_ERR_INVALID_ARGUMENT;
 	dgpu_status st = ensure_gl(c);
@@ -1369,6 +1433,7 @@ static dgpu_status enqueue_rk_step_host(dgpu_ctx* c, double dt, bool want_max, c
 
 dgpu_status dgpu_ssp_rk3_step_host(dgpu_ctx* c, double dt, const double* sol_in, double* sol_out, double* max_rhs)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || !sol_in || !sol_out || !(dt == dt))
 		return DGPU_ERR_INVALID_ARGUMENT;
 	if (!c->launch_volume_in || !c->launch_lift_out || c->timing) {   // Navier-Stokes, or per-kernel timing
@@ -1645,7 +1710,7 @@ __global__ void noalloc_pack_volumes(const NoallocWeights W, int n_vol, const do
 }
 
 // Face data, connectivity (vol_face) and the inverse right-trace permutation, with bounds checks: an entry
-// outside the mesh raises the error flag and is skipped.
+// outside the mesh, or a (volume, local face) claimed by two face sides, raises the error flag and is skipped.
 template <int D, int Q>
 __global__ void noalloc_pack_faces(const NoallocWeights W, int n_vol, int n_face, const int* __restrict__ face_vol,
                                    const int* __restrict__ face_lf, const int* __restrict__ nc,
@@ -1668,7 +1733,9 @@ __global__ void noalloc_pack_faces(const NoallocWeights W, int n_vol, int n_face
 				atomicExch(err, 1);
 				continue;
 			}
-			vol_face[(size_t)v * 2 * D + lf] = (int)(2 * f + s);
+			// each (volume, local face) belongs to exactly one face side: a second claim is a bad mesh
+			if (atomicCAS(&vol_face[(size_t)v * 2 * D + lf], -1, (int)(2 * f + s)) != -1)
+				atomicExch(err, 1);
 		}
 	}
 	if (nc) {
@@ -1721,7 +1788,8 @@ cudaError_t noalloc_pack_q(int q, const NoallocWeights& W, const dgpu_mesh* m, d
 
 size_t round_up_256(size_t doubles) { return (doubles + 31) / 32 * 32; }
 
-bool is_device_pointer(const void* p)
+// Device memory of device `dev` (managed memory of any device is reachable from every device).
+bool is_device_pointer(const void* p, int dev)
 {
 	if (!p)
 		return false;
@@ -1730,8 +1798,12 @@ bool is_device_pointer(const void* p)
 		cudaGetLastError();
 		return false;
 	}
-	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+	return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev);
 }
+
+// Per device: 0 = not checked yet, 1 = compute capability 10.3, -1 = another device. Read once per device with
+// cudaDeviceGetAttribute (cudaGetDeviceProperties fills the whole property struct, far slower).
+signed char g_noalloc_cc[kMaxDevices];
 
 }  // namespace
 
@@ -1764,11 +1836,16 @@ extern "C" dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const 
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "empty mesh");
 	if (d_mesh->bc_fc || d_mesh->bc_state_fc || d_mesh->bc_data)
 		return fail(nullptr, DGPU_ERR_UNSUPPORTED, "boundary faces are not supported here (use dgpu_create)");
-	if (!is_device_pointer(d_sol) || !is_device_pointer(d_rhs) || !is_device_pointer(d_mesh->metrics_vc) ||
-	    !is_device_pointer(d_mesh->jacobian_det_vc) || !is_device_pointer(d_mesh->face_vol) ||
-	    !is_device_pointer(d_mesh->face_lf) || !is_device_pointer(d_mesh->normals_fc) ||
-	    !is_device_pointer(d_mesh->jacobian_det_fc) || (d_mesh->nc_fc && !is_device_pointer(d_mesh->nc_fc)))
-		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "state, residual and mesh arrays must be device memory");
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+		return fail(nullptr, DGPU_ERR_NO_DEVICE, "no current CUDA device");
+	if (!is_device_pointer(d_sol, dev) || !is_device_pointer(d_rhs, dev) ||
+	    !is_device_pointer(d_mesh->metrics_vc, dev) || !is_device_pointer(d_mesh->jacobian_det_vc, dev) ||
+	    !is_device_pointer(d_mesh->face_vol, dev) || !is_device_pointer(d_mesh->face_lf, dev) ||
+	    !is_device_pointer(d_mesh->normals_fc, dev) || !is_device_pointer(d_mesh->jacobian_det_fc, dev) ||
+	    (d_mesh->nc_fc && !is_device_pointer(d_mesh->nc_fc, dev)))
+		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT,
+		            "state, residual and mesh arrays must be device memory of the current device");
 
 	const int q = ops->p + 1;
 	const int N = (d == 2 ? q * q : q * q * q), NF = (d == 2 ? q : q * q);
@@ -1793,12 +1870,16 @@ extern "C" dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const 
 		return fail(nullptr, DGPU_ERR_INVALID_ARGUMENT, msg);
 	}
 
-	// set-up once per device, with that device current: the device address of the scratch array
-	int dev = 0;
-	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-		return fail(nullptr, DGPU_ERR_NO_DEVICE, "no current CUDA device");
-	cudaDeviceProp prop;
-	if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess || prop.major * 10 + prop.minor != 103)
+	// set-up once per device, with that device current: its compute capability and the device address of the
+	// scratch array
+	if (!g_noalloc_cc[dev]) {
+		int major = 0, minor = 0;
+		if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+		    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
+			return fail(nullptr, DGPU_ERR_NO_DEVICE, "cannot read the device's compute capability");
+		g_noalloc_cc[dev] = (major * 10 + minor == 103) ? 1 : -1;
+	}
+	if (g_noalloc_cc[dev] != 1)
 		return fail(nullptr, DGPU_ERR_NO_DEVICE, "device is not compute capability 10.3 (sm_103a build)");
 	if (!g_noalloc_ptr[dev]) {
 		double* p = nullptr;
@@ -2029,6 +2110,7 @@ dgpu_status jacobian_setup(dgpu_ctx* c)
 
 extern "C" dgpu_status dgpu_jacobian_structure(dgpu_ctx* c, int* block_size, long long* n_blocks, int* n_colours)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	const dgpu_status st = jacobian_setup(c);
@@ -2046,6 +2128,7 @@ extern "C" dgpu_status dgpu_jacobian_structure(dgpu_ctx* c, int* block_size, lon
 extern "C" dgpu_status dgpu_jacobian_bsr(dgpu_ctx* c, const double* sol, int raw, int* row_ptr, int* col_idx,
                                          double* values)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	dgpu_status st = jacobian_setup(c);
@@ -2116,6 +2199,7 @@ extern "C" dgpu_status dgpu_jacobian_bsr(dgpu_ctx* c, const double* sol, int raw
 
 extern "C" dgpu_status dgpu_jvp(dgpu_ctx* c, const double* sol, const double* dir, double* rhs, double* jv)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || !sol || !dir || !jv)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	const size_t ns = state_size(c);
@@ -2139,6 +2223,7 @@ extern "C" dgpu_status dgpu_jvp(dgpu_ctx* c, const double* sol, const double* di
 
 extern "C" dgpu_status dgpu_vjp_forward(dgpu_ctx* c, const double* sol, double* rhs, double* max_rhs)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	if (c->ns)
@@ -2164,6 +2249,7 @@ extern "C" dgpu_status dgpu_vjp_forward(dgpu_ctx* c, const double* sol, double* 
 
 extern "C" dgpu_status dgpu_vjp_backward(dgpu_ctx* c, const double* cotangent, double* grad_sol)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || !cotangent || !grad_sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	if (c->ns)
@@ -2183,6 +2269,7 @@ extern "C" dgpu_status dgpu_vjp_backward(dgpu_ctx* c, const double* cotangent, d
 // ---------------------------------------------------------------------------------------------------------------
 extern "C" dgpu_status dgpu_set_objective_faces(dgpu_ctx* c, int n_faces, const int* faces)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || n_faces < 1 || !faces)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	if (c->ns)
@@ -2273,6 +2360,7 @@ struct DeviceBlock {
 
 extern "C" dgpu_status dgpu_objective(dgpu_ctx* c, const double* sol, double* J, double* dJ_dsol)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || !sol || !J)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	if (c->ns)
@@ -2292,6 +2380,7 @@ extern "C" dgpu_status dgpu_objective(dgpu_ctx* c, const double* sol, double* J,
 extern "C" dgpu_status dgpu_adjoint_ssp_rk3(dgpu_ctx* c, double dt, int n_steps, size_t budget_bytes,
                                             const double* sol0, double* J, double* dJ_dsol0, int* segment_out)
 {
+	DGPU_WHOLE_MESH(c);
 	if (!c || n_steps < 1 || !sol0 || !J || !dJ_dsol0 || !(dt == dt))
 		return DGPU_ERR_INVALID_ARGUMENT;
 	if (c->ns)
@@ -2505,3 +2594,134 @@ extern "C" dgpu_status dgpu_blend_geometry(int d, int p_g, int n_volumes, const 
 		return cuda_fail(nullptr, e, "dgpu_blend_geometry");
 	return DGPU_OK;
 }
+
+// ---------------------------------------------------------------------------------------------------------------
+// Element partitions: the residual and the SSP-RK3 stages in two halves around the exchange of the traces of the
+// faces cut by the partition (one process per GPU, the exchange by the caller, e.g. NCCL send/recv on the context's
+// stream). The reference runs on one process; this is the distributed form of compute_rhs_dg / time_step_ssp_rk_33.
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" {
+
+dgpu_status dgpu_halo_setup(dgpu_ctx* c, int n_slots, const int* send_slots, const int* recv_slots)
+{
+	if (!c || n_slots < 0 || (n_slots > 0 && (!send_slots || !recv_slots)))
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->n_halo > 0 || c->halo_send)
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "the halo is already set up");
+	if (n_slots != c->n_remote)
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT,
+		            "the halo must receive every remote face side once: " + std::to_string(c->n_remote) + " sides, " +
+		                std::to_string(n_slots) + " slots");
+	std::vector<char> seen(2 * (size_t)c->n_face, 0);
+	for (int i = 0; i < n_slots; ++i) {
+		const int a = send_slots[i], b = recv_slots[i];
+		if (a < 0 || b < 0 || a >= 2 * c->n_face || b >= 2 * c->n_face || a / 2 != b / 2 || a == b ||
+		    c->h_face_vol[a] < 0 || c->h_face_vol[b] != DGPU_REMOTE_VOLUME || seen[b])
+			return fail(c, DGPU_ERR_INVALID_ARGUMENT,
+			            "halo slot " + std::to_string(i) + ": send the local side and receive the remote side of a face");
+		seen[b] = 1;
+	}
+	if (n_slots == 0)
+		return DGPU_OK;
+	const size_t slot = (size_t)c->nv * c->NF;
+	DGPU_CUDA(c, cudaMalloc((void**)&c->halo_send, n_slots * sizeof(int)));
+	DGPU_CUDA(c, cudaMalloc((void**)&c->halo_recv, n_slots * sizeof(int)));
+	DGPU_CUDA(c, cudaMalloc((void**)&c->halo_sbuf, n_slots * slot * sizeof(double)));
+	DGPU_CUDA(c, cudaMalloc((void**)&c->halo_rbuf, n_slots * slot * sizeof(double)));
+	DGPU_CUDA(c, cudaMemcpy(c->halo_send, send_slots, n_slots * sizeof(int), cudaMemcpyHostToDevice));
+	DGPU_CUDA(c, cudaMemcpy(c->halo_recv, recv_slots, n_slots * sizeof(int), cudaMemcpyHostToDevice));
+	DGPU_CUDA(c, cudaMemset(c->halo_sbuf, 0, n_slots * slot * sizeof(double)));
+	DGPU_CUDA(c, cudaMemset(c->halo_rbuf, 0, n_slots * slot * sizeof(double)));
+	c->n_halo = n_slots;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_halo_buffers(dgpu_ctx* c, double** d_send, double** d_recv, size_t* slot_doubles)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (d_send)
+		*d_send = c->halo_sbuf;
+	if (d_recv)
+		*d_recv = c->halo_rbuf;
+	if (slot_doubles)
+		*slot_doubles = (size_t)c->nv * c->NF;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_get_stream(dgpu_ctx* c, void** cuda_stream)
+{
+	if (!c || !cuda_stream)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	*cuda_stream = (void*)c->stream;
+	return DGPU_OK;
+}
+
+static dgpu_status halo_ready(dgpu_ctx* c)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->n_remote > 0 && c->n_halo != c->n_remote)
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "call dgpu_halo_setup first");
+	if (c->ns)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "partitioned meshes: Euler and advection only");
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_halo_rhs_begin(dgpu_ctx* c)
+{
+	dgpu_status st = halo_ready(c);
+	if (st != DGPU_OK || (st = ensure_coef(c)) != DGPU_OK)
+		return st;
+	DGPU_CUDA(c, c->launch_volume(c));
+	DGPU_CUDA(c, launch_halo_copy(c, true));
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_halo_rhs_end(dgpu_ctx* c, double* max_rhs)
+{
+	dgpu_status st = halo_ready(c);
+	if (st != DGPU_OK)
+		return st;
+	DGPU_CUDA(c, launch_halo_copy(c, false));
+	DGPU_CUDA(c, c->launch_face(c));
+	DGPU_CUDA(c, c->launch_lift_rhs(c));
+	return read_max(c, max_rhs);
+}
+
+dgpu_status dgpu_halo_stage_begin(dgpu_ctx* c, int stage)
+{
+	dgpu_status st = halo_ready(c);
+	if (st != DGPU_OK)
+		return st;
+	if (stage < 0 || stage > 2)
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "stage must be 0, 1 or 2");
+	if (stage == 0 && (st = ensure_gl(c)) != DGPU_OK)
+		return st;
+	DGPU_CUDA(c, c->launch_volume_gl(c));
+	DGPU_CUDA(c, launch_halo_copy(c, true));
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_halo_stage_end(dgpu_ctx* c, double dt, int stage, double* max_rhs)
+{
+	dgpu_status st = halo_ready(c);
+	if (st != DGPU_OK)
+		return st;
+	if (stage < 0 || stage > 2 || !(dt == dt))
+		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "stage must be 0, 1 or 2 and dt a number");
+	DGPU_CUDA(c, launch_halo_copy(c, false));
+	DGPU_CUDA(c, c->launch_face(c));
+	const bool want_max = (max_rhs != nullptr) && stage == 2;
+	DGPU_CUDA(c, c->launch_lift_rk(c, dt, stage, want_max ? 1 : 0));
+	if (stage == 2) {
+		c->coef_valid = false;   // the current state is ug
+		if (want_max && (st = read_max(c, max_rhs)) != DGPU_OK)
+			return st;
+		if (max_rhs && (st = check_positivity_flag(c)) != DGPU_OK)
+			return st;
+	}
+	return DGPU_OK;
+}
+
+}  // extern "C"

@@ -192,9 +192,12 @@ def euler_vortex_2d(n: int = 64, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, 
 
 
 def euler_hex_3d(n: int = 32, p: int = 3, num_flux: int = NUM_FLUX_LAX_FRIEDRICHS, amplitude: float = 0.03,
-                 seed: int = 0, perturb: float = 1e-3, dt: float | None = None, n_steps: int = 200) -> DGProblem:
+                 seed: int = 0, perturb: float = 1e-3, dt: float | None = None, n_steps: int = 200,
+                 stack: int = 1) -> DGProblem:
+    """The curved 3D vortex on [0,10]^3 (n^3 volumes); stack > 1 repeats the box along z (n x n x stack n volumes on
+    [0,10]^2 x [0,10 stack], the same map and vortex), the weak-scaling mesh of stack element partitions."""
     L = 10.0
-    mesh = StructuredMesh(3, n, 0.0, L)
+    mesh = StructuredMesh(3, [n, n, n * stack], 0.0, [L, L, L * stack]) if stack > 1 else StructuredMesh(3, n, 0.0, L)
     ops = TPOperatorSet(mesh.e_type, p)
     geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_3d(amplitude, L), curved=True)
     prob = DGProblem("euler_hex_3d", 3, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,

@@ -504,6 +504,62 @@ class BatchSimulation:
         return n.value
 
 
+class _DeviceArray:
+    """__cuda_array_interface__ view of a device buffer the library owns (for torch.as_tensor, zero copy)."""
+
+    def __init__(self, ptr: int, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(int(x) for x in shape), "typestr": "<f8",
+                                         "data": (int(ptr), False), "version": 3}
+
+
+class PartitionSimulation(Simulation):
+    """One rank's share of an element-partitioned mesh (dpgsolver_gb300.partition.Partition) on this process's GPU:
+    a dgpu context on the rank's volumes and faces, the halo plan (dgpu_halo_setup), and the residual / SSP-RK3
+    stages split around the exchange of the cut faces' traces (dgpu_halo_*_begin / _end). The whole-mesh calls of
+    Simulation (compute_rhs, ssp_rk3_steps, ...) are refused by the library on such a context."""
+
+    def __init__(self, prob, part, stream=None):
+        super().__init__(part.local_problem(prob), stream=stream)
+        self.part = part
+        send = np.ascontiguousarray(part.send_slots, dtype=np.int32)
+        recv = np.ascontiguousarray(part.recv_slots, dtype=np.int32)
+        check(self._lib.dgpu_halo_setup(self._h, len(send), _ip(send), _ip(recv)), self._h)
+        ps, pr, sd = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_size_t()
+        check(self._lib.dgpu_halo_buffers(self._h, ctypes.byref(ps), ctypes.byref(pr), ctypes.byref(sd)), self._h)
+        st = ctypes.c_void_p()
+        check(self._lib.dgpu_get_stream(self._h, ctypes.byref(st)), self._h)
+        self.slot_doubles = sd.value
+        self._send_ptr, self._recv_ptr, self.stream_ptr = ps.value, pr.value, st.value
+
+    def halo_tensors(self):
+        """(send, recv) torch views (n_halo, slot_doubles) of the library's halo buffers, for NCCL or copies; None
+        when this rank has no cut face."""
+        import torch
+        n = self.part.n_halo
+        if n == 0:
+            return None, None
+        shape = (n, self.slot_doubles)
+        return (torch.as_tensor(_DeviceArray(self._send_ptr, shape), device="cuda"),
+                torch.as_tensor(_DeviceArray(self._recv_ptr, shape), device="cuda"))
+
+    def rhs_begin(self):
+        check(self._lib.dgpu_halo_rhs_begin(self._h), self._h)
+
+    def rhs_end(self, want_max: bool = True):
+        mx = ctypes.c_double()
+        check(self._lib.dgpu_halo_rhs_end(self._h, ctypes.byref(mx) if want_max else None), self._h)
+        return mx.value if want_max else None
+
+    def stage_begin(self, stage: int):
+        check(self._lib.dgpu_halo_stage_begin(self._h, int(stage)), self._h)
+
+    def stage_end(self, dt: float, stage: int, want_max: bool = False):
+        mx = ctypes.c_double()
+        check(self._lib.dgpu_halo_stage_end(self._h, float(dt), int(stage), ctypes.byref(mx) if want_max else None),
+              self._h)
+        return mx.value if want_max else None
+
+
 def compute_rhs_dg(sim: Simulation) -> float:
     """compute_rhs_dg (solvers/dg/solve_dg.c:130-136): residual of sim's state into sim's rhs; max |rhs|."""
     return sim.compute_rhs()

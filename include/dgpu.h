@@ -292,6 +292,35 @@ dgpu_status dgpu_set_kernel_timing(dgpu_ctx* ctx, int enable);
 dgpu_status dgpu_kernel_time(dgpu_ctx* ctx, const char* name, double* total_ms, long long* count);
 /* Text of the last error recorded on this context (or of the last failed dgpu_create when ctx is NULL). */
 const char* dgpu_last_error(const dgpu_ctx* ctx);
+
+/* Element partitions across GPUs, one process per GPU: the distributed form of compute_rhs_dg and
+ * time_step_ssp_rk_33 (the reference itself runs on one process: src/simulation/simulation.c:360-369 records rank and
+ * size only). Each rank creates its context with dgpu_create on its own volumes and every face that has one of
+ * them, in the global face order, keeping the global side numbering; a side whose volume belongs to another rank
+ * has face_vol = DGPU_REMOTE_VOLUME (its face_lf is ignored). Such a face is an interior face: its remote side's
+ * trace arrives by exchange. Both ranks evaluate the face's numerical flux from the same two traces, and each lifts
+ * it into its own volume only, so the partitioned residual equals the single-domain one bit for bit.
+ * dgpu_halo_setup: the n_slots cut faces (n_slots must equal the number of remote sides), slot = 2 f + side in the
+ *   local face list: send_slots[i] the local side of cut face i, recv_slots[i] its remote side. Order them per
+ *   neighbour rank in global face order, so that rank A's send list towards B is B's receive list from A.
+ * dgpu_halo_buffers: device buffers owned by the context, n_slots x slot_doubles (n_var x n_fc) each: the traces
+ *   to send (written by *_begin) and the traces received (read by *_end).
+ * One SSP-RK3 step = for stage 0, 1, 2: dgpu_halo_stage_begin (volume term, traces packed into d_send; enqueued on
+ * the context's stream, dgpu_get_stream) -> the caller moves every neighbour's d_send block into this rank's
+ * d_recv (NCCL send/recv or peer copies, enqueued on that stream or completed before the next call) ->
+ * dgpu_halo_stage_end (face term, lift, stage update and positivity). max_rhs (stage 2 only, may be NULL) is this
+ * rank's max |rhs|, read after a stream synchronisation; reduce it over the ranks when needed. The residual alone:
+ * dgpu_halo_rhs_begin / dgpu_halo_rhs_end, on the uploaded state. Euler and advection, QUAD/HEX. On a partitioned
+ * context the whole-mesh entry points (dgpu_compute_rhs[_host], dgpu_ssp_rk3_step[s|_host], the Jacobian, JVP and
+ * adjoint calls) return DGPU_ERR_INVALID_ARGUMENT. */
+#define DGPU_REMOTE_VOLUME (-2)
+dgpu_status dgpu_halo_setup(dgpu_ctx* ctx, int n_slots, const int* send_slots, const int* recv_slots);
+dgpu_status dgpu_halo_buffers(dgpu_ctx* ctx, double** d_send, double** d_recv, size_t* slot_doubles);
+dgpu_status dgpu_get_stream(dgpu_ctx* ctx, void** cuda_stream);
+dgpu_status dgpu_halo_rhs_begin(dgpu_ctx* ctx);
+dgpu_status dgpu_halo_rhs_end(dgpu_ctx* ctx, double* max_rhs);
+dgpu_status dgpu_halo_stage_begin(dgpu_ctx* ctx, int stage);
+dgpu_status dgpu_halo_stage_end(dgpu_ctx* ctx, double dt, int stage, double* max_rhs);
 /* Measured FP64 FMA throughput of the current device in TFLOP/s (8 independent chains per thread, `iters`
  * iterations): the denominator of the FP64-pipe roofline. Measurement aid; no reference counterpart. */
 dgpu_status dgpu_probe_fp64(int iters, double* tflops);

@@ -85,6 +85,13 @@ def _load():
         lib.oracle_ssp_rk3_step.restype = ctypes.c_int
         lib.oracle_enforce_positivity.argtypes = [ctypes.c_void_p, _c_double_p, _c_int_p]
         lib.oracle_enforce_positivity.restype = ctypes.c_int
+        lib.oracle_face_traces.argtypes = [ctypes.c_void_p, _c_double_p, ctypes.c_int, _c_int_p, _c_double_p]
+        lib.oracle_face_traces.restype = ctypes.c_int
+        lib.oracle_compute_rhs_remote.argtypes = [ctypes.c_void_p, _c_double_p, _c_double_p, _c_double_p,
+                                                  _c_double_p]
+        lib.oracle_compute_rhs_remote.restype = ctypes.c_int
+        lib.oracle_face_node_total.argtypes = [ctypes.c_void_p]
+        lib.oracle_face_node_total.restype = ctypes.c_size_t
         lib.oracle_m_inv.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.oracle_m_inv.restype = _c_double_p
         _lib = lib
@@ -138,7 +145,8 @@ class Oracle:
         for f in range(mesh.n_faces):
             for s in range(2):
                 o = int(face_ord[f, s]) if face_ord is not None else 0
-                v = mesh.face_vol[f, s] if mesh.face_vol[f, s] >= 0 else mesh.face_vol[f, 0]   # boundary: unused
+                # boundary side / side of another partition: unused, any valid key
+                v = mesh.face_vol[f, s] if mesh.face_vol[f, s] >= 0 else mesh.face_vol[f, 1 - s]
                 key = (int(vol_group[v]), int(face_q[f]), o)
                 if key not in pairs:
                     pairs[key] = len(pairs)
@@ -204,6 +212,8 @@ class Oracle:
         self._lib = lib
         self.prob = prob
         self.n_state = int(fl["sol"].size)
+        self._n_var = int(prob.n_var)
+        self._n_fc = int(max(FO[k].n_fc for k in range(len(pairs)))) if len(pairs) else 0
 
     def __del__(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -223,6 +233,31 @@ class Oracle:
         st = self._lib.oracle_compute_rhs(self._h, _dp(s), _dp(r), ctypes.byref(mx))
         if st != 0:
             raise RuntimeError(f"oracle_compute_rhs failed: {st}")
+        return r.reshape(np.shape(sol)), mx.value
+
+    def face_traces(self, sol, slots):
+        """Traces of the face sides slots (2 f + s), each (n_var, n_fc) in the side's own face-node order."""
+        s = self._flat(sol)
+        sl = np.ascontiguousarray(slots, dtype=np.int32)
+        n_fc = self._n_fc
+        out = np.empty((len(sl), self._n_var, n_fc))
+        st = self._lib.oracle_face_traces(self._h, _dp(s), len(sl), _ip(sl), _dp(out))
+        if st != 0:
+            raise RuntimeError(f"oracle_face_traces failed: {st}")
+        return out
+
+    def compute_rhs_remote(self, sol, remote):
+        """Residual of a partition: remote (n_faces, n_var, n_fc) holds the traces of the faces' sides that belong
+        to other partitions (face_vol == -2), in those sides' own face-node order; other entries are ignored."""
+        s = self._flat(sol)
+        rm = np.ascontiguousarray(remote, dtype=np.float64)
+        if rm.size != self._lib.oracle_face_node_total(self._h) * self._n_var:
+            raise ValueError("remote traces: one (n_var, n_fc) block per face")
+        r = np.empty_like(s)
+        mx = ctypes.c_double()
+        st = self._lib.oracle_compute_rhs_remote(self._h, _dp(s), _dp(rm), _dp(r), ctypes.byref(mx))
+        if st != 0:
+            raise RuntimeError(f"oracle_compute_rhs_remote failed: {st}")
         return r.reshape(np.shape(sol)), mx.value
 
     def compute_rhs_raw(self, sol):

@@ -166,8 +166,10 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 	for (size_t f = 0; f < nF; ++f) {
 		const struct oracle_face_ops* FL = &in->face_ops[in->face_ops_idx[2 * f]];
 		const struct oracle_face_ops* FR = &in->face_ops[in->face_ops_idx[2 * f + 1]];
-		const int boundary = in->face_vol[2 * f + 1] < 0;
-		if ((!boundary && FL->n_fc != FR->n_fc) || (boundary && (!in->bc_fc || !in->bc_state_fc))) {
+		const int rem0 = in->face_vol[2 * f] == ORACLE_REMOTE_VOLUME, rem1 = in->face_vol[2 * f + 1] == ORACLE_REMOTE_VOLUME;
+		const int boundary = in->face_vol[2 * f + 1] < 0 && !rem1;
+		if ((!boundary && FL->n_fc != FR->n_fc) || (boundary && (!in->bc_fc || !in->bc_state_fc)) || (rem0 && rem1) ||
+		    (!rem0 && (in->face_vol[2 * f] < 0 || in->face_vol[2 * f] >= in->n_volumes))) {
 			oracle_destroy(c);
 			return ORACLE_ERR_ARG;
 		}
@@ -223,7 +225,7 @@ size_t oracle_state_size(const struct oracle_ctx* c)
 
 int oracle_compute_rhs(const struct oracle_ctx* c, const double* sol, double* rhs, double* max_rhs)
 {
-	int st = residual_raw_d(c, sol, rhs);
+	int st = residual_raw_d(c, sol, rhs, NULL);
 	if (st != ORACLE_OK)
 		return st;
 	scale_m_inv_d(c, rhs);
@@ -239,7 +241,56 @@ int oracle_compute_rhs(const struct oracle_ctx* c, const double* sol, double* rh
 
 int oracle_compute_rhs_raw(const struct oracle_ctx* c, const double* sol, double* rhs)
 {
-	return residual_raw_d(c, sol, rhs);
+	return residual_raw_d(c, sol, rhs, NULL);
+}
+
+/* Partitioned meshes: the traces of the given face sides (slot 2f+s, a side with a volume of this mesh), each
+ * n_fc x n_var column-major in the side's own face-node order (cv0_vs_fc[ind_lf] s_coef, compute_face_rlhs_T.c:67-81),
+ * at out + i * n_fc * n_var. */
+int oracle_face_traces(const struct oracle_ctx* c, const double* sol, int n, const int* slots, double* out)
+{
+	const struct oracle_problem* P = &c->P;
+	const int nv = P->n_var;
+	size_t o = 0;
+	for (int i = 0; i < n; ++i) {
+		const int f = slots[i] / 2, s = slots[i] % 2;
+		if (slots[i] < 0 || f >= P->n_faces)
+			return ORACLE_ERR_ARG;
+		const int v = P->face_vol[2 * f + s], lf = P->face_lf[2 * f + s];
+		if (v < 0 || v >= P->n_volumes)
+			return ORACLE_ERR_ARG;
+		const struct oracle_face_ops* F = &P->face_ops[P->face_ops_idx[2 * f + s]];
+		for (size_t k = 0; k < (size_t)F->n_fc * nv; ++k)
+			out[o + k] = 0.0;
+		mm_acc_d(F->n_fc, F->n_vs, nv, 1.0, &F->cv0_vs_fc[(size_t)lf * F->n_fc * F->n_vs], &sol[c->state_off[v]],
+		         &out[o]);
+		o += (size_t)F->n_fc * nv;
+	}
+	return ORACLE_OK;
+}
+
+/* oracle_compute_rhs on a partition: remote holds, per face, the trace of its side that belongs to another
+ * partition (face_vol == ORACLE_REMOTE_VOLUME), n_fc x n_var column-major at fc_off[f] * n_var. */
+int oracle_compute_rhs_remote(const struct oracle_ctx* c, const double* sol, const double* remote, double* rhs,
+                              double* max_rhs)
+{
+	int st = residual_raw_d(c, sol, rhs, remote);
+	if (st != ORACLE_OK)
+		return st;
+	scale_m_inv_d(c, rhs);
+	double mx = 0.0;
+	const size_t n = oracle_state_size(c);
+	for (size_t i = 0; i < n; ++i)
+		if (fabs(rhs[i]) > mx)
+			mx = fabs(rhs[i]);
+	if (max_rhs)
+		*max_rhs = mx;
+	return ORACLE_OK;
+}
+
+size_t oracle_face_node_total(const struct oracle_ctx* c)
+{
+	return c->fc_off[c->P.n_faces];
 }
 
 int oracle_compute_rhs_cmplx(const struct oracle_ctx* c, const double* sol_re, const double* sol_im,
@@ -250,7 +301,7 @@ int oracle_compute_rhs_cmplx(const struct oracle_ctx* c, const double* sol_re, c
 	double complex* r = malloc(sizeof(double complex) * n);
 	for (size_t i = 0; i < n; ++i)
 		s[i] = sol_re[i] + I * (sol_im ? sol_im[i] : 0.0);
-	int st = residual_raw_c(c, s, r);
+	int st = residual_raw_c(c, s, r, NULL);
 	if (st == ORACLE_OK) {
 		scale_m_inv_c(c, r);
 		for (size_t i = 0; i < n; ++i) {

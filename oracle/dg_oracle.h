@@ -15,6 +15,9 @@ enum {
 	ORACLE_ERR_POSITIVITY = -3,
 };
 
+/* face_vol entry of a face side whose volume belongs to another partition of the mesh */
+#define ORACLE_REMOTE_VOLUME (-2)
+
 enum { ORACLE_PDE_ADVECTION = 1, ORACLE_PDE_EULER = 3, ORACLE_PDE_NAVIER_STOKES = 4 };   /* definitions_test_case.h */
 enum { ORACLE_VISCOSITY_CONSTANT = 101, ORACLE_VISCOSITY_SUTHERLAND = 102 };  /* definitions_physics.h:34-36 */
 enum { ORACLE_NUM_FLUX_UPWIND = 11, ORACLE_NUM_FLUX_ROE_PIKE = 31, ORACLE_NUM_FLUX_LAX_FRIEDRICHS = 32 };
@@ -90,6 +93,10 @@ int oracle_compute_rhs_raw(const struct oracle_ctx* c, const double* sol, double
 int oracle_compute_rhs_cmplx(const struct oracle_ctx* c, const double* sol_re, const double* sol_im,
                              double* rhs_re, double* rhs_im);
 int oracle_ssp_rk3_step(const struct oracle_ctx* c, double dt, double* sol, double* max_rhs, int* n_corrections);
+int oracle_face_traces(const struct oracle_ctx* c, const double* sol, int n, const int* slots, double* out);
+int oracle_compute_rhs_remote(const struct oracle_ctx* c, const double* sol, const double* remote, double* rhs,
+                              double* max_rhs);
+size_t oracle_face_node_total(const struct oracle_ctx* c);
 int oracle_enforce_positivity(const struct oracle_ctx* c, double* sol, int* n_corrections);
 /* M^-1 of volume v (n_vs x n_vs row-major) */
 const double* oracle_m_inv(const struct oracle_ctx* c, int v);

@@ -602,7 +602,9 @@ static void SUF(ns_gradients)(const struct oracle_ctx* c, const Type* sol, Type*
 	free(dr); free(t); free(y); free(sL); free(sR0); free(X); free(XR);
 }
 
-static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* rhs)
+/* remote: per face n_fc x n_var column-major (at fc_off[f] n_var), the trace of a side whose volume belongs to another
+ * partition (face_vol == ORACLE_REMOTE_VOLUME), in that side's own face-node order; NULL when no side is remote. */
+static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* rhs, const double* remote)
 {
 	const struct oracle_problem* P = &c->P;
 	const int d = P->d, nv = P->n_var, neq = P->n_var;
@@ -687,7 +689,13 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 	/* ---- face term ---- */
 	for (int f = 0; f < P->n_faces; ++f) {
 		const int vL = P->face_vol[2 * f], vR = P->face_vol[2 * f + 1];
-		if (vR < 0) {
+		const int remL = (vL == ORACLE_REMOTE_VOLUME), remR = (vR == ORACLE_REMOTE_VOLUME);
+		if ((remL || remR) && (!remote || ns_pde)) {
+			free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);
+			free(gv); free(gf); free(gt); free(g_vc); free(gpL); free(gpR0); free(gpR); free(tmp);
+			return ORACLE_ERR_ARG;
+		}
+		if (vR < 0 && !remR) {
 			if (SUF(boundary_face)(c, f, sol, rhs, sL, nnf, gv, gf) != 0) {
 				free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);
 				free(gv); free(gf); free(gt); free(g_vc); free(gpL); free(gpR0); free(gpR); free(tmp);
@@ -704,8 +712,16 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 		const double* jf = &P->jacobian_det_fc[c->fc_off[f]];
 		for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
 			sL[i] = sR0[i] = 0.0;
-		SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], &sol[c->state_off[vL]], sL);
-		SUF(mm_acc)(n_fc, FR->n_vs, nv, 1.0, &FR->cv0_vs_fc[(size_t)lfR * n_fc * FR->n_vs], &sol[c->state_off[vR]], sR0);
+		if (remL)
+			for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
+				sL[i] = remote[c->fc_off[f] * nv + i];
+		else
+			SUF(mm_acc)(n_fc, FL->n_vs, nv, 1.0, &FL->cv0_vs_fc[(size_t)lfL * n_fc * FL->n_vs], &sol[c->state_off[vL]], sL);
+		if (remR)
+			for (size_t i = 0; i < (size_t)n_fc * nv; ++i)
+				sR0[i] = remote[c->fc_off[f] * nv + i];
+		else
+			SUF(mm_acc)(n_fc, FR->n_vs, nv, 1.0, &FR->cv0_vs_fc[(size_t)lfR * n_fc * FR->n_vs], &sol[c->state_off[vR]], sR0);
 		/* right trace reordered to the left's face-node order (boundary_T.c:80-92) */
 		for (int k = 0; k < nv; ++k)
 			for (int i = 0; i < n_fc; ++i)
@@ -775,11 +791,13 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 		 * (compute_face_rlhs_T.c:297-310, 347-359). The right side is brought back to its own face-node
 		 * order with the inverse of the trace permutation; the reference applies nc_fc itself, which is the
 		 * same whenever nc_fc is an involution. */
-		SUF(mm_acc)(FL->n_vs, n_fc, neq, -1.0, &FL->tw0_vt_fc[(size_t)lfL * FL->n_vs * n_fc], nnf, &rhs[c->state_off[vL]]);
+		if (!remL)
+			SUF(mm_acc)(FL->n_vs, n_fc, neq, -1.0, &FL->tw0_vt_fc[(size_t)lfL * FL->n_vs * n_fc], nnf, &rhs[c->state_off[vL]]);
 		for (int k = 0; k < neq; ++k)
 			for (int i = 0; i < n_fc; ++i)
 				nnfR[nc[i] + (size_t)n_fc * k] = -nnf[i + (size_t)n_fc * k];
-		SUF(mm_acc)(FR->n_vs, n_fc, neq, -1.0, &FR->tw0_vt_fc[(size_t)lfR * FR->n_vs * n_fc], nnfR, &rhs[c->state_off[vR]]);
+		if (!remR)
+			SUF(mm_acc)(FR->n_vs, n_fc, neq, -1.0, &FR->tw0_vt_fc[(size_t)lfR * FR->n_vs * n_fc], nnfR, &rhs[c->state_off[vR]]);
 	}
 
 	free(s_vc); free(fr); free(sL); free(sR0); free(sR); free(nnf); free(nnfR);

@@ -1,0 +1,72 @@
+"""The C ABI called from compiled C host code (tests/c/dgpu_caller.c), not through ctypes.
+
+The program keeps the mesh the way the reference does (lists of solver volumes and faces owning their multiarrays),
+packs it once in list order, and replaces compute_rhs_dg and time_step_ssp_rk_33 by dgpu_compute_rhs_host and
+dgpu_ssp_rk3_step_host. On the CPU it must compile with -Wall -Wextra -Werror against include/dgpu.h and link to
+libdgpu.so; on the GPU its residual and RK states must match the reference's own (the golden fixtures of
+tests/golden/make_ref_golden.py) to 1e-12.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle.reference as R
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(REPO, "tests", "c", "dgpu_caller.c")
+
+
+def build_caller(out_dir):
+    import dpgsolver_gb300
+    lib = dpgsolver_gb300.build()
+    exe = os.path.join(out_dir, "dgpu_caller")
+    subprocess.run(["gcc", "-std=c11", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(REPO, "include"),
+                    SRC, "-o", exe, lib, "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+    return exe
+
+
+def test_c_caller_compiles_against_the_header(tmp_path):
+    exe = build_caller(str(tmp_path))
+    assert os.path.exists(exe)
+
+
+def write_case(path, prob, ref, n_steps):
+    """The case in the reference's layouts: per volume metrics_vc (n_vc, d, d) and sol_coef (n_vs, n_var)
+    column-major, per face normals_fc (n_fc, d) row-major."""
+    ops = prob.ops
+    with open(path, "wb") as fh:
+        np.array([0x55504744, prob.d, ops.p, prob.pde, prob.num_flux, int(prob.positivity), prob.n_volumes,
+                  prob.mesh.n_faces, n_steps], dtype=np.int32).tofile(fh)
+        np.array([float(ref["dt"])] + [float(b) for b in prob.b_adv[:3]], dtype=np.float64).tofile(fh)
+        for a in (ops.cv0_1d, ops.cv1_1d, ops.cv0_bnd_1d, ops.w_vc_1d, ops.ccSB0_1d, ops.ccBS0_1d):
+            np.ascontiguousarray(a, dtype=np.float64).tofile(fh)
+        met = np.transpose(ref["metrics_vc"], (0, 3, 2, 1))
+        for v in range(prob.n_volumes):
+            np.ascontiguousarray(met[v]).tofile(fh)
+            np.ascontiguousarray(ref["jacobian_det_vc"][v]).tofile(fh)
+            np.ascontiguousarray(ref["sol_in"][v]).tofile(fh)
+        for f in range(prob.mesh.n_faces):
+            np.concatenate([ref["face_vol"][f], ref["face_lf"][f], ref["face_ord"][f]]).astype(np.int32).tofile(fh)
+            np.ascontiguousarray(ref["normals_fc"][f]).tofile(fh)
+            np.ascontiguousarray(ref["jacobian_det_fc"][f]).tofile(fh)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["c1", "c2_n8", "c2_lf_n8"])
+def test_c_caller_matches_reference(gpu_lib, tmp_path, name):
+    ref = dict(np.load(os.path.join(REPO, "tests", "golden", f"reference_{name}.npz")))
+    prob = R.with_reference_inputs(R.host_problem(name), ref)
+    exe = build_caller(str(tmp_path))
+    case, out = str(tmp_path / "case.bin"), str(tmp_path / "out.bin")
+    n_steps = int(ref["steps"])
+    write_case(case, prob, ref, n_steps)
+    subprocess.run([exe, case, out], check=True)
+    res = np.fromfile(out, dtype=np.float64)
+    n = prob.sol.size
+    assert res.size == 2 * n + 2
+    rhs, mx0, sol, _ = res[:n].reshape(prob.sol.shape), res[n], res[n + 1:2 * n + 1].reshape(prob.sol.shape), res[-1]
+    assert np.max(np.abs(rhs - ref["rhs"])) / np.max(np.abs(ref["rhs"])) <= 1e-12
+    assert abs(mx0 - float(ref["max_rhs"])) <= 1e-12 * float(ref["max_rhs"])
+    assert np.max(np.abs(sol - ref["sol_steps"])) / np.max(np.abs(ref["sol_steps"])) <= 1e-12

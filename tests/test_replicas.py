@@ -1,6 +1,7 @@
-"""The multi-rank path of bench.py on CPU ranks (gloo, world size 2, 127.0.0.1): the run shards nothing (replicas
-only), so its cross-rank steps are the barrier around the timed region and the maximum of the ranks' times, and the
-reference arm runs on rank 0 alone."""
+"""The timing steps of bench.py's multi-rank path on CPU ranks (gloo, world size 2, 127.0.0.1): the barrier around the
+timed region and the maximum of the ranks' times; the reference arm runs on rank 0 alone. (The partitioned data path
+itself, trace exchange included, is covered by tests/test_partition.py on gloo ranks and tests/test_gpu_partition.py
+on the GPU.)"""
 import os
 import socket
 import sys

@@ -124,3 +124,45 @@ def test_noalloc_after_other_mesh_and_oversize_rejected(gpu_lib):
         s = _host_structs(prob, b)
         r, _ = _noalloc_rhs(gpu_lib, prob, b, s)
         assert np.max(np.abs(r - r_ref)) / np.max(np.abs(r_ref)) <= TOL
+
+
+def test_noalloc_rejects_bad_inputs_without_running(gpu_lib):
+    """A face list that gives one (volume, local face) to two face sides, and a state in page-locked host memory
+    instead of device memory, are refused with DGPU_ERR_INVALID_ARGUMENT and the residual is left untouched."""
+    import torch
+    from dpgsolver_gb300.solver import Simulation
+    prob = P.euler_hex_3d(4, 2)
+    bufs = _device_inputs(prob)
+    structs = _host_structs(prob, bufs)
+    phys, tp, m, _ = structs
+
+    # one face more than the mesh has, repeating face 0: every (volume, local face) is still covered, face 0's twice
+    dup = {k: torch.cat([bufs[k], bufs[k][:1]]) for k in ("fv", "flf", "nc", "nrm", "jf")}
+    m_dup = _lib.Mesh()
+    m_dup.n_volumes, m_dup.n_faces = m.n_volumes, m.n_faces + 1
+    m_dup.metrics_vc, m_dup.jacobian_det_vc = m.metrics_vc, m.jacobian_det_vc
+    m_dup.face_vol = ctypes.cast(dup["fv"].data_ptr(), _lib.c_int_p)
+    m_dup.face_lf = ctypes.cast(dup["flf"].data_ptr(), _lib.c_int_p)
+    m_dup.nc_fc = ctypes.cast(dup["nc"].data_ptr(), _lib.c_int_p)
+    m_dup.normals_fc = ctypes.cast(dup["nrm"].data_ptr(), _lib.c_double_p)
+    m_dup.jacobian_det_fc = ctypes.cast(dup["jf"].data_ptr(), _lib.c_double_p)
+    bufs["rhs"].fill_(float("nan"))
+    st = gpu_lib.dgpu_compute_rhs_noalloc(ctypes.byref(phys), ctypes.byref(tp), ctypes.byref(m_dup),
+                                          ctypes.c_void_p(bufs["sol"].data_ptr()),
+                                          ctypes.c_void_p(bufs["rhs"].data_ptr()), None, None)
+    assert st == 1 and b"bad mesh" in gpu_lib.dgpu_last_error(None)
+    assert torch.isnan(bufs["rhs"]).all()
+
+    pinned = bufs["sol"].cpu().pin_memory()
+    st = gpu_lib.dgpu_compute_rhs_noalloc(ctypes.byref(phys), ctypes.byref(tp), ctypes.byref(m),
+                                          ctypes.c_void_p(pinned.data_ptr()),
+                                          ctypes.c_void_p(bufs["rhs"].data_ptr()), None, None)
+    assert st == 1 and b"device memory of the current device" in gpu_lib.dgpu_last_error(None)
+    assert torch.isnan(bufs["rhs"]).all()
+
+    # the same arrays, well formed, still work afterwards
+    with Simulation(prob) as sim:
+        sim.compute_rhs()
+        r_ref = sim.rhs
+    r, _ = _noalloc_rhs(gpu_lib, prob, bufs, structs)
+    assert np.max(np.abs(r - r_ref)) / np.max(np.abs(r_ref)) <= TOL
