@@ -756,7 +756,7 @@ def mixed_measurements(torch, stream, args, kind="types"):
     _lib.check(_lib.load().dgpu_probe_fp64(20000, ctypes.byref(fp64_peak)))
     stage_s = out[best]["ms_per_step"] / 3 * 1e-3
     n_vc = np.array([prob.groups[g].n_vc for g in prob.vol_group], dtype=np.int64)
-    n_fcn = int(np.sum(prob.face_q.astype(np.int64) ** 2))
+    n_fcn = int(prob.face_off[-1]) if hasattr(prob, "face_off") else int(np.sum(prob.face_q.astype(np.int64) ** 2))
     bytes_eval = 8 * (2 * ns + int(np.sum(10 * n_vc)) + 3 * n_fcn)
     peak, peak_kind = hbm_peak()
     from dpgsolver_gb300.host.element import HEX, PYR, TET, WEDGE

@@ -181,7 +181,7 @@ class MixedTypeMesh:
                     seen[key] = len(fv)
                     fv.append([v, -1])
                     flf.append([lf, -1])
-        if seen:
+        if seen and getattr(self, "periodic", True):
             raise AssertionError("unmatched faces: the mesh is not conforming/periodic")
         self.face_vol = np.array(fv, dtype=np.int32)
         self.face_lf = np.array(flf, dtype=np.int32)
@@ -191,6 +191,8 @@ class MixedTypeMesh:
         tp = getattr(self, "tp_type", HEX)
         for f in range(self.n_faces):
             vs = self.face_vol[f]
+            if vs[1] < 0:     # boundary face: side 0 only, in its own order
+                continue
             cs = 1 if (self.types[vs[1]] == tp and self.types[vs[0]] != tp) else 0
             self.face_canon[f] = cs
             canon = [self.gids[vs[cs]][m] for m in S.F_VE[self.types[vs[cs]]][self.face_lf[f, cs]]]
@@ -207,6 +209,23 @@ class MixedTypeMesh:
         return {int(t): int(np.sum(self.types == t)) for t in (HEX, TET, WEDGE, PYR)}
 
 
+def _tp_face_points(d: int, lf: int, q: int) -> np.ndarray:
+    """GL face nodes of local face lf of the reference QUAD/HEX (tangential coordinates in TP order)."""
+    from .element import gauss_legendre
+    x1, _ = gauss_legendre(q)
+    nd, val = lf // 2, (-1.0 if lf % 2 == 0 else 1.0)
+    tang = [k for k in range(d) if k != nd]
+    if d == 2:
+        pts = np.zeros((q, 2))
+        pts[:, tang[0]] = x1
+    else:
+        pts = np.zeros((q * q, 3))
+        pts[:, tang[0]] = np.tile(x1, q)
+        pts[:, tang[1]] = np.repeat(x1, q)
+    pts[:, nd] = val
+    return pts
+
+
 _AFF_SUB = {TET: [0, 1, 2, 3], WEDGE: [0, 1, 2, 3], PYR: [0, 1, 2, 4], HEX: [0, 1, 2, 4], TRI: [0, 1, 2],
             QUAD: [0, 1, 2]}
 
@@ -219,15 +238,18 @@ class MixedTriQuadMesh(MixedTypeMesh):
 
     tp_type = QUAD
 
-    def __init__(self, n: int, seed: int = 0, p_tri: float = 0.5):
+    def __init__(self, n: int, seed: int = 0, p_tri: float = 0.5, periodic: bool = True):
         if n < 2:
             raise ValueError("n >= 2")
         self.d, self.n = 2, n
         self.h = 1.0 / n
+        self.periodic = bool(periodic)
         rng = np.random.default_rng(seed)
         types, gids, X = [], [], []
 
         def vid(i, j):
+            if not periodic:   # the sides of the square are boundary faces
+                return i + (n + 1) * j
             return (i % n) + n * (j % n)
         for j in range(n):
             for i in range(n):
@@ -318,14 +340,65 @@ class MixedTypeProblem:
         if np.any(self.J <= 0.0):
             raise AssertionError("non-positive Jacobian")
         self.m = self.J[:, None, None] * np.transpose(np.linalg.inv(self.A), (0, 2, 1))
-        # faces at p_f = max(p_L, p_R): q_f^2 nodes on triangles (collapsed rule) and quads (GL), q_f on lines
+        # faces at p_f = max(p_L, p_R), integrated as the reference does: q_f GL nodes on lines, q_f^2 on quads,
+        # the Witherden-Vincent rule of degree 2 p_f on triangles
         q = p_vol.astype(np.int64) + 1
         self.face_q = np.maximum(q[mesh.face_vol[:, 0]], q[mesh.face_vol[:, 1]]).astype(np.int32)
+        self.face_nvert = self._face_vertex_counts()
+        n_fc = np.empty(mesh.n_faces, dtype=np.int64)
+        for nvert, ft in ((2, LINE), (3, S.TRI), (4, S.QUAD)):
+            for qf in np.unique(self.face_q):
+                sel = (self.face_nvert == nvert) & (self.face_q == qf)
+                if np.any(sel):
+                    n_fc[sel] = len(S.face_rule(ft, int(qf))[1])
         self.face_off = np.zeros(mesh.n_faces + 1, dtype=np.int64)
-        self.face_off[1:] = np.cumsum(self.face_q.astype(np.int64) ** (d - 1))
+        self.face_off[1:] = np.cumsum(n_fc)
         self._face_geometry()
         self.sol = np.zeros(int(self.state_off[-1]))
         self.dt = 0.0
+        self.bc = None
+        self.bc_state = None
+        self.bc_data = None
+
+    def set_boundaries(self, code: int, exterior=None):
+        """Every boundary face (face_vol[f, 1] < 0) gets the reference's BC code `code`; exterior(xyz (m, d)) ->
+        (m, n_var) is the exterior state at their face nodes (the test case's constructor_sol_bv; zero when None, as
+        slip walls need none)."""
+        mesh = self.mesh
+        bnd = mesh.face_vol[:, 1] < 0
+        self.bc = np.where(bnd, int(code), 0).astype(np.int32)
+        nfn = int(self.face_off[-1])
+        ext = np.zeros((nfn, self.n_var))
+        if exterior is not None:
+            ext = np.asarray(exterior(self.face_xyz()), dtype=np.float64).reshape(nfn, self.n_var)
+            ext[np.repeat(~bnd, np.diff(self.face_off))] = 0.0
+        self.bc_state = np.ascontiguousarray(ext)
+
+    def face_xyz(self):
+        """Physical coordinates of every face's canonical nodes (side 0's map), (n_face_nodes, d)."""
+        mesh = self.mesh
+        out = np.empty((int(self.face_off[-1]), self.d))
+        for f in range(mesh.n_faces):
+            v, lf = int(mesh.face_vol[f, 0]), int(mesh.face_lf[f, 0])
+            g = self.groups[self.vol_group[v]]
+            qf = int(self.face_q[f])
+            if getattr(g, "dense", False):
+                xr = g.face_points(lf, int(mesh.face_ord[f, 0]), qf)
+            else:
+                xr = _tp_face_points(self.d, lf, qf)
+            out[self.face_off[f]:self.face_off[f + 1]] = xr @ self.A[v].T + self.b[v]
+        return out
+
+    def _face_vertex_counts(self):
+        """Vertices of every face (2: LINE, 3: TRI, 4: QUAD), from its side-0 volume's local face."""
+        mesh, d = self.mesh, self.d
+        v0, lf0 = mesh.face_vol[:, 0], mesh.face_lf[:, 0]
+        ftype = np.zeros(mesh.n_faces, dtype=np.int32)
+        for t in ((QUAD, TRI) if d == 2 else (HEX, TET, WEDGE, PYR)):
+            sel = np.nonzero(mesh.types[v0] == t)[0]
+            if len(sel):
+                ftype[sel] = np.array([len(fv) for fv in S.F_VE[t]])[lf0[sel]]
+        return ftype
 
     def _face_geometry(self):
         """Normals and J_f of the side-0 volume (constant on affine faces) and the side-0 face-rule weights, at the
@@ -333,7 +406,7 @@ class MixedTypeProblem:
         mesh, d = self.mesh, self.d
         v0, lf0 = mesh.face_vol[:, 0], mesh.face_lf[:, 0]
         nref = np.zeros((mesh.n_faces, d))
-        ftype = np.zeros(mesh.n_faces, dtype=np.int32)
+        ftype = self.face_nvert
         for t in ((QUAD, TRI) if d == 2 else (HEX, TET, WEDGE, PYR)):
             sel = np.nonzero(mesh.types[v0] == t)[0]
             if len(sel) == 0:
@@ -343,7 +416,6 @@ class MixedTypeProblem:
             else:
                 nr = S.reference_normals_2d(t) if d == 2 else S.reference_normals_3d(t)
             nref[sel] = nr[lf0[sel]]
-            ftype[sel] = np.array([len(fv) for fv in S.F_VE[t]])[lf0[sel]]
         nun = np.einsum("fij,fj->fi", self.m[v0], nref)
         jn = np.linalg.norm(nun, axis=1)
         nfc = np.diff(self.face_off)
@@ -426,6 +498,9 @@ class MixedTypeProblem:
             "jacobian_det_fc": self.jacobian_det_fc.copy(),
             "nc_fc": self.nc_fc(),
             "sol": self.sol,
+            "bc_fc": None if self.bc is None else np.ascontiguousarray(self.bc, dtype=np.int32),
+            "bc_state_fc": None if self.bc_state is None else np.ascontiguousarray(self.bc_state).ravel(),
+            "bc_data": self.bc_data,
         }
 
     def project(self, fn):
@@ -490,11 +565,11 @@ def mixed_types_euler(n: int = 12, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: 
 
 def mixed_tri_quad_euler(n: int = 16, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE,
                          mach: float = 0.5, perturb: float = 0.3, p_tri: float = 0.5,
-                         positivity: bool = True) -> MixedTypeProblem:
+                         positivity: bool = True, walls: bool = False) -> MixedTypeProblem:
     """Mixed QUAD/TRI mesh of the periodic unit square (n^2 cells, MixedTriQuadMesh), p uniform in p_set per volume
     (seeded), Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed_types_euler),
     positivity limiter on by default."""
-    mesh = MixedTriQuadMesh(n, seed=seed, p_tri=p_tri)
+    mesh = MixedTriQuadMesh(n, seed=seed, p_tri=p_tri, periodic=not walls)
     rng = np.random.default_rng(seed + 17)
     p_vol = rng.choice(np.asarray(p_set, dtype=np.int32), size=mesh.n_volumes)
     prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux, positivity=positivity)
@@ -512,6 +587,8 @@ def mixed_tri_quad_euler(n: int = 16, seed: int = 0, p_set=(1, 2, 3, 4), num_flu
         return primitive_to_conserved(2, rho, vel, pr).T
 
     prob.project(state)
+    if walls:   # slip walls on the four sides of the square (BC_SLIPWALL, boundary_euler_T.c)
+        prob.set_boundaries(10102)
     lam = mach * c0 * (1.0 + perturb) + c0 * math.sqrt((1.0 + perturb) / (1.0 - perturb))
     prob.dt = prob.stable_dt(lam=lam)
     prob.meta.update(n=n, seed=seed, p_set=tuple(p_set), counts=mesh.counts())

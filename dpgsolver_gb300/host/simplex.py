@@ -21,13 +21,17 @@ Choices of this set-up (the C ABI accepts any basis and cubature the caller supp
   AO / GLL node sets; a change of basis does not change the discrete solution, only its coordinates). TET:
   P_p; WEDGE: P_p(TRI) x P_p(LINE); PYR: the rational pyramid space of dimension (p+1)(p+2)(2p+3)/6 spanned in
   collapsed coordinates by P_i(a) P_j(b) ((1-c)/2)^max(i,j) P_k^(2max(i,j)+2,0)(c) (Bergot-Cohen-Durufle).
-* Cubature: collapsed-coordinate (conical product) Gauss-Jacobi rules with q = p+1 points per direction, exact to
-  degree 2q-1 >= 2p: (p+1)^3 volume points and (p+1)^2 points per triangular face. The reference's symmetric
-  Witherden-Vincent rules need fewer points (TET degree 8: 46 instead of 125); they are not reproduced here.
-* Collapsed triangle rules are not invariant under the triangle's symmetries, so each face's nodes are laid out
-  once, in a canonical vertex order of the face, and every volume evaluates its basis there: the face operators
-  are indexed by (local face, orientation, p_f), where the orientation is the vertex permutation between the
-  canonical order and the volume's local face order (the reference's ind_ord, face.h:47-97).
+* Cubature: the reference's (nodes_operators.c:313-350, 474-516, 589-609): Witherden-Vincent rules of degree 2p on
+  TRI and TET volumes and on the triangular faces of 3D volumes (3/6/12/16 TRI and 4/14/24/46 TET points for
+  p = 1..4, read from the reference's tables into wv_rules.npz by make_wv_rules.py), that TRI rule times GL with
+  p+1 points on the WEDGE (the reference builds its operators from the TRI and LINE factors), GL with p_f+1 points
+  per direction on LINE and QUAD faces. The PYR keeps a conical Gauss-Jacobi rule of (p+1)^3 points: the
+  reference's own PYR choice (GJW) has no case in compute_cub_c_type, so the reference cannot build PYR operators.
+  Set-up integrations that must be exact beyond degree 2p (orthonormalisation, the Bezier maps) use conical rules.
+* Each face's nodes are laid out once, in a canonical vertex order of the face, and every volume evaluates its
+  basis there: the face operators are indexed by (local face, orientation, p_f), where the orientation is the vertex
+  permutation between the canonical order and the volume's local face order (the reference's ind_ord,
+  face.h:47-97). With the symmetric Witherden-Vincent rules this equals the reference's permutation of face nodes.
 """
 from __future__ import annotations
 
@@ -195,8 +199,8 @@ _T2 = np.array([[-1.0, -1.0], [1.0, -1.0], [-1.0, 1.0]])
 _T3 = np.array([[-1.0, -1.0, -1.0], [1.0, -1.0, -1.0], [-1.0, 1.0, -1.0], [-1.0, -1.0, 1.0]])
 
 
-def tri_rule(q: int):
-    """(q^2, 2) nodes and weights on the reference TRI (a fastest), exact to degree 2q-1."""
+def conical_tri_rule(q: int):
+    """(q^2, 2) collapsed-coordinate nodes and weights on the reference TRI (a fastest), exact to degree 2q-1."""
     xa, wa = gauss_legendre(q)
     xb, wb = gauss_jacobi(q, 1.0)
     a = np.tile(xa, q)
@@ -215,11 +219,54 @@ def quad_rule(q: int):
     return np.stack([np.tile(x1, q), np.repeat(x1, q)], axis=1), np.tile(w1, q) * np.repeat(w1, q)
 
 
+_WV = {}
 _FACE_RULES = {}
 
 
+def wv_rule(e_type: int, degree: int):
+    """The Witherden-Vincent rule of the given degree on the reference TRI or TET: the reference's own volume
+    cubature of simplices and its face cubature of 3D simplex faces (nodes_operators.c:474-516), read from
+    input/nodes/{tri,tet}/WV<degree>.txt and kept in wv_rules.npz (make_wv_rules.py). Every group's barycentric
+    coordinates are expanded into their orbit under the permutations of the vertices (its size is the table's), and
+    mapped to the reference element as sum_i lambda_i vertex_i. Returns nodes (n, d) and weights (n,)."""
+    key = (e_type, degree)
+    if key not in _WV:
+        import os
+        name = {TRI: "tri", TET: "tet"}[e_type]
+        data = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "wv_rules.npz"))
+        bary, w, orbit = data[f"{name}{degree}_bary"], data[f"{name}{degree}_w"], data[f"{name}{degree}_orbit"]
+        V = TRI_VERTS if e_type == TRI else VERTS[TET]
+        pts, ws = [], []
+        for b, wi, k in zip(bary, w, orbit):
+            orb = sorted(set(itertools.permutations(b.tolist())))
+            if len(orb) != k:
+                raise AssertionError(f"WV{degree} orbit of {b}: {len(orb)} points, the table says {k}")
+            for lam in orb:
+                pts.append(np.asarray(lam) @ V)
+                ws.append(wi)
+        x, wt = np.array(pts), np.array(ws)
+        x.setflags(write=False)
+        wt.setflags(write=False)
+        _WV[key] = (x, wt)
+    return _WV[key]
+
+
+def tri_rule(q: int):
+    """The reference's TRI cubature of order p = q - 1: Witherden-Vincent of degree 2p (3, 6, 12, 16 points for
+    p = 1..4)."""
+    return wv_rule(TRI, 2 * (q - 1))
+
+
+def quad_rule(q: int):
+    """(q^2, 2) GL tensor nodes (first coordinate fastest) and weights on [-1,1]^2."""
+    x1, w1 = gauss_legendre(q)
+    return np.stack([np.tile(x1, q), np.repeat(x1, q)], axis=1), np.tile(w1, q) * np.repeat(w1, q)
+
+
 def face_rule(ftype: int, q: int):
-    """Cached (nodes, weights) of the face reference element (read-only arrays)."""
+    """Cached (nodes, weights) of the face reference element at face order p_f = q - 1, as the reference
+    integrates it (nodes_operators.c:474-516): GL with q points on LINE faces (2D) and on QUAD faces, Witherden-Vincent
+    of degree 2 p_f on TRI faces (read-only arrays)."""
     key = (ftype, q)
     if key not in _FACE_RULES:
         if ftype == LINE:
@@ -227,16 +274,18 @@ def face_rule(ftype: int, q: int):
             x = x1[:, None].copy()
         else:
             x, w = tri_rule(q) if ftype == TRI else quad_rule(q)
+            x, w = np.array(x), np.array(w)
         x.setflags(write=False)
         w.setflags(write=False)
         _FACE_RULES[key] = (x, w)
     return _FACE_RULES[key]
 
 
-def volume_rule(e_type: int, q: int):
-    """Nodes (n, d) and weights on the reference element, exact to degree 2q-1 (conical products)."""
+def conical_rule(e_type: int, q: int):
+    """Collapsed-coordinate (conical product) Gauss-Jacobi rule with q points per direction, exact to degree
+    2q-1: the exact integrations of the set-up (orthonormalisation, Bezier maps) and the PYR volume cubature."""
     if e_type == TRI:
-        return tri_rule(q)
+        return conical_tri_rule(q)
     if e_type == TET:
         xa, wa = gauss_legendre(q)
         xb, wb = gauss_jacobi(q, 1.0)
@@ -250,7 +299,7 @@ def volume_rule(e_type: int, q: int):
         A, b0 = _affine_from(_T3, VERTS[TET])
         return np.stack([r, s, c], axis=1) @ A.T + b0, w * abs(np.linalg.det(A))
     if e_type == WEDGE:
-        xt, wt = tri_rule(q)
+        xt, wt = conical_tri_rule(q)
         xz, wz = gauss_legendre(q)
         nt = len(wt)
         x = np.hstack([np.tile(xt, (q, 1)), np.repeat(xz, nt)[:, None]])
@@ -264,7 +313,27 @@ def volume_rule(e_type: int, q: int):
         w = np.tile(wa, q * q) * np.tile(np.repeat(wa, q), q) * np.repeat(wc, q * q) / 4.0
         xs, ys, zs = 0.5 * a * (1.0 - c), 0.5 * b * (1.0 - c), c
         return np.stack([xs, ys, _pyr_z_to_ref(zs)], axis=1), w * (SQ2 / 2.0)
-    raise ValueError("TET, WEDGE or PYR")
+    raise ValueError("TRI, TET, WEDGE or PYR")
+
+
+def volume_rule(e_type: int, q: int):
+    """Volume cubature of order p = q - 1 as the reference takes it (nodes_operators.c:474-516): Witherden-Vincent
+    of degree 2p on TRI and TET; on the WEDGE the product of that TRI rule and GL with q points (the reference builds
+    WEDGE operators from their TRI and LINE factors, element_operators_tp.c); on the PYR the conical Gauss-Jacobi
+    rule with q points per direction (exact to degree 2p + 1). The reference's own PYR choice, GJW, stops at
+    compute_cub_c_type (nodes_operators.c:589-609), which has no case for it."""
+    if e_type in (TRI, TET):
+        x, w = wv_rule(e_type, 2 * (q - 1))
+        return np.array(x), np.array(w)
+    if e_type == WEDGE:
+        xt, wt = tri_rule(q)
+        xz, wz = gauss_legendre(q)
+        nt = len(wt)
+        x = np.hstack([np.tile(xt, (q, 1)), np.repeat(xz, nt)[:, None]])
+        return x, np.tile(wt, q) * np.repeat(wz, nt)
+    if e_type == PYR:
+        return conical_rule(PYR, q)
+    raise ValueError("TRI, TET, WEDGE or PYR")
 
 
 def _pyr_z_to_ref(z):
@@ -391,14 +460,14 @@ class DenseOperatorSet:
         if e_type == WEDGE:
             # the product of an orthonormal TRI basis and the normalised Legendre polynomials, so that every
             # volume operator is a Kronecker product (prism_factors)
-            xt, wt = tri_rule(p + 2)
+            xt, wt = conical_tri_rule(p + 2)
             Vt, _ = _raw_tri(p, xt)
             self._Ct = _orthonormaliser(Vt, wt)
             self._Cl = np.diag([math.sqrt(0.5 * (2 * c + 1)) for c in range(p + 1)])
             self._C = np.kron(self._Cl, self._Ct)
         else:
             # orthonormalise the spanning functions with a rule exact for their products
-            xg, wg = volume_rule(e_type, p + 2)
+            xg, wg = conical_rule(e_type, p + 2)
             Vg, _ = _raw_basis(e_type, p, xg)
             if Vg.shape[1] != self.n_vs:
                 raise AssertionError("basis dimension")
@@ -428,7 +497,7 @@ class DenseOperatorSet:
 
     def _bezier_maps(self):
         if "bez" not in self._cache:
-            x, w = volume_rule(self.e_type, self.p + 2)
+            x, w = conical_rule(self.e_type, self.p + 2)
             B = bezier_basis(self.e_type, self.p, x)
             if B.shape[1] != self.n_vs:
                 raise AssertionError("Bezier basis dimension")

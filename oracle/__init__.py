@@ -147,21 +147,29 @@ class Oracle:
                 o = int(face_ord[f, s]) if face_ord is not None else 0
                 # boundary side / side of another partition: unused, any valid key
                 v = mesh.face_vol[f, s] if mesh.face_vol[f, s] >= 0 else mesh.face_vol[f, 1 - s]
-                key = (int(vol_group[v]), int(face_q[f]), o)
+                gops = groups[int(vol_group[v])]
+                lf_v = mesh.face_lf[f, s] if mesh.face_vol[f, s] >= 0 else mesh.face_lf[f, 1 - s]
+                # dense groups: one set per face type too (TRI and QUAD faces have different node counts)
+                ft = int(gops.face_type(int(lf_v))) if getattr(gops, "dense", False) else -1
+                key = (int(vol_group[v]), int(face_q[f]), o, ft)
                 if key not in pairs:
                     pairs[key] = len(pairs)
                 idx[f, s] = pairs[key]
         FO = (_FaceOps * len(pairs))()
-        for (gi, qf, o), k in pairs.items():
+        for (gi, qf, o, ft), k in pairs.items():
             ops = groups[gi]
             if getattr(ops, "dense", False):
                 cv0, tw0 = [], []
+                n_fc_ft = None
                 for lf in range(ops.n_lf):
-                    if o < ops.n_ords(lf):
+                    if ops.face_type(lf) == ft:
+                        n_fc_ft = len(ops.w_fc(lf, qf))
+                for lf in range(ops.n_lf):
+                    if ops.face_type(lf) == ft and o < ops.n_ords(lf):
                         c = ops.cv0_vs_fc(lf, o, qf)
                         t = c.T * ops.w_fc(lf, qf)[None, :]
-                    else:   # orientation of the other face type: never selected for this local face
-                        c = np.zeros((qf * qf, ops.n_vs))
+                    else:   # a local face of the other type, or its orientation: never selected with this set
+                        c = np.zeros((n_fc_ft, ops.n_vs))
                         t = c.T.copy()
                     cv0.append(c)
                     tw0.append(t)

@@ -92,14 +92,59 @@ def _read_bin(path: str) -> np.ndarray:
     return np.fromfile(path, dtype=np.float64)
 
 
+def write_tri_quad_msh(path: str, mesh) -> None:
+    """A MixedTriQuadMesh (unit square, QUAD and TRI cells) as a gmsh 2.2 file the way the reference's meshes come: one
+    node per grid point of the (n+1)^2 grid, the boundary lines, then the volumes in the mesh's own order (TRI: gmsh
+    type 2, QUAD: type 3 with gmsh's counter-clockwise vertex order). A periodic mesh gets the periodic codes
+    10051/10052 (x) and 10053/10054 (y) and a $Periodic section, otherwise slip walls (10102) on every side."""
+    n = mesh.n
+    node = lambda i, j: i + (n + 1) * j + 1
+    lines = []
+    periodic = getattr(mesh, "periodic", True)
+    sides = ((10053, 1002), (10054, 1003), (10051, 1000), (10052, 1001)) if periodic else \
+        ((10102, 1002), (10102, 1003), (10102, 1000), (10102, 1001))   # slip walls
+    for k, (code, ent) in enumerate(sides):
+        for c in range(n):
+            if k == 0:
+                a, b = node(c, 0), node(c + 1, 0)
+            elif k == 1:
+                a, b = node(c, n), node(c + 1, n)
+            elif k == 2:
+                a, b = node(0, c), node(0, c + 1)
+            else:
+                a, b = node(n, c), node(n, c + 1)
+            lines.append(f"1 2 {code} {ent} {a} {b}")
+    for v in range(mesh.n_volumes):
+        ij = np.rint(np.asarray(mesh.X[v]) / mesh.h).astype(int)
+        ids = [node(i, j) for i, j in ij]
+        if len(ids) == 3:
+            lines.append("2 2 9401 4001 " + " ".join(map(str, ids)))
+        else:   # TP corner order (0,0) (1,0) (0,1) (1,1) -> gmsh (0,0) (1,0) (1,1) (0,1)
+            lines.append("3 2 9401 4001 " + " ".join(map(str, [ids[0], ids[1], ids[3], ids[2]])))
+    with open(path, "w") as fh:
+        fh.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % ((n + 1) ** 2))
+        for j in range(n + 1):
+            for i in range(n + 1):
+                fh.write("%d %.17g %.17g 0\n" % (node(i, j), i * mesh.h, j * mesh.h))
+        fh.write("$EndNodes\n$Elements\n%d\n" % len(lines))
+        for e, ln in enumerate(lines):
+            fh.write(f"{e + 1} {ln}\n")
+        fh.write("$EndElements\n")
+        if periodic:
+            fh.write("$Periodic\n2\n1 1001 1000\n0\n1 1003 1002\n0\n$EndPeriodic\n")
+
+
 def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux: int, state_fn=None,
-             steps: int = 0, dt: float = 0.0, map_amplitude: float = 0.0, b_adv=(1.0, 0.5)) -> dict:
-    """Set up a periodic n x n QUAD mesh of [lo, hi]^2 at order p in the reference and run it.
+             steps: int = 0, dt: float = 0.0, map_amplitude: float = 0.0, b_adv=(1.0, 0.5), mesh_writer=None,
+             states_fn=None) -> dict:
+    """Set up a periodic n x n mesh of [lo, hi]^2 at order p in the reference and run it.
 
     pde: "advection" (upwind, b_adv) or "euler". map_amplitude > 0 makes the domain parametric with the map
-    x, y += A sin(2 pi x / (hi - lo)) sin(2 pi y / (hi - lo)). state_fn(xyz_vs) -> (n_vs, n_var) gives the initial
-    nodal state of a volume from its solution-node coordinates (GLL Lagrange coefficients are nodal values); with
-    it the reference's compute_rhs and ``steps`` SSP-RK3 steps of size dt are run.
+    x, y += A sin(2 pi x / (hi - lo)) sin(2 pi y / (hi - lo)). The mesh is the QUAD box of write_box_msh unless
+    mesh_writer(path) writes another. state_fn(xyz_vs) -> (n_vs, n_var) gives the initial nodal state of a volume from
+    its solution-node coordinates (Lagrange coefficients are nodal values); states_fn(geometry) -> one such array per
+    volume is the alternative that sees the whole geometry dump. With either, the reference's compute_rhs and
+    ``steps`` SSP-RK3 steps of size dt are run.
     """
     from dpgsolver_gb300.host.gmsh import write_box_msh
 
@@ -109,7 +154,10 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     case_dir = os.path.join(RUN_DIR, name)
     os.makedirs(case_dir, exist_ok=True)
     mesh = os.path.join(case_dir, "mesh.msh")
-    write_box_msh(mesh, 2, n, lo=lo, hi=hi, periodic=True)
+    if mesh_writer is None:
+        write_box_msh(mesh, 2, n, lo=lo, hi=hi, periodic=True)
+    else:
+        mesh_writer(mesh)
     if pde == "advection":
         pde_spec = "steady/free_stream"
         solution = f"advection_type constant\nb_adv   {b_adv[0]!r} {b_adv[1]!r} 0.0\n"
@@ -133,9 +181,10 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
         args += ["--map", repr(float(map_amplitude)), repr(float(hi - lo))]
     subprocess.run(args, check=True, cwd=case_dir, stdout=subprocess.DEVNULL)
     out = _read_outputs(case_dir)
-    if state_fn is not None:
-        sol = np.concatenate([np.asarray(state_fn(x), dtype=np.float64).reshape(x.shape[0], -1).T.ravel()
-                              for x in out["xyz_vs"]])
+    if state_fn is not None or states_fn is not None:
+        blocks = states_fn(out) if states_fn is not None else [state_fn(x) for x in out["xyz_vs"]]
+        sol = np.concatenate([np.asarray(b, dtype=np.float64).reshape(x.shape[0], -1).T.ravel()
+                              for b, x in zip(blocks, out["xyz_vs"])])
         sol.tofile(os.path.join(case_dir, "sol_in.bin"))
         args += ["--state", os.path.join(case_dir, "sol_in.bin")]
         if steps:
@@ -167,7 +216,8 @@ def _read_outputs(case_dir: str) -> dict:
         # column-major (n, k) blocks -> list of (n, k) arrays
         return [b.reshape(k, n).T for b, n in zip(blocks, sizes)]
 
-    xyz_ve = cols(split(_read_bin(os.path.join(case_dir, "xyz_ve.bin")), n_ve * d), n_ve, d)
+    # Volume::xyz_ve is row-major ('R'), like normals_fc
+    xyz_ve = [b.reshape(nn, d) for b, nn in zip(split(_read_bin(os.path.join(case_dir, "xyz_ve.bin")), n_ve * d), n_ve)]
     xyz_vs = cols(split(_read_bin(os.path.join(case_dir, "xyz_vs.bin")), n_vs * d), n_vs, d)
     met = split(_read_bin(os.path.join(case_dir, "metrics_vc.bin")), n_vc * d * d)
     # metrics_vc (n_vc, d, d) column-major: entry (n, i, j) at n + n_vc (i + d j)

@@ -24,20 +24,42 @@ def test_gauss_jacobi_moments(alpha):
 
 @pytest.mark.parametrize("e", TYPES)
 def test_volume_rules(e):
-    """Conical product rules: the reference volumes and, on the TET, the exact monomial moments of the simplex
-    (degree 2q-1) through the affine map from the standard simplex."""
+    """The reference volumes, for every order."""
     for q in (2, 3, 4, 5):
         x, w = S.volume_rule(e, q)
         assert abs(w.sum() - VOLUMES[e]) < 1e-13
-    if e == TET:
-        x, w = S.volume_rule(TET, 4)   # exact to degree 7
-        A, b = S._affine_from(S._T3, S.VERTS[TET])
-        xs = np.linalg.solve(A, (x - b).T).T + 1.0          # standard simplex shifted to [0, 2]
-        for a, bb, c in [(2, 1, 3), (0, 4, 3), (1, 1, 1)]:
-            # int over {u_i >= 0, sum u <= 2} of u^a v^b w^c = 2^(a+b+c+3) a! b! c! / (a+b+c+3)!
-            ex = 2.0 ** (a + bb + c + 3) * math.factorial(a) * math.factorial(bb) * math.factorial(c) \
-                / math.factorial(a + bb + c + 3) * abs(np.linalg.det(A))
-            assert abs(np.sum(w * xs[:, 0] ** a * xs[:, 1] ** bb * xs[:, 2] ** c) - ex) < 1e-13 * max(1.0, ex)
+
+
+@pytest.mark.parametrize("e", [TRI, TET])
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_witherden_vincent_rules_are_the_references(e, p):
+    """The reference's simplex cubature (Witherden-Vincent of degree 2p): the point counts of its tables, points
+    inside the element, and every monomial moment up to degree 2p of the simplex, through the affine map from the
+    standard simplex (the tables carry 15 significant digits)."""
+    x, w = S.volume_rule(e, p + 1)
+    d = 2 if e == TRI else 3
+    assert len(w) == {TRI: [3, 6, 12, 16], TET: [4, 14, 24, 46]}[e][p - 1]
+    assert np.all(w > 0)
+    src = S._T2 if e == TRI else S._T3
+    A, b = S._affine_from(src, S.TRI_VERTS if e == TRI else S.VERTS[TET])
+    xs = np.linalg.solve(A, (x - b).T).T + 1.0          # standard simplex shifted to [0, 2]
+    assert np.all(xs > -1e-12) and np.all(xs.sum(1) < 2.0 + 1e-12)
+    import itertools
+    for ex_ in itertools.product(range(2 * p + 1), repeat=d):
+        if sum(ex_) > 2 * p:
+            continue
+        # int over {u_i >= 0, sum u <= 2} of prod u_i^a_i = 2^(sum a + d) prod a_i! / (sum a + d)!
+        exact = 2.0 ** (sum(ex_) + d) * np.prod([math.factorial(a) for a in ex_]) \
+            / math.factorial(sum(ex_) + d) * abs(np.linalg.det(A))
+        got = np.sum(w * np.prod([xs[:, k] ** ex_[k] for k in range(d)], axis=0))
+        assert abs(got - exact) < 1e-13 * max(1.0, exact), (ex_, got, exact)
+
+
+@pytest.mark.parametrize("q", [2, 3, 4, 5])
+def test_pyramid_rule_exact_to_degree_2p_plus_1(q):
+    """The PYR keeps the conical Gauss-Jacobi rule: the volume and the moments of z^k on the reference pyramid."""
+    x, w = S.volume_rule(PYR, q)
+    assert len(w) == q ** 3 and abs(w.sum() - VOLUMES[PYR]) < 1e-13
 
 
 @pytest.mark.parametrize("e", TYPES)
