@@ -180,13 +180,45 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 	c->fc_off[nF] = fo;
 	(void)d;
 
-	/* M = cv0_vs_vc^T diag(w_vc J_vc) cv0_vs_vc, m_inv = M^-1 (volume_solver_T.c:115-145) */
+	/* M = cv0_vs_vc^T diag(w_vc J_vc) cv0_vs_vc, m_inv = M^-1 (volume_solver_T.c:115-145). A volume whose J is the
+	 * same at every cubature node (an affine volume) has M = J M_ref: its inverse is the group's M_ref^-1 / J, formed
+	 * once per group (equal to inverting J M_ref up to rounding). */
 	c->m_inv = malloc(sizeof(double) * (mo ? mo : 1));
 	double* M = malloc(sizeof(double) * (size_t)c->max_vs * c->max_vs);
+	double** ref_inv = calloc((size_t)in->n_groups, sizeof(double*));
 	for (size_t v = 0; v < nV; ++v) {
-		const struct oracle_group* G = &in->groups[in->vol_group[v]];
+		const int g = in->vol_group[v];
+		const struct oracle_group* G = &in->groups[g];
 		const int n_vs = G->n_vs, n_vc = G->n_vc;
 		const double* J = &in->jacobian_det_vc[c->vc_off[v]];
+		int affine = 1;
+		for (int k = 1; k < n_vc && affine; ++k)
+			affine = (J[k] == J[0]);
+		if (affine) {
+			if (!ref_inv[g]) {
+				for (int i = 0; i < n_vs; ++i)
+					for (int j = 0; j < n_vs; ++j) {
+						double s = 0.0;
+						for (int k = 0; k < n_vc; ++k)
+							s += G->cv0_vs_vc[k * n_vs + i] * G->w_vc[k] * G->cv0_vs_vc[k * n_vs + j];
+						M[i * n_vs + j] = s;
+					}
+				ref_inv[g] = malloc(sizeof(double) * (size_t)n_vs * n_vs);
+				const int st = invert(n_vs, M, ref_inv[g]);
+				if (st != ORACLE_OK) {
+					for (int k = 0; k < in->n_groups; ++k)
+						free(ref_inv[k]);
+					free(ref_inv);
+					free(M);
+					oracle_destroy(c);
+					return st;
+				}
+			}
+			double* Mi = &c->m_inv[c->minv_off[v]];
+			for (int i = 0; i < n_vs * n_vs; ++i)
+				Mi[i] = ref_inv[g][i] / J[0];
+			continue;
+		}
 		for (int i = 0; i < n_vs; ++i)
 			for (int j = 0; j < n_vs; ++j) {
 				double s = 0.0;
@@ -196,12 +228,18 @@ int oracle_create(const struct oracle_problem* in, struct oracle_ctx** out)
 			}
 		int st = invert(n_vs, M, &c->m_inv[c->minv_off[v]]);
 		if (st != ORACLE_OK) {
+			for (int k = 0; k < in->n_groups; ++k)
+				free(ref_inv[k]);
+			free(ref_inv);
 			free(M);
 			oracle_destroy(c);
 			return st;
 		}
 	}
 	free(M);
+	for (int k = 0; k < in->n_groups; ++k)
+		free(ref_inv[k]);
+	free(ref_inv);
 	*out = c;
 	return ORACLE_OK;
 }

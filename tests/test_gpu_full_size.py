@@ -7,8 +7,10 @@ on the periodic mesh, per conserved variable), free-stream preservation (of the 
 rounding by 1/J, about 270 on these volumes), determinism and linearity of the JVP.
 
 The 32^3 state is the z-axis vortex plus 1e-3 density noise: its residual is a small difference of flux terms, and
-the oracle's own response to one-ulp input noise (the noise floor) is 1.3e-12 of max |R|. The residual is held to
-max(1e-12, 4 x that floor), as in test_gpu_ns.py; the RK state, O(1), is held to 1e-12.
+the oracle's own response to one-ulp input noise (the noise floor, measured in the test) is about 1.3e-12 of
+max |R|. That is the conditioning of the residual itself, not of an implementation: on the 2D vortex at 64^2 the
+reference's own residual moves by 1.06e-12 under one-ulp input noise (tests/test_reference_parity.py). The residual is
+held to max(1e-12, 2 x that floor); the RK state, O(1), is held to 1e-12.
 """
 import numpy as np
 import pytest
@@ -42,8 +44,8 @@ def test_headline_residual_and_step_match_oracle(gpu_lib, headline):
         r = sim.rhs
         sim.ssp_rk3_steps(prob.dt, 1)
         s = sim.sol_coef
-    assert rel(r, r_ref) <= max(TOL, 4.0 * floor)
-    assert abs(mx - mx_ref) <= max(TOL, 4.0 * floor) * mx_ref
+    assert rel(r, r_ref) <= max(TOL, 2.0 * floor)
+    assert abs(mx - mx_ref) <= max(TOL, 2.0 * floor) * mx_ref
     assert rel(s, s_ref) <= TOL
 
 
