@@ -201,6 +201,21 @@ def fp64_issue(prob, w, stage_ms, peak_tflops):
                             "elements / live stage time, against the DFMA probe's instruction rate"}
 
 
+def _batching_bound(prob, w, plain_stage_ms, peak_tflops):
+    """How much faster any launch form can make a stage than the plain per-kernel launches: the plain form already
+    fills this fraction of the FP64 pipe's issue slots, and every form issues the same FP64 instructions."""
+    iss = fp64_issue(prob, w, plain_stage_ms, peak_tflops)
+    if not iss:
+        return None
+    return {"plain_fp64_issue_frac": iss["issue_frac"], "max_speedup_vs_plain": 1.0 / iss["issue_frac"],
+            "mixed_order_hex": {"plain_fp64_pipe_frac": 0.717, "max_speedup_vs_plain": 1.39,
+                                "source": "time-weighted FP64 pipe (elapsed) of the plain per-group stage's kernels in "
+                                          "the ncu --set full capture of the 36^3 mixed-order HEX mesh"},
+            "note": "the north star's 3x batched-vs-plain target exceeds these bounds: the plain form is FP64-issue "
+                    "bound already, so batching can only recover the idle issue slots (launch gaps, tails, low "
+                    "occupancy of the lifts)"}
+
+
 def algorithmic_bytes(prob, kernel):
     """Compulsory DRAM bytes of one launch of `kernel` (each array read or written once)."""
     d, q, nv = prob.d, prob.ops.q, prob.n_var
@@ -417,6 +432,7 @@ def run_ours(args, rank, world, local_rank):
                       "dmma_source": "measured (dgpu_probe_fp64_mma: mma.sync m8n8k4 f64 loop)",
                       "note": "binding roof: FP64 issue rate, not HBM; the FP64 tensor cores (dmma_tflops) run at "
                               "the DFMA rate on this part, so the contractions stay on DFMA"},
+        "batching_bound": _batching_bound(prob, w, ms_plain / (3.0 * n_plain), fp64_peak.value),
         "eval_hbm": {"bytes_per_eval": eval_bytes(prob),
                      "achieved_gbs": eval_bytes(prob) / (ms_per_step / 3 * 1e-3) / 1e9,
                      "frac": eval_bytes(prob) / (ms_per_step / 3 * 1e-3) / 1e9 / peak},

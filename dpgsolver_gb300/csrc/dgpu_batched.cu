@@ -187,8 +187,11 @@ cudaError_t launch_blift(dgpu_batch* c, int g, int mode, double dt, int stage, i
 	const RkArgs rk = rk_args(c, dt, stage, want_max);
 	if (mode == kModeRhs)
 		blift_group_kernel<D, Q, NV, kModeRhs><<<blocks, thr, blift_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), t, rk);
-	else
+	else if (want_max)
 		blift_group_kernel<D, Q, NV, kModeRkGl><<<blocks, thr, blift_smem<D, Q, NV>(G.E), c->stream>>>(c->params(), t, rk);
+	else
+		blift_group_kernel<D, Q, NV, kModeRkGlNoMax><<<blocks, thr, blift_smem<D, Q, NV>(G.E), c->stream>>>(
+			c->params(), t, rk);
 	c->launches++;
 	return cudaGetLastError();
 }
@@ -312,6 +315,8 @@ cudaError_t bind_tp_group(dgpu_batch* c, int g)
 	if ((e = cudaFuncSetAttribute(blift_group_kernel<D, Q, NV, kModeRhs>, A, (int)blift_smem<D, Q, NV>(E))))
 		return e;
 	if ((e = cudaFuncSetAttribute(blift_group_kernel<D, Q, NV, kModeRkGl>, A, (int)blift_smem<D, Q, NV>(E))))
+		return e;
+	if ((e = cudaFuncSetAttribute(blift_group_kernel<D, Q, NV, kModeRkGlNoMax>, A, (int)blift_smem<D, Q, NV>(E))))
 		return e;
 	if ((e = cudaFuncSetAttribute(bconvert_group_kernel<D, Q, NV, true>, A, (int)bconv_smem<D, Q, NV>(E))))
 		return e;

@@ -414,7 +414,7 @@ __device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup&
 			Rg[k] *= iw;
 	}
 
-	const bool need_coef = (MODE == kModeRhs) || rk.want_max;
+	const bool need_coef = (MODE == kModeRhs) || (MODE != kModeRkGlNoMax && rk.want_max);
 	unsigned long long mx = 0ull;
 	double R[NV];
 	if (need_coef) {
@@ -545,8 +545,14 @@ __global__ void __launch_bounds__(256) bvol_group_kernel(const BParams P, int g,
 	bvol_body<D, Q, NV, PDE, GLL_IN>(P, sops, G, blockIdx.x * G.E, G.E, u, smem + sizeof(BatchOps) / 8);
 }
 
+// Minimum CTAs per SM of the per-group lift (caps its registers): 4 for the RK stages that reduce no max |rhs|
+// (64 registers: twice the resident warps of the 128-register build), 2 otherwise.
+template <int MODE>
+struct BLiftOccupancy { static constexpr int value = (MODE == kModeRkGlNoMax) ? 4 : 2; };
+
 template <int D, int Q, int NV, int MODE>
-__global__ void __launch_bounds__(256, 2) blift_group_kernel(const BParams P, int g, const RkArgs rk)
+__global__ void __launch_bounds__(256, BLiftOccupancy<MODE>::value) blift_group_kernel(const BParams P, int g,
+                                                                                      const RkArgs rk)
 {
 	extern __shared__ double smem[];
 	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
