@@ -149,6 +149,7 @@ EXPORTS = {
     "dgpu_kernel_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "dgpu_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "dgpu_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dgpu_set_source": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dgpu_halo_setup": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_int_p, c_int_p]),
     "dgpu_halo_buffers": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
                                          ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t)]),

@@ -79,6 +79,7 @@ struct dgpu_ctx {
 	unsigned long long* max_bits = nullptr;
 	int* err_flag = nullptr;
 	unsigned long long* n_corr = nullptr;
+	double* source = nullptr;             // the test case's source at the cubature nodes (dgpu_set_source), or null
 	// execution
 	cudaStream_t stream = nullptr;
 	bool own_stream = false;
@@ -145,6 +146,7 @@ struct dgpu_ctx {
 		P.ns_gv = ns_gv;
 		P.ns = ns_phys;
 		P.ns_eta = 1.01 * 2 * d;   // PENALTY_SCALING * NFMAX (compute_face_rlhs_dg_T.c:273-295)
+		P.source = source;
 		return P;
 	}
 };
@@ -432,6 +434,7 @@ cudaError_t launch_jvp_t(dgpu_ctx* c)
 	Pd.vol_gl = c->jv_vol;
 	Pd.traces = c->jv_traces;
 	Pd.nnf = c->jv_nnf;
+	Pd.source = nullptr;   // the source does not depend on the state
 	Pd.max_bits = nullptr;
 	cudaError_t e = PRIMAL ? cudaMemsetAsync(c->max_bits, 0, sizeof(unsigned long long), c->stream) : cudaSuccess;
 	if (e != cudaSuccess)
@@ -565,6 +568,7 @@ cudaError_t launch_ns_jvp_t(dgpu_ctx* c)
 	Pd.ns_gtr = c->ns_gtr_d;
 	Pd.ns_X = c->ns_X_d;
 	Pd.ns_gv = c->ns_gv_d;
+	Pd.source = nullptr;
 	Pd.max_bits = nullptr;
 	cudaError_t e = PRIMAL ? cudaMemsetAsync(c->max_bits, 0, sizeof(unsigned long long), c->stream) : cudaSuccess;
 	if (e != cudaSuccess)
@@ -647,20 +651,33 @@ cudaError_t bind_q(dgpu_ctx* c)
 	}
 }
 
+// Drops the captured step graphs (they hold the kernels' parameters by value: a stream or a buffer that changes makes
+// them stale); the next step captures again.
+void discard_graphs(dgpu_ctx* c)
+{
+	if (c->rk_graph) {
+		cudaGraphExecDestroy(c->rk_graph);
+		c->rk_graph = nullptr;
+	}
+	if (c->rk_graph_max) {
+		cudaGraphExecDestroy(c->rk_graph_max);
+		c->rk_graph_max = nullptr;
+	}
+	if (c->host_graph) {
+		cudaGraphExecDestroy(c->host_graph);
+		c->host_graph = nullptr;
+	}
+}
+
 void free_all(dgpu_ctx* c)
 {
-	if (c->rk_graph)
-		cudaGraphExecDestroy(c->rk_graph);
-	if (c->rk_graph_max)
-		cudaGraphExecDestroy(c->rk_graph_max);
-	if (c->host_graph)
-		cudaGraphExecDestroy(c->host_graph);
+	discard_graphs(c);
 	for (auto& t : c->timers) {
 		cudaEventDestroy(t.start);
 		cudaEventDestroy(t.stop);
 	}
 	c->timers.clear();
-	void* ptrs[] = {c->halo_send, c->halo_recv, c->halo_sbuf, c->halo_rbuf, c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
+	void* ptrs[] = {c->source, c->halo_send, c->halo_recv, c->halo_sbuf, c->halo_rbuf, c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
 	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X, c->ns_gv, c->ns_gtr_d, c->ns_X_d, c->ns_gv_d,
 	                c->bnd, c->bc_code, c->bc_ext, c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
@@ -1529,18 +1546,7 @@ dgpu_status dgpu_set_stream(dgpu_ctx* c, void* stream)
 		cudaStreamDestroy(c->stream);
 	c->own_stream = false;
 	c->stream = (cudaStream_t)stream;
-	if (c->rk_graph) {
-		cudaGraphExecDestroy(c->rk_graph);
-		c->rk_graph = nullptr;
-	}
-	if (c->rk_graph_max) {
-		cudaGraphExecDestroy(c->rk_graph_max);
-		c->rk_graph_max = nullptr;
-	}
-	if (c->host_graph) {
-		cudaGraphExecDestroy(c->host_graph);
-		c->host_graph = nullptr;
-	}
+	discard_graphs(c);
 	return DGPU_OK;
 }
 
@@ -2725,3 +2731,30 @@ dgpu_status dgpu_halo_stage_end(dgpu_ctx* c, double dt, int stage, double* max_r
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------------------
+// Source term (compute_source_rhs_dg_like, src/simulation/solvers/compute_rlhs.c:47-57)
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" dgpu_status dgpu_set_source(dgpu_ctx* c, const double* source_vc)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	const size_t n = state_size(c);
+	if (!source_vc) {
+		if (c->source) {
+			DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+			cudaFree(c->source);
+			c->source = nullptr;
+			discard_graphs(c);
+		}
+		return DGPU_OK;
+	}
+	if (!c->source) {
+		DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->source, n * sizeof(double)));
+		discard_graphs(c);   // captured steps hold the kernels' parameters, the source pointer among them
+	}
+	DGPU_CUDA(c, cudaMemcpyAsync(c->source, source_vc, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+	DGPU_CUDA(c, cudaStreamSynchronize(c->stream));
+	return DGPU_OK;
+}

@@ -79,6 +79,10 @@ struct TPParams {
 	// formed, so that one pass over a caller's host buffer both uploads the state and starts the RK step.
 	double* keep_coef = nullptr;   // [v][NV][N]
 	double* keep_gl = nullptr;     // [v][NV][N]
+	// The test case's source term at the volume cubature nodes, or null (compute_source_rhs_dg_like,
+	// src/simulation/solvers/compute_rlhs.c:47-57). M^-1 tw0_vt_vc (J s) = V^-1 s on the GL nodes, so it adds to the
+	// GL nodal residual after the 1/(w J) scaling.
+	const double* source = nullptr;   // [v][NV][N]
 };
 
 // Right-hand state of face node i of boundary face b: the boundary value of its BC from the interior trace WL.
@@ -531,6 +535,10 @@ __device__ __forceinline__ void tp_lift_body(const TPOps* sops, const TPParams& 
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
 			Rg[k] *= iw;
+		if (P.source)
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				Rg[k] += P.source[((size_t)v * NV + k) * N + node];
 	}
 
 	const bool need_coef = (MODE == kModeRhs) || ((MODE == kModeRkGl || MODE == kModeRkGlOut) && rk.want_max);

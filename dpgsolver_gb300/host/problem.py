@@ -53,6 +53,8 @@ class DGProblem:
     bc_state: np.ndarray | None = None    # (n_faces, n_fc, n_var) exterior conserved state at the face nodes
     bc_data: tuple | None = None          # (p_back, t_total, p_total, r_s): BC_Data of boundary_euler_T.c:44-49
     ns: dict | None = None                # Navier-Stokes: {"viscosity": 101|102, "mu", "Pr", "r_s"}
+    source_vc: np.ndarray | None = None   # (n_volumes, n_var, n_vc): the test case's source at the volume cubature
+                                          # nodes (compute_source_rhs_dg_like), before the J scaling
 
     @property
     def n_var(self) -> int:
@@ -106,6 +108,7 @@ def flat_arrays(prob) -> dict:
         "bc_fc": None if prob.bc is None else np.ascontiguousarray(prob.bc, dtype=np.int32),
         "bc_state_fc": None if prob.bc_state is None else np.ascontiguousarray(prob.bc_state).ravel(),
         "bc_data": prob.bc_data,
+        "source_vc": None if prob.source_vc is None else np.ascontiguousarray(prob.source_vc).ravel(),
     }
 
 
@@ -170,6 +173,43 @@ def advection_2d(n: int = 16, p: int = 2, b=(1.0, 0.5), cfl: float = 0.1, n_step
     prob.dt = cfl * h / float(np.linalg.norm(b_adv))
     prob.meta.update(n=n, p=p, h=h, cfl=cfl)
     return prob
+
+
+# constants of the reference's steady linear-advection case u = sin(M x + A) sin(M y + A)
+# (solution_advection_default_T.c:38-39)
+SOURCE_M = 2.15
+SOURCE_A = 0.23
+
+
+def advection_default_2d(n: int = 8, p: int = 3, b=(1.0, 0.5), amplitude: float = 0.05, cfl: float = 0.1,
+                         n_steps: int = 20, periodic: bool = True) -> DGProblem:
+    """The reference's steady linear-advection case with a source ("steady/default",
+    solution_advection_default_T.c): u = sin(M x + A) sin(M y + A), source s = b . grad u at the volume cubature
+    nodes, on a QUAD mesh of [-1,1]^2 mapped by x, y += amplitude sin(pi x) sin(pi y) (parametric: the mapped faces
+    blended into the volumes). The state starts at u on the solution nodes. periodic=False puts upwind boundaries
+    (BC_UPWIND) on the four sides with u as the exterior state, where u is the steady solution (the periodic mesh
+    leaves a jump of u at the seams, u not being periodic on [-1,1])."""
+    mesh = StructuredMesh(2, n, -1.0, 1.0, periodic=(True, True) if periodic else (False, False))
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops, deform=sinusoidal_deform_2d(amplitude, 2.0), curved=True, parametric=True)
+    b_adv = np.array([b[0], b[1], 0.0])
+    prob = DGProblem("advection_default_2d", 2, PDE_ADVECTION, NUM_FLUX_UPWIND, False, b_adv, ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, 1, ops.n_vs)), dt=0.0, n_steps=n_steps)
+    xyz = prob.solution_node_xyz()
+    prob.sol[:, 0, :] = np.sin(SOURCE_M * xyz[..., 0] + SOURCE_A) * np.sin(SOURCE_M * xyz[..., 1] + SOURCE_A)
+    x, y = geom.xyz_vc[..., 0], geom.xyz_vc[..., 1]
+    sx, cx = np.sin(SOURCE_M * x + SOURCE_A), np.cos(SOURCE_M * x + SOURCE_A)
+    sy, cy = np.sin(SOURCE_M * y + SOURCE_A), np.cos(SOURCE_M * y + SOURCE_A)
+    prob.source_vc = (b[0] * SOURCE_M * cx * sy + b[1] * SOURCE_M * sx * cy)[:, None, :]
+    h = float(mesh.h[0])
+    prob.dt = cfl * h / float(np.linalg.norm(b_adv))
+    prob.meta.update(n=n, p=p, h=h, cfl=cfl, amplitude=amplitude)
+    if periodic:
+        return prob
+
+    def ext(xy):
+        return (np.sin(SOURCE_M * xy[:, 0] + SOURCE_A) * np.sin(SOURCE_M * xy[:, 1] + SOURCE_A))[:, None]
+    return _set_boundaries(prob, {(dd, sd): BC_UPWIND for dd in range(2) for sd in range(2)}, ext)
 
 
 def euler_vortex_2d(n: int = 64, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, amplitude: float = 0.05,

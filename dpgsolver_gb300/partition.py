@@ -157,6 +157,8 @@ class Partition:
             sub.bc = np.ascontiguousarray(prob.bc[self.faces])
         if prob.bc_state is not None:
             sub.bc_state = np.ascontiguousarray(prob.bc_state[self.faces])
+        if getattr(prob, "source_vc", None) is not None:
+            sub.source_vc = np.ascontiguousarray(prob.source_vc[self.volumes])
         return sub
 
     def local_state(self, sol: np.ndarray) -> np.ndarray:

@@ -141,6 +141,8 @@ class Simulation:
         if stream is not None:
             check(lib.dgpu_set_stream(h, ctypes.c_void_p(stream)), h)
         self.upload_state(prob.sol)
+        if getattr(prob, "source_vc", None) is not None:
+            self.set_source(prob.source_vc)
 
     # -- lifetime ------------------------------------------------------------------------------------------------
     def close(self):
@@ -181,6 +183,16 @@ class Simulation:
         return out
 
     # -- compute -------------------------------------------------------------------------------------------------
+    def set_source(self, source_vc):
+        """The test case's source at the volume cubature nodes, in the state's shape (None removes it)."""
+        if source_vc is None:
+            check(self._lib.dgpu_set_source(self._h, None), self._h)
+            return
+        s = np.ascontiguousarray(source_vc, dtype=np.float64)
+        if s.shape != self.shape:
+            raise ValueError(f"source shape {s.shape} != {self.shape}")
+        check(self._lib.dgpu_set_source(self._h, _dp(s)), self._h)
+
     def compute_rhs(self, want_max: bool = True):
         mx = ctypes.c_double()
         check(self._lib.dgpu_compute_rhs(self._h, ctypes.byref(mx) if want_max else None), self._h)

@@ -290,6 +290,15 @@ dgpu_status dgpu_set_stream(dgpu_ctx* ctx, void* cuda_stream);
  * "tp_face_kernel", "tp_lift_kernel"). Measurement aids; no reference counterpart. */
 dgpu_status dgpu_set_kernel_timing(dgpu_ctx* ctx, int enable);
 dgpu_status dgpu_kernel_time(dgpu_ctx* ctx, const char* name, double* total_ms, long long* count);
+/* Source term of the test case: compute_source_rhs_dg_like (src/simulation/solvers/compute_rlhs.c:47-57), called by
+ * compute_rlhs_common_dg (src/simulation/solvers/dg/solve_dg.c:188), which adds tw0_vt_vc (J_vc s) to every volume's
+ * rhs before M^-1 (e.g. compute_source_rhs_advection_default_T, solution_advection_default_T.c:79-94). source_vc:
+ * host, per volume (n_vc x n_var) column-major, the test case's source at the volume cubature nodes (what its
+ * constructor_source_* returns, before the J scaling), in the state's layout (n_vc = n_vs for these elements); NULL
+ * removes it. The values are copied. Every later residual and RK stage of this context includes the source, and so
+ * does the primal of the linearisations (their derivatives do not depend on it). */
+dgpu_status dgpu_set_source(dgpu_ctx* ctx, const double* source_vc);
+
 /* Text of the last error recorded on this context (or of the last failed dgpu_create when ctx is NULL). */
 const char* dgpu_last_error(const dgpu_ctx* ctx);
 

@@ -44,7 +44,7 @@ class _Problem(ctypes.Structure):
         ("nc_fc", _c_int_p), ("normals_fc", _c_double_p), ("jacobian_det_fc", _c_double_p),
         ("bc_fc", _c_int_p), ("bc_state_fc", _c_double_p), ("bc_data", ctypes.c_double * 4),
         ("viscosity", ctypes.c_int), ("mu", ctypes.c_double), ("Pr", ctypes.c_double), ("r_s", ctypes.c_double),
-        ("dTdn", ctypes.c_double),
+        ("dTdn", ctypes.c_double), ("source_vc", _c_double_p),
     ]
 
 
@@ -211,6 +211,8 @@ class Oracle:
         if ns is not None:
             P.viscosity, P.mu, P.Pr, P.r_s = int(ns["viscosity"]), float(ns["mu"]), float(ns["Pr"]), float(ns["r_s"])
             P.dTdn = float(ns.get("dTdn", 0.0))
+        if fl.get("source_vc") is not None:
+            P.source_vc = _dp(arr(fl["source_vc"]))
         self._keep = (keep, G, FO, P)
         h = ctypes.c_void_p()
         st = lib.oracle_create(ctypes.byref(P), ctypes.byref(h))

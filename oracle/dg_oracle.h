@@ -81,6 +81,11 @@ struct oracle_problem {
 	 * constant_zero), which sets the wall's normal energy flux nf_E = -mu Cp / Pr dTdn (get_normal_flux_Energy,
 	 * solution_navier_stokes.c:93-150). */
 	double dTdn;
+	/* Source term of the test case: per volume (n_vc x n_var) column-major, the source at the volume cubature nodes
+	 * before the J scaling (what constructor_source_* returns), or NULL. compute_source_rhs_dg_like
+	 * (compute_rlhs.c:47-57) adds tw0_vt_vc (J_vc s) to each volume's rhs
+	 * (compute_source_rhs_advection_default_T, solution_advection_default_T.c:79-94). */
+	const double* source_vc;
 };
 
 struct oracle_ctx;

@@ -684,6 +684,19 @@ static int SUF(residual_raw)(const struct oracle_ctx* c, const Type* sol, Type* 
 		for (int dim = 0; dim < d; ++dim)
 			SUF(mm_acc)(n_vs, n_vc, neq, 1.0, &G->tw1_vt_vc[(size_t)dim * n_vs * n_vc],
 			            &fr[(size_t)n_vc * neq * dim], r);
+		/* rhs += tw0_vt_vc (J_vc s), tw0_vt_vc = cv0_vs_vc^T diag(w_vc) (compute_source_rhs_dg_like,
+		 * compute_rlhs.c:47-57; solution_advection_default_T.c:79-94) */
+		if (P->source_vc) {
+			const double* sv = &P->source_vc[c->vc_off[v] * nv];
+			const double* J = &P->jacobian_det_vc[c->vc_off[v]];
+			for (int k = 0; k < neq; ++k)
+				for (int i = 0; i < n_vs; ++i) {
+					double acc = 0.0;
+					for (int n = 0; n < n_vc; ++n)
+						acc += G->cv0_vs_vc[(size_t)n * n_vs + i] * (G->w_vc[n] * (J[n] * sv[n + (size_t)n_vc * k]));
+					r[i + (size_t)n_vs * k] += acc;
+				}
+		}
 	}
 
 	/* ---- face term ---- */

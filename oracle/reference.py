@@ -136,7 +136,7 @@ def write_tri_quad_msh(path: str, mesh) -> None:
 
 def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux: int, state_fn=None,
              steps: int = 0, dt: float = 0.0, map_amplitude: float = 0.0, b_adv=(1.0, 0.5), mesh_writer=None,
-             states_fn=None) -> dict:
+             states_fn=None, pde_spec: str | None = None) -> dict:
     """Set up a periodic n x n mesh of [lo, hi]^2 at order p in the reference and run it.
 
     pde: "advection" (upwind, b_adv) or "euler". map_amplitude > 0 makes the domain parametric with the map
@@ -144,7 +144,8 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     mesh_writer(path) writes another. state_fn(xyz_vs) -> (n_vs, n_var) gives the initial nodal state of a volume from
     its solution-node coordinates (Lagrange coefficients are nodal values); states_fn(geometry) -> one such array per
     volume is the alternative that sees the whole geometry dump. With either, the reference's compute_rhs and
-    ``steps`` SSP-RK3 steps of size dt are run.
+    ``steps`` SSP-RK3 steps of size dt are run. pde_spec overrides the test case (advection: "steady/free_stream",
+    no source; "steady/default", the source of solution_advection_default_T.c).
     """
     from dpgsolver_gb300.host.gmsh import write_box_msh
 
@@ -159,10 +160,10 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     else:
         mesh_writer(mesh)
     if pde == "advection":
-        pde_spec = "steady/free_stream"
+        pde_spec = pde_spec or "steady/free_stream"
         solution = f"advection_type constant\nb_adv   {b_adv[0]!r} {b_adv[1]!r} 0.0\n"
     elif pde == "euler":
-        pde_spec = "periodic/periodic_vortex"
+        pde_spec = pde_spec or "periodic/periodic_vortex"
         solution = ("r_v   0.165\ntheta 0.7853981633974483\nV_inf 0.5916079783099616\np_inf 1.0\nt_inf 1.0\n"
                     "Rg    1.0\n\np_frac 0.05\n")
     else:
@@ -240,6 +241,11 @@ def _advection_state(x):
     return np.sin(np.pi * x[:, 0]) * np.sin(np.pi * x[:, 1])
 
 
+def _advection_default_state(x):
+    from dpgsolver_gb300.host.problem import SOURCE_A, SOURCE_M
+    return np.sin(SOURCE_M * x[:, 0] + SOURCE_A) * np.sin(SOURCE_M * x[:, 1] + SOURCE_A)
+
+
 def _vortex_state(x):
     from dpgsolver_gb300.host.problem import isentropic_vortex, primitive_to_conserved
     rho, u, v, pr = isentropic_vortex(x, 5.0, 5.0, 5.0)
@@ -250,9 +256,12 @@ def _vortex_state(x):
 # (QUAD 16^2 on [-1,1]^2, p = 2, b = (1, 0.5), upwind, u0 = sin(pi x) sin(pi y), dt = 0.1 h / |b|, 100 steps);
 # the "c2*" cases are the curved isentropic-vortex configuration (QUAD on [0,10]^2 mapped by
 # 0.05 sin(pi x/5) sin(pi y/5), vortex strength 5 at (5,5) on (1,1,1,1)) on smaller meshes and other fluxes and
-# orders; "c2" itself (64^2, p = 3, Roe) is run live by the CPU tests.
+# orders; "c2" itself (64^2, p = 3, Roe) is run live by the CPU tests. "c1_source" is the reference's steady
+# advection case with a source term (steady/default: u = sin(2.15 x + 0.23) sin(2.15 y + 0.23), s = b . grad u) on
+# a periodic QUAD 8^2 mesh of [-1,1]^2 mapped by 0.05 sin(pi x) sin(pi y), p = 3, upwind, 20 steps.
 CASES = {
     "c1": ("advection", 16, 2, 11, 100),
+    "c1_source": ("advection_default", 8, 3, 11, 20),
     "c2_n8": ("euler", 8, 3, 31, 1000),
     "c2_lf_n8": ("euler", 8, 3, 32, 20),
     "c2_p1_n8": ("euler", 8, 1, 32, 20),
@@ -267,6 +276,8 @@ def host_problem(name: str):
     pde, n, p, flux, steps = CASES[name]
     if pde == "advection":
         return P.advection_2d(n, p)
+    if pde == "advection_default":
+        return P.advection_default_2d(n, p, n_steps=steps)
     return P.euler_vortex_2d(n=n, p=p, num_flux=flux)
 
 
@@ -276,6 +287,9 @@ def run_named(name: str) -> dict:
     prob = host_problem(name)
     if pde == "advection":
         return run_case(name, pde, n, p, -1.0, 1.0, flux, state_fn=_advection_state, steps=steps, dt=prob.dt)
+    if pde == "advection_default":
+        return run_case(name, "advection", n, p, -1.0, 1.0, flux, state_fn=_advection_default_state, steps=steps,
+                        dt=prob.dt, map_amplitude=prob.meta["amplitude"], pde_spec="steady/default")
     return run_case(name, pde, n, p, 0.0, 10.0, flux, state_fn=_vortex_state, steps=steps, dt=prob.dt,
                     map_amplitude=0.05)
 

@@ -16,6 +16,7 @@ PROBLEMS = {
     "hex_roe_p2_6": lambda: P.euler_hex_3d(6, 2, num_flux=P.NUM_FLUX_ROE_PIKE),
     "hex_lf_p3_8": lambda: P.euler_hex_3d(8, 3),
     "channel2d_bc": lambda: P.euler_channel_2d(6, 2),
+    "adv2d_source_p3_8": lambda: P.advection_default_2d(8, 3, periodic=False),
 }
 
 

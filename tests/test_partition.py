@@ -25,6 +25,7 @@ PROBLEMS = {
     "hex_roe_p2_4": lambda: P.euler_hex_3d(4, 2, num_flux=P.NUM_FLUX_ROE_PIKE),
     "hex_lf_p1_5": lambda: P.euler_hex_3d(5, 1),
     "channel2d_bc": lambda: P.euler_channel_2d(6, 2),
+    "adv2d_source_p3_6": lambda: P.advection_default_2d(6, 3, periodic=False),
 }
 
 
