@@ -802,6 +802,9 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	c->sorted_off.resize(nV);
 	std::vector<double> gmet, inv_wJ;
 	std::vector<std::vector<double>> inv_J(c->n_dense);
+	// curved (non-affine) dense volumes: their group keeps a per-volume M^-1, formed from w J at every node
+	std::vector<char> dense_curved(c->n_dense, 0);
+	std::vector<std::vector<double>> dense_wJ(c->n_dense);
 	for (int g = 0; g < nG; ++g) {
 		const int N = g_nvc[g];
 		for (int e = 0; e < count[g]; ++e) {
@@ -817,11 +820,13 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 				if (!(J[n] > 0.0))
 					return reject(DGPU_ERR_INVALID_ARGUMENT, "non-positive jacobian_det_vc");
 			if (c->gl[g].dense) {
+				const int t = c->gl[g].idx;
 				for (int n = 1; n < N; ++n)
 					if (fabs(J[n] - J[0]) > 1e-12 * J[0])
-						return reject(DGPU_ERR_UNSUPPORTED,
-						              "TET/WEDGE/PYR volumes must be affine (constant jacobian_det_vc)");
-				inv_J[c->gl[g].idx].push_back(1.0 / J[0]);
+						dense_curved[t] = 1;
+				inv_J[t].push_back(1.0 / J[0]);
+				for (int n = 0; n < N; ++n)
+					dense_wJ[t].push_back(w[g][n] * J[n]);
 			} else {
 				for (int n = 0; n < N; ++n)
 					inv_wJ.push_back(1.0 / (w[g][n] * J[n]));
@@ -1120,6 +1125,24 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 		G.fops = d_fops;
 		G.fop_off = d_foff;
 		G.inv_J = d_ij;
+		G.minv_vol = nullptr;
+		if (dense_curved[t] && G.n_vol > 0) {
+			// a group with a curved volume: M^-1 = (cv0^T diag(w J) cv0)^-1 for each of its volumes
+			// (constructor_inverse_mass_T, volume_solver_T.c:115-145), formed on the device once
+			const size_t smem = dense_minv_smem(nvs);
+			if (smem > 227 * 1024)
+				return reject(DGPU_ERR_UNSUPPORTED, "curved dense group too large for the mass-matrix inversion");
+			double *d_wj = nullptr, *d_mv = nullptr;
+			B_TRY(upload_vec(&d_wj, dense_wJ[t]));
+			B_TRY(cudaMalloc((void**)&d_mv, (size_t)G.n_vol * nvs * nvs * sizeof(double)));
+			c->dense_bufs.push_back(d_mv);
+			B_TRY(cudaFuncSetAttribute(dense_minv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+			dense_minv_kernel<<<G.n_vol, 128, smem, c->stream>>>(d_cv0, d_wj, nvs, nvc, G.n_vol, d_mv);
+			B_TRY(cudaGetLastError());
+			B_TRY(cudaStreamSynchronize(c->stream));
+			B_TRY(cudaFree(d_wj));
+			G.minv_vol = d_mv;
+		}
 	}
 	B_TRY(upload_vec(&c->d_ops, c->hops));
 	B_TRY(upload_vec(&c->d_groups, c->hgroups));

@@ -44,6 +44,7 @@ struct DGroup {
 	const double* cv1;          // D x n_vc x n_vs
 	const double* minv;         // n_vs x n_vs (M_ref^-1)
 	const double* inv_J;        // per element 1 / J
+	const double* minv_vol;     // per element n_vs x n_vs M^-1 when the group has a curved volume, else null
 	const double* fops;         // face operator table
 	const long long* fop_off;   // [(lf * n_ord + ord) * (kQMax + 1) + q_f] -> offset in fops, -1 if absent
 	int vol_per_e, lift_per_e;  // shared memory per volume (doubles) of the volume and lift bodies

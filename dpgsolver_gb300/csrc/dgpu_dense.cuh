@@ -6,7 +6,8 @@
 // (w fr_j) (compute_rhs_v_dg_like_T, compute_volume_rlhs_T.c:166-177), face traces cv0_vs_fc s at the face's
 // canonical nodes, rhs -= cv0_vs_fc^T (w_f J_f F*) per face (compute_rhs_f_dg_like_T, compute_face_rlhs_T.c:
 // 297-310) and M^-1 (scale_rhs_by_m_inv_std, solve_dg.c:265-272). Volumes are affine (constant J), so
-// M^-1 = M_ref^-1 / J with M_ref = cv0^T diag(w) cv0 inverted once on the host.
+// M^-1 = M_ref^-1 / J with M_ref = cv0^T diag(w) cv0 inverted once on the host. A group with a curved volume (J
+// varying over the cubature nodes) keeps every volume's own M^-1 instead (dense_minv_kernel).
 //
 // One CTA handles E volumes of one group; every phase maps one thread to one output row of one volume (all
 // variables per thread), reading the operators through the L1 cache (they are shared by every CTA of the group)
@@ -446,15 +447,22 @@ __device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, con
 		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
 		const double* sr = smem + e * PER_E + k * nvs;
 		double R;
-		if (G.minv_identity) {
-			R = sr[m];
-		} else {
-			const double* row = minv + (long long)m * nvs;
+		if (G.minv_vol) {   // curved volumes: the volume's own M^-1
+			const double* row = G.minv_vol + ((long long)(e0 + e) * nvs + m) * nvs;
 			R = 0.0;
 			for (int a = 0; a < nvs; ++a)
 				R += __ldg(row + a) * sr[a];
+		} else {
+			if (G.minv_identity) {
+				R = sr[m];
+			} else {
+				const double* row = minv + (long long)m * nvs;
+				R = 0.0;
+				for (int a = 0; a < nvs; ++a)
+					R += __ldg(row + a) * sr[a];
+			}
+			R *= G.inv_J[e0 + e];
 		}
-		R *= G.inv_J[e0 + e];
 		const long long o = G.state_off + (long long)(e0 + e) * NV * nvs + rem;
 		if (MODE == kModeRhs || rk.want_max) {
 			const unsigned long long bits = abs_bits(R);
@@ -496,6 +504,56 @@ __device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, con
 // ---------------------------------------------------------------------------------------------------------------
 // Kernels: one launch per dense group, and the bodies the fused kernels dispatch to
 // ---------------------------------------------------------------------------------------------------------------
+
+// Shared memory of dense_minv_kernel: the augmented matrix [M | I] (n_vs x 2 n_vs) and one column.
+__host__ __device__ inline size_t dense_minv_smem(int nvs) { return (size_t)(2 * nvs * nvs + nvs) * sizeof(double); }
+
+// M^-1 of one curved volume per CTA (set-up, once per context): M = cv0^T diag(w J) cv0 (constructor_mass_T,
+// volume_solver_T.c:115-145) formed in shared memory, then inverted by Gauss-Jordan elimination. M is symmetric
+// positive definite, so the pivots (Schur complements) are positive and no row exchange is needed.
+// cv0: n_vc x n_vs; wJ: per volume n_vc values w_n J_n; minv: per volume n_vs x n_vs row-major.
+__global__ void __launch_bounds__(128) dense_minv_kernel(const double* __restrict__ cv0,
+                                                         const double* __restrict__ wJ, int nvs, int nvc,
+                                                         int n_vol, double* __restrict__ minv)
+{
+	extern __shared__ double sm[];
+	const int v = blockIdx.x;
+	if (v >= n_vol)
+		return;
+	const int w2 = 2 * nvs;
+	double* A = sm;                // [M | I]
+	double* col = sm + nvs * w2;   // column k before elimination step k
+	const double* wj = wJ + (long long)v * nvc;
+	for (int it = threadIdx.x; it < nvs * nvs; it += blockDim.x) {
+		const int a = it / nvs, b = it % nvs;
+		double s = 0.0;
+		for (int r = 0; r < nvc; ++r)
+			s += cv0[(long long)r * nvs + a] * wj[r] * cv0[(long long)r * nvs + b];
+		A[a * w2 + b] = s;
+		A[a * w2 + nvs + b] = (a == b) ? 1.0 : 0.0;
+	}
+	__syncthreads();
+	for (int k = 0; k < nvs; ++k) {
+		for (int i = threadIdx.x; i < nvs; i += blockDim.x)
+			col[i] = A[i * w2 + k];
+		__syncthreads();
+		const double inv_p = 1.0 / col[k];
+		for (int j = threadIdx.x; j < w2; j += blockDim.x)
+			A[k * w2 + j] *= inv_p;
+		__syncthreads();
+		for (int it = threadIdx.x; it < nvs * w2; it += blockDim.x) {
+			const int i = it / w2, j = it - i * w2;
+			if (i != k)
+				A[i * w2 + j] -= col[i] * A[k * w2 + j];
+		}
+		__syncthreads();
+	}
+	for (int it = threadIdx.x; it < nvs * nvs; it += blockDim.x) {
+		const int a = it / nvs, b = it % nvs;
+		minv[((long long)v * nvs + a) * nvs + b] = A[a * w2 + nvs + b];
+	}
+}
+
 template <int D, int NV, int PDE>
 __global__ void __launch_bounds__(256) dvol_group_kernel(const BParams P, int g, const double* __restrict__ u)
 {

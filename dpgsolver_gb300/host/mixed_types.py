@@ -12,8 +12,9 @@ The unit cube is divided into n^3 cells on a periodic grid, and each cell into v
 A cell face is a quad or two triangles the same way from both cells (the diagonal rule is translation invariant),
 so the mesh is conforming; conflicting H/W neighbours are resolved by turning one of them into a C cell. All
 volumes are affine images of the reference elements (dpgsolver_gb300.host.simplex), so metric terms and face
-normals are constant per volume. Cell kinds, wedge axes, the quad/triangle choice between C cells and the p of
-every volume are drawn from seeded generators.
+normals are constant per volume; a problem built with a ``deform`` (SineDeform) maps every volume through it
+instead, and then they vary node by node (curved volumes). Cell kinds, wedge axes, the quad/triangle choice between
+C cells and the p of every volume are drawn from seeded generators.
 
 The face list follows the reference's rule (face.c:86-160): volumes are visited in list order and local faces in
 index order, and the first volume met is side 0. Face nodes are laid out in one canonical vertex order per face:
@@ -306,11 +307,34 @@ def _affine(t, x):
     return A, b
 
 
-class MixedTypeProblem:
-    """Mixed-type mesh + per-volume p + per-(type, p) operators + affine geometry + state (flat layout as
-    MixedTPProblem: per volume the (n_var x n_vs(v)) block, volume-list order)."""
+class SineDeform:
+    """x -> x + a prod_j sin(2 pi x_j) on every coordinate: a smooth map of the unit square / cube onto itself that
+    is periodic and fixes its boundary, so a mesh of it stays conforming, periodic and bounded by the same faces."""
 
-    def __init__(self, mesh: MixedTypeMesh, p_vol, pde=PDE_EULER, num_flux=NUM_FLUX_ROE_PIKE, positivity=False):
+    def __init__(self, d: int, amplitude: float):
+        self.d, self.a = d, float(amplitude)
+
+    def __call__(self, x):
+        s = np.prod(np.sin(2.0 * math.pi * x), axis=-1)
+        return x + self.a * s[..., None]
+
+    def jac(self, x):
+        """dx'/dx at x (..., d) -> (..., d, d)."""
+        sn, cs = np.sin(2.0 * math.pi * x), np.cos(2.0 * math.pi * x)
+        g = np.empty_like(x)
+        for j in range(self.d):
+            g[..., j] = 2.0 * math.pi * cs[..., j] * np.prod(np.delete(sn, j, axis=-1), axis=-1)
+        return np.eye(self.d) + self.a * g[..., None, :]
+
+
+class MixedTypeProblem:
+    """Mixed-type mesh + per-volume p + per-(type, p) operators + geometry + state (flat layout as MixedTPProblem:
+    per volume the (n_var x n_vs(v)) block, volume-list order). Affine geometry, or with ``deform`` every volume's
+    map composed with it: x(r) = deform(A r + b), whose metric terms m = J (dx/dr)^-T and Jacobian J are then taken
+    at every cubature node, and the face normals and J_f at every face node (side 0's map)."""
+
+    def __init__(self, mesh: MixedTypeMesh, p_vol, pde=PDE_EULER, num_flux=NUM_FLUX_ROE_PIKE, positivity=False,
+                 deform=None):
         self.mesh = mesh
         self.d = d = getattr(mesh, "d", 3)
         tp = QUAD if d == 2 else HEX
@@ -340,6 +364,14 @@ class MixedTypeProblem:
         if np.any(self.J <= 0.0):
             raise AssertionError("non-positive Jacobian")
         self.m = self.J[:, None, None] * np.transpose(np.linalg.inv(self.A), (0, 2, 1))
+        self.deform = deform
+        if deform is not None:
+            # per group (n_vols_g, n_vc, d, d) metric terms and (n_vols_g, n_vc) Jacobians at the cubature nodes
+            self.m_vc, self.J_vc = [], []
+            for g in range(len(self.groups)):
+                m, J = self._map_metrics(self.group_vols[g], self._vc_ref(g))
+                self.m_vc.append(m)
+                self.J_vc.append(J)
         # faces at p_f = max(p_L, p_R), integrated as the reference does: q_f GL nodes on lines, q_f^2 on quads,
         # the Witherden-Vincent rule of degree 2 p_f on triangles
         q = p_vol.astype(np.int64) + 1
@@ -359,6 +391,34 @@ class MixedTypeProblem:
         self.bc = None
         self.bc_state = None
         self.bc_data = None
+
+    def _vc_ref(self, g):
+        ops = self.groups[g]
+        if getattr(ops, "dense", False):
+            return ops.x_vc
+        from .element import tp_nodes
+        return tp_nodes(ops.x_vc, self.d)
+
+    def _map(self, vols, xr):
+        """Physical points (len(vols), n, d) of reference points xr (n, d), or (len(vols), n, d) per volume."""
+        if xr.ndim == 2:
+            y = np.einsum("vij,nj->vni", self.A[vols], xr) + self.b[vols][:, None, :]
+        else:
+            y = np.einsum("vij,vnj->vni", self.A[vols], xr) + self.b[vols][:, None, :]
+        return y if self.deform is None else self.deform(y)
+
+    def _map_metrics(self, vols, xr):
+        """(m, J) at reference points xr of the volumes: dx/dr = D deform(A r + b) A, J = det, m = J (dx/dr)^-T
+        (m(n, i, j) = J dr_j / dx_i, the reference's metrics_vc)."""
+        if xr.ndim == 2:
+            y = np.einsum("vij,nj->vni", self.A[vols], xr) + self.b[vols][:, None, :]
+        else:
+            y = np.einsum("vij,vnj->vni", self.A[vols], xr) + self.b[vols][:, None, :]
+        F = self.deform.jac(y) @ self.A[vols][:, None, :, :]
+        J = np.linalg.det(F)
+        if np.any(J <= 0.0):
+            raise AssertionError("non-positive Jacobian")
+        return J[..., None, None] * np.swapaxes(np.linalg.inv(F), -1, -2), J
 
     def set_boundaries(self, code: int, exterior=None):
         """Every boundary face (face_vol[f, 1] < 0) gets the reference's BC code `code`; exterior(xyz (m, d)) ->
@@ -386,7 +446,7 @@ class MixedTypeProblem:
                 xr = g.face_points(lf, int(mesh.face_ord[f, 0]), qf)
             else:
                 xr = _tp_face_points(self.d, lf, qf)
-            out[self.face_off[f]:self.face_off[f + 1]] = xr @ self.A[v].T + self.b[v]
+            out[self.face_off[f]:self.face_off[f + 1]] = self._map(np.array([v]), xr)[0]
         return out
 
     def _face_vertex_counts(self):
@@ -416,11 +476,29 @@ class MixedTypeProblem:
             else:
                 nr = S.reference_normals_2d(t) if d == 2 else S.reference_normals_3d(t)
             nref[sel] = nr[lf0[sel]]
-        nun = np.einsum("fij,fj->fi", self.m[v0], nref)
-        jn = np.linalg.norm(nun, axis=1)
         nfc = np.diff(self.face_off)
-        self.normals_fc = np.repeat(nun / jn[:, None], nfc, axis=0)
-        self.jacobian_det_fc = np.repeat(jn, nfc)
+        if self.deform is None:
+            nun = np.einsum("fij,fj->fi", self.m[v0], nref)
+            jn = np.linalg.norm(nun, axis=1)
+            self.normals_fc = np.repeat(nun / jn[:, None], nfc, axis=0)
+            self.jacobian_det_fc = np.repeat(jn, nfc)
+        else:
+            # per face node: side 0's metric terms there applied to the reference normal of its local face
+            self.normals_fc = np.empty((int(self.face_off[-1]), d))
+            self.jacobian_det_fc = np.empty(int(self.face_off[-1]))
+            o0 = mesh.face_ord[:, 0] if getattr(mesh, "face_ord", None) is not None else np.zeros(mesh.n_faces, int)
+            keys = np.stack([self.vol_group[v0], lf0, o0, self.face_q], axis=1)
+            for key in np.unique(keys, axis=0):
+                g, lf, o, qf = (int(k) for k in key)
+                sel = np.nonzero(np.all(keys == key, axis=1))[0]
+                ops = self.groups[g]
+                xr = ops.face_points(lf, o, qf) if getattr(ops, "dense", False) else _tp_face_points(d, lf, qf)
+                m, _ = self._map_metrics(v0[sel], xr)                       # (n_sel, n_fc, d, d)
+                nun = np.einsum("fnij,fj->fni", m, nref[sel])
+                jn = np.linalg.norm(nun, axis=2)
+                idx = (self.face_off[sel][:, None] + np.arange(len(xr))[None, :]).ravel()
+                self.normals_fc[idx] = (nun / jn[..., None]).reshape(-1, d)
+                self.jacobian_det_fc[idx] = jn.ravel()
         self.w_fc = np.empty(int(self.face_off[-1]))
         for nvert, ft in ((2, LINE), (3, S.TRI), (4, S.QUAD)):
             for qf in np.unique(self.face_q):
@@ -459,12 +537,7 @@ class MixedTypeProblem:
         """Physical coordinates of group g's volume cubature nodes (n_vols_g, n_vc, d)."""
         ops = self.groups[g]
         vols = self.group_vols[g]
-        if getattr(ops, "dense", False):
-            xr = ops.x_vc
-        else:
-            from .element import tp_nodes
-            xr = tp_nodes(ops.x_vc, self.d)
-        return np.einsum("vij,nj->vni", self.A[vols], xr) + self.b[vols][:, None, :]
+        return self._map(vols, self._vc_ref(g))
 
     def nc_fc(self) -> np.ndarray:
         return np.concatenate([np.arange(n, dtype=np.int32) for n in np.diff(self.face_off)])
@@ -480,12 +553,15 @@ class MixedTypeProblem:
             if len(vols) == 0:
                 continue
             nq = self.groups[g].n_vc
-            mt = np.transpose(self.m[vols], (0, 2, 1)).reshape(len(vols), dd)     # [j][i] per volume
-            blk = np.repeat(mt[:, :, None], nq, axis=2).reshape(len(vols), dd * nq)
             idx = (dd * vc_off[vols])[:, None] + np.arange(dd * nq)[None, :]
-            mflat[idx] = blk
             jidx = vc_off[vols][:, None] + np.arange(nq)[None, :]
-            jflat[jidx] = np.repeat(self.J[vols][:, None], nq, axis=1)
+            if self.deform is None:
+                mt = np.transpose(self.m[vols], (0, 2, 1)).reshape(len(vols), dd)     # [j][i] per volume
+                mflat[idx] = np.repeat(mt[:, :, None], nq, axis=2).reshape(len(vols), dd * nq)
+                jflat[jidx] = np.repeat(self.J[vols][:, None], nq, axis=1)
+            else:   # (n, i, j) at n + n_vc (i + d j)
+                mflat[idx] = np.transpose(self.m_vc[g], (0, 3, 2, 1)).reshape(len(vols), dd * nq)
+                jflat[jidx] = self.J_vc[g]
         mvc, jvc = [mflat], [jflat]
         return {
             "groups": self.groups,
@@ -514,12 +590,20 @@ class MixedTypeProblem:
             if getattr(ops, "dense", False):
                 x = self.vc_xyz(g)
                 U = fn(x.reshape(-1, self.d)).reshape(len(vols), ops.n_vc, self.n_var)
-                # orthonormal basis, affine volume: coef = M_ref^-1 cv0^T diag(w) U
-                Pm = np.linalg.inv(ops.mass()) @ (ops.cv0_vs_vc().T * ops.w_vc[None, :])   # (n_vs, n_vc)
-                coef = np.transpose(U, (0, 2, 1)) @ Pm.T                                   # (v, k, a)
+                if self.deform is None:
+                    # affine volume: coef = M_ref^-1 cv0^T diag(w) U
+                    Pm = np.linalg.inv(ops.mass()) @ (ops.cv0_vs_vc().T * ops.w_vc[None, :])   # (n_vs, n_vc)
+                    coef = np.transpose(U, (0, 2, 1)) @ Pm.T                                   # (v, k, a)
+                else:
+                    # curved volume: coef = M^-1 cv0^T diag(w J) U, M = cv0^T diag(w J) cv0
+                    cv0 = ops.cv0_vs_vc()
+                    wJ = ops.w_vc[None, :] * self.J_vc[g]                                     # (v, n)
+                    M = np.einsum("na,vn,nb->vab", cv0, wJ, cv0)
+                    rhs = np.einsum("na,vn,vnk->vak", cv0, wJ, U)
+                    coef = np.transpose(np.linalg.solve(M, rhs), (0, 2, 1))
             else:
                 xs = tp_nodes(ops.x_vs, self.d)
-                x = np.einsum("vij,nj->vni", self.A[vols], xs) + self.b[vols][:, None, :]
+                x = self._map(vols, xs)
                 coef = np.transpose(fn(x.reshape(-1, self.d)).reshape(len(vols), ops.n_vs, self.n_var), (0, 2, 1))
             self.set_group(self.sol, g, coef)
 
@@ -530,15 +614,16 @@ class MixedTypeProblem:
 
 def mixed_types_euler(n: int = 12, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE,
                       mach: float = 0.5, perturb: float = 0.05, c_blocks: float = 0.06, w_columns: float = 0.15,
-                      p_tri: float = 1.0, positivity: bool = True) -> MixedTypeProblem:
+                      p_tri: float = 1.0, positivity: bool = True, curved: float = 0.0) -> MixedTypeProblem:
     """Mixed HEX/TET/WEDGE/PYR mesh of the periodic unit cube (n^3 cells), p uniform in p_set per volume (seeded),
     Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed.mixed_euler). The
     positivity limiter is on by default, as the reference applies it to every Euler stage
-    (test_case_requires_positivity)."""
+    (test_case_requires_positivity). curved > 0 maps the cube by SineDeform(3, curved): every volume curved."""
     mesh = MixedTypeMesh(n, seed=seed, c_blocks=c_blocks, w_columns=w_columns, p_tri=p_tri)
     rng = np.random.default_rng(seed + 17)
     p_vol = rng.choice(np.asarray(p_set, dtype=np.int32), size=mesh.n_volumes)
-    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux, positivity=positivity)
+    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux, positivity=positivity,
+                            deform=SineDeform(3, curved) if curved else None)
     rng2 = np.random.default_rng(seed + 1)
     ph = rng2.uniform(0.0, 2.0 * math.pi, size=(5, 3))
     c0 = math.sqrt(GAMMA)
@@ -565,14 +650,15 @@ def mixed_types_euler(n: int = 12, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: 
 
 def mixed_tri_quad_euler(n: int = 16, seed: int = 0, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE,
                          mach: float = 0.5, perturb: float = 0.3, p_tri: float = 0.5,
-                         positivity: bool = True, walls: bool = False) -> MixedTypeProblem:
+                         positivity: bool = True, walls: bool = False, curved: float = 0.0) -> MixedTypeProblem:
     """Mixed QUAD/TRI mesh of the periodic unit square (n^2 cells, MixedTriQuadMesh), p uniform in p_set per volume
     (seeded), Euler with a smooth seeded sinusoidal state around a Mach `mach` free stream (as mixed_types_euler),
-    positivity limiter on by default."""
+    positivity limiter on by default. curved > 0 maps the square by SineDeform(2, curved)."""
     mesh = MixedTriQuadMesh(n, seed=seed, p_tri=p_tri, periodic=not walls)
     rng = np.random.default_rng(seed + 17)
     p_vol = rng.choice(np.asarray(p_set, dtype=np.int32), size=mesh.n_volumes)
-    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux, positivity=positivity)
+    prob = MixedTypeProblem(mesh, p_vol, num_flux=num_flux, positivity=positivity,
+                            deform=SineDeform(2, curved) if curved else None)
     rng2 = np.random.default_rng(seed + 1)
     ph = rng2.uniform(0.0, 2.0 * math.pi, size=(4, 2))
     c0 = math.sqrt(GAMMA)

@@ -368,8 +368,10 @@ dgpu_status dgpu_batch_create(const dgpu_physics* phys, int n_groups, const dgpu
 
 /* Dense operator set of one non-tensor-product (TET, WEDGE or PYR, p) group: the reference's op_std operators
  * (cv0_vs_vc, cv1_vs_vc, cv0_vs_fc: element_operators.c; applied per volume by operator_T.c:96-156) for any
- * solution basis and cubature the caller uses. Row-major. The volumes must be affine (constant
- * jacobian_det_vc), so that M^-1 = (cv0^T diag(w_vc) cv0)^-1 / J (constructor_mass_T, volume_solver_T.c:115-145).
+ * solution basis and cubature the caller uses. Row-major. M^-1 is constructor_mass_T's (volume_solver_T.c:115-145):
+ * (cv0^T diag(w_vc) cv0)^-1 / J for an affine volume (constant jacobian_det_vc); in a group with a curved volume
+ * (J varying over its nodes) every volume keeps its own (cv0^T diag(w_vc J_vc) cv0)^-1, formed on the device at
+ * creation (n_vs^2 doubles per volume).
  * Face operators are evaluated at the face's canonical nodes (the node order the face's other side and the face
  * geometry use) as seen from local face lf under orientation ord (the reference's ind_ord, face.h:47-97):
  *   cv0_vs_fc[(lf * n_ord + ord) * 5 + p_f]   n_fc x n_vs, NULL where not provided;

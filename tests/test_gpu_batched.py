@@ -270,6 +270,8 @@ TYPE_CASES = {
     "types_roe_4": lambda: _types_case(4, 0),
     "types_lf_4": lambda: _types_case(4, 1, P.NUM_FLUX_LAX_FRIEDRICHS),
     "types_roe_6": lambda: _types_case(6, 2),
+    # every volume curved (the cube mapped by SineDeform): per-node metric terms, per-volume M^-1 of the dense groups
+    "types_roe_curved_4": lambda: MT.mixed_types_euler(4, seed=0, perturb=0.3, curved=0.03),
 }
 
 
@@ -287,10 +289,11 @@ def test_mixed_types_residual_matches_oracle(gpu_lib, name, form):
     assert abs(mx - mx_ref) <= TOL * mx_ref
 
 
+@pytest.mark.parametrize("name", ["types_roe_4", "types_roe_curved_4"])
 @pytest.mark.parametrize("form", FORMS)
-def test_mixed_types_rk3_matches_oracle(gpu_lib, form):
+def test_mixed_types_rk3_matches_oracle(gpu_lib, form, name):
     from dpgsolver_gb300.solver import BatchSimulation
-    prob = TYPE_CASES["types_roe_4"]()
+    prob = TYPE_CASES[name]()
     ref = oracle.Oracle(prob)
     s_ref = prob.sol.copy()
     for _ in range(3):
@@ -349,7 +352,11 @@ def _create_error(prob, **kw):
     return ei.value
 
 
-def test_create_rejects_non_affine_dense_volumes(gpu_lib):
+def test_one_curved_dense_volume_gets_its_own_mass_matrix(gpu_lib):
+    """A single non-affine volume (J changed at one node) in an otherwise affine dense group: its group switches to
+    per-volume M^-1 (formed on the device at creation), and the residual still matches the oracle's, which inverts
+    that volume's M = cv0^T diag(w J) cv0 on its own."""
+    from dpgsolver_gb300.solver import BatchSimulation
     prob = TYPE_CASES["types_roe_4"]()
     flat = prob.flat
 
@@ -362,8 +369,12 @@ def test_create_rejects_non_affine_dense_volumes(gpu_lib):
         fl["jacobian_det_vc"][off + 1] *= 1.01
         return fl
     prob.flat = bent
-    e = _create_error(prob)
-    assert e.status == 2 and "affine" in str(e)
+    r_ref, mx_ref = oracle.Oracle(prob).compute_rhs(prob.sol)
+    with BatchSimulation(prob) as sim:
+        mx = sim.compute_rhs()
+        r = sim.rhs
+    assert rel_err(r, r_ref) <= TOL
+    assert abs(mx - mx_ref) <= TOL * mx_ref
 
 
 def test_create_rejects_bad_orientation(gpu_lib):
@@ -418,6 +429,7 @@ TRI_CASES = {
     "tri_quad_lf_p13_8": lambda: MT.mixed_tri_quad_euler(8, seed=2, p_set=(1, 3),
                                                          num_flux=P.NUM_FLUX_LAX_FRIEDRICHS),
     "tri_only_roe_5": lambda: MT.mixed_tri_quad_euler(5, seed=3, p_tri=1.0),
+    "tri_quad_curved_roe_6": lambda: MT.mixed_tri_quad_euler(6, seed=1, curved=0.03),
 }
 
 

@@ -295,3 +295,37 @@ def test_bezier_maps(p):
         assert np.abs(bs @ sb - np.eye(o.n_vs)).max() < 1e-11
         b1 = sb @ _one_coefficients(o)
         assert np.abs(b1 - 1.0).max() < 1e-12
+
+
+@pytest.mark.parametrize("make", [lambda: MT.mixed_types_euler(4, seed=1, curved=0.03),
+                                  lambda: MT.mixed_tri_quad_euler(4, seed=2, curved=0.03)])
+def test_curved_mixed_geometry_is_conforming(make):
+    """With the SineDeform map, every face's canonical nodes seen from its two sides land on the same physical points
+    (up to periodic images), and side 1's area-weighted normal there is the negative of side 0's, so the faces of the
+    curved mesh close; J varies over the volumes' nodes (the dense groups are curved)."""
+    from dpgsolver_gb300.host.element import TPOperatorSet, gauss_legendre
+    prob = make()
+    mesh, d = prob.mesh, prob.d
+    nw = prob.normals_fc * prob.jacobian_det_fc[:, None]
+    for f in range(mesh.n_faces):
+        pts, nrm = [], []
+        for s in range(2):
+            v = int(mesh.face_vol[f, s])
+            ops = prob.groups[prob.vol_group[v]]
+            lf, o = int(mesh.face_lf[f, s]), int(mesh.face_ord[f, s])
+            if getattr(ops, "dense", False):
+                xr = ops.face_points(lf, o, int(prob.face_q[f]))
+                nref = ops.normals_ref[lf]
+            else:
+                xr = MT._tp_face_points(d, lf, int(prob.face_q[f]))
+                nref = TPOperatorSet(ops.e_type, 1).normals_ref[lf]
+            pts.append(prob._map(np.array([v]), xr)[0])
+            m, _ = prob._map_metrics(np.array([v]), xr)
+            nrm.append(np.einsum("nij,j->ni", m[0], nref))
+        dd = pts[0] - pts[1]
+        dd -= np.round(dd)          # periodic images
+        assert np.abs(dd).max() < 1e-13
+        assert np.abs(nrm[0] + nrm[1]).max() < 1e-12
+        assert np.abs(nrm[0] - nw[prob.face_off[f]:prob.face_off[f + 1]]).max() < 1e-13
+    dense = [g for g, o in enumerate(prob.groups) if getattr(o, "dense", False)]
+    assert dense and all(np.ptp(prob.J_vc[g], axis=1).min() > 0.0 for g in dense)
