@@ -910,6 +910,14 @@ def ns_measurements(torch, stream, args):
     e2e_step()
     n_e2e = 10
     ms_e2e = _timed(torch, stream, lambda: [e2e_step() for _ in range(n_e2e)], 1) / n_e2e
+    # the discrete adjoint: one VJP of R through the host-buffer forward/backward pair
+    v = np.random.default_rng(0).standard_normal(prob.sol.shape)
+    sim.vjp_forward(prob.sol)
+    sim.vjp_backward(v)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        sim.vjp_backward(v)
+    vjp_s = (time.perf_counter() - t0) / 3
     sim.close()
     res = {"workload": "3D Navier-Stokes Taylor-Green vortex, Re 1600, Mach 0.1, HEX 32^3 p3, Roe-Pike + BR2",
            "n_state": prob.n_state, "steps": n, "dt": prob.dt,
@@ -919,7 +927,9 @@ def ns_measurements(torch, stream, args):
                    "h2d_bytes_per_step": int(prob.n_state * 8), "d2h_bytes_per_step": int(prob.n_state * 8),
                    "note": "dgpu_ssp_rk3_step_host on pinned buffers (upload, graph-replayed step, download)"},
            "kinetic_energy": {"initial": kinetic_energy(prob, prob.sol), "final": kinetic_energy(prob, final)},
-           "launches_per_stage": 4}
+           "launches_per_stage": 4,
+           "vjp_backward_s": vjp_s,
+           "vjp_note": "dgpu_vjp_backward: host cotangent in, host gradient out (84 MB each way included)"}
     if not args.no_cpu_baseline:
         sample = ns_taylor_green(6, 3, Re=1600.0, mach=0.1)
         o = oracle.Oracle(sample)

@@ -19,6 +19,7 @@
 #include "dgpu_geometry.cuh"
 #include "dgpu_jacobian.cuh"
 #include "dgpu_ns.cuh"
+#include "dgpu_ns_adjoint.cuh"
 #include "dgpu_jvp.cuh"
 #include "dgpu_host_ops.h"
 
@@ -70,6 +71,7 @@ struct dgpu_ctx {
 	NsPhys ns_phys = {0.0, 1.0, 1.0, 101, 0.0};
 	double *ns_gtr = nullptr, *ns_lam = nullptr, *ns_X = nullptr, *ns_gv = nullptr;
 	double *ns_gtr_d = nullptr, *ns_X_d = nullptr, *ns_gv_d = nullptr;   // their tangents (linearisations)
+	double *ns_gbar = nullptr, *ns_xbar = nullptr, *ns_gtbar = nullptr;  // cotangents (VJP, dgpu_ns_adjoint.cuh)
 	int stage_launches = 3;               // kernels per residual evaluation / RK stage
 	int n_bnd = 0;                        // boundary faces (face_vol[2f+1] < 0)
 	int *bnd = nullptr, *bc_code = nullptr;
@@ -546,6 +548,13 @@ cudaError_t launch_ns_t(dgpu_ctx* c)
 }
 
 template <int D, int Q, int NV>
+size_t ns_adj_smem_bytes()
+{
+	using S = TPShape<D, Q>;
+	return (sizeof(TPOps) + 7) / 8 * 8 + (size_t)S::E * NsAdjSmem<D, Q, NV>::PER_E * sizeof(double);
+}
+
+template <int D, int Q, int NV>
 size_t ns_jvp_smem_bytes()
 {
 	using S = TPShape<D, Q>;
@@ -597,6 +606,43 @@ cudaError_t launch_ns_jvp_t(dgpu_ctx* c)
 	return cudaGetLastError();
 }
 
+// VJP of the Navier-Stokes residual at state u (GLL): the forward gradient and face kernels at u (traces, gradient
+// traces, volume gradients, X), then the three adjoint kernels of dgpu_ns_adjoint.cuh.
+template <int D, int Q, int FLUX>
+cudaError_t launch_ns_adjoint_t(dgpu_ctx* c, const double* u, const double* rbar, double* ubar)
+{
+	using S = TPShape<D, Q>;
+	constexpr int NV = D + 2;
+	const int blocks = (c->n_vol + S::E - 1) / S::E;
+	const TPParams P = c->params();
+	const long long nfn = (long long)c->n_face * S::NF;
+	tp_ns_grad_kernel<D, Q, NV, true><<<blocks, S::THREADS, ns_smem_bytes<D, Q, NV>(), c->stream>>>(c->ops, P, u);
+	tp_ns_face_kernel<D, Q, FLUX><<<(unsigned)((nfn + 127) / 128), 128, 0, c->stream>>>(P);
+	AdjArgs A;
+	A.u = u;
+	A.rbar = rbar;
+	A.ubar = ubar;
+	A.atraces = c->atraces;
+	A.wbar = c->wbar;
+	NsAdjArgs B;
+	B.gbar = c->ns_gbar;
+	B.xbar = c->ns_xbar;
+	B.gtbar = c->ns_gtbar;
+	record_start(c, "tp_ns_adj_volume_kernel");
+	tp_ns_adj_volume_kernel<D, Q, NV><<<blocks, S::THREADS, ns_adj_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, P, A, B);
+	record_stop(c);
+	record_start(c, "tp_ns_adj_face_kernel");
+	tp_ns_adj_face_kernel<D, Q, FLUX><<<(unsigned)((nfn + 127) / 128), 128, 0, c->stream>>>(P, A, B);
+	record_stop(c);
+	record_start(c, "tp_ns_adj_lift_kernel");
+	tp_ns_adj_lift_kernel<D, Q, NV><<<blocks, S::THREADS, ns_adj_smem_bytes<D, Q, NV>(), c->stream>>>(
+		c->ops, P, A, B);
+	record_stop(c);
+	c->launches += 5;
+	return cudaGetLastError();
+}
+
 cudaError_t launch_nothing(dgpu_ctx*) { return cudaSuccess; }
 
 template <int D, int Q, int FLUX>
@@ -611,12 +657,15 @@ cudaError_t bind_ns(dgpu_ctx* c)
 	c->launch_volume = launch_ns_t<D, Q, FLUX, true>;
 	c->launch_volume_gl = launch_ns_t<D, Q, FLUX, false>;
 	c->launch_face = launch_nothing;
-	c->launch_adjoint = nullptr;
-	c->launch_objective = nullptr;
+	c->launch_adjoint = launch_ns_adjoint_t<D, Q, FLUX>;
+	c->launch_objective = launch_objective_t<D, Q, NV>;
 	c->launch_jvp = launch_ns_jvp_t<D, Q, FLUX, true>;
 	c->launch_jvp_tangent = launch_ns_jvp_t<D, Q, FLUX, false>;
 	const cudaFuncAttribute smem = cudaFuncAttributeMaxDynamicSharedMemorySize;
 	if ((e = cudaFuncSetAttribute(tp_ns_jvp_volume_kernel<D, Q, NV>, smem, (int)ns_jvp_smem_bytes<D, Q, NV>())))
+		return e;
+	if ((e = cudaFuncSetAttribute(tp_ns_adj_volume_kernel<D, Q, NV>, smem, (int)ns_adj_smem_bytes<D, Q, NV>())) ||
+	    (e = cudaFuncSetAttribute(tp_ns_adj_lift_kernel<D, Q, NV>, smem, (int)ns_adj_smem_bytes<D, Q, NV>())))
 		return e;
 	const int bytes = (int)ns_smem_bytes<D, Q, NV>();
 	if ((e = cudaFuncSetAttribute(tp_ns_grad_kernel<D, Q, NV, true>, smem, bytes)) ||
@@ -678,7 +727,7 @@ void free_all(dgpu_ctx* c)
 	}
 	c->timers.clear();
 	void* ptrs[] = {c->source, c->halo_send, c->halo_recv, c->halo_sbuf, c->halo_rbuf, c->jv_du, c->jv_vol, c->jv_traces, c->jv_nnf, c->jv_out, c->obj_faces, c->obj_contrib, c->u_saved, c->vbar, c->ubar, c->atraces, c->wbar, c->u, c->u0, c->ug, c->rhs, c->gmet, c->inv_wJ, c->fgeo, c->vol_face, c->nc, c->nc_inv,
-	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X, c->ns_gv, c->ns_gtr_d, c->ns_X_d, c->ns_gv_d,
+	                c->jac_slot, c->jac_members, c->ns_gtr, c->ns_lam, c->ns_X, c->ns_gv, c->ns_gtr_d, c->ns_X_d, c->ns_gv_d, c->ns_gbar, c->ns_xbar, c->ns_gtbar,
 	                c->bnd, c->bc_code, c->bc_ext, c->traces, c->nnf, c->vol_gl, c->max_bits, c->err_flag, c->n_corr};
 	for (void* p : ptrs)
 		if (p)
@@ -2022,6 +2071,11 @@ dgpu_status ensure_adjoint_buffers(dgpu_ctx* c)
 	DGPU_CUDA(c, cudaMalloc((void**)&c->ubar, ns * sizeof(double)));
 	DGPU_CUDA(c, cudaMalloc((void**)&c->atraces, nt * sizeof(double)));
 	DGPU_CUDA(c, cudaMalloc((void**)&c->wbar, nt * sizeof(double)));
+	if (c->ns) {
+		DGPU_CUDA(c, cudaMalloc((void**)&c->ns_gbar, ns * c->d * sizeof(double)));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->ns_xbar, nt * c->d * sizeof(double)));
+		DGPU_CUDA(c, cudaMalloc((void**)&c->ns_gtbar, nt * c->d * sizeof(double)));
+	}
 	return DGPU_OK;
 }
 
@@ -2232,8 +2286,6 @@ extern "C" dgpu_status dgpu_vjp_forward(dgpu_ctx* c, const double* sol, double* 
 	DGPU_WHOLE_MESH(c);
 	if (!c || !sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	if (c->ns)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_vjp_forward is not provided for Navier-Stokes");
 	dgpu_status st = ensure_adjoint_buffers(c);
 	if (st != DGPU_OK)
 		return st;
@@ -2258,8 +2310,6 @@ extern "C" dgpu_status dgpu_vjp_backward(dgpu_ctx* c, const double* cotangent, d
 	DGPU_WHOLE_MESH(c);
 	if (!c || !cotangent || !grad_sol)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	if (c->ns)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_vjp_backward is not provided for Navier-Stokes");
 	if (!c->u_saved)
 		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "dgpu_vjp_backward needs a preceding dgpu_vjp_forward");
 	const size_t bytes = state_size(c) * sizeof(double);
@@ -2278,10 +2328,8 @@ extern "C" dgpu_status dgpu_set_objective_faces(dgpu_ctx* c, int n_faces, const 
 	DGPU_WHOLE_MESH(c);
 	if (!c || n_faces < 1 || !faces)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	if (c->ns)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_set_objective_faces is not provided for Navier-Stokes");
-	if (c->pde != DGPU_PDE_EULER)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "the pressure objective needs the Euler equations");
+	if (c->pde != DGPU_PDE_EULER && c->pde != DGPU_PDE_NAVIER_STOKES)
+		return fail(c, DGPU_ERR_UNSUPPORTED, "the pressure objective needs the Euler or Navier-Stokes equations");
 	for (int i = 0; i < n_faces; ++i)
 		if (faces[i] < 0 || faces[i] >= c->n_face)
 			return fail(c, DGPU_ERR_INVALID_ARGUMENT, "objective face index out of range");
@@ -2369,8 +2417,6 @@ extern "C" dgpu_status dgpu_objective(dgpu_ctx* c, const double* sol, double* J,
 	DGPU_WHOLE_MESH(c);
 	if (!c || !sol || !J)
 		return DGPU_ERR_INVALID_ARGUMENT;
-	if (c->ns)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_objective is not provided for Navier-Stokes");
 	if (!c->obj_faces)
 		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "no objective faces: call dgpu_set_objective_faces");
 	const size_t bytes = state_size(c) * sizeof(double);
@@ -2389,8 +2435,6 @@ extern "C" dgpu_status dgpu_adjoint_ssp_rk3(dgpu_ctx* c, double dt, int n_steps,
 	DGPU_WHOLE_MESH(c);
 	if (!c || n_steps < 1 || !sol0 || !J || !dJ_dsol0 || !(dt == dt))
 		return DGPU_ERR_INVALID_ARGUMENT;
-	if (c->ns)
-		return fail(c, DGPU_ERR_UNSUPPORTED, "dgpu_adjoint_ssp_rk3 is not provided for Navier-Stokes");
 	if (!c->obj_faces)
 		return fail(c, DGPU_ERR_INVALID_ARGUMENT, "no objective faces: call dgpu_set_objective_faces");
 	const size_t ns = state_size(c), sb = ns * sizeof(double);

@@ -172,6 +172,33 @@ tp_ns_grad_kernel(const TPOps ops, const TPParams P, const double* __restrict__ 
 	}
 }
 
+// The contravariant Euler minus viscous flux at a volume node: fr_j = sum_i w J dr_j/dx_i (f_i(W) - f_v,i(W, G))
+// (compute_volume_rlhs_T.c:71-110 with the Navier-Stokes flux of flux_navier_stokes_T.c), gm the weighted metric terms.
+template <int D, typename T>
+__device__ __forceinline__ void ns_flux_ref(const T* W, const T (*G)[D + 2], const double* gm, const NsPhys& ns,
+                                            T (*fr)[D + 2])
+{
+	constexpr int NV = D + 2;
+	euler_flux_ref<D>(W, gm, fr);
+	T Fv[D][NV];
+#pragma unroll
+	for (int i = 0; i < D; ++i)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			Fv[i][k] = T(0.0);
+	ns_viscous_sub<D, T>(W, G, ns, Fv);
+#pragma unroll
+	for (int j = 0; j < D; ++j)
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			T a = T(0.0);
+#pragma unroll
+			for (int i = 0; i < D; ++i)
+				a = a + gm[j * D + i] * Fv[i][k];
+			fr[j][k] = fr[j][k] + a;
+		}
+}
+
 // Scalar helpers of the face and volume bodies below: T = double (the residual) or Dual<1> (the residual and its
 // directional derivative, the tangent quantities read from and written to a second parameter set Pd).
 __device__ __forceinline__ void ns_set(double& x, double v, double) { x = v; }
@@ -185,32 +212,19 @@ __device__ __forceinline__ double ns_val(const Dual<1>& x) { return x.v; }
 __device__ __forceinline__ double ns_der(const double&) { return 0.0; }
 __device__ __forceinline__ double ns_der(const Dual<1>& x) { return x.d[0]; }
 
-// One face node: the boundary value or right trace, X, the partial face gradients, Roe-Pike / Lax-Friedrichs plus
-// the central viscous flux, times w_f J_f. With T = Dual<1> the tangent traces, gradient traces and outputs are Pd's.
-template <int D, int Q, int FLUX, typename T>
-__device__ __forceinline__ void ns_face_node(const TPParams& P, const TPParams& Pd, int f, int t)
+// The face-node function on scalar type T (double, or dual numbers for the linearisations): from the left trace WL,
+// the right trace WR (a boundary face forms it from WL instead, as its BC), the gradient traces GtL, GtR (GtR unused
+// on a boundary face), it gives X = w_f J_f n (W_R - W_L) / 2 and the face flux
+// o = w_f J_f (F*(W_L, W_R) + n . (F_v(W_L, G_L) + F_v(W_R, G_R)) / 2) with the partial face gradients
+// G_s = Gt_s + eta lambda_s X. b: the face's index in the boundary list, or -1.
+template <int D, int FLUX, typename T>
+__device__ __forceinline__ void ns_face_core(const TPParams& P, int b, int t, int NF, const double* n, double sc,
+                                             double lamL, double lamR, const T* WL, T* WR, const T (*GtL)[D + 2],
+                                             const T (*GtR)[D + 2], T (*X)[D + 2], T* o)
 {
-	constexpr int NF = TPShape<D, Q>::NF, NV = D + 2;
-	constexpr bool TAN = !std::is_same<T, double>::value;
-	const int b = P.bnd ? P.bnd[f] : -1;   // boundary face: its index in the boundary list
-	const int tR = (b < 0 && P.nc) ? P.nc[(size_t)f * NF + t] : t;
-	const double* fg = P.fgeo + (size_t)f * (D + 1) * NF;
-	double n[D];
-	T WL[NV], WR[NV];
-#pragma unroll
-	for (int k = 0; k < D; ++k)
-		n[k] = fg[k * NF + t];
-	const double sc = fg[D * NF + t];
-	const size_t oL = (size_t)(2 * f) * NV * NF, oR = (size_t)(2 * f + 1) * NV * NF;
-#pragma unroll
-	for (int k = 0; k < NV; ++k)
-		ns_set(WL[k], P.traces[oL + k * NF + t], TAN ? Pd.traces[oL + k * NF + t] : 0.0);
+	constexpr int NV = D + 2;
 	int code = 0;
-	if (b < 0) {
-#pragma unroll
-		for (int k = 0; k < NV; ++k)
-			ns_set(WR[k], P.traces[oR + k * NF + tR], TAN ? Pd.traces[oR + k * NF + tR] : 0.0);
-	} else {
+	if (b >= 0) {
 		// the reference's Navier-Stokes boundary values (set_function_pointers_num_flux_bc_navier_stokes,
 		// face_solver_T.c:277-300): Riemann and supersonic in/outflow as for Euler; the static no-slip walls keep
 		// rho and E and mirror the momentum (boundary_navier_stokes_T.c:258-304); the rotating wall takes
@@ -231,31 +245,15 @@ __device__ __forceinline__ void ns_face_node(const TPParams& P, const TPParams& 
 			boundary_value<D, NV, kEuler, T>(P, b, t, NF, WL, n, WR);
 		}
 	}
-	const double lamL = P.ns_lam[(size_t)(2 * f) * NF + t];
-	const double lamR = b < 0 ? P.ns_lam[(size_t)(2 * f + 1) * NF + tR] : lamL;
-	const size_t gL = (size_t)(2 * f) * D * NV * NF, gR = (size_t)(2 * f + 1) * D * NV * NF;
 	T GL[D][NV], GR[D][NV];
 #pragma unroll
 	for (int dir = 0; dir < D; ++dir)
 #pragma unroll
 		for (int k = 0; k < NV; ++k) {
-			const T X = (0.5 * sc * n[dir]) * (WR[k] - WL[k]);
-			const size_t ox = ((size_t)f * D * NV + dir * NV + k) * NF + t;
-			P.ns_X[ox] = ns_val(X);
-			if (TAN)
-				Pd.ns_X[ox] = ns_der(X);
-			const size_t cl = gL + (dir * NV + k) * NF + t;
-			T g;
-			ns_set(g, P.ns_gtr[cl], TAN ? Pd.ns_gtr[cl] : 0.0);
-			GL[dir][k] = g + (P.ns_eta * lamL) * X;
+			X[dir][k] = (0.5 * sc * n[dir]) * (WR[k] - WL[k]);
+			GL[dir][k] = GtL[dir][k] + (P.ns_eta * lamL) * X[dir][k];
 			// on a boundary face the exterior gradient is the interior one (grad_from_internal; the walls copy it)
-			if (b < 0) {
-				const size_t cr = gR + (dir * NV + k) * NF + tR;
-				ns_set(g, P.ns_gtr[cr], TAN ? Pd.ns_gtr[cr] : 0.0);
-				GR[dir][k] = g + (P.ns_eta * lamR) * X;
-			} else {
-				GR[dir][k] = GL[dir][k];
-			}
+			GR[dir][k] = b < 0 ? GtR[dir][k] + (P.ns_eta * lamR) * X[dir][k] : GL[dir][k];
 		}
 	T nF[NV];
 	if constexpr (FLUX == kRoePike)
@@ -270,7 +268,6 @@ __device__ __forceinline__ void ns_face_node(const TPParams& P, const TPParams& 
 			FL[dir][k] = FR[dir][k] = T(0.0);
 	ns_viscous_sub<D, T>(WL, GL, P.ns, FL);
 	ns_viscous_sub<D, T>(WR, GR, P.ns, FR);
-	const size_t on = (size_t)f * NV * NF + t;
 #pragma unroll
 	for (int k = 0; k < NV; ++k) {
 		T s = T(0.0);
@@ -281,10 +278,66 @@ __device__ __forceinline__ void ns_face_node(const TPParams& P, const TPParams& 
 		// diabatic (set_provided_Numerical_Flux_members, numerical_flux_central_T.c:222-231)
 		const bool wall_E = (k == D + 1 && (code == kBcNoSlipAdiabatic || code == kBcNoSlipDiabatic));
 		const double nf_E = code == kBcNoSlipDiabatic ? P.ns.wall_nf_E * sc : 0.0;
-		const T o = (nF[k] + 0.5 * s) * sc;
-		P.nnf[on + k * NF] = wall_E ? nf_E : ns_val(o);
+		o[k] = wall_E ? T(nf_E) : (nF[k] + 0.5 * s) * sc;
+	}
+}
+
+// One face node of the residual (T = double) or of the residual and its directional derivative (T = Dual<1>, the
+// tangent traces, gradient traces and outputs in Pd): loads the traces, runs ns_face_core, stores X and the flux.
+template <int D, int Q, int FLUX, typename T>
+__device__ __forceinline__ void ns_face_node(const TPParams& P, const TPParams& Pd, int f, int t)
+{
+	constexpr int NF = TPShape<D, Q>::NF, NV = D + 2;
+	constexpr bool TAN = !std::is_same<T, double>::value;
+	const int b = P.bnd ? P.bnd[f] : -1;   // boundary face: its index in the boundary list
+	const int tR = (b < 0 && P.nc) ? P.nc[(size_t)f * NF + t] : t;
+	const double* fg = P.fgeo + (size_t)f * (D + 1) * NF;
+	double n[D];
+	T WL[NV], WR[NV];
+#pragma unroll
+	for (int k = 0; k < D; ++k)
+		n[k] = fg[k * NF + t];
+	const double sc = fg[D * NF + t];
+	const size_t oL = (size_t)(2 * f) * NV * NF, oR = (size_t)(2 * f + 1) * NV * NF;
+#pragma unroll
+	for (int k = 0; k < NV; ++k)
+		ns_set(WL[k], P.traces[oL + k * NF + t], TAN ? Pd.traces[oL + k * NF + t] : 0.0);
+	if (b < 0)
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			ns_set(WR[k], P.traces[oR + k * NF + tR], TAN ? Pd.traces[oR + k * NF + tR] : 0.0);
+	const double lamL = P.ns_lam[(size_t)(2 * f) * NF + t];
+	const double lamR = b < 0 ? P.ns_lam[(size_t)(2 * f + 1) * NF + tR] : lamL;
+	const size_t gL = (size_t)(2 * f) * D * NV * NF, gR = (size_t)(2 * f + 1) * D * NV * NF;
+	T GtL[D][NV], GtR[D][NV];
+#pragma unroll
+	for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			const size_t cl = gL + (dir * NV + k) * NF + t;
+			ns_set(GtL[dir][k], P.ns_gtr[cl], TAN ? Pd.ns_gtr[cl] : 0.0);
+			if (b < 0) {
+				const size_t cr = gR + (dir * NV + k) * NF + tR;
+				ns_set(GtR[dir][k], P.ns_gtr[cr], TAN ? Pd.ns_gtr[cr] : 0.0);
+			}
+		}
+	T X[D][NV], o[NV];
+	ns_face_core<D, FLUX, T>(P, b, t, NF, n, sc, lamL, lamR, WL, WR, GtL, GtR, X, o);
+#pragma unroll
+	for (int dir = 0; dir < D; ++dir)
+#pragma unroll
+		for (int k = 0; k < NV; ++k) {
+			const size_t ox = ((size_t)f * D * NV + dir * NV + k) * NF + t;
+			P.ns_X[ox] = ns_val(X[dir][k]);
+			if (TAN)
+				Pd.ns_X[ox] = ns_der(X[dir][k]);
+		}
+	const size_t on = (size_t)f * NV * NF + t;
+#pragma unroll
+	for (int k = 0; k < NV; ++k) {
+		P.nnf[on + k * NF] = ns_val(o[k]);
 		if (TAN)
-			Pd.nnf[on + k * NF] = wall_E ? 0.0 : ns_der(o);
+			Pd.nnf[on + k * NF] = ns_der(o[k]);
 	}
 }
 
@@ -366,24 +419,7 @@ tp_ns_volume_kernel(const TPOps ops, const TPParams P, const double* __restrict_
 #pragma unroll
 		for (int c = 0; c < D * D; ++c)
 			gm[c] = P.gmet[((size_t)v * D * D + c) * N + node];
-		euler_flux_ref<D>(W, gm, fr);
-		double Fv[D][NV];
-#pragma unroll
-		for (int i = 0; i < D; ++i)
-#pragma unroll
-			for (int k = 0; k < NV; ++k)
-				Fv[i][k] = 0.0;
-		ns_viscous_sub<D, double>(W, g, P.ns, Fv);
-#pragma unroll
-		for (int j = 0; j < D; ++j)
-#pragma unroll
-			for (int k = 0; k < NV; ++k) {
-				double a = 0.0;
-#pragma unroll
-				for (int i = 0; i < D; ++i)
-					a += gm[j * D + i] * Fv[i][k];
-				fr[j][k] += a;
-			}
+		ns_flux_ref<D, double>(W, g, gm, P.ns, fr);
 	}
 	__syncthreads();   // everyone is done with sf's derivatives
 	if (active)

@@ -226,7 +226,8 @@ dgpu_status dgpu_compute_rhs_noalloc(const dgpu_physics* phys, const dgpu_tp_ope
  * src/testing/support/simulation/solvers/dg/test_support_solve_dg.c:83-110) and assembles its Jacobian for the
  * implicit solver (compute_rlhs_dg, src/simulation/solvers/dg/solve_dg.c:138-145); grad is that Jacobian's
  * transpose applied to the cotangent. Kinks of the fluxes take the derivative of the branch the value takes.
- * Advection and Euler: a Navier-Stokes context returns DGPU_ERR_UNSUPPORTED. */
+ * Every PDE: for Navier-Stokes the BR2 gradients, their liftings, the viscous fluxes and the boundary values (walls
+ * included) are differentiated with the rest. */
 dgpu_status dgpu_vjp_forward(dgpu_ctx* ctx, const double* sol, double* rhs, double* max_rhs);
 dgpu_status dgpu_vjp_backward(dgpu_ctx* ctx, const double* cotangent, double* grad_sol);
 
@@ -259,7 +260,7 @@ dgpu_status dgpu_jacobian_bsr(dgpu_ctx* ctx, const double* sol, int raw, int* ro
                               double* values);
 
 /* Output functional for the adjoint: J(sol) = sum over the listed faces of the integral of pressure on side 0
- * (sum over face cubature nodes of w_fc J_fc p(W_L)), e.g. the faces of the plane z = 0. Euler only. The
+ * (sum over face cubature nodes of w_fc J_fc p(W_L)), e.g. the faces of the plane z = 0. Euler and Navier-Stokes. The
  * reference computes such integrals as error functionals (src/simulation/test_case/compute_error/) but has no
  * adjoint; no counterpart. */
 dgpu_status dgpu_set_objective_faces(dgpu_ctx* ctx, int n_faces, const int* faces);
