@@ -233,6 +233,45 @@ def write_annulus_msh(path, n_r: int, n_t: int, r_i: float = 0.5, r_o: float = 1
         fh.write("$EndElements\n")
 
 
+def write_square_annulus_msh(path, n_t: int, n_r: int, r_i: float = 0.5, r_o: float = 1.0, inner: int = 20113,
+                             outer: int = 20111):
+    """Write the square annulus r_i <= max(|x|, |y|) <= r_o as a QUAD gmsh 2.2 file, the parametric domain of the
+    reference's n-cylinder_hollow/2d.geo (mesh_domain PARAMETRIC: the squares of half-sides r_i and r_o, four
+    transfinite blocks split along the diagonals) that its cylinder map takes to the circular annulus. n_t volumes
+    along each side of a block, n_r across; the boundary lines of the inner and outer squares carry the codes inner
+    and outer (as the .geo's Physical Lines: 2 BC_STEP_SC + BC_NOSLIP_ALL_ROTATING inside, + BC_NOSLIP_ADIABATIC or
+    BC_NOSLIP_DIABATIC outside), then the volumes, all with the same local frame (r radial, s counter-clockwise)."""
+    n_a = 4 * n_t
+
+    def node(i, j):
+        return i + (n_r + 1) * (j % n_a)
+
+    pts = []
+    for j in range(n_a):
+        side, a = divmod(j, n_t)
+        a = a / n_t
+        for i in range(n_r + 1):
+            r = r_i + (r_o - r_i) * i / n_r
+            pts.append(((-r + 2.0 * r * a, -r), (r, -r + 2.0 * r * a), (r - 2.0 * r * a, r),
+                        (-r, r - 2.0 * r * a))[side])
+    elems = []
+    for j in range(n_a):
+        elems.append((LINE, (inner, 1001), [node(0, j), node(0, j + 1)]))
+    for j in range(n_a):
+        elems.append((LINE, (outer, 1005), [node(n_r, j), node(n_r, j + 1)]))
+    for j in range(n_a):
+        for i in range(n_r):   # gmsh's counter-clockwise order
+            elems.append((QUAD, (9401, 4001), [node(i, j), node(i + 1, j), node(i + 1, j + 1), node(i, j + 1)]))
+    with open(path, "w") as fh:
+        fh.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % len(pts))
+        for k, (x, y) in enumerate(pts):
+            fh.write("%d %.17g %.17g 0\n" % (k + 1, x, y))
+        fh.write("$EndNodes\n$Elements\n%d\n" % len(elems))
+        for k, (t, tags, verts) in enumerate(elems):
+            fh.write("%d %d 2 %d %d %s\n" % (k + 1, t, tags[0], tags[1], " ".join(str(v + 1) for v in verts)))
+        fh.write("$EndElements\n")
+
+
 # ---- a TP problem on a mesh read from a file ------------------------------------------------------------------------
 def tp_face_permutation(match, q: int, d: int) -> np.ndarray:
     """The right-trace gather permutation nc (sR[i] = sR_own[nc[i]]) of a TP face's q^(d-1) GL nodes from the
@@ -302,13 +341,15 @@ def curved_faces(mesh) -> np.ndarray:
 
 
 def gmsh_tp_problem(path, d: int, p: int, pde: int, num_flux: int, state, b_adv=(1.0, 0.5, 0.0), exterior=None,
-                    bc_data=None, cfl: float = 0.1, name: str | None = None, ns=None, blend=None):
+                    bc_data=None, cfl: float = 0.1, name: str | None = None, ns=None, blend=None, parametric=None):
     """A DGProblem on the QUAD/HEX mesh in a gmsh file: geometry coefficients = the volumes' vertices (p_g = 1),
     state(xyz (m, d)) -> (m, n_var) the conserved initial state at the solution nodes, exterior(xyz) likewise the
     exterior state of the boundary faces (their BC codes come from the file), bc_data the BC_Data scalars, ns the
     Navier-Stokes constants (pde 4). blend(xyz_ve (n_volumes, 2, 4), face_curved, p) -> (n_volumes, (p+1)^2, 2):
     the blended domain's geometry coefficients at order p for the volumes with curved faces (2D; e.g.
-    solver.blend_geometry on the device)."""
+    solver.blend_geometry on the device). parametric(xy (m, 2)) -> (m, 2): the domain map of a parametric QUAD mesh,
+    applied as the reference applies it (geometry.parametric_quad_nodes: the map on every face, blended into the
+    volume) at p_g = p."""
     from .element import TPOperatorSet
     from .geometry import TPGeometry
     from .problem import DGProblem, PDE_ADVECTION, stable_dt
@@ -318,6 +359,17 @@ def gmsh_tp_problem(path, d: int, p: int, pde: int, num_flux: int, state, b_adv=
     if blend is not None:
         coef = blend(np.ascontiguousarray(np.transpose(mesh.vertices, (0, 2, 1))), curved_faces(mesh), p)
         geom = TPGeometry(mesh, ops, curved=True, coef=coef)
+    elif parametric is not None:
+        from .element import gauss_lobatto, tp_nodes
+        from .geometry import parametric_quad_nodes
+        if d != 2:
+            raise ValueError("parametric meshes are built for QUAD volumes")
+        x_g, _ = gauss_lobatto(p + 1)
+        xi = tp_nodes(x_g, 2)
+        hat = [0.25 * (1.0 + sa * xi[:, 0]) * (1.0 + sb * xi[:, 1]) for sb in (-1.0, 1.0) for sa in (-1.0, 1.0)]
+        straight = np.stack([sum(hat[k][None, :] * mesh.vertices[:, k, c][:, None] for k in range(4))
+                             for c in range(2)], axis=2)
+        geom = TPGeometry(mesh, ops, curved=True, coef=parametric_quad_nodes(straight, x_g, parametric))
     else:
         geom = TPGeometry(mesh, ops, curved=False, coef=mesh.vertices)
     n_var = 1 if pde == PDE_ADVECTION else d + 2

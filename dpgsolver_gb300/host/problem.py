@@ -590,15 +590,68 @@ def ns_taylor_couette(n=8, p: int = 3, mu: float = 1e-3, omega: float = 1.0, dia
         U = U * (1.0 + perturb * np.sin(3.0 * TH) * np.sin(math.pi * (R - r_i) / (r_o - r_i)))[None]
     prob.sol = _pack_state(U)
     prob.dt = stable_dt(prob, h=min((r_o - r_i) / n_r, 2.0 * math.pi * r_i / n_t))
-    rho_b = 1.0
+    outer = BC_NOSLIP_DIABATIC if diabatic else BC_NOSLIP_ADIABATIC
+    prob.meta.update(n=(n_r, n_t), p=p, omega=omega, r_i=r_i, r_o=r_o)
+    return _set_boundaries(prob, {(0, 0): BC_NOSLIP_ALL_ROTATING, (0, 1): outer},
+                           _taylor_couette_wall(r_i, omega, p_b))
+
+
+def _taylor_couette_wall(r_i: float, omega: float, p_b: float, rho_b: float = 1.0):
+    """The rotating wall's state (rho_b, rho_b u_wall, E_b) at face points xyz (m, 2): compute_uvw_ex_rotating
+    (boundary_navier_stokes_T.c:507-523), the wall's velocity omega r e_theta; E_b = p_b / (gamma - 1) +
+    rho_b (omega r_i)^2 / 2."""
     E_b = p_b / GM1 + 0.5 * rho_b * (omega * r_i) ** 2
 
     def wall_state(xyz):
-        # compute_uvw_ex_rotating (boundary_navier_stokes_T.c:507-523): the wall's velocity omega r e_theta
         r, th = np.sqrt(xyz[:, 0] ** 2 + xyz[:, 1] ** 2), np.arctan2(xyz[:, 1], xyz[:, 0])
         vt = omega * r
         return np.stack([np.full(len(r), rho_b), -rho_b * np.sin(th) * vt, rho_b * np.cos(th) * vt,
                          np.full(len(r), E_b)], axis=1)
-    outer = BC_NOSLIP_DIABATIC if diabatic else BC_NOSLIP_ADIABATIC
-    prob.meta.update(n=(n_r, n_t), p=p, omega=omega, r_i=r_i, r_o=r_o)
-    return _set_boundaries(prob, {(0, 0): BC_NOSLIP_ALL_ROTATING, (0, 1): outer}, wall_state)
+    return wall_state
+
+
+def cylinder_parametric_map(xy):
+    """The reference's map of its square annulus onto the circular annulus (constructor_xyz_cylinder_parametric_T,
+    geometry_parametric_T.c:128-173): the radius is max(|x|, |y|) and the polar angle runs linearly along each side
+    of the square, with the same branches on the angle of (x, y)."""
+    x, y = xy[:, 0], xy[:, 1]
+    r = np.maximum(np.abs(x), np.abs(y))
+    t = np.arctan2(y, x)
+    q = math.pi / 4.0
+    out = np.full_like(t, np.nan)
+    c0 = (t >= -q) & (t < q)
+    c1 = (t >= q) & (t < 3.0 * q)
+    c2 = ((t >= 3.0 * q) & (t <= 4.0 * q)) | ((t >= -4.0 * q) & (t < -3.0 * q))
+    c3 = (t >= -3.0 * q) & (t < -q)
+    out[c0] = y[c0] / r[c0] * q
+    out[c1] = 0.5 * math.pi - x[c1] / r[c1] * q
+    out[c2] = math.pi - y[c2] / r[c2] * q
+    out[c3] = 1.5 * math.pi + x[c3] / r[c3] * q
+    if np.any(np.isnan(out)):
+        raise ValueError("point outside the map's branches")
+    return np.stack([r * np.cos(out), r * np.sin(out)], axis=1)
+
+
+def ns_taylor_couette_parametric(path, p: int = 3, mu: float = 1e-3, omega: float = 1.0, diabatic: bool = False,
+                                 dTdn: float = 1.0, num_flux: int = NUM_FLUX_ROE_PIKE, perturb: float = 0.0):
+    """The reference's Taylor-Couette case on its own parametric domain: the square-annulus QUAD mesh of the gmsh
+    file `path` (gmsh.write_square_annulus_msh, the PARAMETRIC domain of meshes/n-cylinder_hollow/2d.geo) mapped by
+    cylinder_parametric_map the way the reference maps a parametric domain. Walls, constants and state as
+    ns_taylor_couette (the state's density scaled by 1 + perturb sin(3 theta) sin(pi (r - r_i) / (r_o - r_i)));
+    the BC codes come from the file (the outer wall's code sets adiabatic or diabatic)."""
+    from .gmsh import gmsh_tp_problem
+    r_i, r_o, Pr, r_s, p_b, t_b = 0.5, 1.0, 0.72, 1.0, 1.0, 1.0
+    ns = _ns_params(mu, Pr=Pr, r_s=r_s)
+    ns["dTdn"] = float(dTdn) if diabatic else 0.0
+
+    def state(xy):
+        X, Y = xy[:, 0], xy[:, 1]
+        U = taylor_couette_state(X, Y, r_i, r_o, omega, mu, Pr, r_s, t_b, p_b, ns["dTdn"])
+        if perturb:
+            R, TH = np.sqrt(X * X + Y * Y), np.arctan2(Y, X)
+            U = U * (1.0 + perturb * np.sin(3.0 * TH) * np.sin(math.pi * (R - r_i) / (r_o - r_i)))[None]
+        return np.asarray(U).T
+    prob = gmsh_tp_problem(path, 2, p, PDE_NAVIER_STOKES, num_flux, state, exterior=_taylor_couette_wall(r_i, omega, p_b),
+                           ns=ns, parametric=cylinder_parametric_map, name="ns_taylor_couette_parametric")
+    prob.meta.update(p=p, omega=omega, r_i=r_i, r_o=r_o)
+    return prob

@@ -15,7 +15,8 @@
  * --steps it then runs N steps of time_step_ssp_rk_33 (solve_explicit.c:252-301, compiled from the reference's
  * file below) and writes sol_steps.bin and the per-step max_rhs.
  * --map A L makes the domain's parametric map x,y += A sin(pi x / (L/2)) sin(pi y / (L/2)) (both coordinates),
- * the test case's constructor_xyz for a parametric mesh (geometry_T.c:857-874). */
+ * the test case's constructor_xyz for a parametric mesh (geometry_T.c:857-874). Without it a parametric mesh keeps
+ * the test case's own map (e.g. constructor_xyz_cylinder_parametric_T of the Taylor-Couette case). */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -202,7 +203,7 @@ int main(int argc, char** argv)
 	/* structor_simulation(..., 'c', ADAPT_0, ..., 'r', ...) of test_integration.c:104-126. */
 	struct Simulation* sim = constructor_Simulation(ctrl_name);
 	struct Test_Case* test_case = (struct Test_Case*)sim->test_case_rc->tc;
-	if (sim->domain_type == DOM_PARAMETRIC)
+	if (sim->domain_type == DOM_PARAMETRIC && g_map_a != 0.0)
 		test_case->constructor_xyz = constructor_xyz_sinusoidal;
 	test_case->set_sol = test_case->set_sol_start = set_sol_zero;
 	test_case->constructor_sol = test_case->constructor_sol_start = constructor_sol_zero;

@@ -39,8 +39,8 @@ def build(ref_dir: str, jobs: int | None = None) -> str:
 _CTRL = """pde_name  {pde_name}
 pde_spec  {pde_spec}
 
-geom_name n-cube
-geom_spec NONE
+geom_name {geom_name}
+geom_spec {geom_spec}
 
 dimension 2
 
@@ -71,7 +71,7 @@ _TEST_CASE = """solver_proc   explicit
 solver_type_e ssp_rk_33
 
 num_flux_1st {num_flux}
-
+{extra}
 time_step  {dt!r}
 time_final {t_final!r}
 
@@ -136,7 +136,7 @@ def write_tri_quad_msh(path: str, mesh) -> None:
 
 def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux: int, state_fn=None,
              steps: int = 0, dt: float = 0.0, map_amplitude: float = 0.0, b_adv=(1.0, 0.5), mesh_writer=None,
-             states_fn=None, pde_spec: str | None = None) -> dict:
+             states_fn=None, pde_spec: str | None = None, ns: dict | None = None) -> dict:
     """Set up a periodic n x n mesh of [lo, hi]^2 at order p in the reference and run it.
 
     pde: "advection" (upwind, b_adv) or "euler". map_amplitude > 0 makes the domain parametric with the map
@@ -145,7 +145,9 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     its solution-node coordinates (Lagrange coefficients are nodal values); states_fn(geometry) -> one such array per
     volume is the alternative that sees the whole geometry dump. With either, the reference's compute_rhs and
     ``steps`` SSP-RK3 steps of size dt are run. pde_spec overrides the test case (advection: "steady/free_stream",
-    no source; "steady/default", the source of solution_advection_default_T.c).
+    no source; "steady/default", the source of solution_advection_default_T.c). pde "navier_stokes" runs the
+    reference's steady/taylor_couette case on the parametric mesh of mesh_writer with the constants of ns (mu, Pr,
+    r_s, omega, p_b, t_b, rho_b, E_b and dTdn; dTdn != 0 makes the outer wall diabatic), BR2 for the viscous terms.
     """
     from dpgsolver_gb300.host.gmsh import write_box_msh
 
@@ -159,6 +161,8 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
         write_box_msh(mesh, 2, n, lo=lo, hi=hi, periodic=True)
     else:
         mesh_writer(mesh)
+    geom_name, geom_spec, extra = "n-cube", "NONE", ""
+    domain = "parametric" if map_amplitude else "straight"
     if pde == "advection":
         pde_spec = pde_spec or "steady/free_stream"
         solution = f"advection_type constant\nb_adv   {b_adv[0]!r} {b_adv[1]!r} 0.0\n"
@@ -166,16 +170,26 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
         pde_spec = pde_spec or "periodic/periodic_vortex"
         solution = ("r_v   0.165\ntheta 0.7853981633974483\nV_inf 0.5916079783099616\np_inf 1.0\nt_inf 1.0\n"
                     "Rg    1.0\n\np_frac 0.05\n")
+    elif pde == "navier_stokes":
+        pde_spec = pde_spec or "steady/taylor_couette"
+        geom_name, domain, extra = "n-cylinder_hollow", "parametric", "num_flux_2nd BR2_stable\n"
+        geom_spec = ("diabatic_o" if ns["dTdn"] != 0.0 else "adiabatic_o") + "/geom_ar_1"
+        flux_type = "constant" if ns["dTdn"] != 0.0 else "constant_zero"
+        solution = (f"Pr  {ns['Pr']!r}\nr_s {ns['r_s']!r}\n\nviscosity_type constant\nmu {ns['mu']!r}\n\n"
+                    f"diabatic_flux_type {flux_type}\ndTdn {ns['dTdn']!r}\n\nno_slip_type rotating\n"
+                    f"omega {ns['omega']!r}\n\nno_slip_all_type density_energy\np_b {ns['p_b']!r}\n"
+                    f"t_b {ns['t_b']!r}\n\nrho_b {ns['rho_b']!r}\nE_b {ns['E_b']!r}\n")
     else:
         raise ValueError(pde)
-    domain = "parametric" if map_amplitude else "straight"
     _write(os.path.join(INPUT_DIR, "testing", "control_files", ctrl_name + ".ctrl"),
-           _CTRL.format(pde_name=pde, pde_spec=pde_spec, domain=domain, mesh=mesh, p=p))
+           _CTRL.format(pde_name=pde, pde_spec=pde_spec, geom_name=geom_name, geom_spec=geom_spec, domain=domain, mesh=mesh, p=p))
     data_dir = os.path.join(INPUT_DIR, "input_files", pde, pde_spec)
     _write(os.path.join(data_dir, "test_case.data"),
-           _TEST_CASE.format(num_flux=NUM_FLUX_NAMES[num_flux], dt=float(dt or 1e-3),
+           _TEST_CASE.format(num_flux=NUM_FLUX_NAMES[num_flux], extra=extra, dt=float(dt or 1e-3),
                              t_final=float((dt or 1e-3) * max(steps, 1))))
     _write(os.path.join(data_dir, "solution.data"), solution)
+    if pde == "navier_stokes":   # the annulus radii the Taylor-Couette solution functions read
+        _write(os.path.join(data_dir, "geometry_parameters.geo"), "r_i = 0.5;\nr_o = 1.0;\n")
 
     args = [HARNESS, ctrl_name, case_dir]
     if map_amplitude:
@@ -246,6 +260,14 @@ def _advection_default_state(x):
     return np.sin(SOURCE_M * x[:, 0] + SOURCE_A) * np.sin(SOURCE_M * x[:, 1] + SOURCE_A)
 
 
+def _tc_state(x, diabatic):
+    from dpgsolver_gb300.host.problem import taylor_couette_state
+    X, Y = x[:, 0], x[:, 1]
+    U = taylor_couette_state(X, Y, 0.5, 1.0, 1.0, _TC_MU, 0.72, 1.0, 1.0, 1.0, 1.0 if diabatic else 0.0)
+    R, TH = np.sqrt(X * X + Y * Y), np.arctan2(Y, X)
+    return (np.asarray(U) * (1.0 + 0.2 * np.sin(3.0 * TH) * np.sin(np.pi * (R - 0.5) / 0.5))[None]).T
+
+
 def _vortex_state(x):
     from dpgsolver_gb300.host.problem import isentropic_vortex, primitive_to_conserved
     rho, u, v, pr = isentropic_vortex(x, 5.0, 5.0, 5.0)
@@ -258,10 +280,16 @@ def _vortex_state(x):
 # 0.05 sin(pi x/5) sin(pi y/5), vortex strength 5 at (5,5) on (1,1,1,1)) on smaller meshes and other fluxes and
 # orders; "c2" itself (64^2, p = 3, Roe) is run live by the CPU tests. "c1_source" is the reference's steady
 # advection case with a source term (steady/default: u = sin(2.15 x + 0.23) sin(2.15 y + 0.23), s = b . grad u) on
-# a periodic QUAD 8^2 mesh of [-1,1]^2 mapped by 0.05 sin(pi x) sin(pi y), p = 3, upwind, 20 steps.
+# a periodic QUAD 8^2 mesh of [-1,1]^2 mapped by 0.05 sin(pi x) sin(pi y), p = 3, upwind, 20 steps. "tc_*" are the
+# reference's Navier-Stokes Taylor-Couette case (steady/taylor_couette, mu = 0.02, omega = 1) on its parametric square
+# annulus with 2 x 2 volumes per block (16 volumes): rotating inner wall, adiabatic (p = 3) or diabatic (dTdn = 1,
+# p = 2) outer wall; Roe-Pike (the only inviscid flux the reference's Navier-Stokes takes) and BR2, the state
+# perturbed by 20 %, 10 steps.
 CASES = {
     "c1": ("advection", 16, 2, 11, 100),
     "c1_source": ("advection_default", 8, 3, 11, 20),
+    "tc_n2": ("navier_stokes_tc", 2, 3, 31, 10),
+    "tc_diab_n2": ("navier_stokes_tc_diabatic", 2, 2, 31, 10),
     "c2_n8": ("euler", 8, 3, 31, 1000),
     "c2_lf_n8": ("euler", 8, 3, 32, 20),
     "c2_p1_n8": ("euler", 8, 1, 32, 20),
@@ -278,7 +306,22 @@ def host_problem(name: str):
         return P.advection_2d(n, p)
     if pde == "advection_default":
         return P.advection_default_2d(n, p, n_steps=steps)
+    if pde.startswith("navier_stokes_tc"):
+        return P.ns_taylor_couette_parametric(_tc_mesh(name, n, pde.endswith("diabatic")), p, mu=_TC_MU,
+                                              diabatic=pde.endswith("diabatic"), num_flux=flux, perturb=0.2)
     return P.euler_vortex_2d(n=n, p=p, num_flux=flux)
+
+
+_TC_MU = 0.02
+
+
+def _tc_mesh(name: str, n: int, diabatic: bool) -> str:
+    """The Taylor-Couette cases' square-annulus mesh (n x n volumes per block), written to the temporary directory."""
+    import tempfile
+    from dpgsolver_gb300.host.gmsh import write_square_annulus_msh
+    path = os.path.join(tempfile.gettempdir(), f"dpgsolver_gb300_{name}_{os.getpid()}.msh")
+    write_square_annulus_msh(path, n, n, outer=20112 if diabatic else 20111)
+    return path
 
 
 def run_named(name: str) -> dict:
@@ -290,6 +333,17 @@ def run_named(name: str) -> dict:
     if pde == "advection_default":
         return run_case(name, "advection", n, p, -1.0, 1.0, flux, state_fn=_advection_default_state, steps=steps,
                         dt=prob.dt, map_amplitude=prob.meta["amplitude"], pde_spec="steady/default")
+    if pde.startswith("navier_stokes_tc"):
+        from dpgsolver_gb300.host.gmsh import write_square_annulus_msh
+        diabatic = pde.endswith("diabatic")
+        ns = dict(prob.ns, omega=1.0, p_b=1.0, t_b=1.0, rho_b=1.0, E_b=1.0 / 0.4 + 0.5 * 0.5 ** 2)
+
+        def states(out):   # the host problem's state formula at the reference's solution nodes
+            return [_tc_state(x, diabatic) for x in out["xyz_vs"]]
+        return run_case(name, "navier_stokes", n, p, 0.0, 1.0, flux, states_fn=states, steps=steps, dt=prob.dt,
+                        mesh_writer=lambda path: write_square_annulus_msh(path, n, n,
+                                                                          outer=20112 if diabatic else 20111),
+                        ns=ns)
     return run_case(name, pde, n, p, 0.0, 10.0, flux, state_fn=_vortex_state, steps=steps, dt=prob.dt,
                     map_amplitude=0.05)
 
@@ -319,12 +373,14 @@ def to_arrays(out: dict) -> dict:
 def with_reference_inputs(prob, ref: dict):
     """Give the host problem the reference's own geometry and initial state: what a caller packing the reference's
     Solver_Volume / Solver_Face lists would pass. Checks first that both list the same volumes (solution nodes within
-    1e-12) and faces (volumes and local faces per side, identity face-node orders) in the same order."""
+    1e-12) and faces (volumes and local faces per side, identity face-node orders on interior faces) in the same
+    order."""
     xyz = prob.solution_node_xyz()
     if np.abs(xyz - ref["xyz_vs"]).max() > 1e-12:
         raise AssertionError("volume lists differ")
+    interior = ref["face_vol"][:, 1] >= 0
     if not (np.array_equal(prob.mesh.face_vol, ref["face_vol"]) and np.array_equal(prob.mesh.face_lf, ref["face_lf"])
-            and not np.any(ref["face_ord"])):
+            and not np.any(ref["face_ord"][interior])):
         raise AssertionError("face lists differ")
     g = prob.geom
     g.metrics_vc = np.array(ref["metrics_vc"], dtype=np.float64)

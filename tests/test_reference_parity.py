@@ -3,9 +3,11 @@ time_step_ssp_rk_33, compiled from its sources into oracle/_ref).
 
 * Golden fixtures (tests/golden/reference_*.npz, made by tests/golden/make_ref_golden.py) hold the reference's
   residual and RK states on the 2D configurations: the advection case at its stated size (QUAD 16^2, p = 2, 100
-  steps) and the curved Euler vortex on 8^2 / 4^2 meshes (Roe and Lax-Friedrichs, p = 1, 3, 4; 1000 Roe steps).
-  The oracle, given the reference's geometry and state, must reproduce them to 1e-12; the repo's own geometry must
-  reproduce the reference's to 1e-13.
+  steps), the steady advection case with its source term, the curved Euler vortex on 8^2 / 4^2 meshes (Roe and
+  Lax-Friedrichs, p = 1, 3, 4; 1000 Roe steps), and the Navier-Stokes Taylor-Couette case on the reference's
+  parametric annulus (BR2, rotating inner wall, adiabatic or diabatic outer wall). The oracle, given the reference's
+  geometry and state, must reproduce them to 1e-12 (the residual to max(1e-12, twice its one-ulp noise floor)); the
+  repo's own geometry must reproduce the reference's to 1e-13.
 * Where oracle/_ref is built (the reference tree is present), the full-size vortex (QUAD 64^2, p = 3, Roe) is run
   live: residual, ten RK steps and geometry.
 """
@@ -28,12 +30,19 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
+def _residual_tol(o, prob, r):
+    """max(1e-12, 2 x the residual's response to one-ulp noise on its input state)."""
+    noisy = prob.sol * (1.0 + np.random.default_rng(0).choice([-1.0, 1.0], prob.sol.shape) * 2.0 ** -52)
+    return max(1e-12, 2.0 * _rel(o.compute_rhs(noisy)[0], r))
+
+
 @pytest.mark.parametrize("name", FIXTURE_CASES)
 def test_oracle_residual_matches_reference_fixture(name):
     ref = _fixture(name)
     prob = R.with_reference_inputs(R.host_problem(name), ref)
-    r, mx = oracle.Oracle(prob).compute_rhs(prob.sol)
-    assert _rel(r, ref["rhs"]) <= 1e-12
+    o = oracle.Oracle(prob)
+    r, mx = o.compute_rhs(prob.sol)
+    assert _rel(r, ref["rhs"]) <= _residual_tol(o, prob, r)
     assert abs(mx - float(ref["max_rhs"])) <= 1e-12 * float(ref["max_rhs"])
 
 
