@@ -272,6 +272,46 @@ def write_square_annulus_msh(path, n_t: int, n_r: int, r_i: float = 0.5, r_o: fl
         fh.write("$EndElements\n")
 
 
+def write_quarter_square_annulus_msh(path, n_t: int, n_r: int, r_i: float = 1.0, r_o: float = 1.384,
+                                     radial: int = 10101, inner: int = 20102, outer: int = 30102):
+    """Write the quarter square annulus x, y >= 0, r_i <= max(x, y) <= r_o as a QUAD gmsh 2.2 file, the parametric
+    domain of the reference's n-cylinder_hollow_section/2d.geo (mesh_domain PARAMETRIC: two transfinite blocks split
+    along the diagonal from (r_i, r_i) to (r_o, r_o)) that its cylinder map takes to the quarter annulus. n_t volumes
+    along each side of a block, n_r across; the boundary lines carry the .geo's Euler codes: radial (the lines on
+    y = 0 and x = 0, BC_STEP_SC + BC_RIEMANN), inner (2 BC_STEP_SC + BC_SLIPWALL) and outer (3 BC_STEP_SC +
+    BC_SLIPWALL). Then the volumes, all with the same local frame (r radial, s counter-clockwise)."""
+    n_a = 2 * n_t
+
+    def node(i, j):
+        return i + (n_r + 1) * j
+
+    pts = []
+    for j in range(n_a + 1):
+        for i in range(n_r + 1):
+            r = r_i + (r_o - r_i) * i / n_r
+            pts.append((r, r * j / n_t) if j <= n_t else (r - r * (j - n_t) / n_t, r))
+    elems = []
+    for i in range(n_r):
+        elems.append((LINE, (radial, 1001), [node(i, 0), node(i + 1, 0)]))
+    for i in range(n_r):
+        elems.append((LINE, (radial, 1002), [node(i, n_a), node(i + 1, n_a)]))
+    for j in range(n_a):
+        elems.append((LINE, (inner, 1003), [node(0, j), node(0, j + 1)]))
+    for j in range(n_a):
+        elems.append((LINE, (outer, 1005), [node(n_r, j), node(n_r, j + 1)]))
+    for j in range(n_a):
+        for i in range(n_r):   # gmsh's counter-clockwise order
+            elems.append((QUAD, (9401, 4001), [node(i, j), node(i + 1, j), node(i + 1, j + 1), node(i, j + 1)]))
+    with open(path, "w") as fh:
+        fh.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % len(pts))
+        for k, (x, y) in enumerate(pts):
+            fh.write("%d %.17g %.17g 0\n" % (k + 1, x, y))
+        fh.write("$EndNodes\n$Elements\n%d\n" % len(elems))
+        for k, (t, tags, verts) in enumerate(elems):
+            fh.write("%d %d 2 %d %d %s\n" % (k + 1, t, tags[0], tags[1], " ".join(str(v + 1) for v in verts)))
+        fh.write("$EndElements\n")
+
+
 # ---- a TP problem on a mesh read from a file ------------------------------------------------------------------------
 def tp_face_permutation(match, q: int, d: int) -> np.ndarray:
     """The right-trace gather permutation nc (sR[i] = sR_own[nc[i]]) of a TP face's q^(d-1) GL nodes from the

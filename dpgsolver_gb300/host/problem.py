@@ -632,6 +632,41 @@ def cylinder_parametric_map(xy):
     return np.stack([r * np.cos(out), r * np.sin(out)], axis=1)
 
 
+def supersonic_vortex_state(x, y, r_i: float = 1.0, m_i: float = 2.25, rho_i: float = 1.0):
+    """The reference's supersonic vortex (solution_supersonic_vortex_T.c:70-107, after Aftosmis et al. 1995):
+    rho = rho_i (1 + (gamma - 1) / 2 m_i^2 (1 - (r_i / r)^2))^(1 / (gamma - 1)), p = rho^gamma, the azimuthal
+    velocity r_i c_i m_i / r (c_i = sqrt(gamma) rho_i^((gamma - 1) / 2)) turning clockwise. Conserved (4, ...)."""
+    r, t = np.sqrt(x * x + y * y), np.arctan2(y, x)
+    c_i = math.sqrt(GAMMA) * rho_i ** (0.5 * GM1)
+    vt = -r_i * c_i * m_i / r
+    rho = rho_i * (1.0 + 0.5 * GM1 * m_i * m_i * (1.0 - (r_i / r) ** 2)) ** (1.0 / GM1)
+    return primitive_to_conserved(2, rho, np.stack([-np.sin(t) * vt, np.cos(t) * vt]), rho ** GAMMA)
+
+
+def euler_supersonic_vortex(path, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, perturb: float = 0.0):
+    """The reference's steady/supersonic_vortex case on its own parametric domain: the quarter square annulus of the
+    gmsh file `path` (gmsh.write_quarter_square_annulus_msh; r_i = 1, r_o = 1.384) mapped by cylinder_parametric_map
+    the way the reference maps a parametric domain; m_i = 2.25, rho_i = 1. Riemann faces on the radial lines (their
+    exterior state the exact solution), slip walls on the arcs; the state is the exact solution with its density
+    scaled by 1 + perturb sin(4 theta) sin(pi (r - r_i) / (r_o - r_i))."""
+    from .gmsh import gmsh_tp_problem
+    r_i, r_o = 1.0, 1.384
+
+    def exact(xy):
+        return np.asarray(supersonic_vortex_state(xy[:, 0], xy[:, 1], r_i)).T
+
+    def state(xy):
+        U = exact(xy)
+        if perturb:
+            R, TH = np.sqrt(xy[:, 0] ** 2 + xy[:, 1] ** 2), np.arctan2(xy[:, 1], xy[:, 0])
+            U = U * (1.0 + perturb * np.sin(4.0 * TH) * np.sin(math.pi * (R - r_i) / (r_o - r_i)))[:, None]
+        return U
+    prob = gmsh_tp_problem(path, 2, p, PDE_EULER, num_flux, state, exterior=exact,
+                           parametric=cylinder_parametric_map, name="euler_supersonic_vortex")
+    prob.meta.update(p=p, r_i=r_i, r_o=r_o)
+    return prob
+
+
 def ns_taylor_couette_parametric(path, p: int = 3, mu: float = 1e-3, omega: float = 1.0, diabatic: bool = False,
                                  dTdn: float = 1.0, num_flux: int = NUM_FLUX_ROE_PIKE, perturb: float = 0.0):
     """The reference's Taylor-Couette case on its own parametric domain: the square-annulus QUAD mesh of the gmsh

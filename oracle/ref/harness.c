@@ -1,6 +1,6 @@
 /* Driver of the reference's own explicit-DG code for parity pins (oracle/_ref only: TEST INFRASTRUCTURE).
  *
- *   dpg_ref_harness <ctrl_name> <out_dir> [--map A L] [--state sol.bin] [--steps N --dt DT]
+ *   dpg_ref_harness <ctrl_name> <out_dir> [--map A L] [--keep-sol] [--state sol.bin] [--steps N --dt DT]
  *
  * It sets a simulation up the way the reference's integration tests do (structor_simulation,
  * src/testing/integration/test_integration.c:104-126, then the explicit solver's set-up of
@@ -16,7 +16,9 @@
  * file below) and writes sol_steps.bin and the per-step max_rhs.
  * --map A L makes the domain's parametric map x,y += A sin(pi x / (L/2)) sin(pi y / (L/2)) (both coordinates),
  * the test case's constructor_xyz for a parametric mesh (geometry_T.c:857-874). Without it a parametric mesh keeps
- * the test case's own map (e.g. constructor_xyz_cylinder_parametric_T of the Taylor-Couette case). */
+ * the test case's own map (e.g. constructor_xyz_cylinder_parametric_T of the Taylor-Couette case).
+ * --keep-sol leaves the test case's constructor_sol in place (only the initial state is replaced): the boundary
+ * values that read it (the Riemann faces' exterior state, boundary_euler_T.c) then see the test case's solution. */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -176,7 +178,8 @@ static void write_volume_field(const struct Simulation* sim, FILE* f, int which)
 int main(int argc, char** argv)
 {
 	if (argc < 3) {
-		fprintf(stderr,"usage: %s ctrl_name out_dir [--map A L] [--state sol.bin] [--steps N --dt DT]\n",argv[0]);
+		fprintf(stderr,"usage: %s ctrl_name out_dir [--map A L] [--keep-sol] [--state sol.bin] [--steps N --dt DT]\n",
+		        argv[0]);
 		return 2;
 	}
 	const char* ctrl_name = argv[1];
@@ -184,8 +187,11 @@ int main(int argc, char** argv)
 	const char* state = NULL;
 	int n_steps = 0;
 	double dt = 0.0;
+	int keep_sol = 0;
 	for (int i = 3; i < argc; ++i) {
-		if (!strcmp(argv[i],"--map") && i + 2 < argc) {
+		if (!strcmp(argv[i],"--keep-sol")) {
+			keep_sol = 1;
+		} else if (!strcmp(argv[i],"--map") && i + 2 < argc) {
 			g_map_a = atof(argv[++i]);
 			g_map_l = atof(argv[++i]);
 		} else if (!strcmp(argv[i],"--state") && i + 1 < argc) {
@@ -206,7 +212,8 @@ int main(int argc, char** argv)
 	if (sim->domain_type == DOM_PARAMETRIC && g_map_a != 0.0)
 		test_case->constructor_xyz = constructor_xyz_sinusoidal;
 	test_case->set_sol = test_case->set_sol_start = set_sol_zero;
-	test_case->constructor_sol = test_case->constructor_sol_start = constructor_sol_zero;
+	if (!keep_sol)
+		test_case->constructor_sol = test_case->constructor_sol_start = constructor_sol_zero;
 	constructor_derived_Elements(sim,IL_ELEMENT_SOLVER);
 	constructor_derived_computational_elements(sim,IL_SOLVER);
 	set_up_solver_geometry(sim);

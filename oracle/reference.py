@@ -166,6 +166,9 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     if pde == "advection":
         pde_spec = pde_spec or "steady/free_stream"
         solution = f"advection_type constant\nb_adv   {b_adv[0]!r} {b_adv[1]!r} 0.0\n"
+    elif pde == "euler" and pde_spec == "steady/supersonic_vortex":
+        geom_name, domain = "n-cylinder_hollow_section", "parametric"
+        solution = "m_i   2.25\nrho_i 1.0\n"
     elif pde == "euler":
         pde_spec = pde_spec or "periodic/periodic_vortex"
         solution = ("r_v   0.165\ntheta 0.7853981633974483\nV_inf 0.5916079783099616\np_inf 1.0\nt_inf 1.0\n"
@@ -190,8 +193,12 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     _write(os.path.join(data_dir, "solution.data"), solution)
     if pde == "navier_stokes":   # the annulus radii the Taylor-Couette solution functions read
         _write(os.path.join(data_dir, "geometry_parameters.geo"), "r_i = 0.5;\nr_o = 1.0;\n")
+    if pde_spec == "steady/supersonic_vortex":
+        _write(os.path.join(data_dir, "geometry_parameters.geo"), "r_i = 1.0;\nr_o = 1.384;\n")
 
     args = [HARNESS, ctrl_name, case_dir]
+    if pde_spec == "steady/supersonic_vortex":   # its Riemann faces read the test case's solution
+        args.append("--keep-sol")
     if map_amplitude:
         args += ["--map", repr(float(map_amplitude)), repr(float(hi - lo))]
     subprocess.run(args, check=True, cwd=case_dir, stdout=subprocess.DEVNULL)
@@ -260,6 +267,14 @@ def _advection_default_state(x):
     return np.sin(SOURCE_M * x[:, 0] + SOURCE_A) * np.sin(SOURCE_M * x[:, 1] + SOURCE_A)
 
 
+def _sv_state(x):
+    from dpgsolver_gb300.host.problem import supersonic_vortex_state
+    X, Y = x[:, 0], x[:, 1]
+    R, TH = np.sqrt(X * X + Y * Y), np.arctan2(Y, X)
+    return (np.asarray(supersonic_vortex_state(X, Y)) *
+            (1.0 + 0.05 * np.sin(4.0 * TH) * np.sin(np.pi * (R - 1.0) / 0.384))[None]).T
+
+
 def _tc_state(x, diabatic):
     from dpgsolver_gb300.host.problem import taylor_couette_state
     X, Y = x[:, 0], x[:, 1]
@@ -284,11 +299,15 @@ def _vortex_state(x):
 # reference's Navier-Stokes Taylor-Couette case (steady/taylor_couette, mu = 0.02, omega = 1) on its parametric square
 # annulus with 2 x 2 volumes per block (16 volumes): rotating inner wall, adiabatic (p = 3) or diabatic (dTdn = 1,
 # p = 2) outer wall; Roe-Pike (the only inviscid flux the reference's Navier-Stokes takes) and BR2, the state
-# perturbed by 20 %, 10 steps.
+# perturbed by 20 %, 10 steps. "sv_*" are the reference's Euler supersonic vortex (steady/supersonic_vortex,
+# m_i = 2.25) on its parametric quarter square annulus (3 x 3 and 2 x 2 volumes per block): Riemann faces with the
+# exact solution outside, slip walls on both arcs; Roe-Pike p = 3 and Lax-Friedrichs p = 2, density perturbed by 5 %.
 CASES = {
     "c1": ("advection", 16, 2, 11, 100),
     "c1_source": ("advection_default", 8, 3, 11, 20),
     "tc_n2": ("navier_stokes_tc", 2, 3, 31, 10),
+    "sv_n3": ("euler_sv", 3, 3, 31, 10),
+    "sv_lf_p2_n2": ("euler_sv", 2, 2, 32, 10),
     "tc_diab_n2": ("navier_stokes_tc_diabatic", 2, 2, 31, 10),
     "c2_n8": ("euler", 8, 3, 31, 1000),
     "c2_lf_n8": ("euler", 8, 3, 32, 20),
@@ -306,6 +325,9 @@ def host_problem(name: str):
         return P.advection_2d(n, p)
     if pde == "advection_default":
         return P.advection_default_2d(n, p, n_steps=steps)
+    if pde == "euler_sv":
+        return P.euler_supersonic_vortex(_case_mesh(name, lambda path: _sv_mesh(path, n)), p, num_flux=flux,
+                                         perturb=0.05)
     if pde.startswith("navier_stokes_tc"):
         return P.ns_taylor_couette_parametric(_tc_mesh(name, n, pde.endswith("diabatic")), p, mu=_TC_MU,
                                               diabatic=pde.endswith("diabatic"), num_flux=flux, perturb=0.2)
@@ -315,13 +337,24 @@ def host_problem(name: str):
 _TC_MU = 0.02
 
 
-def _tc_mesh(name: str, n: int, diabatic: bool) -> str:
-    """The Taylor-Couette cases' square-annulus mesh (n x n volumes per block), written to the temporary directory."""
+def _case_mesh(name: str, writer) -> str:
+    """A case's mesh file, written by writer(path) into the temporary directory."""
     import tempfile
-    from dpgsolver_gb300.host.gmsh import write_square_annulus_msh
     path = os.path.join(tempfile.gettempdir(), f"dpgsolver_gb300_{name}_{os.getpid()}.msh")
-    write_square_annulus_msh(path, n, n, outer=20112 if diabatic else 20111)
+    writer(path)
     return path
+
+
+def _tc_mesh(name: str, n: int, diabatic: bool) -> str:
+    """The Taylor-Couette cases' square-annulus mesh (n x n volumes per block)."""
+    from dpgsolver_gb300.host.gmsh import write_square_annulus_msh
+    return _case_mesh(name, lambda path: write_square_annulus_msh(path, n, n, outer=20112 if diabatic else 20111))
+
+
+def _sv_mesh(path: str, n: int) -> None:
+    """The supersonic vortex cases' quarter square annulus (n x n volumes per block)."""
+    from dpgsolver_gb300.host.gmsh import write_quarter_square_annulus_msh
+    write_quarter_square_annulus_msh(path, n, n)
 
 
 def run_named(name: str) -> dict:
@@ -333,6 +366,11 @@ def run_named(name: str) -> dict:
     if pde == "advection_default":
         return run_case(name, "advection", n, p, -1.0, 1.0, flux, state_fn=_advection_default_state, steps=steps,
                         dt=prob.dt, map_amplitude=prob.meta["amplitude"], pde_spec="steady/default")
+    if pde == "euler_sv":
+        def sv_states(out):   # the host problem's state formula at the reference's solution nodes
+            return [_sv_state(x) for x in out["xyz_vs"]]
+        return run_case(name, "euler", n, p, 0.0, 1.0, flux, states_fn=sv_states, steps=steps, dt=prob.dt,
+                        mesh_writer=lambda path: _sv_mesh(path, n), pde_spec="steady/supersonic_vortex")
     if pde.startswith("navier_stokes_tc"):
         from dpgsolver_gb300.host.gmsh import write_square_annulus_msh
         diabatic = pde.endswith("diabatic")
