@@ -380,6 +380,22 @@ def advection_box_2d(n: int = 8, p: int = 2, b=(1.0, 0.5)) -> DGProblem:
     return _set_boundaries(prob, sides, ext)
 
 
+def subsonic_duct_state(xyz, d: int, mach: float, perturb: float, seed: int, L: float = 10.0):
+    """The subsonic duct's state at points xyz (..., d): the stream (rho, u, p) = (1, mach sqrt(gamma), 1) along x
+    with seeded smooth perturbations of relative size perturb. Conserved (d + 2, ...)."""
+    rng = np.random.default_rng(seed)
+    ph = rng.uniform(0.0, 2.0 * math.pi, size=(d + 2, d))
+
+    def wave(k):
+        s = np.ones(xyz.shape[:-1])
+        for j in range(d):
+            s = s * np.sin(2.0 * math.pi * xyz[..., j] / L + ph[k, j])
+        return s
+    u0 = mach * math.sqrt(GAMMA)
+    vel = np.stack([u0 * (1.0 + perturb * wave(2))] + [u0 * perturb * wave(3 + j) for j in range(d - 1)])
+    return primitive_to_conserved(d, 1.0 + perturb * wave(0), vel, 1.0 + perturb * wave(1))
+
+
 def euler_subsonic_duct(d: int = 2, n: int = 6, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, mach: float = 0.4,
                         amplitude: float = 0.03, seed: int = 0, perturb: float = 0.02) -> DGProblem:
     """Curved QUAD/HEX box [0,10]^d with a subsonic stream along x: total temperature and pressure inflow at x = 0
@@ -393,18 +409,8 @@ def euler_subsonic_duct(d: int = 2, n: int = 6, p: int = 3, num_flux: int = NUM_
     geom = TPGeometry(mesh, ops, deform=deform, curved=True)
     prob = DGProblem(f"euler_subsonic_duct_{d}d", d, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
                      sol=np.zeros((mesh.n_volumes, d + 2, ops.n_vs)), dt=0.0, n_steps=100)
-    xyz = prob.solution_node_xyz()
-    rng = np.random.default_rng(seed)
-    ph = rng.uniform(0.0, 2.0 * math.pi, size=(d + 2, d))
-
-    def wave(k):
-        s = np.ones(xyz.shape[:2])
-        for j in range(d):
-            s = s * np.sin(2.0 * math.pi * xyz[..., j] / L + ph[k, j])
-        return s
+    prob.sol = _pack_state(subsonic_duct_state(prob.solution_node_xyz(), d, mach, perturb, seed, L))
     u0 = mach * math.sqrt(GAMMA)
-    vel = np.stack([u0 * (1.0 + perturb * wave(2))] + [u0 * perturb * wave(3 + j) for j in range(d - 1)])
-    prob.sol = _pack_state(primitive_to_conserved(d, 1.0 + perturb * wave(0), vel, 1.0 + perturb * wave(1)))
     prob.dt = stable_dt(prob)
     T_tot = 1.0 + 0.5 * GM1 * mach * mach
     prob.bc_data = (1.0, T_tot, T_tot ** (GAMMA / GM1), 1.0)

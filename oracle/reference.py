@@ -136,7 +136,7 @@ def write_tri_quad_msh(path: str, mesh) -> None:
 
 def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux: int, state_fn=None,
              steps: int = 0, dt: float = 0.0, map_amplitude: float = 0.0, b_adv=(1.0, 0.5), mesh_writer=None,
-             states_fn=None, pde_spec: str | None = None, ns: dict | None = None) -> dict:
+             states_fn=None, pde_spec: str | None = None, ns: dict | None = None, bc_data=None) -> dict:
     """Set up a periodic n x n mesh of [lo, hi]^2 at order p in the reference and run it.
 
     pde: "advection" (upwind, b_adv) or "euler". map_amplitude > 0 makes the domain parametric with the map
@@ -148,6 +148,8 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     no source; "steady/default", the source of solution_advection_default_T.c). pde "navier_stokes" runs the
     reference's steady/taylor_couette case on the parametric mesh of mesh_writer with the constants of ns (mu, Pr,
     r_s, omega, p_b, t_b, rho_b, E_b and dTdn; dTdn != 0 makes the outer wall diabatic), BR2 for the viscous terms.
+    Euler with pde_spec "steady/free_stream" takes bc_data = (p_back, t_total, p_total, r_s) for its back-pressure
+    and total T/p faces; "steady/supersonic_vortex" runs the supersonic vortex on the parametric quarter annulus.
     """
     from dpgsolver_gb300.host.gmsh import write_box_msh
 
@@ -166,6 +168,11 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     if pde == "advection":
         pde_spec = pde_spec or "steady/free_stream"
         solution = f"advection_type constant\nb_adv   {b_adv[0]!r} {b_adv[1]!r} 0.0\n"
+    elif pde == "euler" and pde_spec == "steady/free_stream":
+        # the stream of the subsonic duct; the back-pressure and total T/p faces read their data here too
+        p_back, t_total, p_total, r_s = bc_data
+        solution = (f"density   1.0\npressure  1.0\nmach      0.4\ntheta_deg 0.0\n\nboundary_perturb_type none\n\n"
+                    f"p_back  {p_back!r}\nt_total {t_total!r}\np_total {p_total!r}\nr_s     {r_s!r}\n")
     elif pde == "euler" and pde_spec == "steady/supersonic_vortex":
         geom_name, domain = "n-cylinder_hollow_section", "parametric"
         solution = "m_i   2.25\nrho_i 1.0\n"
@@ -299,13 +306,17 @@ def _vortex_state(x):
 # reference's Navier-Stokes Taylor-Couette case (steady/taylor_couette, mu = 0.02, omega = 1) on its parametric square
 # annulus with 2 x 2 volumes per block (16 volumes): rotating inner wall, adiabatic (p = 3) or diabatic (dTdn = 1,
 # p = 2) outer wall; Roe-Pike (the only inviscid flux the reference's Navier-Stokes takes) and BR2, the state
-# perturbed by 20 %, 10 steps. "sv_*" are the reference's Euler supersonic vortex (steady/supersonic_vortex,
+# perturbed by 20 %, 10 steps. "duct_*" are the subsonic duct on a straight 4^2 / 3^2 box of [0,10]^2 in the
+# reference's free-stream case with its internal-flow boundaries (n-cube/2d.geo, GEOM_ADV_INTERNAL): total T/p inflow,
+# back-pressure outflow, slip walls; Roe-Pike p = 3, Lax-Friedrichs p = 2, 10 steps. "sv_*" are the reference's Euler supersonic vortex (steady/supersonic_vortex,
 # m_i = 2.25) on its parametric quarter square annulus (3 x 3 and 2 x 2 volumes per block): Riemann faces with the
 # exact solution outside, slip walls on both arcs; Roe-Pike p = 3 and Lax-Friedrichs p = 2, density perturbed by 5 %.
 CASES = {
     "c1": ("advection", 16, 2, 11, 100),
     "c1_source": ("advection_default", 8, 3, 11, 20),
     "tc_n2": ("navier_stokes_tc", 2, 3, 31, 10),
+    "duct_n4": ("euler_duct", 4, 3, 31, 10),
+    "duct_lf_p2_n3": ("euler_duct", 3, 2, 32, 10),
     "sv_n3": ("euler_sv", 3, 3, 31, 10),
     "sv_lf_p2_n2": ("euler_sv", 2, 2, 32, 10),
     "tc_diab_n2": ("navier_stokes_tc_diabatic", 2, 2, 31, 10),
@@ -325,6 +336,8 @@ def host_problem(name: str):
         return P.advection_2d(n, p)
     if pde == "advection_default":
         return P.advection_default_2d(n, p, n_steps=steps)
+    if pde == "euler_duct":
+        return P.euler_subsonic_duct(2, n, p, num_flux=flux, amplitude=0.0)
     if pde == "euler_sv":
         return P.euler_supersonic_vortex(_case_mesh(name, lambda path: _sv_mesh(path, n)), p, num_flux=flux,
                                          perturb=0.05)
@@ -366,6 +379,17 @@ def run_named(name: str) -> dict:
     if pde == "advection_default":
         return run_case(name, "advection", n, p, -1.0, 1.0, flux, state_fn=_advection_default_state, steps=steps,
                         dt=prob.dt, map_amplitude=prob.meta["amplitude"], pde_spec="steady/default")
+    if pde == "euler_duct":
+        from dpgsolver_gb300.host.gmsh import write_box_msh
+        from dpgsolver_gb300.host.problem import subsonic_duct_state
+
+        def duct_state(x):
+            return np.asarray(subsonic_duct_state(x, 2, 0.4, 0.02, 0)).T
+        codes = {(0, 0): 10104, (0, 1): 10103, (1, 0): 10102, (1, 1): 10102}
+        return run_case(name, "euler", n, p, 0.0, 10.0, flux, state_fn=duct_state, steps=steps, dt=prob.dt,
+                        mesh_writer=lambda path: write_box_msh(path, 2, n, lo=0.0, hi=10.0, periodic=False,
+                                                               codes=codes),
+                        pde_spec="steady/free_stream", bc_data=prob.bc_data)
     if pde == "euler_sv":
         def sv_states(out):   # the host problem's state formula at the reference's solution nodes
             return [_sv_state(x) for x in out["xyz_vs"]]

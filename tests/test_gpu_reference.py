@@ -8,7 +8,8 @@ the reference's to 1e-12 normwise relative error (the residual to max(1e-12, twi
 with the oracle: the Taylor-Couette residual moves by 7e-13 when its input moves by one ulp), the advection
 configuration at its stated size (QUAD 16^2,
 p = 2, 100 steps), the steady advection case with its source term, the curved Euler vortex (Roe and
-Lax-Friedrichs, p = 1, 3, 4; 1000 Roe steps on 8^2), the Euler supersonic vortex (Riemann faces, slip walls) and
+Lax-Friedrichs, p = 1, 3, 4; 1000 Roe steps on 8^2), the subsonic duct (total T/p inflow, back-pressure outflow,
+slip walls), the Euler supersonic vortex (Riemann faces, slip walls) and
 the Navier-Stokes Taylor-Couette case on the reference's
 parametric annulus (BR2, rotating and adiabatic or diabatic walls, 10 steps).
 """

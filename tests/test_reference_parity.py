@@ -4,7 +4,8 @@ time_step_ssp_rk_33, compiled from its sources into oracle/_ref).
 * Golden fixtures (tests/golden/reference_*.npz, made by tests/golden/make_ref_golden.py) hold the reference's
   residual and RK states on the 2D configurations: the advection case at its stated size (QUAD 16^2, p = 2, 100
   steps), the steady advection case with its source term, the curved Euler vortex on 8^2 / 4^2 meshes (Roe and
-  Lax-Friedrichs, p = 1, 3, 4; 1000 Roe steps), the Euler supersonic vortex on the reference's parametric quarter
+  Lax-Friedrichs, p = 1, 3, 4; 1000 Roe steps), the subsonic duct with total T/p inflow and back-pressure outflow, the
+  Euler supersonic vortex on the reference's parametric quarter
   annulus (Riemann faces and slip walls), and the Navier-Stokes Taylor-Couette case on the reference's
   parametric annulus (BR2, rotating inner wall, adiabatic or diabatic outer wall). The oracle, given the reference's
   geometry and state, must reproduce them to 1e-12 (the residual to max(1e-12, twice its one-ulp noise floor)); the
