@@ -290,6 +290,12 @@ def _tc_state(x, diabatic):
     return (np.asarray(U) * (1.0 + 0.2 * np.sin(3.0 * TH) * np.sin(np.pi * (R - 0.5) / 0.5))[None]).T
 
 
+def _pos_dip(x):
+    """The near-vacuum dip of the positivity case: every conserved variable scaled by
+    1 - (1 - 1e-6) exp(-|x - (5, 5)|^2 / 0.09) (velocity and temperature unchanged)."""
+    return 1.0 - (1.0 - 1e-6) * np.exp(-((x[:, 0] - 5.0) ** 2 + (x[:, 1] - 5.0) ** 2) / 0.09)
+
+
 def _vortex_state(x):
     from dpgsolver_gb300.host.problem import isentropic_vortex, primitive_to_conserved
     rho, u, v, pr = isentropic_vortex(x, 5.0, 5.0, 5.0)
@@ -300,7 +306,10 @@ def _vortex_state(x):
 # (QUAD 16^2 on [-1,1]^2, p = 2, b = (1, 0.5), upwind, u0 = sin(pi x) sin(pi y), dt = 0.1 h / |b|, 100 steps);
 # the "c2*" cases are the curved isentropic-vortex configuration (QUAD on [0,10]^2 mapped by
 # 0.05 sin(pi x/5) sin(pi y/5), vortex strength 5 at (5,5) on (1,1,1,1)) on smaller meshes and other fluxes and
-# orders; "c2" itself (64^2, p = 3, Roe) is run live by the CPU tests. "c1_source" is the reference's steady
+# orders ("c2_pos_n8": the vortex with a near-vacuum dip at its centre, density and energy scaled down to 1e-6 there,
+# which makes enforce_positivity_highorder correct volumes in every step: 32 corrections in its 5 steps; the limiter's
+# blend amplifies rounding, so longer runs drift apart: 1.5e-13 after one step, 2.4e-13 after five, 6.6e-10 after
+# twenty between the oracle and the reference); "c2" itself (64^2, p = 3, Roe) is run live by the CPU tests. "c1_source" is the reference's steady
 # advection case with a source term (steady/default: u = sin(2.15 x + 0.23) sin(2.15 y + 0.23), s = b . grad u) on
 # a periodic QUAD 8^2 mesh of [-1,1]^2 mapped by 0.05 sin(pi x) sin(pi y), p = 3, upwind, 20 steps. "tc_*" are the
 # reference's Navier-Stokes Taylor-Couette case (steady/taylor_couette, mu = 0.02, omega = 1) on its parametric square
@@ -324,6 +333,7 @@ CASES = {
     "c2_lf_n8": ("euler", 8, 3, 32, 20),
     "c2_p1_n8": ("euler", 8, 1, 32, 20),
     "c2_p4_n4": ("euler", 4, 4, 31, 20),
+    "c2_pos_n8": ("euler_pos", 8, 3, 31, 5),
     "c2": ("euler", 64, 3, 31, 10),
 }
 
@@ -338,6 +348,11 @@ def host_problem(name: str):
         return P.advection_default_2d(n, p, n_steps=steps)
     if pde == "euler_duct":
         return P.euler_subsonic_duct(2, n, p, num_flux=flux, amplitude=0.0)
+    if pde == "euler_pos":
+        prob = P.euler_vortex_2d(n=n, p=p, num_flux=flux)
+        x = prob.solution_node_xyz()
+        prob.sol = prob.sol * _pos_dip(x.reshape(-1, 2)).reshape(x.shape[:2])[:, None, :]
+        return prob
     if pde == "euler_sv":
         return P.euler_supersonic_vortex(_case_mesh(name, lambda path: _sv_mesh(path, n)), p, num_flux=flux,
                                          perturb=0.05)
@@ -379,6 +394,11 @@ def run_named(name: str) -> dict:
     if pde == "advection_default":
         return run_case(name, "advection", n, p, -1.0, 1.0, flux, state_fn=_advection_default_state, steps=steps,
                         dt=prob.dt, map_amplitude=prob.meta["amplitude"], pde_spec="steady/default")
+    if pde == "euler_pos":
+        def pos_state(x):
+            return _vortex_state(x) * _pos_dip(x)[:, None]
+        return run_case(name, "euler", n, p, 0.0, 10.0, flux, state_fn=pos_state, steps=steps, dt=prob.dt,
+                        map_amplitude=0.05)
     if pde == "euler_duct":
         from dpgsolver_gb300.host.gmsh import write_box_msh
         from dpgsolver_gb300.host.problem import subsonic_duct_state

@@ -11,7 +11,8 @@ p = 2, 100 steps), the steady advection case with its source term, the curved Eu
 Lax-Friedrichs, p = 1, 3, 4; 1000 Roe steps on 8^2), the subsonic duct (total T/p inflow, back-pressure outflow,
 slip walls), the Euler supersonic vortex (Riemann faces, slip walls) and
 the Navier-Stokes Taylor-Couette case on the reference's
-parametric annulus (BR2, rotating and adiabatic or diabatic walls, 10 steps).
+parametric annulus (BR2, rotating and adiabatic or diabatic walls, 10 steps); the positivity limiter on the vortex
+with a near-vacuum dip (its RK states at 1e-10, the limiter's bar, with the oracle's correction count).
 """
 import os
 
@@ -23,6 +24,10 @@ import oracle.reference as R
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
+# The positivity case: correct_coef's blend of a near-vacuum volume towards its mean amplifies rounding (the oracle and
+# the reference drift from 1.5e-13 after one step to 2.4e-13 after five and 6.6e-10 after twenty), so its RK states
+# are held to the bar of the limiter's other GPU tests.
+RK_TOL = {"c2_pos_n8": 1e-10}
 CASES = [c for c in R.CASES if c != "c2"]
 
 
@@ -63,7 +68,15 @@ def test_rk3_steps_match_reference(gpu_lib, name):
     with Simulation(prob) as sim:
         sim.ssp_rk3_steps(float(ref["dt"]), int(ref["steps"]))
         s = sim.sol_coef
-    assert _rel(s, ref["sol_steps"]) <= TOL
+        n_corr = sim.positivity_corrections()
+    assert _rel(s, ref["sol_steps"]) <= RK_TOL.get(name, TOL)
+    if name in RK_TOL:   # the same limiter decisions as the oracle's restatement
+        o = oracle.Oracle(prob)
+        x, total = prob.sol.copy(), 0
+        for _ in range(int(ref["steps"])):
+            x, _, nc = o.ssp_rk3_step(x, float(ref["dt"]))
+            total += nc
+        assert n_corr == total > 0
 
 
 @pytest.mark.parametrize("name", ["c1", "c2_n8"])
