@@ -910,6 +910,12 @@ def ns_measurements(torch, stream, args):
     e2e_step()
     n_e2e = 10
     ms_e2e = _timed(torch, stream, lambda: [e2e_step() for _ in range(n_e2e)], 1) / n_e2e
+    # the end-to-end step's result against upload + graph-replayed step + download from the same input, bit for bit
+    e2e_step()
+    torch.cuda.synchronize()
+    sim.upload_state(prob.sol)
+    sim.ssp_rk3_steps(prob.dt, 1, want_max=False)
+    e2e_bitwise = bool(np.array_equal(out_h.numpy(), sim.sol_coef))
     # the discrete adjoint: one VJP of R through the host-buffer forward/backward pair
     v = np.random.default_rng(0).standard_normal(prob.sol.shape)
     sim.vjp_forward(prob.sol)
@@ -925,7 +931,8 @@ def ns_measurements(torch, stream, args):
            "rhs_value": prob.n_state / (ms_rhs * 1e-3), "rhs_ms": ms_rhs,
            "e2e": {"value": 3 * prob.n_state / (ms_e2e * 1e-3), "unit": "DOF-residual-evals/s", "ms_per_step": ms_e2e,
                    "h2d_bytes_per_step": int(prob.n_state * 8), "d2h_bytes_per_step": int(prob.n_state * 8),
-                   "note": "dgpu_ssp_rk3_step_host on pinned buffers (upload, graph-replayed step, download)"},
+                   "note": "dgpu_ssp_rk3_step_host on pinned buffers (upload, graph-replayed step, download)",
+                   "bitwise_equal_to_upload_step_download": e2e_bitwise},
            "kinetic_energy": {"initial": kinetic_energy(prob, prob.sol), "final": kinetic_energy(prob, final)},
            "launches_per_stage": 4,
            "vjp_backward_s": vjp_s,
