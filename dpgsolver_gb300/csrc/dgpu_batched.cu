@@ -57,6 +57,7 @@ struct dgpu_batch {
 	std::vector<void*> dense_bufs;         // per dense group: operators, face operators, offsets, 1/J
 	int4* d_elf = nullptr;
 	long long* d_fbase = nullptr;
+	int *d_nc = nullptr, *d_nc_inv = nullptr;   // right-trace gather permutation per face node and its inverse, or null
 	int* d_node_face = nullptr;
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	double *u = nullptr, *ug = nullptr, *u0 = nullptr, *rhs = nullptr, *vol_gl = nullptr;
@@ -99,6 +100,8 @@ struct dgpu_batch {
 		P.groups = d_groups;
 		P.elf = d_elf;
 		P.fbase = d_fbase;
+		P.nc = d_nc;
+		P.nc_inv = d_nc_inv;
 		P.gmet = gmet;
 		P.inv_wJ = inv_wJ;
 		P.fgeo = fgeo;
@@ -414,7 +417,7 @@ void drop_graphs(dgpu_batch* c)
 void free_batch(dgpu_batch* c)
 {
 	drop_graphs(c);
-	void* ptrs[] = {c->d_ops, c->d_groups, c->d_dgroups, c->d_elf, c->d_fbase, c->d_node_face, c->gmet, c->inv_wJ,
+	void* ptrs[] = {c->d_nc, c->d_nc_inv, c->d_ops, c->d_groups, c->d_dgroups, c->d_elf, c->d_fbase, c->d_node_face, c->gmet, c->inv_wJ,
 	                c->fgeo, c->u, c->ug, c->u0, c->rhs, c->vol_gl, c->traces, c->nnf, c->max_bits, c->err_flag,
 	                c->n_corr, c->d_tiles, c->d_fbc, c->d_fext};
 	for (void* p : ptrs)
@@ -908,13 +911,33 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 		c->qnode[++cur_q] = fb;
 	fbase[nF] = fb;
 	std::vector<int4> elf((size_t)nV * kMaxLf, int4{-1, -1, -1, 0});
+	// the right-trace gather permutation of every interior face (get_operator__nc_fc_T(1, face),
+	// compute_face_rlhs_T.c:133-146) in the internal face-node layout, and its inverse for side 1's lift; both stay
+	// off the device when every face's is the identity
+	std::vector<int> nc_int, nc_inv_int;
+	bool nc_identity = true;
+	if (mesh->nc_fc) {
+		nc_int.resize(fb);
+		nc_inv_int.resize(fb);
+		for (int f = 0; f < nF; ++f) {
+			const long long b0 = fbase[internal_face[f]];
+			const int nff = face_nfc[f];
+			const bool interior = mesh->face_vol[2 * f + 1] >= 0;
+			for (int i = 0; i < nff; ++i)
+				nc_inv_int[b0 + i] = -1;
+			for (int i = 0; i < nff; ++i) {
+				const int j = interior ? mesh->nc_fc[caller_fc_off[f] + i] : i;
+				if (j < 0 || j >= nff || nc_inv_int[b0 + j] != -1)
+					return reject(DGPU_ERR_INVALID_ARGUMENT, "nc_fc of face " + std::to_string(f) +
+					                                         " is not a permutation of its face nodes");
+				nc_int[b0 + i] = j;
+				nc_inv_int[b0 + j] = i;
+				nc_identity = nc_identity && j == i;
+			}
+		}
+	}
 	for (int f = 0; f < nF; ++f) {
 		const int ns_f = (mesh->face_vol[2 * f + 1] < 0) ? 1 : 2;
-		if (mesh->nc_fc && ns_f == 2)
-			for (int i = 0; i < face_nfc[f]; ++i)
-				if (mesh->nc_fc[caller_fc_off[f] + i] != i)
-					return reject(DGPU_ERR_UNSUPPORTED, "the batched path needs face nodes in one canonical order "
-					                                    "(identity nc_fc); orient dense faces with face_ord");
 		for (int s = 0; s < ns_f; ++s) {
 			const int v = mesh->face_vol[2 * f + s], lf = mesh->face_lf[2 * f + s];
 			int4& slot = elf[(size_t)sorted_pos[v] * kMaxLf + lf];
@@ -1149,6 +1172,10 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	B_TRY(upload_vec(&c->d_dgroups, c->hdgroups));
 	B_TRY(upload_vec(&c->d_elf, elf));
 	B_TRY(upload_vec(&c->d_fbase, fbase));
+	if (!nc_identity) {
+		B_TRY(upload_vec(&c->d_nc, nc_int));
+		B_TRY(upload_vec(&c->d_nc_inv, nc_inv_int));
+	}
 	B_TRY(upload_vec(&c->d_node_face, node_face));
 	B_TRY(upload_vec(&c->gmet, gmet));
 	B_TRY(upload_vec(&c->inv_wJ, inv_wJ));

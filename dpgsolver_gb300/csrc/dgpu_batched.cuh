@@ -69,6 +69,11 @@ struct BParams {
 	const BGroup* groups;     // [group]
 	const int4* elf;          // [element][kMaxLf]: (face, side, q_f, orientation)
 	const long long* fbase;   // [face + 1]: first face node of the face (faces laid out by increasing q_f)
+	// right-trace gather permutation per face node (side 1's trace in side 0's node order is tR[nc[fbase + i]]) and
+	// its inverse (side 1's own node j holds side 0's node nc_inv[fbase + j]); both null when every face's is the
+	// identity (get_operator__nc_fc_T(1, face), compute_face_rlhs_T.c:133-146)
+	const int* nc = nullptr;
+	const int* nc_inv = nullptr;
 	const double* gmet;
 	const double* inv_wJ;
 	const double* fgeo;       // [node][D+1] blocks per face: (D+1) * fbase[f] + k * NF_f + i
@@ -281,9 +286,10 @@ __device__ __forceinline__ void bface_node_rt(const BParams& P, int f, int i, in
 	for (int k = 0; k < NV; ++k)
 		WL[k] = tL[k * nff + i];
 	if (code < 0) {
+		const int iR = P.nc ? P.nc[fb + i] : i;
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			WR[k] = tR[k * nff + i];
+			WR[k] = tR[k * nff + iR];
 	} else {
 		// a boundary face: the boundary value of its BC from the interior trace (face_solver_T.c:203-275)
 		const double* ext = P.fext + NV * fb + i;
@@ -343,12 +349,17 @@ __device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup&
 			const int4 fd = ef[lf];
 			const int qf = fd.z;
 			const int nff = (D == 2 ? qf : qf * qf);
-			const double* src = P.nnf + NV * P.fbase[fd.x];
+			const long long fb = P.fbase[fd.x];
+			const double* src = P.nnf + NV * fb;
 			const double sgn = (fd.y == 0 ? -1.0 : 1.0);   // side 0: rhs -= ; side 1: rhs -= (-nnf)
+			// side 1 reads the face flux (side 0's node order) at its own nodes through the inverse permutation
+			const int* ci = (fd.y == 1 && P.nc_inv) ? P.nc_inv + fb : nullptr;
 			double* out = sg + lf * NV * NFQ;
 			if (qf == Q) {
-				for (int it = node; it < NV * NFQ; it += N)
-					out[it] = sgn * src[it];
+				for (int it = node; it < NV * NFQ; it += N) {
+					const int k = it / NFQ, i = it % NFQ;
+					out[it] = sgn * src[k * NFQ + (ci ? ci[i] : i)];
+				}
 				continue;
 			}
 			const double(*I)[kQMax] = sops->Iup[qf];
@@ -357,7 +368,7 @@ __device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup&
 					const int k = it / Q, t = it % Q;
 					double s = 0.0;
 					for (int i = 0; i < qf; ++i)
-						s += I[i][t] * src[k * qf + i];
+						s += I[i][t] * src[k * qf + (ci ? ci[i] : i)];
 					out[k * NFQ + t] = sgn * s;
 				}
 			} else {
@@ -368,8 +379,10 @@ __device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup&
 					for (int i1 = 0; i1 < kQMax; ++i1) {
 						double acc = 0.0;
 						if (i1 < qf)
-							for (int i0 = 0; i0 < qf; ++i0)
-								acc += I[i0][a] * src[k * nff + i0 + qf * i1];
+							for (int i0 = 0; i0 < qf; ++i0) {
+								const int i = i0 + qf * i1;
+								acc += I[i0][a] * src[k * nff + (ci ? ci[i] : i)];
+							}
 						r[i1] = acc;
 					}
 #pragma unroll

@@ -432,9 +432,11 @@ __device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, con
 			const int nff = (int)(P.fbase[fd.x + 1] - fb);
 			const double* op = G.fops + G.fop_off[(lf * G.n_ord + fd.w) * (kQMax + 1) + fd.z] + m;
 			const double* src = P.nnf + NV * fb + (long long)k * nff;
+			// side 1 reads the face flux (side 0's node order) at its own nodes through the inverse permutation
+			const int* ci = (fd.y == 1 && P.nc_inv) ? P.nc_inv + fb : nullptr;
 			double s = 0.0;
 			for (int i = 0; i < nff; ++i)
-				s += __ldg(op + (long long)i * nvs) * src[i];
+				s += __ldg(op + (long long)i * nvs) * src[ci ? ci[i] : i];
 			acc += (fd.y == 0 ? -s : s);   // side 0: rhs -= ; side 1: rhs -= (-nnf)
 		}
 		smem[e * PER_E + rem] = acc;

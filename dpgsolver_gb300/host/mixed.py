@@ -53,10 +53,18 @@ class MixedTPProblem:
         # geometry per group
         self.geoms = []
         self.group_vols = []
+        from_file = getattr(mesh, "gmsh", None) is not None   # a QUAD/HEX mesh read from a file (GmshTPMesh)
+        if from_file and (deform is not None or curved):
+            raise ValueError("a mesh read from a file is taken straight (its vertices)")
         for g, ops in enumerate(self.groups):
             vols = np.nonzero(self.vol_group == g)[0]
             self.group_vols.append(vols)
-            self.geoms.append(TPGeometry(mesh, ops, deform=deform, curved=curved, vols=vols) if len(vols) else None)
+            if not len(vols):
+                self.geoms.append(None)
+            elif from_file:
+                self.geoms.append(TPGeometry(mesh, ops, curved=False, coef=mesh.vertices, vols=vols))
+            else:
+                self.geoms.append(TPGeometry(mesh, ops, deform=deform, curved=curved, vols=vols))
         self.curved = bool(curved)
         self._face_geometry()
         self.sol = np.zeros(int(self.state_off[-1]))
@@ -141,9 +149,23 @@ class MixedTPProblem:
         return apply_nodes(L, geom.X_geom)
 
     def nc_fc(self) -> np.ndarray:
-        """Identity right-trace permutation of every face (aligned structured mesh), concatenated."""
-        return np.concatenate([np.arange(n, dtype=np.int32)
-                               for n in np.diff(self.face_off)]) if self.mesh.n_faces else np.zeros(0, np.int32)
+        """Right-trace gather permutation of every face at its order q_f, concatenated: the identity on an aligned
+        structured mesh; on a mesh read from a file, the one its two sides' vertex correspondence gives
+        (get_operator__nc_fc_T(1, face), compute_face_rlhs_T.c:133-146)."""
+        if not self.mesh.n_faces:
+            return np.zeros(0, np.int32)
+        gm = getattr(self.mesh, "gmsh", None)
+        if gm is None:
+            return np.concatenate([np.arange(n, dtype=np.int32) for n in np.diff(self.face_off)])
+        from .gmsh import tp_face_permutation
+        out = []
+        for f in range(self.mesh.n_faces):
+            qf = int(self.face_q[f])
+            if self.mesh.face_vol[f, 1] >= 0:
+                out.append(np.asarray(tp_face_permutation(gm.face_match[f], qf, self.d), dtype=np.int32))
+            else:
+                out.append(np.arange(qf ** (self.d - 1), dtype=np.int32))
+        return np.concatenate(out)
 
     def flat(self) -> dict:
         """The flat multi-group layout of the C ABIs (volume blocks in list order, face blocks in face order)."""
@@ -213,14 +235,16 @@ def _seeded_p(n_volumes, p_set, seed):
 
 def mixed_euler(d: int = 3, n: int = 58, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE, seed: int = 0,
                 curved: bool = False, amplitude: float = 0.03, mach: float = 0.5, perturb: float = 0.05,
-                positivity: bool = True, periodic=True, codes=None) -> MixedTPProblem:
+                positivity: bool = True, periodic=True, codes=None, mesh=None) -> MixedTPProblem:
     """Unit square/cube, per-volume p drawn uniformly from p_set (seeded), smooth seeded sinusoidal state
     around a free stream of Mach `mach`: rho = 1 + perturb * prod sin(2 pi x_k + phi_k), p = 1 + perturb * ...,
     velocity Mach * c along a fixed oblique direction with perturbations of the same form. periodic: per direction
     (all by default); codes: {(dim, side): BC code} for the ends of the other directions, whose exterior state is
-    the unperturbed free stream."""
+    the unperturbed free stream. mesh: a QUAD/HEX mesh of the unit square/cube read from a file (gmsh.GmshTPMesh)
+    instead of the structured one, e.g. with rotated local frames (its faces' nc_fc then permute)."""
     L = 1.0
-    mesh = StructuredMesh(d, n, 0.0, L, periodic=periodic)
+    if mesh is None:
+        mesh = StructuredMesh(d, n, 0.0, L, periodic=periodic)
     deform = None
     if curved:
         deform = sinusoidal_deform_2d(amplitude, L) if d == 2 else sinusoidal_deform_3d(amplitude, L)

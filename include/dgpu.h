@@ -352,8 +352,12 @@ const char* dgpu_status_string(dgpu_status st);
  *   vol_group[v]      group of volume v
  *   mesh              as for dgpu_create with ragged blocks: volume v holds n_vc(v) = q(v)^d nodes, face f
  *                     holds n_fc(f) = q_f^(d-1) nodes with q_f = max(q(L), q(R)) (q(L) on a boundary face);
- *                     every array concatenates the blocks in list order. nc_fc must be NULL or the identity
- *                     (aligned faces). Boundary faces take bc_fc / bc_state_fc / bc_data as for dgpu_create
+ *                     every array concatenates the blocks in list order. nc_fc (NULL: the identity) is, per
+ *                     interior face, the reference's right-trace gather permutation at the face's q_f nodes
+ *                     (get_operator__nc_fc_T(1, face), compute_face_rlhs_T.c:133-146): side 1's trace is read
+ *                     at nc_fc[i] for side 0's node i, and side 1's lift reads the face flux through the
+ *                     inverse; every side then writes its traces in its own face-node order (QUAD/HEX frames
+ *                     may differ between neighbours). Boundary faces take bc_fc / bc_state_fc / bc_data as for dgpu_create
  *                     (Euler: BC_RIEMANN .. BC_SUPERSONIC_OUT; advection: the upwind codes).
  *
  * The state is the volumes' (n_vs(v) x n_var) column-major sol_coef blocks concatenated in volume-list order.
@@ -412,8 +416,11 @@ typedef struct {
 } dgpu_group;
 
 /* Batched context over TP and dense groups. face_ord (n_faces x 2, may be NULL = all 0) gives each side's
- * orientation index into its face operator table; QUAD/HEX sides must have orientation 0 (their own face-node
- * order is the face's canonical order). With positivity every dense group must give its Bezier maps. */
+ * orientation index into its face operator table; QUAD/HEX sides must have orientation 0. Two ways to describe a
+ * face's nodes: a canonical order that each side's orientation-specific operators produce (face_ord, nc_fc NULL),
+ * or the reference's own: every side's operators in its own face-node order (n_ord = 1, face_ord NULL) and the
+ * face's data in side 0's order, with nc_fc (above) relating the sides. With positivity every dense group must
+ * give its Bezier maps. */
 dgpu_status dgpu_batch_create_groups(const dgpu_physics* phys, int n_groups, const dgpu_group* groups,
                                      const int* vol_group, const dgpu_mesh* mesh, const int* face_ord,
                                      dgpu_batch** out);

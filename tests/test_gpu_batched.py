@@ -477,3 +477,104 @@ def test_dense_positivity_matches_oracle(gpu_lib, make):
             ncorr = sim.positivity_corrections()
         assert ncorr == ncorr_ref, form
         assert rel_err(s, s_ref) <= 1e-10, form
+
+
+# ---- the reference's face interface: nc_fc instead of a canonical face-node order ------------------------------
+
+@pytest.mark.parametrize("d,n", [(2, 6), (3, 3)])
+@pytest.mark.parametrize("form", FORMS)
+def test_rotated_frames_take_nc_fc(gpu_lib, tmp_path, d, n, form):
+    """A mixed-order QUAD/HEX mesh read from a gmsh file whose volumes have random local frames: neighbours see their
+    common face in different orientations, and the caller passes the reference's right-trace permutation nc_fc
+    (get_operator__nc_fc_T) per face. Residual and RK steps against the oracle, and max |R| as on the same mesh with
+    aligned frames."""
+    from dpgsolver_gb300.host import gmsh as G
+    from dpgsolver_gb300.solver import BatchSimulation
+    path = str(tmp_path / f"box{d}.msh")
+    G.write_box_msh(path, d, n, 0.0, 1.0, periodic=True, rotate_seed=3)
+    prob = M.mixed_euler(d, n, seed=1, mesh=G.GmshTPMesh(G.GmshMesh(path, d)))
+    ident = np.concatenate([np.arange(k) for k in np.diff(prob.face_off)])
+    assert np.any(prob.nc_fc() != ident)
+    ref = oracle.Oracle(prob)
+    r_ref, mx_ref = ref.compute_rhs(prob.sol)
+    s_ref = prob.sol.copy()
+    for _ in range(2):
+        s_ref, _, _ = ref.ssp_rk3_step(s_ref, prob.dt)
+    with BatchSimulation(prob) as sim:
+        sim.form = form
+        mx = sim.compute_rhs()
+        r = sim.rhs
+        sim.ssp_rk3_steps(prob.dt, 2)
+        s = sim.sol_coef
+    assert rel_err(r, r_ref) <= TOL
+    assert abs(mx - mx_ref) <= TOL * mx_ref
+    assert rel_err(s, s_ref) <= TOL
+    aligned = M.mixed_euler(d, n, seed=1)
+    with BatchSimulation(aligned) as sim:
+        assert abs(sim.compute_rhs() - mx) <= 1e-12 * mx
+
+
+def _reference_layout(prob):
+    """The mixed-type mesh as the reference's face interface describes it: every side's face operators in its own
+    face-node order (orientation 0), the face's data in side 0's own order, and nc_fc, the right-trace gather
+    permutation, instead of the canonical order that orientation-specific operators produce."""
+    fl0 = prob.flat()
+    mesh = prob.mesh
+    fo = np.asarray(fl0["face_ord"]).copy()
+    nc = np.asarray(fl0["nc_fc"], dtype=np.int32).copy()
+    d = prob.d
+    nrm = np.asarray(fl0["normals_fc"]).reshape(-1, d).copy()
+    jf = np.asarray(fl0["jacobian_det_fc"]).copy()
+
+    def canon(f, s):   # own face node j -> canonical node
+        v = int(mesh.face_vol[f, s])
+        ops = prob.groups[prob.vol_group[v]]
+        nf = int(prob.face_off[f + 1] - prob.face_off[f])
+        if not getattr(ops, "dense", False) or fo[f, s] == 0:
+            return np.arange(nf)
+        lf, qf = int(mesh.face_lf[f, s]), int(prob.face_q[f])
+        own, can = ops.face_points(lf, 0, qf), ops.face_points(lf, int(fo[f, s]), qf)
+        return np.array([int(np.argmin(np.sum((can - x) ** 2, axis=1))) for x in own])
+    for f in range(mesh.n_faces):
+        a, b = int(prob.face_off[f]), int(prob.face_off[f + 1])
+        c0 = canon(f, 0)
+        nrm[a:b] = nrm[a:b][c0]
+        jf[a:b] = jf[a:b][c0]
+        if mesh.face_vol[f, 1] >= 0:
+            c1 = canon(f, 1)
+            inv1 = np.empty_like(c1)
+            inv1[c1] = np.arange(len(c1))
+            nc[a:b] = inv1[c0]
+        fo[f] = 0
+    flat = prob.flat
+
+    def new_flat():
+        fl = flat()
+        fl.update(face_ord=fo, nc_fc=nc, normals_fc=nrm.ravel(), jacobian_det_fc=jf)
+        return fl
+    prob.flat = new_flat
+    return prob
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_dense_faces_in_the_reference_layout(gpu_lib, form):
+    """TET/WEDGE/PYR sides given their own-order face operators and nc_fc (as the reference's shim would pass them)
+    instead of orientation-specific operators: the same residual as the canonical layout, and the oracle's."""
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = TYPE_CASES["types_roe_4"]()
+    with BatchSimulation(prob) as sim:
+        sim.form = form
+        mx_can = sim.compute_rhs()
+        r_can = sim.rhs
+    prob = _reference_layout(prob)
+    ident = np.concatenate([np.arange(k) for k in np.diff(prob.face_off)])
+    assert np.any(prob.flat()["nc_fc"] != ident) and not np.any(prob.flat()["face_ord"])
+    r_ref, mx_ref = oracle.Oracle(prob).compute_rhs(prob.sol)
+    with BatchSimulation(prob) as sim:
+        sim.form = form
+        mx = sim.compute_rhs()
+        r = sim.rhs
+        sim.ssp_rk3_steps(prob.dt, 1)
+    assert rel_err(r, r_ref) <= TOL
+    assert rel_err(r, r_can) <= TOL
+    assert abs(mx - mx_can) <= TOL * mx_can
