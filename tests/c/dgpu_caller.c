@@ -11,9 +11,13 @@
  * case.bin (little endian, written by tests/test_gpu_c_caller.py):
  *   int32  magic 0x55504744, d, p, pde, num_flux, positivity, n_volumes, n_faces, n_steps
  *   f64    dt, b_adv[3]
+ *   int32  viscosity; f64 mu, Pr, r_s, dTdn (Navier-Stokes constants of the test case's input; 0 otherwise)
+ *   f64    bc_data[4] (p_back, t_total, p_total, r_s of the back-pressure / total T/p faces; 0 when none)
  *   f64    1D operators: cv0_vs_vc (q x q), cv1_vs_vc (q x q), cv0_vs_fc (2 x q), w_vc (q), ccSB0 (q x q), ccBS0 (q x q)
  *   per volume:  f64 metrics_vc (n_vc, d, d) 'C', jacobian_det_vc (n_vc), sol_coef (n_vs, n_var) 'C'
- *   per face:    int32 volume[2], ind_lf[2], ind_ord[2]; f64 normals_fc (n_fc, d) 'R', jacobian_det_fc (n_fc)
+ *   per face:    int32 volume[2], ind_lf[2], ind_ord[2] (volume -1 on a boundary face's missing side), bc;
+ *                f64 normals_fc (n_fc, d) 'R', jacobian_det_fc (n_fc); on a boundary face also the exterior state
+ *                (n_fc, n_var) 'R' (constructor_sol_bv at its nodes, or the rotating wall's state)
  * out.bin: per volume rhs (n_vs, n_var) 'C' after compute_rhs_dg, then f64 max_rhs; per volume sol_coef after
  * n_steps calls of time_step_ssp_rk_33, then f64 max_rhs of the last step.
  */
@@ -53,13 +57,17 @@ struct Neigh_Info {
 struct Solver_Face {
 	struct Intrusive_Link lnk;
 	int index;
+	int boundary, bc;                 /* Face::boundary, Face::bc */
 	struct Neigh_Info neigh_info[2];
 	struct Multiarray_d normals_fc, jacobian_det_fc;
+	struct Multiarray_d s_bv;         /* the exterior state at the face nodes (boundary faces) */
 };
 
 struct Simulation {
 	int d, p, pde, num_flux, positivity, n_var, n_vs, n_vc, n_fc, n_v, n_f;
 	double b_adv[3];
+	int viscosity;
+	double mu, Pr, r_s, dTdn, bc_data[4];
 	struct Intrusive_Link* volumes;   /* first link of each list */
 	struct Intrusive_Link* faces;
 };
@@ -121,6 +129,16 @@ static void read_case(const char* path, struct Simulation* sim, struct Operators
 	*n_steps = h[8];
 	rd(dt, sizeof(double), 1, f);
 	rd(sim->b_adv, sizeof(double), 3, f);
+	int32_t visc;
+	double nsc[4];
+	rd(&visc, sizeof(int32_t), 1, f);
+	rd(nsc, sizeof(double), 4, f);
+	rd(sim->bc_data, sizeof(double), 4, f);
+	sim->viscosity = visc;
+	sim->mu = nsc[0];
+	sim->Pr = nsc[1];
+	sim->r_s = nsc[2];
+	sim->dTdn = nsc[3];
 	const int q = sim->p + 1, d = sim->d;
 	sim->n_var = (sim->pde == DGPU_PDE_ADVECTION ? 1 : d + 2);
 	sim->n_vs = sim->n_vc = (d == 2 ? q * q : q * q * q);
@@ -151,8 +169,10 @@ static void read_case(const char* path, struct Simulation* sim, struct Operators
 		struct Solver_Face* s = &faces[i];
 		s->index = i;
 		s->lnk.next = (i + 1 < sim->n_f) ? &faces[i + 1].lnk : NULL;
-		int32_t nb[6];
-		rd(nb, sizeof(int32_t), 6, f);
+		int32_t nb[7];
+		rd(nb, sizeof(int32_t), 7, f);
+		s->boundary = (nb[1] < 0);
+		s->bc = nb[6];
 		for (int side = 0; side < 2; ++side) {
 			const int v = nb[side];
 			if (v < -1 || v >= sim->n_v)
@@ -165,6 +185,10 @@ static void read_case(const char* path, struct Simulation* sim, struct Operators
 		ma_init(&s->jacobian_det_fc, 'C', 1, sim->n_fc, 1, 1);
 		rd(s->normals_fc.data, sizeof(double), ma_size(&s->normals_fc), f);
 		rd(s->jacobian_det_fc.data, sizeof(double), ma_size(&s->jacobian_det_fc), f);
+		if (s->boundary) {
+			ma_init(&s->s_bv, 'R', 2, sim->n_fc, sim->n_var, 1);
+			rd(s->s_bv.data, sizeof(double), ma_size(&s->s_bv), f);
+		}
 	}
 	double extra;
 	if (fread(&extra, sizeof extra, 1, f) == 1)
@@ -191,6 +215,11 @@ static void pack_from_sim(const struct Simulation* sim, const struct Operators* 
 	phys.positivity = sim->positivity;
 	for (int k = 0; k < 3; ++k)
 		phys.b_adv[k] = sim->b_adv[k];
+	phys.viscosity = sim->viscosity;   /* Navier-Stokes: the test case's constants */
+	phys.mu = sim->mu;
+	phys.Pr = sim->Pr;
+	phys.r_s = sim->r_s;
+	phys.dTdn = sim->dTdn;
 
 	dgpu_tp_operators ops = {.elem_type = (d == 2 ? DGPU_QUAD : DGPU_HEX), .p = sim->p, .cv0_vs_vc = o->cv0,
 	                         .cv1_vs_vc = o->cv1, .cv0_vs_fc = o->cv0_fc, .w_vc = o->w, .ccSB0_vs_vs = o->sb,
@@ -204,8 +233,12 @@ static void pack_from_sim(const struct Simulation* sim, const struct Operators* 
 	double* jf = malloc(sizeof(double) * fj * (size_t)sim->n_f);
 	int* fv = malloc(sizeof(int) * 2 * (size_t)sim->n_f);
 	int* flf = malloc(sizeof(int) * 2 * (size_t)sim->n_f);
-	if (!met || !jac || !nrm || !jf || !fv || !flf)
+	int* bc = malloc(sizeof(int) * (size_t)sim->n_f);
+	const size_t fb = (size_t)sim->n_fc * (size_t)sim->n_var;
+	double* sbv = calloc(fb * (size_t)sim->n_f, sizeof(double));
+	if (!met || !jac || !nrm || !jf || !fv || !flf || !bc || !sbv)
 		die("out of memory");
+	int n_bnd = 0;
 
 	int v = 0;
 	for (struct Intrusive_Link* c = sim->volumes; c; c = c->next, ++v) {
@@ -224,8 +257,13 @@ static void pack_from_sim(const struct Simulation* sim, const struct Operators* 
 			flf[2 * f + side] = ni->volume ? ni->ind_lf : -1;
 			/* the right-trace permutation of get_operator__nc_fc_T is the identity for every face of these
 			 * aligned meshes; a mesh with other orientations passes its nc_fc rows instead of NULL */
-			if (ni->ind_ord != 0)
+			if (ni->volume && !s->boundary && ni->ind_ord != 0)   /* a boundary face has no orientation (-1) */
 				die("this caller packs aligned faces only (ind_ord 0)");
+		}
+		bc[f] = s->bc;
+		if (s->boundary) {   /* constructor_sol_bv's values, for the boundary conditions that read them */
+			++n_bnd;
+			memcpy(sbv + f * fb, s->s_bv.data, sizeof(double) * fb);
 		}
 		if (s->normals_fc.layout != 'R')
 			die("normals not row-major");
@@ -243,12 +281,18 @@ static void pack_from_sim(const struct Simulation* sim, const struct Operators* 
 	mesh.nc_fc = NULL;
 	mesh.normals_fc = nrm;
 	mesh.jacobian_det_fc = jf;
+	if (n_bnd > 0) {
+		mesh.bc_fc = bc;
+		mesh.bc_state_fc = sbv;
+		if (sim->bc_data[0] != 0.0 || sim->bc_data[1] != 0.0)
+			mesh.bc_data = sim->bc_data;
+	}
 	if (dgpu_create(&phys, &ops, &mesh, &g_dgpu) != DGPU_OK) {
 		fprintf(stderr, "dgpu_create: %s\n", dgpu_last_error(NULL));
 		exit(1);
 	}
 	/* dgpu_create copied everything: the packed arrays may go */
-	free(met); free(jac); free(nrm); free(jf); free(fv); free(flf);
+	free(met); free(jac); free(nrm); free(jf); free(fv); free(flf); free(bc); free(sbv);
 
 	size_t n_state = 0;
 	if (dgpu_state_size(g_dgpu, &n_state) != DGPU_OK ||
