@@ -204,8 +204,8 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
         _write(os.path.join(data_dir, "geometry_parameters.geo"), "r_i = 1.0;\nr_o = 1.384;\n")
 
     args = [HARNESS, ctrl_name, case_dir]
-    if pde_spec == "steady/supersonic_vortex":   # its Riemann faces read the test case's solution
-        args.append("--keep-sol")
+    if pde_spec in ("steady/supersonic_vortex", "steady/default") and mesh_writer is not None:
+        args.append("--keep-sol")   # boundary faces that read the test case's solution
     if map_amplitude:
         args += ["--map", repr(float(map_amplitude)), repr(float(hi - lo))]
     subprocess.run(args, check=True, cwd=case_dir, stdout=subprocess.DEVNULL)
@@ -311,7 +311,9 @@ def _vortex_state(x):
 # blend amplifies rounding, so longer runs drift apart: 1.5e-13 after one step, 2.4e-13 after five, 6.6e-10 after
 # twenty between the oracle and the reference); "c2" itself (64^2, p = 3, Roe) is run live by the CPU tests. "c1_source" is the reference's steady
 # advection case with a source term (steady/default: u = sin(2.15 x + 0.23) sin(2.15 y + 0.23), s = b . grad u) on
-# a periodic QUAD 8^2 mesh of [-1,1]^2 mapped by 0.05 sin(pi x) sin(pi y), p = 3, upwind, 20 steps. "tc_*" are the
+# a periodic QUAD 8^2 mesh of [-1,1]^2 mapped by 0.05 sin(pi x) sin(pi y), p = 3, upwind, 20 steps; "c1_source_bc"
+# the same case on a 6^2 box with upwind boundaries (BC_UPWIND) on its four sides, whose exterior state is the test
+# case's steady solution. "tc_*" are the
 # reference's Navier-Stokes Taylor-Couette case (steady/taylor_couette, mu = 0.02, omega = 1) on its parametric square
 # annulus with 2 x 2 volumes per block (16 volumes): rotating inner wall, adiabatic (p = 3) or diabatic (dTdn = 1,
 # p = 2) outer wall; Roe-Pike (the only inviscid flux the reference's Navier-Stokes takes) and BR2, the state
@@ -323,6 +325,7 @@ def _vortex_state(x):
 CASES = {
     "c1": ("advection", 16, 2, 11, 100),
     "c1_source": ("advection_default", 8, 3, 11, 20),
+    "c1_source_bc": ("advection_default_bc", 6, 3, 11, 20),
     "tc_n2": ("navier_stokes_tc", 2, 3, 31, 10),
     "duct_n4": ("euler_duct", 4, 3, 31, 10),
     "duct_lf_p2_n3": ("euler_duct", 3, 2, 32, 10),
@@ -346,6 +349,8 @@ def host_problem(name: str):
         return P.advection_2d(n, p)
     if pde == "advection_default":
         return P.advection_default_2d(n, p, n_steps=steps)
+    if pde == "advection_default_bc":
+        return P.advection_default_2d(n, p, n_steps=steps, periodic=False)
     if pde == "euler_duct":
         return P.euler_subsonic_duct(2, n, p, num_flux=flux, amplitude=0.0)
     if pde == "euler_pos":
@@ -391,6 +396,13 @@ def run_named(name: str) -> dict:
     prob = host_problem(name)
     if pde == "advection":
         return run_case(name, pde, n, p, -1.0, 1.0, flux, state_fn=_advection_state, steps=steps, dt=prob.dt)
+    if pde == "advection_default_bc":   # upwind faces on the four sides, the steady solution outside
+        from dpgsolver_gb300.host.gmsh import write_box_msh
+        codes = {(k, s): 10041 for k in range(2) for s in range(2)}
+        return run_case(name, "advection", n, p, -1.0, 1.0, flux, state_fn=_advection_default_state, steps=steps,
+                        dt=prob.dt, map_amplitude=prob.meta["amplitude"], pde_spec="steady/default",
+                        mesh_writer=lambda path: write_box_msh(path, 2, n, lo=-1.0, hi=1.0, periodic=False,
+                                                               codes=codes))
     if pde == "advection_default":
         return run_case(name, "advection", n, p, -1.0, 1.0, flux, state_fn=_advection_default_state, steps=steps,
                         dt=prob.dt, map_amplitude=prob.meta["amplitude"], pde_spec="steady/default")
