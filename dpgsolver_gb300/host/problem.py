@@ -419,6 +419,23 @@ def euler_subsonic_duct(d: int = 2, n: int = 6, p: int = 3, num_flux: int = NUM_
     return _set_boundaries(prob, sides, _uniform_flow(d, 1.0, (u0,) + (0.0,) * (d - 1), 1.0))
 
 
+def euler_supersonic_duct_2d(n: int = 4, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE, mach: float = 1.5,
+                             seed: int = 0, perturb: float = 0.02) -> DGProblem:
+    """Straight QUAD box [0,10]^2 with a supersonic stream along x: supersonic inflow at x = 0 (BC_SUPERSONIC_IN,
+    the unperturbed stream (rho, p) = (1, 1) outside), supersonic outflow at x = 10 (BC_SUPERSONIC_OUT), slip walls
+    at y = 0 and 10; the state is the stream with seeded smooth perturbations (subsonic_duct_state at this Mach)."""
+    L = 10.0
+    mesh = StructuredMesh(2, n, 0.0, L, periodic=(False, False))
+    ops = TPOperatorSet(mesh.e_type, p)
+    geom = TPGeometry(mesh, ops)
+    prob = DGProblem("euler_supersonic_duct_2d", 2, PDE_EULER, num_flux, True, np.zeros(3), ops, mesh, geom,
+                     sol=np.zeros((mesh.n_volumes, 4, ops.n_vs)), dt=0.0, n_steps=100)
+    prob.sol = _pack_state(subsonic_duct_state(prob.solution_node_xyz(), 2, mach, perturb, seed, L))
+    prob.dt = stable_dt(prob)
+    sides = {(0, 0): BC_SUPERSONIC_IN, (0, 1): BC_SUPERSONIC_OUT, (1, 0): BC_SLIPWALL, (1, 1): BC_SLIPWALL}
+    return _set_boundaries(prob, sides, _uniform_flow(2, 1.0, (mach * math.sqrt(GAMMA), 0.0), 1.0))
+
+
 # ---- Navier-Stokes (pde 4: Euler inviscid flux + viscous flux, BR2 second-order numerical flux) ----------------------
 def _ns_params(mu, Pr=0.72, viscosity=VISCOSITY_CONSTANT, r_s=1.0):
     return {"viscosity": int(viscosity), "mu": float(mu), "Pr": float(Pr), "r_s": float(r_s)}

@@ -136,7 +136,8 @@ def write_tri_quad_msh(path: str, mesh) -> None:
 
 def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux: int, state_fn=None,
              steps: int = 0, dt: float = 0.0, map_amplitude: float = 0.0, b_adv=(1.0, 0.5), mesh_writer=None,
-             states_fn=None, pde_spec: str | None = None, ns: dict | None = None, bc_data=None) -> dict:
+             states_fn=None, pde_spec: str | None = None, ns: dict | None = None, bc_data=None,
+             mach: float = 0.4) -> dict:
     """Set up a periodic n x n mesh of [lo, hi]^2 at order p in the reference and run it.
 
     pde: "advection" (upwind, b_adv) or "euler". map_amplitude > 0 makes the domain parametric with the map
@@ -171,7 +172,7 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     elif pde == "euler" and pde_spec == "steady/free_stream":
         # the stream of the subsonic duct; the back-pressure and total T/p faces read their data here too
         p_back, t_total, p_total, r_s = bc_data
-        solution = (f"density   1.0\npressure  1.0\nmach      0.4\ntheta_deg 0.0\n\nboundary_perturb_type none\n\n"
+        solution = (f"density   1.0\npressure  1.0\nmach      {mach!r}\ntheta_deg 0.0\n\nboundary_perturb_type none\n\n"
                     f"p_back  {p_back!r}\nt_total {t_total!r}\np_total {p_total!r}\nr_s     {r_s!r}\n")
     elif pde == "euler" and pde_spec == "steady/supersonic_vortex":
         geom_name, domain = "n-cylinder_hollow_section", "parametric"
@@ -204,7 +205,7 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
         _write(os.path.join(data_dir, "geometry_parameters.geo"), "r_i = 1.0;\nr_o = 1.384;\n")
 
     args = [HARNESS, ctrl_name, case_dir]
-    if pde_spec in ("steady/supersonic_vortex", "steady/default") and mesh_writer is not None:
+    if pde_spec in ("steady/supersonic_vortex", "steady/default", "steady/free_stream") and mesh_writer is not None:
         args.append("--keep-sol")   # boundary faces that read the test case's solution
     if map_amplitude:
         args += ["--map", repr(float(map_amplitude)), repr(float(hi - lo))]
@@ -319,7 +320,8 @@ def _vortex_state(x):
 # p = 2) outer wall; Roe-Pike (the only inviscid flux the reference's Navier-Stokes takes) and BR2, the state
 # perturbed by 20 %, 10 steps. "duct_*" are the subsonic duct on a straight 4^2 / 3^2 box of [0,10]^2 in the
 # reference's free-stream case with its internal-flow boundaries (n-cube/2d.geo, GEOM_ADV_INTERNAL): total T/p inflow,
-# back-pressure outflow, slip walls; Roe-Pike p = 3, Lax-Friedrichs p = 2, 10 steps. "sv_*" are the reference's Euler supersonic vortex (steady/supersonic_vortex,
+# back-pressure outflow, slip walls; Roe-Pike p = 3, Lax-Friedrichs p = 2, 10 steps. "sduct_n4": the same box at
+# Mach 1.5 with supersonic inflow (the free stream outside) and outflow (GEOM_ADV_XL), Roe-Pike p = 3. "sv_*" are the reference's Euler supersonic vortex (steady/supersonic_vortex,
 # m_i = 2.25) on its parametric quarter square annulus (3 x 3 and 2 x 2 volumes per block): Riemann faces with the
 # exact solution outside, slip walls on both arcs; Roe-Pike p = 3 and Lax-Friedrichs p = 2, density perturbed by 5 %.
 CASES = {
@@ -329,6 +331,7 @@ CASES = {
     "tc_n2": ("navier_stokes_tc", 2, 3, 31, 10),
     "duct_n4": ("euler_duct", 4, 3, 31, 10),
     "duct_lf_p2_n3": ("euler_duct", 3, 2, 32, 10),
+    "sduct_n4": ("euler_sduct", 4, 3, 31, 10),
     "sv_n3": ("euler_sv", 3, 3, 31, 10),
     "sv_lf_p2_n2": ("euler_sv", 2, 2, 32, 10),
     "tc_diab_n2": ("navier_stokes_tc_diabatic", 2, 2, 31, 10),
@@ -353,6 +356,8 @@ def host_problem(name: str):
         return P.advection_default_2d(n, p, n_steps=steps, periodic=False)
     if pde == "euler_duct":
         return P.euler_subsonic_duct(2, n, p, num_flux=flux, amplitude=0.0)
+    if pde == "euler_sduct":
+        return P.euler_supersonic_duct_2d(n, p, num_flux=flux)
     if pde == "euler_pos":
         prob = P.euler_vortex_2d(n=n, p=p, num_flux=flux)
         x = prob.solution_node_xyz()
@@ -411,6 +416,17 @@ def run_named(name: str) -> dict:
             return _vortex_state(x) * _pos_dip(x)[:, None]
         return run_case(name, "euler", n, p, 0.0, 10.0, flux, state_fn=pos_state, steps=steps, dt=prob.dt,
                         map_amplitude=0.05)
+    if pde == "euler_sduct":   # supersonic in/out faces (n-cube/2d.geo, GEOM_ADV_XL), slip walls
+        from dpgsolver_gb300.host.gmsh import write_box_msh
+        from dpgsolver_gb300.host.problem import subsonic_duct_state
+
+        def sduct_state(x):
+            return np.asarray(subsonic_duct_state(x, 2, 1.5, 0.02, 0)).T
+        codes = {(0, 0): 10105, (0, 1): 10106, (1, 0): 10102, (1, 1): 10102}
+        return run_case(name, "euler", n, p, 0.0, 10.0, flux, state_fn=sduct_state, steps=steps, dt=prob.dt,
+                        mesh_writer=lambda path: write_box_msh(path, 2, n, lo=0.0, hi=10.0, periodic=False,
+                                                               codes=codes),
+                        pde_spec="steady/free_stream", bc_data=(0.0, 0.0, 0.0, 0.0), mach=1.5)
     if pde == "euler_duct":
         from dpgsolver_gb300.host.gmsh import write_box_msh
         from dpgsolver_gb300.host.problem import subsonic_duct_state
