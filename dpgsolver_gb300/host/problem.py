@@ -691,15 +691,17 @@ def euler_supersonic_vortex(path, p: int = 3, num_flux: int = NUM_FLUX_ROE_PIKE,
 
 
 def ns_taylor_couette_parametric(path, p: int = 3, mu: float = 1e-3, omega: float = 1.0, diabatic: bool = False,
-                                 dTdn: float = 1.0, num_flux: int = NUM_FLUX_ROE_PIKE, perturb: float = 0.0):
+                                 dTdn: float = 1.0, num_flux: int = NUM_FLUX_ROE_PIKE, perturb: float = 0.0,
+                                 viscosity: int = VISCOSITY_CONSTANT):
     """The reference's Taylor-Couette case on its own parametric domain: the square-annulus QUAD mesh of the gmsh
     file `path` (gmsh.write_square_annulus_msh, the PARAMETRIC domain of meshes/n-cylinder_hollow/2d.geo) mapped by
     cylinder_parametric_map the way the reference maps a parametric domain. Walls, constants and state as
     ns_taylor_couette (the state's density scaled by 1 + perturb sin(3 theta) sin(pi (r - r_i) / (r_o - r_i)));
-    the BC codes come from the file (the outer wall's code sets adiabatic or diabatic)."""
+    the BC codes come from the file (the outer wall's code sets adiabatic or diabatic); viscosity: constant mu or
+    Sutherland's law scaled by mu."""
     from .gmsh import gmsh_tp_problem
     r_i, r_o, Pr, r_s, p_b, t_b = 0.5, 1.0, 0.72, 1.0, 1.0, 1.0
-    ns = _ns_params(mu, Pr=Pr, r_s=r_s)
+    ns = _ns_params(mu, Pr=Pr, r_s=r_s, viscosity=viscosity)
     ns["dTdn"] = float(dTdn) if diabatic else 0.0
 
     def state(xy):

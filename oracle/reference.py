@@ -186,7 +186,8 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
         geom_name, domain, extra = "n-cylinder_hollow", "parametric", "num_flux_2nd BR2_stable\n"
         geom_spec = ("diabatic_o" if ns["dTdn"] != 0.0 else "adiabatic_o") + "/geom_ar_1"
         flux_type = "constant" if ns["dTdn"] != 0.0 else "constant_zero"
-        solution = (f"Pr  {ns['Pr']!r}\nr_s {ns['r_s']!r}\n\nviscosity_type constant\nmu {ns['mu']!r}\n\n"
+        visc = "sutherland" if ns.get("viscosity") == 102 else "constant"
+        solution = (f"Pr  {ns['Pr']!r}\nr_s {ns['r_s']!r}\n\nviscosity_type {visc}\nmu {ns['mu']!r}\n\n"
                     f"diabatic_flux_type {flux_type}\ndTdn {ns['dTdn']!r}\n\nno_slip_type rotating\n"
                     f"omega {ns['omega']!r}\n\nno_slip_all_type density_energy\np_b {ns['p_b']!r}\n"
                     f"t_b {ns['t_b']!r}\n\nrho_b {ns['rho_b']!r}\nE_b {ns['E_b']!r}\n")
@@ -318,7 +319,7 @@ def _vortex_state(x):
 # reference's Navier-Stokes Taylor-Couette case (steady/taylor_couette, mu = 0.02, omega = 1) on its parametric square
 # annulus with 2 x 2 volumes per block (16 volumes): rotating inner wall, adiabatic (p = 3) or diabatic (dTdn = 1,
 # p = 2) outer wall; Roe-Pike (the only inviscid flux the reference's Navier-Stokes takes) and BR2, the state
-# perturbed by 20 %, 10 steps. "duct_*" are the subsonic duct on a straight 4^2 / 3^2 box of [0,10]^2 in the
+# perturbed by 20 %, 10 steps ("tc_suth_n2": adiabatic, with Sutherland's law scaled by mu). "duct_*" are the subsonic duct on a straight 4^2 / 3^2 box of [0,10]^2 in the
 # reference's free-stream case with its internal-flow boundaries (n-cube/2d.geo, GEOM_ADV_INTERNAL): total T/p inflow,
 # back-pressure outflow, slip walls; Roe-Pike p = 3, Lax-Friedrichs p = 2, 10 steps. "sduct_n4": the same box at
 # Mach 1.5 with supersonic inflow (the free stream outside) and outflow (GEOM_ADV_XL), Roe-Pike p = 3. "sv_*" are the reference's Euler supersonic vortex (steady/supersonic_vortex,
@@ -329,6 +330,7 @@ CASES = {
     "c1_source": ("advection_default", 8, 3, 11, 20),
     "c1_source_bc": ("advection_default_bc", 6, 3, 11, 20),
     "tc_n2": ("navier_stokes_tc", 2, 3, 31, 10),
+    "tc_suth_n2": ("navier_stokes_tc_sutherland", 2, 3, 31, 10),
     "duct_n4": ("euler_duct", 4, 3, 31, 10),
     "duct_lf_p2_n3": ("euler_duct", 3, 2, 32, 10),
     "sduct_n4": ("euler_sduct", 4, 3, 31, 10),
@@ -368,7 +370,9 @@ def host_problem(name: str):
                                          perturb=0.05)
     if pde.startswith("navier_stokes_tc"):
         return P.ns_taylor_couette_parametric(_tc_mesh(name, n, pde.endswith("diabatic")), p, mu=_TC_MU,
-                                              diabatic=pde.endswith("diabatic"), num_flux=flux, perturb=0.2)
+                                              diabatic=pde.endswith("diabatic"), num_flux=flux, perturb=0.2,
+                                              viscosity=P.VISCOSITY_SUTHERLAND if "sutherland" in pde
+                                              else P.VISCOSITY_CONSTANT)
     return P.euler_vortex_2d(n=n, p=p, num_flux=flux)
 
 

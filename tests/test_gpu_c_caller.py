@@ -65,7 +65,8 @@ def write_case(path, prob, ref, n_steps):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["c1", "c2_n8", "c2_lf_n8", "duct_n4", "sv_n3", "tc_n2", "tc_diab_n2"])
+@pytest.mark.parametrize("name", ["c1", "c2_n8", "c2_lf_n8", "duct_n4", "sduct_n4", "sv_n3", "tc_n2", "tc_diab_n2",
+                                  "tc_suth_n2"])
 def test_c_caller_matches_reference(gpu_lib, tmp_path, name):
     ref = dict(np.load(os.path.join(REPO, "tests", "golden", f"reference_{name}.npz")))
     prob = R.with_reference_inputs(R.host_problem(name), ref)
