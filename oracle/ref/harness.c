@@ -1,6 +1,7 @@
 /* Driver of the reference's own explicit-DG code for parity pins (oracle/_ref only: TEST INFRASTRUCTURE).
  *
- *   dpg_ref_harness <ctrl_name> <out_dir> [--map A L] [--keep-sol] [--state sol.bin] [--steps N --dt DT]
+ *   dpg_ref_harness <ctrl_name> <out_dir> [--map A L] [--keep-sol] [--adapt-p list.txt] [--state sol.bin]
+ *                   [--steps N --dt DT]
  *
  * It sets a simulation up the way the reference's integration tests do (structor_simulation,
  * src/testing/integration/test_integration.c:104-126, then the explicit solver's set-up of
@@ -17,6 +18,12 @@
  * --map A L makes the domain's parametric map x,y += A sin(pi x / (L/2)) sin(pi y / (L/2)) (both coordinates),
  * the test case's constructor_xyz for a parametric mesh (geometry_T.c:857-874). Without it a parametric mesh keeps
  * the test case's own map (e.g. constructor_xyz_cylinder_parametric_T of the Taylor-Couette case).
+ * --adapt-p reads lines "x y p" and, after the initial solution, adapts the orders the way the reference's
+ * integration tests adapt an initial mesh (adapt_initial_mesh_if_required, test_integration.c:253-298: adapt_hp with
+ * ADAPT_S_XYZ_VE, src/simulation/solvers/adaptation/adaptation.c:112-133): the volumes with vertex (x, y) move
+ * towards order p within the control file's p_ref range (every volume starts at its lower end), and the reference
+ * keeps neighbouring orders within one of each other; volumes.txt then lists
+ * every volume's order and faces.txt every face's node count at p_f = max of its sides.
  * --keep-sol leaves the test case's constructor_sol in place (only the initial state is replaced): the boundary
  * values that read it (the Riemann faces' exterior state, boundary_euler_T.c) then see the test case's solution. */
 #include <math.h>
@@ -34,6 +41,11 @@
 #include "face_solver.h"
 #include "element.h"
 #include "definitions_mesh.h"
+#include "adaptation.h"
+#include "definitions_adaptation.h"
+#include "multiarray_constructors.h"
+#include "vector.h"
+#include "vector_constructors.h"
 
 static double g_map_a = 0.0, g_map_l = 10.0;
 
@@ -144,6 +156,36 @@ static void dump_geometry(const struct Simulation* sim, const char* out)
 	fclose(ff); fclose(fn); fclose(fjf); fclose(fxf);
 }
 
+static void adapt_orders(struct Simulation* sim, const char* path)
+{
+	FILE* f = fopen(path,"r");
+	if (!f) {
+		fprintf(stderr,"cannot open %s\n",path);
+		exit(2);
+	}
+	int n = 0;
+	double x, y;
+	int p;
+	while (fscanf(f,"%lf %lf %d",&x,&y,&p) == 3)
+		++n;
+	rewind(f);
+	struct Multiarray_d* xyz = constructor_empty_Multiarray_d('R',2,(ptrdiff_t[]){n,2});
+	struct Vector_i* ps = constructor_empty_Vector_i(n);
+	for (int i = 0; i < n; ++i) {
+		if (fscanf(f,"%lf %lf %d",&x,&y,&p) != 3)
+			exit(2);
+		xyz->data[2*i] = x;
+		xyz->data[2*i+1] = y;
+		ps->data[i] = p;
+	}
+	fclose(f);
+	struct Adaptation_Data adapt_data = { .adapt_h = { 0, 0, }, .xyz_ve_refine = (const struct const_Multiarray_d*)xyz,
+	                                      .xyz_ve_ml = NULL, .xyz_ve_p = (const struct const_Vector_i*)ps, };
+	adapt_hp(sim,ADAPT_S_XYZ_VE,&adapt_data);
+	destructor_Multiarray_d(xyz);
+	destructor_Vector_i(ps);
+}
+
 static void read_state(const struct Simulation* sim, const char* path)
 {
 	FILE* f = fopen(path,"rb");
@@ -178,7 +220,8 @@ static void write_volume_field(const struct Simulation* sim, FILE* f, int which)
 int main(int argc, char** argv)
 {
 	if (argc < 3) {
-		fprintf(stderr,"usage: %s ctrl_name out_dir [--map A L] [--keep-sol] [--state sol.bin] [--steps N --dt DT]\n",
+		fprintf(stderr,"usage: %s ctrl_name out_dir [--map A L] [--keep-sol] [--adapt-p list.txt] [--state sol.bin] "
+		        "[--steps N --dt DT]\n",
 		        argv[0]);
 		return 2;
 	}
@@ -188,9 +231,12 @@ int main(int argc, char** argv)
 	int n_steps = 0;
 	double dt = 0.0;
 	int keep_sol = 0;
+	const char* adapt_p = NULL;
 	for (int i = 3; i < argc; ++i) {
 		if (!strcmp(argv[i],"--keep-sol")) {
 			keep_sol = 1;
+		} else if (!strcmp(argv[i],"--adapt-p") && i + 1 < argc) {
+			adapt_p = argv[++i];
 		} else if (!strcmp(argv[i],"--map") && i + 2 < argc) {
 			g_map_a = atof(argv[++i]);
 			g_map_l = atof(argv[++i]);
@@ -218,6 +264,8 @@ int main(int argc, char** argv)
 	constructor_derived_computational_elements(sim,IL_SOLVER);
 	set_up_solver_geometry(sim);
 	set_initial_solution(sim);
+	if (adapt_p)
+		adapt_orders(sim,adapt_p);
 
 	dump_geometry(sim,out);
 

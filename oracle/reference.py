@@ -62,7 +62,7 @@ geom_representation  isoparametric
 geom_blending_tp     gordon_hall
 geom_blending_si     szabo_babuska_gen
 
-p_ref    {p} {p}
+p_ref    {p} {p_max}
 
 fe_method 1
 """
@@ -137,7 +137,7 @@ def write_tri_quad_msh(path: str, mesh) -> None:
 def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux: int, state_fn=None,
              steps: int = 0, dt: float = 0.0, map_amplitude: float = 0.0, b_adv=(1.0, 0.5), mesh_writer=None,
              states_fn=None, pde_spec: str | None = None, ns: dict | None = None, bc_data=None,
-             mach: float = 0.4) -> dict:
+             mach: float = 0.4, adapt_p=None, p_max: int | None = None) -> dict:
     """Set up a periodic n x n mesh of [lo, hi]^2 at order p in the reference and run it.
 
     pde: "advection" (upwind, b_adv) or "euler". map_amplitude > 0 makes the domain parametric with the map
@@ -151,6 +151,8 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     r_s, omega, p_b, t_b, rho_b, E_b and dTdn; dTdn != 0 makes the outer wall diabatic), BR2 for the viscous terms.
     Euler with pde_spec "steady/free_stream" takes bc_data = (p_back, t_total, p_total, r_s) for its back-pressure
     and total T/p faces; "steady/supersonic_vortex" runs the supersonic vortex on the parametric quarter annulus.
+    adapt_p: [(x, y, p), ...] adapts the orders around those vertices after set-up (the harness's --adapt-p); every
+    volume starts at p and may move within [p, p_max] (the control file's p_ref range).
     """
     from dpgsolver_gb300.host.gmsh import write_box_msh
 
@@ -194,7 +196,8 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
     else:
         raise ValueError(pde)
     _write(os.path.join(INPUT_DIR, "testing", "control_files", ctrl_name + ".ctrl"),
-           _CTRL.format(pde_name=pde, pde_spec=pde_spec, geom_name=geom_name, geom_spec=geom_spec, domain=domain, mesh=mesh, p=p))
+           _CTRL.format(pde_name=pde, pde_spec=pde_spec, geom_name=geom_name, geom_spec=geom_spec, domain=domain, mesh=mesh, p=p,
+                       p_max=p if p_max is None else p_max))
     data_dir = os.path.join(INPUT_DIR, "input_files", pde, pde_spec)
     _write(os.path.join(data_dir, "test_case.data"),
            _TEST_CASE.format(num_flux=NUM_FLUX_NAMES[num_flux], extra=extra, dt=float(dt or 1e-3),
@@ -210,6 +213,12 @@ def run_case(name: str, pde: str, n: int, p: int, lo: float, hi: float, num_flux
         args.append("--keep-sol")   # boundary faces that read the test case's solution
     if map_amplitude:
         args += ["--map", repr(float(map_amplitude)), repr(float(hi - lo))]
+    if adapt_p:
+        path = os.path.join(case_dir, "adapt.txt")
+        with open(path, "w") as fh:
+            for x, y, q in adapt_p:
+                fh.write(f"{float(x)!r} {float(y)!r} {int(q)}\n")
+        args += ["--adapt-p", path]
     subprocess.run(args, check=True, cwd=case_dir, stdout=subprocess.DEVNULL)
     out = _read_outputs(case_dir)
     if state_fn is not None or states_fn is not None:
@@ -503,4 +512,108 @@ def with_reference_inputs(prob, ref: dict):
     g.jacobian_det_fc = np.array(ref["jacobian_det_fc"], dtype=np.float64)
     if "sol_in" in ref:
         prob.sol = np.array(ref["sol_in"], dtype=np.float64)
+    return prob
+
+
+# ------------------------------------------------------------------------------------------------------------------
+# Mixed-order meshes: the reference's own p-adaptation (adapt_hp around given vertices) on a straight periodic QUAD
+# mesh; the batched context's path (faces at p_f = max(p_L, p_R)) against it.
+
+# name -> (pde, n, base p, highest p, numerical flux, RK steps, [(x, y, target p), ...]); the volumes around each
+# vertex are raised to its target, the rest stay at the base order.
+MIXED_CASES = {
+    "mx_adv_n8": ("advection", 8, 2, 4, 11, 20, [(-0.5, -0.5, 4), (0.5, 0.5, 3), (0.0, -0.75, 3), (-0.75, 0.5, 4)]),
+    "mx_euler_n8": ("euler", 8, 1, 3, 31, 10, [(2.5, 2.5, 3), (7.5, 7.5, 2), (5.0, 1.25, 2), (1.25, 7.5, 3)]),
+}
+
+
+def _mixed_box(pde):
+    return (-1.0, 1.0) if pde == "advection" else (0.0, 10.0)
+
+
+def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
+    """The repo's own mixed-order set-up of a case with the orders p_vol (the reference's, after its adaptation):
+    a straight periodic QUAD mesh, the case's state at every volume's solution nodes, dt from the CFL estimate.
+
+    face_vol / face_lf: the reference's face list after adaptation. It keeps the structured mesh's faces in the same
+    order, but the faces it rebuilt around adapted volumes may list their two sides the other way round; the mesh
+    takes those sides (checked to be the same two volumes and local faces)."""
+    from dpgsolver_gb300.host import mixed as M
+    from dpgsolver_gb300.host.mesh import StructuredMesh
+    from dpgsolver_gb300.host import problem as P
+    pde, n, p, p_max, flux, steps, _ = MIXED_CASES[name]
+    lo, hi = _mixed_box(pde)
+    mesh = StructuredMesh(2, n, lo, hi)
+    if face_vol is not None:
+        fv, fl = np.asarray(face_vol), np.asarray(face_lf)
+        same = np.all(fv == mesh.face_vol, axis=1) & np.all(fl == mesh.face_lf, axis=1)
+        swap = np.all(fv == mesh.face_vol[:, ::-1], axis=1) & np.all(fl == mesh.face_lf[:, ::-1], axis=1)
+        if fv.shape != mesh.face_vol.shape or not np.all(same | swap):
+            raise AssertionError("face lists differ")
+        mesh.face_vol = fv.astype(mesh.face_vol.dtype)
+        mesh.face_lf = fl.astype(mesh.face_lf.dtype)
+    if pde == "advection":
+        prob = M.MixedTPProblem(name, 2, P.PDE_ADVECTION, flux, False, np.array([1.0, 0.5, 0.0]), mesh, p_vol)
+        fn = _advection_state
+    else:
+        prob = M.MixedTPProblem(name, 2, P.PDE_EULER, flux, True, np.zeros(3), mesh, p_vol)
+        fn = _vortex_state
+    for g in range(len(prob.groups)):
+        if len(prob.group_vols[g]):
+            x = prob.solution_node_xyz(g)
+            U = np.asarray(fn(x.reshape(-1, 2))).reshape(x.shape[0], x.shape[1], -1)
+            prob.set_group(prob.sol, g, np.transpose(U, (0, 2, 1)))
+    prob.dt = prob.stable_dt()
+    return prob
+
+
+def run_mixed(name: str) -> dict:
+    """Run a mixed-order case through the reference: its adaptation decides every volume's order; the host problem
+    with those orders gives the state formula's values and dt. Returns the flat arrays of the fixture."""
+    pde, n, p, p_max, flux, steps, adapt = MIXED_CASES[name]
+    lo, hi = _mixed_box(pde)
+    fn = _advection_state if pde == "advection" else _vortex_state
+    out0 = run_case(name, pde, n, p, lo, hi, flux, adapt_p=adapt, p_max=p_max)
+    p_vol = out0["volumes"][:, 2].astype(np.int32)
+    prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
+    out = run_case(name, pde, n, p, lo, hi, flux, state_fn=lambda x: np.asarray(fn(x)).reshape(len(x), -1),
+                   steps=steps, dt=prob.dt, adapt_p=adapt, p_max=p_max)
+    case_dir = os.path.join(RUN_DIR, name)
+    raw = lambda f: _read_bin(os.path.join(case_dir, f))   # noqa: E731
+    mx = np.loadtxt(os.path.join(case_dir, "max_rhs.txt"), ndmin=1)
+    return dict(p_vol=p_vol, n=np.int64(n), num_flux=np.int64(flux), steps=np.int64(steps), dt=np.float64(prob.dt),
+                face_vol=out["faces"][:, [4, 7]].astype(np.int32), face_lf=out["faces"][:, [5, 8]].astype(np.int32),
+                face_ord=out["faces"][:, [6, 9]].astype(np.int32), n_fc=out["faces"][:, 3].astype(np.int32),
+                xyz_vs=np.concatenate([x.ravel() for x in out["xyz_vs"]]),
+                metrics_vc=raw("metrics_vc.bin"), jacobian_det_vc=raw("jacobian_det_vc.bin"),
+                normals_fc=raw("normals_fc.bin"), jacobian_det_fc=raw("jacobian_det_fc.bin"),
+                sol_in=out["sol_in"], rhs=out["rhs"], max_rhs=np.float64(mx[0]),
+                sol_steps=out["sol_steps"], max_rhs_steps=mx[1:])
+
+
+def with_reference_mixed_inputs(prob, ref: dict):
+    """The mixed-order host problem given the reference's geometry and initial state (flat layouts), after checking
+    that both list the same volumes (orders and solution nodes) and faces in the same order."""
+    if not np.array_equal(prob.p_vol, ref["p_vol"]):
+        raise AssertionError("orders differ")
+    xyz = np.concatenate([prob.solution_node_xyz(g)[k].ravel()
+                          for v in range(prob.n_volumes)
+                          for g in [prob.vol_group[v]]
+                          for k in [int(np.nonzero(prob.group_vols[g] == v)[0][0])]])
+    if np.abs(xyz - ref["xyz_vs"]).max() > 1e-12:
+        raise AssertionError("volume lists differ")
+    interior = ref["face_vol"][:, 1] >= 0
+    if not (np.array_equal(prob.mesh.face_vol, ref["face_vol"]) and np.array_equal(prob.mesh.face_lf, ref["face_lf"])
+            and not np.any(ref["face_ord"][interior]) and np.array_equal(np.diff(prob.face_off), ref["n_fc"])):
+        raise AssertionError("face lists differ")
+    flat = prob.flat
+    prob.sol = np.array(ref["sol_in"], dtype=np.float64)
+
+    def ref_flat():
+        fl = flat()
+        fl.update(metrics_vc=np.array(ref["metrics_vc"]), jacobian_det_vc=np.array(ref["jacobian_det_vc"]),
+                  normals_fc=np.array(ref["normals_fc"]), jacobian_det_fc=np.array(ref["jacobian_det_fc"]),
+                  sol=prob.sol)
+        return fl
+    prob.flat = ref_flat
     return prob

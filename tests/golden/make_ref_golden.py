@@ -9,7 +9,9 @@ oracle.reference.CASES but the full-size "c2" through it (oracle.reference.run_n
 tests/golden/reference_<case>.npz: the reference's geometry as its Solver_Volume / Solver_Face lists hold it
 (metrics_vc, jacobian_det_vc, normals_fc, jacobian_det_fc), its volume and face lists (solution-node coordinates,
 volumes / local faces / node orders per face side), the initial state, the residual and max|rhs| of compute_rhs,
-and the state and max|rhs| after the case's SSP-RK3 steps. Case names after the path limit it to those cases.
+and the state and max|rhs| after the case's SSP-RK3 steps. The mixed-order cases (oracle.reference.MIXED_CASES) go
+through the reference's own p-adaptation first; their fixtures add every volume's order (p_vol). Case names after
+the path limit it to those cases.
 """
 from __future__ import annotations
 
@@ -31,9 +33,16 @@ def main(ref_dir: str, names=()) -> None:
         arrays = R.to_arrays(R.run_named(name))
         arrays.update(n=np.int64(n), p=np.int64(p), num_flux=np.int64(flux), steps=np.int64(steps),
                       dt=np.float64(R.host_problem(name).dt))
-        path = os.path.join(HERE, f"reference_{name}.npz")
-        np.savez_compressed(path, **arrays)
-        print(f"{path}: {os.path.getsize(path)} bytes")
+        _save(name, arrays)
+    for name in R.MIXED_CASES:
+        if not names or name in names:
+            _save(name, R.run_mixed(name))
+
+
+def _save(name, arrays) -> None:
+    path = os.path.join(HERE, f"reference_{name}.npz")
+    np.savez_compressed(path, **arrays)
+    print(f"{path}: {os.path.getsize(path)} bytes")
 
 
 if __name__ == "__main__":

@@ -13,6 +13,8 @@ slip walls), the Euler supersonic vortex (Riemann faces, slip walls) and
 the Navier-Stokes Taylor-Couette case on the reference's
 parametric annulus (BR2, rotating and adiabatic or diabatic walls, 10 steps); the positivity limiter on the vortex
 with a near-vacuum dip (its RK states at 1e-10, the limiter's bar, with the oracle's correction count).
+The batched (mixed-order) context on periodic QUAD meshes whose orders the reference's own p-adaptation set (three
+orders, advection and the Euler vortex), in each of its launch forms.
 """
 import os
 
@@ -90,3 +92,23 @@ def test_host_buffer_step_matches_reference(gpu_lib, name):
     tol = _residual_tol(prob)
     assert _rel(r, ref["rhs"]) <= tol
     assert abs(mx - float(ref["max_rhs"])) <= tol * float(ref["max_rhs"])
+
+
+@pytest.mark.parametrize("name", sorted(R.MIXED_CASES))
+@pytest.mark.parametrize("form", ["plain", "fused", "branches"])
+def test_batched_path_matches_reference_on_adapted_orders(gpu_lib, name, form):
+    """The batched (mixed-order) context given the reference's volume and face lists after its own p-adaptation
+    (three orders; faces at max(p_L, p_R), some listing their sides the other way round), its geometry and state."""
+    from dpgsolver_gb300.solver import BatchSimulation
+    ref = _fixture(name)
+    prob = R.with_reference_mixed_inputs(R.host_mixed_problem(name, ref["p_vol"], ref["face_vol"], ref["face_lf"]),
+                                         ref)
+    tol = _residual_tol(prob)
+    with BatchSimulation(prob) as sim:
+        sim.form = form
+        mx = sim.compute_rhs()
+        assert _rel(sim.rhs, ref["rhs"]) <= tol
+        assert abs(mx - float(ref["max_rhs"])) <= tol * float(ref["max_rhs"])
+        mx = sim.ssp_rk3_steps(float(ref["dt"]), int(ref["steps"]))
+        assert _rel(sim.sol_coef, ref["sol_steps"]) <= TOL
+        assert abs(mx - float(ref["max_rhs_steps"][-1])) <= 1e-10 * float(ref["max_rhs_steps"][-1])

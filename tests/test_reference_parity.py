@@ -10,6 +10,8 @@ time_step_ssp_rk_33, compiled from its sources into oracle/_ref).
   parametric annulus (BR2, rotating inner wall, adiabatic or diabatic outer wall). The oracle, given the reference's
   geometry and state, must reproduce them to 1e-12 (the residual to max(1e-12, twice its one-ulp noise floor)); the
   repo's own geometry must reproduce the reference's to 1e-13.
+* Mixed orders: periodic QUAD meshes after the reference's own adapt_hp raised the volumes around given vertices
+  (three orders per mesh, advection and the Euler vortex); oracle and host set-up as above.
 * Where oracle/_ref is built (the reference tree is present), the full-size vortex (QUAD 64^2, p = 3, Roe) is run
   live: residual, ten RK steps and geometry.
 """
@@ -148,3 +150,43 @@ def test_live_c2_host_geometry_at_stated_size(c2_live):
     assert np.max(np.abs(prob.solution_node_xyz() - ref["xyz_vs"])) <= 1e-13 * np.max(np.abs(ref["xyz_vs"]))
     for key in ("metrics_vc", "jacobian_det_vc", "normals_fc", "jacobian_det_fc"):
         assert _rel(getattr(g, key), ref[key]) <= 1e-12, key
+
+
+# ---- mixed orders: the reference's own p-adaptation decides every volume's order ---------------------------------
+
+def _mixed(name):
+    ref = _fixture(name)
+    prob = R.host_mixed_problem(name, ref["p_vol"], ref["face_vol"], ref["face_lf"])
+    return ref, prob
+
+
+@pytest.mark.parametrize("name", sorted(R.MIXED_CASES))
+def test_oracle_matches_reference_on_adapted_orders(name):
+    """Residual and SSP-RK3 states of the periodic QUAD mesh after the reference's adapt_hp raised the volumes
+    around given vertices by one or two orders (faces at max(p_L, p_R), its ensure_1_irregular neighbours)."""
+    ref, prob = _mixed(name)
+    assert len(set(ref["p_vol"].tolist())) == 3
+    assert float(ref["dt"]) == prob.dt
+    prob = R.with_reference_mixed_inputs(prob, ref)
+    o = oracle.Oracle(prob)
+    r, mx = o.compute_rhs(prob.sol)
+    tol = _residual_tol(o, prob, r)
+    assert _rel(r, ref["rhs"]) <= tol
+    assert abs(mx - float(ref["max_rhs"])) <= tol * float(ref["max_rhs"])
+    s = prob.sol.copy()
+    for _ in range(int(ref["steps"])):
+        s, mx, _ = o.ssp_rk3_step(s, prob.dt)
+    assert _rel(s, ref["sol_steps"]) <= 1e-12
+    assert abs(mx - float(ref["max_rhs_steps"][-1])) <= 1e-10 * float(ref["max_rhs_steps"][-1])
+
+
+@pytest.mark.parametrize("name", sorted(R.MIXED_CASES))
+def test_host_mixed_geometry_and_state_match_reference(name):
+    """The repo's mixed-order set-up (per-order solution nodes, metric terms, normals of faces whichever side the
+    reference lists first, Jacobians, initial state) is the reference's."""
+    ref, prob = _mixed(name)
+    fl = prob.flat()
+    for key in ("metrics_vc", "jacobian_det_vc", "normals_fc", "jacobian_det_fc"):
+        assert _rel(fl[key], ref[key]) <= 1e-13, key
+    assert _rel(prob.sol, ref["sol_in"]) <= 1e-13
+    R.with_reference_mixed_inputs(prob, ref)      # same volume list (orders and nodes) and face list
