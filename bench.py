@@ -706,6 +706,7 @@ def _batched_forms(torch, stream, args, sim, prob, n_steps, autotune=True):
     run("per_group_graph", "plain", True)
     run("fused_graph", "fused", True)
     run("branches_graph", "branches", True)
+    run("stage_graph", "stage", True)
     report, tuned_form = None, None
     if autotune:
         sim.upload_state(prob.sol)
@@ -790,6 +791,7 @@ def mixed_measurements(torch, stream, args, kind="types"):
         "forms": out,
         "speedup_fused_graph_vs_plain": out["fused_graph"]["value"] / out["plain_per_group"]["value"],
         "speedup_branches_graph_vs_plain": out["branches_graph"]["value"] / out["plain_per_group"]["value"],
+        "speedup_stage_graph_vs_plain": out["stage_graph"]["value"] / out["plain_per_group"]["value"],
         "speedup_best_vs_plain": out[best]["value"] / out["plain_per_group"]["value"],
         "autotune": {"form": tuned_form, "report": report},
         "fp64_pipe": {"flops_per_stage": flops, "achieved_tflops": flops / stage_s / 1e12,
@@ -848,7 +850,7 @@ def mixed_only_rk(torch, stream, args):
     prob = make_mixed(kind, args.types_n if kind == "types" else args.mixed_n)
     sim = BatchSimulation(prob, stream=stream.cuda_stream)
     sim.form = {"plain": "plain", "per_group_graph": "plain", "fused": "fused",
-                "branches": "branches"}[args.mixed_form]
+                "branches": "branches", "stage": "stage"}[args.mixed_form]
     sim.set_graphs(args.mixed_form != "plain")
     sim.ssp_rk3_steps(prob.dt, max(args.warmup, 3), want_max=False)
     ms = _timed(torch, stream, lambda: sim.ssp_rk3_steps(prob.dt, 1, want_max=False), args.steps)
@@ -1116,7 +1118,7 @@ def main():
     ap.add_argument("--mixed-n", type=int, default=58, help="volumes per direction of the mixed-order HEX mesh")
     ap.add_argument("--types-n", type=int, default=50, help="cells per direction of the mixed-type mesh (even)")
     ap.add_argument("--tri-n", type=int, default=384, help="cells per direction of the 2D QUAD/TRI mesh")
-    ap.add_argument("--mixed-form", choices=["plain", "per_group_graph", "fused", "branches"], default="fused",
+    ap.add_argument("--mixed-form", choices=["plain", "per_group_graph", "fused", "branches", "stage"], default="fused",
                     help="form of the mixed-order stages for --workload mixed3d --only-rk")
     args = ap.parse_args()
 

@@ -70,22 +70,28 @@ struct dgpu_batch {
 	unsigned long long* n_corr = nullptr;
 	long long qnode[kQMax + 2] = {0};      // face nodes of order q_f: [qnode[q_f], qnode[q_f + 1])
 	BTile* d_tiles = nullptr;
-	int n_tiles = 0, fused_blocks_vol = 0, fused_blocks_lift = 0, fused_blocks_face = 0;
+	int n_tiles = 0, fused_blocks_vol = 0, fused_blocks_lift = 0, fused_blocks_lift_nomax = 0, fused_blocks_face = 0;
 	size_t fused_vol_smem = 0, fused_lift_smem = 0;
 	cudaError_t (*fused_vol)(dgpu_batch*, bool gll_in) = nullptr;
 	cudaError_t (*fused_lift)(dgpu_batch*, int mode, double dt, int stage, int want_max) = nullptr;
+	// form 3: the stage kernel's grid per mode (residual, RK stage with max |rhs|, without), its barrier words
+	int stage_blocks[3] = {0, 0, 0};
+	unsigned* d_bar = nullptr;
+	cudaError_t (*stage_launch)(dgpu_batch*, bool rhs_mode, double dt, int stage, int want_max) = nullptr;
 	cudaError_t (*face_nodes)(dgpu_batch*, long long lo, long long hi, int blocks) = nullptr;
 	// execution
 	cudaStream_t stream = nullptr;
 	bool own_stream = false;
 	bool coef_valid = true, gl_valid = false;
-	int mode = 0;   // 0: one launch per group and face order; 1: fused persistent launches; 2: as 0 on parallel branches
+	// 0: one launch per group and face order; 1: fused persistent launches; 2: as 0 on parallel branches;
+	// 3: the whole stage in one cooperative persistent launch
+	int mode = 0;
 	cudaStream_t aux[kBranches] = {nullptr};
 	cudaEvent_t ev_fork = nullptr, ev_join[kBranches] = {nullptr};
 	bool use_graphs = true;
-	cudaGraphExec_t graph[3][2] = {};   // [mode][want_max]
-	double graph_dt[3][2] = {};
-	long long graph_launches[3][2] = {};   // kernels per replay
+	cudaGraphExec_t graph[4][2] = {};   // [mode][want_max]
+	double graph_dt[4][2] = {};
+	long long graph_launches[4][2] = {};   // kernels per replay
 	long long launches = 0;
 	std::string err;
 
@@ -293,11 +299,72 @@ cudaError_t launch_fused_lift(dgpu_batch* c, int mode, double dt, int stage, int
 	if (mode == kModeRhs)
 		blift_fused_kernel<D, NV, kModeRhs><<<c->fused_blocks_lift, 256, c->fused_lift_smem, c->stream>>>(
 			c->params(), c->d_tiles, c->n_tiles, rk);
-	else
+	else if (want_max)
 		blift_fused_kernel<D, NV, kModeRkGl><<<c->fused_blocks_lift, 256, c->fused_lift_smem, c->stream>>>(
 			c->params(), c->d_tiles, c->n_tiles, rk);
+	else
+		blift_fused_kernel<D, NV, kModeRkGlNoMax><<<c->fused_blocks_lift_nomax, 256, c->fused_lift_smem,
+		                                            c->stream>>>(c->params(), c->d_tiles, c->n_tiles, rk);
 	c->launches++;
 	return cudaGetLastError();
+}
+
+// Form 3: the stage kernel, cooperatively (all CTAs resident: the grid barriers between its phases complete).
+template <int D, int NV, int PDE, int FLUX>
+cudaError_t launch_stage(dgpu_batch* c, bool rhs_mode, double dt, int stage, int want_max)
+{
+	cudaError_t e = cudaMemsetAsync(c->d_bar, 0, 2 * sizeof(unsigned), c->stream);
+	if (e != cudaSuccess)
+		return e;
+	BParams P = c->params();
+	RkArgs rk = rk_args(c, dt, stage, want_max);
+	const BTile* tiles = c->d_tiles;
+	int n_tiles = c->n_tiles;
+	const double* u = rhs_mode ? c->u : c->ug;
+	const int* node_face = c->d_node_face;
+	long long n_nodes = c->qnode[kQMax + 1];
+	unsigned* bar = c->d_bar;
+	void* args[] = {&P, &tiles, &n_tiles, &u, &node_face, &n_nodes, &rk, &bar};
+	const void* k;
+	int blocks;
+	if (rhs_mode) {
+		k = (const void*)bstage_kernel<D, NV, PDE, FLUX, kModeRhs, true>;
+		blocks = c->stage_blocks[0];
+	} else if (want_max) {
+		k = (const void*)bstage_kernel<D, NV, PDE, FLUX, kModeRkGl, false>;
+		blocks = c->stage_blocks[1];
+	} else {
+		k = (const void*)bstage_kernel<D, NV, PDE, FLUX, kModeRkGlNoMax, false>;
+		blocks = c->stage_blocks[2];
+	}
+	if (blocks < 1)
+		return cudaErrorCooperativeLaunchTooLarge;
+	e = cudaLaunchCooperativeKernel(k, dim3(blocks), dim3(256), args,
+	                                std::max(c->fused_vol_smem, c->fused_lift_smem), c->stream);
+	c->launches++;
+	return e;
+}
+
+// The stage kernel's attributes and its grid: every SM times the CTAs that fit on one (the cooperative limit).
+template <int D, int NV, int PDE, int FLUX>
+cudaError_t bind_stage(dgpu_batch* c, int sms)
+{
+	const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+	const size_t smem = std::max(c->fused_vol_smem, c->fused_lift_smem);
+	const void* ks[3] = {(const void*)bstage_kernel<D, NV, PDE, FLUX, kModeRhs, true>,
+	                     (const void*)bstage_kernel<D, NV, PDE, FLUX, kModeRkGl, false>,
+	                     (const void*)bstage_kernel<D, NV, PDE, FLUX, kModeRkGlNoMax, false>};
+	for (int m = 0; m < 3; ++m) {
+		cudaError_t e = cudaFuncSetAttribute(ks[m], A, (int)smem);
+		if (e != cudaSuccess)
+			return e;
+		int per_sm = 0;
+		if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ks[m], 256, smem)) != cudaSuccess)
+			return e;
+		c->stage_blocks[m] = sms * per_sm;
+	}
+	c->stage_launch = launch_stage<D, NV, PDE, FLUX>;
+	return cudaSuccess;
 }
 
 template <int D, int Q, int NV, int PDE>
@@ -379,6 +446,8 @@ cudaError_t bind_all(dgpu_batch* c)
 		return e;
 	if ((e = cudaFuncSetAttribute(blift_fused_kernel<D, NV, kModeRkGl>, A, (int)c->fused_lift_smem)))
 		return e;
+	if ((e = cudaFuncSetAttribute(blift_fused_kernel<D, NV, kModeRkGlNoMax>, A, (int)c->fused_lift_smem)))
+		return e;
 	// persistent grids: as many CTAs as fit on the device at once
 	int dev = 0, sms = 0, per_sm = 0;
 	cudaGetDevice(&dev);
@@ -387,8 +456,13 @@ cudaError_t bind_all(dgpu_batch* c)
 	c->fused_blocks_vol = std::max(1, std::min(c->n_tiles, sms * std::max(1, per_sm)));
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blift_fused_kernel<D, NV, kModeRkGl>, 256, c->fused_lift_smem);
 	c->fused_blocks_lift = std::max(1, std::min(c->n_tiles, sms * std::max(1, per_sm)));
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, blift_fused_kernel<D, NV, kModeRkGlNoMax>, 256,
+	                                              c->fused_lift_smem);
+	c->fused_blocks_lift_nomax = std::max(1, std::min(c->n_tiles, sms * std::max(1, per_sm)));
 	c->fused_blocks_face = (int)std::max<long long>(1, std::min<long long>((c->qnode[kQMax + 1] + 255) / 256,
 	                                                                       (long long)sms * 8));
+	if ((e = bind_stage<D, NV, PDE, FLUX>(c, sms)) != cudaSuccess)
+		return e;
 	return cudaGetLastError();
 }
 
@@ -418,7 +492,7 @@ void free_batch(dgpu_batch* c)
 {
 	drop_graphs(c);
 	void* ptrs[] = {c->d_nc, c->d_nc_inv, c->d_ops, c->d_groups, c->d_dgroups, c->d_elf, c->d_fbase, c->d_node_face, c->gmet, c->inv_wJ,
-	                c->fgeo, c->u, c->ug, c->u0, c->rhs, c->vol_gl, c->traces, c->nnf, c->max_bits, c->err_flag,
+	                c->fgeo, c->u, c->ug, c->u0, c->rhs, c->vol_gl, c->traces, c->nnf, c->max_bits, c->err_flag, c->d_bar,
 	                c->n_corr, c->d_tiles, c->d_fbc, c->d_fext};
 	for (void* p : ptrs)
 		if (p)
@@ -476,7 +550,9 @@ dgpu_status on_branches(dgpu_batch* c, int n_items, F launch)
 dgpu_status enqueue_stage(dgpu_batch* c, bool rhs_mode, double dt, int stage, int want_max)
 {
 	const int lmode = rhs_mode ? kModeRhs : kModeRkGl;
-	if (c->mode == 1) {
+	if (c->mode == 3) {
+		BATCH_CUDA(c, c->stage_launch(c, rhs_mode, dt, stage, want_max));
+	} else if (c->mode == 1) {
 		BATCH_CUDA(c, c->fused_vol(c, rhs_mode));
 		BATCH_CUDA(c, c->face_nodes(c, 0, c->qnode[kQMax + 1], c->fused_blocks_face));
 		BATCH_CUDA(c, c->fused_lift(c, lmode, dt, stage, want_max));
@@ -1045,6 +1121,8 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	B_TRY(cudaMalloc((void**)&c->nnf, (size_t)nv * fb * sizeof(double)));
 	B_TRY(cudaMalloc((void**)&c->max_bits, sizeof(unsigned long long)));
 	B_TRY(cudaMalloc((void**)&c->err_flag, sizeof(int)));
+	B_TRY(cudaMalloc((void**)&c->d_bar, 2 * sizeof(unsigned)));
+	B_TRY(cudaMemset(c->d_bar, 0, 2 * sizeof(unsigned)));
 	B_TRY(cudaMalloc((void**)&c->n_corr, sizeof(unsigned long long)));
 	B_TRY(cudaMemset(c->u, 0, ns * sizeof(double)));
 	B_TRY(cudaMemset(c->traces, 0, (size_t)2 * nv * fb * sizeof(double)));
@@ -1288,6 +1366,22 @@ dgpu_status dgpu_batch_download_rhs(dgpu_batch* c, double* rhs)
 	return download_perm(c, c->rhs, rhs);
 }
 
+// The device error flag: 1 when the positivity limiter met a negative average, kErrBarrier when a grid barrier of
+// the stage kernel (form 3) gave up waiting.
+static dgpu_status check_flag(dgpu_batch* c)
+{
+	if (!c->positivity && c->mode != 3)
+		return DGPU_OK;
+	int flag = 0;
+	BATCH_CUDA(c, cudaMemcpyAsync(&flag, c->err_flag, sizeof flag, cudaMemcpyDeviceToHost, c->stream));
+	BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
+	if (flag == kErrBarrier)
+		return bfail(c, DGPU_ERR_CUDA, "stage kernel: a grid barrier timed out");
+	if (flag)
+		return bfail(c, DGPU_ERR_POSITIVITY, "average density or pressure below EPS_PHYS");
+	return DGPU_OK;
+}
+
 dgpu_status dgpu_batch_compute_rhs(dgpu_batch* c, double* max_rhs)
 {
 	if (!c)
@@ -1296,6 +1390,8 @@ dgpu_status dgpu_batch_compute_rhs(dgpu_batch* c, double* max_rhs)
 	if (st != DGPU_OK)
 		return st;
 	if ((st = enqueue_stage(c, true, 0.0, 0, 1)) != DGPU_OK)
+		return st;
+	if (c->mode == 3 && (st = check_flag(c)) != DGPU_OK)
 		return st;
 	return read_max(c, max_rhs);
 }
@@ -1344,19 +1440,14 @@ dgpu_status dgpu_batch_ssp_rk3_steps(dgpu_batch* c, double dt, int n_steps, doub
 	}
 	if (n_steps > 0)
 		c->coef_valid = false;
-	if (c->positivity) {
-		int flag = 0;
-		BATCH_CUDA(c, cudaMemcpyAsync(&flag, c->err_flag, sizeof flag, cudaMemcpyDeviceToHost, c->stream));
-		BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
-		if (flag)
-			return bfail(c, DGPU_ERR_POSITIVITY, "average density or pressure below EPS_PHYS");
-	}
+	if ((st = check_flag(c)) != DGPU_OK)
+		return st;
 	return read_max(c, max_rhs);
 }
 
 dgpu_status dgpu_batch_set_mode(dgpu_batch* c, int form)
 {
-	if (!c || form < 0 || form > 2)
+	if (!c || form < 0 || form > 3)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	c->mode = form;
 	return DGPU_OK;
@@ -1446,10 +1537,10 @@ dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report
 	}
 	drop_graphs(c);
 	// the three forms on RK steps (graph-replayed unless graphs are off)
-	static const char* names[3] = {"plain", "fused", "branches"};
-	float tmode[3] = {0.f, 0.f, 0.f};
+	static const char* names[4] = {"plain", "fused", "branches", "stage"};
+	float tmode[4] = {0.f, 0.f, 0.f, 0.f};
 	int best = 0;
-	for (int m = 0; m < 3; ++m) {
+	for (int m = 0; m < 4; ++m) {
 		c->mode = m;
 		if ((st = dgpu_batch_ssp_rk3_steps(c, dt, 1, nullptr)) != DGPU_OK)
 			break;

@@ -307,13 +307,17 @@ __device__ __forceinline__ void bface_node_rt(const BParams& P, int f, int i, in
 	double* out = P.nnf + NV * fb;
 	if constexpr (PDE == kEuler) {
 		double nF[NV];
-		if constexpr (FLUX == kRoePike)
+		if constexpr (FLUX == kRoePike) {
 			num_flux_roe_pike<D>(WL, WR, n, nF);
-		else
-			num_flux_lax_friedrichs<D>(WL, WR, n, nF);
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				nF[k] *= sc;
+		} else {
+			num_flux_lax_friedrichs<D>(WL, WR, n, nF, sc);
+		}
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			out[k * nff + i] = nF[k] * sc;
+			out[k * nff + i] = nF[k];
 	} else {
 		out[i] = num_flux_upwind<D>(WL[0], WR[0], n, P.b_adv) * sc;
 	}

@@ -576,6 +576,36 @@ __global__ void __launch_bounds__(256) dlift_group_kernel(const BParams P, int g
 
 // Fused persistent kernels: a CTA walks the tile list (grid-stride) and dispatches on the tile's group: a TP
 // group's order (its operator set is reloaded into shared memory when the group changes) or a dense group.
+// Each (group kind, q) body is called as a separate function (not inlined): the kernel then needs the registers
+// of its largest body, not those of all bodies inlined into one switch.
+template <int D, int Q, int NV, int PDE, bool GLL_IN>
+__device__ __noinline__ void bvol_tile(const BParams& P, const BatchOps* sops, const BGroup& G, int e0, int E,
+                                       const double* __restrict__ u, double* base)
+{
+	bvol_body<D, Q, NV, PDE, GLL_IN>(P, sops, G, e0, E, u, base);
+}
+
+template <int D, int NV, int PDE>
+__device__ __noinline__ void dvol_tile(const BParams& P, const DGroup& G, int e0, int E, const double* __restrict__ u,
+                                       double* base)
+{
+	dvol_body<D, NV, PDE>(P, G, e0, E, u, base);
+}
+
+template <int D, int Q, int NV, int MODE>
+__device__ __noinline__ void blift_tile(const BParams& P, const BatchOps* sops, const BGroup& G, int e0, int E,
+                                        const RkArgs& rk, double* base)
+{
+	blift_body<D, Q, NV, MODE>(P, sops, G, e0, E, rk, base);
+}
+
+template <int NV, int MODE>
+__device__ __noinline__ void dlift_tile(const BParams& P, const DGroup& G, int e0, int E, const RkArgs& rk,
+                                        double* base)
+{
+	dlift_body<NV, MODE>(P, G, e0, E, rk, base);
+}
+
 template <int D, int NV, int PDE, bool GLL_IN>
 __global__ void __launch_bounds__(256) bvol_fused_kernel(const BParams P, const BTile* tiles, int n_tiles,
                                                            const double* __restrict__ u)
@@ -590,7 +620,7 @@ __global__ void __launch_bounds__(256) bvol_fused_kernel(const BParams P, const 
 		const BTile tl = tiles[t];
 		if (tl.group >= P.n_groups) {
 			const DGroup G = P.dgroups[tl.group - P.n_groups];
-			dvol_body<D, NV, PDE>(P, G, tl.e0, G.E_fused, u, base);
+			dvol_tile<D, NV, PDE>(P, G, tl.e0, G.E_fused, u, base);
 			continue;
 		}
 		if (tl.group != cur) {
@@ -602,18 +632,22 @@ __global__ void __launch_bounds__(256) bvol_fused_kernel(const BParams P, const 
 		const BGroup G = P.groups[tl.group];
 		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
 		switch (G.q) {
-		case 2: bvol_body<D, 2, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
-		case 3: bvol_body<D, 3, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
-		case 4: bvol_body<D, 4, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
-		default: bvol_body<D, 5, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 2: bvol_tile<D, 2, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 3: bvol_tile<D, 3, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 4: bvol_tile<D, 4, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		default: bvol_tile<D, 5, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
 		}
 	}
 }
 
+// The RK stages that reduce no max |rhs| run the TP tiles without that path (as the per-group form does), capped at
+// 4 CTAs per SM; the dense tiles take the want_max flag at run time.
 template <int D, int NV, int MODE>
-__global__ void __launch_bounds__(256, 2) blift_fused_kernel(const BParams P, const BTile* tiles, int n_tiles,
-                                                               const RkArgs rk)
+__global__ void __launch_bounds__(256, BLiftOccupancy<MODE>::value) blift_fused_kernel(const BParams P,
+                                                                                     const BTile* tiles, int n_tiles,
+                                                                                     const RkArgs rk)
 {
+	constexpr int DMODE = (MODE == kModeRkGlNoMax) ? kModeRkGl : MODE;
 	extern __shared__ double smem[];
 	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
 	double* base = smem + sizeof(BatchOps) / 8;
@@ -622,7 +656,7 @@ __global__ void __launch_bounds__(256, 2) blift_fused_kernel(const BParams P, co
 		const BTile tl = tiles[t];
 		if (tl.group >= P.n_groups) {
 			const DGroup G = P.dgroups[tl.group - P.n_groups];
-			dlift_body<NV, MODE>(P, G, tl.e0, G.E_fused, rk, base);
+			dlift_tile<NV, DMODE>(P, G, tl.e0, G.E_fused, rk, base);
 			continue;
 		}
 		if (tl.group != cur) {
@@ -634,10 +668,129 @@ __global__ void __launch_bounds__(256, 2) blift_fused_kernel(const BParams P, co
 		const BGroup G = P.groups[tl.group];
 		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
 		switch (G.q) {
-		case 2: blift_body<D, 2, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
-		case 3: blift_body<D, 3, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
-		case 4: blift_body<D, 4, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
-		default: blift_body<D, 5, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 2: blift_tile<D, 2, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 3: blift_tile<D, 3, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 4: blift_tile<D, 4, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		default: blift_tile<D, 5, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Form 3: a whole stage in one cooperative persistent launch (volume tiles | face nodes | lift tiles)
+// ---------------------------------------------------------------------------------------------------------------
+// Barrier between the phases over every CTA of the grid. The launch is cooperative, so all CTAs are resident at
+// once and the barrier completes; each wait is still bounded (kBarrierLimitNs of the global timer): a CTA that
+// gives up sets *err = kErrBarrier and returns false, and the kernel then ends. bar[0] counts the arrivals of the
+// current barrier and bar[1] its generation; the host zeroes both before each launch.
+constexpr int kErrBarrier = 2;
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err)
+{
+	__shared__ int ok;
+	__syncthreads();   // the CTA's writes of this phase are issued
+	if (threadIdx.x == 0) {
+		ok = 1;
+		volatile unsigned* gen = bar + 1;
+		const unsigned g = *gen;   // cannot advance before this CTA arrives
+		__threadfence();           // this CTA's writes are visible before its arrival
+		if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+			atomicExch(bar, 0u);
+			__threadfence();
+			atomicAdd(bar + 1, 1u);
+		} else {
+			const unsigned long long t0 = global_ns();
+			while (*gen == g) {
+				if (global_ns() - t0 > kBarrierLimitNs) {
+					atomicExch(err, kErrBarrier);
+					ok = 0;
+					break;
+				}
+				__nanosleep(64);
+			}
+		}
+		__threadfence();
+	}
+	__syncthreads();
+	return ok != 0;
+}
+
+// The three phases of the fused form in one kernel: the volume tiles, every face node of the q_f-sorted list, the
+// lift tiles; grid barriers in between. One occupancy serves all three phases: the shared memory of the largest
+// tile (the q = 2 volume tile in 3D, 82 KB) already limits it to 2 CTAs per SM, so registers are capped there too
+// (a 64-register cap would only add spills).
+template <int D, int NV, int PDE, int FLUX, int MODE, bool GLL_IN>
+__global__ void __launch_bounds__(256, 2)
+bstage_kernel(const BParams P, const BTile* __restrict__ tiles, int n_tiles, const double* __restrict__ u,
+              const int* __restrict__ node_face, long long n_nodes, const RkArgs rk, unsigned* bar)
+{
+	constexpr int DMODE = (MODE == kModeRkGlNoMax) ? kModeRkGl : MODE;
+	extern __shared__ double smem[];
+	BatchOps* sops = reinterpret_cast<BatchOps*>(smem);
+	double* base = smem + sizeof(BatchOps) / 8;
+	if (blockIdx.x == 0 && threadIdx.x == 0 && P.max_bits)
+		*P.max_bits = 0ull;
+	int cur = -1;
+	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+		const BTile tl = tiles[t];
+		if (tl.group >= P.n_groups) {
+			const DGroup G = P.dgroups[tl.group - P.n_groups];
+			dvol_tile<D, NV, PDE>(P, G, tl.e0, G.E_fused, u, base);
+			continue;
+		}
+		if (tl.group != cur) {
+			__syncthreads();
+			load_batch_ops(sops, &P.ops[tl.group]);
+			cur = tl.group;
+			__syncthreads();
+		}
+		const BGroup G = P.groups[tl.group];
+		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
+		switch (G.q) {
+		case 2: bvol_tile<D, 2, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 3: bvol_tile<D, 3, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		case 4: bvol_tile<D, 4, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		default: bvol_tile<D, 5, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
+		}
+	}
+	if (!grid_barrier(bar, P.err_flag))
+		return;
+	for (long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x; gid < n_nodes;
+	     gid += (long long)gridDim.x * blockDim.x) {
+		const int f = node_face[gid];
+		const long long fb = P.fbase[f];
+		bface_node_rt<D, NV, PDE, FLUX>(P, f, (int)(gid - fb), (int)(P.fbase[f + 1] - fb));
+	}
+	if (!grid_barrier(bar, P.err_flag))
+		return;
+	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+		const BTile tl = tiles[t];
+		if (tl.group >= P.n_groups) {
+			const DGroup G = P.dgroups[tl.group - P.n_groups];
+			dlift_tile<NV, DMODE>(P, G, tl.e0, G.E_fused, rk, base);
+			continue;
+		}
+		if (tl.group != cur) {
+			__syncthreads();
+			load_batch_ops(sops, &P.ops[tl.group]);
+			cur = tl.group;
+			__syncthreads();
+		}
+		const BGroup G = P.groups[tl.group];
+		const int E = (int)(blockDim.x / (D == 2 ? G.q * G.q : G.q * G.q * G.q));
+		switch (G.q) {
+		case 2: blift_tile<D, 2, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 3: blift_tile<D, 3, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		case 4: blift_tile<D, 4, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
+		default: blift_tile<D, 5, NV, MODE>(P, sops, G, tl.e0, E, rk, base); break;
 		}
 	}
 }

@@ -45,29 +45,28 @@ __device__ __forceinline__ T max_abs_real(const T& a, const T& b)
 //   fr_j[eq] = sum_i g[j*D+i] f_i[eq]
 // with f the physical flux of compute_Flux_T_euler / compute_Flux_euler_0 (flux_euler_T.c:71-143, 259-298)
 // and g the metric terms (pre-multiplied by the cubature weight) of constructor_flux_ref_piece_T
-// (compute_rlhs_T.c:71-110). The contraction is regrouped through the contravariant velocity
-// U_j = sum_i g[j*D+i] u_i, which is the same sum with fewer FP64 operations.
+// (compute_rlhs_T.c:71-110). The contraction is regrouped through the contravariant momentum
+// M_j = sum_i g[j*D+i] m_i (the mass flux fr_j[0] itself) and velocity U_j = M_j / rho, and the pressure takes
+// rho |u|^2 as |m|^2 / rho: the same sums with fewer FP64 operations.
 template <int D, typename T = double>
 __device__ __forceinline__ void euler_flux_ref(const T* W, const double* g, T (*fr)[D + 2])
 {
 	const T rho = W[0], E = W[D + 1];
 	const T rho_inv = 1.0 / rho;
-	T u[D];
-	T V2 = 0.0;
+	T m2 = 0.0;
 #pragma unroll
-	for (int k = 0; k < D; ++k) {
-		u[k] = rho_inv * W[1 + k];
-		V2 += u[k] * u[k];
-	}
-	const T p = kGm1 * (E - 0.5 * rho * V2);
+	for (int k = 0; k < D; ++k)
+		m2 += W[1 + k] * W[1 + k];
+	const T p = kGm1 * (E - 0.5 * (m2 * rho_inv));
 	const T Ep = E + p;
 #pragma unroll
 	for (int j = 0; j < D; ++j) {
-		T U = 0.0;
+		T M = 0.0;
 #pragma unroll
 		for (int i = 0; i < D; ++i)
-			U += g[j * D + i] * u[i];
-		fr[j][0] = rho * U;
+			M += g[j * D + i] * W[1 + i];
+		const T U = M * rho_inv;
+		fr[j][0] = M;
 #pragma unroll
 		for (int m = 0; m < D; ++m)
 			fr[j][1 + m] = W[1 + m] * U + p * g[j * D + m];
@@ -75,42 +74,45 @@ __device__ __forceinline__ void euler_flux_ref(const T* W, const double* g, T (*
 	}
 }
 
-// One side of a face node: the normal physical flux n.f(W) (compute_Flux_euler_0 contracted with n) and the
-// Lax-Friedrichs wave speed |V| + c.
+// One side of a face node for Lax-Friedrichs: m.n, the normal velocity Vn = m.n / rho, the pressure and the wave
+// speed |V| + c, with rho |V|^2 formed as |m|^2 / rho (one reciprocal of the density, no velocity vector).
 template <int D, typename T>
-__device__ __forceinline__ T euler_normal_flux(const T* W, const double* n, T* Fn)
+__device__ __forceinline__ void euler_side_lf(const T* W, const double* n, T& mn, T& Vn, T& p, T& lam)
 {
-	const T rho = W[0], E = W[D + 1];
-	const T rho_inv = 1.0 / rho;
-	T V2 = 0.0, Vn = 0.0, mn = 0.0;
+	const T rho_inv = 1.0 / W[0];
+	T m2 = 0.0;
+	mn = 0.0;
 #pragma unroll
 	for (int k = 0; k < D; ++k) {
-		const T u = W[1 + k] * rho_inv;
-		V2 += u * u;
-		Vn += n[k] * u;
+		m2 += W[1 + k] * W[1 + k];
 		mn += n[k] * W[1 + k];
 	}
-	const T p = kGm1 * (E - 0.5 * rho * V2);
-	Fn[0] = mn;
-#pragma unroll
-	for (int k = 0; k < D; ++k)
-		Fn[1 + k] = W[1 + k] * Vn + p * n[k];
-	Fn[D + 1] = (E + p) * Vn;
-	return sqrt(V2) + sqrt(kGamma * p * rho_inv);
+	const T q = m2 * rho_inv;   // rho |V|^2
+	Vn = mn * rho_inv;
+	p = kGm1 * (W[D + 1] - 0.5 * q);
+	lam = sqrt(q * rho_inv) + sqrt(kGamma * p * rho_inv);
 }
 
 // Lax-Friedrichs (compute_Numerical_Flux_T_euler_lax_friedrichs, numerical_flux_euler_T.c:60-327):
-//   nF = 1/2 [ n.(F_L + F_R) + max(|V_L| + c_L, |V_R| + c_R) (W_L - W_R) ].
+//   nF = 1/2 [ n.(F_L + F_R) + max(|V_L| + c_L, |V_R| + c_R) (W_L - W_R) ] x scale
+// with n.F = (m.n, m Vn + p n, (E + p) Vn) of each side (compute_Flux_euler_0 contracted with n); the two sides'
+// pressure terms share one product with n. scale (the face node's w J, or 1) is folded into the factor 1/2, which
+// gives the same bits as scaling afterwards (the factor 1/2 is exact).
 template <int D, typename T = double>
-__device__ __forceinline__ void num_flux_lax_friedrichs(const T* WL, const T* WR, const double* n, T* nF)
+__device__ __forceinline__ void num_flux_lax_friedrichs(const T* WL, const T* WR, const double* n, T* nF,
+                                                        double scale = 1.0)
 {
-	T FL[D + 2], FR[D + 2];
-	const T maxlL = euler_normal_flux<D>(WL, n, FL);
-	const T maxlR = euler_normal_flux<D>(WR, n, FR);
-	const T maxV = (maxlL > maxlR ? maxlL : maxlR);
+	T mnL, VnL, pL, lamL, mnR, VnR, pR, lamR;
+	euler_side_lf<D>(WL, n, mnL, VnL, pL, lamL);
+	euler_side_lf<D>(WR, n, mnR, VnR, pR, lamR);
+	const T maxV = (lamL > lamR ? lamL : lamR);
+	const double h = 0.5 * scale;
+	const T pLR = pL + pR;
+	nF[0] = h * ((mnL + mnR) + maxV * (WL[0] - WR[0]));
 #pragma unroll
-	for (int eq = 0; eq < D + 2; ++eq)
-		nF[eq] = 0.5 * ((FL[eq] + FR[eq]) + maxV * (WL[eq] - WR[eq]));
+	for (int k = 0; k < D; ++k)
+		nF[1 + k] = h * ((WL[1 + k] * VnL + WR[1 + k] * VnR + pLR * n[k]) + maxV * (WL[1 + k] - WR[1 + k]));
+	nF[D + 1] = h * (((WL[D + 1] + pL) * VnL + (WR[D + 1] + pR) * VnR) + maxV * (WL[D + 1] - WR[D + 1]));
 }
 
 // Roe-Pike with the entropy fix of Qu et al. 2015 (compute_Numerical_Flux_T_euler_roe_pike,

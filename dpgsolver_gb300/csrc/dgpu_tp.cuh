@@ -361,13 +361,17 @@ tp_face_kernel(const TPParams P)
 	double* out = P.nnf + (size_t)f * NV * NF;
 	if constexpr (PDE == kEuler) {
 		double nF[NV];
-		if constexpr (FLUX == kRoePike)
+		if constexpr (FLUX == kRoePike) {
 			num_flux_roe_pike<D>(WL, WR, n, nF);
-		else
-			num_flux_lax_friedrichs<D>(WL, WR, n, nF);
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				nF[k] *= sc;
+		} else {
+			num_flux_lax_friedrichs<D>(WL, WR, n, nF, sc);
+		}
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
-			out[k * NF + i] = nF[k] * sc;
+			out[k * NF + i] = nF[k];
 	} else {
 		out[i] = num_flux_upwind<D>(WL[0], WR[0], n, P.b_adv) * sc;
 	}

@@ -471,12 +471,13 @@ class BatchSimulation:
                                                        ctypes.byref(mx) if want_max else None))
         return mx.value if want_max else None
 
-    FORMS = {"plain": 0, "fused": 1, "branches": 2}
+    FORMS = {"plain": 0, "fused": 1, "branches": 2, "stage": 3}
 
     @property
     def form(self) -> str:
         """Launch form of the stages: "plain" (one launch per group / face order), "fused" (persistent launches
-        over all groups) or "branches" (the plain launches on parallel graph branches)."""
+        over all groups), "branches" (the plain launches on parallel graph branches) or "stage" (the whole stage
+        in one cooperative persistent launch)."""
         v = ctypes.c_int()
         self._check(self._lib.dgpu_batch_get_mode(self._h, ctypes.byref(v)))
         return {v: k for k, v in self.FORMS.items()}[v.value]

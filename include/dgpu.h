@@ -362,9 +362,11 @@ const char* dgpu_status_string(dgpu_status st);
  *
  * The state is the volumes' (n_vs(v) x n_var) column-major sol_coef blocks concatenated in volume-list order.
  * On the device the volumes are stored group by group; uploads and downloads permute. Each RK stage runs in one
- * of three forms: one launch per group for the volume and lift kernels and one per face order for the face kernel,
- * in sequence (form 0); one persistent launch each over a tile list that covers every group (form 1); or the
- * launches of form 0 on parallel branches, so that the groups' kernels run concurrently (form 2). A step is
+ * of four forms: one launch per group for the volume and lift kernels and one per face order for the face kernel,
+ * in sequence (form 0); one persistent launch each over a tile list that covers every group (form 1); the
+ * launches of form 0 on parallel branches, so that the groups' kernels run concurrently (form 2); or the whole
+ * stage as one cooperative persistent launch, its volume, face and lift phases separated by grid barriers
+ * (form 3; a barrier that waits more than 2 s gives up and the call returns DGPU_ERR_CUDA). A step is
  * replayed from a captured CUDA graph in every form. No reference counterpart for the forms, the tile size or the
  * autotuner. */
 typedef struct dgpu_batch dgpu_batch;
@@ -436,7 +438,7 @@ dgpu_status dgpu_batch_compute_rhs(dgpu_batch* b, double* max_rhs);
 /* n_steps SSP-RK3 steps (positivity included), graph-replayed. */
 dgpu_status dgpu_batch_ssp_rk3_steps(dgpu_batch* b, double dt, int n_steps, double* max_rhs);
 /* Form of the stages: 0 = one launch per group / face order in sequence, 1 = fused persistent launches,
- * 2 = the launches of form 0 on parallel branches. */
+ * 2 = the launches of form 0 on parallel branches, 3 = one cooperative persistent launch per stage. */
 dgpu_status dgpu_batch_set_mode(dgpu_batch* b, int form);
 dgpu_status dgpu_batch_get_mode(const dgpu_batch* b, int* form);
 /* 1 (default): RK steps replay a captured CUDA graph; 0: every kernel is launched from the host each step. */
@@ -444,7 +446,7 @@ dgpu_status dgpu_batch_set_graphs(dgpu_batch* b, int enable);
 /* Elements per CTA of group g in form 0 (1 .. 256 / q^d). */
 dgpu_status dgpu_batch_set_group_tile(dgpu_batch* b, int group, int elements_per_cta);
 /* Times every group's volume + lift kernels for each elements-per-CTA candidate (256/q^d, halved down to 1)
- * and keeps the fastest, then times `reps` RK steps of size dt in each of the three forms and keeps the
+ * and keeps the fastest, then times `reps` RK steps of size dt in each of the four forms and keeps the
  * fastest. The device state is restored afterwards. A text report of the timings goes to `report`
  * (may be NULL). */
 dgpu_status dgpu_batch_autotune(dgpu_batch* b, double dt, int reps, char* report, size_t report_len);

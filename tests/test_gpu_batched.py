@@ -40,7 +40,7 @@ CASES = {
 }
 
 
-FORMS = ["plain", "fused", "branches"]
+FORMS = ["plain", "fused", "branches", "stage"]
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
@@ -156,8 +156,8 @@ def test_forms_and_tiles_agree_bitwise(gpu_lib):
     prob = CASES["hex_roe_mixed_10"]()
     out = []
     with BatchSimulation(prob) as sim:
-        for form, tiles in [("plain", None), ("fused", None), ("branches", None), ("plain", [1, 3, 2, 1]),
-                            ("branches", [4, 9, 1, 2])]:
+        for form, tiles in [("plain", None), ("fused", None), ("branches", None), ("stage", None),
+                            ("plain", [1, 3, 2, 1]), ("branches", [4, 9, 1, 2])]:
             sim.form = form
             if tiles:
                 for g, e in enumerate(tiles):
@@ -208,7 +208,7 @@ def test_autotune_keeps_state_and_results(gpu_lib):
         sim.compute_rhs()
         r0 = sim.rhs
         rep = sim.autotune(prob.dt, reps=2)
-        assert "plain" in rep and "fused" in rep and "branches" in rep and "E=" in rep
+        assert "plain" in rep and "fused" in rep and "branches" in rep and "stage" in rep and "E=" in rep
         assert np.array_equal(sim.sol_coef, prob.sol)
         sim.compute_rhs()
         assert np.array_equal(sim.rhs, r0)
@@ -311,7 +311,8 @@ def test_mixed_types_forms_and_tiles_agree_bitwise(gpu_lib):
     prob = TYPE_CASES["types_roe_6"]()
     out = []
     with BatchSimulation(prob) as sim:
-        for form, halve in [("plain", False), ("fused", False), ("branches", False), ("plain", True)]:
+        for form, halve in [("plain", False), ("fused", False), ("branches", False), ("stage", False),
+                            ("plain", True)]:
             sim.form = form
             if halve:
                 for g in range(len(prob.groups)):

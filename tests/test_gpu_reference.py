@@ -14,7 +14,7 @@ the Navier-Stokes Taylor-Couette case on the reference's
 parametric annulus (BR2, rotating and adiabatic or diabatic walls, 10 steps); the positivity limiter on the vortex
 with a near-vacuum dip (its RK states at 1e-10, the limiter's bar, with the oracle's correction count).
 The batched (mixed-order) context on periodic QUAD meshes whose orders the reference's own p-adaptation set (three
-orders, advection and the Euler vortex), in each of its launch forms.
+orders, advection and the Euler vortex), in each of its four launch forms.
 """
 import os
 
@@ -95,7 +95,7 @@ def test_host_buffer_step_matches_reference(gpu_lib, name):
 
 
 @pytest.mark.parametrize("name", sorted(R.MIXED_CASES))
-@pytest.mark.parametrize("form", ["plain", "fused", "branches"])
+@pytest.mark.parametrize("form", ["plain", "fused", "branches", "stage"])
 def test_batched_path_matches_reference_on_adapted_orders(gpu_lib, name, form):
     """The batched (mixed-order) context given the reference's volume and face lists after its own p-adaptation
     (three orders; faces at max(p_L, p_R), some listing their sides the other way round), its geometry and state."""

@@ -37,7 +37,7 @@ def test_mixed_types_at_stated_size_match_oracle(gpu_lib):
     tol = max(1e-12, 2.0 * floor)
     s_ref, _, nc_ref = o.ssp_rk3_step(prob.sol, prob.dt)
     with BatchSimulation(prob) as sim:
-        for form in ("fused", "branches"):
+        for form in ("fused", "branches", "stage"):
             sim.form = form
             sim.upload_state(prob.sol)
             mx = sim.compute_rhs()
