@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/dgpu.h"
+#include "dgpu_batched_ns.cuh"
 #include "dgpu_dense.cuh"
 #include "dgpu_host_ops.h"
 
@@ -30,6 +31,9 @@ struct GroupLaunch {
 	cudaError_t (*vol)(dgpu_batch*, int g, bool gll_in) = nullptr;
 	cudaError_t (*lift)(dgpu_batch*, int g, int mode, double dt, int stage, int want_max) = nullptr;
 	cudaError_t (*conv)(dgpu_batch*, int g, bool to_gl) = nullptr;
+	// Navier-Stokes: the gradient and the volume kernels of the group (TP groups only)
+	cudaError_t (*ns_grad)(dgpu_batch*, int g, bool gll_in) = nullptr;
+	cudaError_t (*ns_vol)(dgpu_batch*, int g, bool gll_in) = nullptr;
 	int E_max = 0;
 	bool dense = false;
 	int idx = 0;        // index among the TP or among the dense groups
@@ -62,6 +66,11 @@ struct dgpu_batch {
 	double *gmet = nullptr, *inv_wJ = nullptr, *fgeo = nullptr;
 	double *u = nullptr, *ug = nullptr, *u0 = nullptr, *rhs = nullptr, *vol_gl = nullptr;
 	double *traces = nullptr, *nnf = nullptr;
+	// Navier-Stokes (BR2): kept volume gradient, gradient traces, jumps and each side's own lifting at the faces
+	bool navier_stokes = false;
+	NsPhys ns_phys = {0.0, 1.0, 1.0, kViscosityConstant, 0.0};
+	double *ns_gv = nullptr, *ns_gtr = nullptr, *ns_dw = nullptr, *ns_y = nullptr;
+	cudaError_t (*ns_nodes)(dgpu_batch*, bool face) = nullptr;   // the jump (false) or face (true) kernel
 	int* d_fbc = nullptr;                  // boundary faces (null without any): code per internal face, -1 inside
 	double* d_fext = nullptr;              // their exterior state, [NV][NF_f] at NV fbase[f]
 	BcData bc_data = {0.0, 0.0, 0.0, 0.0};
@@ -120,6 +129,14 @@ struct dgpu_batch {
 		P.fbc = d_fbc;
 		P.fext = d_fext;
 		P.bc_data = bc_data;
+		if (navier_stokes) {
+			P.ns_gv = ns_gv;
+			P.ns_gtr = ns_gtr;
+			P.ns_dw = ns_dw;
+			P.ns_y = ns_y;
+			P.ns = ns_phys;
+			P.ns_eta = 1.01 * 2 * d;   // PENALTY_SCALING * NFMAX (compute_face_rlhs_dg_T.c:273-295)
+		}
 		return P;
 	}
 	int group_n_vol(int g) const { return gl[g].dense ? hdgroups[gl[g].idx].n_vol : hgroups[gl[g].idx].n_vol; }
@@ -466,8 +483,119 @@ cudaError_t bind_all(dgpu_batch* c)
 	return cudaGetLastError();
 }
 
+// ---- Navier-Stokes (dgpu_batched_ns.cuh) ----
+template <int D, int Q, int NV>
+size_t bns_smem(int E)
+{
+	return sizeof(BatchOps) + (size_t)E * BnsSmem<D, Q, NV>::MAX * sizeof(double);
+}
+
+template <int D, int Q, int NV>
+cudaError_t launch_bns(dgpu_batch* c, int g, bool gll_in, bool volume)
+{
+	const int t = c->gl[g].idx;
+	const BGroup& G = c->hgroups[t];
+	if (G.n_vol == 0)
+		return cudaSuccess;
+	const int blocks = (G.n_vol + G.E_ns - 1) / G.E_ns, thr = threads_for(G.E_ns, TPShape<D, Q>::N);
+	const size_t sm = bns_smem<D, Q, NV>(G.E_ns);
+	const double* u = gll_in ? c->u : c->ug;
+	if (volume) {
+		if (gll_in)
+			bns_volume_group_kernel<D, Q, NV, true><<<blocks, thr, sm, c->stream>>>(c->params(), t, u);
+		else
+			bns_volume_group_kernel<D, Q, NV, false><<<blocks, thr, sm, c->stream>>>(c->params(), t, u);
+	} else {
+		if (gll_in)
+			bns_grad_group_kernel<D, Q, NV, true><<<blocks, thr, sm, c->stream>>>(c->params(), t, u);
+		else
+			bns_grad_group_kernel<D, Q, NV, false><<<blocks, thr, sm, c->stream>>>(c->params(), t, u);
+	}
+	c->launches++;
+	return cudaGetLastError();
+}
+
+template <int D, int Q, int NV>
+cudaError_t launch_bns_grad(dgpu_batch* c, int g, bool gll_in) { return launch_bns<D, Q, NV>(c, g, gll_in, false); }
+template <int D, int Q, int NV>
+cudaError_t launch_bns_vol(dgpu_batch* c, int g, bool gll_in) { return launch_bns<D, Q, NV>(c, g, gll_in, true); }
+
+template <int D, int NV, int FLUX>
+cudaError_t launch_bns_nodes(dgpu_batch* c, bool face)
+{
+	const long long n = c->qnode[kQMax + 1];
+	if (n == 0)
+		return cudaSuccess;
+	if (face) {
+		const int blocks = (int)std::min<long long>((n + 127) / 128, 1ll << 30);
+		bns_face_kernel<D, NV, FLUX><<<blocks, 128, 0, c->stream>>>(c->params(), c->d_node_face, n);
+	} else {
+		const int blocks = (int)std::min<long long>((n + 255) / 256, 1ll << 30);
+		bns_jump_kernel<D, NV><<<blocks, 256, 0, c->stream>>>(c->params(), c->d_node_face, n);
+	}
+	c->launches++;
+	return cudaGetLastError();
+}
+
+// The Navier-Stokes launchers of every group: elements per CTA as for Euler, fewer where the gradient and volume
+// bodies' shared memory (state, D gradient or flux components, face values) would exceed 110 KB per CTA.
+template <int D, int Q, int NV>
+cudaError_t bind_ns_group(dgpu_batch* c, int g)
+{
+	GroupLaunch& L = c->gl[g];
+	L.ns_grad = launch_bns_grad<D, Q, NV>;
+	L.ns_vol = launch_bns_vol<D, Q, NV>;
+	constexpr int N = TPShape<D, Q>::N;
+	const int by_smem = (int)((110 * 1024 - sizeof(BatchOps)) / (BnsSmem<D, Q, NV>::MAX * sizeof(double)));
+	const int E = std::max(1, std::min(256 / N, by_smem));
+	c->hgroups[L.idx].E_ns = E;
+	const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+	const int sm = (int)bns_smem<D, Q, NV>(E);
+	cudaError_t e;
+	if ((e = cudaFuncSetAttribute(bns_grad_group_kernel<D, Q, NV, true>, A, sm)))
+		return e;
+	if ((e = cudaFuncSetAttribute(bns_grad_group_kernel<D, Q, NV, false>, A, sm)))
+		return e;
+	if ((e = cudaFuncSetAttribute(bns_volume_group_kernel<D, Q, NV, true>, A, sm)))
+		return e;
+	return cudaFuncSetAttribute(bns_volume_group_kernel<D, Q, NV, false>, A, sm);
+}
+
+template <int D, int FLUX>
+cudaError_t bind_ns(dgpu_batch* c)
+{
+	constexpr int NV = D + 2;
+	for (int g = 0; g < c->n_all; ++g) {
+		cudaError_t e;
+		switch (c->hgroups[c->gl[g].idx].q) {
+		case 2: e = bind_ns_group<D, 2, NV>(c, g); break;
+		case 3: e = bind_ns_group<D, 3, NV>(c, g); break;
+		case 4: e = bind_ns_group<D, 4, NV>(c, g); break;
+		default: e = bind_ns_group<D, 5, NV>(c, g); break;
+		}
+		if (e != cudaSuccess)
+			return e;
+	}
+	c->ns_nodes = launch_bns_nodes<D, NV, FLUX>;
+	return cudaSuccess;
+}
+
 cudaError_t bind(dgpu_batch* c)
 {
+	if (c->navier_stokes) {   // the lift and conversion kernels are the Euler ones
+		cudaError_t e;
+		if (c->d == 2)
+			e = c->flux == DGPU_NUM_FLUX_ROE_PIKE ? bind_all<2, 4, kEuler, kRoePike>(c)
+			                                      : bind_all<2, 4, kEuler, kLaxFriedrichs>(c);
+		else
+			e = c->flux == DGPU_NUM_FLUX_ROE_PIKE ? bind_all<3, 5, kEuler, kRoePike>(c)
+			                                      : bind_all<3, 5, kEuler, kLaxFriedrichs>(c);
+		if (e != cudaSuccess)
+			return e;
+		if (c->d == 2)
+			return c->flux == DGPU_NUM_FLUX_ROE_PIKE ? bind_ns<2, kRoePike>(c) : bind_ns<2, kLaxFriedrichs>(c);
+		return c->flux == DGPU_NUM_FLUX_ROE_PIKE ? bind_ns<3, kRoePike>(c) : bind_ns<3, kLaxFriedrichs>(c);
+	}
 	if (c->d == 2) {
 		if (c->pde == DGPU_PDE_ADVECTION) return bind_all<2, 1, kAdvection, kUpwind>(c);
 		if (c->flux == DGPU_NUM_FLUX_ROE_PIKE) return bind_all<2, 4, kEuler, kRoePike>(c);
@@ -493,7 +621,7 @@ void free_batch(dgpu_batch* c)
 	drop_graphs(c);
 	void* ptrs[] = {c->d_nc, c->d_nc_inv, c->d_ops, c->d_groups, c->d_dgroups, c->d_elf, c->d_fbase, c->d_node_face, c->gmet, c->inv_wJ,
 	                c->fgeo, c->u, c->ug, c->u0, c->rhs, c->vol_gl, c->traces, c->nnf, c->max_bits, c->err_flag, c->d_bar,
-	                c->n_corr, c->d_tiles, c->d_fbc, c->d_fext};
+	                c->n_corr, c->d_tiles, c->d_fbc, c->d_fext, c->ns_gv, c->ns_gtr, c->ns_dw, c->ns_y};
 	for (void* p : ptrs)
 		if (p)
 			cudaFree(p);
@@ -550,6 +678,23 @@ dgpu_status on_branches(dgpu_batch* c, int n_items, F launch)
 dgpu_status enqueue_stage(dgpu_batch* c, bool rhs_mode, double dt, int stage, int want_max)
 {
 	const int lmode = rhs_mode ? kModeRhs : kModeRkGl;
+	if (c->navier_stokes) {   // forms 0 and 2: gradient | jump | volume | face | lift
+		dgpu_status st;
+		auto phase = [&](auto launch) -> dgpu_status {
+			if (c->mode == 2)
+				return on_branches(c, c->n_all, launch);
+			for (int g = 0; g < c->n_all; ++g)
+				BATCH_CUDA(c, launch(g));
+			return DGPU_OK;
+		};
+		if ((st = phase([&](int g) { return c->gl[g].ns_grad(c, g, rhs_mode); })) != DGPU_OK)
+			return st;
+		BATCH_CUDA(c, c->ns_nodes(c, false));
+		if ((st = phase([&](int g) { return c->gl[g].ns_vol(c, g, rhs_mode); })) != DGPU_OK)
+			return st;
+		BATCH_CUDA(c, c->ns_nodes(c, true));
+		return phase([&](int g) { return c->gl[g].lift(c, g, lmode, dt, stage, want_max); });
+	}
 	if (c->mode == 3) {
 		BATCH_CUDA(c, c->stage_launch(c, rhs_mode, dt, stage, want_max));
 	} else if (c->mode == 1) {
@@ -651,11 +796,20 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	const int d = phys->d;
 	if (d != 2 && d != 3)
 		return bfail(nullptr, DGPU_ERR_UNSUPPORTED, "d must be 2 or 3");
+	const bool ns_pde = phys->pde == DGPU_PDE_NAVIER_STOKES;
 	if (phys->pde == DGPU_PDE_ADVECTION ? phys->num_flux != DGPU_NUM_FLUX_UPWIND
-	                                    : (phys->pde != DGPU_PDE_EULER ||
+	                                    : ((phys->pde != DGPU_PDE_EULER && !ns_pde) ||
 	                                       (phys->num_flux != DGPU_NUM_FLUX_ROE_PIKE &&
 	                                        phys->num_flux != DGPU_NUM_FLUX_LAX_FRIEDRICHS)))
-		return bfail(nullptr, DGPU_ERR_UNSUPPORTED, "advection/upwind or Euler/Roe-Pike/Lax-Friedrichs only");
+		return bfail(nullptr, DGPU_ERR_UNSUPPORTED,
+		             "advection/upwind or Euler, Navier-Stokes/Roe-Pike, Lax-Friedrichs only");
+	if (ns_pde && ((phys->viscosity != DGPU_VISCOSITY_CONSTANT && phys->viscosity != DGPU_VISCOSITY_SUTHERLAND) ||
+	               !(phys->mu >= 0.0) || !(phys->Pr > 0.0) ||
+	               (phys->viscosity == DGPU_VISCOSITY_SUTHERLAND && !(phys->r_s > 0.0))))
+		return bfail(nullptr, DGPU_ERR_INVALID_ARGUMENT,
+		             "Navier-Stokes needs a viscosity model, mu >= 0, Pr > 0 (and r_s > 0 for Sutherland's law)");
+	if (ns_pde && phys->dTdn != 0.0 && phys->viscosity != DGPU_VISCOSITY_CONSTANT)
+		return bfail(nullptr, DGPU_ERR_UNSUPPORTED, "a diabatic wall flux (dTdn != 0) needs constant viscosity");
 	if (mesh->n_volumes < 1 || mesh->n_faces < 1 || !mesh->metrics_vc || !mesh->jacobian_det_vc ||
 	    !mesh->face_vol || !mesh->face_lf || !mesh->normals_fc || !mesh->jacobian_det_fc)
 		return bfail(nullptr, DGPU_ERR_INVALID_ARGUMENT, "incomplete mesh");
@@ -671,8 +825,12 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	c->d = d;
 	c->pde = phys->pde;
 	c->flux = phys->num_flux;
-	c->nv = (phys->pde == DGPU_PDE_EULER ? d + 2 : 1);
-	c->positivity = (phys->pde == DGPU_PDE_EULER && phys->positivity) ? 1 : 0;
+	c->nv = (phys->pde != DGPU_PDE_ADVECTION ? d + 2 : 1);
+	c->positivity = (phys->pde != DGPU_PDE_ADVECTION && phys->positivity) ? 1 : 0;
+	c->navier_stokes = ns_pde;
+	if (ns_pde)
+		c->ns_phys = NsPhys{phys->mu, phys->Pr, phys->r_s, phys->viscosity,
+		                    -phys->mu * (kGamma / kGm1 * phys->r_s) / phys->Pr * phys->dTdn};
 	for (int k = 0; k < 3; ++k)
 		c->b_adv[k] = phys->b_adv[k];
 	c->n_vol = mesh->n_volumes;
@@ -701,6 +859,8 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	c->hgroups.resize(c->n_tp);
 	c->hops.resize(c->n_tp);
 	c->hdgroups.resize(c->n_dense);
+	if (c->navier_stokes && c->n_dense > 0)
+		return reject(DGPU_ERR_UNSUPPORTED, "Navier-Stokes in the batched context takes QUAD/HEX groups only");
 	std::vector<int> g_q(nG), g_nvs(nG), g_nvc(nG), g_type(nG);   // per internal group
 	std::vector<std::vector<double>> w(nG);                         // volume cubature weights per node
 	std::vector<const dgpu_dense_operators*> dops(c->n_dense);
@@ -922,7 +1082,8 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 			if (!mesh->bc_fc || !mesh->bc_state_fc)
 				return reject(DGPU_ERR_INVALID_ARGUMENT, "boundary faces need bc_fc and bc_state_fc");
 			const int code = mesh->bc_fc[f] % kBcStepSC;
-			if (code < 0 || (c->pde == DGPU_PDE_EULER ? !bc_is_euler(code) : !bc_is_advection_upwind(code)))
+			if (code < 0 || (c->navier_stokes ? !bc_is_navier_stokes(code)
+			                       : (c->pde == DGPU_PDE_EULER ? !bc_is_euler(code) : !bc_is_advection_upwind(code))))
 				return reject(DGPU_ERR_UNSUPPORTED,
 				              "BC code " + std::to_string(mesh->bc_fc[f]) + " is not provided for this pde");
 			if ((code == kBcBackPressure || code == kBcTotalTP) && !mesh->bc_data)
@@ -1119,6 +1280,14 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 	B_TRY(cudaMalloc((void**)&c->vol_gl, ns * sizeof(double)));
 	B_TRY(cudaMalloc((void**)&c->traces, (size_t)2 * nv * fb * sizeof(double)));
 	B_TRY(cudaMalloc((void**)&c->nnf, (size_t)nv * fb * sizeof(double)));
+	if (c->navier_stokes) {
+		B_TRY(cudaMalloc((void**)&c->ns_gv, (size_t)d * ns * sizeof(double)));
+		B_TRY(cudaMalloc((void**)&c->ns_gtr, (size_t)2 * d * nv * fb * sizeof(double)));
+		B_TRY(cudaMalloc((void**)&c->ns_dw, (size_t)nv * fb * sizeof(double)));
+		B_TRY(cudaMalloc((void**)&c->ns_y, (size_t)2 * d * nv * fb * sizeof(double)));
+		B_TRY(cudaMemset(c->ns_gtr, 0, (size_t)2 * d * nv * fb * sizeof(double)));
+		B_TRY(cudaMemset(c->ns_y, 0, (size_t)2 * d * nv * fb * sizeof(double)));
+	}
 	B_TRY(cudaMalloc((void**)&c->max_bits, sizeof(unsigned long long)));
 	B_TRY(cudaMalloc((void**)&c->err_flag, sizeof(int)));
 	B_TRY(cudaMalloc((void**)&c->d_bar, 2 * sizeof(unsigned)));
@@ -1264,6 +1433,8 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 		B_TRY(upload_vec(&c->d_fext, fext));
 	}
 	B_TRY(bind(c));
+	if (c->navier_stokes)   // bind set every group's E_ns
+		B_TRY(cudaMemcpy(c->d_groups, c->hgroups.data(), c->hgroups.size() * sizeof(BGroup), cudaMemcpyHostToDevice));
 #undef B_TRY
 	*out = c;
 	return DGPU_OK;
@@ -1449,6 +1620,8 @@ dgpu_status dgpu_batch_set_mode(dgpu_batch* c, int form)
 {
 	if (!c || form < 0 || form > 3)
 		return DGPU_ERR_INVALID_ARGUMENT;
+	if (c->navier_stokes && (form == 1 || form == 3))
+		return bfail(c, DGPU_ERR_UNSUPPORTED, "Navier-Stokes runs in forms 0 and 2");
 	c->mode = form;
 	return DGPU_OK;
 }
@@ -1507,7 +1680,7 @@ dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report
 	};
 	c->mode = 0;
 	for (int g = 0; g < c->n_all; ++g) {
-		if (c->group_n_vol(g) == 0)
+		if (c->group_n_vol(g) == 0 || c->navier_stokes)   // Navier-Stokes: the lifts keep the Euler default
 			continue;
 		int bestE = c->group_E(g);
 		float bestT = -1.f;
@@ -1541,6 +1714,10 @@ dgpu_status dgpu_batch_autotune(dgpu_batch* c, double dt, int reps, char* report
 	float tmode[4] = {0.f, 0.f, 0.f, 0.f};
 	int best = 0;
 	for (int m = 0; m < 4; ++m) {
+		if (c->navier_stokes && (m == 1 || m == 3)) {   // forms 0 and 2 only
+			tmode[m] = 1e30f;
+			continue;
+		}
 		c->mode = m;
 		if ((st = dgpu_batch_ssp_rk3_steps(c, dt, 1, nullptr)) != DGPU_OK)
 			break;

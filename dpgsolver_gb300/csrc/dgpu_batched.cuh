@@ -27,6 +27,7 @@ static_assert(sizeof(BatchOps) % 8 == 0, "BatchOps is copied to shared memory as
 struct BGroup {
 	int q, n_vol, E;          // order+1, volumes, elements per CTA of the per-group form
 	int first_tile;           // first tile of this group in the fused tile list
+	int E_ns;                 // elements per CTA of the Navier-Stokes gradient and volume kernels
 	long long elem0;          // first element (group-sorted element index)
 	long long state_off;      // offset of the group's first element in state-sized arrays
 	long long gmet_off;       // ... in the metric array
@@ -87,6 +88,13 @@ struct BParams {
 	const int* fbc;           // [face]: BC code modulo BC_STEP_SC, -1 on interior faces
 	const double* fext;       // per face: NV NF_f at NV fbase[f]: [NV][NF_f] exterior state at the face nodes
 	BcData bc_data;
+	// Navier-Stokes (BR2, dgpu_batched_ns.cuh), all null otherwise:
+	double* ns_gv = nullptr;  // per element [D][NV][N] at D * its state offset: the kept volume gradient
+	double* ns_gtr = nullptr; // per face: 2 D NV NF_f at 2 D NV fbase[f]: [side][D][NV][NF_f] gradient traces
+	double* ns_dw = nullptr;  // per face: NV NF_f at NV fbase[f]: w_f J_f (W_R - W_L) / 2, side-0 node order
+	double* ns_y = nullptr;   // per face, as ns_gtr: each side's own lifting of X at the face nodes (own node order)
+	NsPhys ns = {0.0, 1.0, 1.0, kViscosityConstant, 0.0};
+	double ns_eta = 0.0;      // BR2 scaling of a face's own lifting in its face gradient
 };
 
 // Fused tile list entry: group and first element within the group.

@@ -212,48 +212,59 @@ __device__ __forceinline__ double ns_val(const Dual<1>& x) { return x.v; }
 __device__ __forceinline__ double ns_der(const double&) { return 0.0; }
 __device__ __forceinline__ double ns_der(const Dual<1>& x) { return x.d[0]; }
 
+// The Navier-Stokes boundary value WR of a face node from the interior trace WL (set_function_pointers_num_flux_bc_
+// navier_stokes, face_solver_T.c:277-300): Riemann and supersonic in/outflow as for Euler; the static no-slip walls
+// keep rho and E and mirror the momentum (boundary_navier_stokes_T.c:258-304); the rotating wall takes 2 s_ex - s_l
+// for every variable, s_ex = (rho_b, rho_b u_wall, E_b) given as the exterior state (:196-244). ext: the node's
+// exterior state, its variables ext_stride apart.
+template <int D, typename T>
+__device__ __forceinline__ void ns_boundary_state(int code, const T* WL, const double* ext, int ext_stride,
+                                                  const double* n, const BcData& bcd, T* WR)
+{
+	constexpr int NV = D + 2;
+	if (code == kBcNoSlipAdiabatic || code == kBcNoSlipDiabatic) {
+		WR[0] = WL[0];
+#pragma unroll
+		for (int k = 0; k < D; ++k)
+			WR[1 + k] = -WL[1 + k];
+		WR[D + 1] = WL[D + 1];
+	} else if (code == kBcNoSlipAllRotating) {
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			WR[k] = 2.0 * ext[k * ext_stride] - WL[k];
+	} else {
+		double e[NV];
+#pragma unroll
+		for (int k = 0; k < NV; ++k)
+			e[k] = ext[k * ext_stride];
+		euler_boundary_state<D, T>(code, WL, e, n, WR, bcd);
+	}
+}
+
 // The face-node function on scalar type T (double, or dual numbers for the linearisations): from the left trace WL,
-// the right trace WR (a boundary face forms it from WL instead, as its BC), the gradient traces GtL, GtR (GtR unused
-// on a boundary face), it gives X = w_f J_f n (W_R - W_L) / 2 and the face flux
+// the right trace WR (a boundary face, code >= 0, forms it from WL instead, as its BC), the gradient traces GtL, GtR
+// (GtR unused on a boundary face), it gives X = w_f J_f n (W_R - W_L) / 2 and the face flux
 // o = w_f J_f (F*(W_L, W_R) + n . (F_v(W_L, G_L) + F_v(W_R, G_R)) / 2) with the partial face gradients
-// G_s = Gt_s + eta lambda_s X. b: the face's index in the boundary list, or -1.
+// G_s = Gt_s + eta lambda_s X. code: the face's BC code, or -1 inside; ext: its exterior state at the node.
 template <int D, int FLUX, typename T>
-__device__ __forceinline__ void ns_face_core(const TPParams& P, int b, int t, int NF, const double* n, double sc,
-                                             double lamL, double lamR, const T* WL, T* WR, const T (*GtL)[D + 2],
+__device__ __forceinline__ void ns_face_flux(int code, const double* ext, int ext_stride, const BcData& bcd,
+                                             const NsPhys& ph, double eta, const double* n, double sc, double lamL,
+                                             double lamR, const T* WL, T* WR, const T (*GtL)[D + 2],
                                              const T (*GtR)[D + 2], T (*X)[D + 2], T* o)
 {
 	constexpr int NV = D + 2;
-	int code = 0;
-	if (b >= 0) {
-		// the reference's Navier-Stokes boundary values (set_function_pointers_num_flux_bc_navier_stokes,
-		// face_solver_T.c:277-300): Riemann and supersonic in/outflow as for Euler; the static no-slip walls keep
-		// rho and E and mirror the momentum (boundary_navier_stokes_T.c:258-304); the rotating wall takes
-		// 2 s_ex - s_l for every variable, s_ex = (rho_b, rho_b u_wall, E_b) given as the exterior state (:196-244)
-		code = P.bc_code[b];
-		if (code == kBcNoSlipAdiabatic || code == kBcNoSlipDiabatic) {
-			WR[0] = WL[0];
-#pragma unroll
-			for (int k = 0; k < D; ++k)
-				WR[1 + k] = -WL[1 + k];
-			WR[D + 1] = WL[D + 1];
-		} else if (code == kBcNoSlipAllRotating) {
-			const double* ext = P.bc_ext + (size_t)b * NV * NF + t;
-#pragma unroll
-			for (int k = 0; k < NV; ++k)
-				WR[k] = 2.0 * ext[k * NF] - WL[k];
-		} else {
-			boundary_value<D, NV, kEuler, T>(P, b, t, NF, WL, n, WR);
-		}
-	}
+	const bool bnd = code >= 0;
+	if (bnd)
+		ns_boundary_state<D, T>(code, WL, ext, ext_stride, n, bcd, WR);
 	T GL[D][NV], GR[D][NV];
 #pragma unroll
 	for (int dir = 0; dir < D; ++dir)
 #pragma unroll
 		for (int k = 0; k < NV; ++k) {
 			X[dir][k] = (0.5 * sc * n[dir]) * (WR[k] - WL[k]);
-			GL[dir][k] = GtL[dir][k] + (P.ns_eta * lamL) * X[dir][k];
+			GL[dir][k] = GtL[dir][k] + (eta * lamL) * X[dir][k];
 			// on a boundary face the exterior gradient is the interior one (grad_from_internal; the walls copy it)
-			GR[dir][k] = b < 0 ? GtR[dir][k] + (P.ns_eta * lamR) * X[dir][k] : GL[dir][k];
+			GR[dir][k] = !bnd ? GtR[dir][k] + (eta * lamR) * X[dir][k] : GL[dir][k];
 		}
 	T nF[NV];
 	if constexpr (FLUX == kRoePike)
@@ -266,8 +277,8 @@ __device__ __forceinline__ void ns_face_core(const TPParams& P, int b, int t, in
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
 			FL[dir][k] = FR[dir][k] = T(0.0);
-	ns_viscous_sub<D, T>(WL, GL, P.ns, FL);
-	ns_viscous_sub<D, T>(WR, GR, P.ns, FR);
+	ns_viscous_sub<D, T>(WL, GL, ph, FL);
+	ns_viscous_sub<D, T>(WR, GR, ph, FR);
 #pragma unroll
 	for (int k = 0; k < NV; ++k) {
 		T s = T(0.0);
@@ -277,9 +288,20 @@ __device__ __forceinline__ void ns_face_core(const TPParams& P, int b, int t, in
 		// a static wall sets the total normal energy flux to nf_E: 0 when adiabatic, -mu Cp / Pr dTdn when
 		// diabatic (set_provided_Numerical_Flux_members, numerical_flux_central_T.c:222-231)
 		const bool wall_E = (k == D + 1 && (code == kBcNoSlipAdiabatic || code == kBcNoSlipDiabatic));
-		const double nf_E = code == kBcNoSlipDiabatic ? P.ns.wall_nf_E * sc : 0.0;
+		const double nf_E = code == kBcNoSlipDiabatic ? ph.wall_nf_E * sc : 0.0;
 		o[k] = wall_E ? T(nf_E) : (nF[k] + 0.5 * s) * sc;
 	}
+}
+
+// ns_face_flux with the uniform context's boundary list: b is the face's index in it, or -1.
+template <int D, int FLUX, typename T>
+__device__ __forceinline__ void ns_face_core(const TPParams& P, int b, int t, int NF, const double* n, double sc,
+                                             double lamL, double lamR, const T* WL, T* WR, const T (*GtL)[D + 2],
+                                             const T (*GtR)[D + 2], T (*X)[D + 2], T* o)
+{
+	const int code = b >= 0 ? P.bc_code[b] : -1;
+	const double* ext = b >= 0 ? P.bc_ext + (size_t)b * (D + 2) * NF + t : nullptr;
+	ns_face_flux<D, FLUX, T>(code, ext, NF, P.bc_data, P.ns, P.ns_eta, n, sc, lamL, lamR, WL, WR, GtL, GtR, X, o);
 }
 
 // One face node of the residual (T = double) or of the residual and its directional derivative (T = Dual<1>, the

@@ -20,8 +20,10 @@ import numpy as np
 from .element import TPOperatorSet, gauss_lobatto, gauss_legendre, lagrange_matrix, kron_tp, tp_weights
 from .geometry import TPGeometry, apply_nodes, sinusoidal_deform_2d, sinusoidal_deform_3d
 from .mesh import StructuredMesh
-from .problem import (GAMMA, GM1, NUM_FLUX_LAX_FRIEDRICHS, NUM_FLUX_ROE_PIKE, NUM_FLUX_UPWIND, PDE_ADVECTION,
-                      PDE_EULER, isentropic_vortex, primitive_to_conserved)
+from .problem import (BC_NOSLIP_ADIABATIC, BC_NOSLIP_ALL_ROTATING, BC_NOSLIP_DIABATIC, BC_RIEMANN, GAMMA, GM1,
+                      NUM_FLUX_LAX_FRIEDRICHS, NUM_FLUX_ROE_PIKE, NUM_FLUX_UPWIND, PDE_ADVECTION, PDE_EULER,
+                      PDE_NAVIER_STOKES, VISCOSITY_CONSTANT, VISCOSITY_SUTHERLAND, _ns_params, isentropic_vortex,
+                      primitive_to_conserved)
 
 
 class MixedTPProblem:
@@ -36,7 +38,8 @@ class MixedTPProblem:
         self.positivity = bool(positivity)
         self.b_adv = np.asarray(b_adv, dtype=np.float64)
         self.mesh = mesh
-        self.n_var = (d + 2) if pde == PDE_EULER else 1
+        self.n_var = 1 if pde == PDE_ADVECTION else d + 2
+        self.ns = None          # Navier-Stokes constants (viscosity model, mu, Pr, r_s, dTdn) when pde is 4
         p_vol = np.asarray(p_vol, dtype=np.int32)
         ps = sorted(set(int(p) for p in p_vol))
         self.groups = [TPOperatorSet(mesh.e_type, p) for p in ps]
@@ -209,23 +212,33 @@ class MixedTPProblem:
         self.bc_state = np.ascontiguousarray(ext)
 
     def stable_dt(self, cfl: float = 0.1) -> float:
-        """dt = cfl * h / ((2 p_max + 1) * max(|V| + c)) over the solution nodes."""
+        """dt = cfl * h / ((2 p_max + 1) * max(|V| + c)) over the solution nodes; with viscosity also the viscous
+        bound of problem.stable_dt."""
         d = self.d
-        lam = 0.0
+        lam, rho_min, T_max = 0.0, np.inf, 0.0
         for g in range(len(self.groups)):
             if len(self.group_vols[g]) == 0:
                 continue
             U = self.group_view(self.sol, g)
-            if self.pde == PDE_EULER:
+            if self.pde != PDE_ADVECTION:
                 rho = U[:, 0]
                 vel = U[:, 1:1 + d] / rho[:, None]
                 V2 = np.sum(vel * vel, axis=1)
                 pr = GM1 * (U[:, d + 1] - 0.5 * rho * V2)
                 lam = max(lam, float(np.max(np.sqrt(V2) + np.sqrt(GAMMA * pr / rho))))
+                rho_min = min(rho_min, float(np.min(rho)))
+                T_max = max(T_max, float(np.max(pr / rho)))
             else:
                 lam = max(lam, float(np.linalg.norm(self.b_adv[:d])))
         h = float(np.min(self.mesh.h))
-        return cfl * h / ((2 * max(g.p for g in self.groups) + 1) * lam)
+        k = 2 * max(g.p for g in self.groups) + 1
+        dt = cfl * h / (k * lam)
+        if self.ns is not None and self.ns["mu"] > 0.0:   # the viscous bound of problem.stable_dt
+            mu = self.ns["mu"]
+            if self.ns["viscosity"] == VISCOSITY_SUTHERLAND:
+                mu *= 0.08 * math.sqrt(T_max / self.ns["r_s"])
+            dt = min(dt, cfl * h * h / (k * k * GAMMA * mu / (self.ns["Pr"] * rho_min)))
+        return dt
 
 
 def _seeded_p(n_volumes, p_set, seed):
@@ -322,4 +335,48 @@ def mixed_vortex_2d(n: int = 8, p_set=(1, 2, 3, 4), seed: int = 0, num_flux: int
         prob.set_group(prob.sol, g, np.transpose(U, (1, 0, 2)))
     prob.dt = prob.stable_dt()
     prob.meta.update(n=n, p_set=tuple(p_set), seed=seed, curved=curved)
+    return prob
+
+
+def mixed_ns(d: int = 2, n: int = 6, p_set=(1, 2, 3, 4), num_flux: int = NUM_FLUX_ROE_PIKE, seed: int = 0,
+             mu: float = 0.02, viscosity: int = VISCOSITY_CONSTANT, mach: float = 0.3, perturb: float = 0.1,
+             curved: bool = False, amplitude: float = 0.03, walls=None, dTdn: float = 0.0) -> MixedTPProblem:
+    """Navier-Stokes on [0, 2 pi]^d with per-volume p from p_set (seeded): rho = 1 + perturb sin x cos y,
+    p = 1 / (gamma Ma^2), u = sin(y / 2) (1 + perturb cos x), v = perturb sin x sin(y / 2), w = perturb sin z
+    (3D). walls: None (periodic) or {(1, side): BC code} for the ends y = 0 and y = 2 pi (no-slip adiabatic,
+    diabatic with dTdn, rotating with the exterior state moving at u = 0.5, or Riemann with the unperturbed
+    state outside); the other directions stay periodic."""
+    L = 2.0 * math.pi
+    per = True if walls is None else tuple(k != 1 for k in range(d))
+    mesh = StructuredMesh(d, n, 0.0, L, periodic=per)
+    deform = None
+    if curved:
+        deform = sinusoidal_deform_2d(amplitude, L) if d == 2 else sinusoidal_deform_3d(amplitude, L)
+    prob = MixedTPProblem("mixed_ns", d, PDE_NAVIER_STOKES, num_flux, True, np.zeros(3), mesh,
+                          _seeded_p(mesh.n_volumes, p_set, seed), deform=deform, curved=curved)
+    prob.ns = dict(_ns_params(mu, viscosity=viscosity), dTdn=float(dTdn))
+    p0 = 1.0 / (GAMMA * mach * mach)
+    for g in range(len(prob.groups)):
+        if len(prob.group_vols[g]) == 0:
+            continue
+        x = prob.solution_node_xyz(g)
+        X, Y = x[..., 0], x[..., 1]
+        wall = np.sin(0.5 * Y)
+        vel = [wall * (1.0 + perturb * np.cos(X)), perturb * np.sin(X) * wall]
+        if d == 3:
+            vel.append(perturb * np.sin(x[..., 2]))
+        rho = 1.0 + perturb * np.sin(X) * np.cos(Y)
+        U = primitive_to_conserved(d, rho, np.stack(vel), np.full_like(X, p0))
+        prob.set_group(prob.sol, g, np.transpose(U, (1, 0, 2)))
+    prob.dt = prob.stable_dt()
+    prob.meta.update(n=n, p_set=tuple(p_set), seed=seed, curved=curved, mu=mu)
+    if walls is not None:
+        def outside(xb):
+            m = len(xb)
+            u = np.zeros((d, m))
+            rotating = any(c == BC_NOSLIP_ALL_ROTATING for c in walls.values())
+            if rotating:
+                u[0] = 0.5
+            return primitive_to_conserved(d, np.ones(m), u, np.full(m, p0)).T
+        prob.set_boundaries(walls, outside)
     return prob

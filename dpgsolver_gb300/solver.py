@@ -333,6 +333,10 @@ class BatchSimulation:
         phys.positivity = 1 if prob.positivity else 0
         for k in range(3):
             phys.b_adv[k] = float(prob.b_adv[k])
+        ns = getattr(prob, "ns", None)
+        if ns is not None:
+            phys.viscosity, phys.mu, phys.Pr, phys.r_s = int(ns["viscosity"]), ns["mu"], ns["Pr"], ns["r_s"]
+            phys.dTdn = float(ns.get("dTdn", 0.0))
         groups = fl["groups"]
         dense = any(getattr(o, "dense", False) for o in groups)
         tps = (_lib.TPOperators * len(groups))()

@@ -342,7 +342,8 @@ const char* dgpu_status_string(dgpu_status st);
 
 /* ---- Batched residual over a mixed-order mesh ------------------------------------------------------------------
  * One context for a mesh whose volumes belong to several (element type, p) groups: QUAD (d = 2) or HEX (d = 3),
- * p = 1..4, one group per p. Replaces the same reference entry points as the uniform context above
+ * p = 1..4, one group per p. Advection, Euler, and Navier-Stokes (BR2, as dgpu_create; QUAD/HEX groups only, in
+ * forms 0 and 2 below: the other forms and dense groups return DGPU_ERR_UNSUPPORTED). Replaces the same reference entry points as the uniform context above
  * (compute_rhs_dg, solve_dg.c:130-136; time_step_ssp_rk_33, solve_explicit.c:252-301) for a mesh with p
  * adaptation, where the reference's element loops visit volumes of different operator sets
  * (get_operator__cv0_vs_vc_T ... indexed by p, compute_volume_rlhs_dg_T.c) and integrates each face with the

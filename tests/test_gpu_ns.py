@@ -218,15 +218,17 @@ def test_ns_jacobian_matches_complex_step(gpu_lib, name):
 
 def test_ns_refusals(gpu_lib):
     from dpgsolver_gb300.solver import BatchSimulation, Simulation
-    prob = P.ns_vortex_2d(4, 2)
-    with pytest.raises(_lib.DGPUError) as e:
-        BatchSimulation(prob)
-    assert e.value.status == 2
+    prob = P.ns_taylor_couette(3, 2, mu=0.02, perturb=0.2)
+    with Simulation(prob) as a, BatchSimulation(prob) as b:   # the batched context takes it as one group
+        a.compute_rhs()
+        b.compute_rhs()
+        assert np.max(np.abs(b.rhs - a.rhs)) <= 1e-12 * np.max(np.abs(a.rhs))
     slip = P.euler_channel_2d(4, 2)             # slip walls: an Euler boundary the reference's NS does not take
     slip.pde, slip.ns = P.PDE_NAVIER_STOKES, {"viscosity": 101, "mu": 0.01, "Pr": 0.72, "r_s": 1.0}
-    with pytest.raises(_lib.DGPUError) as e:
-        Simulation(slip)
-    assert e.value.status == 2
+    for ctx in (Simulation, BatchSimulation):
+        with pytest.raises(_lib.DGPUError) as e:
+            ctx(slip)
+        assert e.value.status == 2
     bad = P.ns_vortex_2d(4, 2)
     bad.ns["Pr"] = 0.0
     with pytest.raises(_lib.DGPUError) as e:

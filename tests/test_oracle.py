@@ -129,10 +129,11 @@ def test_rk3_step_consistent_with_residual():
 def _mixed_cases():
     from dpgsolver_gb300.host import mixed as M
     return [lambda: M.mixed_euler(3, 3, seed=0), lambda: M.mixed_euler(2, 5, seed=1),
-            lambda: M.mixed_advection_2d(5), lambda: M.mixed_vortex_2d(5)]
+            lambda: M.mixed_advection_2d(5), lambda: M.mixed_vortex_2d(5),
+            lambda: M.mixed_ns(2, 4, seed=2), lambda: M.mixed_ns(3, 3, seed=3, curved=True)]
 
 
-@pytest.mark.parametrize("k", range(4))
+@pytest.mark.parametrize("k", range(6))
 def test_mixed_conservation(k):
     """Face fluxes at p_f telescope across volumes of different p: the sum of raw residuals vanishes."""
     prob = _mixed_cases()[k]()
