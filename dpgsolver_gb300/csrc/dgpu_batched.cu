@@ -53,6 +53,11 @@ struct dgpu_batch {
 	std::vector<int> order;                // sorted element -> list index
 	std::vector<long long> list_off;       // list index -> offset in the caller's state
 	std::vector<long long> sorted_off;     // sorted element -> offset in the device state
+	// the source term (dgpu_batch_set_source): the caller's cubature-node offsets, and per dense group its cv0
+	// (n_vc x n_vs) and every volume's w J at its nodes (group-sorted), for the projection cv0^T diag(w J) s
+	std::vector<long long> list_vc_off;
+	std::vector<std::vector<double>> dense_cv0_h, dense_wJ_h;
+	double* source = nullptr;              // state layout (group-sorted), or null
 	size_t ns = 0;
 	// device
 	BatchOps* d_ops = nullptr;
@@ -129,6 +134,7 @@ struct dgpu_batch {
 		P.fbc = d_fbc;
 		P.fext = d_fext;
 		P.bc_data = bc_data;
+		P.source = source;
 		if (navier_stokes) {
 			P.ns_gv = ns_gv;
 			P.ns_gtr = ns_gtr;
@@ -621,7 +627,7 @@ void free_batch(dgpu_batch* c)
 	drop_graphs(c);
 	void* ptrs[] = {c->d_nc, c->d_nc_inv, c->d_ops, c->d_groups, c->d_dgroups, c->d_elf, c->d_fbase, c->d_node_face, c->gmet, c->inv_wJ,
 	                c->fgeo, c->u, c->ug, c->u0, c->rhs, c->vol_gl, c->traces, c->nnf, c->max_bits, c->err_flag, c->d_bar,
-	                c->n_corr, c->d_tiles, c->d_fbc, c->d_fext, c->ns_gv, c->ns_gtr, c->ns_dw, c->ns_y};
+	                c->n_corr, c->d_tiles, c->d_fbc, c->d_fext, c->ns_gv, c->ns_gtr, c->ns_dw, c->ns_y, c->source};
 	for (void* p : ptrs)
 		if (p)
 			cudaFree(p);
@@ -987,7 +993,8 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 		count[vg[v]]++;
 	}
 	c->list_off.resize(nV + 1);
-	std::vector<long long> list_vc_off(nV + 1);
+	std::vector<long long>& list_vc_off = c->list_vc_off;
+	list_vc_off.resize(nV + 1);
 	long long so = 0, vco = 0;
 	for (int v = 0; v < nV; ++v) {
 		c->list_off[v] = so;
@@ -996,6 +1003,7 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 		vco += g_nvc[vg[v]];
 	}
 	c->list_off[nV] = so;
+	list_vc_off[nV] = vco;
 	c->ns = (size_t)so;
 	c->order.resize(nV);
 	std::vector<int> sorted_pos(nV);
@@ -1305,6 +1313,8 @@ dgpu_status create_impl(const dgpu_physics* phys, const std::vector<GroupIn>& gi
 		DGroup& G = c->hdgroups[t];
 		const int nvs = op->n_vs, nvc = op->n_vc;
 		std::vector<double> cv0(op->cv0_vs_vc, op->cv0_vs_vc + (size_t)nvc * nvs);
+		c->dense_cv0_h.push_back(cv0);
+		c->dense_wJ_h.push_back(dense_wJ[t]);
 		std::vector<double> cv1(op->cv1_vs_vc, op->cv1_vs_vc + (size_t)d * nvc * nvs);
 		std::vector<double> M((size_t)nvs * nvs, 0.0), Minv((size_t)nvs * nvs);
 		for (int a = 0; a < nvs; ++a)
@@ -1488,6 +1498,59 @@ dgpu_status dgpu_batch_state_size(const dgpu_batch* c, size_t* n)
 	if (!c || !n)
 		return DGPU_ERR_INVALID_ARGUMENT;
 	*n = c->ns;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_batch_set_source(dgpu_batch* c, const double* source_vc)
+{
+	if (!c)
+		return DGPU_ERR_INVALID_ARGUMENT;
+	if (!source_vc) {
+		if (c->source) {
+			BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
+			cudaFree(c->source);
+			c->source = nullptr;
+			drop_graphs(c);
+		}
+		return DGPU_OK;
+	}
+	// per sorted element: a TP volume's source is its GL nodal values (added after 1/(w J)); a dense volume's is
+	// tw0_vt_vc (J s) = cv0^T diag(w J) s (added before M^-1)
+	const int nv = c->nv;
+	std::vector<double> h(c->ns, 0.0);
+	for (int g = 0; g < c->n_all; ++g) {
+		const bool dense = c->gl[g].dense;
+		const int t = c->gl[g].idx;
+		const long long elem0 = dense ? c->hdgroups[t].elem0 : c->hgroups[t].elem0;
+		const int n_vol = c->group_n_vol(g);
+		for (int e = 0; e < n_vol; ++e) {
+			const long long p = elem0 + e;
+			const int v = c->order[p];
+			const double* src = source_vc + c->list_vc_off[v] * nv;
+			double* o = h.data() + c->sorted_off[p];
+			if (!dense) {
+				std::copy(src, src + (c->list_off[v + 1] - c->list_off[v]), o);
+				continue;
+			}
+			const int nvs = c->hdgroups[t].n_vs, nvc = c->hdgroups[t].n_vc;
+			const double* cv0 = c->dense_cv0_h[t].data();
+			const double* wJ = c->dense_wJ_h[t].data() + (size_t)e * nvc;
+			for (int k = 0; k < nv; ++k)
+				for (int m = 0; m < nvs; ++m) {
+					double a = 0.0;
+					for (int n = 0; n < nvc; ++n)
+						a += cv0[(size_t)n * nvs + m] * (wJ[n] * src[n + (size_t)nvc * k]);
+					o[(size_t)k * nvs + m] = a;
+				}
+		}
+	}
+	if (!c->source) {
+		BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
+		BATCH_CUDA(c, cudaMalloc((void**)&c->source, c->ns * sizeof(double)));
+		drop_graphs(c);   // captured steps hold the kernels' parameters, the source pointer among them
+	}
+	BATCH_CUDA(c, cudaMemcpyAsync(c->source, h.data(), c->ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+	BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
 	return DGPU_OK;
 }
 

@@ -95,6 +95,10 @@ struct BParams {
 	double* ns_y = nullptr;   // per face, as ns_gtr: each side's own lifting of X at the face nodes (own node order)
 	NsPhys ns = {0.0, 1.0, 1.0, kViscosityConstant, 0.0};
 	double ns_eta = 0.0;      // BR2 scaling of a face's own lifting in its face gradient
+	// The test case's source term (compute_source_rhs_dg_like, compute_rlhs.c:47-57) in the state layout, or null:
+	// a TP element's GL nodal values of s (M^-1 tw0_vt_vc (J s) = V^-1 s: added after 1/(w J)); a dense element's
+	// tw0_vt_vc (J s) = cv0^T diag(w J) s (added before M^-1).
+	const double* source = nullptr;
 };
 
 // Fused tile list entry: group and first element within the group.
@@ -438,6 +442,12 @@ __device__ void blift_body(const BParams& P, const BatchOps* sops, const BGroup&
 #pragma unroll
 		for (int k = 0; k < NV; ++k)
 			Rg[k] *= iw;
+		if (P.source) {
+			const double* sv = P.source + G.state_off + (long long)(e0 + e) * NV * N + node;
+#pragma unroll
+			for (int k = 0; k < NV; ++k)
+				Rg[k] += sv[(long long)k * N];
+		}
 	}
 
 	const bool need_coef = (MODE == kModeRhs) || (MODE != kModeRkGlNoMax && rk.want_max);

@@ -426,6 +426,8 @@ __device__ void dlift_body(const BParams& P, const DGroup& G, int e0, int E, con
 		const int e = it / (NV * nvs), rem = it % (NV * nvs), k = rem / nvs, m = rem % nvs;
 		const long long v = G.elem0 + e0 + e;
 		double acc = P.vol_gl[G.state_off + (long long)(e0 + e) * NV * nvs + rem];
+		if (P.source)   // cv0^T diag(w J) s
+			acc += P.source[G.state_off + (long long)(e0 + e) * NV * nvs + rem];
 		for (int lf = 0; lf < G.n_lf; ++lf) {
 			const int4 fd = P.elf[v * kMaxLf + lf];
 			const long long fb = P.fbase[fd.x];

@@ -196,6 +196,7 @@ class MixedTPProblem:
             "bc_fc": None if self.bc is None else np.ascontiguousarray(self.bc, dtype=np.int32),
             "bc_state_fc": None if self.bc_state is None else np.ascontiguousarray(self.bc_state).ravel(),
             "bc_data": self.bc_data,
+            "source_vc": getattr(self, "source_vc", None),
         }
 
     def set_boundaries(self, side_bc: dict, exterior):

@@ -577,6 +577,7 @@ class MixedTypeProblem:
             "bc_fc": None if self.bc is None else np.ascontiguousarray(self.bc, dtype=np.int32),
             "bc_state_fc": None if self.bc_state is None else np.ascontiguousarray(self.bc_state).ravel(),
             "bc_data": self.bc_data,
+            "source_vc": getattr(self, "source_vc", None),
         }
 
     def project(self, fn):

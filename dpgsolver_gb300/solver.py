@@ -394,6 +394,10 @@ class BatchSimulation:
         if stream is not None:
             check(lib.dgpu_batch_set_stream(h, ctypes.c_void_p(stream)), h, batch=True)
         self.upload_state(prob.sol)
+        n_vc = np.array([int(o.n_vc) for o in groups], dtype=np.int64)
+        self._n_source = int(n_vc[np.asarray(fl["vol_group"])].sum()) * int(prob.n_var)
+        if getattr(prob, "source_vc", None) is not None:
+            self.set_source(prob.source_vc)
 
     @staticmethod
     def _dense_operators(D, ops, arr, keep, factorised=True):
@@ -474,6 +478,17 @@ class BatchSimulation:
         self._check(self._lib.dgpu_batch_ssp_rk3_steps(self._h, float(dt), int(n_steps),
                                                        ctypes.byref(mx) if want_max else None))
         return mx.value if want_max else None
+
+    def set_source(self, source_vc):
+        """The test case's source at every volume's cubature nodes (flat, volume-list order, per volume
+        (n_var x n_vc) blocks as the reference's column-major (n_vc x n_var)), or None to remove it."""
+        if source_vc is None:
+            self._check(self._lib.dgpu_batch_set_source(self._h, None))
+            return
+        s = np.ascontiguousarray(source_vc, dtype=np.float64).ravel()
+        if s.size != self._n_source:
+            raise ValueError(f"source of {s.size} values, expected {self._n_source}")
+        self._check(self._lib.dgpu_batch_set_source(self._h, _dp(s)))
 
     FORMS = {"plain": 0, "fused": 1, "branches": 2, "stage": 3}
 

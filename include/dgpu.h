@@ -432,6 +432,13 @@ dgpu_status dgpu_batch_destroy(dgpu_batch* b);
 const char* dgpu_batch_last_error(const dgpu_batch* b);
 dgpu_status dgpu_batch_state_size(const dgpu_batch* b, size_t* n_doubles);
 dgpu_status dgpu_batch_upload_state(dgpu_batch* b, const double* sol);   /* host, list order; synchronous */
+/* The test case's source term, as dgpu_set_source: source_vc host, per volume (n_vc(v) x n_var) column-major, the
+ * source at the volume cubature nodes before the J scaling, concatenated in volume-list order (n_vc of a dense
+ * volume is its cubature node count); NULL removes it. The reference adds tw0_vt_vc (J s) to the rhs before M^-1
+ * (compute_source_rhs_dg_like, src/simulation/solvers/compute_rlhs.c:47-57): a TP volume adds s to its GL nodal
+ * residual after 1/(w J) (M^-1 tw0_vt_vc (J s) = V^-1 s); a TRI/TET/WEDGE/PYR volume's cv0^T diag(w J) s is formed
+ * once here, on the host, and added before its M^-1. Every later residual and RK stage includes it, in every form. */
+dgpu_status dgpu_batch_set_source(dgpu_batch* b, const double* source_vc);
 dgpu_status dgpu_batch_download_state(dgpu_batch* b, double* sol);
 dgpu_status dgpu_batch_download_rhs(dgpu_batch* b, double* rhs);
 /* compute_rhs_dg on the device state; max_rhs as for dgpu_compute_rhs. */
