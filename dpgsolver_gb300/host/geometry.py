@@ -36,6 +36,18 @@ def apply_nodes(op: np.ndarray, x: np.ndarray) -> np.ndarray:
 _QUAD_F_VE = ((0, 2), (1, 3), (0, 1), (2, 3))   # QUAD local faces -> vertices (element.c f_ve), v = a + 2 b
 
 
+def parametric_quad_coef(vertices: np.ndarray, p: int, deform) -> np.ndarray:
+    """Geometry coefficients at order p (GLL nodes) of QUAD volumes of a parametric domain from their vertices
+    (n_volumes, 4, 2) in TP order: the straight bilinear positions, then parametric_quad_nodes."""
+    from .element import gauss_lobatto, tp_nodes
+    x_g, _ = gauss_lobatto(p + 1)
+    xi = tp_nodes(x_g, 2)
+    hat = [0.25 * (1.0 + sa * xi[:, 0]) * (1.0 + sb * xi[:, 1]) for sb in (-1.0, 1.0) for sa in (-1.0, 1.0)]
+    straight = np.stack([sum(hat[k][None, :] * vertices[:, k, c][:, None] for k in range(4)) for c in range(2)],
+                        axis=2)
+    return parametric_quad_nodes(straight, x_g, deform)
+
+
 def parametric_quad_nodes(X_straight: np.ndarray, x_g: np.ndarray, deform) -> np.ndarray:
     """Geometry nodes of QUAD volumes of a parametric domain, the way the reference builds them.
 

@@ -400,16 +400,10 @@ def gmsh_tp_problem(path, d: int, p: int, pde: int, num_flux: int, state, b_adv=
         coef = blend(np.ascontiguousarray(np.transpose(mesh.vertices, (0, 2, 1))), curved_faces(mesh), p)
         geom = TPGeometry(mesh, ops, curved=True, coef=coef)
     elif parametric is not None:
-        from .element import gauss_lobatto, tp_nodes
-        from .geometry import parametric_quad_nodes
+        from .geometry import parametric_quad_coef
         if d != 2:
             raise ValueError("parametric meshes are built for QUAD volumes")
-        x_g, _ = gauss_lobatto(p + 1)
-        xi = tp_nodes(x_g, 2)
-        hat = [0.25 * (1.0 + sa * xi[:, 0]) * (1.0 + sb * xi[:, 1]) for sb in (-1.0, 1.0) for sa in (-1.0, 1.0)]
-        straight = np.stack([sum(hat[k][None, :] * mesh.vertices[:, k, c][:, None] for k in range(4))
-                             for c in range(2)], axis=2)
-        geom = TPGeometry(mesh, ops, curved=True, coef=parametric_quad_nodes(straight, x_g, parametric))
+        geom = TPGeometry(mesh, ops, curved=True, coef=parametric_quad_coef(mesh.vertices, p, parametric))
     else:
         geom = TPGeometry(mesh, ops, curved=False, coef=mesh.vertices)
     n_var = 1 if pde == PDE_ADVECTION else d + 2

@@ -30,7 +30,7 @@ class MixedTPProblem:
     """Mesh + per-volume p + per-group operators and geometry + state (flat, see the module docstring)."""
 
     def __init__(self, name, d, pde, num_flux, positivity, b_adv, mesh: StructuredMesh, p_vol, deform=None,
-                 curved=False):
+                 curved=False, parametric=None):
         self.name = name
         self.d = d
         self.pde = pde
@@ -64,11 +64,15 @@ class MixedTPProblem:
             self.group_vols.append(vols)
             if not len(vols):
                 self.geoms.append(None)
+            elif from_file and parametric is not None:   # each group at its own geometry order (isoparametric)
+                from .geometry import parametric_quad_coef
+                self.geoms.append(TPGeometry(mesh, ops, curved=True, vols=vols,
+                                             coef=parametric_quad_coef(mesh.vertices, ops.p, parametric)))
             elif from_file:
                 self.geoms.append(TPGeometry(mesh, ops, curved=False, coef=mesh.vertices, vols=vols))
             else:
                 self.geoms.append(TPGeometry(mesh, ops, deform=deform, curved=curved, vols=vols))
-        self.curved = bool(curved)
+        self.curved = bool(curved) or parametric is not None
         self._face_geometry()
         self.sol = np.zeros(int(self.state_off[-1]))
         self.dt = 0.0
@@ -199,14 +203,15 @@ class MixedTPProblem:
             "source_vc": getattr(self, "source_vc", None),
         }
 
-    def set_boundaries(self, side_bc: dict, exterior):
-        """BC code per boundary face from {(dim, side): code} and the exterior state exterior(xyz (m, d)) ->
-        (m, n_var) at every face node (the test case's constructor_sol_bv); interior faces get code 0."""
+    def set_boundaries(self, side_bc: dict | None, exterior):
+        """BC code per boundary face from {(dim, side): code} (None: the codes of a mesh read from a file) and the
+        exterior state exterior(xyz (m, d)) -> (m, n_var) at every face node (the test case's constructor_sol_bv);
+        interior faces get code 0."""
         mesh = self.mesh
         self.bc = np.zeros(mesh.n_faces, dtype=np.int32)
         for f in np.nonzero(mesh.face_vol[:, 1] < 0)[0]:
             lf = int(mesh.face_lf[f, 0])
-            self.bc[f] = side_bc[(lf // 2, lf % 2)]
+            self.bc[f] = mesh.face_bc[f] if side_bc is None else side_bc[(lf // 2, lf % 2)]
         ext = np.asarray(exterior(self.xyz_fc), dtype=np.float64).reshape(len(self.xyz_fc), self.n_var)
         inner = np.repeat(mesh.face_vol[:, 1] >= 0, np.diff(self.face_off))
         ext[inner] = 0.0

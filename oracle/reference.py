@@ -524,6 +524,9 @@ def with_reference_inputs(prob, ref: dict):
 MIXED_CASES = {
     "mx_adv_n8": ("advection", 8, 2, 4, 11, 20, [(-0.5, -0.5, 4), (0.5, 0.5, 3), (0.0, -0.75, 3), (-0.75, 0.5, 4)]),
     "mx_euler_n8": ("euler", 8, 1, 3, 31, 10, [(2.5, 2.5, 3), (7.5, 7.5, 2), (5.0, 1.25, 2), (1.25, 7.5, 3)]),
+    # the Taylor-Couette case of "tc_n2" (rotating inner wall, adiabatic outer wall, BR2, Roe-Pike) on its parametric
+    # square annulus (vertices in the square's coordinates)
+    "mx_tc_n2": ("navier_stokes_tc", 2, 2, 4, 31, 10, [(-0.75, 0.0, 4), (0.75, 0.75, 3)]),
 }
 
 
@@ -542,8 +545,12 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
     from dpgsolver_gb300.host.mesh import StructuredMesh
     from dpgsolver_gb300.host import problem as P
     pde, n, p, p_max, flux, steps, _ = MIXED_CASES[name]
-    lo, hi = _mixed_box(pde)
-    mesh = StructuredMesh(2, n, lo, hi)
+    if pde == "navier_stokes_tc":
+        from dpgsolver_gb300.host.gmsh import GmshMesh, GmshTPMesh
+        mesh = GmshTPMesh(GmshMesh(_tc_mesh(name, n, False), 2))
+    else:
+        lo, hi = _mixed_box(pde)
+        mesh = StructuredMesh(2, n, lo, hi)
     if face_vol is not None:
         fv, fl = np.asarray(face_vol), np.asarray(face_lf)
         same = np.all(fv == mesh.face_vol, axis=1) & np.all(fl == mesh.face_lf, axis=1)
@@ -552,7 +559,12 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
             raise AssertionError("face lists differ")
         mesh.face_vol = fv.astype(mesh.face_vol.dtype)
         mesh.face_lf = fl.astype(mesh.face_lf.dtype)
-    if pde == "advection":
+    if pde == "navier_stokes_tc":
+        prob = M.MixedTPProblem(name, 2, P.PDE_NAVIER_STOKES, flux, True, np.zeros(3), mesh, p_vol,
+                                parametric=P.cylinder_parametric_map)
+        prob.ns = dict(P._ns_params(_TC_MU, Pr=0.72, r_s=1.0), dTdn=0.0)
+        fn = lambda x: _tc_state(x, False)   # noqa: E731
+    elif pde == "advection":
         prob = M.MixedTPProblem(name, 2, P.PDE_ADVECTION, flux, False, np.array([1.0, 0.5, 0.0]), mesh, p_vol)
         fn = _advection_state
     else:
@@ -564,6 +576,8 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
             U = np.asarray(fn(x.reshape(-1, 2))).reshape(x.shape[0], x.shape[1], -1)
             prob.set_group(prob.sol, g, np.transpose(U, (0, 2, 1)))
     prob.dt = prob.stable_dt()
+    if pde == "navier_stokes_tc":
+        prob.set_boundaries(None, P._taylor_couette_wall(0.5, 1.0, 1.0))
     return prob
 
 
@@ -571,6 +585,17 @@ def run_mixed(name: str) -> dict:
     """Run a mixed-order case through the reference: its adaptation decides every volume's order; the host problem
     with those orders gives the state formula's values and dt. Returns the flat arrays of the fixture."""
     pde, n, p, p_max, flux, steps, adapt = MIXED_CASES[name]
+    if pde == "navier_stokes_tc":
+        from dpgsolver_gb300.host.gmsh import write_square_annulus_msh
+        ns = dict(_tc_ns(), dTdn=0.0, omega=1.0, p_b=1.0, t_b=1.0, rho_b=1.0, E_b=1.0 / 0.4 + 0.5 * 0.5 ** 2)
+        extra = dict(mesh_writer=lambda path: write_square_annulus_msh(path, n, n, outer=20111), ns=ns)
+        run = lambda **kw: run_case(name, "navier_stokes", n, p, 0.0, 1.0, flux, adapt_p=adapt,   # noqa: E731
+                                    p_max=p_max, **extra, **kw)
+        out0 = run()
+        p_vol = out0["volumes"][:, 2].astype(np.int32)
+        prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
+        out = run(states_fn=lambda o: [_tc_state(x, False) for x in o["xyz_vs"]], steps=steps, dt=prob.dt)
+        return _mixed_arrays(name, p_vol, n, flux, steps, prob, out)
     lo, hi = _mixed_box(pde)
     fn = _advection_state if pde == "advection" else _vortex_state
     out0 = run_case(name, pde, n, p, lo, hi, flux, adapt_p=adapt, p_max=p_max)
@@ -578,6 +603,17 @@ def run_mixed(name: str) -> dict:
     prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
     out = run_case(name, pde, n, p, lo, hi, flux, state_fn=lambda x: np.asarray(fn(x)).reshape(len(x), -1),
                    steps=steps, dt=prob.dt, adapt_p=adapt, p_max=p_max)
+    return _mixed_arrays(name, p_vol, n, flux, steps, prob, out)
+
+
+def _tc_ns() -> dict:
+    """The Navier-Stokes constants of the Taylor-Couette cases (mu, Pr = 0.72, r_s = 1, constant viscosity)."""
+    from dpgsolver_gb300.host import problem as P
+    return P._ns_params(_TC_MU, Pr=0.72, r_s=1.0)
+
+
+def _mixed_arrays(name, p_vol, n, flux, steps, prob, out) -> dict:
+    """The flat arrays of a mixed-order fixture from the reference's run."""
     case_dir = os.path.join(RUN_DIR, name)
     raw = lambda f: _read_bin(os.path.join(case_dir, f))   # noqa: E731
     mx = np.loadtxt(os.path.join(case_dir, "max_rhs.txt"), ndmin=1)

@@ -13,8 +13,9 @@ slip walls), the Euler supersonic vortex (Riemann faces, slip walls) and
 the Navier-Stokes Taylor-Couette case on the reference's
 parametric annulus (BR2, rotating and adiabatic or diabatic walls, 10 steps); the positivity limiter on the vortex
 with a near-vacuum dip (its RK states at 1e-10, the limiter's bar, with the oracle's correction count).
-The batched (mixed-order) context on periodic QUAD meshes whose orders the reference's own p-adaptation set (three
-orders, advection and the Euler vortex), in each of its four launch forms.
+The batched (mixed-order) context on meshes whose orders the reference's own p-adaptation set (three orders each):
+advection and the Euler vortex on periodic QUAD meshes in each of its four launch forms, and the Navier-Stokes
+Taylor-Couette case on its parametric annulus in the two forms that take Navier-Stokes.
 """
 import os
 
@@ -94,8 +95,12 @@ def test_host_buffer_step_matches_reference(gpu_lib, name):
     assert abs(mx - float(ref["max_rhs"])) <= tol * float(ref["max_rhs"])
 
 
-@pytest.mark.parametrize("name", sorted(R.MIXED_CASES))
-@pytest.mark.parametrize("form", ["plain", "fused", "branches", "stage"])
+# Navier-Stokes runs in the per-group and branch forms only
+_MIXED_FORMS = [(name, form) for name in sorted(R.MIXED_CASES) for form in ("plain", "fused", "branches", "stage")
+                if not (R.MIXED_CASES[name][0].startswith("navier_stokes") and form in ("fused", "stage"))]
+
+
+@pytest.mark.parametrize("name,form", _MIXED_FORMS)
 def test_batched_path_matches_reference_on_adapted_orders(gpu_lib, name, form):
     """The batched (mixed-order) context given the reference's volume and face lists after its own p-adaptation
     (three orders; faces at max(p_L, p_R), some listing their sides the other way round), its geometry and state."""
@@ -104,6 +109,12 @@ def test_batched_path_matches_reference_on_adapted_orders(gpu_lib, name, form):
     prob = R.with_reference_mixed_inputs(R.host_mixed_problem(name, ref["p_vol"], ref["face_vol"], ref["face_lf"]),
                                          ref)
     tol = _residual_tol(prob)
+    if R.MIXED_CASES[name][0].startswith("navier_stokes"):
+        # the face values of a lower-order neighbour reach a face of higher order through V, the trace and the
+        # GL(q) -> GL(q_f) interpolation (three roundings where the reference's cv0_vs_fc has one), and the energy
+        # residual carries the heat flux, a difference of gradients: measured 2.3 x the one-ulp floor (1.5e-12), all
+        # of it in the energy equation of the p = 4 volumes next to p = 3 ones
+        tol = 2.0 * tol   # max(2e-12, 4 x the floor)
     with BatchSimulation(prob) as sim:
         sim.form = form
         mx = sim.compute_rhs()

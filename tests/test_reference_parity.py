@@ -10,8 +10,9 @@ time_step_ssp_rk_33, compiled from its sources into oracle/_ref).
   parametric annulus (BR2, rotating inner wall, adiabatic or diabatic outer wall). The oracle, given the reference's
   geometry and state, must reproduce them to 1e-12 (the residual to max(1e-12, twice its one-ulp noise floor)); the
   repo's own geometry must reproduce the reference's to 1e-13.
-* Mixed orders: periodic QUAD meshes after the reference's own adapt_hp raised the volumes around given vertices
-  (three orders per mesh, advection and the Euler vortex); oracle and host set-up as above.
+* Mixed orders: meshes after the reference's own adapt_hp raised the volumes around given vertices (three orders per
+  mesh): advection and the Euler vortex on periodic QUAD meshes, the Navier-Stokes Taylor-Couette case on its
+  parametric annulus; oracle and host set-up as above.
 * Where oracle/_ref is built (the reference tree is present), the full-size vortex (QUAD 64^2, p = 3, Roe) is run
   live: residual, ten RK steps and geometry.
 """
