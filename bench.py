@@ -168,8 +168,8 @@ def flops_per_element(d, q, nv, flux, coef_io):
 
 # FP64 thread-instructions (DFMA + DMUL + DADD) per element of one RK stage, from ncu
 # (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on of the volume, face and lift kernels on the 24^3 p3
-# Lax-Friedrichs case, the --set full capture of one stage): 8.84 k + 5.67 k + 2.94 k.
-FP64_INSTR_PER_ELEMENT = {(3, 3, "lf"): 17450}
+# Lax-Friedrichs case, the --set full capture of one stage): 8.64 k + 4.85 k + 2.94 k.
+FP64_INSTR_PER_ELEMENT = {(3, 3, "lf"): 16432}
 
 
 def ranks_barrier(torch, world):
@@ -234,9 +234,9 @@ def algorithmic_bytes(prob, kernel):
 
 
 # DRAM bytes per element of one tp_volume_kernel launch (GL state in) measured by ncu on curved HEX 24^3, p = 3,
-# 5 variables: 99.5 MB read + 42.4 MB written over 13,824 elements (writes stay below the algorithmic vol_gl +
+# 5 variables: 99.5 MB read + 42.7 MB written over 13,824 elements (writes stay below the algorithmic vol_gl +
 # traces because L2 holds part of them until the face kernel reads them).
-_VOLUME_DRAM_BYTES_PER_ELEMENT_HEX_P3 = (99.5e6 + 42.4e6) / 13824
+_VOLUME_DRAM_BYTES_PER_ELEMENT_HEX_P3 = (99.5e6 + 42.7e6) / 13824
 
 
 def volume_traffic(prob, kernel):
