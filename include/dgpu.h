@@ -44,7 +44,7 @@ typedef int dgpu_status;
  *  definitions_numerical_flux.h, src/element/definitions_elements.h). */
 #define DGPU_PDE_ADVECTION 1
 #define DGPU_PDE_EULER     3
-#define DGPU_PDE_NAVIER_STOKES 4   /* Euler flux + viscous flux, BR2 second-order terms (dgpu_create only) */
+#define DGPU_PDE_NAVIER_STOKES 4   /* Euler flux + viscous flux, BR2 second-order terms (QUAD/HEX volumes) */
 #define DGPU_VISCOSITY_CONSTANT   101   /* definitions_physics.h:34-36 */
 #define DGPU_VISCOSITY_SUTHERLAND 102
 #define DGPU_NUM_FLUX_UPWIND          11

@@ -6,7 +6,9 @@ dgpu_ssp_rk3_step_host. On the CPU it must compile with -Wall -Wextra -Werror ag
 libdgpu.so; on the GPU its residual and RK states must match the reference's own (the golden fixtures of
 tests/golden/make_ref_golden.py) to 1e-12: periodic advection and Euler, the duct with total T/p and back-pressure
 faces, the supersonic vortex with Riemann faces and slip walls, and the Navier-Stokes Taylor-Couette case with its
-walls.
+walls. The second program (tests/c/dgpu_batch_caller.c) does the same for a p-adapted mesh through the batched
+context: the reference's own adapt_hp orders (three per mesh) for advection, the Euler vortex and the Navier-Stokes
+Taylor-Couette case.
 """
 import os
 import subprocess
@@ -21,18 +23,21 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(REPO, "tests", "c", "dgpu_caller.c")
 
 
-def build_caller(out_dir):
+BATCH_SRC = os.path.join(REPO, "tests", "c", "dgpu_batch_caller.c")
+
+
+def build_caller(out_dir, src=SRC):
     import dpgsolver_gb300
     lib = dpgsolver_gb300.build()
-    exe = os.path.join(out_dir, "dgpu_caller")
+    exe = os.path.join(out_dir, os.path.splitext(os.path.basename(src))[0])
     subprocess.run(["gcc", "-std=c11", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(REPO, "include"),
-                    SRC, "-o", exe, lib, "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+                    src, "-o", exe, lib, "-Wl,-rpath," + os.path.dirname(lib)], check=True)
     return exe
 
 
 def test_c_caller_compiles_against_the_header(tmp_path):
-    exe = build_caller(str(tmp_path))
-    assert os.path.exists(exe)
+    for src in (SRC, BATCH_SRC):
+        assert os.path.exists(build_caller(str(tmp_path), src))
 
 
 def write_case(path, prob, ref, n_steps):
@@ -85,6 +90,69 @@ def test_c_caller_matches_reference(gpu_lib, tmp_path, name):
     noisy = prob.sol * (1.0 + np.random.default_rng(0).choice([-1.0, 1.0], prob.sol.shape) * 2.0 ** -52)
     floor = np.max(np.abs(o.compute_rhs(noisy)[0] - r0)) / np.max(np.abs(r0))
     tol = max(1e-12, 2.0 * floor)
+    assert np.max(np.abs(rhs - ref["rhs"])) / np.max(np.abs(ref["rhs"])) <= tol
+    assert abs(mx0 - float(ref["max_rhs"])) <= tol * float(ref["max_rhs"])
+    assert np.max(np.abs(sol - ref["sol_steps"])) / np.max(np.abs(ref["sol_steps"])) <= 1e-12
+
+
+def write_mixed_case(path, prob, ref):
+    """A p-adapted case in the reference's layouts: one TP operator set per order, per volume its group and its
+    blocks at its own order, per face its node count at p_f."""
+    d = prob.d
+    groups = prob.groups
+    with open(path, "wb") as fh:
+        np.array([0x48435442, d, prob.pde, prob.num_flux, int(prob.positivity), len(groups), prob.n_volumes,
+                  prob.mesh.n_faces, int(ref["steps"])], dtype=np.int32).tofile(fh)
+        np.array([float(ref["dt"])] + [float(b) for b in prob.b_adv[:3]], dtype=np.float64).tofile(fh)
+        ns = getattr(prob, "ns", None) or {}
+        np.array([int(ns.get("viscosity", 0))], dtype=np.int32).tofile(fh)
+        np.array([ns.get("mu", 0.0), ns.get("Pr", 0.0), ns.get("r_s", 0.0), ns.get("dTdn", 0.0)],
+                 dtype=np.float64).tofile(fh)
+        np.asarray(prob.bc_data if prob.bc_data is not None else (0.0,) * 4, dtype=np.float64).tofile(fh)
+        for ops in groups:
+            np.array([ops.p], dtype=np.int32).tofile(fh)
+            for a in (ops.cv0_1d, ops.cv1_1d, ops.cv0_bnd_1d, ops.w_vc_1d, ops.ccSB0_1d, ops.ccBS0_1d):
+                np.ascontiguousarray(a, dtype=np.float64).tofile(fh)
+        nv = prob.n_var
+        n_vc = np.array([groups[g].n_vc for g in prob.vol_group], dtype=np.int64)
+        vc_off = np.concatenate([[0], np.cumsum(n_vc)])
+        for v in range(prob.n_volumes):
+            np.array([prob.vol_group[v]], dtype=np.int32).tofile(fh)
+            a, b = vc_off[v], vc_off[v + 1]
+            np.ascontiguousarray(ref["metrics_vc"][a * d * d:b * d * d]).tofile(fh)
+            np.ascontiguousarray(ref["jacobian_det_vc"][a:b]).tofile(fh)
+            np.ascontiguousarray(ref["sol_in"][a * nv:b * nv]).tofile(fh)
+        fo = prob.face_off
+        for f in range(prob.mesh.n_faces):
+            bc = int(prob.bc[f]) if prob.bc is not None else 0
+            nfc = int(fo[f + 1] - fo[f])
+            np.concatenate([ref["face_vol"][f], ref["face_lf"][f], [bc, nfc]]).astype(np.int32).tofile(fh)
+            np.ascontiguousarray(ref["normals_fc"][fo[f] * d:fo[f + 1] * d]).tofile(fh)
+            np.ascontiguousarray(ref["jacobian_det_fc"][fo[f]:fo[f + 1]]).tofile(fh)
+            if ref["face_vol"][f][1] < 0:
+                np.ascontiguousarray(prob.bc_state[fo[f]:fo[f + 1]]).tofile(fh)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(R.MIXED_CASES))
+def test_c_batch_caller_matches_reference(gpu_lib, tmp_path, name):
+    ref = dict(np.load(os.path.join(REPO, "tests", "golden", f"reference_{name}.npz")))
+    prob = R.with_reference_mixed_inputs(R.host_mixed_problem(name, ref["p_vol"], ref["face_vol"], ref["face_lf"]),
+                                         ref)
+    exe = build_caller(str(tmp_path), BATCH_SRC)
+    case, out = str(tmp_path / "case.bin"), str(tmp_path / "out.bin")
+    write_mixed_case(case, prob, ref)
+    subprocess.run([exe, case, out], check=True)
+    res = np.fromfile(out, dtype=np.float64)
+    n = prob.sol.size
+    assert res.size == 2 * n + 2
+    rhs, mx0, sol = res[:n], res[n], res[n + 1:2 * n + 1]
+    o = oracle.Oracle(prob)
+    r0, _ = o.compute_rhs(prob.sol)
+    noisy = prob.sol * (1.0 + np.random.default_rng(0).choice([-1.0, 1.0], prob.sol.shape) * 2.0 ** -52)
+    floor = np.max(np.abs(o.compute_rhs(noisy)[0] - r0)) / np.max(np.abs(r0))
+    # as tests/test_gpu_reference.py: 4 x the floor for the mixed-order Navier-Stokes case, 2 x elsewhere
+    tol = max(1e-12, (4.0 if R.MIXED_CASES[name][0].startswith("navier_stokes") else 2.0) * floor)
     assert np.max(np.abs(rhs - ref["rhs"])) / np.max(np.abs(ref["rhs"])) <= tol
     assert abs(mx0 - float(ref["max_rhs"])) <= tol * float(ref["max_rhs"])
     assert np.max(np.abs(sol - ref["sol_steps"])) / np.max(np.abs(ref["sol_steps"])) <= 1e-12
