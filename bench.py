@@ -452,6 +452,7 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_mixed:
         res["mixed_types"] = mixed_measurements(torch, stream, args, "types")
         res["mixed"] = mixed_measurements(torch, stream, args, "hex")
+        res["mixed_ns"] = mixed_ns_measurements(torch, stream, args)
         res["tri_quad_2d"] = tri_quad_measurements(torch, stream, args)
     if rank == 0 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, workers=1, prob=prob)
@@ -702,11 +703,14 @@ def _batched_forms(torch, stream, args, sim, prob, n_steps, autotune=True):
         out[label] = {"value": 3 * ns * n_steps / (ms * 1e-3), "ms_per_step": ms / n_steps,
                       "launches_per_step": (sim.kernel_launches() - l0) / n_steps}
 
+    persistent = getattr(prob, "ns", None) is None   # Navier-Stokes runs in the per-group and branch forms only
     run("plain_per_group", "plain", False)
     run("per_group_graph", "plain", True)
-    run("fused_graph", "fused", True)
+    if persistent:
+        run("fused_graph", "fused", True)
     run("branches_graph", "branches", True)
-    run("stage_graph", "stage", True)
+    if persistent:
+        run("stage_graph", "stage", True)
     report, tuned_form = None, None
     if autotune:
         sim.upload_state(prob.sol)
@@ -738,6 +742,25 @@ def tri_quad_measurements(torch, stream, args):
             "groups": {f"{tname[getattr(o, 'e_type', QUAD)]} p{o.p}": int(np.sum(prob.vol_group == i))
                        for i, o in enumerate(prob.groups)},
             "unit": "DOF-residual-evals/s", "steps": n_steps, "forms": out, "setup_s": setup_s}
+
+
+def mixed_ns_measurements(torch, stream, args):
+    """Navier-Stokes in the batched context: mixed-order HEX n^3 on [0, 2 pi]^3 (mixed_ns: p uniform in {1,2,3,4}
+    per volume with seed 0, Roe-Pike + BR2, mu = 0.02, Mach 0.3 channel-like state, no-slip adiabatic walls at
+    y = 0 and 2 pi, periodic in x and z): SSP-RK3 steps per-group and on graph branches."""
+    from dpgsolver_gb300.host import problem as P
+    from dpgsolver_gb300.host.mixed import mixed_ns
+    from dpgsolver_gb300.solver import BatchSimulation
+    n = args.mixed_ns_n
+    prob = mixed_ns(3, n, seed=0, walls={(1, 0): P.BC_NOSLIP_ADIABATIC, (1, 1): P.BC_NOSLIP_ADIABATIC})
+    n_steps = max(3, min(args.steps, 10))
+    with BatchSimulation(prob, stream=stream.cuda_stream) as sim:
+        out, report, tuned = _batched_forms(torch, stream, args, sim, prob, n_steps, autotune=True)
+    return {"workload": f"3D Navier-Stokes mixed-order HEX {n}^3 on [0, 2 pi]^3, p uniform in {{1,2,3,4}} (seed 0), "
+                        "Roe-Pike + BR2, mu 0.02, adiabatic no-slip walls at y = 0, 2 pi",
+            "elements": prob.n_volumes, "n_state": prob.n_state,
+            "groups": {f"HEX p{o.p}": int(np.sum(prob.vol_group == i)) for i, o in enumerate(prob.groups)},
+            "unit": "DOF-residual-evals/s", "steps": n_steps, "forms": out, "autotune": {"form": tuned}}
 
 
 def mixed_measurements(torch, stream, args, kind="types"):
@@ -1117,6 +1140,7 @@ def main():
     ap.add_argument("--vortex-steps", type=int, default=1000)
     ap.add_argument("--mixed-n", type=int, default=58, help="volumes per direction of the mixed-order HEX mesh")
     ap.add_argument("--types-n", type=int, default=50, help="cells per direction of the mixed-type mesh (even)")
+    ap.add_argument("--mixed-ns-n", type=int, default=24, help="volumes per direction of the mixed-order NS mesh")
     ap.add_argument("--tri-n", type=int, default=384, help="cells per direction of the 2D QUAD/TRI mesh")
     ap.add_argument("--mixed-form", choices=["plain", "per_group_graph", "fused", "branches", "stage"], default="fused",
                     help="form of the mixed-order stages for --workload mixed3d --only-rk")
