@@ -211,7 +211,7 @@ def _batching_bound(prob, w, plain_stage_ms, peak_tflops):
             "mixed_order_hex": {"plain_fp64_pipe_frac": 0.717, "max_speedup_vs_plain": 1.39,
                                 "source": "time-weighted FP64 pipe (elapsed) of the plain per-group stage's kernels in "
                                           "the ncu --set full capture of the 36^3 mixed-order HEX mesh"},
-            "note": "the north star's 3x batched-vs-plain target exceeds these bounds: the plain form is FP64-issue "
+            "note": "a 3x batched-vs-plain speed-up exceeds these bounds: the plain form is FP64-issue "
                     "bound already, so batching can only recover the idle issue slots (launch gaps, tails, low "
                     "occupancy of the lifts)"}
 
