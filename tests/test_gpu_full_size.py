@@ -10,7 +10,8 @@ The 32^3 state is the z-axis vortex plus 1e-3 density noise: its residual is a s
 the oracle's own response to one-ulp input noise (the noise floor, measured in the test) is about 1.3e-12 of
 max |R|. That is the conditioning of the residual itself, not of an implementation: on the 2D vortex at 64^2 the
 reference's own residual moves by 1.06e-12 under one-ulp input noise (tests/test_reference_parity.py). The residual is
-held to max(1e-12, 2 x that floor); the RK state, O(1), is held to 1e-12.
+held to max(1e-12, 2 x that floor); the RK state, O(1), is held to 1e-12. On the same mesh with a state whose
+residual is well conditioned (seeded 5 % nodal noise, floor 3e-14), the residual itself is held to 1e-12.
 """
 import numpy as np
 import pytest
@@ -47,6 +48,26 @@ def test_headline_residual_and_step_match_oracle(gpu_lib, headline):
     assert rel(r, r_ref) <= max(TOL, 2.0 * floor)
     assert abs(mx - mx_ref) <= max(TOL, 2.0 * floor) * mx_ref
     assert rel(s, s_ref) <= TOL
+
+
+def test_headline_mesh_residual_within_1e12_on_a_well_conditioned_state(gpu_lib, headline):
+    """The same 32^3 p = 3 mesh and flux with every conserved variable at every node scaled by a seeded factor in
+    [0.95, 1.05] (velocity and temperature unchanged): the residual is then no longer a small difference of flux
+    terms (max |R| 117 instead of 3.3), its one-ulp noise floor falls to 3e-14, and the GPU is held to 1e-12."""
+    from dpgsolver_gb300.solver import Simulation
+    prob, o = headline
+    f = 1.0 + 0.05 * np.random.default_rng(5).uniform(-1.0, 1.0, size=(prob.n_volumes, 1, prob.ops.n_vs))
+    u = prob.sol * f
+    r_ref, mx_ref = o.compute_rhs(u)
+    noisy = u * (1.0 + np.random.default_rng(0).choice([-1.0, 1.0], u.shape) * 2.0 ** -52)
+    floor = rel(o.compute_rhs(noisy)[0], r_ref)
+    assert floor < 0.2 * TOL
+    with Simulation(prob) as sim:
+        sim.upload_state(u)
+        mx = sim.compute_rhs()
+        r = sim.rhs
+    assert rel(r, r_ref) <= TOL
+    assert abs(mx - mx_ref) <= TOL * mx_ref
 
 
 def test_headline_conservation_free_stream_and_determinism(gpu_lib, headline):
