@@ -56,6 +56,9 @@ WORKLOADS = {
     "mixed_types": dict(kind="mixed", n=50, p=None, flux="roe_pike",
                         desc="3D Euler HEX/TET/WEDGE/PYR 50^3 cells unit cube, p uniform in {1,2,3,4} (seed 0), "
                              "Roe-Pike"),
+    "mixed_ns": dict(kind="mixed", n=24, p=None, flux="roe_pike",
+                     desc="3D Navier-Stokes mixed-order HEX 24^3 on [0, 2 pi]^3 with adiabatic walls, p uniform in "
+                          "{1,2,3,4} (seed 0), Roe-Pike + BR2"),
 }
 
 
@@ -282,7 +285,10 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.set_stream(stream)
         if args.only_rk:
             return mixed_only_rk(torch, stream, args)
-        mx = mixed_measurements(torch, stream, args, "types" if args.workload == "mixed_types" else "hex")
+        if args.workload == "mixed_ns":
+            mx = mixed_ns_measurements(torch, stream, args)
+        else:
+            mx = mixed_measurements(torch, stream, args, "types" if args.workload == "mixed_types" else "hex")
         best = max(mx["forms"], key=lambda k: mx["forms"][k]["value"])
         return {"metric": "DOF-residual-evals/sec FP64 (batched graph vs plain per-group) at <=1e-12; %HBM peak",
                 "value": mx["forms"][best]["value"], "unit": "DOF-residual-evals/s", "n_gpus": world,
@@ -869,8 +875,14 @@ def mixed_cpu_baseline(kind, seconds, workers=1):
 def mixed_only_rk(torch, stream, args):
     """One form of the mixed stages, graph-replayed RK steps only (profiling)."""
     from dpgsolver_gb300.solver import BatchSimulation
-    kind = "types" if args.workload == "mixed_types" else "hex"
-    prob = make_mixed(kind, args.types_n if kind == "types" else args.mixed_n)
+    if args.workload == "mixed_ns":
+        from dpgsolver_gb300.host import problem as P
+        from dpgsolver_gb300.host.mixed import mixed_ns
+        prob = mixed_ns(3, args.mixed_ns_n, seed=0, walls={(1, 0): P.BC_NOSLIP_ADIABATIC,
+                                                           (1, 1): P.BC_NOSLIP_ADIABATIC})
+    else:
+        kind = "types" if args.workload == "mixed_types" else "hex"
+        prob = make_mixed(kind, args.types_n if kind == "types" else args.mixed_n)
     sim = BatchSimulation(prob, stream=stream.cuda_stream)
     sim.form = {"plain": "plain", "per_group_graph": "plain", "fused": "fused",
                 "branches": "branches", "stage": "stage"}[args.mixed_form]

@@ -29,8 +29,10 @@ template <int D, int Q, int NV>
 struct BnsSmem {
 	static constexpr int N = TPShape<D, Q>::N;
 	static constexpr int NFQ = TPShape<D, Q>::NF;
+	static constexpr int NF_MAX = (D == 2 ? kQMax : kQMax * kQMax);                // nodes of a face at q_f = 5
 	static constexpr int GRAD = (1 + D) * NV * N + 2 * D * (1 + D) * NV * NFQ;   // su, sd, traces of both
-	static constexpr int VOL = (1 + D) * NV * N + 2 * D * D * NV * NFQ;          // su, sf, I^T X per face
+	// su, sf, I^T X per face, X of one face at its q_f nodes
+	static constexpr int VOL = (1 + D) * NV * N + 2 * D * D * NV * NFQ + D * NV * NF_MAX;
 	static constexpr int MAX = GRAD > VOL ? GRAD : VOL;
 };
 
@@ -272,6 +274,7 @@ __device__ void bns_volume_body(const BParams& P, const BatchOps* sops, const BG
 	double* su = base + e * PER_E;
 	double* sf = su + NV * N;          // D NV N: contravariant flux (the GLL -> GL temporaries first)
 	double* sx = sf + D * NV * N;      // [lf][C][NFQ]: I^T X at the element's own face points
+	double* sxf = sx + 2 * D * C * NFQ;   // [C][nff]: X of one face at its q_f nodes, in this side's node order
 	if (GLL_IN) {
 		tp_apply<D, Q, NV>(su, sf, sf + NV * N, sops->t.B, node, active);
 		if (active)
@@ -281,24 +284,42 @@ __device__ void bns_volume_body(const BParams& P, const BatchOps* sops, const BG
 		__syncthreads();
 	}
 	const long long el = (long long)(e0 + e);
-	const int4* ef = P.elf + (G.elem0 + el) * kMaxLf;
-	if (active)
-		for (int lf = 0; lf < 2 * D; ++lf) {
+	const int4* ef = P.elf + (G.elem0 + (active ? el : 0)) * kMaxLf;
+	for (int lf = 0; lf < 2 * D; ++lf) {   // every thread of the CTA: the loop synchronises
+		int qf = Q, nff = 0;
+		if (active) {
 			const int4 fd = ef[lf];
-			const int qf = fd.z, nff = (D == 2 ? qf : qf * qf);
+			qf = fd.z;
+			nff = (D == 2 ? qf : qf * qf);
 			const long long fb = P.fbase[fd.x];
 			// side 1 reads the side-0-ordered jump and normal at its own nodes through the inverse permutation;
-			// X = n (side 0's) times the jump serves both sides (the same values seen from either side)
+			// X = n (side 0's) times the jump serves both sides (the same values seen from either side). Each
+			// value is read from global memory once, into sxf.
 			const int* ci = (fd.y == 1 && P.nc_inv) ? P.nc_inv + fb : nullptr;
 			const double* dw = P.ns_dw + NV * fb;
 			const double* fg = P.fgeo + (D + 1) * fb;
-			auto src = [&](int c, int i) {
+			for (int i = node; i < nff; i += N) {
 				const int j = ci ? ci[i] : i;
-				return fg[(c / NV) * nff + j] * dw[(c % NV) * nff + j];
-			};
+				double w[NV];
+#pragma unroll
+				for (int k = 0; k < NV; ++k)
+					w[k] = dw[k * nff + j];
+#pragma unroll
+				for (int dir = 0; dir < D; ++dir) {
+					const double nd = fg[dir * nff + j];
+#pragma unroll
+					for (int k = 0; k < NV; ++k)
+						sxf[(dir * NV + k) * nff + i] = nd * w[k];
+				}
+			}
+		}
+		__syncthreads();
+		if (active) {
+			auto src = [&](int c, int i) { return sxf[c * nff + i]; };
 			bface_get<D, Q>(sops, qf, C, src, sx + lf * C * NFQ, node);
 		}
-	__syncthreads();
+		__syncthreads();
+	}
 	double fr[D][NV];
 	const double* iwJp = P.inv_wJ + G.wj_off + el * N;
 	if (active) {
