@@ -186,6 +186,7 @@ EXPORTS = {
     "dgpu_batch_state_size": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
     "dgpu_batch_upload_state": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dgpu_batch_set_source": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dgpu_batch_set_barrier_timeout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "dgpu_batch_download_state": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dgpu_batch_download_rhs": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dgpu_batch_compute_rhs": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),

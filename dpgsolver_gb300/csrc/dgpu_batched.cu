@@ -91,6 +91,7 @@ struct dgpu_batch {
 	// form 3: the stage kernel's grid per mode (residual, RK stage with max |rhs|, without), its barrier words
 	int stage_blocks[3] = {0, 0, 0};
 	unsigned* d_bar = nullptr;
+	unsigned long long barrier_ns = kBarrierLimitNs;   // bound of each grid-barrier wait
 	cudaError_t (*stage_launch)(dgpu_batch*, bool rhs_mode, double dt, int stage, int want_max) = nullptr;
 	cudaError_t (*face_nodes)(dgpu_batch*, long long lo, long long hi, int blocks) = nullptr;
 	// execution
@@ -347,7 +348,8 @@ cudaError_t launch_stage(dgpu_batch* c, bool rhs_mode, double dt, int stage, int
 	const int* node_face = c->d_node_face;
 	long long n_nodes = c->qnode[kQMax + 1];
 	unsigned* bar = c->d_bar;
-	void* args[] = {&P, &tiles, &n_tiles, &u, &node_face, &n_nodes, &rk, &bar};
+	unsigned long long limit_ns = c->barrier_ns;
+	void* args[] = {&P, &tiles, &n_tiles, &u, &node_face, &n_nodes, &rk, &bar, &limit_ns};
 	const void* k;
 	int blocks;
 	if (rhs_mode) {
@@ -1609,8 +1611,11 @@ static dgpu_status check_flag(dgpu_batch* c)
 	int flag = 0;
 	BATCH_CUDA(c, cudaMemcpyAsync(&flag, c->err_flag, sizeof flag, cudaMemcpyDeviceToHost, c->stream));
 	BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
-	if (flag == kErrBarrier)
+	if (flag == kErrBarrier) {   // reported once: the next launch starts from zeroed barrier words
+		BATCH_CUDA(c, cudaMemsetAsync(c->err_flag, 0, sizeof(int), c->stream));
+		BATCH_CUDA(c, cudaStreamSynchronize(c->stream));
 		return bfail(c, DGPU_ERR_CUDA, "stage kernel: a grid barrier timed out");
+	}
 	if (flag)
 		return bfail(c, DGPU_ERR_POSITIVITY, "average density or pressure below EPS_PHYS");
 	return DGPU_OK;
@@ -1686,6 +1691,15 @@ dgpu_status dgpu_batch_set_mode(dgpu_batch* c, int form)
 	if (c->navier_stokes && (form == 1 || form == 3))
 		return bfail(c, DGPU_ERR_UNSUPPORTED, "Navier-Stokes runs in forms 0 and 2");
 	c->mode = form;
+	return DGPU_OK;
+}
+
+dgpu_status dgpu_batch_set_barrier_timeout(dgpu_batch* c, double seconds)
+{
+	if (!c || !(seconds > 0.0) || !(seconds <= 60.0))
+		return DGPU_ERR_INVALID_ARGUMENT;
+	c->barrier_ns = (unsigned long long)(seconds * 1e9);
+	drop_graphs(c);   // captured stages hold the bound among their kernel parameters
 	return DGPU_OK;
 }
 

@@ -682,9 +682,9 @@ __global__ void __launch_bounds__(256, BLiftOccupancy<MODE>::value) blift_fused_
 // Form 3: a whole stage in one cooperative persistent launch (volume tiles | face nodes | lift tiles)
 // ---------------------------------------------------------------------------------------------------------------
 // Barrier between the phases over every CTA of the grid. The launch is cooperative, so all CTAs are resident at
-// once and the barrier completes; each wait is still bounded (kBarrierLimitNs of the global timer): a CTA that
-// gives up sets *err = kErrBarrier and returns false, and the kernel then ends. bar[0] counts the arrivals of the
-// current barrier and bar[1] its generation; the host zeroes both before each launch.
+// once and the barrier completes; each wait is still bounded (limit_ns of the global timer, 2 s by default): a CTA
+// that gives up sets *err = kErrBarrier and returns false, and the kernel then ends. bar[0] counts the arrivals of
+// the current barrier and bar[1] its generation; the host zeroes both before each launch.
 constexpr int kErrBarrier = 2;
 constexpr unsigned long long kBarrierLimitNs = 2000000000ull;
 
@@ -695,7 +695,7 @@ __device__ __forceinline__ unsigned long long global_ns()
 	return t;
 }
 
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err)
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, unsigned long long limit_ns)
 {
 	__shared__ int ok;
 	__syncthreads();   // the CTA's writes of this phase are issued
@@ -711,7 +711,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err)
 		} else {
 			const unsigned long long t0 = global_ns();
 			while (*gen == g) {
-				if (global_ns() - t0 > kBarrierLimitNs) {
+				if (global_ns() - t0 > limit_ns) {
 					atomicExch(err, kErrBarrier);
 					ok = 0;
 					break;
@@ -732,7 +732,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err)
 template <int D, int NV, int PDE, int FLUX, int MODE, bool GLL_IN>
 __global__ void __launch_bounds__(256, 2)
 bstage_kernel(const BParams P, const BTile* __restrict__ tiles, int n_tiles, const double* __restrict__ u,
-              const int* __restrict__ node_face, long long n_nodes, const RkArgs rk, unsigned* bar)
+              const int* __restrict__ node_face, long long n_nodes, const RkArgs rk, unsigned* bar,
+              unsigned long long limit_ns)
 {
 	constexpr int DMODE = (MODE == kModeRkGlNoMax) ? kModeRkGl : MODE;
 	extern __shared__ double smem[];
@@ -763,7 +764,7 @@ bstage_kernel(const BParams P, const BTile* __restrict__ tiles, int n_tiles, con
 		default: bvol_tile<D, 5, NV, PDE, GLL_IN>(P, sops, G, tl.e0, E, u, base); break;
 		}
 	}
-	if (!grid_barrier(bar, P.err_flag))
+	if (!grid_barrier(bar, P.err_flag, limit_ns))
 		return;
 	for (long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x; gid < n_nodes;
 	     gid += (long long)gridDim.x * blockDim.x) {
@@ -771,7 +772,7 @@ bstage_kernel(const BParams P, const BTile* __restrict__ tiles, int n_tiles, con
 		const long long fb = P.fbase[f];
 		bface_node_rt<D, NV, PDE, FLUX>(P, f, (int)(gid - fb), (int)(P.fbase[f + 1] - fb));
 	}
-	if (!grid_barrier(bar, P.err_flag))
+	if (!grid_barrier(bar, P.err_flag, limit_ns))
 		return;
 	for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
 		const BTile tl = tiles[t];

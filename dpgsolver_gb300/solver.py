@@ -490,6 +490,10 @@ class BatchSimulation:
             raise ValueError(f"source of {s.size} values, expected {self._n_source}")
         self._check(self._lib.dgpu_batch_set_source(self._h, _dp(s)))
 
+    def set_barrier_timeout(self, seconds: float):
+        """Bound of each grid-barrier wait of the "stage" form (2 s by default)."""
+        self._check(self._lib.dgpu_batch_set_barrier_timeout(self._h, float(seconds)))
+
     FORMS = {"plain": 0, "fused": 1, "branches": 2, "stage": 3}
 
     @property

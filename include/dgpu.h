@@ -448,6 +448,9 @@ dgpu_status dgpu_batch_ssp_rk3_steps(dgpu_batch* b, double dt, int n_steps, doub
 /* Form of the stages: 0 = one launch per group / face order in sequence, 1 = fused persistent launches,
  * 2 = the launches of form 0 on parallel branches, 3 = one cooperative persistent launch per stage. */
 dgpu_status dgpu_batch_set_mode(dgpu_batch* b, int form);
+/* Bound of each grid-barrier wait of form 3, in seconds (0 < seconds <= 60; 2 by default). A wait that runs out
+ * ends the stage kernel and the call returns DGPU_ERR_CUDA; the context stays usable. */
+dgpu_status dgpu_batch_set_barrier_timeout(dgpu_batch* b, double seconds);
 dgpu_status dgpu_batch_get_mode(const dgpu_batch* b, int* form);
 /* 1 (default): RK steps replay a captured CUDA graph; 0: every kernel is launched from the host each step. */
 dgpu_status dgpu_batch_set_graphs(dgpu_batch* b, int enable);

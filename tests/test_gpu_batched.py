@@ -579,3 +579,23 @@ def test_dense_faces_in_the_reference_layout(gpu_lib, form):
     assert rel_err(r, r_ref) <= TOL
     assert rel_err(r, r_can) <= TOL
     assert abs(mx - mx_can) <= TOL * mx_can
+
+
+def test_stage_barrier_wait_is_bounded_and_the_context_recovers(gpu_lib):
+    """The "stage" form's grid barriers wait a bounded time: with a bound of 1 ns the waits run out (most CTAs have
+    no tile of this small mesh and wait for the others), the stage kernel ends and the call returns DGPU_ERR_CUDA;
+    with the default bound the same context then computes the oracle's residual. Nothing waits without a bound."""
+    from dpgsolver_gb300._lib import DGPUError
+    from dpgsolver_gb300.solver import BatchSimulation
+    prob = CASES["hex_roe_mixed_4"]()
+    r_ref, _ = oracle.Oracle(prob).compute_rhs(prob.sol)
+    with BatchSimulation(prob) as sim:
+        sim.form = "stage"
+        sim.set_barrier_timeout(1e-9)
+        with pytest.raises(DGPUError) as e:
+            sim.compute_rhs()
+        assert e.value.status == 3 and "barrier" in str(e.value)
+        sim.set_barrier_timeout(2.0)
+        sim.upload_state(prob.sol)
+        sim.compute_rhs()
+        assert rel_err(sim.rhs, r_ref) <= TOL
