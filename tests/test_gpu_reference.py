@@ -109,11 +109,11 @@ def test_batched_path_matches_reference_on_adapted_orders(gpu_lib, name, form):
     prob = R.with_reference_mixed_inputs(R.host_mixed_problem(name, ref["p_vol"], ref["face_vol"], ref["face_lf"]),
                                          ref)
     tol = _residual_tol(prob)
-    if R.MIXED_CASES[name][0].startswith("navier_stokes"):
+    if name in R.WIDE_FLOOR:
         # the face values of a lower-order neighbour reach a face of higher order through V, the trace and the
-        # GL(q) -> GL(q_f) interpolation (three roundings where the reference's cv0_vs_fc has one), and the energy
-        # residual carries the heat flux, a difference of gradients: measured 2.3 x the one-ulp floor (1.5e-12), all
-        # of it in the energy equation of the p = 4 volumes next to p = 3 ones
+        # GL(q) -> GL(q_f) interpolation (three roundings where the reference's cv0_vs_fc has one). On the
+        # Taylor-Couette case the energy residual carries the heat flux, a difference of gradients: measured 2.3 x
+        # the one-ulp floor (1.5e-12), all of it in the energy equation of the p = 4 volumes next to p = 3 ones.
         tol = 2.0 * tol   # max(2e-12, 4 x the floor)
     with BatchSimulation(prob) as sim:
         sim.form = form
