@@ -293,6 +293,11 @@ def _sv_state(x):
             (1.0 + 0.05 * np.sin(4.0 * TH) * np.sin(np.pi * (R - 1.0) / 0.384))[None]).T
 
 
+def _duct_state(x):
+    from dpgsolver_gb300.host.problem import subsonic_duct_state
+    return np.asarray(subsonic_duct_state(x, 2, 0.4, 0.02, 0)).T
+
+
 def _tc_state(x, diabatic):
     from dpgsolver_gb300.host.problem import taylor_couette_state
     X, Y = x[:, 0], x[:, 1]
@@ -530,6 +535,8 @@ MIXED_CASES = {
     # the Euler supersonic vortex of "sv_n3" (Riemann faces with the exact solution outside, slip walls on both arcs)
     # on its parametric quarter square annulus
     "mx_sv_n3": ("euler_sv", 3, 2, 4, 31, 10, [(0.376, 1.128, 4), (1.256, 1.256, 3)]),
+    # the subsonic duct of "duct_n4" (total T/p inflow, back-pressure outflow, slip walls) on its straight box
+    "mx_duct_n4": ("euler_duct", 4, 2, 4, 31, 10, [(2.5, 2.5, 4), (7.5, 5.0, 3)]),
 }
 
 
@@ -554,6 +561,8 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
     elif pde == "euler_sv":
         from dpgsolver_gb300.host.gmsh import GmshMesh, GmshTPMesh
         mesh = GmshTPMesh(GmshMesh(_case_mesh(name, lambda path: _sv_mesh(path, n)), 2))
+    elif pde == "euler_duct":
+        mesh = StructuredMesh(2, n, 0.0, 10.0, periodic=(False, False))
     else:
         lo, hi = _mixed_box(pde)
         mesh = StructuredMesh(2, n, lo, hi)
@@ -574,6 +583,9 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
         prob = M.MixedTPProblem(name, 2, P.PDE_EULER, flux, True, np.zeros(3), mesh, p_vol,
                                 parametric=P.cylinder_parametric_map)
         fn = _sv_state
+    elif pde == "euler_duct":
+        prob = M.MixedTPProblem(name, 2, P.PDE_EULER, flux, True, np.zeros(3), mesh, p_vol)
+        fn = _duct_state
     elif pde == "advection":
         prob = M.MixedTPProblem(name, 2, P.PDE_ADVECTION, flux, False, np.array([1.0, 0.5, 0.0]), mesh, p_vol)
         fn = _advection_state
@@ -590,6 +602,12 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
         prob.set_boundaries(None, P._taylor_couette_wall(0.5, 1.0, 1.0))
     elif pde == "euler_sv":   # the Riemann faces' exterior state: the exact solution
         prob.set_boundaries(None, lambda xy: np.asarray(P.supersonic_vortex_state(xy[:, 0], xy[:, 1], 1.0)).T)
+    elif pde == "euler_duct":   # as P.euler_subsonic_duct: the unperturbed Mach 0.4 stream's BC data
+        T_tot = 1.0 + 0.5 * P.GM1 * 0.4 ** 2
+        prob.bc_data = (1.0, T_tot, T_tot ** (P.GAMMA / P.GM1), 1.0)
+        prob.set_boundaries({(0, 0): P.BC_TOTAL_TP, (0, 1): P.BC_BACKPRESSURE, (1, 0): P.BC_SLIPWALL,
+                             (1, 1): P.BC_SLIPWALL},
+                            P._uniform_flow(2, 1.0, (0.4 * np.sqrt(P.GAMMA), 0.0), 1.0))
     return prob
 
 
@@ -607,6 +625,19 @@ def run_mixed(name: str) -> dict:
         p_vol = out0["volumes"][:, 2].astype(np.int32)
         prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
         out = run(states_fn=lambda o: [_tc_state(x, False) for x in o["xyz_vs"]], steps=steps, dt=prob.dt)
+        return _mixed_arrays(name, p_vol, n, flux, steps, prob, out)
+    if pde == "euler_duct":
+        from dpgsolver_gb300.host.gmsh import write_box_msh
+        codes = {(0, 0): 10104, (0, 1): 10103, (1, 0): 10102, (1, 1): 10102}
+        prob0 = host_mixed_problem(name, np.full(n * n, p, dtype=np.int32))
+        extra = dict(mesh_writer=lambda path: write_box_msh(path, 2, n, lo=0.0, hi=10.0, periodic=False, codes=codes),
+                     pde_spec="steady/free_stream", bc_data=prob0.bc_data)
+        run = lambda **kw: run_case(name, "euler", n, p, 0.0, 10.0, flux, adapt_p=adapt,   # noqa: E731
+                                    p_max=p_max, **extra, **kw)
+        out0 = run()
+        p_vol = out0["volumes"][:, 2].astype(np.int32)
+        prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
+        out = run(state_fn=_duct_state, steps=steps, dt=prob.dt)
         return _mixed_arrays(name, p_vol, n, flux, steps, prob, out)
     if pde == "euler_sv":
         extra = dict(mesh_writer=lambda path: _sv_mesh(path, n), pde_spec="steady/supersonic_vortex")
