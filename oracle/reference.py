@@ -298,6 +298,11 @@ def _duct_state(x):
     return np.asarray(subsonic_duct_state(x, 2, 0.4, 0.02, 0)).T
 
 
+def _sduct_state(x):
+    from dpgsolver_gb300.host.problem import subsonic_duct_state
+    return np.asarray(subsonic_duct_state(x, 2, 1.5, 0.02, 0)).T
+
+
 def _tc_state(x, diabatic):
     from dpgsolver_gb300.host.problem import taylor_couette_state
     X, Y = x[:, 0], x[:, 1]
@@ -537,6 +542,8 @@ MIXED_CASES = {
     "mx_sv_n3": ("euler_sv", 3, 2, 4, 31, 10, [(0.376, 1.128, 4), (1.256, 1.256, 3)]),
     # the subsonic duct of "duct_n4" (total T/p inflow, back-pressure outflow, slip walls) on its straight box
     "mx_duct_n4": ("euler_duct", 4, 2, 4, 31, 10, [(2.5, 2.5, 4), (7.5, 5.0, 3)]),
+    # the same box at Mach 1.5 with supersonic inflow and outflow ("sduct_n4")
+    "mx_sduct_n4": ("euler_sduct", 4, 2, 4, 31, 10, [(5.0, 2.5, 4), (2.5, 7.5, 3)]),
 }
 
 
@@ -561,7 +568,7 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
     elif pde == "euler_sv":
         from dpgsolver_gb300.host.gmsh import GmshMesh, GmshTPMesh
         mesh = GmshTPMesh(GmshMesh(_case_mesh(name, lambda path: _sv_mesh(path, n)), 2))
-    elif pde == "euler_duct":
+    elif pde in ("euler_duct", "euler_sduct"):
         mesh = StructuredMesh(2, n, 0.0, 10.0, periodic=(False, False))
     else:
         lo, hi = _mixed_box(pde)
@@ -583,9 +590,9 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
         prob = M.MixedTPProblem(name, 2, P.PDE_EULER, flux, True, np.zeros(3), mesh, p_vol,
                                 parametric=P.cylinder_parametric_map)
         fn = _sv_state
-    elif pde == "euler_duct":
+    elif pde in ("euler_duct", "euler_sduct"):
         prob = M.MixedTPProblem(name, 2, P.PDE_EULER, flux, True, np.zeros(3), mesh, p_vol)
-        fn = _duct_state
+        fn = _duct_state if pde == "euler_duct" else _sduct_state
     elif pde == "advection":
         prob = M.MixedTPProblem(name, 2, P.PDE_ADVECTION, flux, False, np.array([1.0, 0.5, 0.0]), mesh, p_vol)
         fn = _advection_state
@@ -608,6 +615,11 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
         prob.set_boundaries({(0, 0): P.BC_TOTAL_TP, (0, 1): P.BC_BACKPRESSURE, (1, 0): P.BC_SLIPWALL,
                              (1, 1): P.BC_SLIPWALL},
                             P._uniform_flow(2, 1.0, (0.4 * np.sqrt(P.GAMMA), 0.0), 1.0))
+    elif pde == "euler_sduct":   # as P.euler_supersonic_duct_2d: the unperturbed Mach 1.5 stream outside
+        prob.bc_data = (0.0, 0.0, 0.0, 0.0)
+        prob.set_boundaries({(0, 0): P.BC_SUPERSONIC_IN, (0, 1): P.BC_SUPERSONIC_OUT, (1, 0): P.BC_SLIPWALL,
+                             (1, 1): P.BC_SLIPWALL},
+                            P._uniform_flow(2, 1.0, (1.5 * np.sqrt(P.GAMMA), 0.0), 1.0))
     return prob
 
 
@@ -626,18 +638,19 @@ def run_mixed(name: str) -> dict:
         prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
         out = run(states_fn=lambda o: [_tc_state(x, False) for x in o["xyz_vs"]], steps=steps, dt=prob.dt)
         return _mixed_arrays(name, p_vol, n, flux, steps, prob, out)
-    if pde == "euler_duct":
+    if pde in ("euler_duct", "euler_sduct"):
         from dpgsolver_gb300.host.gmsh import write_box_msh
-        codes = {(0, 0): 10104, (0, 1): 10103, (1, 0): 10102, (1, 1): 10102}
+        sup = pde == "euler_sduct"
+        codes = {(0, 0): 10105 if sup else 10104, (0, 1): 10106 if sup else 10103, (1, 0): 10102, (1, 1): 10102}
         prob0 = host_mixed_problem(name, np.full(n * n, p, dtype=np.int32))
         extra = dict(mesh_writer=lambda path: write_box_msh(path, 2, n, lo=0.0, hi=10.0, periodic=False, codes=codes),
-                     pde_spec="steady/free_stream", bc_data=prob0.bc_data)
+                     pde_spec="steady/free_stream", bc_data=prob0.bc_data, mach=1.5 if sup else 0.4)
         run = lambda **kw: run_case(name, "euler", n, p, 0.0, 10.0, flux, adapt_p=adapt,   # noqa: E731
                                     p_max=p_max, **extra, **kw)
         out0 = run()
         p_vol = out0["volumes"][:, 2].astype(np.int32)
         prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
-        out = run(state_fn=_duct_state, steps=steps, dt=prob.dt)
+        out = run(state_fn=_sduct_state if sup else _duct_state, steps=steps, dt=prob.dt)
         return _mixed_arrays(name, p_vol, n, flux, steps, prob, out)
     if pde == "euler_sv":
         extra = dict(mesh_writer=lambda path: _sv_mesh(path, n), pde_spec="steady/supersonic_vortex")
