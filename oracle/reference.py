@@ -544,6 +544,9 @@ MIXED_CASES = {
     "mx_duct_n4": ("euler_duct", 4, 2, 4, 31, 10, [(2.5, 2.5, 4), (7.5, 5.0, 3)]),
     # the same box at Mach 1.5 with supersonic inflow and outflow ("sduct_n4")
     "mx_sduct_n4": ("euler_sduct", 4, 2, 4, 31, 10, [(5.0, 2.5, 4), (2.5, 7.5, 3)]),
+    # the steady advection case with its source term (steady/default, "c1_source_bc") on a straight 6^2 box of
+    # [-1,1]^2 with upwind faces on its four sides (the steady solution outside)
+    "mx_src_n6": ("advection_default_bc", 6, 2, 4, 11, 20, [(0.0, 0.0, 4), (-2.0 / 3.0, 1.0 / 3.0, 3)]),
 }
 
 
@@ -570,6 +573,8 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
         mesh = GmshTPMesh(GmshMesh(_case_mesh(name, lambda path: _sv_mesh(path, n)), 2))
     elif pde in ("euler_duct", "euler_sduct"):
         mesh = StructuredMesh(2, n, 0.0, 10.0, periodic=(False, False))
+    elif pde == "advection_default_bc":
+        mesh = StructuredMesh(2, n, -1.0, 1.0, periodic=(False, False))
     else:
         lo, hi = _mixed_box(pde)
         mesh = StructuredMesh(2, n, lo, hi)
@@ -590,6 +595,9 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
         prob = M.MixedTPProblem(name, 2, P.PDE_EULER, flux, True, np.zeros(3), mesh, p_vol,
                                 parametric=P.cylinder_parametric_map)
         fn = _sv_state
+    elif pde == "advection_default_bc":
+        prob = M.MixedTPProblem(name, 2, P.PDE_ADVECTION, flux, False, np.array([1.0, 0.5, 0.0]), mesh, p_vol)
+        fn = _advection_default_state
     elif pde in ("euler_duct", "euler_sduct"):
         prob = M.MixedTPProblem(name, 2, P.PDE_EULER, flux, True, np.zeros(3), mesh, p_vol)
         fn = _duct_state if pde == "euler_duct" else _sduct_state
@@ -615,6 +623,19 @@ def host_mixed_problem(name: str, p_vol, face_vol=None, face_lf=None):
         prob.set_boundaries({(0, 0): P.BC_TOTAL_TP, (0, 1): P.BC_BACKPRESSURE, (1, 0): P.BC_SLIPWALL,
                              (1, 1): P.BC_SLIPWALL},
                             P._uniform_flow(2, 1.0, (0.4 * np.sqrt(P.GAMMA), 0.0), 1.0))
+    elif pde == "advection_default_bc":   # as P.advection_default_2d: s = b . grad u at the cubature nodes
+        blocks = [None] * prob.n_volumes
+        for g, vols in enumerate(prob.group_vols):
+            if len(vols) == 0:
+                continue
+            x, y = prob.geoms[g].xyz_vc[..., 0], prob.geoms[g].xyz_vc[..., 1]
+            m, a = P.SOURCE_M, P.SOURCE_A
+            src = 1.0 * m * np.cos(m * x + a) * np.sin(m * y + a) + 0.5 * m * np.sin(m * x + a) * np.cos(m * y + a)
+            for k, v in enumerate(vols):
+                blocks[v] = src[k]
+        prob.source_vc = np.concatenate(blocks)
+        prob.set_boundaries({(dd, sd): P.BC_UPWIND for dd in range(2) for sd in range(2)},
+                            lambda xy: np.asarray(_advection_default_state(xy)).reshape(len(xy), 1))
     elif pde == "euler_sduct":   # as P.euler_supersonic_duct_2d: the unperturbed Mach 1.5 stream outside
         prob.bc_data = (0.0, 0.0, 0.0, 0.0)
         prob.set_boundaries({(0, 0): P.BC_SUPERSONIC_IN, (0, 1): P.BC_SUPERSONIC_OUT, (1, 0): P.BC_SLIPWALL,
@@ -637,6 +658,18 @@ def run_mixed(name: str) -> dict:
         p_vol = out0["volumes"][:, 2].astype(np.int32)
         prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
         out = run(states_fn=lambda o: [_tc_state(x, False) for x in o["xyz_vs"]], steps=steps, dt=prob.dt)
+        return _mixed_arrays(name, p_vol, n, flux, steps, prob, out)
+    if pde == "advection_default_bc":
+        from dpgsolver_gb300.host.gmsh import write_box_msh
+        codes = {(k, s_): 10041 for k in range(2) for s_ in range(2)}
+        extra = dict(mesh_writer=lambda path: write_box_msh(path, 2, n, lo=-1.0, hi=1.0, periodic=False, codes=codes),
+                     pde_spec="steady/default")
+        run = lambda **kw: run_case(name, "advection", n, p, -1.0, 1.0, flux, adapt_p=adapt,   # noqa: E731
+                                    p_max=p_max, **extra, **kw)
+        out0 = run()
+        p_vol = out0["volumes"][:, 2].astype(np.int32)
+        prob = host_mixed_problem(name, p_vol, out0["faces"][:, [4, 7]], out0["faces"][:, [5, 8]])
+        out = run(state_fn=_advection_default_state, steps=steps, dt=prob.dt)
         return _mixed_arrays(name, p_vol, n, flux, steps, prob, out)
     if pde in ("euler_duct", "euler_sduct"):
         from dpgsolver_gb300.host.gmsh import write_box_msh

@@ -10,9 +10,10 @@
  * case.bin (little endian, written by tests/test_gpu_c_caller.py):
  *   int32  magic 0x48435442, d, pde, num_flux, positivity, n_groups, n_volumes, n_faces, n_steps
  *   f64    dt, b_adv[3]
- *   int32  viscosity; f64 mu, Pr, r_s, dTdn; f64 bc_data[4]
+ *   int32  viscosity; f64 mu, Pr, r_s, dTdn; f64 bc_data[4]; int32 has_source
  *   per group: int32 p; f64 cv0_vs_vc (q x q), cv1_vs_vc (q x q), cv0_vs_fc (2 x q), w_vc (q), ccSB0, ccBS0 (q x q)
- *   per volume: int32 group; f64 metrics_vc (n_vc, d, d) 'C', jacobian_det_vc (n_vc), sol_coef (n_vs, n_var) 'C'
+ *   per volume: int32 group; f64 metrics_vc (n_vc, d, d) 'C', jacobian_det_vc (n_vc), sol_coef (n_vs, n_var) 'C';
+ *               with has_source also the test case's source at its cubature nodes (n_vc, n_var) 'C'
  *   per face:   int32 volume[2], ind_lf[2], bc, n_fc; f64 normals_fc (n_fc, d) 'R', jacobian_det_fc (n_fc); on a
  *               boundary face also the exterior state (n_fc, n_var) 'R'
  * out.bin: per volume rhs (n_vs, n_var) 'C' after compute_rhs_dg, then f64 max_rhs; per volume sol_coef after
@@ -41,6 +42,7 @@ struct Solver_Volume {
 	struct Intrusive_Link lnk;
 	int index, p_ref, group;
 	struct Multiarray_d sol_coef, rhs, metrics_vc, jacobian_det_vc;
+	struct Multiarray_d source;   /* the test case's source at the cubature nodes (compute_source_rhs_dg_like) */
 };
 
 struct Solver_Face {
@@ -56,7 +58,7 @@ struct Group {
 };
 
 struct Simulation {
-	int d, pde, num_flux, positivity, n_var, n_g, n_v, n_f;
+	int d, pde, num_flux, positivity, n_var, n_g, n_v, n_f, has_source;
 	double b_adv[3];
 	int viscosity;
 	double mu, Pr, r_s, dTdn, bc_data[4];
@@ -122,6 +124,9 @@ static void read_case(const char* path, struct Simulation* sim, int* n_steps, do
 	rd(&visc, sizeof(int32_t), 1, f);
 	rd(nsc, sizeof(double), 4, f);
 	rd(sim->bc_data, sizeof(double), 4, f);
+	int32_t has_source;
+	rd(&has_source, sizeof has_source, 1, f);
+	sim->has_source = has_source != 0;
 	sim->viscosity = visc;
 	sim->mu = nsc[0];
 	sim->Pr = nsc[1];
@@ -165,6 +170,10 @@ static void read_case(const char* path, struct Simulation* sim, int* n_steps, do
 		rd(s->metrics_vc.data, sizeof(double), ma_size(&s->metrics_vc), f);
 		rd(s->jacobian_det_vc.data, sizeof(double), ma_size(&s->jacobian_det_vc), f);
 		rd(s->sol_coef.data, sizeof(double), ma_size(&s->sol_coef), f);
+		if (sim->has_source) {
+			ma_init(&s->source, 'C', 2, n, sim->n_var, 1);
+			rd(s->source.data, sizeof(double), ma_size(&s->source), f);
+		}
 	}
 	struct Solver_Face* faces = calloc((size_t)sim->n_f, sizeof *faces);
 	for (int i = 0; i < sim->n_f; ++i) {
@@ -308,6 +317,12 @@ static void pack_from_sim(const struct Simulation* sim)
 		die(dgpu_batch_last_error(g_batch));
 	if (dgpu_batch_state_size(g_batch, &g_n_state) != DGPU_OK)
 		die("dgpu_batch_state_size");
+	if (sim->has_source) {   /* compute_source_rhs_dg_like, solve_dg.c:188 */
+		double* src = cat_volumes(sim, offsetof(struct Solver_Volume, source));
+		if (dgpu_batch_set_source(g_batch, src) != DGPU_OK)
+			die(dgpu_batch_last_error(g_batch));
+		free(src);
+	}
 	/* the context keeps its own copies */
 	free(ops);
 	free(vol_group);

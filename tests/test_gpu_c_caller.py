@@ -109,6 +109,8 @@ def write_mixed_case(path, prob, ref):
         np.array([ns.get("mu", 0.0), ns.get("Pr", 0.0), ns.get("r_s", 0.0), ns.get("dTdn", 0.0)],
                  dtype=np.float64).tofile(fh)
         np.asarray(prob.bc_data if prob.bc_data is not None else (0.0,) * 4, dtype=np.float64).tofile(fh)
+        source = getattr(prob, "source_vc", None)
+        np.array([0 if source is None else 1], dtype=np.int32).tofile(fh)
         for ops in groups:
             np.array([ops.p], dtype=np.int32).tofile(fh)
             for a in (ops.cv0_1d, ops.cv1_1d, ops.cv0_bnd_1d, ops.w_vc_1d, ops.ccSB0_1d, ops.ccBS0_1d):
@@ -122,6 +124,8 @@ def write_mixed_case(path, prob, ref):
             np.ascontiguousarray(ref["metrics_vc"][a * d * d:b * d * d]).tofile(fh)
             np.ascontiguousarray(ref["jacobian_det_vc"][a:b]).tofile(fh)
             np.ascontiguousarray(ref["sol_in"][a * nv:b * nv]).tofile(fh)
+            if source is not None:   # the same (n_vc, n_var) column-major block layout as sol_coef
+                np.ascontiguousarray(np.asarray(source).ravel()[a * nv:b * nv]).tofile(fh)
         fo = prob.face_off
         for f in range(prob.mesh.n_faces):
             bc = int(prob.bc[f]) if prob.bc is not None else 0
